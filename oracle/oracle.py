@@ -1,0 +1,160 @@
+"""ctypes binding of the CPU restatement (slvof_oracle.cpp).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg, as the checker.  The product library never loads this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "slvof_oracle.cpp")
+INC = os.path.join(os.path.dirname(HERE), "ns_multiphase_gb300", "csrc")
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement with gcc: -O2, OpenMP, and no FMA contraction so that every
+    expression rounds as the reference's Julia code (and as the FP64 CUDA path) does."""
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    deps = [SRC, os.path.join(INC, "detmath.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
+        return LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC",
+           "-shared", "-I", INC, SRC, "-o", LIB + ".tmp"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        d, i, p = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
+        for name in ("orc_detm_cbrt", "orc_detm_acos", "orc_detm_sin", "orc_detm_cos"):
+            getattr(L, name).restype = d
+            getattr(L, name).argtypes = [d]
+        L.orc_compute_alpha.restype = d
+        L.orc_compute_alpha.argtypes = [p, d]
+        L.orc_compute_dist.restype = d
+        L.orc_compute_dist.argtypes = [p, i, i, i, d, d, d, d]
+        L.orc_compute_plic2vf.restype = d
+        L.orc_compute_plic2vf.argtypes = [p, i, i, i, d, d, d, d]
+        L.orc_tet_vol.restype = d
+        L.orc_tet_vol.argtypes = [p]
+        L.orc_elvira.restype = i
+        L.orc_elvira.argtypes = [p, p, p, p, p, i, i]
+        L.orc_compute_plic.restype = i
+        L.orc_compute_plic.argtypes = [p, p, p, p, p, p]
+        L.orc_compute_band.restype = i
+        L.orc_compute_band.argtypes = [p, p, p]
+        L.orc_vf_ghost_fill.restype = i
+        L.orc_vf_ghost_fill.argtypes = [p, p]
+        L.orc_transport.restype = i
+        L.orc_transport.argtypes = [p, d, p, p, p, p, p, p, p, p, p, p, i, i]
+        L.orc_sl_cell.restype = d
+        L.orc_sl_cell.argtypes = [p, d, i, i, i, p, p, p, p, p, p, p, p, p]
+        L.orc_project.restype = i
+        L.orc_project.argtypes = [p, p, i, i, i, p, p, p, d]
+        L.orc_mass.restype = d
+        L.orc_mass.argtypes = [p, p]
+        L.orc_step.restype = i
+        L.orc_step.argtypes = [p, d, p, p, p, p, p, p, p, p, p, p, i]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert a.flags.f_contiguous or a.ndim <= 1, "arrays must be Fortran-ordered parents"
+    return a.ctypes.data
+
+
+def _m(mesh):
+    return ctypes.byref(mesh.desc())
+
+
+class Oracle:
+    """Reference-named wrappers over one Mesh (see ns_multiphase_gb300.mesh)."""
+
+    def __init__(self, mesh):
+        self.mesh = mesh
+        self.L = lib()
+
+    def computeDist(self, i, j, k, nx, ny, nz, VF):
+        return self.L.orc_compute_dist(_m(self.mesh), i, j, k, nx, ny, nz, VF)
+
+    def computePLIC2VF(self, i, j, k, nx, ny, nz, dist):
+        return self.L.orc_compute_plic2vf(_m(self.mesh), i, j, k, nx, ny, nz, dist)
+
+    def computeAlpha(self, m, VF):
+        m = np.ascontiguousarray(m, dtype=np.float64)
+        return self.L.orc_compute_alpha(m.ctypes.data, VF)
+
+    def vf_ghost_fill(self, VF):
+        self.L.orc_vf_ghost_fill(_m(self.mesh), _p(VF))
+
+    def ELVIRA(self, VF, nx=None, ny=None, nz=None, klo=1, khi=0):
+        m = self.mesh
+        nx = m.cell_array() if nx is None else nx
+        ny = m.cell_array() if ny is None else ny
+        nz = m.cell_array() if nz is None else nz
+        flags = self.L.orc_elvira(_m(m), _p(VF), _p(nx), _p(ny), _p(nz), klo, khi)
+        return nx, ny, nz, flags
+
+    def computePLIC(self, nx, ny, nz, VF, D=None):
+        D = self.mesh.cell_array() if D is None else D
+        self.L.orc_compute_plic(_m(self.mesh), _p(D), _p(nx), _p(ny), _p(nz), _p(VF))
+        return D
+
+    def computeBand(self, VF, band=None):
+        band = self.mesh.cell_array(np.int16) if band is None else band
+        self.L.orc_compute_band(_m(self.mesh), _p(band), _p(VF))
+        return band
+
+    def transport(self, dt, VF, uf, vf, wf, nx, ny, nz, D, band, klo=1, khi=0, VFnew=None):
+        """SL cell loop + VF copy + ghost fill; VF updated in place (sample mode when
+        klo <= khi: only VFnew is written)."""
+        VFnew = self.mesh.vf_array() if VFnew is None else VFnew
+        flags = self.L.orc_transport(_m(self.mesh), dt, _p(VF), _p(VFnew), _p(uf), _p(vf), _p(wf),
+                                     _p(nx), _p(ny), _p(nz), _p(D), _p(band), klo, khi)
+        return flags, VFnew
+
+    def sl_cell(self, dt, i, j, k, uf, vf, wf, nx, ny, nz, D):
+        vol = ctypes.c_double()
+        flags = ctypes.c_int()
+        r = self.L.orc_sl_cell(_m(self.mesh), dt, i, j, k, _p(uf), _p(vf), _p(wf), _p(nx), _p(ny),
+                               _p(nz), _p(D), ctypes.addressof(vol), ctypes.addressof(flags))
+        return r, vol.value, flags.value
+
+    def project(self, pt, i, j, k, uf, vf, wf, dt):
+        p = np.ascontiguousarray(pt, dtype=np.float64).copy()
+        self.L.orc_project(_m(self.mesh), p.ctypes.data, i, j, k, _p(uf), _p(vf), _p(wf), dt)
+        return p
+
+    def mass(self, VF):
+        return self.L.orc_mass(_m(self.mesh), _p(VF))
+
+    def step(self, dt, VF, uf, vf, wf, nx, ny, nz, D, band, do_band=True):
+        VFnew = self.mesh.vf_array()
+        return self.L.orc_step(_m(self.mesh), dt, _p(VF), _p(VFnew), _p(uf), _p(vf), _p(wf),
+                               _p(nx), _p(ny), _p(nz), _p(D), _p(band), int(do_band))
+
+    def init_state(self, VF, do_band=True):
+        """run_solver's start (src/NavierStokes_Parallel.jl:73-98): Neumann!+VF borders,
+        computeBand!, computeNormal!, computePLIC!.  VF is modified in place."""
+        self.vf_ghost_fill(VF)
+        band = self.computeBand(VF) if do_band else self.mesh.cell_array(np.int16)
+        nx, ny, nz, flags = self.ELVIRA(VF)
+        D = self.computePLIC(nx, ny, nz, VF)
+        return band, nx, ny, nz, D

@@ -1,0 +1,872 @@
+/*
+ * slvof_oracle.cpp — TEST INFRASTRUCTURE, NOT PART OF THE PRODUCT.
+ *
+ * CPU restatement of Mist.jl's semi-Lagrangian geometric VOF transport path, written from
+ * the reference's Julia source: ELVIRA normals, PLIC plane-distance solve, PLIC->VF clip,
+ * band gate, single-rank ghost fill, backward RK tracing of cell vertices, the recursive
+ * mesh/PLIC tet clip and the SL cell update.  Only tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py load this library, and only as the checker.
+ *
+ * Pinning.  The PLIC distance solve and the PLIC->VF clip are pinned to the reference's own
+ * tests: the known answers of test/test_PLIC_dist.jl:41-51 and the 1e-12 round trip of
+ * test/runtests.jl:32-45 + test/test_PLIC_dist_cutting.jl:35-49.  ELVIRA, the RK
+ * projection, cutTet and the full step have no reference fixture (the reference is Julia and
+ * Julia is not installed), so for those this restatement is "parity unpinned" by the
+ * reference and is checked against analytic invariants in tests/ instead (exact
+ * reconstruction of planar interfaces, exact transport of a plane by a uniform velocity,
+ * pre-image volume of divergence-free linear flows).
+ *
+ * Arithmetic.  Every expression keeps the reference's operation order (Julia evaluates
+ * a+b+c as (a+b)+c, x^2 as x*x, x^3 as x*x*x, and never contracts to FMA).  Build with
+ * -ffp-contract=off.  cbrt/acos/sin/cos come from the package's deterministic math header
+ * (csrc/detmath.h) so that this file and the FP64 CUDA path round identically.
+ *
+ * Indices are the reference's Julia indices: interior cells 1..N, ghost cells 1-g..0 and
+ * N+1..N+g (g = mesh.nghost), and VF carries three more ghost layers (src/Tools.jl:144).
+ * Arrays are the OffsetArray parents, column-major with i fastest.
+ */
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+#include "detmath.h"
+
+extern "C" {
+typedef struct orc_mesh {
+    int32_t Nx, Ny, Nz;      /* global = local interior cells (single rank) */
+    int32_t nghost;          /* src/Mesh.jl:66 */
+    int32_t nband;           /* src/Parameters.jl:70 */
+    int32_t projection;      /* 0 Euler, 1 Midpoint, 2 RK4 (src/Tools.jl:392-418) */
+    int32_t xper, yper, zper;
+    double Lx, Ly, Lz, dx, dy, dz;
+    double VFlo, VFhi, rho_liq, rho_gas;
+    const double *x, *y, *z;    /* faces, index 1-g .. N+g+1 */
+    const double *xm, *ym, *zm; /* centres, index 1-g .. N+g */
+} orc_mesh;
+}
+
+namespace {
+
+const double EPS = 2.220446049250313e-16; /* Julia eps() */
+
+/* Julia min/max on Float64: NaN-propagating. */
+inline double jmax(double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a : (b > a ? b : (std::signbit(a) ? b : a))); }
+inline double jmin(double a, double b) { return (a != a || b != b) ? NAN : (a < b ? a : (b < a ? b : (std::signbit(a) ? a : b))); }
+
+/* /̂  (src/Tools.jl:375-377) */
+inline double sdiv(double a, double b) { return std::fabs(b) <= EPS ? INFINITY : a / b; }
+
+struct Grid {
+    const orc_mesh* m;
+    int g, N[3];
+    int lo[3], hi[3];   /* cell arrays imino_..imaxo_ */
+    int vlo[3], vhi[3]; /* VF array */
+    long n[3], vn[3];
+    explicit Grid(const orc_mesh* mm) : m(mm)
+    {
+        g = mm->nghost;
+        N[0] = mm->Nx; N[1] = mm->Ny; N[2] = mm->Nz;
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = 1 - g; hi[d] = N[d] + g; n[d] = hi[d] - lo[d] + 1;
+            vlo[d] = lo[d] - 3; vhi[d] = hi[d] + 3; vn[d] = vhi[d] - vlo[d] + 1;
+        }
+    }
+    long c(int i, int j, int k) const { return (i - lo[0]) + n[0] * ((j - lo[1]) + n[1] * (long)(k - lo[2])); }
+    long v(int i, int j, int k) const { return (i - vlo[0]) + vn[0] * ((j - vlo[1]) + vn[1] * (long)(k - vlo[2])); }
+    double x(int i) const { return m->x[i - lo[0]]; }
+    double y(int j) const { return m->y[j - lo[1]]; }
+    double z(int k) const { return m->z[k - lo[2]]; }
+    double xm(int i) const { return m->xm[i - lo[0]]; }
+    double ym(int j) const { return m->ym[j - lo[1]]; }
+    double zm(int k) const { return m->zm[k - lo[2]]; }
+    double fc(int d, int i) const { return d == 0 ? x(i) : (d == 1 ? y(i) : z(i)); }
+};
+
+/* ---------------------------------------------------------------------------------------
+ * Cut tables, src/VFgeom.jl:55-165, kept in the reference's 1-based layout:
+ * T_V1[case-1][n-1] == cut_v1[n,case], T_VTET[case-1][n-1][t-1] == cut_vtet[t,n,case],
+ * T_SIDE[case-1][n-1] == cut_side[n,case].
+ * ------------------------------------------------------------------------------------- */
+const int T_NVERT[16] = {0, 3, 3, 4, 3, 4, 4, 3, 3, 4, 4, 3, 4, 3, 3, 0};
+const int T_NTETS[16] = {1, 4, 4, 6, 4, 6, 6, 4, 4, 6, 6, 4, 6, 4, 4, 1};
+const int T_NNTET[16] = {1, 2, 2, 4, 2, 4, 4, 4, 2, 4, 4, 4, 4, 4, 4, 2};
+const int T_V1[16][4] = {
+    {-1, -1, -1, -1}, {1, 1, 1, -1}, {2, 2, 2, -1}, {1, 2, 1, 2}, {3, 3, 3, -1}, {1, 3, 1, 3},
+    {2, 3, 2, 3},     {4, 4, 4, -1}, {4, 4, 4, -1}, {1, 4, 1, 4}, {2, 4, 2, 4}, {3, 3, 3, -1},
+    {3, 4, 3, 4},     {2, 2, 2, -1}, {1, 1, 1, -1}, {-1, -1, -1, -1}};
+const int T_V2[16][4] = {
+    {-1, -1, -1, -1}, {2, 3, 4, -1}, {3, 4, 1, -1}, {4, 4, 3, 3}, {4, 1, 2, -1}, {4, 4, 2, 2},
+    {4, 4, 1, 1},     {1, 2, 3, -1}, {1, 2, 3, -1}, {3, 3, 2, 2}, {3, 3, 1, 1}, {4, 1, 2, -1},
+    {2, 2, 1, 1},     {3, 4, 1, -1}, {2, 3, 4, -1}, {-1, -1, -1, -1}};
+const int T_VTET[16][6][4] = {
+    {{1, 2, 3, 4}, {-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{5, 7, 6, 1}, {6, 2, 3, 4}, {4, 2, 5, 6}, {5, 6, 7, 4}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{7, 5, 6, 2}, {1, 3, 4, 6}, {1, 5, 3, 6}, {5, 7, 6, 1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{5, 8, 6, 2}, {5, 7, 8, 1}, {5, 1, 8, 2}, {5, 6, 8, 4}, {5, 8, 7, 3}, {5, 8, 3, 4}},
+    {{6, 5, 7, 3}, {2, 1, 4, 6}, {6, 5, 4, 2}, {6, 7, 5, 2}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{5, 6, 8, 3}, {5, 8, 7, 1}, {5, 8, 1, 3}, {5, 8, 6, 4}, {5, 7, 8, 2}, {5, 8, 4, 2}},
+    {{8, 6, 5, 3}, {5, 7, 8, 2}, {8, 5, 2, 3}, {8, 5, 6, 4}, {5, 8, 7, 1}, {5, 8, 1, 4}},
+    {{1, 2, 3, 7}, {1, 2, 7, 6}, {5, 7, 6, 1}, {5, 6, 7, 4}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{5, 6, 7, 4}, {1, 2, 3, 6}, {5, 1, 3, 6}, {5, 7, 6, 3}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{5, 8, 6, 4}, {5, 7, 8, 1}, {5, 8, 4, 1}, {5, 6, 8, 3}, {5, 8, 7, 2}, {5, 8, 2, 3}},
+    {{8, 5, 6, 4}, {5, 8, 7, 2}, {8, 2, 5, 4}, {8, 6, 5, 3}, {5, 7, 8, 1}, {5, 8, 3, 1}},
+    {{1, 4, 2, 7}, {4, 1, 6, 7}, {6, 7, 5, 4}, {6, 5, 7, 3}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{8, 6, 5, 4}, {5, 7, 8, 3}, {8, 4, 5, 3}, {8, 5, 6, 2}, {5, 8, 7, 1}, {5, 8, 1, 2}},
+    {{3, 4, 1, 7}, {7, 6, 3, 4}, {7, 6, 5, 3}, {7, 5, 6, 2}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{7, 4, 2, 3}, {2, 3, 6, 7}, {5, 6, 7, 2}, {5, 7, 6, 1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}},
+    {{1, 2, 3, 4}, {-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}, {-1, -1, -1, -1}}};
+const int T_SIDE[16][6] = {
+    {1, -1, -1, -1, -1, -1}, {2, 1, 1, 1, -1, -1}, {2, 1, 1, 1, -1, -1}, {2, 2, 2, 1, 1, 1},
+    {2, 1, 1, 1, -1, -1},    {2, 2, 2, 1, 1, 1},   {2, 2, 2, 1, 1, 1},   {2, 2, 2, 1, -1, -1},
+    {2, 1, 1, 1, -1, -1},    {2, 2, 2, 1, 1, 1},   {2, 2, 2, 1, 1, 1},   {2, 2, 2, 1, -1, -1},
+    {2, 2, 2, 1, 1, 1},      {2, 2, 2, 1, -1, -1}, {2, 2, 2, 1, -1, -1}, {2, -1, -1, -1, -1, -1}};
+
+/* 5-tet decomposition of the 8 cell vertices, src/VFgeom.jl:235-256 (1-based vertex ids). */
+const int TET5[5][4] = {{1, 2, 4, 6}, {1, 4, 3, 7}, {1, 5, 6, 7}, {4, 7, 6, 8}, {1, 4, 7, 6}};
+
+struct Err { int flags = 0; };
+enum { E_INDEX = 1, E_DEPTH = 2, E_NAN = 4, E_VOLUME = 8 };
+
+/* tet_vol, src/VFgeom.jl:669-681.  v[vertex][coord]. */
+inline double tet_vol(const double v[4][3])
+{
+    const double a1 = v[0][0] - v[3][0], a2 = v[0][1] - v[3][1], a3 = v[0][2] - v[3][2];
+    const double b1 = v[1][0] - v[3][0], b2 = v[1][1] - v[3][1], b3 = v[1][2] - v[3][2];
+    const double c1 = v[2][0] - v[3][0], c2 = v[2][1] - v[3][1], c3 = v[2][2] - v[3][2];
+    return -1.0 / 6.0 * ((a1 * (b2 * c3 - c2 * b3) - a2 * (b1 * c3 - c1 * b3)) + a3 * (b1 * c2 - c1 * b2));
+}
+
+/* d2case, src/VFgeom.jl:693-708.  Modifies d (callers pass a copy where the reference does). */
+inline int d2case(double d[4], Err* err)
+{
+    int npos = 0, nneg = 0;
+    for (int n = 0; n < 4; ++n) { npos += d[n] > 0.0; nneg += d[n] < 0.0; }
+    for (int n = 0; n < 4; ++n)
+        if (std::fabs(d[n]) < EPS) d[n] = npos > nneg ? EPS : -EPS;
+    int c = 1;
+    for (int n = 0; n < 4; ++n) {
+        if (d[n] != d[n]) { if (err) err->flags |= E_NAN; continue; }
+        c += (1 << n) * (d[n] > 0.0 ? 1 : 0);
+    }
+    return c;
+}
+
+inline double clamp_mu(double q) { return jmin(1.0, jmax(0.0, q)); }
+
+/* oddEvenCell + cell2verts!, src/VFgeom.jl:171-216 (5_tets). verts[vertex][coord]. */
+double cell2verts(const Grid& G, int i, int j, int k, double verts[8][3])
+{
+    const bool even = ((i + j + k) % 2) == 0;
+    const int ia = even ? i : i + 1, ib = even ? i + 1 : i;
+    const double xs[2] = {G.x(ia), G.x(ib)};
+    const double ys[2] = {G.y(j), G.y(j + 1)};
+    const double zs[2] = {G.z(k), G.z(k + 1)};
+    for (int c = 0; c < 2; ++c)
+        for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) {
+                double* p = verts[a + 2 * b + 4 * c];
+                p[0] = xs[a]; p[1] = ys[b]; p[2] = zs[c];
+            }
+    return even ? 1.0 : -1.0;
+}
+
+/* computeAlpha, src/VF.jl:164-214. */
+double compute_alpha(const double min[3], double VF)
+{
+    double m[3] = {min[0], min[1], min[2]};
+    std::sort(m, m + 3);
+    const double m1 = m[0], m2 = m[1], m3 = m[2];
+    const double m12 = m[0] + m[1];
+    const double V1 = m[0] * m[0] / jmax(6.0 * m[1] * m[2], EPS);
+    const double V2 = V1 + sdiv(0.5 * (m[1] - m[0]), m3);
+    double V3;
+    if (m12 <= m[2]) V3 = sdiv(0.5 * m12, m3);
+    else V3 = sdiv((m3 * m3 * (3.0 * m12 - m3) + m1 * m1 * (m1 - 3.0 * m3)) + m2 * m2 * (m2 - 3.0 * m3), 6.0 * m1 * m2 * m3);
+    double alpha;
+    if (0.0 <= VF && VF < V1) {
+        alpha = detm_cbrt(6.0 * m1 * m2 * m3 * VF);
+    } else if (V1 <= VF && VF < V2) {
+        alpha = 0.5 * (m1 + std::sqrt(m1 * m1 + 8.0 * m2 * m3 * (VF - V1)));
+    } else if (V2 <= VF && VF < V3) {
+        double a0 = (m1 * m1 * m1 + m2 * m2 * m2) - 6.0 * m1 * m2 * m3 * VF;
+        double a1 = -3.0 * (m1 * m1 + m2 * m2);
+        double a2 = 3.0 * m12;
+        double a3 = -1.0;
+        a0 = a0 / a3; a1 = a1 / a3; a2 = a2 / a3; a3 = a3 / a3;
+        const double p0 = a1 / 3.0 - a2 * a2 / 9.0;
+        const double q0 = (a1 * a2 - 3.0 * a0) / 6.0 - a2 * a2 * a2 / 27.0;
+        const double theta = detm_acos(jmin(1.0, jmax(-1.0, q0 / std::sqrt(-1.0 * (p0 * p0 * p0))))) / 3.0;
+        alpha = std::sqrt(-p0) * (std::sqrt(3.0) * detm_sin(theta) - detm_cos(theta)) - a2 / 3.0;
+    } else {
+        if (m12 <= m3) {
+            alpha = m3 * VF + 0.5 * m12;
+        } else {
+            double a0 = ((m1 * m1 * m1 + m2 * m2 * m2) + m3 * m3 * m3) - 6.0 * m1 * m2 * m3 * VF;
+            double a1 = -3.0 * ((m1 * m1 + m2 * m2) + m3 * m3);
+            double a2 = 3.0;
+            double a3 = -2.0;
+            a0 = a0 / a3; a1 = a1 / a3; a2 = a2 / a3; a3 = a3 / a3;
+            const double p0 = a1 / 3.0 - a2 * a2 / 9.0;
+            const double q0 = (a1 * a2 - 3.0 * a0) / 6.0 - a2 * a2 * a2 / 27.0;
+            const double theta = detm_acos(jmin(1.0, jmax(-1.0, q0 / std::sqrt(-(p0 * p0 * p0))))) / 3.0;
+            alpha = std::sqrt(-p0) * (std::sqrt(3.0) * detm_sin(theta) - detm_cos(theta)) - a2 / 3.0;
+        }
+    }
+    return alpha;
+}
+
+/* computeDist, src/VF.jl:109-156. */
+double compute_dist(const Grid& G, int i, int j, int k, double nx, double ny, double nz, double VF)
+{
+    const orc_mesh* M = G.m;
+    if (VF < M->VFlo) return -((M->Lx + M->Ly) + M->Lz);
+    if (VF > M->VFhi) return +((M->Lx + M->Ly) + M->Lz);
+    double mm[3] = {nx * M->dx, ny * M->dy, nz * M->dz};
+    const double norm = ((std::fabs(mm[0]) + std::fabs(mm[1])) + std::fabs(mm[2])) + EPS;
+    mm[0] = mm[0] / norm; mm[1] = mm[1] / norm; mm[2] = mm[2] / norm;
+    double factor = 0.0;
+    if (mm[0] < 0.0) factor += mm[0];
+    if (mm[1] < 0.0) factor += mm[1];
+    if (mm[2] < 0.0) factor += mm[2];
+    const double VFo = VF > 0.5 ? 1.0 - VF : VF;
+    const double am[3] = {std::fabs(mm[0]), std::fabs(mm[1]), std::fabs(mm[2])};
+    double alpha = compute_alpha(am, VFo);
+    alpha = VF > 0.5 ? 1.0 - alpha : alpha;
+    alpha += factor;
+    alpha -= 0.5 * ((mm[0] + mm[1]) + mm[2]);
+    double dist = alpha * norm;
+    dist += (nx * G.xm(i) + ny * G.ym(j)) + nz * G.zm(k);
+    return dist;
+}
+
+/* computePLIC2VF, src/VF.jl:219-278 (5_tets).  d2case modifies d in place here. */
+double compute_plic2vf(const Grid& G, int i, int j, int k, double nx, double ny, double nz, double dist, Err* err)
+{
+    const orc_mesh* M = G.m;
+    double verts[8][3];
+    const double tetsign = cell2verts(G, i, j, k, verts);
+    double VF = 0.0;
+    for (int t = 0; t < 5; ++t) {
+        double vert[8][3];
+        for (int n = 0; n < 4; ++n)
+            for (int p = 0; p < 3; ++p) vert[n][p] = verts[TET5[t][n] - 1][p];
+        double d[4];
+        for (int n = 0; n < 4; ++n) d[n] = ((nx * vert[n][0] + ny * vert[n][1]) + nz * vert[n][2]) - dist;
+        const int cs = d2case(d, err) - 1;
+        for (int n = 0; n < T_NVERT[cs]; ++n) {
+            const int v1 = T_V1[cs][n] - 1, v2 = T_V2[cs][n] - 1;
+            const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+            for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
+        }
+        for (int n = T_NTETS[cs]; n >= T_NNTET[cs]; --n) {
+            double tet[4][3];
+            for (int tt = 0; tt < 4; ++tt)
+                for (int p = 0; p < 3; ++p) tet[tt][p] = vert[T_VTET[cs][n - 1][tt] - 1][p];
+            VF += tetsign * tet_vol(tet) / (M->dx * M->dy * M->dz);
+        }
+    }
+    return VF;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Ghost fill, single rank (src/Tools.jl:4-18 Neumann!, src/Parallel.jl:63-143
+ * update_borders!).  Each statement reads the state before it (Julia slices copy).
+ * ------------------------------------------------------------------------------------- */
+template <class T>
+struct Arr3 {
+    T* a; int lo[3], hi[3]; long n[3];
+    Arr3(T* p, const int l[3], const int h[3]) : a(p)
+    {
+        for (int d = 0; d < 3; ++d) { lo[d] = l[d]; hi[d] = h[d]; n[d] = h[d] - l[d] + 1; }
+    }
+    T& at(int i, int j, int k) const { return a[(i - lo[0]) + n[0] * ((j - lo[1]) + n[1] * (long)(k - lo[2]))]; }
+};
+
+/* Copy A[dst range along dim] = A[src range along dim] (full extent in the other dims),
+ * reading the pre-statement state. */
+template <class T>
+void slab_copy(Arr3<T>& A, int dim, int dlo, int dhi, int slo)
+{
+    const int cnt = dhi - dlo + 1;
+    int r0[3] = {A.lo[0], A.lo[1], A.lo[2]}, r1[3] = {A.hi[0], A.hi[1], A.hi[2]};
+    r0[dim] = 0; r1[dim] = cnt - 1;
+    std::vector<T> tmp;
+    tmp.reserve((size_t)(r1[0] - r0[0] + 1) * (r1[1] - r0[1] + 1) * (r1[2] - r0[2] + 1));
+    for (int k = r0[2]; k <= r1[2]; ++k)
+        for (int j = r0[1]; j <= r1[1]; ++j)
+            for (int i = r0[0]; i <= r1[0]; ++i) {
+                int s[3] = {i, j, k}; s[dim] += slo;
+                tmp.push_back(A.at(s[0], s[1], s[2]));
+            }
+    size_t q = 0;
+    for (int k = r0[2]; k <= r1[2]; ++k)
+        for (int j = r0[1]; j <= r1[1]; ++j)
+            for (int i = r0[0]; i <= r1[0]; ++i) {
+                int d[3] = {i, j, k}; d[dim] += dlo;
+                A.at(d[0], d[1], d[2]) = tmp[q++];
+            }
+}
+
+template <class T>
+void neumann(const Grid& G, Arr3<T>& A)
+{
+    for (int d = 0; d < 3; ++d) {
+        slab_copy(A, d, 0, 0, 1);                  /* A[min_-1] = A[min_] */
+        slab_copy(A, d, G.N[d] + 1, G.N[d] + 1, G.N[d]); /* A[max_+1] = A[max_] */
+    }
+}
+
+template <class T>
+void update_borders(const Grid& G, Arr3<T>& A)
+{
+    const int per[3] = {G.m->xper, G.m->yper, G.m->zper};
+    const int g = G.g;
+    for (int d = 0; d < 3; ++d) {
+        if (!per[d]) continue; /* MPI.PROC_NULL neighbours: receive buffer unchanged */
+        const int mn = 1, mx = G.N[d];
+        slab_copy(A, d, mx + 1, mx + g, mn);             /* [max_+1:maxo_] <- [min_:min_+g-1] */
+        slab_copy(A, d, mn - g, mn - 1, mx - g + 1);     /* [mino_:min_-1] <- [max_-g+1:max_] */
+    }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * ELVIRA, src/ELVIRA.jl:6-137.
+ * ------------------------------------------------------------------------------------- */
+struct Fields {
+    const Grid* G;
+    const double* VF;
+    double VFat(int i, int j, int k) const { return VF[G->v(i, j, k)]; }
+};
+
+void check_normal(const Grid& G, const Fields& F, double& err, double nx_, double ny_, double nz_,
+                  double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
+{
+    double err_ = 0.0;
+    const double norm = std::sqrt((nx_ * nx_ + ny_ * ny_) + nz_ * nz_);
+    nx_ = nx_ / norm; ny_ = ny_ / norm; nz_ = nz_ / norm;
+    const double dist = compute_dist(G, i, j, k, nx_, ny_, nz_, F.VFat(i, j, k));
+    for (int kk = k - 1; kk <= k + 1; ++kk)
+        for (int jj = j - 1; jj <= j + 1; ++jj)
+            for (int ii = i - 1; ii <= i + 1; ++ii) {
+                const double VF_ = compute_plic2vf(G, ii, jj, kk, nx_, ny_, nz_, dist, e);
+                const double r = F.VFat(ii, jj, kk) - VF_;
+                err_ += r * r;
+            }
+    if (err_ < err) {
+        err = err_;
+        const long c = G.c(i, j, k);
+        nx[c] = nx_; ny[c] = ny_; nz[c] = nz_;
+    }
+}
+
+void elvira_calc(const Grid& G, const Fields& F, double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
+{
+    const orc_mesh* M = G.m;
+    double err = INFINITY;
+    const int P[3][2] = {{-1, 0}, {-1, 1}, {0, 1}};
+    if (M->Nz > 1) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const int jj1 = j + P[a][0], jj2 = j + P[a][1], ii1 = i + P[b][0], ii2 = i + P[b][1];
+                const double s2x = (F.VFat(ii2, j, k - 1) * M->dz + F.VFat(ii2, j, k) * M->dz) + F.VFat(ii2, j, k + 1) * M->dz;
+                const double s1x = (F.VFat(ii1, j, k - 1) * M->dz + F.VFat(ii1, j, k) * M->dz) + F.VFat(ii1, j, k + 1) * M->dz;
+                const double nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
+                const double s2y = (F.VFat(i, jj2, k - 1) * M->dz + F.VFat(i, jj2, k) * M->dz) + F.VFat(i, jj2, k + 1) * M->dz;
+                const double s1y = (F.VFat(i, jj1, k - 1) * M->dz + F.VFat(i, jj1, k) * M->dz) + F.VFat(i, jj1, k + 1) * M->dz;
+                const double ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
+                const double nz_ = F.VFat(i, j, k + 1) > F.VFat(i, j, k - 1) ? -1.0 : 1.0;
+                check_normal(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+            }
+    }
+    if (M->Ny > 1) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const int kk1 = k + P[a][0], kk2 = k + P[a][1], ii1 = i + P[b][0], ii2 = i + P[b][1];
+                const double s2x = (F.VFat(ii2, j - 1, k) * M->dy + F.VFat(ii2, j, k) * M->dy) + F.VFat(ii2, j + 1, k) * M->dy;
+                const double s1x = (F.VFat(ii1, j - 1, k) * M->dy + F.VFat(ii1, j, k) * M->dy) + F.VFat(ii1, j + 1, k) * M->dy;
+                const double nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
+                const double ny_ = F.VFat(i, j + 1, k) > F.VFat(i, j - 1, k) ? -1.0 : 1.0;
+                const double s2z = (F.VFat(i, j - 1, kk2) * M->dy + F.VFat(i, j, kk2) * M->dy) + F.VFat(i, j + 1, kk2) * M->dy;
+                const double s1z = (F.VFat(i, j - 1, kk1) * M->dy + F.VFat(i, j, kk1) * M->dy) + F.VFat(i, j + 1, kk1) * M->dy;
+                const double nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
+                check_normal(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+            }
+    }
+    if (M->Nx > 1) {
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                const int kk1 = k + P[a][0], kk2 = k + P[a][1], jj1 = j + P[b][0], jj2 = j + P[b][1];
+                const double nx_ = F.VFat(i + 1, j, k) > F.VFat(i - 1, j, k) ? -1.0 : 1.0;
+                const double s2y = (F.VFat(i - 1, jj2, k) * M->dx + F.VFat(i, jj2, k) * M->dx) + F.VFat(i + 1, jj2, k) * M->dx;
+                const double s1y = (F.VFat(i - 1, jj1, k) * M->dx + F.VFat(i, jj1, k) * M->dx) + F.VFat(i + 1, jj1, k) * M->dx;
+                const double ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
+                const double s2z = (F.VFat(i - 1, j, kk2) * M->dx + F.VFat(i, j, kk2) * M->dx) + F.VFat(i + 1, j, kk2) * M->dx;
+                const double s1z = (F.VFat(i - 1, j, kk1) * M->dx + F.VFat(i, j, kk1) * M->dx) + F.VFat(i + 1, j, kk1) * M->dx;
+                const double nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
+                check_normal(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+            }
+    }
+}
+
+void elvira_cell(const Grid& G, const Fields& F, double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
+{
+    const orc_mesh* M = G.m;
+    const double lo = M->VFlo, hi = M->VFhi;
+    const double v = F.VFat(i, j, k);
+    const long c = G.c(i, j, k);
+    if (v >= lo && v <= hi) {
+        elvira_calc(G, F, nx, ny, nz, i, j, k, e);
+    } else if (v < lo) {
+        if (F.VFat(i - 1, j, k) > hi) nx[c] = 1;
+        else if (F.VFat(i + 1, j, k) > hi) nx[c] = -1;
+        else if (F.VFat(i, j - 1, k) > hi) ny[c] = 1;
+        else if (F.VFat(i, j + 1, k) > hi) ny[c] = -1;
+        else if (F.VFat(i, j, k - 1) > hi) nz[c] = 1;
+        else if (F.VFat(i, j, k + 1) > hi) nz[c] = -1;
+    } else if (v > hi) {
+        if (F.VFat(i - 1, j, k) < lo) nx[c] = -1;
+        else if (F.VFat(i + 1, j, k) < lo) nx[c] = 1;
+        else if (F.VFat(i, j - 1, k) < lo) ny[c] = -1;
+        else if (F.VFat(i, j + 1, k) < lo) ny[c] = 1;
+        else if (F.VFat(i, j, k - 1) < lo) nz[c] = -1;
+        else if (F.VFat(i, j, k + 1) < lo) nz[c] = 1;
+    }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Velocity interpolation and projection, src/Tools.jl:392-641.
+ * ------------------------------------------------------------------------------------- */
+struct Vel { const double *uf, *vf, *wf; };
+
+/* get_velocity_{u,v,w}face: stag = which direction uses face coordinates. */
+double interp_face(const Grid& G, const double* f, int stag, const double pt[3], int i, int j, int k)
+{
+    int I[3] = {i, j, k};
+    for (int d = 0; d < 3; ++d) {
+        auto co = [&](int q) { return d == stag ? G.fc(d, q) : (d == 0 ? G.xm(q) : (d == 1 ? G.ym(q) : G.zm(q))); };
+        while (pt[d] - co(I[d]) < 0.0 && I[d] > G.lo[d]) I[d] = I[d] - 1;
+        while (pt[d] - co(I[d] + 1) >= 0.0 && I[d] + 1 < G.hi[d]) I[d] = I[d] + 1;
+    }
+    double w1[3], w2[3];
+    for (int d = 0; d < 3; ++d) {
+        auto co = [&](int q) { return d == stag ? G.fc(d, q) : (d == 0 ? G.xm(q) : (d == 1 ? G.ym(q) : G.zm(q))); };
+        w1[d] = sdiv(pt[d] - co(I[d]), co(I[d] + 1) - co(I[d]));
+        w2[d] = 1.0 - w1[d];
+    }
+    const int a = I[0], b = I[1], c = I[2];
+    auto F = [&](int ii, int jj, int kk) { return f[G.c(ii, jj, kk)]; };
+    return w1[2] * (w1[1] * (w1[0] * F(a + 1, b + 1, c + 1) + w2[0] * F(a, b + 1, c + 1)) +
+                    w2[1] * (w1[0] * F(a + 1, b, c + 1) + w2[0] * F(a, b, c + 1))) +
+           w2[2] * (w1[1] * (w1[0] * F(a + 1, b + 1, c) + w2[0] * F(a, b + 1, c)) +
+                    w2[1] * (w1[0] * F(a + 1, b, c) + w2[0] * F(a, b, c)));
+}
+
+void velocity(const Grid& G, const Vel& V, const double pt[3], int i, int j, int k, double out[3])
+{
+    out[0] = interp_face(G, V.uf, 0, pt, i, j, k);
+    out[1] = interp_face(G, V.vf, 1, pt, i, j, k);
+    out[2] = interp_face(G, V.wf, 2, pt, i, j, k);
+}
+
+void project(const Grid& G, const Vel& V, double pt[3], int i, int j, int k, double dt)
+{
+    const int method = G.m->projection;
+    if (method == 2) {
+        double v1[3], v2[3], v3[3], v4[3], p[3];
+        velocity(G, V, pt, i, j, k, v1);
+        for (int d = 0; d < 3; ++d) p[d] = pt[d] - 0.5 * dt * v1[d];
+        velocity(G, V, p, i, j, k, v2);
+        for (int d = 0; d < 3; ++d) p[d] = pt[d] - 0.5 * dt * v2[d];
+        velocity(G, V, p, i, j, k, v3);
+        for (int d = 0; d < 3; ++d) p[d] = pt[d] - dt * v3[d];
+        velocity(G, V, p, i, j, k, v4);
+        for (int d = 0; d < 3; ++d) pt[d] = pt[d] + (-dt) / 6.0 * (((v1[d] + 2.0 * v2[d]) + 2.0 * v3[d]) + v4[d]);
+    } else if (method == 0) {
+        double v1[3];
+        velocity(G, V, pt, i, j, k, v1);
+        for (int d = 0; d < 3; ++d) pt[d] = pt[d] + (-dt) * v1[d];
+    } else {
+        double v1[3], v2[3], p[3];
+        velocity(G, V, pt, i, j, k, v1);
+        for (int d = 0; d < 3; ++d) p[d] = pt[d] - 0.5 * dt * v1[d];
+        velocity(G, V, p, i, j, k, v2);
+        for (int d = 0; d < 3; ++d) pt[d] = pt[d] + (-dt) * v2[d];
+    }
+}
+
+/* pt2index!, src/Tools.jl:424-434.  The reference's loops are unbounded; here leaving the
+ * coordinate arrays raises E_INDEX and clamps. */
+void pt2index(const Grid& G, int I[3], const double pt[3], int i, int j, int k, Err* e)
+{
+    I[0] = i; I[1] = j; I[2] = k;
+    for (int d = 0; d < 3; ++d) {
+        while (pt[d] > G.fc(d, I[d] + 1) + EPS) {
+            if (I[d] >= G.hi[d]) { e->flags |= E_INDEX; break; }
+            I[d] += 1;
+        }
+        while (pt[d] < G.fc(d, I[d]) - EPS) {
+            if (I[d] <= G.lo[d]) { e->flags |= E_INDEX; break; }
+            I[d] -= 1;
+        }
+    }
+}
+
+/* ---------------------------------------------------------------------------------------
+ * cutTet, src/VFgeom.jl:713-900, kept recursive as in the reference.
+ * ------------------------------------------------------------------------------------- */
+struct Plic { const double *nx, *ny, *nz, *D; };
+
+struct CutOut { double vol, vLiq; };
+
+CutOut cut_tet(const Grid& G, const Plic& P, double tet[4][3], int ind[4][3], bool xdone, bool ydone, bool zdone,
+               int lvl, Err* e)
+{
+    if (lvl > 64) { e->flags |= E_DEPTH; return {0.0, 0.0}; }
+    int dir = -1, cut_ind = 0;
+    double d[4];
+    for (;;) {
+        bool* done[3] = {&xdone, &ydone, &zdone};
+        int q = -1;
+        for (int dd = 0; dd < 3; ++dd)
+            if (!*done[dd]) { q = dd; break; }
+        if (q < 0) break; /* PLIC leaf */
+        int mx = ind[0][q], mn = ind[0][q];
+        for (int n = 1; n < 4; ++n) { mx = std::max(mx, ind[n][q]); mn = std::min(mn, ind[n][q]); }
+        if (mx > mn) {
+            dir = q; cut_ind = mx;
+            for (int n = 0; n < 4; ++n) d[n] = tet[n][q] - G.fc(q, cut_ind);
+            break;
+        }
+        *done[q] = true; /* tail call cutTet(..., xdone=true, ...) at the same level */
+    }
+    if (dir < 0) {
+        /* Leaf: clip by the donor cell's PLIC plane (src/VFgeom.jl:757-830). */
+        double vert[8][3];
+        for (int n = 0; n < 4; ++n)
+            for (int p = 0; p < 3; ++p) vert[n][p] = tet[n][p];
+        const int i = ind[0][0], j = ind[0][1], k = ind[0][2];
+        const long c = G.c(i, j, k);
+        for (int n = 0; n < 4; ++n) d[n] = ((P.nx[c] * vert[n][0] + P.ny[c] * vert[n][1]) + P.nz[c] * vert[n][2]) - P.D[c];
+        double dc[4] = {d[0], d[1], d[2], d[3]};
+        const int cs = d2case(dc, e) - 1;
+        for (int n = 0; n < T_NVERT[cs]; ++n) {
+            const int v1 = T_V1[cs][n] - 1, v2 = T_V2[cs][n] - 1;
+            const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+            for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
+        }
+        double vol = 0.0, vLiq = 0.0;
+        for (int n = T_NTETS[cs]; n >= T_NNTET[cs]; --n) {
+            double nt[4][3];
+            for (int t = 0; t < 4; ++t)
+                for (int p = 0; p < 3; ++p) nt[t][p] = vert[T_VTET[cs][n - 1][t] - 1][p];
+            const double tv = tet_vol(nt);
+            vol += tv;
+            vLiq += tv;
+        }
+        for (int n = 1; n <= T_NNTET[cs] - 1; ++n) {
+            double nt[4][3];
+            for (int t = 0; t < 4; ++t)
+                for (int p = 0; p < 3; ++p) nt[t][p] = vert[T_VTET[cs][n - 1][t] - 1][p];
+            vol += tet_vol(nt);
+        }
+        return {vol, vLiq};
+    }
+    /* Cut by the mesh plane (src/VFgeom.jl:832-899). */
+    double dc[4] = {d[0], d[1], d[2], d[3]};
+    const int cs = d2case(dc, e) - 1;
+    double vert[8][3];
+    int vind[8][3][2];
+    for (int n = 0; n < 4; ++n) {
+        for (int p = 0; p < 3; ++p) {
+            vert[n][p] = tet[n][p];
+            vind[n][p][0] = ind[n][p];
+            vind[n][p][1] = ind[n][p];
+        }
+        vind[n][dir][0] = std::min(vind[n][dir][0], cut_ind - 1);
+        vind[n][dir][1] = std::max(vind[n][dir][0], cut_ind);
+    }
+    for (int n = 0; n < T_NVERT[cs]; ++n) {
+        const int v1 = T_V1[cs][n] - 1, v2 = T_V2[cs][n] - 1;
+        const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+        for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
+        /* seed: side-1 index of vertex n (src/VFgeom.jl:854-857) */
+        int I[3];
+        pt2index(G, I, vert[4 + n], vind[n][0][0], vind[n][1][0], vind[n][2][0], e);
+        for (int p = 0; p < 3; ++p) {
+            int val = I[p];
+            val = std::max(val, std::min(vind[v1][p][0], vind[v2][p][0]));
+            val = std::min(val, std::max(vind[v1][p][0], vind[v2][p][0]));
+            vind[4 + n][p][0] = val;
+            vind[4 + n][p][1] = val;
+        }
+        vind[4 + n][dir][0] = cut_ind - 1;
+        vind[4 + n][dir][1] = cut_ind;
+    }
+    double vol = 0.0, vLiq = 0.0;
+    for (int n = 0; n < T_NTETS[cs]; ++n) {
+        double ct[4][3];
+        int ci[4][3];
+        const int side = T_SIDE[cs][n] - 1;
+        for (int nn = 0; nn < 4; ++nn) {
+            const int vt = T_VTET[cs][n][nn] - 1;
+            for (int p = 0; p < 3; ++p) {
+                ct[nn][p] = vert[vt][p];
+                ci[nn][p] = vind[vt][p][side];
+            }
+        }
+        const CutOut r = cut_tet(G, P, ct, ci, xdone, ydone, zdone, lvl + 1, e);
+        vol += r.vol;
+        vLiq += r.vLiq;
+    }
+    return {vol, vLiq};
+}
+
+/* SL update of one cell, src/Transport.jl:111-148 with cell2tets!(project_verts=true,
+ * compute_indices=true) (src/VFgeom.jl:345-420). Returns VFnew. */
+double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out)
+{
+    double verts[8][3];
+    const double tetsign = cell2verts(G, i, j, k, verts);
+    for (int n = 0; n < 8; ++n) project(G, V, verts[n], i, j, k, dt);
+    int vInds[8][3];
+    for (int n = 0; n < 8; ++n) pt2index(G, vInds[n], verts[n], i, j, k, e);
+    double vol = 0.0, vLiq = 0.0;
+    for (int t = 0; t < 5; ++t) {
+        double tet[4][3];
+        int ind[4][3];
+        for (int n = 0; n < 4; ++n)
+            for (int p = 0; p < 3; ++p) {
+                tet[n][p] = verts[TET5[t][n] - 1][p];
+                ind[n][p] = vInds[TET5[t][n] - 1][p];
+            }
+        const CutOut r = cut_tet(G, P, tet, ind, false, false, false, 1, e);
+        vol += tetsign * r.vol;
+        vLiq += tetsign * r.vLiq;
+    }
+    if (!(vol > 0.0) || !std::isfinite(vol)) e->flags |= E_VOLUME;
+    if (vol_out) *vol_out = vol;
+    return vLiq / vol;
+}
+
+} // namespace
+
+/* =========================================================================================
+ * C API (ctypes).  All arrays are OffsetArray parents: cell arrays (N+2g)^3, VF (N+2g+6)^3.
+ * ======================================================================================= */
+extern "C" {
+
+double orc_detm_cbrt(double x) { return detm_cbrt(x); }
+double orc_detm_acos(double x) { return detm_acos(x); }
+double orc_detm_sin(double x) { return detm_sin(x); }
+double orc_detm_cos(double x) { return detm_cos(x); }
+
+double orc_compute_alpha(const double m[3], double VF) { return compute_alpha(m, VF); }
+
+double orc_compute_dist(const orc_mesh* M, int i, int j, int k, double nx, double ny, double nz, double VF)
+{
+    Grid G(M);
+    return compute_dist(G, i, j, k, nx, ny, nz, VF);
+}
+
+double orc_compute_plic2vf(const orc_mesh* M, int i, int j, int k, double nx, double ny, double nz, double dist)
+{
+    Grid G(M);
+    Err e;
+    return compute_plic2vf(G, i, j, k, nx, ny, nz, dist, &e);
+}
+
+double orc_tet_vol(const double v[12])
+{
+    double t[4][3];
+    for (int n = 0; n < 4; ++n)
+        for (int p = 0; p < 3; ++p) t[n][p] = v[3 * n + p];
+    return tet_vol(t);
+}
+
+/* ELVIRA! (src/ELVIRA.jl:6-55): zero the whole normal arrays, compute the interior, then
+ * update_borders! on each.  Cells k in [klo, khi] only when klo <= khi (bench sample). */
+int orc_elvira(const orc_mesh* M, const double* VF, double* nx, double* ny, double* nz, int klo, int khi)
+{
+    Grid G(M);
+    const long ncell = G.n[0] * G.n[1] * G.n[2];
+    if (klo > khi) { klo = 1; khi = G.N[2]; }
+    std::fill(nx, nx + ncell, 0.0);
+    std::fill(ny, ny + ncell, 0.0);
+    std::fill(nz, nz + ncell, 0.0);
+    Fields F{&G, VF};
+    int flags = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : flags)
+    for (int k = klo; k <= khi; ++k)
+        for (int j = 1; j <= G.N[1]; ++j) {
+            Err e;
+            for (int i = 1; i <= G.N[0]; ++i) elvira_cell(G, F, nx, ny, nz, i, j, k, &e);
+            flags |= e.flags;
+        }
+    Arr3<double> A(nx, G.lo, G.hi), B(ny, G.lo, G.hi), C(nz, G.lo, G.hi);
+    update_borders(G, A); update_borders(G, B); update_borders(G, C);
+    return flags;
+}
+
+/* computePLIC! (src/VF.jl:94-103): D at every cell including ghosts, then update_borders!. */
+int orc_compute_plic(const orc_mesh* M, double* D, const double* nx, const double* ny, const double* nz, const double* VF)
+{
+    Grid G(M);
+#pragma omp parallel for collapse(2)
+    for (int k = G.lo[2]; k <= G.hi[2]; ++k)
+        for (int j = G.lo[1]; j <= G.hi[1]; ++j)
+            for (int i = G.lo[0]; i <= G.hi[0]; ++i) {
+                const long c = G.c(i, j, k);
+                D[c] = compute_dist(G, i, j, k, nx[c], ny[c], nz[c], VF[G.v(i, j, k)]);
+            }
+    Arr3<double> A(D, G.lo, G.hi);
+    update_borders(G, A);
+    return 0;
+}
+
+/* computeBand! (src/VF.jl:16-74).  Julia's combined for-loop "break" leaves all three loops. */
+int orc_compute_band(const orc_mesh* M, int16_t* band, const double* VF)
+{
+    Grid G(M);
+    const int nb = M->nband;
+    Arr3<int16_t> B(band, G.lo, G.hi);
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i) {
+                const double v = VF[G.v(i, j, k)];
+                int16_t& b = B.at(i, j, k);
+                if (v < M->VFlo) {
+                    bool hit = false;
+                    for (int kk = k - 1; kk <= k + 1 && !hit; ++kk)
+                        for (int jj = j - 1; jj <= j + 1 && !hit; ++jj)
+                            for (int ii = i - 1; ii <= i + 1 && !hit; ++ii)
+                                if (VF[G.v(ii, jj, kk)] >= M->VFhi) hit = true;
+                    b = hit ? 0 : (int16_t)(-nb - 1);
+                } else if (v > M->VFhi) {
+                    bool hit = false;
+                    for (int kk = k - 1; kk <= k + 1 && !hit; ++kk)
+                        for (int jj = j - 1; jj <= j + 1 && !hit; ++jj)
+                            for (int ii = i - 1; ii <= i + 1 && !hit; ++ii)
+                                if (VF[G.v(ii, jj, kk)] <= M->VFlo) hit = true;
+                    b = hit ? 0 : (int16_t)(nb + 1);
+                } else {
+                    b = 0;
+                }
+            }
+    neumann(G, B);
+    update_borders(G, B);
+    for (int n = 1; n <= nb; ++n) {
+        for (int k = 1; k <= G.N[2]; ++k)
+            for (int j = 1; j <= G.N[1]; ++j)
+                for (int i = 1; i <= G.N[0]; ++i) {
+                    int16_t& b = B.at(i, j, k);
+                    if (std::abs((int)b) > n) {
+                        for (int kk = k - 1; kk <= k + 1; ++kk)
+                            for (int jj = j - 1; jj <= j + 1; ++jj)
+                                for (int ii = i - 1; ii <= i + 1; ++ii)
+                                    if (std::abs((int)B.at(ii, jj, kk)) == n - 1) b = (int16_t)(n * (b > 0 ? 1 : (b < 0 ? -1 : 0)));
+                    }
+                }
+        update_borders(G, B);
+    }
+    return 0;
+}
+
+/* Neumann!(VF) + update_VF_borders!(VF) (src/Transport.jl:180-181). */
+int orc_vf_ghost_fill(const orc_mesh* M, double* VF)
+{
+    Grid G(M);
+    Arr3<double> A(VF, G.vlo, G.vhi);
+    neumann(G, A);
+    update_borders(G, A);
+    return 0;
+}
+
+/* The SL cell loop + VF copy + ghost fill (src/Transport.jl:108-151,179-181).
+ * VF is updated in place.  If klo <= khi only cells k in [klo,khi] are advanced and the VF
+ * copy/ghost fill is skipped (bench sample mode); VFnew then receives the sample. */
+int orc_transport(const orc_mesh* M, double dt, double* VF, double* VFnew, const double* uf, const double* vf,
+                  const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                  const int16_t* band, int klo, int khi)
+{
+    Grid G(M);
+    const bool sample = klo <= khi;
+    if (!sample) { klo = 1; khi = G.N[2]; }
+    Vel V{uf, vf, wf};
+    Plic P{nx, ny, nz, D};
+    int flags = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : flags)
+    for (int k = klo; k <= khi; ++k)
+        for (int j = 1; j <= G.N[1]; ++j) {
+            Err e;
+            for (int i = 1; i <= G.N[0]; ++i) {
+                const long c = G.c(i, j, k);
+                const long v = G.v(i, j, k);
+                if (std::abs((int)band[c]) <= M->nband) VFnew[v] = sl_cell(G, V, P, dt, i, j, k, &e, nullptr);
+                else VFnew[v] = VF[v];
+            }
+            flags |= e.flags;
+        }
+    if (sample) return flags;
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i) VF[G.v(i, j, k)] = VFnew[G.v(i, j, k)];
+    orc_vf_ghost_fill(M, VF);
+    return flags;
+}
+
+/* Pre-image of one cell: projected vertices and indices + the SL result, for unit tests. */
+double orc_sl_cell(const orc_mesh* M, double dt, int i, int j, int k, const double* uf, const double* vf,
+                   const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                   double* vol_out, int* flags)
+{
+    Grid G(M);
+    Vel V{uf, vf, wf};
+    Plic P{nx, ny, nz, D};
+    Err e;
+    const double r = sl_cell(G, V, P, dt, i, j, k, &e, vol_out);
+    if (flags) *flags = e.flags;
+    return r;
+}
+
+int orc_project(const orc_mesh* M, double pt[3], int i, int j, int k, const double* uf, const double* vf,
+                const double* wf, double dt)
+{
+    Grid G(M);
+    Vel V{uf, vf, wf};
+    project(G, V, pt, i, j, k, dt);
+    return 0;
+}
+
+/* Sum of interior VF * dx*dy*dz (src/WriteData.jl:33), Neumaier-compensated. */
+double orc_mass(const orc_mesh* M, const double* VF)
+{
+    Grid G(M);
+    const double cv = (M->dx * M->dy) * M->dz;
+    double s = 0.0, comp = 0.0;
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i) {
+                const double x = VF[G.v(i, j, k)] * cv;
+                const double t = s + x;
+                comp += std::fabs(s) >= std::fabs(x) ? (s - t) + x : (x - t) + s;
+                s = t;
+            }
+    return s + comp;
+}
+
+/* One full step as the reference's transport! leaves the state (SL section):
+ * SL update + VF ghosts (Transport.jl:108-181), ELVIRA (:184), computePLIC! (:260);
+ * then, if do_band, computeBand! as run_solver does next (NavierStokes_Parallel.jl:143). */
+int orc_step(const orc_mesh* M, double dt, double* VF, double* VFnew, const double* uf, const double* vf,
+             const double* wf, double* nx, double* ny, double* nz, double* D, int16_t* band, int do_band)
+{
+    int f = orc_transport(M, dt, VF, VFnew, uf, vf, wf, nx, ny, nz, D, band, 1, 0);
+    f |= orc_elvira(M, VF, nx, ny, nz, 1, 0);
+    f |= orc_compute_plic(M, D, nx, ny, nz, VF);
+    if (do_band) f |= orc_compute_band(M, band, VF);
+    return f;
+}
+
+} // extern "C"
