@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""SL-VOF transport step benchmark (one JSON line on rank 0).
+
+Workload (the reference path's 256^3 configuration): 256^3 unit cube, VF = union of 200
+spheres (radii U[0.02,0.08], centres U[0.1,0.9]^3, numpy default_rng(20261203)) sampled by
+VFsphere's rule with nF=20, Deformation3D face velocities with period T=3, CFL 0.5
+(dt = 0.5*dx/max|u| = 0.25/256), band recomputed every step (nband = 1) and the mass summed
+every step.  A step is one resident call of slvof_step: SL update of the band cells, VF ghost
+fill, ELVIRA, PLIC distances, band, mass.  1 cell-update = 1 interior cell advanced one step
+(all 256^3 cells count).  The face velocities are the field at t0 + dt/2 and stay resident
+over the timed window; every field is larger than L2 (129 MB), so no flush is needed.
+
+Arms:
+  value      mixed precision (FP32 trajectories/geometry/ELVIRA errors, FP64 PLIC root,
+             volume sums, mass), device-resident, CUDA events on the launching stream;
+  fp64       the plain FP64 path (bit-identical to the CPU restatement) on the same state;
+  e2e        slvof_step_host: H2D of the step's face velocities from pinned memory, the
+             step, D2H of VF and the mass;
+  cpu_baseline / --impl reference: the CPU restatement of the reference (C++, OpenMP on
+             all host cores) on a bounded z-slab of the same state.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SL-VOF cell-updates/s at 256³: mixed vs FP64 at ≤1e-10 mass err; adj/fwd time"
+SEED = 20261203
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=256)
+    p.add_argument("--fp64-steps", type=int, default=3)
+    p.add_argument("--drift-steps", type=int, default=8)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(n):
+    from ns_multiphase_gb300 import cases
+    from ns_multiphase_gb300.mesh import Mesh
+    m = Mesh(Nx=n, Ny=n, Nz=n, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    centres, radii = cases.config_spheres(200, SEED)
+    dt = 0.5 * m.dx / 2.0
+    return m, centres, radii, dt
+
+
+def make_ctx(m, centres, radii, precision, t):
+    from ns_multiphase_gb300.slvof import SLVOF
+    g = SLVOF(m, precision)
+    g.case_vf_spheres(centres, radii, nF=20, dims=3)
+    g.init_state(band=True)
+    g.case_deformation3d(t, 3.0)
+    return g
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in rows for q in range(4) if r[5 + q].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": num(rows[0][2]),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def timed_steps(g, dt, steps, torch):
+    """K resident steps bracketed by synchronize + CUDA events on the library's stream."""
+    stream = torch.cuda.current_stream()
+    g.set_stream(stream.cuda_stream)
+    stage = {}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        g.step(dt, band=True, mass=True)
+        for k, v in g.stage_ms().items():
+            stage[k] = stage.get(k, 0.0) + v
+    e1.record(stream)
+    torch.cuda.synchronize()
+    g.set_stream(None)
+    return e0.elapsed_time(e1), {k: v / steps for k, v in stage.items()}
+
+
+def cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, budget_s):
+    """CPU restatement on a centred z-slab: ELVIRA of the slab cells and the SL update of the
+    slab's band cells, all host threads.  Returns (cell-updates/s, slab layers, seconds)."""
+    from oracle.oracle import Oracle
+    o = Oracle(m)
+    N = m.Nz
+    nk = 2
+    while True:
+        klo = N // 2 - nk // 2 + 1
+        khi = klo + nk - 1
+        t0 = time.perf_counter()
+        o.transport(dt, VF, uf, vf, wf, nx, ny, nz, D, band, klo=klo, khi=khi)
+        o.ELVIRA(VF, klo=klo, khi=khi)
+        sec = time.perf_counter() - t0
+        if sec >= budget_s / 4 or nk >= N:
+            break
+        nk = min(N, max(nk * 2, int(nk * budget_s / 4 / max(sec, 1e-3))))
+    return m.Nx * m.Ny * nk / sec, nk, sec
+
+
+def reference_arm(args, rank):
+    """--impl reference: the CPU restatement (the Julia reference cannot run here)."""
+    import torch
+    from oracle.oracle import Oracle, build
+    build()
+    m, centres, radii, dt = workload(args.n)
+    if rank != 0:
+        return
+    torch.cuda.set_device(0)
+    g = make_ctx(m, centres, radii, "fp64", 0.5 * dt)
+    VF = g.download_vf()
+    nx, ny, nz = g.download_normals()
+    D = g.download_plic()
+    band = g.download_band()
+    from ns_multiphase_gb300 import cases
+    uf, vf, wf = cases.deformation3d_faces(m, 0.5 * dt, 3.0)
+    g.close()
+    vals = []
+    layers = 0
+    for s in range(max(1, args.steps)):
+        v, layers, sec = cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt,
+                                    budget_s=min(args.cpu_seconds, 120.0 / max(1, args.steps)))
+        vals.append(v)
+    value = statistics.median(vals)
+    cores = os.cpu_count()
+    line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"SL-VOF 256^3 200-sphere deformation (slab sample at {args.n}^3)"},
+            "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": "port",
+                             "sample": f"ELVIRA + SL update of {layers} centred z-layers of the {args.n}^3 state, "
+                                       f"C++ restatement (the Julia reference is not installed)"},
+            "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "vs_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    import torch
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args, rank)
+        if ws > 1:
+            tdist.destroy_process_group()
+        return
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from ns_multiphase_gb300.slvof import SLVOF
+    torch.cuda.set_device(local)
+    m, centres, radii, dt = workload(args.n)
+    cells = m.Nx * m.Ny * m.Nz
+
+    # ---- mixed precision, resident (value) -----------------------------------------------
+    g = make_ctx(m, centres, radii, "mixed", 0.5 * dt)
+    for _ in range(args.warmup):
+        g.step(dt, band=True, mass=True)
+    if ws > 1:
+        tdist.barrier()
+    with Clocks(local) as ck:
+        ms, stage = timed_steps(g, dt, args.steps, torch)
+    clocks = ck.summary()
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * cells * args.steps / (ms / 1e3)
+    ms_step = ms / args.steps
+    g.close()
+
+    out = None
+    if rank == 0:
+        # ---- FP64 arm and mixed-vs-FP64 accuracy on the same state ------------------------
+        g64 = make_ctx(m, centres, radii, "fp64", 0.5 * dt)
+        g32 = make_ctx(m, centres, radii, "mixed", 0.5 * dt)
+        M0 = g64.mass()
+        for s in range(args.drift_steps):
+            m64 = g64.step(dt)
+            m32 = g32.step(dt)
+        V64, V32 = g64.download_vf(), g32.download_vf()
+        dVF = float(np.max(np.abs(m.interior(V64) - m.interior(V32))))
+        drift_vs_fp64 = abs(m32 - m64) / abs(m64)
+        ms64, stage64 = timed_steps(g64, dt, args.fp64_steps, torch)
+        value64 = cells * args.fp64_steps / (ms64 / 1e3)
+        g32.close()
+        VF = g64.download_vf()
+        nx, ny, nz = g64.download_normals()
+        D = g64.download_plic()
+        band = g64.download_band()
+        g64.close()
+
+        # ---- e2e through the host-buffer drop-in -------------------------------------------
+        from ns_multiphase_gb300 import cases
+        uf, vf, wf = cases.deformation3d_faces(m, 0.5 * dt, 3.0)
+        shp = tuple(reversed(m.cell_shape))
+
+        def pinned(a, shape):
+            t = torch.empty(shape, dtype=torch.float64, pin_memory=True)
+            h = t.numpy().T
+            if a is not None:
+                h[...] = a
+            return t, h
+        tu, huf = pinned(uf, shp)
+        tv, hvf = pinned(vf, shp)
+        tw, hwf = pinned(wf, shp)
+        tV, hVF = pinned(None, tuple(reversed(m.vf_shape)))
+        ge = make_ctx(m, centres, radii, "mixed", 0.5 * dt)
+        ge.step_host(dt, huf, hvf, hwf, hVF)  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            ge.step_host(dt, huf, hvf, hwf, hVF)
+        e2e_s = time.perf_counter() - t0
+        ge.close()
+        e2e = {"value": cells * args.e2e_steps / e2e_s, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": int(3 * huf.nbytes), "d2h_bytes_per_step": int(hVF.nbytes + 8),
+               "api": "slvof_step_host (pinned host face velocities in, VF + mass out)"}
+
+        # ---- CPU restatement on a bounded slab ---------------------------------------------
+        cpu = None
+        if not args.no_cpu:
+            from oracle.oracle import build
+            build()
+            v, layers, sec = cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, args.cpu_seconds)
+            cpu = {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"ELVIRA + SL update of {layers} centred z-layers ({sec:.1f} s) of the {args.n}^3 "
+                             f"state, C++ restatement, OpenMP on all host cores"}
+
+        # ---- roofline of the dominant kernel -----------------------------------------------
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except OSError:
+            pass
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        dom = max(stage, key=stage.get)
+        alg = algorithmic_bytes(m, dom)
+        achieved = alg / (stage[dom] / 1e3) / 1e9 if stage[dom] > 0 else 0.0
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": profiled_traffic(dom),
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                "algorithmic_bytes": alg, "kernel_ms": stage[dom],
+                "note": "ALU-bound (FP32 pipe); HBM fraction is reported per the contract"}
+        out = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+               "config": {"workload": f"SL-VOF transport step, {args.n}^3, 200 spheres seed {SEED}, "
+                                      f"Deformation3D T=3, CFL 0.5, nband 1, RK4, 5 tets",
+                          "precision": "mixed", "parallelism": "replicas" if ws > 1 else "1 GPU",
+                          "l2": "every field > L2 (no flush needed)"},
+               "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "speedup_mixed": value / ws / value64,
+                        "stages_ms": stage64},
+               "accuracy": {"steps": args.drift_steps, "mass_rel_diff_mixed_vs_fp64": drift_vs_fp64,
+                            "max_abs_dVF_mixed_vs_fp64": dVF, "mass_rel_change_fp64": abs(m64 - M0) / M0},
+               "stages_ms": stage, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+               "gpu_launches": launches_per_step(m) * args.steps}
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        tdist.barrier()
+        tdist.destroy_process_group()
+
+
+def algorithmic_bytes(m, stage):
+    """Minimum unique HBM bytes of one launch of a stage (mixed precision storage)."""
+    interior = m.Nx * m.Ny * m.Nz
+    ncell = int(np.prod(m.cell_shape))
+    table = {
+        "sl_classify": interior * (2 + 8 + 8),
+        "sl_update": interior * (12 + 16 + 8),      # FP32 velocities + donor planes + VF, upper bound
+        "vf_ghost": (int(np.prod(m.vf_shape)) - interior) * 16,
+        "elvira_pure": interior * (8 + 24),
+        "elvira_candidates": interior * (8 + 24),   # upper bound: VF block + normals of listed cells
+        "normal_ghost": (ncell - interior) * 24,
+        "plic": ncell * (8 * 5 + 16 + 1),
+        "band": interior * (8 + 2 * 2 * 2),
+        "mass": 8 * 1024,
+    }
+    return table.get(stage, interior * 28)
+
+
+def profiled_traffic(stage):
+    """dram read+write bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "slvof_256_mixed_ncu.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 3 and parts[0] == "traffic_bytes" and parts[1] == stage:
+                return float(parts[2])
+    except OSError:
+        pass
+    return None
+
+
+def launches_per_step(m):
+    # classify, SL, VF ghost, ELVIRA pure, ELVIRA candidates, normal ghost, PLIC,
+    # band (first + ghost + nband*(sweep + ghost)), mass final
+    return 7 + 2 + 2 * int(m.nband) + 1
+
+
+if __name__ == "__main__":
+    main()

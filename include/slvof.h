@@ -1,0 +1,143 @@
+/*
+ * slvof.h — C ABI of the GB300 (sm_103a) SL-VOF transport library.
+ *
+ * Drop-in for Mist.jl's semi-Lagrangian geometric VOF transport path: the Julia host keeps
+ * its OffsetArrays and calls these entry points through ccall with pointers to the arrays'
+ * parents (column-major, i fastest).  Extents follow src/Tools.jl:136-191:
+ *   cell arrays (uf, vf, wf, nx, ny, nz, D, band): (Nx+2g) x (Ny+2g) x (Nz+2g), g = nghost;
+ *   VF: (Nx+2g+6) x (Ny+2g+6) x (Nz+2g+6)  (three extra ghost layers, src/Tools.jl:144).
+ * Reals are IEEE double, band is int16.  One MPI rank: the library fills ghost cells itself
+ * with the reference's single-rank semantics (Neumann! src/Tools.jl:4-18, update_borders!
+ * src/Parallel.jl:63-143, periodic directions wrapping onto the same rank).
+ *
+ * Return codes: SLVOF_OK, a positive OR of SLVOF_DEV_* bits raised by a kernel (the result
+ * of that call is still written), or a negative SLVOF_E_* host error.  No call aborts or
+ * throws across the ABI; slvof_last_error() gives a message for the last nonzero status.
+ * Calls on one context are serialised by the caller; distinct contexts are independent.
+ */
+#ifndef SLVOF_H
+#define SLVOF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SLVOF_OK 0
+/* device-side error bits (kernels record them instead of trapping) */
+#define SLVOF_DEV_INDEX 1  /* a pre-image vertex left the ghost region (pt2index!, src/Tools.jl:424-434) */
+#define SLVOF_DEV_DEPTH 2  /* cutTet recursion deeper than the clip stack (src/VFgeom.jl:713-900) */
+#define SLVOF_DEV_NAN 4    /* NaN signed distance in a cut (reference: InexactError in d2case) */
+#define SLVOF_DEV_VOLUME 8 /* non-positive or non-finite pre-image volume (src/Transport.jl:145) */
+/* host errors */
+#define SLVOF_E_ARG (-1)
+#define SLVOF_E_CUDA (-2)
+#define SLVOF_E_UNSUPPORTED (-3)
+#define SLVOF_E_NOMEM (-4)
+
+#define SLVOF_FP64 0  /* every stage in FP64, rounding identical to the CPU restatement */
+#define SLVOF_MIXED 1 /* FP32 trajectories, interpolation, clip geometry and ELVIRA candidate errors;
+                         FP64 PLIC root, volume accumulation and mass sums */
+
+#define SLVOF_STEP_BAND 1 /* recompute the band after the step (run_solver, src/NavierStokes_Parallel.jl:143) */
+#define SLVOF_STEP_MASS 2 /* return sum(VF)*dx*dy*dz over the interior (src/WriteData.jl:33) */
+
+/* Mesh and parameters.  Mirrors mesh_struct (src/Mesh.jl:1-53) and the parameters knobs the
+ * path reads (src/Parameters.jl:68-77).  Coordinate arrays are the parents of mesh.x/y/z
+ * (length N+2g+1, starting at imino_) and mesh.xm/ym/zm (length N+2g); they are copied at
+ * slvof_create and not retained. */
+typedef struct slvof_mesh {
+    int32_t Nx, Ny, Nz;
+    int32_t nghost;     /* 3 + max(0, ceil(CFL)-2), src/Mesh.jl:66 */
+    int32_t nband;      /* ceil(CFL), src/Parameters.jl:70 */
+    int32_t projection; /* 0 Euler, 1 Midpoint, 2 RK4 (src/Tools.jl:392-418) */
+    int32_t xper, yper, zper;
+    double Lx, Ly, Lz, dx, dy, dz;
+    double VFlo, VFhi, rho_liq, rho_gas;
+    const double *x, *y, *z;
+    const double *xm, *ym, *zm;
+} slvof_mesh;
+
+typedef struct slvof_ctx slvof_ctx;
+
+/* ---- context ----------------------------------------------------------------------------
+ * Device-resident state for one mesh: VF (double-buffered), face velocities, normals, PLIC
+ * distances, band, cell lists and the error word, on a private CUDA stream of the current
+ * device.  Replaces the per-call scratch of transport! (src/Transport.jl:23-27). */
+int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out);
+int slvof_destroy(slvof_ctx* ctx);
+int slvof_last_error(const slvof_ctx* ctx, char* buf, size_t n);
+/* Kernel-side time of the last call, milliseconds (CUDA events on the context's stream). */
+int slvof_last_kernel_ms(const slvof_ctx* ctx, double* ms);
+/* Device time of each stage of the last call, milliseconds; stages that did not run give 0.
+ * Order: SL classify, SL update, VF ghost fill, ELVIRA pure cells, ELVIRA candidates,
+ * normal borders, PLIC, band, mass (SLVOF_NSTAGES entries).  No counterpart in the reference
+ * (its only instrumentation is @time around run_solver). */
+#define SLVOF_NSTAGES 9
+int slvof_stage_ms(const slvof_ctx* ctx, double* ms, int n);
+/* Run the context's work on a caller-owned cudaStream_t (NULL: back to the private stream),
+ * e.g. the stream of a Julia CUDA.jl task.  No counterpart in the reference (CPU only). */
+int slvof_set_stream(slvof_ctx* ctx, void* stream);
+
+/* ---- host <-> device ---------------------------------------------------------------------- */
+int slvof_upload_vf(slvof_ctx* ctx, const double* VF);
+int slvof_upload_velocity(slvof_ctx* ctx, const double* uf, const double* vf, const double* wf);
+int slvof_upload_band(slvof_ctx* ctx, const int16_t* band);
+int slvof_upload_plic(slvof_ctx* ctx, const double* nx, const double* ny, const double* nz, const double* D);
+int slvof_download_vf(slvof_ctx* ctx, double* VF);
+int slvof_download_normals(slvof_ctx* ctx, double* nx, double* ny, double* nz);
+int slvof_download_plic(slvof_ctx* ctx, double* D);
+int slvof_download_band(slvof_ctx* ctx, int16_t* band);
+
+/* ---- resident operations (device state in, device state out) ---------------------------- */
+/* Neumann!(VF) + update_VF_borders!(VF): src/Tools.jl:4-18, src/Parallel.jl:71-77. */
+int slvof_vf_ghost_fill(slvof_ctx* ctx);
+/* computeNormal! -> ELVIRA!: src/VF.jl:79-89, src/ELVIRA.jl:6-137. */
+int slvof_compute_normal(slvof_ctx* ctx);
+/* computePLIC!: src/VF.jl:94-156 (computeDist, computeAlpha). */
+int slvof_compute_plic(slvof_ctx* ctx);
+/* computeBand!: src/VF.jl:16-74. */
+int slvof_compute_band(slvof_ctx* ctx);
+/* The SL cell loop of transport! with the VF copy and ghost fill that follow it:
+ * src/Transport.jl:108-151,179-181 (cell2tets!, project!, pt2index!, cutTet, d2case). */
+int slvof_transport(slvof_ctx* ctx, double dt);
+/* One resident step as transport! leaves the SL state: SL update + VF ghosts, ELVIRA
+ * (src/Transport.jl:184), computePLIC! (src/Transport.jl:260); optionally computeBand!
+ * (SLVOF_STEP_BAND) and the mass sum (SLVOF_STEP_MASS, written to *mass).  The normals used
+ * by the SL update are the ones already in the context (the reference's first ELVIRA call at
+ * src/Transport.jl:17 recomputes exactly those from the unchanged VF). */
+int slvof_step(slvof_ctx* ctx, double dt, int flags, double* mass);
+/* sum(VF[interior])*dx*dy*dz, compensated FP64 (src/WriteData.jl:33). */
+int slvof_mass(slvof_ctx* ctx, double* mass);
+
+/* ---- host-buffer drop-ins: one call per reference function, arrays in host memory --------
+ * Each copies its inputs to the device, runs the operation and copies the outputs back.  */
+/* computeNormal!(nx,ny,nz,VF,param,mesh,par_env), src/VF.jl:79 */
+int slvof_computeNormal(slvof_ctx* ctx, double* nx, double* ny, double* nz, const double* VF);
+/* computePLIC!(D,nx,ny,nz,VF,param,mesh,par_env), src/VF.jl:94 */
+int slvof_computePLIC(slvof_ctx* ctx, double* D, const double* nx, const double* ny, const double* nz,
+                      const double* VF);
+/* computeBand!(band,VF,param,mesh,par_env), src/VF.jl:16 */
+int slvof_computeBand(slvof_ctx* ctx, int16_t* band, const double* VF);
+/* SL section of transport!(...): src/Transport.jl:108-151,179-181.  VF is updated in place. */
+int slvof_transportSL(slvof_ctx* ctx, double dt, double* VF, const double* uf, const double* vf, const double* wf,
+                      const double* nx, const double* ny, const double* nz, const double* D, const int16_t* band);
+/* Per-step drop-in for run_solver's loop with the state resident between calls: uploads
+ * this step's face velocities, runs slvof_step and downloads VF (and the mass). */
+int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, const double* vf, const double* wf,
+                    double* VF, double* mass);
+
+/* ---- synthetic inputs (not part of the reference path) -----------------------------------
+ * VF of a union of spheres by VFsphere's sub-sampling rule (src/Tools.jl:907-922), nF points
+ * per direction, written to every cell of imino_:imaxo_ (extra VF layers zero); dims=2 uses
+ * circles in x-y.  Then Neumann! + VF borders as run_solver does after IC!. */
+int slvof_case_vf_spheres(slvof_ctx* ctx, const double* centres, const double* radii, int n, int nF, int dims);
+/* Deformation3D face velocities at time t with period T (src/Tools.jl:660-662). */
+int slvof_case_deformation3d(slvof_ctx* ctx, double t, double T);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SLVOF_H */

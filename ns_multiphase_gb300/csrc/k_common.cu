@@ -1,0 +1,358 @@
+/*
+ * k_common.cu — kernels shared by the FP64 and mixed paths (exact integer/copy work and the
+ * pure-cell part of ELVIRA).  Built with -fmad=false.
+ */
+#include "slvof_kernels.h"
+#include "slvof_dev.cuh"
+
+namespace slvof {
+
+__device__ __forceinline__ bool interior(const DevMesh& m, int i, int j, int k)
+{
+    return i >= 1 && i <= m.N[0] && j >= 1 && j <= m.N[1] && k >= 1 && k <= m.N[2];
+}
+
+/* Neumann!(VF) + update_VF_borders!(VF) after the interior was overwritten
+ * (src/Transport.jl:179-181): ghost p takes the pre-fill value at its source cell, which is
+ * the new interior value or an old ghost value.  update_VF_borders! moves nghost layers, not
+ * six (src/Parallel.jl:71-83 compares nghost == VFghost without assigning), so the three
+ * extra layers keep their values. */
+__global__ void k_vf_ghost(DevMesh m, const double* __restrict__ VFin, double* __restrict__ VFout)
+{
+    const long n0 = m.N[0] + 2 * m.g + 6, n1 = m.N[1] + 2 * m.g + 6, n2 = m.N[2] + 2 * m.g + 6;
+    const long total = n0 * n1 * n2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % n0) + m.vlo, j = (int)((t / n0) % n1) + m.vlo, k = (int)(t / (n0 * n1)) + m.vlo;
+        if (interior(m, i, j, k)) continue;
+        const int si = ghost_src_1d(i, m.N[0], m.g, m.per[0], true);
+        const int sj = ghost_src_1d(j, m.N[1], m.g, m.per[1], true);
+        const int sk = ghost_src_1d(k, m.N[2], m.g, m.per[2], true);
+        const long s = vidx(m, si, sj, sk);
+        VFout[t] = interior(m, si, sj, sk) ? VFout[s] : VFin[s];
+    }
+}
+
+/* ELVIRA! pure cells (src/ELVIRA.jl:19-46), the interface-cell list for the candidate
+ * kernel, and per-block compensated partial sums of the interior VF. */
+constexpr int PURE_THREADS = 256;
+
+__global__ void __launch_bounds__(PURE_THREADS) k_elvira_pure(DevMesh m, const double* __restrict__ VF,
+                                                              double* __restrict__ nx, double* __restrict__ ny,
+                                                              double* __restrict__ nz, int* list, int* count,
+                                                              double* partials)
+{
+    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
+    const long total = N0 * N1 * N2;
+    const double lo = m.VFlo, hi = m.VFhi;
+    const long sj = m.vs1, sk = m.vs2;
+    Comp acc{0.0, 0.0};
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x; base < total; base += stride) {
+        const long t = base + threadIdx.x;
+        bool iface = false;
+        if (t < total) {
+            const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
+            const long v = vidx(m, i, j, k);
+            const double c = VF[v];
+            comp_add(acc, c);
+            double ax = 0.0, ay = 0.0, az = 0.0;
+            if (c >= lo && c <= hi) {
+                iface = true;
+            } else if (c < lo) {
+                if (VF[v - 1] > hi) ax = 1.0;
+                else if (VF[v + 1] > hi) ax = -1.0;
+                else if (VF[v - sj] > hi) ay = 1.0;
+                else if (VF[v + sj] > hi) ay = -1.0;
+                else if (VF[v - sk] > hi) az = 1.0;
+                else if (VF[v + sk] > hi) az = -1.0;
+            } else if (c > hi) {
+                if (VF[v - 1] < lo) ax = -1.0;
+                else if (VF[v + 1] < lo) ax = 1.0;
+                else if (VF[v - sj] < lo) ay = -1.0;
+                else if (VF[v + sj] < lo) ay = 1.0;
+                else if (VF[v - sk] < lo) az = -1.0;
+                else if (VF[v + sk] < lo) az = 1.0;
+            }
+            if (nx) {
+                const long o = cidx(m, i, j, k);
+                nx[o] = ax; ny[o] = ay; nz[o] = az;
+            }
+        }
+        if (list) warp_append(iface, (int)t, list, count);
+    }
+    /* block reduction of the compensated pair */
+    for (int off = 16; off > 0; off >>= 1) {
+        Comp o{__shfl_down_sync(0xffffffffu, acc.s, off), __shfl_down_sync(0xffffffffu, acc.c, off)};
+        comp_merge(acc, o);
+    }
+    __shared__ double ss[PURE_THREADS / 32], sc[PURE_THREADS / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { ss[w] = acc.s; sc[w] = acc.c; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Comp b{ss[0], sc[0]};
+        for (int q = 1; q < PURE_THREADS / 32; ++q) comp_merge(b, Comp{ss[q], sc[q]});
+        partials[2 * blockIdx.x] = b.s;
+        partials[2 * blockIdx.x + 1] = b.c;
+    }
+}
+
+__global__ void k_mass_final(const double* __restrict__ partials, int nblocks, double cellvol, double* out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Comp a{0.0, 0.0};
+    for (int b = 0; b < nblocks; ++b) comp_merge(a, Comp{partials[2 * b], partials[2 * b + 1]});
+    out[0] = (a.s + a.c) * cellvol;
+}
+
+/* update_borders!(nx/ny/nz) after ELVIRA! zeroed the whole arrays (src/ELVIRA.jl:11-13,50-52):
+ * periodic ghosts copy the interior, all other ghosts stay zero. */
+__global__ void k_normal_ghost(DevMesh m, double* nx, double* ny, double* nz)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = n0 * n1 * n2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % n0) + m.lo, j = (int)((t / n0) % n1) + m.lo, k = (int)(t / (n0 * n1)) + m.lo;
+        if (interior(m, i, j, k)) continue;
+        const int si = ghost_src_1d(i, m.N[0], m.g, m.per[0], false);
+        const int sj = ghost_src_1d(j, m.N[1], m.g, m.per[1], false);
+        const int sk = ghost_src_1d(k, m.N[2], m.g, m.per[2], false);
+        double a = 0.0, b = 0.0, c = 0.0;
+        if (interior(m, si, sj, sk)) {
+            const long s = cidx(m, si, sj, sk);
+            a = nx[s]; b = ny[s]; c = nz[s];
+        }
+        nx[t] = a; ny[t] = b; nz[t] = c;
+    }
+}
+
+/* computeBand! (src/VF.jl:16-74).  The first pass marks pure cells touching the opposite
+ * pure phase (Julia's combined for-loop break leaves all three loops: band 0 if any of the
+ * 27 cells qualifies). */
+__global__ void k_band_first(DevMesh m, const double* __restrict__ VF, short* __restrict__ bout)
+{
+    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
+    const long total = N0 * N1 * N2;
+    const short nb1 = (short)(m.nband + 1);
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
+        const double c = VF[vidx(m, i, j, k)];
+        short b = 0;
+        if (c < m.VFlo) {
+            bool hit = false;
+            for (int kk = -1; kk <= 1; ++kk)
+                for (int jj = -1; jj <= 1; ++jj)
+                    for (int ii = -1; ii <= 1; ++ii) hit |= VF[vidx(m, i + ii, j + jj, k + kk)] >= m.VFhi;
+            b = hit ? (short)0 : (short)-nb1;
+        } else if (c > m.VFhi) {
+            bool hit = false;
+            for (int kk = -1; kk <= 1; ++kk)
+                for (int jj = -1; jj <= 1; ++jj)
+                    for (int ii = -1; ii <= 1; ++ii) hit |= VF[vidx(m, i + ii, j + jj, k + kk)] <= m.VFlo;
+            b = hit ? (short)0 : nb1;
+        }
+        bout[cidx(m, i, j, k)] = b;
+    }
+}
+
+/* Neumann!(band) + update_borders!(band) (neumann=true) or update_borders!(band) alone. */
+__global__ void k_band_ghost(DevMesh m, const short* __restrict__ bin, short* __restrict__ bout, bool neumann)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = n0 * n1 * n2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % n0) + m.lo, j = (int)((t / n0) % n1) + m.lo, k = (int)(t / (n0 * n1)) + m.lo;
+        if (interior(m, i, j, k)) continue;
+        const int si = ghost_src_1d(i, m.N[0], m.g, m.per[0], neumann);
+        const int sj = ghost_src_1d(j, m.N[1], m.g, m.per[1], neumann);
+        const int sk = ghost_src_1d(k, m.N[2], m.g, m.per[2], neumann);
+        const long s = cidx(m, si, sj, sk);
+        bout[t] = interior(m, si, sj, sk) ? bout[s] : bin[s];
+    }
+}
+
+/* One band sweep: |band| > n next to |band| == n-1 becomes n*sign(band).  The result does
+ * not depend on the update order, so the sweep reads one buffer and writes the other. */
+__global__ void k_band_sweep(DevMesh m, const short* __restrict__ bin, short* __restrict__ bout, int n)
+{
+    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
+    const long total = N0 * N1 * N2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
+        const long c = cidx(m, i, j, k);
+        short b = bin[c];
+        if (abs((int)b) > n) {
+            bool hit = false;
+            for (int kk = -1; kk <= 1; ++kk)
+                for (int jj = -1; jj <= 1; ++jj)
+                    for (int ii = -1; ii <= 1; ++ii) hit |= abs((int)bin[cidx(m, i + ii, j + jj, k + kk)]) == n - 1;
+            if (hit) b = (short)(b > 0 ? n : -n);
+        }
+        bout[c] = b;
+    }
+}
+
+/* transport! band gate (src/Transport.jl:111,153): band cells go to the SL list, the rest
+ * keep VF. */
+__global__ void k_sl_classify(DevMesh m, const short* __restrict__ band, const double* __restrict__ VFin,
+                              double* __restrict__ VFout, int* list, int* count)
+{
+    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
+    const long total = N0 * N1 * N2;
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x; base < total; base += stride) {
+        const long t = base + threadIdx.x;
+        bool sl = false;
+        if (t < total) {
+            const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
+            sl = abs((int)band[cidx(m, i, j, k)]) <= m.nband;
+            if (!sl) {
+                const long v = vidx(m, i, j, k);
+                VFout[v] = VFin[v];
+            }
+        }
+        warp_append(sl, (int)t, list, count);
+    }
+}
+
+__global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, long n, double scale)
+{
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        b[t] = (float)(a[t] * scale);
+}
+
+/* ---- synthetic inputs ------------------------------------------------------------------
+ * VFsphere's rule (src/Tools.jl:907-922) for a union of spheres: nF points per direction at
+ * xmin + i/(nF+1)*(xmax-xmin); a point is liquid when rad^2 - ((xh-xo)^2 + (yh-yo)^2 +
+ * (zh-zo)^2) > 0 for some sphere; VF is the sequential sum of count copies of 1/nF^dims. */
+constexpr int CASE_MAXS = 32;
+
+__global__ void k_case_spheres(DevMesh m, const double* __restrict__ cen, const double* __restrict__ rad, int ns,
+                               int nF, int dims, const double* __restrict__ table, double* __restrict__ VF)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = n0 * n1 * n2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % n0) + m.lo, j = (int)((t / n0) % n1) + m.lo, k = (int)(t / (n0 * n1)) + m.lo;
+        const double x0 = fco(m, 0, i), x1 = fco(m, 0, i + 1);
+        const double y0 = fco(m, 1, j), y1 = fco(m, 1, j + 1);
+        const double z0 = fco(m, 2, k), z1 = fco(m, 2, k + 1);
+        int cand[CASE_MAXS];
+        int nc = 0;
+        bool overflow = false, full = false;
+        for (int s = 0; s < ns; ++s) {
+            const double cx = cen[3 * s], cy = cen[3 * s + 1], cz = cen[3 * s + 2], r = rad[s];
+            /* conservative box-box reject */
+            if (x1 < cx - r || x0 > cx + r || y1 < cy - r || y0 > cy + r) continue;
+            if (dims == 3 && (z1 < cz - r || z0 > cz + r)) continue;
+            const double fx = fmax(fabs(x0 - cx), fabs(x1 - cx)), fy = fmax(fabs(y0 - cy), fabs(y1 - cy));
+            const double fz = dims == 3 ? fmax(fabs(z0 - cz), fabs(z1 - cz)) : 0.0;
+            if (fx * fx + fy * fy + fz * fz < r * r * (1.0 - 1e-12)) { full = true; break; }
+            if (nc < CASE_MAXS) cand[nc++] = s;
+            else overflow = true;
+        }
+        const int npts = dims == 3 ? nF * nF * nF : nF * nF;
+        int cnt = 0;
+        if (full) {
+            cnt = npts;
+        } else if (nc > 0) {
+            const int nzp = dims == 3 ? nF : 1;
+            for (int c = 1; c <= nzp; ++c) {
+                const double zh = z0 + (double)c / (double)(nF + 1) * (z1 - z0);
+                for (int b = 1; b <= nF; ++b) {
+                    const double yh = y0 + (double)b / (double)(nF + 1) * (y1 - y0);
+                    for (int a = 1; a <= nF; ++a) {
+                        const double xh = x0 + (double)a / (double)(nF + 1) * (x1 - x0);
+                        bool hit = false;
+                        const int nloop = overflow ? ns : nc;
+                        for (int q = 0; q < nloop && !hit; ++q) {
+                            const int s = overflow ? q : cand[q];
+                            const double r = rad[s];
+                            const double ex = xh - cen[3 * s], ey = yh - cen[3 * s + 1];
+                            double G;
+                            if (dims == 3) {
+                                const double ez = zh - cen[3 * s + 2];
+                                G = r * r - ((ex * ex + ey * ey) + ez * ez);
+                            } else {
+                                G = r * r - (ex * ex + ey * ey);
+                            }
+                            hit = G > 0.0;
+                        }
+                        cnt += hit;
+                    }
+                }
+            }
+        }
+        VF[vidx(m, i, j, k)] = table[cnt];
+    }
+}
+
+/* Deformation3D (src/Tools.jl:660-662) with period T, sampled at face centres incl. ghosts. */
+__global__ void k_case_deformation3d(DevMesh m, double t, double T, double* uf, double* vf, double* wf)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = n0 * n1 * n2;
+    const double pi = 3.141592653589793;
+    const double ct = cos(pi * t / T);
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < total; q += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(q % n0) + m.lo, j = (int)((q / n0) % n1) + m.lo, k = (int)(q / (n0 * n1)) + m.lo;
+        const double x = fco(m, 0, i), y = fco(m, 1, j), z = fco(m, 2, k);
+        const double xm = cco(m, 0, i), ym = cco(m, 1, j), zm = cco(m, 2, k);
+        const double sx = sin(pi * x), sy = sin(pi * y), sz = sin(pi * z);
+        uf[q] = ((2.0 * (sx * sx)) * sin(2.0 * pi * ym)) * sin(2.0 * pi * zm) * ct;
+        vf[q] = ((-(sy * sy)) * sin(2.0 * pi * xm)) * sin(2.0 * pi * zm) * ct;
+        wf[q] = ((-(sz * sz)) * sin(2.0 * pi * xm)) * sin(2.0 * pi * ym) * ct;
+    }
+}
+
+/* ---- launchers ------------------------------------------------------------------------ */
+void launch_vf_ghost(const DevMesh& m, const double* VFin, double* VFout, int nsm, cudaStream_t s)
+{
+    k_vf_ghost<<<nsm * 8, 256, 0, s>>>(m, VFin, VFout);
+}
+void launch_elvira_pure(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, int* list, int* count,
+                        double* partials, int nblocks, cudaStream_t s)
+{
+    k_elvira_pure<<<nblocks, PURE_THREADS, 0, s>>>(m, VF, nx, ny, nz, list, count, partials);
+}
+void launch_normal_ghost(const DevMesh& m, double* nx, double* ny, double* nz, int nsm, cudaStream_t s)
+{
+    k_normal_ghost<<<nsm * 8, 256, 0, s>>>(m, nx, ny, nz);
+}
+void launch_mass_final(const double* partials, int nblocks, double cellvol, double* out, cudaStream_t s)
+{
+    k_mass_final<<<1, 32, 0, s>>>(partials, nblocks, cellvol, out);
+}
+void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s)
+{
+    k_band_first<<<nsm * 8, 256, 0, s>>>(m, VF, bout);
+}
+void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neumann, int nsm, cudaStream_t s)
+{
+    k_band_ghost<<<nsm * 8, 256, 0, s>>>(m, bin, bout, neumann);
+}
+void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, int nsm, cudaStream_t s)
+{
+    k_band_sweep<<<nsm * 8, 256, 0, s>>>(m, bin, bout, n);
+}
+void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin, double* VFout, int* list, int* count,
+                        int nsm, cudaStream_t s)
+{
+    k_sl_classify<<<nsm * 8, 256, 0, s>>>(m, band, VFin, VFout, list, count);
+}
+void launch_to_float(const double* a, float* b, long n, double scale, int nsm, cudaStream_t s)
+{
+    k_to_float<<<nsm * 8, 256, 0, s>>>(a, b, n, scale);
+}
+void launch_case_spheres(const DevMesh& m, const double* cen, const double* rad, int n, int nF, int dims,
+                         const double* table, double* VF, int nsm, cudaStream_t s)
+{
+    k_case_spheres<<<nsm * 8, 128, 0, s>>>(m, cen, rad, n, nF, dims, table, VF);
+}
+void launch_case_deformation3d(const DevMesh& m, double t, double T, double* uf, double* vf, double* wf, int nsm,
+                               cudaStream_t s)
+{
+    k_case_deformation3d<<<nsm * 8, 256, 0, s>>>(m, t, T, uf, vf, wf);
+}
+
+} // namespace slvof

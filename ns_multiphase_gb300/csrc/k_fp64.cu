@@ -1,0 +1,654 @@
+/*
+ * k_fp64.cu — FP64 kernels of the SL-VOF path.  Built with -fmad=false: every expression
+ * keeps the reference's operation order and IEEE rounding, so results match the CPU
+ * restatement bit for bit (the elementary functions come from detmath.h).
+ *
+ *   k_elvira_iface64 : ELVIRA_calc!/check_normal! (src/ELVIRA.jl:62-137) for interface cells,
+ *                      one warp per cell, lane = candidate normal, warp argmin.
+ *   k_plic64         : computePLIC! (src/VF.jl:94-103) on every cell incl. ghosts, with the
+ *                      single-rank border copy folded in through the ghost source map.
+ *   k_sl64           : the SL cell update of transport! (src/Transport.jl:111-148): RK
+ *                      pre-image (project!, src/Tools.jl:392-641), pt2index!, cutTet
+ *                      (src/VFgeom.jl:713-900) with an explicit stack.
+ */
+#include "slvof_kernels.h"
+#include "slvof_dev.cuh"
+
+namespace slvof {
+
+__device__ __forceinline__ void load_table(CutCase* s_tab)
+{
+    for (int t = threadIdx.x; t < 16 * (int)sizeof(CutCase); t += blockDim.x)
+        reinterpret_cast<char*>(s_tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
+    __syncthreads();
+}
+
+/* ======================================================================================
+ * computePLIC2VF (src/VF.jl:219-278) of one cell for one plane.  The five "uncut" terms
+ * tetsign*tet_vol/(dx*dy*dz) of the cell are precomputed; a tet whose four distances are all
+ * negative is d2case case 1 and contributes exactly that term, so the running sum
+ * VF += ... is bit-identical to the reference's.
+ * ==================================================================================== */
+struct NbrGeom {
+    double X[2], Y[2], Z[2]; /* cell2verts corners (odd cells mirrored in x, src/VFgeom.jl:190-216) */
+    double tetsign;
+};
+
+__device__ __forceinline__ void nbr_geom(const DevMesh& m, int ii, int jj, int kk, NbrGeom& G)
+{
+    const bool even = ((ii + jj + kk) % 2) == 0;
+    G.X[0] = fco(m, 0, even ? ii : ii + 1);
+    G.X[1] = fco(m, 0, even ? ii + 1 : ii);
+    G.Y[0] = fco(m, 1, jj); G.Y[1] = fco(m, 1, jj + 1);
+    G.Z[0] = fco(m, 2, kk); G.Z[1] = fco(m, 2, kk + 1);
+    G.tetsign = even ? 1.0 : -1.0;
+}
+
+__device__ __noinline__ void cut_tet_accum64(const CutCase* tab, const NbrGeom& G, int t, double d0, double d1,
+                                             double d2, double d3, double cellvol, double& VF, int& err)
+{
+    double vx[8], vy[8], vz[8], d[4];
+    for (int n = 0; n < 4; ++n) {
+        const int v = tet5(t, n);
+        vx[n] = G.X[v & 1]; vy[n] = G.Y[(v >> 1) & 1]; vz[n] = G.Z[v >> 2];
+    }
+    const int cs = d2case(d0, d1, d2, d3, EPS64, err); /* in place, as computePLIC2VF does */
+    d[0] = d0; d[1] = d1; d[2] = d2; d[3] = d3;
+    const CutCase& C = tab[cs];
+    for (int n = 0; n < C.nvert; ++n) {
+        const int v1 = C.v1[n], v2 = C.v2[n];
+        const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+        vx[4 + n] = (1.0 - mu) * vx[v1] + mu * vx[v2];
+        vy[4 + n] = (1.0 - mu) * vy[v1] + mu * vy[v2];
+        vz[4 + n] = (1.0 - mu) * vz[v1] + mu * vz[v2];
+    }
+    for (int n = C.ntets - 1; n >= C.nntet - 1; --n) {
+        const int a = C.vtet[n][0], b = C.vtet[n][1], c = C.vtet[n][2], e = C.vtet[n][3];
+        const double tv = tet_vol(vx[a], vy[a], vz[a], vx[b], vy[b], vz[b], vx[c], vy[c], vz[c], vx[e], vy[e], vz[e]);
+        VF += G.tetsign * tv / cellvol;
+    }
+}
+
+__device__ __forceinline__ double plic2vf64(const CutCase* tab, const NbrGeom& G, const double* term, double full,
+                                            double a, double b, double e, double dist, double cellvol, int& err)
+{
+    const double px0 = a * G.X[0], px1 = a * G.X[1];
+    const double py0 = b * G.Y[0], py1 = b * G.Y[1];
+    const double pz0 = e * G.Z[0], pz1 = e * G.Z[1];
+    const double s00 = px0 + py0, s10 = px1 + py0, s01 = px0 + py1, s11 = px1 + py1;
+    double dv[8];
+    dv[0] = (s00 + pz0) - dist; dv[1] = (s10 + pz0) - dist; dv[2] = (s01 + pz0) - dist; dv[3] = (s11 + pz0) - dist;
+    dv[4] = (s00 + pz1) - dist; dv[5] = (s10 + pz1) - dist; dv[6] = (s01 + pz1) - dist; dv[7] = (s11 + pz1) - dist;
+    bool allneg = true, allpos = true;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) { allneg = allneg && dv[v] < 0.0; allpos = allpos && dv[v] > 0.0; }
+    if (allneg) return full;
+    if (allpos) return 0.0;
+    double VF = 0.0;
+#pragma unroll
+    for (int t = 0; t < 5; ++t) {
+        const double d0 = dv[tet5(t, 0)], d1 = dv[tet5(t, 1)], d2 = dv[tet5(t, 2)], d3 = dv[tet5(t, 3)];
+        if (d0 < 0.0 && d1 < 0.0 && d2 < 0.0 && d3 < 0.0) { VF += term[t]; continue; }
+        if (d0 > 0.0 && d1 > 0.0 && d2 > 0.0 && d3 > 0.0) continue;
+        cut_tet_accum64(tab, G, t, d0, d1, d2, d3, cellvol, VF, err);
+    }
+    return VF;
+}
+
+/* ======================================================================================
+ * ELVIRA for interface cells: one warp per cell, lane = candidate (family XY, XZ, YZ in the
+ * reference's order, outer list first), warp argmin keeping the first strict minimum.
+ * ==================================================================================== */
+constexpr int EL_WARPS = 4;
+
+__global__ void __launch_bounds__(EL_WARPS * 32) k_elvira_iface64(DevMesh m, const double* __restrict__ VF,
+                                                                  double* __restrict__ nx, double* __restrict__ ny,
+                                                                  double* __restrict__ nz, const int* __restrict__ list,
+                                                                  const int* __restrict__ count, int* work, int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    __shared__ double s_term[EL_WARPS][27][5];
+    __shared__ double s_full[EL_WARPS][27];
+    __shared__ double s_vf[EL_WARPS][27];
+    load_table(s_tab);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_items = *count;
+    const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
+    const int ncand = 9 * (fam_on[0] + fam_on[1] + fam_on[2]);
+    int err = 0;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(work, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= n_items) break;
+        const int L = list[item];
+        const int i = 1 + L % m.N[0];
+        const int j = 1 + (L / m.N[0]) % m.N[1];
+        const int k = 1 + L / (m.N[0] * m.N[1]);
+        if (lane < 27) {
+            NbrGeom G;
+            nbr_geom(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9, G);
+            double full = 0.0;
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+                const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), e = tet5(t, 3);
+                const double tv = tet_vol(G.X[a & 1], G.Y[(a >> 1) & 1], G.Z[a >> 2], G.X[b & 1], G.Y[(b >> 1) & 1],
+                                          G.Z[b >> 2], G.X[c & 1], G.Y[(c >> 1) & 1], G.Z[c >> 2], G.X[e & 1],
+                                          G.Y[(e >> 1) & 1], G.Z[e >> 2]);
+                const double term = G.tetsign * tv / m.cellvol;
+                s_term[w][lane][t] = term;
+                full += term;
+            }
+            s_full[w][lane] = full;
+            s_vf[w][lane] = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
+        }
+        __syncwarp();
+        const double* sv = s_vf[w];
+#define V3(a, b, c) sv[((c) + 1) * 9 + ((b) + 1) * 3 + ((a) + 1)]
+        double err_ = INFINITY, cx = 0.0, cy = 0.0, cz = 0.0;
+        if (lane < ncand) {
+            const int fam = lane / 9, a = (lane % 9) / 3, b = lane % 3;
+            int f = 0;
+            for (int q = 0, seen = 0; q < 3; ++q)
+                if (fam_on[q]) { if (seen == fam) { f = q; break; } ++seen; }
+            const int o1 = a == 2 ? 0 : -1, o2 = a == 0 ? 0 : 1; /* {-1,0},{-1,1},{0,1} */
+            const int i1 = b == 2 ? 0 : -1, i2 = b == 0 ? 0 : 1;
+            if (f == 0) { /* X-Y stencils: jj outer, ii inner (src/ELVIRA.jl:71-78) */
+                const double s2x = (V3(i2, 0, -1) * m.d[2] + V3(i2, 0, 0) * m.d[2]) + V3(i2, 0, 1) * m.d[2];
+                const double s1x = (V3(i1, 0, -1) * m.d[2] + V3(i1, 0, 0) * m.d[2]) + V3(i1, 0, 1) * m.d[2];
+                cx = -(s2x - s1x) / (cco(m, 0, i + i2) - cco(m, 0, i + i1));
+                const double s2y = (V3(0, o2, -1) * m.d[2] + V3(0, o2, 0) * m.d[2]) + V3(0, o2, 1) * m.d[2];
+                const double s1y = (V3(0, o1, -1) * m.d[2] + V3(0, o1, 0) * m.d[2]) + V3(0, o1, 1) * m.d[2];
+                cy = -(s2y - s1y) / (cco(m, 1, j + o2) - cco(m, 1, j + o1));
+                cz = V3(0, 0, 1) > V3(0, 0, -1) ? -1.0 : 1.0;
+            } else if (f == 1) { /* X-Z stencils: kk outer, ii inner (src/ELVIRA.jl:81-88) */
+                const double s2x = (V3(i2, -1, 0) * m.d[1] + V3(i2, 0, 0) * m.d[1]) + V3(i2, 1, 0) * m.d[1];
+                const double s1x = (V3(i1, -1, 0) * m.d[1] + V3(i1, 0, 0) * m.d[1]) + V3(i1, 1, 0) * m.d[1];
+                cx = -(s2x - s1x) / (cco(m, 0, i + i2) - cco(m, 0, i + i1));
+                cy = V3(0, 1, 0) > V3(0, -1, 0) ? -1.0 : 1.0;
+                const double s2z = (V3(0, -1, o2) * m.d[1] + V3(0, 0, o2) * m.d[1]) + V3(0, 1, o2) * m.d[1];
+                const double s1z = (V3(0, -1, o1) * m.d[1] + V3(0, 0, o1) * m.d[1]) + V3(0, 1, o1) * m.d[1];
+                cz = -(s2z - s1z) / (cco(m, 2, k + o2) - cco(m, 2, k + o1));
+            } else { /* Y-Z stencils: kk outer, jj inner (src/ELVIRA.jl:91-98) */
+                cx = V3(1, 0, 0) > V3(-1, 0, 0) ? -1.0 : 1.0;
+                const double s2y = (V3(-1, i2, 0) * m.d[0] + V3(0, i2, 0) * m.d[0]) + V3(1, i2, 0) * m.d[0];
+                const double s1y = (V3(-1, i1, 0) * m.d[0] + V3(0, i1, 0) * m.d[0]) + V3(1, i1, 0) * m.d[0];
+                cy = -(s2y - s1y) / (cco(m, 1, j + i2) - cco(m, 1, j + i1));
+                const double s2z = (V3(-1, 0, o2) * m.d[0] + V3(0, 0, o2) * m.d[0]) + V3(1, 0, o2) * m.d[0];
+                const double s1z = (V3(-1, 0, o1) * m.d[0] + V3(0, 0, o1) * m.d[0]) + V3(1, 0, o1) * m.d[0];
+                cz = -(s2z - s1z) / (cco(m, 2, k + o2) - cco(m, 2, k + o1));
+            }
+            /* check_normal! (src/ELVIRA.jl:106-137) */
+            const double norm = sqrt((cx * cx + cy * cy) + cz * cz);
+            cx = cx / norm; cy = cy / norm; cz = cz / norm;
+            const double dist = compute_dist64(m, i, j, k, cx, cy, cz, V3(0, 0, 0));
+            double e2 = 0.0;
+            for (int c = 0; c < 27; ++c) {
+                NbrGeom G;
+                nbr_geom(m, i - 1 + c % 3, j - 1 + (c / 3) % 3, k - 1 + c / 9, G);
+                const double v_ = plic2vf64(s_tab, G, s_term[w][c], s_full[w][c], cx, cy, cz, dist, m.cellvol, err);
+                const double r = sv[c] - v_;
+                e2 += r * r;
+            }
+            err_ = e2;
+        }
+#undef V3
+        /* First strict minimum in candidate order: err < running best starting at Inf, so
+         * NaN and Inf never win and ties go to the lower lane. */
+        double be = err_ < INFINITY ? err_ : INFINITY;
+        int bl = err_ < INFINITY ? lane : 32;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, be, off);
+            const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
+            if (ob < be || (ob == be && ol < bl)) { be = ob; bl = ol; }
+        }
+        if (bl < 32 && lane == bl) {
+            const long c = cidx(m, i, j, k);
+            nx[c] = cx; ny[c] = cy; nz[c] = cz;
+        }
+        __syncwarp();
+    }
+    if (err) atomicOr(errw, err);
+}
+
+/* ======================================================================================
+ * computePLIC! on every cell; D(p) = computeDist at the border-copy source of p.
+ * ==================================================================================== */
+/* The plane each cell donates with: its own border-updated normal and D.  Phase +1/-1 marks
+ * |D| = Lx+Ly+Lz with a zero or axis normal: every point of the domain and its ghosts is then
+ * strictly on one side, so a clip against the plane is all liquid (+1) or all gas (-1). */
+__device__ __forceinline__ void plic_outputs(const DevMesh& m, long t, int ip, int jp, int kp, double dist,
+                                             const double* __restrict__ nx, const double* __restrict__ ny,
+                                             const double* __restrict__ nz, double* __restrict__ D,
+                                             float4* __restrict__ planes, signed char* __restrict__ phase)
+{
+    D[t] = dist;
+    const double a = nx[t], b = ny[t], e = nz[t];
+    const double l1 = fabs(a) + fabs(b) + fabs(e);
+    phase[t] = (l1 <= 1.0 && dist == m.Lsum) ? 1 : ((l1 <= 1.0 && dist == -m.Lsum) ? -1 : 0);
+    if (planes) {
+        const double Dl = dist - ((a * fco(m, 0, ip) + b * fco(m, 1, jp)) + e * fco(m, 2, kp));
+        planes[t] = make_float4((float)(a * m.d[0]), (float)(b * m.d[1]), (float)(e * m.d[2]), (float)Dl);
+    }
+}
+
+/* Pure cells get D = -/+(Lx+Ly+Lz) directly; cells whose border source holds an interface
+ * VF go to a list so that the FP64 plane-constant solve runs in full warps. */
+__global__ void k_plic_pure(DevMesh m, const double* __restrict__ VF, const double* __restrict__ nx,
+                            const double* __restrict__ ny, const double* __restrict__ nz, double* __restrict__ D,
+                            float4* __restrict__ planes, signed char* __restrict__ phase, int* list, int* count)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = n0 * n1 * n2;
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long base = blockIdx.x * (long)blockDim.x; base < total; base += stride) {
+        const long t = base + threadIdx.x;
+        bool defer = false;
+        if (t < total) {
+            const int ip = (int)(t % n0) + m.lo, jp = (int)((t / n0) % n1) + m.lo, kp = (int)(t / (n0 * n1)) + m.lo;
+            const int i = ghost_src_1d(ip, m.N[0], m.g, m.per[0], false);
+            const int j = ghost_src_1d(jp, m.N[1], m.g, m.per[1], false);
+            const int k = ghost_src_1d(kp, m.N[2], m.g, m.per[2], false);
+            const double v = VF[vidx(m, i, j, k)];
+            if (v < m.VFlo) plic_outputs(m, t, ip, jp, kp, -m.Lsum, nx, ny, nz, D, planes, phase);
+            else if (v > m.VFhi) plic_outputs(m, t, ip, jp, kp, m.Lsum, nx, ny, nz, D, planes, phase);
+            else defer = true; /* interface (or NaN) source */
+        }
+        warp_append(defer, (int)t, list, count);
+    }
+}
+
+/* computeDist (src/VF.jl:109-156) for the deferred cells: D(p) = computeDist at the border
+ * source of p (computePLIC! then update_borders!, src/VF.jl:94-103). */
+__global__ void k_plic_iface(DevMesh m, const double* __restrict__ VF, const double* __restrict__ nx,
+                             const double* __restrict__ ny, const double* __restrict__ nz, double* __restrict__ D,
+                             float4* __restrict__ planes, signed char* __restrict__ phase, const int* __restrict__ list,
+                             const int* __restrict__ count)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g;
+    const int n = *count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const long t = list[q];
+        const int ip = (int)(t % n0) + m.lo, jp = (int)((t / n0) % n1) + m.lo, kp = (int)(t / (n0 * n1)) + m.lo;
+        const int i = ghost_src_1d(ip, m.N[0], m.g, m.per[0], false);
+        const int j = ghost_src_1d(jp, m.N[1], m.g, m.per[1], false);
+        const int k = ghost_src_1d(kp, m.N[2], m.g, m.per[2], false);
+        const long c = cidx(m, i, j, k);
+        const double dist = compute_dist64(m, i, j, k, nx[c], ny[c], nz[c], VF[vidx(m, i, j, k)]);
+        plic_outputs(m, t, ip, jp, kp, dist, nx, ny, nz, D, planes, phase);
+    }
+}
+
+/* ======================================================================================
+ * Pre-image tracing.  Face-velocity interpolation (get_velocity_{u,v,w}face,
+ * src/Tools.jl:516-641): the interval search and weight of one coordinate against face or
+ * centre positions are shared between the three components that use them.
+ * ==================================================================================== */
+struct Axis64 {
+    int I;
+    double w1;
+};
+
+__device__ __forceinline__ Axis64 search64(const DevMesh& m, int q, bool face, double p, int seed)
+{
+    const double* a = face ? m.f[q] : m.c[q];
+    int i = seed;
+    while (p - __ldg(a + (i - m.lo)) < 0.0 && i > m.lo) i = i - 1;
+    while (p - __ldg(a + (i + 1 - m.lo)) >= 0.0 && i + 1 < m.hi[q]) i = i + 1;
+    const double lo = __ldg(a + (i - m.lo)), hi = __ldg(a + (i + 1 - m.lo));
+    return {i, sdiv(p - lo, hi - lo)};
+}
+
+__device__ __forceinline__ double trilinear64(const DevMesh& m, const double* __restrict__ f, Axis64 X, Axis64 Y,
+                                              Axis64 Z)
+{
+    const double wx1 = X.w1, wx2 = 1.0 - X.w1, wy1 = Y.w1, wy2 = 1.0 - Y.w1, wz1 = Z.w1, wz2 = 1.0 - Z.w1;
+    const long b = cidx(m, X.I, Y.I, Z.I);
+    const long sj = m.cs1, sk = m.cs2;
+    const double f000 = __ldg(f + b), f100 = __ldg(f + b + 1), f010 = __ldg(f + b + sj), f110 = __ldg(f + b + 1 + sj);
+    const double f001 = __ldg(f + b + sk), f101 = __ldg(f + b + 1 + sk), f011 = __ldg(f + b + sj + sk),
+                 f111 = __ldg(f + b + 1 + sj + sk);
+    return wz1 * (wy1 * (wx1 * f111 + wx2 * f011) + wy2 * (wx1 * f101 + wx2 * f001)) +
+           wz2 * (wy1 * (wx1 * f110 + wx2 * f010) + wy2 * (wx1 * f100 + wx2 * f000));
+}
+
+struct Vel64 {
+    const double *uf, *vf, *wf;
+};
+
+__device__ __forceinline__ void velocity64(const DevMesh& m, const Vel64& V, double px, double py, double pz, int i,
+                                           int j, int k, double& u, double& v, double& w)
+{
+    const Axis64 fx = search64(m, 0, true, px, i), cx = search64(m, 0, false, px, i);
+    const Axis64 fy = search64(m, 1, true, py, j), cy = search64(m, 1, false, py, j);
+    const Axis64 fz = search64(m, 2, true, pz, k), cz = search64(m, 2, false, pz, k);
+    u = trilinear64(m, V.uf, fx, cy, cz);
+    v = trilinear64(m, V.vf, cx, fy, cz);
+    w = trilinear64(m, V.wf, cx, cy, fz);
+}
+
+/* project!, src/Tools.jl:392-418 */
+__device__ __forceinline__ void project64(const DevMesh& m, const Vel64& V, double& px, double& py, double& pz, int i,
+                                          int j, int k, double dt)
+{
+    double u1, v1, w1;
+    velocity64(m, V, px, py, pz, i, j, k, u1, v1, w1);
+    if (m.projection == 2) {
+        double u2, v2, w2, u3, v3, w3, u4, v4, w4;
+        velocity64(m, V, px - 0.5 * dt * u1, py - 0.5 * dt * v1, pz - 0.5 * dt * w1, i, j, k, u2, v2, w2);
+        velocity64(m, V, px - 0.5 * dt * u2, py - 0.5 * dt * v2, pz - 0.5 * dt * w2, i, j, k, u3, v3, w3);
+        velocity64(m, V, px - dt * u3, py - dt * v3, pz - dt * w3, i, j, k, u4, v4, w4);
+        px = px + (-dt) / 6.0 * (((u1 + 2.0 * u2) + 2.0 * u3) + u4);
+        py = py + (-dt) / 6.0 * (((v1 + 2.0 * v2) + 2.0 * v3) + v4);
+        pz = pz + (-dt) / 6.0 * (((w1 + 2.0 * w2) + 2.0 * w3) + w4);
+    } else if (m.projection == 0) {
+        px = px + (-dt) * u1;
+        py = py + (-dt) * v1;
+        pz = pz + (-dt) * w1;
+    } else {
+        double u2, v2, w2;
+        velocity64(m, V, px - 0.5 * dt * u1, py - 0.5 * dt * v1, pz - 0.5 * dt * w1, i, j, k, u2, v2, w2);
+        px = px + (-dt) * u2;
+        py = py + (-dt) * v2;
+        pz = pz + (-dt) * w2;
+    }
+}
+
+/* pt2index!, src/Tools.jl:424-434, with the index kept inside the coordinate arrays. */
+__device__ __forceinline__ int pt2index1(const DevMesh& m, int q, double p, int I, int& err)
+{
+    while (p > fco(m, q, I + 1) + EPS64) {
+        if (I >= m.hi[q]) { err |= ERR_INDEX; break; }
+        I += 1;
+    }
+    while (p < fco(m, q, I) - EPS64) {
+        if (I <= m.lo) { err |= ERR_INDEX; break; }
+        I -= 1;
+    }
+    return I;
+}
+
+/* ======================================================================================
+ * cutTet with an explicit stack.  Each frame is one recursion level of the reference: the
+ * parent tet, the new vertices on the cutting mesh plane, their side-1 indices, the cut
+ * case and the running (vol, vLiq) of its children, so partial sums are added in exactly
+ * the reference's tree order.
+ * ==================================================================================== */
+struct Frame64 {
+    double x[8], y[8], z[8];
+    double acc_v, acc_l;
+    short ind[8][3]; /* side-1 indices; side 2 differs only in the cut direction (= cut) */
+    signed char cs, next, dir, flags;
+    int cut;
+};
+
+struct Plic64 {
+    const double *nx, *ny, *nz, *D;
+};
+
+/* Leaf: clip by the donor cell's PLIC plane (src/VFgeom.jl:757-830). */
+__device__ __forceinline__ void leaf64(const DevMesh& m, const CutCase* tab, const Plic64& P, const double* cx,
+                                       const double* cy, const double* cz, int di, int dj, int dk, double& rv,
+                                       double& rl, int& err)
+{
+    const long c = cidx(m, di, dj, dk);
+    const double a = __ldg(P.nx + c), b = __ldg(P.ny + c), e = __ldg(P.nz + c), Dd = __ldg(P.D + c);
+    double d[4], vx[8], vy[8], vz[8];
+    for (int n = 0; n < 4; ++n) {
+        d[n] = ((a * cx[n] + b * cy[n]) + e * cz[n]) - Dd;
+        vx[n] = cx[n]; vy[n] = cy[n]; vz[n] = cz[n];
+    }
+    double c0 = d[0], c1 = d[1], c2 = d[2], c3 = d[3]; /* d2case works on a copy here */
+    const int cs = d2case(c0, c1, c2, c3, EPS64, err);
+    const CutCase& C = tab[cs];
+    for (int n = 0; n < C.nvert; ++n) {
+        const int v1 = C.v1[n], v2 = C.v2[n];
+        const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+        vx[4 + n] = (1.0 - mu) * vx[v1] + mu * vx[v2];
+        vy[4 + n] = (1.0 - mu) * vy[v1] + mu * vy[v2];
+        vz[4 + n] = (1.0 - mu) * vz[v1] + mu * vz[v2];
+    }
+    double vol = 0.0, liq = 0.0;
+    for (int n = C.ntets - 1; n >= C.nntet - 1; --n) {
+        const int p = C.vtet[n][0], q = C.vtet[n][1], r = C.vtet[n][2], s = C.vtet[n][3];
+        const double tv = tet_vol(vx[p], vy[p], vz[p], vx[q], vy[q], vz[q], vx[r], vy[r], vz[r], vx[s], vy[s], vz[s]);
+        vol += tv;
+        liq += tv;
+    }
+    for (int n = 0; n < C.nntet - 1; ++n) {
+        const int p = C.vtet[n][0], q = C.vtet[n][1], r = C.vtet[n][2], s = C.vtet[n][3];
+        vol += tet_vol(vx[p], vy[p], vz[p], vx[q], vy[q], vz[q], vx[r], vy[r], vz[r], vx[s], vy[s], vz[s]);
+    }
+    rv = vol;
+    rl = liq;
+}
+
+__device__ __forceinline__ void form_child64(const Frame64& F, const CutCase* tab, int n, double* cx, double* cy,
+                                             double* cz, int (*ci)[3])
+{
+    const CutCase& C = tab[F.cs];
+    const int side = C.side[n];
+    for (int nn = 0; nn < 4; ++nn) {
+        const int v = C.vtet[n][nn];
+        cx[nn] = F.x[v]; cy[nn] = F.y[v]; cz[nn] = F.z[v];
+        ci[nn][0] = F.ind[v][0]; ci[nn][1] = F.ind[v][1]; ci[nn][2] = F.ind[v][2];
+        if (side == 1) ci[nn][(int)F.dir] = F.cut;
+    }
+}
+
+__device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P, double* cx, double* cy, double* cz,
+                           int (*ci)[3], double& out_v, double& out_l, int& err)
+{
+    Frame64 st[CLIP_STACK];
+    int depth = 0, flags = 0, leaves = 0;
+    for (;;) {
+        int dir = -1, cut = 0;
+        for (int q = 0; q < 3; ++q) {
+            if (flags & (1 << q)) continue;
+            const int mx = max(max(ci[0][q], ci[1][q]), max(ci[2][q], ci[3][q]));
+            const int mn = min(min(ci[0][q], ci[1][q]), min(ci[2][q], ci[3][q]));
+            if (mx > mn) { dir = q; cut = mx; break; }
+            flags |= 1 << q;
+        }
+        double rv, rl;
+        if (dir >= 0 && depth == CLIP_STACK) { err |= ERR_DEPTH; dir = -1; }
+        if (dir < 0) {
+            if (++leaves > CLIP_MAX_LEAVES) { /* bounded work even for clamped, far-away pre-images */
+                err |= ERR_DEPTH;
+                out_v = 0.0; out_l = 0.0;
+                return;
+            }
+            leaf64(m, tab, P, cx, cy, cz, ci[0][0], ci[0][1], ci[0][2], rv, rl, err);
+        } else {
+            Frame64& F = st[depth];
+            const double pl = fco(m, dir, cut);
+            const double* cd = dir == 0 ? cx : (dir == 1 ? cy : cz);
+            double d[4];
+            for (int n = 0; n < 4; ++n) d[n] = cd[n] - pl;
+            double c0 = d[0], c1 = d[1], c2 = d[2], c3 = d[3];
+            const int cs = d2case(c0, c1, c2, c3, EPS64, err);
+            for (int n = 0; n < 4; ++n) {
+                F.x[n] = cx[n]; F.y[n] = cy[n]; F.z[n] = cz[n];
+                F.ind[n][0] = (short)ci[n][0]; F.ind[n][1] = (short)ci[n][1]; F.ind[n][2] = (short)ci[n][2];
+                F.ind[n][dir] = (short)min(ci[n][dir], cut - 1);
+            }
+            const CutCase& C = tab[cs];
+            for (int n = 0; n < C.nvert; ++n) {
+                const int v1 = C.v1[n], v2 = C.v2[n];
+                const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+                const double x = (1.0 - mu) * F.x[v1] + mu * F.x[v2];
+                const double y = (1.0 - mu) * F.y[v1] + mu * F.y[v2];
+                const double z = (1.0 - mu) * F.z[v1] + mu * F.z[v2];
+                F.x[4 + n] = x; F.y[4 + n] = y; F.z[4 + n] = z;
+                /* pt2index! seeded with vertex n's side-1 index (src/VFgeom.jl:854-857), then
+                 * bounded by the edge end points (src/VFgeom.jl:859-862) */
+                const int I0 = pt2index1(m, 0, x, F.ind[n][0], err);
+                const int I1 = pt2index1(m, 1, y, F.ind[n][1], err);
+                const int I2 = pt2index1(m, 2, z, F.ind[n][2], err);
+                const int Iv[3] = {I0, I1, I2};
+                for (int q = 0; q < 3; ++q) {
+                    int val = max(Iv[q], min((int)F.ind[v1][q], (int)F.ind[v2][q]));
+                    val = min(val, max((int)F.ind[v1][q], (int)F.ind[v2][q]));
+                    F.ind[4 + n][q] = (short)val;
+                }
+                F.ind[4 + n][dir] = (short)(cut - 1);
+            }
+            F.cs = (signed char)cs; F.dir = (signed char)dir; F.cut = cut; F.flags = (signed char)flags;
+            F.acc_v = 0.0; F.acc_l = 0.0; F.next = 1;
+            ++depth;
+            form_child64(F, tab, 0, cx, cy, cz, ci);
+            continue;
+        }
+        for (;;) {
+            if (depth == 0) { out_v = rv; out_l = rl; return; }
+            Frame64& F = st[depth - 1];
+            F.acc_v += rv;
+            F.acc_l += rl;
+            if (F.next < tab[F.cs].ntets) {
+                form_child64(F, tab, F.next, cx, cy, cz, ci);
+                F.next += 1;
+                flags = F.flags;
+                break;
+            }
+            rv = F.acc_v; rl = F.acc_l;
+            --depth;
+        }
+    }
+}
+
+/* Pure-donor shortcut.  If every donor cell the pre-image can reach has phase code +1 (or
+ * every one -1), every leaf of the clip is d2case case 1 (or 16), vLiq and vol are the same
+ * sums (or vLiq is zero), and vLiq/vol is exactly 1 (or 0) whenever vol is positive. */
+__device__ __forceinline__ int pure_phase(const DevMesh& m, const signed char* __restrict__ phase, int lo0, int hi0,
+                                          int lo1, int hi1, int lo2, int hi2)
+{
+    if (hi0 - lo0 > 3 || hi1 - lo1 > 3 || hi2 - lo2 > 3) return 0;
+    int ph = 2;
+    for (int k = lo2; k <= hi2; ++k)
+        for (int j = lo1; j <= hi1; ++j)
+            for (int i = lo0; i <= hi0; ++i) {
+                const int p = __ldg(phase + cidx(m, i, j, k));
+                if (p == 0 || (ph != 2 && p != ph)) return 0;
+                ph = p;
+            }
+    return ph;
+}
+
+constexpr int SL_THREADS = 128;
+
+/* SL update of one band cell: cell2tets!(project_verts=true, compute_indices=true)
+ * (src/VFgeom.jl:345-420), then cutTet on the five tets and VFnew = vLiq/vol
+ * (src/Transport.jl:116-145). */
+__device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, double dt,
+                                          const signed char* __restrict__ phase, double* __restrict__ VFout,
+                                          const Vel64& V, const Plic64& P, int L, int& err)
+{
+    const int i = 1 + L % m.N[0];
+    const int j = 1 + (L / m.N[0]) % m.N[1];
+    const int k = 1 + L / (m.N[0] * m.N[1]);
+    const bool even = ((i + j + k) % 2) == 0;
+    const double tetsign = even ? 1.0 : -1.0;
+    const double X[2] = {fco(m, 0, even ? i : i + 1), fco(m, 0, even ? i + 1 : i)};
+    const double Y[2] = {fco(m, 1, j), fco(m, 1, j + 1)};
+    const double Z[2] = {fco(m, 2, k), fco(m, 2, k + 1)};
+    double px[8], py[8], pz[8];
+    int vi[8][3];
+#pragma unroll 1
+    for (int v = 0; v < 8; ++v) {
+        double x = X[v & 1], y = Y[(v >> 1) & 1], z = Z[v >> 2];
+        project64(m, V, x, y, z, i, j, k, dt);
+        px[v] = x; py[v] = y; pz[v] = z;
+        vi[v][0] = pt2index1(m, 0, x, i, err);
+        vi[v][1] = pt2index1(m, 1, y, j, err);
+        vi[v][2] = pt2index1(m, 2, z, k, err);
+    }
+    const long out = vidx(m, i, j, k);
+    if (m.fast_pure) {
+        int lo0 = vi[0][0], hi0 = vi[0][0], lo1 = vi[0][1], hi1 = vi[0][1], lo2 = vi[0][2], hi2 = vi[0][2];
+        for (int v = 1; v < 8; ++v) {
+            lo0 = min(lo0, vi[v][0]); hi0 = max(hi0, vi[v][0]);
+            lo1 = min(lo1, vi[v][1]); hi1 = max(hi1, vi[v][1]);
+            lo2 = min(lo2, vi[v][2]); hi2 = max(hi2, vi[v][2]);
+        }
+        const int ph = pure_phase(m, phase, lo0, hi0, lo1, hi1, lo2, hi2);
+        if (ph != 0) {
+            double vol = 0.0;
+            for (int t = 0; t < 5; ++t) {
+                const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), e = tet5(t, 3);
+                vol += tetsign * tet_vol(px[a], py[a], pz[a], px[b], py[b], pz[b], px[c], py[c], pz[c], px[e], py[e],
+                                         pz[e]);
+            }
+            if (vol > 0.25 * m.cellvol && vol < 4.0 * m.cellvol) {
+                VFout[out] = ph > 0 ? 1.0 : 0.0;
+                return;
+            }
+        }
+    }
+    double vol = 0.0, liq = 0.0;
+#pragma unroll 1
+    for (int t = 0; t < 5; ++t) {
+        double cx[4], cy[4], cz[4];
+        int ci[4][3];
+        for (int n = 0; n < 4; ++n) {
+            const int v = tet5(t, n);
+            cx[n] = px[v]; cy[n] = py[v]; cz[n] = pz[v];
+            ci[n][0] = vi[v][0]; ci[n][1] = vi[v][1]; ci[n][2] = vi[v][2];
+        }
+        double tv, tl;
+        clip_tet64(m, tab, P, cx, cy, cz, ci, tv, tl, err);
+        vol += tetsign * tv;
+        liq += tetsign * tl;
+    }
+    if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
+    VFout[out] = liq / vol;
+}
+
+__global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const signed char* __restrict__ phase,
+                                                     double* __restrict__ VFout, Vel64 V, Plic64 P,
+                                                     const int* __restrict__ list, const int* __restrict__ count,
+                                                     int* work, int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    load_table(s_tab);
+    const int lane = threadIdx.x & 31;
+    const int n_items = *count;
+    int err = 0;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(work, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_items) break;
+        const int item = base + lane;
+        if (item < n_items) sl_cell64(m, s_tab, dt, phase, VFout, V, P, list[item], err);
+        __syncwarp();
+    }
+    if (err) atomicOr(errw, err);
+}
+
+/* ---- launchers ------------------------------------------------------------------------ */
+void launch_elvira_iface64(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
+                           const int* count, int* work, int* errw, int nsm, cudaStream_t s)
+{
+    k_elvira_iface64<<<nsm * 8, EL_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, errw);
+}
+
+void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz, double* D,
+                   float4* planes, signed char* phase, int* list, int* count, int nsm, cudaStream_t s)
+{
+    k_plic_pure<<<nsm * 8, 256, 0, s>>>(m, VF, nx, ny, nz, D, planes, phase, list, count);
+    k_plic_iface<<<nsm * 4, 128, 0, s>>>(m, VF, nx, ny, nz, D, planes, phase, list, count);
+}
+
+void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout, const double* uf, const double* vf,
+                 const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                 const signed char* phase, const int* list, const int* count, int* work, int* errw, int nsm,
+                 cudaStream_t s)
+{
+    (void)VFin;
+    Vel64 V{uf, vf, wf};
+    Plic64 P{nx, ny, nz, D};
+    k_sl64<<<nsm * 8, SL_THREADS, 0, s>>>(m, dt, phase, VFout, V, P, list, count, work, errw);
+}
+
+} // namespace slvof

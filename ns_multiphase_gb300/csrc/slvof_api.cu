@@ -1,0 +1,654 @@
+/*
+ * slvof_api.cu — C ABI of the SL-VOF library (declared in include/slvof.h).
+ *
+ * A context owns every device buffer of one mesh and a private stream.  The resident step
+ * runs, without host round trips between kernels:
+ *   classify band cells + copy the rest  ->  SL update (FP64 or mixed)  ->  VF ghost fill
+ *   ->  ELVIRA pure cells + interface list + mass partials  ->  ELVIRA candidates
+ *   ->  normal borders  ->  PLIC distances  ->  [band]  ->  [mass]
+ * and reads back the device error word once at the end.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/slvof.h"
+#include "slvof_kernels.h"
+
+using namespace slvof;
+
+struct slvof_ctx {
+    int precision = SLVOF_FP64;
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    DevMesh m{};
+    double* coords = nullptr;
+    long ncell = 0, nvf = 0;
+    double* VF[2] = {nullptr, nullptr};
+    int vcur = 0;
+    double *uf = nullptr, *vf = nullptr, *wf = nullptr;
+    float *uf32 = nullptr, *vf32 = nullptr, *wf32 = nullptr;
+    double *nx = nullptr, *ny = nullptr, *nz = nullptr, *D = nullptr;
+    float4* planes = nullptr;     /* mixed: donor planes in cell units */
+    signed char* phase = nullptr; /* pure-donor codes of the PLIC pass */
+    short* band[2] = {nullptr, nullptr};
+    int bcur = 0;
+    int* list_sl = nullptr;
+    int* list_if = nullptr;
+    int* list_plic = nullptr; /* cells whose PLIC solve is deferred to full warps */
+    int* ctr = nullptr; /* 0 sl count, 1 if count, 2 sl work, 3 if work, 4 error bits */
+    double* partials = nullptr;
+    int npure = 0;
+    double* mass_d = nullptr;
+    double* table = nullptr; /* case generator scratch */
+    int table_n = 0;
+    double* spheres = nullptr;
+    int spheres_n = 0;
+    bool normals_valid = false;
+    double last_ms = 0.0;
+    cudaStream_t own_stream = nullptr;
+    cudaEvent_t sev[SLVOF_NSTAGES][2] = {};
+    bool sran[SLVOF_NSTAGES] = {};
+    std::string err;
+};
+
+namespace {
+
+enum { C_SL = 0, C_IF = 1, C_SLW = 2, C_IFW = 3, C_ERR = 4, C_PL = 5, C_N = 8 };
+
+int fail(slvof_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                             \
+    do {                                                                                                     \
+        cudaError_t e_ = (call);                                                                             \
+        if (e_ != cudaSuccess) return fail(c, SLVOF_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+enum { S_CLASSIFY, S_SL, S_VFGHOST, S_PURE, S_IFACE, S_NGHOST, S_PLIC, S_BAND, S_MASS };
+
+int begin(slvof_ctx* c)
+{
+    if (!c) return SLVOF_E_ARG;
+    CK(cudaSetDevice(c->device));
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (bool& r : c->sran) r = false;
+    return 0;
+}
+
+/* stage markers: events around each launch group */
+void s_beg(slvof_ctx* c, int s)
+{
+    cudaEventRecord(c->sev[s][0], c->stream);
+    c->sran[s] = true;
+}
+void s_end(slvof_ctx* c, int s) { cudaEventRecord(c->sev[s][1], c->stream); }
+
+/* Synchronise, time the call and fold the device error word into the status. */
+int finish(slvof_ctx* c, bool read_err = true)
+{
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    if (!read_err) return SLVOF_OK;
+    int e = 0;
+    CK(cudaMemcpy(&e, c->ctr + C_ERR, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "device error bits 0x%x (1 index range, 2 clip depth, 4 NaN distance, 8 volume)", e);
+        c->err = buf;
+    }
+    return e;
+}
+
+int clear_err(slvof_ctx* c)
+{
+    CK(cudaMemsetAsync(c->ctr + C_ERR, 0, sizeof(int), c->stream));
+    return 0;
+}
+
+/* ---- stages (enqueue only) -------------------------------------------------------------- */
+int st_vf_ghost_inplace(slvof_ctx* c)
+{
+    const int o = 1 - c->vcur;
+    CK(cudaMemcpyAsync(c->VF[o], c->VF[c->vcur], c->nvf * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    launch_vf_ghost(c->m, c->VF[c->vcur], c->VF[o], c->nsm, c->stream);
+    c->vcur = o;
+    return 0;
+}
+
+int st_normals(slvof_ctx* c)
+{
+    CK(cudaMemsetAsync(c->ctr + C_IF, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_IFW, 0, sizeof(int), c->stream));
+    s_beg(c, S_PURE);
+    launch_elvira_pure(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->partials, c->npure,
+                       c->stream);
+    s_end(c, S_PURE);
+    s_beg(c, S_IFACE);
+    if (c->precision == SLVOF_FP64)
+        launch_elvira_iface64(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->ctr + C_IFW,
+                              c->ctr + C_ERR, c->nsm, c->stream);
+    else
+        launch_elvira_iface32(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->ctr + C_IFW,
+                              c->nsm, c->stream);
+    s_end(c, S_IFACE);
+    s_beg(c, S_NGHOST);
+    launch_normal_ghost(c->m, c->nx, c->ny, c->nz, c->nsm, c->stream);
+    s_end(c, S_NGHOST);
+    c->normals_valid = true;
+    return 0;
+}
+
+int st_plic(slvof_ctx* c)
+{
+    s_beg(c, S_PLIC);
+    CK(cudaMemsetAsync(c->ctr + C_PL, 0, sizeof(int), c->stream));
+    launch_plic64(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->D, c->planes, c->phase, c->list_plic, c->ctr + C_PL,
+                  c->nsm, c->stream);
+    s_end(c, S_PLIC);
+    return 0;
+}
+
+int st_band(slvof_ctx* c)
+{
+    int b = c->bcur;
+    s_beg(c, S_BAND);
+    launch_band_first(c->m, c->VF[c->vcur], c->band[1 - b], c->nsm, c->stream);
+    launch_band_ghost(c->m, c->band[b], c->band[1 - b], true, c->nsm, c->stream);
+    b = 1 - b;
+    for (int n = 1; n <= c->m.nband; ++n) {
+        launch_band_sweep(c->m, c->band[b], c->band[1 - b], n, c->nsm, c->stream);
+        launch_band_ghost(c->m, c->band[b], c->band[1 - b], false, c->nsm, c->stream);
+        b = 1 - b;
+    }
+    c->bcur = b;
+    s_end(c, S_BAND);
+    return 0;
+}
+
+int st_transport(slvof_ctx* c, double dt)
+{
+    const int o = 1 - c->vcur;
+    CK(cudaMemsetAsync(c->ctr + C_SL, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_SLW, 0, sizeof(int), c->stream));
+    s_beg(c, S_CLASSIFY);
+    launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
+    s_end(c, S_CLASSIFY);
+    s_beg(c, S_SL);
+    if (c->precision == SLVOF_FP64)
+        launch_sl64(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->phase,
+                    c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
+    else
+        launch_sl32(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
+                    c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
+    s_end(c, S_SL);
+    s_beg(c, S_VFGHOST);
+    launch_vf_ghost(c->m, c->VF[c->vcur], c->VF[o], c->nsm, c->stream);
+    s_end(c, S_VFGHOST);
+    c->vcur = o;
+    c->normals_valid = false;
+    return 0;
+}
+
+int st_mass(slvof_ctx* c, double* mass, bool partials_ready)
+{
+    s_beg(c, S_MASS);
+    if (!partials_ready)
+        launch_elvira_pure(c->m, c->VF[c->vcur], nullptr, nullptr, nullptr, nullptr, nullptr, c->partials, c->npure,
+                           c->stream);
+    launch_mass_final(c->partials, c->npure, c->m.cellvol, c->mass_d, c->stream);
+    s_end(c, S_MASS);
+    CK(cudaMemcpyAsync(mass, c->mass_d, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    return 0;
+}
+
+int h2d(slvof_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    if (!src) return fail(c, SLVOF_E_ARG, "null host pointer");
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream));
+    return 0;
+}
+int d2h(slvof_ctx* c, void* dst, const void* src, size_t bytes)
+{
+    if (!dst) return fail(c, SLVOF_E_ARG, "null host pointer");
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return 0;
+}
+
+/* Mixed mode keeps FP32 face velocities in cells per unit time (u/dx, v/dy, w/dz). */
+void to_float_velocity(slvof_ctx* c)
+{
+    if (c->precision != SLVOF_MIXED) return;
+    launch_to_float(c->uf, c->uf32, c->ncell, 1.0 / c->m.d[0], c->nsm, c->stream);
+    launch_to_float(c->vf, c->vf32, c->ncell, 1.0 / c->m.d[1], c->nsm, c->stream);
+    launch_to_float(c->wf, c->wf32, c->ncell, 1.0 / c->m.d[2], c->nsm, c->stream);
+}
+
+int up_velocity(slvof_ctx* c, const double* uf, const double* vf, const double* wf)
+{
+    int r;
+    const size_t b = c->ncell * sizeof(double);
+    if ((r = h2d(c, c->uf, uf, b)) || (r = h2d(c, c->vf, vf, b)) || (r = h2d(c, c->wf, wf, b))) return r;
+    to_float_velocity(c);
+    return 0;
+}
+
+#define TRY(x)                \
+    do {                      \
+        int r_ = (x);         \
+        if (r_ < 0) return r_; \
+    } while (0)
+
+} // namespace
+
+extern "C" {
+
+int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
+{
+    if (!mesh || !out) return SLVOF_E_ARG;
+    *out = nullptr;
+    if (precision != SLVOF_FP64 && precision != SLVOF_MIXED) return SLVOF_E_ARG;
+    if (mesh->Nx < 1 || mesh->Ny < 1 || mesh->Nz < 1 || mesh->nghost < 3) return SLVOF_E_ARG;
+    if (mesh->projection < 0 || mesh->projection > 2 || mesh->nband < 0) return SLVOF_E_ARG;
+    if (!mesh->x || !mesh->y || !mesh->z || !mesh->xm || !mesh->ym || !mesh->zm) return SLVOF_E_ARG;
+    const long g = mesh->nghost;
+    const long N[3] = {mesh->Nx, mesh->Ny, mesh->Nz};
+    const long n0 = N[0] + 2 * g, n1 = N[1] + 2 * g, n2 = N[2] + 2 * g;
+    if (n0 * n1 * n2 > (1L << 31) - 1 || N[0] > 30000 || N[1] > 30000 || N[2] > 30000) return SLVOF_E_UNSUPPORTED;
+    slvof_ctx* c = new slvof_ctx();
+    c->precision = precision;
+    auto bail = [&](int code) {
+        slvof_destroy(c);
+        return code;
+    };
+    if (cudaGetDevice(&c->device) != cudaSuccess) return bail(SLVOF_E_CUDA);
+    if (cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess) return bail(SLVOF_E_CUDA);
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SLVOF_E_CUDA);
+    c->stream = c->own_stream;
+    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return bail(SLVOF_E_CUDA);
+    for (int q = 0; q < SLVOF_NSTAGES; ++q)
+        if (cudaEventCreate(&c->sev[q][0]) != cudaSuccess || cudaEventCreate(&c->sev[q][1]) != cudaSuccess)
+            return bail(SLVOF_E_CUDA);
+    c->ncell = n0 * n1 * n2;
+    c->nvf = (n0 + 6) * (n1 + 6) * (n2 + 6);
+    const long interior = N[0] * N[1] * N[2];
+    c->npure = c->nsm * 8;
+    auto alloc = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess && cudaMemset(*p, 0, bytes) == cudaSuccess; };
+    const long ncoord = 2 * (n0 + n1 + n2) + 3;
+    bool ok = alloc((void**)&c->coords, ncoord * sizeof(double)) && alloc((void**)&c->VF[0], c->nvf * sizeof(double)) &&
+              alloc((void**)&c->VF[1], c->nvf * sizeof(double)) && alloc((void**)&c->uf, c->ncell * sizeof(double)) &&
+              alloc((void**)&c->vf, c->ncell * sizeof(double)) && alloc((void**)&c->wf, c->ncell * sizeof(double)) &&
+              alloc((void**)&c->nx, c->ncell * sizeof(double)) && alloc((void**)&c->ny, c->ncell * sizeof(double)) &&
+              alloc((void**)&c->nz, c->ncell * sizeof(double)) && alloc((void**)&c->D, c->ncell * sizeof(double)) &&
+              alloc((void**)&c->phase, c->ncell * sizeof(signed char)) &&
+              alloc((void**)&c->band[0], c->ncell * sizeof(short)) && alloc((void**)&c->band[1], c->ncell * sizeof(short)) &&
+              alloc((void**)&c->list_sl, interior * sizeof(int)) && alloc((void**)&c->list_if, interior * sizeof(int)) &&
+              alloc((void**)&c->list_plic, c->ncell * sizeof(int)) &&
+              alloc((void**)&c->ctr, C_N * sizeof(int)) && alloc((void**)&c->partials, 2 * c->npure * sizeof(double)) &&
+              alloc((void**)&c->mass_d, sizeof(double));
+    if (ok && precision == SLVOF_MIXED)
+        ok = alloc((void**)&c->uf32, c->ncell * sizeof(float)) && alloc((void**)&c->vf32, c->ncell * sizeof(float)) &&
+             alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4));
+    if (!ok) return bail(SLVOF_E_NOMEM);
+    /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
+    std::vector<double> h(ncoord);
+    double* p = h.data();
+    const double* fsrc[3] = {mesh->x, mesh->y, mesh->z};
+    const double* csrc[3] = {mesh->xm, mesh->ym, mesh->zm};
+    const long nn[3] = {n0, n1, n2};
+    long off_f[3], off_c[3], o = 0;
+    double maxabs = 0.0;
+    for (int q = 0; q < 3; ++q) {
+        off_f[q] = o;
+        for (long t = 0; t <= nn[q]; ++t) { p[o++] = fsrc[q][t]; maxabs = std::max(maxabs, std::fabs(fsrc[q][t])); }
+    }
+    for (int q = 0; q < 3; ++q) {
+        off_c[q] = o;
+        for (long t = 0; t < nn[q]; ++t) p[o++] = csrc[q][t];
+    }
+    if (precision == SLVOF_MIXED) {
+        /* the FP32 geometry works in cell units and needs a uniform mesh (src/Mesh.jl:83-100) */
+        const double dd[3] = {mesh->dx, mesh->dy, mesh->dz};
+        for (int q = 0; q < 3; ++q)
+            for (long t = 0; t <= nn[q]; ++t)
+                if (std::fabs(fsrc[q][t] - (fsrc[q][0] + (double)t * dd[q])) > 1e-9 * dd[q]) return bail(SLVOF_E_UNSUPPORTED);
+    }
+    if (cudaMemcpy(c->coords, h.data(), ncoord * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(SLVOF_E_CUDA);
+    DevMesh& m = c->m;
+    for (int q = 0; q < 3; ++q) {
+        m.N[q] = (int)N[q];
+        m.hi[q] = (int)(N[q] + g);
+        m.f[q] = c->coords + off_f[q];
+        m.c[q] = c->coords + off_c[q];
+    }
+    m.g = (int)g;
+    m.nband = mesh->nband;
+    m.projection = mesh->projection;
+    m.per[0] = mesh->xper != 0; m.per[1] = mesh->yper != 0; m.per[2] = mesh->zper != 0;
+    m.lo = 1 - (int)g;
+    m.vlo = m.lo - 3;
+    m.d[0] = mesh->dx; m.d[1] = mesh->dy; m.d[2] = mesh->dz;
+    m.VFlo = mesh->VFlo;
+    m.VFhi = mesh->VFhi;
+    m.Lsum = (mesh->Lx + mesh->Ly) + mesh->Lz;
+    m.cellvol = (mesh->dx * mesh->dy) * mesh->dz;
+    m.fast_pure = maxabs < m.Lsum * (1.0 - 1e-9);
+    m.cs1 = n0; m.cs2 = n0 * n1;
+    m.vs1 = n0 + 6; m.vs2 = (n0 + 6) * (n1 + 6);
+    *out = c;
+    return SLVOF_OK;
+}
+
+int slvof_destroy(slvof_ctx* c)
+{
+    if (!c) return SLVOF_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    void* bufs[] = {c->coords, c->VF[0], c->VF[1], c->uf, c->vf, c->wf, c->uf32, c->vf32, c->wf32, c->nx, c->ny,
+                    c->nz, c->D, c->planes, c->phase, c->band[0], c->band[1], c->list_sl, c->list_if, c->list_plic, c->ctr,
+                    c->partials, c->mass_d, c->table, c->spheres};
+    for (void* b : bufs)
+        if (b) cudaFree(b);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int q = 0; q < SLVOF_NSTAGES; ++q)
+        for (int e = 0; e < 2; ++e)
+            if (c->sev[q][e]) cudaEventDestroy(c->sev[q][e]);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return SLVOF_OK;
+}
+
+int slvof_last_error(const slvof_ctx* c, char* buf, size_t n)
+{
+    if (!c || !buf || n == 0) return SLVOF_E_ARG;
+    snprintf(buf, n, "%s", c->err.c_str());
+    return SLVOF_OK;
+}
+
+int slvof_last_kernel_ms(const slvof_ctx* c, double* ms)
+{
+    if (!c || !ms) return SLVOF_E_ARG;
+    *ms = c->last_ms;
+    return SLVOF_OK;
+}
+
+int slvof_stage_ms(const slvof_ctx* c, double* ms, int n)
+{
+    if (!c || !ms || n < 0) return SLVOF_E_ARG;
+    for (int q = 0; q < n && q < SLVOF_NSTAGES; ++q) {
+        float t = 0.f;
+        ms[q] = (c->sran[q] && cudaEventElapsedTime(&t, c->sev[q][0], c->sev[q][1]) == cudaSuccess) ? t : 0.0;
+    }
+    return SLVOF_OK;
+}
+
+int slvof_set_stream(slvof_ctx* c, void* stream)
+{
+    if (!c) return SLVOF_E_ARG;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+    return SLVOF_OK;
+}
+
+int slvof_upload_vf(slvof_ctx* c, const double* VF)
+{
+    TRY(begin(c));
+    TRY(h2d(c, c->VF[c->vcur], VF, c->nvf * sizeof(double)));
+    c->normals_valid = false;
+    return finish(c, false);
+}
+
+int slvof_upload_velocity(slvof_ctx* c, const double* uf, const double* vf, const double* wf)
+{
+    TRY(begin(c));
+    TRY(up_velocity(c, uf, vf, wf));
+    return finish(c, false);
+}
+
+int slvof_upload_band(slvof_ctx* c, const int16_t* band)
+{
+    TRY(begin(c));
+    TRY(h2d(c, c->band[c->bcur], band, c->ncell * sizeof(short)));
+    return finish(c, false);
+}
+
+int slvof_upload_plic(slvof_ctx* c, const double* nx, const double* ny, const double* nz, const double* D)
+{
+    TRY(begin(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(h2d(c, c->nx, nx, b));
+    TRY(h2d(c, c->ny, ny, b));
+    TRY(h2d(c, c->nz, nz, b));
+    TRY(h2d(c, c->D, D, b));
+    c->normals_valid = true;
+    return finish(c, false);
+}
+
+int slvof_download_vf(slvof_ctx* c, double* VF)
+{
+    TRY(begin(c));
+    TRY(d2h(c, VF, c->VF[c->vcur], c->nvf * sizeof(double)));
+    return finish(c, false);
+}
+
+int slvof_download_normals(slvof_ctx* c, double* nx, double* ny, double* nz)
+{
+    TRY(begin(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(d2h(c, nx, c->nx, b));
+    TRY(d2h(c, ny, c->ny, b));
+    TRY(d2h(c, nz, c->nz, b));
+    return finish(c, false);
+}
+
+int slvof_download_plic(slvof_ctx* c, double* D)
+{
+    TRY(begin(c));
+    TRY(d2h(c, D, c->D, c->ncell * sizeof(double)));
+    return finish(c, false);
+}
+
+int slvof_download_band(slvof_ctx* c, int16_t* band)
+{
+    TRY(begin(c));
+    TRY(d2h(c, band, c->band[c->bcur], c->ncell * sizeof(short)));
+    return finish(c, false);
+}
+
+int slvof_vf_ghost_fill(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(st_vf_ghost_inplace(c));
+    c->normals_valid = false;
+    return finish(c, false);
+}
+
+int slvof_compute_normal(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(clear_err(c));
+    TRY(st_normals(c));
+    return finish(c);
+}
+
+int slvof_compute_plic(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(st_plic(c));
+    return finish(c, false);
+}
+
+int slvof_compute_band(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(st_band(c));
+    return finish(c, false);
+}
+
+int slvof_transport(slvof_ctx* c, double dt)
+{
+    TRY(begin(c));
+    TRY(clear_err(c));
+    TRY(st_transport(c, dt));
+    return finish(c);
+}
+
+int slvof_step(slvof_ctx* c, double dt, int flags, double* mass)
+{
+    TRY(begin(c));
+    if ((flags & SLVOF_STEP_MASS) && !mass) return fail(c, SLVOF_E_ARG, "mass requested with a null pointer");
+    TRY(clear_err(c));
+    if (!c->normals_valid) {
+        TRY(st_normals(c));
+        TRY(st_plic(c));
+    }
+    TRY(st_transport(c, dt));
+    TRY(st_normals(c));
+    TRY(st_plic(c));
+    if (flags & SLVOF_STEP_BAND) TRY(st_band(c));
+    if (flags & SLVOF_STEP_MASS) TRY(st_mass(c, mass, true));
+    return finish(c);
+}
+
+int slvof_mass(slvof_ctx* c, double* mass)
+{
+    TRY(begin(c));
+    if (!mass) return fail(c, SLVOF_E_ARG, "null mass pointer");
+    TRY(st_mass(c, mass, false));
+    return finish(c, false);
+}
+
+int slvof_computeNormal(slvof_ctx* c, double* nx, double* ny, double* nz, const double* VF)
+{
+    TRY(begin(c));
+    TRY(clear_err(c));
+    TRY(h2d(c, c->VF[c->vcur], VF, c->nvf * sizeof(double)));
+    TRY(st_normals(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(d2h(c, nx, c->nx, b));
+    TRY(d2h(c, ny, c->ny, b));
+    TRY(d2h(c, nz, c->nz, b));
+    return finish(c);
+}
+
+int slvof_computePLIC(slvof_ctx* c, double* D, const double* nx, const double* ny, const double* nz, const double* VF)
+{
+    TRY(begin(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(h2d(c, c->VF[c->vcur], VF, c->nvf * sizeof(double)));
+    TRY(h2d(c, c->nx, nx, b));
+    TRY(h2d(c, c->ny, ny, b));
+    TRY(h2d(c, c->nz, nz, b));
+    TRY(st_plic(c));
+    TRY(d2h(c, D, c->D, b));
+    c->normals_valid = true;
+    return finish(c, false);
+}
+
+int slvof_computeBand(slvof_ctx* c, int16_t* band, const double* VF)
+{
+    TRY(begin(c));
+    TRY(h2d(c, c->VF[c->vcur], VF, c->nvf * sizeof(double)));
+    TRY(h2d(c, c->band[c->bcur], band, c->ncell * sizeof(short)));
+    TRY(st_band(c));
+    TRY(d2h(c, band, c->band[c->bcur], c->ncell * sizeof(short)));
+    c->normals_valid = false;
+    return finish(c, false);
+}
+
+int slvof_transportSL(slvof_ctx* c, double dt, double* VF, const double* uf, const double* vf, const double* wf,
+                      const double* nx, const double* ny, const double* nz, const double* D, const int16_t* band)
+{
+    TRY(begin(c));
+    TRY(clear_err(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(h2d(c, c->VF[c->vcur], VF, c->nvf * sizeof(double)));
+    TRY(up_velocity(c, uf, vf, wf));
+    TRY(h2d(c, c->nx, nx, b));
+    TRY(h2d(c, c->ny, ny, b));
+    TRY(h2d(c, c->nz, nz, b));
+    TRY(h2d(c, c->D, D, b));
+    TRY(h2d(c, c->band[c->bcur], band, c->ncell * sizeof(short)));
+    TRY(st_transport(c, dt));
+    TRY(d2h(c, VF, c->VF[c->vcur], c->nvf * sizeof(double)));
+    return finish(c);
+}
+
+int slvof_step_host(slvof_ctx* c, double dt, int flags, const double* uf, const double* vf, const double* wf,
+                    double* VF, double* mass)
+{
+    TRY(begin(c));
+    if ((flags & SLVOF_STEP_MASS) && !mass) return fail(c, SLVOF_E_ARG, "mass requested with a null pointer");
+    TRY(clear_err(c));
+    TRY(up_velocity(c, uf, vf, wf));
+    if (!c->normals_valid) {
+        TRY(st_normals(c));
+        TRY(st_plic(c));
+    }
+    TRY(st_transport(c, dt));
+    TRY(st_normals(c));
+    TRY(st_plic(c));
+    if (flags & SLVOF_STEP_BAND) TRY(st_band(c));
+    if (flags & SLVOF_STEP_MASS) TRY(st_mass(c, mass, true));
+    TRY(d2h(c, VF, c->VF[c->vcur], c->nvf * sizeof(double)));
+    return finish(c);
+}
+
+int slvof_case_vf_spheres(slvof_ctx* c, const double* centres, const double* radii, int n, int nF, int dims)
+{
+    if (!c || !centres || !radii || n < 1 || nF < 1 || nF > 64 || (dims != 2 && dims != 3)) return SLVOF_E_ARG;
+    TRY(begin(c));
+    const int npts = dims == 3 ? nF * nF * nF : nF * nF;
+    if (c->table_n < npts + 1) {
+        if (c->table) cudaFree(c->table);
+        c->table = nullptr;
+        CK(cudaMalloc(&c->table, (npts + 1) * sizeof(double)));
+        c->table_n = npts + 1;
+    }
+    if (c->spheres_n < n) {
+        if (c->spheres) cudaFree(c->spheres);
+        c->spheres = nullptr;
+        CK(cudaMalloc(&c->spheres, 4 * n * sizeof(double)));
+        c->spheres_n = n;
+    }
+    /* running sum VF += 1/nF^dims, as the reference accumulates it */
+    std::vector<double> tab(npts + 1);
+    const double sub = 1.0 / (double)npts;
+    double s = 0.0;
+    tab[0] = 0.0;
+    for (int q = 1; q <= npts; ++q) { s = s + sub; tab[q] = s; }
+    CK(cudaMemcpyAsync(c->table, tab.data(), (npts + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->spheres, centres, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->spheres + 3 * n, radii, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->VF[c->vcur], 0, c->nvf * sizeof(double), c->stream));
+    launch_case_spheres(c->m, c->spheres, c->spheres + 3 * n, n, nF, dims, c->table, c->VF[c->vcur], c->nsm, c->stream);
+    CK(cudaStreamSynchronize(c->stream)); /* host vectors go out of scope */
+    TRY(st_vf_ghost_inplace(c));
+    c->normals_valid = false;
+    return finish(c, false);
+}
+
+int slvof_case_deformation3d(slvof_ctx* c, double t, double T)
+{
+    TRY(begin(c));
+    launch_case_deformation3d(c->m, t, T, c->uf, c->vf, c->wf, c->nsm, c->stream);
+    to_float_velocity(c);
+    return finish(c, false);
+}
+
+} // extern "C"

@@ -1,0 +1,44 @@
+/* slvof_kernels.h — host-side launchers of the SL-VOF kernels (internal to the library). */
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "slvof_dev.cuh"
+
+namespace slvof {
+
+/* k_common.cu */
+void launch_vf_ghost(const DevMesh& m, const double* VFin, double* VFout, int nsm, cudaStream_t s);
+void launch_elvira_pure(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, int* list, int* count,
+                        double* partials, int nblocks, cudaStream_t s);
+void launch_normal_ghost(const DevMesh& m, double* nx, double* ny, double* nz, int nsm, cudaStream_t s);
+void launch_mass_final(const double* partials, int nblocks, double cellvol, double* out, cudaStream_t s);
+void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s);
+void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neumann, int nsm, cudaStream_t s);
+void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, int nsm, cudaStream_t s);
+void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin, double* VFout, int* list, int* count,
+                        int nsm, cudaStream_t s);
+void launch_to_float(const double* a, float* b, long n, double scale, int nsm, cudaStream_t s);
+void launch_case_spheres(const DevMesh& m, const double* cen, const double* rad, int n, int nF, int dims,
+                         const double* table, double* VF, int nsm, cudaStream_t s);
+void launch_case_deformation3d(const DevMesh& m, double t, double T, double* uf, double* vf, double* wf, int nsm,
+                               cudaStream_t s);
+
+/* k_fp64.cu */
+void launch_elvira_iface64(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
+                           const int* count, int* work, int* errw, int nsm, cudaStream_t s);
+void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz, double* D,
+                   float4* planes, signed char* phase, int* list, int* count, int nsm, cudaStream_t s);
+void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout, const double* uf, const double* vf,
+                 const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                 const signed char* phase, const int* list, const int* count, int* work, int* errw, int nsm,
+                 cudaStream_t s);
+
+/* k_mixed.cu */
+void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
+                           const int* count, int* work, int nsm, cudaStream_t s);
+void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
+                 const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
+                 int* errw, int nsm, cudaStream_t s);
+
+} // namespace slvof

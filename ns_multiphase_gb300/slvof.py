@@ -1,0 +1,274 @@
+"""Python binding of the sm_103a SL-VOF library (C ABI in include/slvof.h).
+
+This is the host-side mirror of the reference's operator interface for the path:
+``computeNormal!`` (src/VF.jl:79), ``computePLIC!`` (src/VF.jl:94), ``computeBand!``
+(src/VF.jl:16) and the SL section of ``transport!`` (src/Transport.jl:108-151,179-181), with
+the same array arguments (OffsetArray parents, Fortran order).  Like the reference, a failed
+operation raises.  There is no CPU fallback: if the CUDA library is missing or no GPU is
+present, calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .mesh import Mesh
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libslvof.so")
+
+FP64 = 0
+MIXED = 1
+STEP_BAND = 1
+STEP_MASS = 2
+
+# (name, restype, argtypes) of every symbol declared in include/slvof.h
+_P, _I, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+SYMBOLS = [
+    ("slvof_create", _I, [_P, _I, _P]),
+    ("slvof_destroy", _I, [_P]),
+    ("slvof_last_error", _I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    ("slvof_last_kernel_ms", _I, [_P, _P]),
+    ("slvof_stage_ms", _I, [_P, _P, _I]),
+    ("slvof_set_stream", _I, [_P, _P]),
+    ("slvof_upload_vf", _I, [_P, _P]),
+    ("slvof_upload_velocity", _I, [_P, _P, _P, _P]),
+    ("slvof_upload_band", _I, [_P, _P]),
+    ("slvof_upload_plic", _I, [_P, _P, _P, _P, _P]),
+    ("slvof_download_vf", _I, [_P, _P]),
+    ("slvof_download_normals", _I, [_P, _P, _P, _P]),
+    ("slvof_download_plic", _I, [_P, _P]),
+    ("slvof_download_band", _I, [_P, _P]),
+    ("slvof_vf_ghost_fill", _I, [_P]),
+    ("slvof_compute_normal", _I, [_P]),
+    ("slvof_compute_plic", _I, [_P]),
+    ("slvof_compute_band", _I, [_P]),
+    ("slvof_transport", _I, [_P, _D]),
+    ("slvof_step", _I, [_P, _D, _I, _P]),
+    ("slvof_mass", _I, [_P, _P]),
+    ("slvof_computeNormal", _I, [_P, _P, _P, _P, _P]),
+    ("slvof_computePLIC", _I, [_P, _P, _P, _P, _P, _P]),
+    ("slvof_computeBand", _I, [_P, _P, _P]),
+    ("slvof_transportSL", _I, [_P, _D, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("slvof_step_host", _I, [_P, _D, _I, _P, _P, _P, _P, _P]),
+    ("slvof_case_vf_spheres", _I, [_P, _P, _P, _I, _I, _I]),
+    ("slvof_case_deformation3d", _I, [_P, _D, _D]),
+]
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the in-tree library and declare its C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"SL-VOF CUDA library not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    for name, res, args in SYMBOLS:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class DeviceError(RuntimeError):
+    """A kernel raised SLVOF_DEV_* bits (index range, clip depth, NaN distance, volume)."""
+
+    def __init__(self, bits: int, msg: str):
+        super().__init__(msg)
+        self.bits = bits
+
+
+def _ptr(a: np.ndarray, dtype, shape=None):
+    if a.dtype != dtype:
+        raise TypeError(f"expected {np.dtype(dtype)}, got {a.dtype}")
+    if not a.flags.f_contiguous:
+        raise TypeError("arrays must be Fortran-ordered OffsetArray parents")
+    if shape is not None and a.shape != shape:
+        raise ValueError(f"expected shape {shape}, got {a.shape}")
+    return a.ctypes.data
+
+
+class SLVOF:
+    """A device context for one mesh (slvof_create).  precision: "fp64" or "mixed"."""
+
+    def __init__(self, mesh: Mesh, precision: str = "fp64"):
+        self.L = load_library()
+        self.mesh = mesh
+        self.precision = {"fp64": FP64, "mixed": MIXED}[precision]
+        self._desc = mesh.desc()
+        h = ctypes.c_void_p()
+        st = self.L.slvof_create(ctypes.byref(self._desc), self.precision, ctypes.byref(h))
+        if st != 0:
+            raise RuntimeError(f"slvof_create failed with status {st}")
+        self.h = h
+
+    # ---- housekeeping --------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.slvof_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def last_error(self) -> str:
+        buf = ctypes.create_string_buffer(512)
+        self.L.slvof_last_error(self.h, buf, 512)
+        return buf.value.decode()
+
+    def last_kernel_ms(self) -> float:
+        v = ctypes.c_double()
+        self.L.slvof_last_kernel_ms(self.h, ctypes.byref(v))
+        return v.value
+
+    STAGES = ("sl_classify", "sl_update", "vf_ghost", "elvira_pure", "elvira_candidates", "normal_ghost", "plic",
+              "band", "mass")
+
+    def stage_ms(self) -> dict:
+        a = np.zeros(len(self.STAGES))
+        self.L.slvof_stage_ms(self.h, a.ctypes.data, len(a))
+        return dict(zip(self.STAGES, a.tolist()))
+
+    def set_stream(self, stream_handle: int | None):
+        """Run on a caller-owned cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self.L.slvof_set_stream(self.h, stream_handle or None), "set_stream")
+
+    def _check(self, st: int, what: str):
+        if st < 0:
+            raise RuntimeError(f"{what}: status {st}: {self.last_error()}")
+        if st > 0:
+            raise DeviceError(st, f"{what}: {self.last_error()}")
+        return st
+
+    # ---- transfers --------------------------------------------------------------------
+    def upload_vf(self, VF):
+        self._check(self.L.slvof_upload_vf(self.h, _ptr(VF, np.float64, self.mesh.vf_shape)), "upload_vf")
+
+    def upload_velocity(self, uf, vf, wf):
+        s = self.mesh.cell_shape
+        self._check(self.L.slvof_upload_velocity(self.h, _ptr(uf, np.float64, s), _ptr(vf, np.float64, s),
+                                                 _ptr(wf, np.float64, s)), "upload_velocity")
+
+    def upload_band(self, band):
+        self._check(self.L.slvof_upload_band(self.h, _ptr(band, np.int16, self.mesh.cell_shape)), "upload_band")
+
+    def upload_plic(self, nx, ny, nz, D):
+        s = self.mesh.cell_shape
+        self._check(self.L.slvof_upload_plic(self.h, _ptr(nx, np.float64, s), _ptr(ny, np.float64, s),
+                                             _ptr(nz, np.float64, s), _ptr(D, np.float64, s)), "upload_plic")
+
+    def download_vf(self, out=None):
+        out = self.mesh.vf_array() if out is None else out
+        self._check(self.L.slvof_download_vf(self.h, _ptr(out, np.float64, self.mesh.vf_shape)), "download_vf")
+        return out
+
+    def download_normals(self):
+        m = self.mesh
+        nx, ny, nz = m.cell_array(), m.cell_array(), m.cell_array()
+        self._check(self.L.slvof_download_normals(self.h, nx.ctypes.data, ny.ctypes.data, nz.ctypes.data),
+                    "download_normals")
+        return nx, ny, nz
+
+    def download_plic(self):
+        D = self.mesh.cell_array()
+        self._check(self.L.slvof_download_plic(self.h, D.ctypes.data), "download_plic")
+        return D
+
+    def download_band(self):
+        b = self.mesh.cell_array(np.int16)
+        self._check(self.L.slvof_download_band(self.h, b.ctypes.data), "download_band")
+        return b
+
+    # ---- resident operations ------------------------------------------------------------
+    def vf_ghost_fill(self):
+        self._check(self.L.slvof_vf_ghost_fill(self.h), "vf_ghost_fill")
+
+    def compute_normal(self):
+        self._check(self.L.slvof_compute_normal(self.h), "compute_normal")
+
+    def compute_plic(self):
+        self._check(self.L.slvof_compute_plic(self.h), "compute_plic")
+
+    def compute_band(self):
+        self._check(self.L.slvof_compute_band(self.h), "compute_band")
+
+    def transport(self, dt: float):
+        self._check(self.L.slvof_transport(self.h, dt), "transport")
+
+    def step(self, dt: float, band: bool = True, mass: bool = True):
+        flags = (STEP_BAND if band else 0) | (STEP_MASS if mass else 0)
+        m = ctypes.c_double(np.nan)
+        self._check(self.L.slvof_step(self.h, dt, flags, ctypes.byref(m)), "step")
+        return m.value if mass else None
+
+    def mass(self) -> float:
+        m = ctypes.c_double()
+        self._check(self.L.slvof_mass(self.h, ctypes.byref(m)), "mass")
+        return m.value
+
+    def init_state(self, band: bool = True):
+        """run_solver's start after IC! (src/NavierStokes_Parallel.jl:73-98) on device VF:
+        band, normals, PLIC."""
+        if band:
+            self.compute_band()
+        self.compute_normal()
+        self.compute_plic()
+
+    # ---- host-buffer drop-ins (reference signatures) -------------------------------------
+    def computeNormal(self, nx, ny, nz, VF):
+        s = self.mesh.cell_shape
+        self._check(self.L.slvof_computeNormal(self.h, _ptr(nx, np.float64, s), _ptr(ny, np.float64, s),
+                                               _ptr(nz, np.float64, s), _ptr(VF, np.float64, self.mesh.vf_shape)),
+                    "computeNormal")
+
+    def computePLIC(self, D, nx, ny, nz, VF):
+        s = self.mesh.cell_shape
+        self._check(self.L.slvof_computePLIC(self.h, _ptr(D, np.float64, s), _ptr(nx, np.float64, s),
+                                             _ptr(ny, np.float64, s), _ptr(nz, np.float64, s),
+                                             _ptr(VF, np.float64, self.mesh.vf_shape)), "computePLIC")
+
+    def computeBand(self, band, VF):
+        self._check(self.L.slvof_computeBand(self.h, _ptr(band, np.int16, self.mesh.cell_shape),
+                                             _ptr(VF, np.float64, self.mesh.vf_shape)), "computeBand")
+
+    def transportSL(self, dt, VF, uf, vf, wf, nx, ny, nz, D, band):
+        s = self.mesh.cell_shape
+        self._check(self.L.slvof_transportSL(self.h, dt, _ptr(VF, np.float64, self.mesh.vf_shape),
+                                             _ptr(uf, np.float64, s), _ptr(vf, np.float64, s),
+                                             _ptr(wf, np.float64, s), _ptr(nx, np.float64, s),
+                                             _ptr(ny, np.float64, s), _ptr(nz, np.float64, s),
+                                             _ptr(D, np.float64, s), _ptr(band, np.int16, s)), "transportSL")
+
+    def step_host(self, dt, uf, vf, wf, VF_out, band=True, mass=True):
+        s = self.mesh.cell_shape
+        flags = (STEP_BAND if band else 0) | (STEP_MASS if mass else 0)
+        m = ctypes.c_double(np.nan)
+        self._check(self.L.slvof_step_host(self.h, dt, flags, _ptr(uf, np.float64, s), _ptr(vf, np.float64, s),
+                                           _ptr(wf, np.float64, s), _ptr(VF_out, np.float64, self.mesh.vf_shape),
+                                           ctypes.byref(m)), "step_host")
+        return m.value if mass else None
+
+    # ---- synthetic inputs ----------------------------------------------------------------
+    def case_vf_spheres(self, centres, radii, nF=20, dims=3):
+        c = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(radii, dtype=np.float64).reshape(-1)
+        self._check(self.L.slvof_case_vf_spheres(self.h, c.ctypes.data, r.ctypes.data, len(r), nF, dims),
+                    "case_vf_spheres")
+
+    def case_deformation3d(self, t, T=3.0):
+        self._check(self.L.slvof_case_deformation3d(self.h, t, T), "case_deformation3d")

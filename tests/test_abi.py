@@ -1,0 +1,63 @@
+"""The C-ABI library loads and exports every entry point include/slvof.h declares (CPU only:
+no compute calls), and the host-side layout helpers match the reference's extents."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from ns_multiphase_gb300 import build as nb
+from ns_multiphase_gb300 import slvof
+from ns_multiphase_gb300.mesh import Mesh, MeshDesc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "slvof.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(slvof_\w+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    nb.build()
+    return ctypes.CDLL(nb.LIB)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(lib, s), s
+    # the Python binding declares exactly the header's entry points
+    assert sorted(n for n, _, _ in slvof.SYMBOLS) == syms
+
+
+def test_descriptor_layout_matches_header():
+    # slvof_mesh: 9 int32 (36 B) + pad to 40, 10 doubles, 6 pointers
+    assert ctypes.sizeof(MeshDesc) == 40 + 10 * 8 + 6 * ctypes.sizeof(ctypes.c_void_p)
+    assert MeshDesc.Lx.offset == 40
+    assert MeshDesc.x.offset == 120
+
+
+def test_extents_follow_initArrays():
+    m = Mesh(Nx=7, Ny=5, Nz=3, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    assert m.nghost == 3
+    assert m.cell_shape == (13, 11, 9)
+    assert m.vf_shape == (19, 17, 15)
+    m2 = Mesh(Nx=7, Ny=5, Nz=3, Lx=1.0, Ly=1.0, Lz=1.0, CFL=3.5)  # nghost = 3 + ceil(3.5) - 2
+    assert m2.nghost == 5 and m2.nband == 4
+    VF = m.vf_array()
+    assert VF.flags.f_contiguous
+    assert m.interior(VF).shape == (7, 5, 3)
+
+
+def test_create_rejects_bad_descriptor_without_gpu(lib):
+    # argument validation happens before any CUDA call
+    h = ctypes.c_void_p()
+    lib.slvof_create.restype = ctypes.c_int
+    assert lib.slvof_create(None, 0, ctypes.byref(h)) == -1
+    m = Mesh(Nx=4, Ny=4, Nz=4, Lx=1.0, Ly=1.0, Lz=1.0)
+    assert lib.slvof_create(ctypes.byref(m.desc()), 7, ctypes.byref(h)) == -1

@@ -1,0 +1,174 @@
+"""GPU parity: the FP64 CUDA path against the CPU restatement, bit for bit.
+
+Every call goes through the C ABI (ns_multiphase_gb300.slvof -> libslvof.so).  The FP64
+kernels keep the reference's expression order without FMA and share the deterministic
+elementary functions with the restatement, so normals, PLIC distances, band and VF are
+compared with array_equal; the total volume is compared at 1e-13 relative.
+"""
+import numpy as np
+import pytest
+
+from ns_multiphase_gb300 import cases
+from ns_multiphase_gb300.mesh import Mesh
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__
+    __graft_entry__.build()
+
+
+def ctx(mesh, precision="fp64"):
+    from ns_multiphase_gb300.slvof import SLVOF
+    return SLVOF(mesh, precision)
+
+
+def assert_same(a, b, what):
+    if not np.array_equal(a, b):
+        d = np.abs(a.astype(np.float64) - b.astype(np.float64))
+        idx = np.unravel_index(np.argmax(d), d.shape)
+        raise AssertionError(f"{what}: {int((d > 0).sum())} cells differ, max {d.max():.3e} at parent {idx}")
+
+
+def spheres_mesh(N=16, seed=5, n=4):
+    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.25, 0.75, size=(n, 3))
+    r = rng.uniform(0.12, 0.22, size=n)
+    return m, cases.vf_spheres(m, c, r, nF=8)
+
+
+def init_both(m, VF, precision="fp64"):
+    o = Oracle(m)
+    VFo = VF.copy(order="F")
+    band, nx, ny, nz, D = o.init_state(VFo)
+    g = ctx(m, precision)
+    g.upload_vf(VF)
+    g.vf_ghost_fill()
+    g.init_state()
+    return o, g, VFo, band, nx, ny, nz, D
+
+
+def test_vf_ghost_fill_normals_plic_band():
+    m, VF = spheres_mesh()
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    assert_same(g.download_vf(), VFo, "VF ghost fill")
+    gx, gy, gz = g.download_normals()
+    assert_same(gx, nx, "nx")
+    assert_same(gy, ny, "ny")
+    assert_same(gz, nz, "nz")
+    assert_same(g.download_plic(), D, "D")
+    assert_same(g.download_band(), band, "band")
+
+
+def test_one_transport_step():
+    m, VF = spheres_mesh(N=20, seed=9)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    dt = 0.5 * m.dx / 2.0
+    uf, vf, wf = cases.deformation3d_faces(m, 0.3, 3.0)
+    g.upload_velocity(uf, vf, wf)
+    g.transport(dt)
+    flags, _ = o.transport(dt, VFo, uf, vf, wf, nx, ny, nz, D, band)
+    assert flags == 0
+    assert_same(g.download_vf(), VFo, "VF after SL update")
+
+
+@pytest.mark.parametrize("projection", ["RK4", "Euler", "Midpoint"])
+def test_multistep_sphere_deformation(projection):
+    """Config-1 shape (sphere r=0.15 at 0.35^3, Deformation3D T=3) at 24^3, 6 steps."""
+    m = Mesh(Nx=24, Ny=24, Nz=24, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, projection=projection)
+    VF = cases.vf_spheres(m, [[0.35, 0.35, 0.35]], [0.15], nF=20)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    dt = 0.5 * m.dx / 2.0
+    t = 0.0
+    for s in range(6):
+        uf, vf, wf = cases.deformation3d_faces(m, t + 0.5 * dt, 3.0)
+        g.upload_velocity(uf, vf, wf)
+        mass = g.step(dt)
+        assert o.step(dt, VFo, uf, vf, wf, nx, ny, nz, D, band) == 0
+        t += dt
+    assert_same(g.download_vf(), VFo, "VF")
+    gx, gy, gz = g.download_normals()
+    assert_same(gx, nx, "nx")
+    assert_same(gy, ny, "ny")
+    assert_same(gz, nz, "nz")
+    assert_same(g.download_plic(), D, "D")
+    assert_same(g.download_band(), band, "band")
+    mo = o.mass(VFo)
+    assert abs(mass - mo) <= 1e-13 * abs(mo)
+
+
+def test_multistep_2d_vortex_periodic_z():
+    """Config-0 shape: 2D single vortex (T=8), circle r=0.15 at (0.5,0.75), z periodic."""
+    m = Mesh(Nx=32, Ny=32, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / 32, CFL=0.5, zper=True)
+    VF = cases.vf_spheres(m, [[0.5, 0.75, 0.0]], [0.15], nF=10, dims=2)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    dt = 0.5 * m.dx
+    t = 0.0
+    for s in range(12):
+        uf, vf, wf = cases.deformation2d_faces(m, t + 0.5 * dt, 8.0)
+        g.upload_velocity(uf, vf, wf)
+        g.step(dt)
+        assert o.step(dt, VFo, uf, vf, wf, nx, ny, nz, D, band) == 0
+        t += dt
+    assert_same(g.download_vf(), VFo, "VF")
+    gx, gy, gz = g.download_normals()
+    assert_same(gx, nx, "nx")
+    assert_same(gy, ny, "ny")
+    assert_same(g.download_plic(), D, "D")
+    assert_same(g.download_band(), band, "band")
+
+
+def test_all_cells_semi_lagrangian_like_the_test_scripts():
+    """test/test_deformation.jl:144 forces band = 0 so every cell takes the SL update."""
+    m, VF = spheres_mesh(N=14, seed=2, n=3)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    band[...] = 0
+    g.upload_band(band)
+    dt = 0.5 * m.dx / 2.0
+    uf, vf, wf = cases.deformation3d_faces(m, 0.7, 3.0)
+    g.upload_velocity(uf, vf, wf)
+    g.transport(dt)
+    o.transport(dt, VFo, uf, vf, wf, nx, ny, nz, D, band)
+    assert_same(g.download_vf(), VFo, "VF, every cell SL")
+
+
+def test_host_dropins_match_the_restatement():
+    m, VF = spheres_mesh(N=12, seed=3, n=3)
+    o = Oracle(m)
+    o.vf_ghost_fill(VF)
+    g = ctx(m)
+    nx, ny, nz = m.cell_array(), m.cell_array(), m.cell_array()
+    g.computeNormal(nx, ny, nz, VF)
+    ox, oy, oz, _ = o.ELVIRA(VF)
+    assert_same(nx, ox, "computeNormal nx")
+    assert_same(nz, oz, "computeNormal nz")
+    D = m.cell_array()
+    g.computePLIC(D, nx, ny, nz, VF)
+    assert_same(D, o.computePLIC(ox, oy, oz, VF), "computePLIC")
+    band = m.cell_array(np.int16)
+    g.computeBand(band, VF)
+    assert_same(band, o.computeBand(VF), "computeBand")
+    dt = 0.01
+    uf, vf, wf = cases.deformation3d_faces(m, 0.2, 3.0)
+    VFg = VF.copy(order="F")
+    g.transportSL(dt, VFg, uf, vf, wf, nx, ny, nz, D, band)
+    VFo = VF.copy(order="F")
+    o.transport(dt, VFo, uf, vf, wf, ox, oy, oz, D, band)
+    assert_same(VFg, VFo, "transportSL")
+
+
+def test_case_generator_matches_numpy():
+    m = Mesh(Nx=20, Ny=18, Nz=16, Lx=1.0, Ly=1.0, Lz=1.0)
+    c, r = cases.config_spheres(12, seed=11)
+    ref = cases.vf_spheres(m, c, r, nF=6)
+    Oracle(m).vf_ghost_fill(ref)
+    g = ctx(m)
+    g.case_vf_spheres(c, r, nF=6)
+    assert_same(g.download_vf(), ref, "VF spheres")
