@@ -25,6 +25,7 @@ UNITS = {
     "k_common.cu": ["-fmad=false"],
     "k_fp64.cu": ["-fmad=false"],
     "k_mixed.cu": ["-fmad=true"],
+    "k_elvira_mixed.cu": ["-fmad=false"],
 }
 
 

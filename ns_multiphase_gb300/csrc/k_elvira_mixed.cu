@@ -1,0 +1,322 @@
+/*
+ * k_elvira_mixed.cu — ELVIRA for interface cells in the mixed-precision path.  Built with
+ * -fmad=false so that its FP64 part rounds exactly like the FP64 path; the FP32 hot loop uses
+ * explicit fmaf.
+ *
+ * Candidate errors (check_normal!, src/ELVIRA.jl:106-137) are evaluated in FP32: the liquid
+ * fraction of each 3x3x3 neighbour under a candidate plane is the exact plane/cube volume in
+ * closed form (the quantity computePLIC2VF evaluates with five tet clips, src/VF.jl:219-278)
+ * and the plane constant is the inverse of the same function (computeAlpha's role,
+ * src/VF.jl:164-214).  Candidates whose FP32 error lies within its rounding bound of the best
+ * are then re-scored in FP64 exactly as the FP64 path scores them (5-tet clips, lanes =
+ * neighbours, errors summed in neighbour order), and the first strict minimum wins; the chosen
+ * candidate is re-formed and normalised in FP64.
+ */
+#include "slvof_kernels.h"
+#include "slvof_dev.cuh"
+#include "plic64.cuh"
+
+namespace slvof {
+
+/* ======================================================================================
+ * Plane/unit-cube volume.  For m1 <= m2 <= m3, m1+m2+m3 = 1 and 0 <= a <= 1/2, the volume
+ * of {s in [0,1]^3 : m.s < a} is the inclusion-exclusion sum
+ *   [a^3 - (a-m1)_+^3 - (a-m2)_+^3 - (a-m3)_+^3 + ...] / (6 m1 m2 m3),
+ * rewritten per interval so that no term divides a cancellation by a small m_i:
+ *   a < m1            : a^3 / (6 m1 m2 m3)
+ *   m1 <= a < m2      : (3a^2 - 3a m1 + m1^2) / (6 m2 m3)
+ *   m2 <= a < m12,m3  : same - (b/m1) b^2 / (6 m2 m3),  b = a - m2 < m1
+ *   m3 <= a (m3<m12)  : same - [(b/m1) b^2 + (c/m1) c^2] / (6 m2 m3),  c = a - m3
+ *   m12 <= a < m3     : (2a - m12) / (2 m3)
+ * and V(a) = 1 - V(1-a) above 1/2.
+ * ==================================================================================== */
+struct Cube {
+    float m1, m2, m3, m12, i6m23, i2m3, im1;
+};
+
+__device__ __forceinline__ Cube make_cube(float a, float b, float c)
+{
+    float t;
+    if (a > b) { t = a; a = b; b = t; }
+    if (b > c) { t = b; b = c; c = t; }
+    if (a > b) { t = a; a = b; b = t; }
+    Cube q;
+    q.m1 = a; q.m2 = b; q.m3 = c; q.m12 = a + b;
+    q.i6m23 = (b > 0.f) ? 1.f / (6.f * b * c) : 0.f;
+    q.i2m3 = 0.5f / c;
+    q.im1 = (a > 0.f) ? 1.f / a : 0.f;
+    return q;
+}
+
+__device__ __forceinline__ float cube_lower(const Cube& q, float a)
+{
+    if (a < q.m1) return a * a * a * q.im1 * q.i6m23;
+    const float base = fmaf(3.f * a, a - q.m1, q.m1 * q.m1) * q.i6m23;
+    if (a < q.m2) return base;
+    if (a < q.m12 && a < q.m3) {
+        const float b = a - q.m2;
+        return fmaf(-(b * q.im1) * b * b, q.i6m23, base);
+    }
+    if (q.m3 < q.m12) {
+        const float b = a - q.m2, c = a - q.m3;
+        return fmaf(-fmaf((b * q.im1) * b, b, (c * q.im1) * c * c), q.i6m23, base);
+    }
+    return fmaf(2.f, a, -q.m12) * q.i2m3;
+}
+
+__device__ __forceinline__ float cube_frac(const Cube& q, float a)
+{
+    if (a <= 0.f) return 0.f;
+    if (a >= 1.f) return 1.f;
+    return a <= 0.5f ? cube_lower(q, a) : 1.f - cube_lower(q, 1.f - a);
+}
+
+/* d/da of cube_lower (cut area), for the Newton inverse. */
+__device__ __forceinline__ float cube_area(const Cube& q, float a)
+{
+    if (a < q.m1) return 3.f * a * a * q.im1 * q.i6m23;
+    const float base = (6.f * a - 3.f * q.m1) * q.i6m23;
+    if (a < q.m2) return base;
+    if (a < q.m12 && a < q.m3) {
+        const float b = a - q.m2;
+        return base - 3.f * (b * q.im1) * b * q.i6m23;
+    }
+    if (q.m3 < q.m12) {
+        const float b = a - q.m2, c = a - q.m3;
+        return base - 3.f * ((b * q.im1) * b + (c * q.im1) * c) * q.i6m23;
+    }
+    return 2.f * q.i2m3;
+}
+
+/* alpha with cube_lower(alpha) = V for V in [0, 1/2] (computeAlpha's role, src/VF.jl:164-214).
+ * The first two intervals and the linear one are inverted in closed form (cbrt, the
+ * quadratic root, a line); on the cubic interval the bracket end points are known, so a
+ * linear start and bracketed Newton converge to FP32 rounding in a few steps. */
+__device__ __forceinline__ float cube_alpha(const Cube& q, float V)
+{
+    if (V <= 0.f) return 0.f;
+    if (q.m2 <= 0.f) return V; /* plane parallel to a face: V(a) = a */
+    const float V1 = q.m1 * q.m1 * q.i6m23;
+    if (V < V1) return cbrtf(V * 6.f * q.m1 * q.m2 * q.m3);
+    const float V2 = fmaf(3.f * q.m2, q.m2 - q.m1, q.m1 * q.m1) * q.i6m23;
+    if (V < V2) return fmaf(0.5f, q.m1, sqrtf(fmaxf(fmaf(2.f * q.m2 * q.m3, V, -q.m1 * q.m1 * (1.f / 12.f)), 0.f)));
+    float lo, hi;
+    if (q.m3 >= q.m12) {
+        if (V >= q.m12 * q.i2m3) return fmaf(V, q.m3, 0.5f * q.m12);
+        lo = q.m2; hi = q.m12;
+    } else {
+        if (V < cube_lower(q, q.m3)) { lo = q.m2; hi = q.m3; }
+        else { lo = q.m3; hi = 0.5f; }
+    }
+    const float vl = cube_lower(q, lo), vh = cube_lower(q, hi);
+    float a = vh > vl ? fmaf((V - vl) / (vh - vl), hi - lo, lo) : 0.5f * (lo + hi);
+#pragma unroll 1
+    for (int it = 0; it < 5; ++it) {
+        const float f = cube_lower(q, a) - V;
+        if (f > 0.f) hi = a;
+        else lo = a;
+        const float s = cube_area(q, a);
+        float an = s > 0.f ? a - f / s : 0.5f * (lo + hi);
+        if (!(an >= lo && an <= hi)) an = 0.5f * (lo + hi);
+        a = an;
+    }
+    return a;
+}
+
+/* Candidate normal of lane (family f, outer a, inner b) from a 3x3x3 VF block; R = float
+ * for the error pass, double to form candidates exactly as the FP64 path does. */
+template <class R>
+__device__ __forceinline__ void candidate(const R* sv, int f, int a, int b, R dx, R dy, R dz, const R* hx, const R* hy,
+                                          const R* hz, R& cx, R& cy, R& cz)
+{
+    /* h[0] = xm[i]-xm[i-1], h[1] = xm[i+1]-xm[i-1], h[2] = xm[i+1]-xm[i]: the reference's
+     * pairs {i-1,i}, {i-1,i+1}, {i,i+1} (src/ELVIRA.jl:72,82,92) */
+#define V3(p, q, r) sv[((r) + 1) * 9 + ((q) + 1) * 3 + ((p) + 1)]
+    const int o1 = a == 2 ? 0 : -1, o2 = a == 0 ? 0 : 1;
+    const int i1 = b == 2 ? 0 : -1, i2 = b == 0 ? 0 : 1;
+    if (f == 0) {
+        const R s2x = (V3(i2, 0, -1) * dz + V3(i2, 0, 0) * dz) + V3(i2, 0, 1) * dz;
+        const R s1x = (V3(i1, 0, -1) * dz + V3(i1, 0, 0) * dz) + V3(i1, 0, 1) * dz;
+        cx = -(s2x - s1x) / hx[b];
+        const R s2y = (V3(0, o2, -1) * dz + V3(0, o2, 0) * dz) + V3(0, o2, 1) * dz;
+        const R s1y = (V3(0, o1, -1) * dz + V3(0, o1, 0) * dz) + V3(0, o1, 1) * dz;
+        cy = -(s2y - s1y) / hy[a];
+        cz = V3(0, 0, 1) > V3(0, 0, -1) ? R(-1) : R(1);
+    } else if (f == 1) {
+        const R s2x = (V3(i2, -1, 0) * dy + V3(i2, 0, 0) * dy) + V3(i2, 1, 0) * dy;
+        const R s1x = (V3(i1, -1, 0) * dy + V3(i1, 0, 0) * dy) + V3(i1, 1, 0) * dy;
+        cx = -(s2x - s1x) / hx[b];
+        cy = V3(0, 1, 0) > V3(0, -1, 0) ? R(-1) : R(1);
+        const R s2z = (V3(0, -1, o2) * dy + V3(0, 0, o2) * dy) + V3(0, 1, o2) * dy;
+        const R s1z = (V3(0, -1, o1) * dy + V3(0, 0, o1) * dy) + V3(0, 1, o1) * dy;
+        cz = -(s2z - s1z) / hz[a];
+    } else {
+        cx = V3(1, 0, 0) > V3(-1, 0, 0) ? R(-1) : R(1);
+        const R s2y = (V3(-1, i2, 0) * dx + V3(0, i2, 0) * dx) + V3(1, i2, 0) * dx;
+        const R s1y = (V3(-1, i1, 0) * dx + V3(0, i1, 0) * dx) + V3(1, i1, 0) * dx;
+        cy = -(s2y - s1y) / hy[b];
+        const R s2z = (V3(-1, 0, o2) * dx + V3(0, 0, o2) * dx) + V3(1, 0, o2) * dx;
+        const R s1z = (V3(-1, 0, o1) * dx + V3(0, 0, o1) * dx) + V3(1, 0, o1) * dx;
+        cz = -(s2z - s1z) / hz[a];
+    }
+#undef V3
+}
+
+
+constexpr int EL32_WARPS = 8;
+
+__device__ __forceinline__ int lane_family(const int* fam_on, int lane)
+{
+    const int fam = lane / 9;
+    for (int q = 0, seen = 0; q < 3; ++q)
+        if (fam_on[q]) { if (seen == fam) return q; ++seen; }
+    return 0;
+}
+
+/* Candidate of lane c in FP64, L2-normalised (src/ELVIRA.jl:72-98,112-115). */
+__device__ __forceinline__ void candidate64(const DevMesh& m, const double* sv, const int* fam_on, int c, int i, int j,
+                                            int k, double& cx, double& cy, double& cz)
+{
+    const double hx[3] = {cco(m, 0, i) - cco(m, 0, i - 1), cco(m, 0, i + 1) - cco(m, 0, i - 1),
+                          cco(m, 0, i + 1) - cco(m, 0, i)};
+    const double hy[3] = {cco(m, 1, j) - cco(m, 1, j - 1), cco(m, 1, j + 1) - cco(m, 1, j - 1),
+                          cco(m, 1, j + 1) - cco(m, 1, j)};
+    const double hz[3] = {cco(m, 2, k) - cco(m, 2, k - 1), cco(m, 2, k + 1) - cco(m, 2, k - 1),
+                          cco(m, 2, k + 1) - cco(m, 2, k)};
+    candidate<double>(sv, lane_family(fam_on, c), (c % 9) / 3, c % 3, m.d[0], m.d[1], m.d[2], hx, hy, hz, cx, cy, cz);
+    const double norm = sqrt((cx * cx + cy * cy) + cz * cz);
+    cx = cx / norm; cy = cy / norm; cz = cz / norm;
+}
+
+__global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, const double* __restrict__ VF,
+                                                                    double* __restrict__ nx, double* __restrict__ ny,
+                                                                    double* __restrict__ nz,
+                                                                    const int* __restrict__ list,
+                                                                    const int* __restrict__ count, int* work,
+                                                                    int* stats, int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    __shared__ double s_vd[EL32_WARPS][27];
+    __shared__ float s_vf[EL32_WARPS][27];
+    __shared__ double s_term[EL32_WARPS][27][5];
+    __shared__ double s_full[EL32_WARPS][27];
+    load_table(s_tab);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_items = *count;
+    const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
+    const int ncand = 9 * (fam_on[0] + fam_on[1] + fam_on[2]);
+    const float dx = (float)m.d[0], dy = (float)m.d[1], dz = (float)m.d[2];
+    int err = 0, n_arb = 0;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(work, 1);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= n_items) break;
+        const int L = list[item];
+        const int i = 1 + L % m.N[0];
+        const int j = 1 + (L / m.N[0]) % m.N[1];
+        const int k = 1 + L / (m.N[0] * m.N[1]);
+        if (lane < 27) {
+            const double v = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
+            s_vd[w][lane] = v;
+            s_vf[w][lane] = (float)v;
+        }
+        __syncwarp();
+        const float* sv = s_vf[w];
+        float err_ = INFINITY, tol = 0.f;
+        if (lane < ncand) {
+            const int f = lane_family(fam_on, lane);
+            const int a = (lane % 9) / 3, b = lane % 3;
+            float cx, cy, cz;
+            const float hx[3] = {dx, 2.f * dx, dx}, hy[3] = {dy, 2.f * dy, dy}, hz[3] = {dz, 2.f * dz, dz};
+            candidate<float>(sv, f, a, b, dx, dy, dz, hx, hy, hz, cx, cy, cz);
+            const float nrm = sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
+            cx /= nrm; cy /= nrm; cz /= nrm;
+            /* computeDist in cell units: mm = n*d/|n*d|_1; neighbour (p,r,s) holds the cube
+             * fraction at al - mm.(p,r,s) (sign folding absorbed in al) */
+            float m0 = cx * dx, m1 = cy * dy, m2 = cz * dz;
+            const float n1 = fabsf(m0) + fabsf(m1) + fabsf(m2);
+            m0 /= n1; m1 /= n1; m2 /= n1;
+            const Cube q = make_cube(fabsf(m0), fabsf(m1), fabsf(m2));
+            const float vc = sv[13];
+            const float vo = vc > 0.5f ? 1.f - vc : vc;
+            float al = cube_alpha(q, vo);
+            al = vc > 0.5f ? 1.f - al : al;
+            float e2 = 0.f, sa = 0.f;
+#pragma unroll
+            for (int c = 0; c < 27; ++c) {
+                const float p = (float)(c % 3 - 1), r = (float)((c / 3) % 3 - 1), s = (float)(c / 9 - 1);
+                const float ae = al - fmaf(m0, p, fmaf(m1, r, m2 * s));
+                const float d = sv[c] - cube_frac(q, ae);
+                e2 = fmaf(d, d, e2);
+                sa += fabsf(d);
+            }
+            err_ = e2;
+            /* bound on the FP32 error of e2: each fraction is good to a few 1e-7 */
+            tol = 4e-6f * sa + 1e-5f * e2 + 1e-12f;
+        }
+        /* FP32 winner and the set of candidates that could beat it in exact arithmetic */
+        const bool fin = err_ < INFINITY;
+        float hi = fin ? err_ + tol : INFINITY;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) hi = fminf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+        const unsigned contend = __ballot_sync(0xffffffffu, fin && err_ - tol <= hi);
+        int winner = 32;
+        if (__popc(contend) == 1) {
+            winner = __ffs(contend) - 1;
+        } else if (contend) {
+            /* FP64 arbitration, exactly as check_normal! scores candidates in the FP64 path */
+            ++n_arb;
+            if (lane < 27) {
+                NbrGeom G;
+                nbr_geom(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9, G);
+                double full = 0.0;
+#pragma unroll
+                for (int t = 0; t < 5; ++t) {
+                    const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), e = tet5(t, 3);
+                    const double tv = tet_vol(G.X[a & 1], G.Y[(a >> 1) & 1], G.Z[a >> 2], G.X[b & 1],
+                                              G.Y[(b >> 1) & 1], G.Z[b >> 2], G.X[c & 1], G.Y[(c >> 1) & 1],
+                                              G.Z[c >> 2], G.X[e & 1], G.Y[(e >> 1) & 1], G.Z[e >> 2]);
+                    const double term = G.tetsign * tv / m.cellvol;
+                    s_term[w][lane][t] = term;
+                    full += term;
+                }
+                s_full[w][lane] = full;
+            }
+            __syncwarp();
+            NbrGeom G;
+            const int ql = lane < 27 ? lane : 26;
+            nbr_geom(m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, G);
+            double bestE = INFINITY;
+            for (unsigned mask = contend; mask; mask &= mask - 1) {
+                const int c = __ffs(mask) - 1;
+                double cx, cy, cz;
+                candidate64(m, s_vd[w], fam_on, c, i, j, k, cx, cy, cz);
+                const double dist = compute_dist64(m, i, j, k, cx, cy, cz, s_vd[w][13]);
+                const double v_ = plic2vf64(s_tab, G, s_term[w][ql], s_full[w][ql], cx, cy, cz, dist, m.cellvol, err);
+                const double r = s_vd[w][ql] - v_;
+                const double r2 = r * r;
+                double e2 = 0.0;
+                for (int q = 0; q < 27; ++q) e2 += __shfl_sync(0xffffffffu, r2, q);
+                if (e2 < bestE) { bestE = e2; winner = c; }
+            }
+        }
+        if (winner < 32 && lane == winner) {
+            double cx, cy, cz;
+            candidate64(m, s_vd[w], fam_on, winner, i, j, k, cx, cy, cz);
+            const long o = cidx(m, i, j, k);
+            nx[o] = cx; ny[o] = cy; nz[o] = cz;
+        }
+        __syncwarp();
+    }
+    if (lane == 0 && n_arb) atomicAdd(stats, n_arb);
+    if (err) atomicOr(errw, err);
+}
+
+void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
+                           const int* count, int* work, int* stats, int* errw, int nsm, cudaStream_t s)
+{
+    k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, stats, errw);
+}
+
+} // namespace slvof

@@ -6,247 +6,15 @@
  * and the cell volume is 1.  This needs a uniform mesh, which create_mesh builds
  * (src/Mesh.jl:83-100); slvof_create rejects the mixed mode otherwise.
  *
- *   k_elvira_iface32 : ELVIRA candidates (src/ELVIRA.jl:62-137) with FP32 candidate errors.
- *                      The liquid fraction of each 3x3x3 neighbour under a candidate plane is
- *                      the exact plane/cube volume in closed form (the quantity
- *                      computePLIC2VF evaluates with five tet clips), and the plane constant
- *                      is the inverse of the same function (computeAlpha's role).  The chosen
- *                      candidate is re-formed and normalised in FP64.
- *   k_sl32           : SL update (src/Transport.jl:111-148): FP32 RK trajectories through
- *                      FP32 face velocities, FP32 recursive clip (same cut tables and
- *                      recursion as cutTet), FP64 accumulation of the clipped volumes.
+ *   k_sl32_*         : SL update (src/Transport.jl:111-148) in three stages: FP32 RK
+ *                      trajectories through FP32 face velocities (one thread per band cell),
+ *                      FP32 recursive clip of each tet (same cut tables and recursion as
+ *                      cutTet, one thread per tet), FP64 accumulation of the clipped volumes.
  */
 #include "slvof_kernels.h"
 #include "slvof_dev.cuh"
 
 namespace slvof {
-
-/* ======================================================================================
- * Plane/unit-cube volume.  For m1 <= m2 <= m3, m1+m2+m3 = 1 and 0 <= a <= 1/2, the volume
- * of {s in [0,1]^3 : m.s < a} is the inclusion-exclusion sum
- *   [a^3 - (a-m1)_+^3 - (a-m2)_+^3 - (a-m3)_+^3 + ...] / (6 m1 m2 m3),
- * rewritten per interval so that no term divides a cancellation by a small m_i:
- *   a < m1            : a^3 / (6 m1 m2 m3)
- *   m1 <= a < m2      : (3a^2 - 3a m1 + m1^2) / (6 m2 m3)
- *   m2 <= a < m12,m3  : same - (b/m1) b^2 / (6 m2 m3),  b = a - m2 < m1
- *   m3 <= a (m3<m12)  : same - [(b/m1) b^2 + (c/m1) c^2] / (6 m2 m3),  c = a - m3
- *   m12 <= a < m3     : (2a - m12) / (2 m3)
- * and V(a) = 1 - V(1-a) above 1/2.
- * ==================================================================================== */
-struct Cube {
-    float m1, m2, m3, m12, i6m23, i2m3, im1;
-};
-
-__device__ __forceinline__ Cube make_cube(float a, float b, float c)
-{
-    float t;
-    if (a > b) { t = a; a = b; b = t; }
-    if (b > c) { t = b; b = c; c = t; }
-    if (a > b) { t = a; a = b; b = t; }
-    Cube q;
-    q.m1 = a; q.m2 = b; q.m3 = c; q.m12 = a + b;
-    q.i6m23 = (b > 0.f) ? 1.f / (6.f * b * c) : 0.f;
-    q.i2m3 = 0.5f / c;
-    q.im1 = (a > 0.f) ? 1.f / a : 0.f;
-    return q;
-}
-
-__device__ __forceinline__ float cube_lower(const Cube& q, float a)
-{
-    if (a < q.m1) return a * a * a * q.im1 * q.i6m23;
-    const float base = (3.f * a * a - 3.f * a * q.m1 + q.m1 * q.m1) * q.i6m23;
-    if (a < q.m2) return base;
-    if (a < q.m12 && a < q.m3) {
-        const float b = a - q.m2;
-        return base - (b * q.im1) * b * b * q.i6m23;
-    }
-    if (q.m3 < q.m12) {
-        const float b = a - q.m2, c = a - q.m3;
-        return base - ((b * q.im1) * b * b + (c * q.im1) * c * c) * q.i6m23;
-    }
-    return (2.f * a - q.m12) * q.i2m3;
-}
-
-__device__ __forceinline__ float cube_frac(const Cube& q, float a)
-{
-    if (a <= 0.f) return 0.f;
-    if (a >= 1.f) return 1.f;
-    return a <= 0.5f ? cube_lower(q, a) : 1.f - cube_lower(q, 1.f - a);
-}
-
-/* d/da of cube_lower (cut area), for the Newton inverse. */
-__device__ __forceinline__ float cube_area(const Cube& q, float a)
-{
-    if (a < q.m1) return 3.f * a * a * q.im1 * q.i6m23;
-    const float base = (6.f * a - 3.f * q.m1) * q.i6m23;
-    if (a < q.m2) return base;
-    if (a < q.m12 && a < q.m3) {
-        const float b = a - q.m2;
-        return base - 3.f * (b * q.im1) * b * q.i6m23;
-    }
-    if (q.m3 < q.m12) {
-        const float b = a - q.m2, c = a - q.m3;
-        return base - 3.f * ((b * q.im1) * b + (c * q.im1) * c) * q.i6m23;
-    }
-    return 2.f * q.i2m3;
-}
-
-/* alpha with cube_frac(alpha) = V for V in [0, 1/2] (computeAlpha, src/VF.jl:164-214):
- * closed-form start on the first two intervals, then bracketed Newton. */
-__device__ __forceinline__ float cube_alpha(const Cube& q, float V)
-{
-    if (V <= 0.f) return 0.f;
-    if (q.m2 <= 0.f) return V; /* plane parallel to a face */
-    const float V1 = q.m1 * q.m1 * q.i6m23;
-    float a;
-    if (V < V1) a = cbrtf(V * 6.f * q.m1 * q.m2 * q.m3);
-    else a = 0.5f * (q.m1 + sqrtf(fmaxf(q.m1 * q.m1 + 8.f * q.m2 * q.m3 * (V - V1), 0.f)));
-    float lo = 0.f, hi = 0.5f;
-    a = fminf(fmaxf(a, lo), hi);
-#pragma unroll 1
-    for (int it = 0; it < 6; ++it) {
-        const float f = cube_lower(q, a) - V;
-        if (f > 0.f) hi = a;
-        else lo = a;
-        const float s = cube_area(q, a);
-        float an = s > 0.f ? a - f / s : 0.5f * (lo + hi);
-        if (!(an > lo && an < hi)) an = 0.5f * (lo + hi);
-        a = an;
-    }
-    return a;
-}
-
-/* ======================================================================================
- * ELVIRA candidates in FP32.
- * ==================================================================================== */
-constexpr int EL32_WARPS = 8;
-
-/* Candidate normal of lane (family f, outer a, inner b) from a 3x3x3 VF block; R = float
- * for the error pass, double to re-form the chosen candidate exactly as the FP64 path. */
-template <class R>
-__device__ __forceinline__ void candidate(const R* sv, int f, int a, int b, R dx, R dy, R dz, const R* hx, const R* hy,
-                                          const R* hz, R& cx, R& cy, R& cz)
-{
-    /* h[0] = xm[i]-xm[i-1], h[1] = xm[i+1]-xm[i-1], h[2] = xm[i+1]-xm[i]: the reference's
-     * pairs {i-1,i}, {i-1,i+1}, {i,i+1} (src/ELVIRA.jl:72,82,92) */
-#define V3(p, q, r) sv[((r) + 1) * 9 + ((q) + 1) * 3 + ((p) + 1)]
-    const int o1 = a == 2 ? 0 : -1, o2 = a == 0 ? 0 : 1;
-    const int i1 = b == 2 ? 0 : -1, i2 = b == 0 ? 0 : 1;
-    if (f == 0) {
-        const R s2x = (V3(i2, 0, -1) * dz + V3(i2, 0, 0) * dz) + V3(i2, 0, 1) * dz;
-        const R s1x = (V3(i1, 0, -1) * dz + V3(i1, 0, 0) * dz) + V3(i1, 0, 1) * dz;
-        cx = -(s2x - s1x) / hx[b];
-        const R s2y = (V3(0, o2, -1) * dz + V3(0, o2, 0) * dz) + V3(0, o2, 1) * dz;
-        const R s1y = (V3(0, o1, -1) * dz + V3(0, o1, 0) * dz) + V3(0, o1, 1) * dz;
-        cy = -(s2y - s1y) / hy[a];
-        cz = V3(0, 0, 1) > V3(0, 0, -1) ? R(-1) : R(1);
-    } else if (f == 1) {
-        const R s2x = (V3(i2, -1, 0) * dy + V3(i2, 0, 0) * dy) + V3(i2, 1, 0) * dy;
-        const R s1x = (V3(i1, -1, 0) * dy + V3(i1, 0, 0) * dy) + V3(i1, 1, 0) * dy;
-        cx = -(s2x - s1x) / hx[b];
-        cy = V3(0, 1, 0) > V3(0, -1, 0) ? R(-1) : R(1);
-        const R s2z = (V3(0, -1, o2) * dy + V3(0, 0, o2) * dy) + V3(0, 1, o2) * dy;
-        const R s1z = (V3(0, -1, o1) * dy + V3(0, 0, o1) * dy) + V3(0, 1, o1) * dy;
-        cz = -(s2z - s1z) / hz[a];
-    } else {
-        cx = V3(1, 0, 0) > V3(-1, 0, 0) ? R(-1) : R(1);
-        const R s2y = (V3(-1, i2, 0) * dx + V3(0, i2, 0) * dx) + V3(1, i2, 0) * dx;
-        const R s1y = (V3(-1, i1, 0) * dx + V3(0, i1, 0) * dx) + V3(1, i1, 0) * dx;
-        cy = -(s2y - s1y) / hy[b];
-        const R s2z = (V3(-1, 0, o2) * dx + V3(0, 0, o2) * dx) + V3(1, 0, o2) * dx;
-        const R s1z = (V3(-1, 0, o1) * dx + V3(0, 0, o1) * dx) + V3(1, 0, o1) * dx;
-        cz = -(s2z - s1z) / hz[a];
-    }
-#undef V3
-}
-
-__global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, const double* __restrict__ VF,
-                                                                    double* __restrict__ nx, double* __restrict__ ny,
-                                                                    double* __restrict__ nz,
-                                                                    const int* __restrict__ list,
-                                                                    const int* __restrict__ count, int* work)
-{
-    __shared__ double s_vd[EL32_WARPS][27];
-    __shared__ float s_vf[EL32_WARPS][27];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_items = *count;
-    const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
-    const int ncand = 9 * (fam_on[0] + fam_on[1] + fam_on[2]);
-    const float dx = (float)m.d[0], dy = (float)m.d[1], dz = (float)m.d[2];
-    for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(work, 1);
-        item = __shfl_sync(0xffffffffu, item, 0);
-        if (item >= n_items) break;
-        const int L = list[item];
-        const int i = 1 + L % m.N[0];
-        const int j = 1 + (L / m.N[0]) % m.N[1];
-        const int k = 1 + L / (m.N[0] * m.N[1]);
-        if (lane < 27) {
-            const double v = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
-            s_vd[w][lane] = v;
-            s_vf[w][lane] = (float)v;
-        }
-        __syncwarp();
-        const float* sv = s_vf[w];
-        float err_ = INFINITY;
-        int f = 0, a = 0, b = 0;
-        if (lane < ncand) {
-            const int fam = lane / 9;
-            a = (lane % 9) / 3;
-            b = lane % 3;
-            for (int q = 0, seen = 0; q < 3; ++q)
-                if (fam_on[q]) { if (seen == fam) { f = q; break; } ++seen; }
-            float cx, cy, cz;
-            const float hx[3] = {dx, 2.f * dx, dx}, hy[3] = {dy, 2.f * dy, dy}, hz[3] = {dz, 2.f * dz, dz};
-            candidate<float>(sv, f, a, b, dx, dy, dz, hx, hy, hz, cx, cy, cz);
-            const float nrm = sqrtf(cx * cx + cy * cy + cz * cz);
-            cx /= nrm; cy /= nrm; cz /= nrm;
-            /* computeDist in cell units: mm = n*d/|n*d|_1, plane mm.u = alpha' + sum(mm<0) */
-            float m0 = cx * dx, m1 = cy * dy, m2 = cz * dz;
-            const float n1 = fabsf(m0) + fabsf(m1) + fabsf(m2);
-            m0 /= n1; m1 /= n1; m2 /= n1;
-            const Cube q = make_cube(fabsf(m0), fabsf(m1), fabsf(m2));
-            const float vc = sv[13];
-            const float vo = vc > 0.5f ? 1.f - vc : vc;
-            float al = cube_alpha(q, vo);
-            al = vc > 0.5f ? 1.f - al : al;
-            /* neighbour (p,r,s) takes the cube fraction at al - mm.(p,r,s) (sign-folded) */
-            float e2 = 0.f;
-#pragma unroll
-            for (int c = 0; c < 27; ++c) {
-                const float p = (float)(c % 3 - 1), r = (float)((c / 3) % 3 - 1), s = (float)(c / 9 - 1);
-                const float ae = al - (m0 * p + m1 * r + m2 * s);
-                const float d = sv[c] - cube_frac(q, ae);
-                e2 += d * d;
-            }
-            err_ = e2;
-        }
-        float be = err_ < INFINITY ? err_ : INFINITY;
-        int bl = err_ < INFINITY ? lane : 32;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            const float ob = __shfl_xor_sync(0xffffffffu, be, off);
-            const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
-            if (ob < be || (ob == be && ol < bl)) { be = ob; bl = ol; }
-        }
-        if (bl < 32 && lane == bl) {
-            /* re-form the chosen candidate in FP64 as check_normal! does */
-            double cx, cy, cz;
-            const double hx[3] = {cco(m, 0, i) - cco(m, 0, i - 1), cco(m, 0, i + 1) - cco(m, 0, i - 1),
-                                  cco(m, 0, i + 1) - cco(m, 0, i)};
-            const double hy[3] = {cco(m, 1, j) - cco(m, 1, j - 1), cco(m, 1, j + 1) - cco(m, 1, j - 1),
-                                  cco(m, 1, j + 1) - cco(m, 1, j)};
-            const double hz[3] = {cco(m, 2, k) - cco(m, 2, k - 1), cco(m, 2, k + 1) - cco(m, 2, k - 1),
-                                  cco(m, 2, k + 1) - cco(m, 2, k)};
-            candidate<double>(s_vd[w], f, a, b, m.d[0], m.d[1], m.d[2], hx, hy, hz, cx, cy, cz);
-            const double norm = sqrt((cx * cx + cy * cy) + cz * cz);
-            const long o = cidx(m, i, j, k);
-            nx[o] = cx / norm; ny[o] = cy / norm; nz[o] = cz / norm;
-        }
-        __syncwarp();
-    }
-}
 
 /* ======================================================================================
  * SL update in FP32 local coordinates.
@@ -331,12 +99,43 @@ __device__ __forceinline__ int idx32(float u, int s, int lo, int hi, int& err)
     return I;
 }
 
+/* float-float running sum (TwoSum error-free transformation): ~48-bit accumulation of the
+ * FP32 sub-tet volumes without using the FP64 pipe. */
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF& a, float x)
+{
+    const float s = a.hi + x;
+    const float bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (x - bb);
+    a.hi = s;
+    a.lo += e;
+}
+__device__ __forceinline__ void ff_add(FF& a, const FF& b)
+{
+    ff_add(a, b.hi);
+    a.lo += b.lo;
+}
+
+/* One cutTet recursion level: parent tet (vertices 0-3), new vertices on the cutting mesh
+ * plane (4-7), their side-1 cell indices packed as bytes, the children's running sums, and
+ * case / next child / direction / done flags / cut index packed in meta. */
 struct Frame32 {
     float x[8], y[8], z[8];
-    double acc_v, acc_l;
-    signed char ind[8][3];
-    signed char cs, next, dir, flags, cut;
+    unsigned ind[8];
+    FF vol, liq;
+    int meta;
 };
+__device__ __forceinline__ unsigned pack3(int a, int b, int c)
+{
+    return (unsigned)(a + 128) | ((unsigned)(b + 128) << 8) | ((unsigned)(c + 128) << 16);
+}
+__device__ __forceinline__ int unpack(unsigned p, int q) { return (int)((p >> (8 * q)) & 255u) - 128; }
+__device__ __forceinline__ int meta_pack(int cs, int next, int dir, int flags, int cut)
+{
+    return cs | (next << 4) | (dir << 8) | (flags << 10) | ((cut + 128) << 16);
+}
 
 struct Plane32 {
     const float4* P; /* (mx, my, mz, Dl): n*d and D - n.o in the donor's own cell frame */
@@ -349,7 +148,7 @@ __device__ __forceinline__ float tet_vol32(const float* vx, const float* vy, con
 
 __device__ __forceinline__ void leaf32(const DevMesh& m, const CutCase* tab, const Plane32& PL, int i0, int j0, int k0,
                                        const float* cx, const float* cy, const float* cz, int di, int dj, int dk,
-                                       double& rv, double& rl, int& err)
+                                       FF& rv, FF& rl, int& err)
 {
     const float4 pl = __ldg(PL.P + cidx(m, i0 + di, j0 + dj, k0 + dk));
     const float Dt = pl.w + pl.x * (float)di + pl.y * (float)dj + pl.z * (float)dk;
@@ -370,13 +169,13 @@ __device__ __forceinline__ void leaf32(const DevMesh& m, const CutCase* tab, con
         vy[4 + n] = vy[v1] + mu * (vy[v2] - vy[v1]);
         vz[4 + n] = vz[v1] + mu * (vz[v2] - vz[v1]);
     }
-    double vol = 0.0, liq = 0.0;
+    FF vol{0.f, 0.f}, liq{0.f, 0.f};
     for (int n = C.ntets - 1; n >= C.nntet - 1; --n) {
-        const double tv = tet_vol32(vx, vy, vz, C.vtet[n][0], C.vtet[n][1], C.vtet[n][2], C.vtet[n][3]);
-        vol += tv;
-        liq += tv;
+        const float tv = tet_vol32(vx, vy, vz, C.vtet[n][0], C.vtet[n][1], C.vtet[n][2], C.vtet[n][3]);
+        ff_add(vol, tv);
+        ff_add(liq, tv);
     }
-    for (int n = 0; n < C.nntet - 1; ++n) vol += tet_vol32(vx, vy, vz, C.vtet[n][0], C.vtet[n][1], C.vtet[n][2], C.vtet[n][3]);
+    for (int n = 0; n < C.nntet - 1; ++n) ff_add(vol, tet_vol32(vx, vy, vz, C.vtet[n][0], C.vtet[n][1], C.vtet[n][2], C.vtet[n][3]));
     rv = vol;
     rl = liq;
 }
@@ -384,91 +183,157 @@ __device__ __forceinline__ void leaf32(const DevMesh& m, const CutCase* tab, con
 __device__ __forceinline__ void form_child32(const Frame32& F, const CutCase* tab, int n, float* cx, float* cy,
                                              float* cz, int (*ci)[3])
 {
-    const CutCase& C = tab[F.cs];
+    const int cs = F.meta & 15, dir = (F.meta >> 8) & 3, cut = ((F.meta >> 16) & 255) - 128;
+    const CutCase& C = tab[cs];
     const int side = C.side[n];
     for (int nn = 0; nn < 4; ++nn) {
         const int v = C.vtet[n][nn];
         cx[nn] = F.x[v]; cy[nn] = F.y[v]; cz[nn] = F.z[v];
-        ci[nn][0] = F.ind[v][0]; ci[nn][1] = F.ind[v][1]; ci[nn][2] = F.ind[v][2];
-        if (side == 1) ci[nn][(int)F.dir] = F.cut;
+        const unsigned p = F.ind[v];
+        ci[nn][0] = unpack(p, 0); ci[nn][1] = unpack(p, 1); ci[nn][2] = unpack(p, 2);
+        if (side == 1) ci[nn][dir] = cut;
     }
 }
 
-/* cutTet (src/VFgeom.jl:713-900) with an explicit stack; indices relative to the cell. */
-__device__ void clip32(const DevMesh& m, const CutCase* tab, const Plane32& PL, int i0, int j0, int k0,
-                       const int* rlo, const int* rhi, float* cx, float* cy, float* cz, int (*ci)[3], double& out_v,
-                       double& out_l, int& err)
+/* Phase code shared by every donor cell of an index box (+1 all liquid, -1 all gas, 0 mixed
+ * or interface).  Boxes wider than 2 cells in some direction report 0. */
+__device__ __forceinline__ int box_phase(const DevMesh& m, const signed char* __restrict__ phase, int i0, int j0,
+                                         int k0, int lo0, int hi0, int lo1, int hi1, int lo2, int hi2)
 {
-    Frame32 st[CLIP_STACK];
+    if (hi0 - lo0 > 1 || hi1 - lo1 > 1 || hi2 - lo2 > 1) return 0;
+    int ph = 2;
+    for (int c = lo2; c <= hi2; ++c)
+        for (int b = lo1; b <= hi1; ++b)
+            for (int a = lo0; a <= hi0; ++a) {
+                const int p = __ldg(phase + cidx(m, i0 + a, j0 + b, k0 + c));
+                if (p == 0 || (ph != 2 && p != ph)) return 0;
+                ph = p;
+            }
+    return ph;
+}
+
+/* Side of a point set against every donor PLIC plane of an index box (at most 2x2x2 cells):
+ * +1 when every point is strictly on the liquid side of every donor's plane, -1 when strictly
+ * on the gas side of every one, 0 otherwise.  Every PLIC leaf under a (sub-)tet with +1 is
+ * then d2case case 1 (all liquid) and with -1 case 16 (all gas), whatever the mesh cuts, so
+ * the clipped volume needs no cuts.  Pure donors have planes at |D| = Lx+Ly+Lz, which put
+ * everything on one side, so this covers the pure-donor case. */
+template <int NP>
+__device__ __forceinline__ int box_plane_side(const DevMesh& m, const Plane32& PL, int i0, int j0, int k0, int lo0,
+                                              int hi0, int lo1, int hi1, int lo2, int hi2, const float* cx,
+                                              const float* cy, const float* cz)
+{
+    if (hi0 - lo0 > 1 || hi1 - lo1 > 1 || hi2 - lo2 > 1) return 0;
+    int side = 2;
+    for (int c = lo2; c <= hi2; ++c)
+        for (int b = lo1; b <= hi1; ++b)
+            for (int a = lo0; a <= hi0; ++a) {
+                const float4 p = __ldg(PL.P + cidx(m, i0 + a, j0 + b, k0 + c));
+                const float Dt = p.w + p.x * (float)a + p.y * (float)b + p.z * (float)c;
+                bool neg = true, pos = true;
+#pragma unroll
+                for (int n = 0; n < NP; ++n) {
+                    const float d = fmaf(p.x, cx[n], fmaf(p.y, cy[n], fmaf(p.z, cz[n], -Dt)));
+                    neg = neg && d < 0.f;
+                    pos = pos && d > 0.f;
+                }
+                const int sd = neg ? 1 : (pos ? -1 : 0);
+                if (sd == 0 || (side != 2 && sd != side)) return 0;
+                side = sd;
+            }
+    return side;
+}
+
+/* cutTet (src/VFgeom.jl:713-900) with an explicit stack; indices relative to the cell.
+ * A (sub-)tet whose donor box is uniformly pure is one leaf: every PLIC leaf below it would
+ * be d2case case 1 (or 16), so its clipped volume is the tet's own volume, all liquid (or
+ * all gas); the mesh-plane cuts under it are skipped. */
+__device__ void clip32(const DevMesh& m, const CutCase* tab, const Plane32& PL, const signed char* __restrict__ phase,
+                       int i0, int j0, int k0, const int* rlo, const int* rhi, float* cx, float* cy, float* cz,
+                       int (*ci)[3], FF& out_v, FF& out_l, int& err)
+{
+    Frame32 st[CLIP_STACK32];
     int depth = 0, flags = 0, leaves = 0;
     for (;;) {
         int dir = -1, cut = 0;
+        int lo[3], hi[3];
         for (int q = 0; q < 3; ++q) {
-            if (flags & (1 << q)) continue;
-            const int mx = max(max(ci[0][q], ci[1][q]), max(ci[2][q], ci[3][q]));
-            const int mn = min(min(ci[0][q], ci[1][q]), min(ci[2][q], ci[3][q]));
-            if (mx > mn) { dir = q; cut = mx; break; }
-            flags |= 1 << q;
+            lo[q] = min(min(ci[0][q], ci[1][q]), min(ci[2][q], ci[3][q]));
+            hi[q] = max(max(ci[0][q], ci[1][q]), max(ci[2][q], ci[3][q]));
         }
-        double rv, rl;
-        if (dir >= 0 && depth == CLIP_STACK) { err |= ERR_DEPTH; dir = -1; }
-        if (dir < 0) {
-            if (++leaves > CLIP_MAX_LEAVES) {
-                err |= ERR_DEPTH;
-                out_v = 0.0; out_l = 0.0;
-                return;
-            }
-            leaf32(m, tab, PL, i0, j0, k0, cx, cy, cz, ci[0][0], ci[0][1], ci[0][2], rv, rl, err);
+        FF rv, rl;
+        const int bp = m.fast_pure ? box_plane_side<4>(m, PL, i0, j0, k0, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], cx, cy, cz) : 0;
+        if (bp != 0) {
+            const float tv = tet_vol<float>(cx[0], cy[0], cz[0], cx[1], cy[1], cz[1], cx[2], cy[2], cz[2], cx[3], cy[3], cz[3]);
+            rv = FF{tv, 0.f};
+            rl = FF{bp > 0 ? tv : 0.f, 0.f};
+            if (++leaves > CLIP_MAX_LEAVES) { err |= ERR_DEPTH; out_v = FF{0.f, 0.f}; out_l = FF{0.f, 0.f}; return; }
         } else {
-            Frame32& F = st[depth];
-            const float pl = (float)cut;
-            const float* cd = dir == 0 ? cx : (dir == 1 ? cy : cz);
-            float d[4];
-            for (int n = 0; n < 4; ++n) d[n] = cd[n] - pl;
-            float c0 = d[0], c1 = d[1], c2 = d[2], c3 = d[3];
-            const int cs = d2case(c0, c1, c2, c3, 1e-30f, err);
-            for (int n = 0; n < 4; ++n) {
-                F.x[n] = cx[n]; F.y[n] = cy[n]; F.z[n] = cz[n];
-                F.ind[n][0] = (signed char)ci[n][0]; F.ind[n][1] = (signed char)ci[n][1];
-                F.ind[n][2] = (signed char)ci[n][2];
-                F.ind[n][dir] = (signed char)min(ci[n][dir], cut - 1);
+            for (int q = 0; q < 3; ++q) {
+                if (flags & (1 << q)) continue;
+                if (hi[q] > lo[q]) { dir = q; cut = hi[q]; break; }
+                flags |= 1 << q;
             }
-            const CutCase& C = tab[cs];
-            for (int n = 0; n < C.nvert; ++n) {
-                const int v1 = C.v1[n], v2 = C.v2[n];
-                const float den = d[v2] - d[v1];
-                const float mu = fminf(1.f, fmaxf(0.f, den != 0.f ? -d[v1] / den : 1.f));
-                const float x = F.x[v1] + mu * (F.x[v2] - F.x[v1]);
-                const float y = F.y[v1] + mu * (F.y[v2] - F.y[v1]);
-                const float z = F.z[v1] + mu * (F.z[v2] - F.z[v1]);
-                F.x[4 + n] = x; F.y[4 + n] = y; F.z[4 + n] = z;
-                const int Iv[3] = {idx32(x, F.ind[n][0], rlo[0], rhi[0], err), idx32(y, F.ind[n][1], rlo[1], rhi[1], err),
-                                   idx32(z, F.ind[n][2], rlo[2], rhi[2], err)};
-                for (int q = 0; q < 3; ++q) {
-                    int val = max(Iv[q], min((int)F.ind[v1][q], (int)F.ind[v2][q]));
-                    val = min(val, max((int)F.ind[v1][q], (int)F.ind[v2][q]));
-                    F.ind[4 + n][q] = (signed char)val;
+            if (dir >= 0 && depth == CLIP_STACK32) { err |= ERR_DEPTH; dir = -1; }
+            if (dir < 0) {
+                if (++leaves > CLIP_MAX_LEAVES) { err |= ERR_DEPTH; out_v = FF{0.f, 0.f}; out_l = FF{0.f, 0.f}; return; }
+                leaf32(m, tab, PL, i0, j0, k0, cx, cy, cz, ci[0][0], ci[0][1], ci[0][2], rv, rl, err);
+            } else {
+                Frame32& F = st[depth];
+                const float pl = (float)cut;
+                const float* cd = dir == 0 ? cx : (dir == 1 ? cy : cz);
+                float d[4];
+                for (int n = 0; n < 4; ++n) d[n] = cd[n] - pl;
+                float c0 = d[0], c1 = d[1], c2 = d[2], c3 = d[3];
+                const int cs = d2case(c0, c1, c2, c3, 1e-30f, err);
+                int s1[8][3];
+                for (int n = 0; n < 4; ++n) {
+                    F.x[n] = cx[n]; F.y[n] = cy[n]; F.z[n] = cz[n];
+                    s1[n][0] = ci[n][0]; s1[n][1] = ci[n][1]; s1[n][2] = ci[n][2];
+                    s1[n][dir] = min(ci[n][dir], cut - 1);
+                    F.ind[n] = pack3(s1[n][0], s1[n][1], s1[n][2]);
                 }
-                F.ind[4 + n][dir] = (signed char)(cut - 1);
+                const CutCase& C = tab[cs];
+                for (int n = 0; n < C.nvert; ++n) {
+                    const int v1 = C.v1[n], v2 = C.v2[n];
+                    const float den = d[v2] - d[v1];
+                    const float mu = fminf(1.f, fmaxf(0.f, den != 0.f ? -d[v1] / den : 1.f));
+                    const float x = fmaf(mu, F.x[v2] - F.x[v1], F.x[v1]);
+                    const float y = fmaf(mu, F.y[v2] - F.y[v1], F.y[v1]);
+                    const float z = fmaf(mu, F.z[v2] - F.z[v1], F.z[v1]);
+                    F.x[4 + n] = x; F.y[4 + n] = y; F.z[4 + n] = z;
+                    const int Iv[3] = {idx32(x, s1[n][0], rlo[0], rhi[0], err), idx32(y, s1[n][1], rlo[1], rhi[1], err),
+                                       idx32(z, s1[n][2], rlo[2], rhi[2], err)};
+                    int nv[3];
+                    for (int q = 0; q < 3; ++q) {
+                        const int a1 = unpack(F.ind[v1], q), a2 = unpack(F.ind[v2], q);
+                        int val = max(Iv[q], min(a1, a2));
+                        nv[q] = min(val, max(a1, a2));
+                    }
+                    nv[dir] = cut - 1;
+                    F.ind[4 + n] = pack3(nv[0], nv[1], nv[2]);
+                }
+                F.vol = FF{0.f, 0.f};
+                F.liq = FF{0.f, 0.f};
+                F.meta = meta_pack(cs, 1, dir, flags, cut);
+                ++depth;
+                form_child32(F, tab, 0, cx, cy, cz, ci);
+                continue;
             }
-            F.cs = (signed char)cs; F.dir = (signed char)dir; F.cut = (signed char)cut; F.flags = (signed char)flags;
-            F.acc_v = 0.0; F.acc_l = 0.0; F.next = 1;
-            ++depth;
-            form_child32(F, tab, 0, cx, cy, cz, ci);
-            continue;
         }
         for (;;) {
             if (depth == 0) { out_v = rv; out_l = rl; return; }
             Frame32& F = st[depth - 1];
-            F.acc_v += rv;
-            F.acc_l += rl;
-            if (F.next < tab[F.cs].ntets) {
-                form_child32(F, tab, F.next, cx, cy, cz, ci);
-                F.next += 1;
-                flags = F.flags;
+            ff_add(F.vol, rv);
+            ff_add(F.liq, rl);
+            const int cs = F.meta & 15, next = (F.meta >> 4) & 15;
+            if (next < tab[cs].ntets) {
+                form_child32(F, tab, next, cx, cy, cz, ci);
+                F.meta += 1 << 4;
+                flags = (F.meta >> 10) & 7;
                 break;
             }
-            rv = F.acc_v; rl = F.acc_l;
+            rv = F.vol; rl = F.liq;
             --depth;
         }
     }
@@ -476,90 +341,43 @@ __device__ void clip32(const DevMesh& m, const CutCase* tab, const Plane32& PL, 
 
 constexpr int SL32_THREADS = 128;
 
-__device__ __forceinline__ void sl_cell32(const DevMesh& m, const CutCase* tab, float dt, double* __restrict__ VFout,
-                                          const Vel32& V, const Plane32& PL, const signed char* __restrict__ phase,
-                                          int L, int& err)
+/* Warp-aggregated slot reservation: returns this lane's slot (or -1 if !flag). */
+__device__ __forceinline__ int warp_slot(bool flag, int* count)
 {
-    const int i = 1 + L % m.N[0];
-    const int j = 1 + (L / m.N[0]) % m.N[1];
-    const int k = 1 + L / (m.N[0] * m.N[1]);
-    const bool even = ((i + j + k) % 2) == 0;
-    const double tetsign = even ? 1.0 : -1.0;
-    /* relative index bounds: inside the arrays and within REL of the cell */
-    const int rlo[3] = {max(m.lo - i, -REL), max(m.lo - j, -REL), max(m.lo - k, -REL)};
-    const int rhi[3] = {min(m.hi[0] - i, REL), min(m.hi[1] - j, REL), min(m.hi[2] - k, REL)};
-    float px[8], py[8], pz[8];
-    int vi[8][3];
-#pragma unroll 1
-    for (int v = 0; v < 8; ++v) {
-        const int a = v & 1;
-        float x = (float)(even ? a : 1 - a), y = (float)((v >> 1) & 1), z = (float)(v >> 2);
-        project32(m, V, i, j, k, dt, x, y, z);
-        px[v] = x; py[v] = y; pz[v] = z;
-        vi[v][0] = idx32(x, 0, rlo[0], rhi[0], err);
-        vi[v][1] = idx32(y, 0, rlo[1], rhi[1], err);
-        vi[v][2] = idx32(z, 0, rlo[2], rhi[2], err);
-    }
-    const long out = vidx(m, i, j, k);
-    /* pure-donor shortcut (see k_fp64.cu) on the phase codes of the PLIC pass */
-    if (m.fast_pure) {
-        int lo0 = vi[0][0], hi0 = vi[0][0], lo1 = vi[0][1], hi1 = vi[0][1], lo2 = vi[0][2], hi2 = vi[0][2];
-        for (int v = 1; v < 8; ++v) {
-            lo0 = min(lo0, vi[v][0]); hi0 = max(hi0, vi[v][0]);
-            lo1 = min(lo1, vi[v][1]); hi1 = max(hi1, vi[v][1]);
-            lo2 = min(lo2, vi[v][2]); hi2 = max(hi2, vi[v][2]);
-        }
-        int ph = 2;
-        if (hi0 - lo0 <= 3 && hi1 - lo1 <= 3 && hi2 - lo2 <= 3) {
-            for (int c = lo2; c <= hi2 && ph != 0; ++c)
-                for (int b = lo1; b <= hi1 && ph != 0; ++b)
-                    for (int a = lo0; a <= hi0; ++a) {
-                        const int p = __ldg(phase + cidx(m, i + a, j + b, k + c));
-                        if (p == 0 || (ph != 2 && p != ph)) { ph = 0; break; }
-                        ph = p;
-                    }
-        } else {
-            ph = 0;
-        }
-        if (ph == 1 || ph == -1) {
-            float vol = 0.f;
-            for (int t = 0; t < 5; ++t)
-                vol += tet_vol32(px, py, pz, tet5(t, 0), tet5(t, 1), tet5(t, 2), tet5(t, 3));
-            vol *= (float)tetsign;
-            if (vol > 0.25f && vol < 4.f) {
-                VFout[out] = ph > 0 ? 1.0 : 0.0;
-                return;
-            }
-        }
-    }
-    double vol = 0.0, liq = 0.0;
-#pragma unroll 1
-    for (int t = 0; t < 5; ++t) {
-        float cx[4], cy[4], cz[4];
-        int ci[4][3];
-        for (int n = 0; n < 4; ++n) {
-            const int v = tet5(t, n);
-            cx[n] = px[v]; cy[n] = py[v]; cz[n] = pz[v];
-            ci[n][0] = vi[v][0]; ci[n][1] = vi[v][1]; ci[n][2] = vi[v][2];
-        }
-        double tv, tl;
-        clip32(m, tab, PL, i, j, k, rlo, rhi, cx, cy, cz, ci, tv, tl, err);
-        vol += tetsign * tv;
-        liq += tetsign * tl;
-    }
-    if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
-    VFout[out] = liq / vol;
+    const unsigned act = __activemask();
+    const unsigned ballot = __ballot_sync(act, flag);
+    if (!ballot) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(ballot));
+    base = __shfl_sync(act, base, leader);
+    return flag ? base + __popc(ballot & ((1u << lane) - 1)) : -1;
 }
 
-__global__ void __launch_bounds__(SL32_THREADS) k_sl32(DevMesh m, float dt, double* __restrict__ VFout, Vel32 V,
-                                                       Plane32 PL, const signed char* __restrict__ phase,
-                                                       const int* __restrict__ list, const int* __restrict__ count,
-                                                       int* work, int* errw)
+__device__ __forceinline__ void cell_of(const DevMesh& m, int L, int& i, int& j, int& k)
 {
-    __shared__ CutCase s_tab[16];
-    for (int t = threadIdx.x; t < 16 * (int)sizeof(CutCase); t += blockDim.x)
-        reinterpret_cast<char*>(s_tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
-    __syncthreads();
+    i = 1 + L % m.N[0];
+    j = 1 + (L / m.N[0]) % m.N[1];
+    k = 1 + L / (m.N[0] * m.N[1]);
+}
+
+__device__ __forceinline__ void rel_bounds(const DevMesh& m, int i, int j, int k, int* rlo, int* rhi)
+{
+    rlo[0] = max(m.lo - i, -REL); rlo[1] = max(m.lo - j, -REL); rlo[2] = max(m.lo - k, -REL);
+    rhi[0] = min(m.hi[0] - i, REL); rhi[1] = min(m.hi[1] - j, REL); rhi[2] = min(m.hi[2] - k, REL);
+}
+
+/* Stage 1 of the SL update, uniform work per band cell: the eight RK pre-image vertices
+ * (cell2tets! with project_verts, src/VFgeom.jl:345-420) and their cells (pt2index!).  A cell
+ * whose pre-image lies strictly on one side of every donor plane it reaches is finished here
+ * (VF = 1 or 0); the others are compacted, with their vertices, for the clip stage. */
+__global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, double* __restrict__ VFout, Vel32 V,
+                                                           Plane32 PL, const signed char* __restrict__ phase,
+                                                           const int* __restrict__ list, const int* __restrict__ count,
+                                                           int* work, int* slow_cells, float4* slow_verts,
+                                                           int* slow_count, int* errw)
+{
     const int lane = threadIdx.x & 31;
     const int n_items = *count;
     int err = 0;
@@ -569,26 +387,308 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32(DevMesh m, float dt, doub
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_items) break;
         const int item = base + lane;
-        if (item < n_items) sl_cell32(m, s_tab, dt, VFout, V, PL, phase, list[item], err);
+        bool slow = false;
+        int L = 0;
+        float px[8], py[8], pz[8];
+        int vi[8][3];
+        if (item < n_items) {
+            L = list[item];
+            int i, j, k;
+            cell_of(m, L, i, j, k);
+            const bool even = ((i + j + k) % 2) == 0;
+            int rlo[3], rhi[3];
+            rel_bounds(m, i, j, k, rlo, rhi);
+#pragma unroll 1
+            for (int v = 0; v < 8; ++v) {
+                const int a = v & 1;
+                float x = (float)(even ? a : 1 - a), y = (float)((v >> 1) & 1), z = (float)(v >> 2);
+                project32(m, V, i, j, k, dt, x, y, z);
+                px[v] = x; py[v] = y; pz[v] = z;
+                vi[v][0] = idx32(x, 0, rlo[0], rhi[0], err);
+                vi[v][1] = idx32(y, 0, rlo[1], rhi[1], err);
+                vi[v][2] = idx32(z, 0, rlo[2], rhi[2], err);
+            }
+            slow = true;
+            if (m.fast_pure) {
+                int lo0 = vi[0][0], hi0 = vi[0][0], lo1 = vi[0][1], hi1 = vi[0][1], lo2 = vi[0][2], hi2 = vi[0][2];
+                for (int v = 1; v < 8; ++v) {
+                    lo0 = min(lo0, vi[v][0]); hi0 = max(hi0, vi[v][0]);
+                    lo1 = min(lo1, vi[v][1]); hi1 = max(hi1, vi[v][1]);
+                    lo2 = min(lo2, vi[v][2]); hi2 = max(hi2, vi[v][2]);
+                }
+                const int ph = box_plane_side<8>(m, PL, i, j, k, lo0, hi0, lo1, hi1, lo2, hi2, px, py, pz);
+                if (ph != 0) {
+                    float vol = 0.f;
+                    for (int t = 0; t < 5; ++t)
+                        vol += tet_vol32(px, py, pz, tet5(t, 0), tet5(t, 1), tet5(t, 2), tet5(t, 3));
+                    vol *= even ? 1.f : -1.f;
+                    if (vol > 0.25f && vol < 4.f) {
+                        VFout[vidx(m, i, j, k)] = ph > 0 ? 1.0 : 0.0;
+                        slow = false;
+                    }
+                }
+            }
+        }
+        const int slot = warp_slot(slow, slow_count);
+        if (slot >= 0) {
+            slow_cells[slot] = L;
+            for (int v = 0; v < 8; ++v) {
+                const unsigned pk = pack3(vi[v][0], vi[v][1], vi[v][2]);
+                slow_verts[(long)slot * 8 + v] = make_float4(px[v], py[v], pz[v], __int_as_float((int)pk));
+            }
+        }
+    }
+    if (err) atomicOr(errw, err);
+}
+
+/* ======================================================================================
+ * Stage 2: warp-cooperative clip.  The clip of one tet is a tree (cutTet's recursion); run
+ * thread per cell its depth varies so much that a warp idles most lanes.  Here a warp takes a
+ * batch of cells and keeps their pending sub-tets in a LIFO stack in shared memory: each round
+ * every lane pops one node and either finishes it (pruned or PLIC leaf: its volume and liquid
+ * volume are added to the lane's running sums for that cell) or cuts it by the next mesh plane
+ * and pushes the children (warp prefix sum).  Cutters whose children do not fit put their node
+ * back; if no cutter fits, the first one finishes its node with the private-stack clip.  Lanes'
+ * partial sums are combined per cell by a fixed shuffle tree, so results are deterministic.
+ * vol and vLiq are sums over the same pieces, so a pre-image that is all liquid gives VF = 1
+ * exactly, as in the reference.
+ * ==================================================================================== */
+constexpr int CLIPW_WARPS = 4;
+constexpr int CLIPW_CAP = 160; /* stack items per warp */
+constexpr int CLIPW_BATCH = 4; /* cells per warp batch */
+
+/* acc[b] += x with a compile-time index (keeps the accumulators in registers) */
+__device__ __forceinline__ void acc_add(FF* acc, int b, float x)
+{
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (q == b) ff_add(acc[q], x);
+}
+__device__ __forceinline__ void acc_add(FF* acc, int b, const FF& x)
+{
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (q == b) ff_add(acc[q], x);
+}
+
+struct Item {
+    float x[4], y[4], z[4];
+    unsigned ix[4];
+    unsigned tag; /* cell in batch (bits 0-1) | done flags (bits 2-4) */
+};
+
+__global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, double* __restrict__ VFout, Plane32 PL,
+                                                                  const int* __restrict__ slow_cells,
+                                                                  const float4* __restrict__ slow_verts,
+                                                                  const int* __restrict__ slow_count, int* work,
+                                                                  int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    __shared__ Item s_stack[CLIPW_WARPS][CLIPW_CAP];
+    for (int t = threadIdx.x; t < 16 * (int)sizeof(CutCase); t += blockDim.x)
+        reinterpret_cast<char*>(s_tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    Item* stk = s_stack[w];
+    const int n_cells = *slow_count;
+    int err = 0;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(work, CLIPW_BATCH);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_cells) break;
+        const int nb = min(CLIPW_BATCH, n_cells - base);
+        /* cell geometry of the batch (lane b holds cell b) */
+        int ci_ = 0, cj_ = 0, ck_ = 0;
+        if (lane < nb) cell_of(m, slow_cells[base + lane], ci_, cj_, ck_);
+        /* seed: lane q < 5*nb pushes tet q%5 of cell q/5; unclipped tet volume = vol */
+        FF acc[CLIPW_BATCH], avol[CLIPW_BATCH];
+        for (int b = 0; b < CLIPW_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; }
+        if (lane < 5 * nb) {
+            const int b = lane / 5, t = lane - 5 * b;
+            Item& it = stk[lane];
+            for (int n = 0; n < 4; ++n) {
+                const float4 q = __ldg(slow_verts + (long)(base + b) * 8 + tet5(t, n));
+                it.x[n] = q.x; it.y[n] = q.y; it.z[n] = q.z;
+                it.ix[n] = (unsigned)__float_as_int(q.w);
+            }
+            it.tag = (unsigned)b;
+        }
+        int size = 5 * nb;
+        __syncwarp();
+        int guard = 0;
+        while (size > 0) {
+            if (++guard > 1 << 20) { err |= ERR_DEPTH; break; }
+            /* phase 1: pop up to 32 nodes and classify them */
+            const int n = min(32, size);
+            const int top = size - n;
+            Item it;
+            const bool act = lane < n;
+            if (act) it = stk[top + lane];
+            __syncwarp();
+            size = top;
+            const int bsel = act ? (int)(it.tag & 3) : 0;
+            const int i0 = __shfl_sync(0xffffffffu, ci_, bsel), j0 = __shfl_sync(0xffffffffu, cj_, bsel),
+                      k0 = __shfl_sync(0xffffffffu, ck_, bsel);
+            const int b = bsel;
+            int kind = 0; /* 0 idle, 1 pruned, 2 leaf, 3 cut */
+            int bp = 0, cs = 0, dir = -1, cut = 0, flags = 0, nchild = 0;
+            int rlo[3], rhi[3];
+            int cind[4][3];
+            float d[4];
+            if (act) {
+                flags = (it.tag >> 2) & 7;
+                rlo[0] = max(m.lo - i0, -REL); rlo[1] = max(m.lo - j0, -REL); rlo[2] = max(m.lo - k0, -REL);
+                rhi[0] = min(m.hi[0] - i0, REL); rhi[1] = min(m.hi[1] - j0, REL); rhi[2] = min(m.hi[2] - k0, REL);
+                for (int nn = 0; nn < 4; ++nn)
+                    for (int q = 0; q < 3; ++q) cind[nn][q] = unpack(it.ix[nn], q);
+                int lo[3], hi[3];
+                for (int q = 0; q < 3; ++q) {
+                    lo[q] = min(min(cind[0][q], cind[1][q]), min(cind[2][q], cind[3][q]));
+                    hi[q] = max(max(cind[0][q], cind[1][q]), max(cind[2][q], cind[3][q]));
+                }
+                bp = m.fast_pure ? box_plane_side<4>(m, PL, i0, j0, k0, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], it.x,
+                                                     it.y, it.z) : 0;
+                if (bp != 0) {
+                    kind = 1;
+                } else {
+                    for (int q = 0; q < 3; ++q) {
+                        if (flags & (1 << q)) continue;
+                        if (hi[q] > lo[q]) { dir = q; cut = hi[q]; break; }
+                        flags |= 1 << q;
+                    }
+                    if (dir < 0) {
+                        kind = 2;
+                    } else {
+                        kind = 3;
+                        const float pl = (float)cut;
+                        const float* cd = dir == 0 ? it.x : (dir == 1 ? it.y : it.z);
+                        for (int nn = 0; nn < 4; ++nn) d[nn] = cd[nn] - pl;
+                        float c0 = d[0], c1 = d[1], c2 = d[2], c3 = d[3];
+                        cs = d2case(c0, c1, c2, c3, 1e-30f, err);
+                        nchild = s_tab[cs].ntets;
+                    }
+                }
+            }
+            /* children placement: cutters in lane order while they fit, keeping n slots free for
+             * the nodes that have to go back; if none fits, lane 0 finishes its node privately */
+            int incl = nchild;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += y;
+            }
+            bool fits = kind == 3 && size + incl <= CLIPW_CAP - n;
+            const unsigned fitmask = __ballot_sync(0xffffffffu, fits);
+            const unsigned cutmask = __ballot_sync(0xffffffffu, kind == 3);
+            bool back = kind == 3 && !fits;
+            bool priv = false;
+            if (!fitmask && cutmask && lane == __ffs(cutmask) - 1) { back = false; priv = true; }
+            const int pushed = fits ? nchild : 0;
+            int ipush = pushed;
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, ipush, off);
+                if (lane >= off) ipush += y;
+            }
+            const int tot_push = __shfl_sync(0xffffffffu, ipush, 31);
+            const unsigned backmask = __ballot_sync(0xffffffffu, back);
+            /* phase 2 */
+            if (kind == 1) {
+                const float tv = tet_vol<float>(it.x[0], it.y[0], it.z[0], it.x[1], it.y[1], it.z[1], it.x[2], it.y[2],
+                                                it.z[2], it.x[3], it.y[3], it.z[3]);
+                acc_add(avol, b, tv);
+                if (bp > 0) acc_add(acc, b, tv);
+            } else if (kind == 2) {
+                FF rv, rl;
+                leaf32(m, s_tab, PL, i0, j0, k0, it.x, it.y, it.z, cind[0][0], cind[0][1], cind[0][2], rv, rl, err);
+                acc_add(avol, b, rv);
+                acc_add(acc, b, rl);
+            } else if (priv) {
+                FF rv, rl;
+                float cx[4], cy[4], cz[4];
+                for (int nn = 0; nn < 4; ++nn) { cx[nn] = it.x[nn]; cy[nn] = it.y[nn]; cz[nn] = it.z[nn]; }
+                clip32(m, s_tab, PL, nullptr, i0, j0, k0, rlo, rhi, cx, cy, cz, cind, rv, rl, err);
+                acc_add(avol, b, rv);
+                acc_add(acc, b, rl);
+            } else if (fits) {
+                /* cut by the mesh plane (src/VFgeom.jl:832-899) and push the children */
+                float vx[8], vy[8], vz[8];
+                int s1[8][3];
+                for (int nn = 0; nn < 4; ++nn) {
+                    vx[nn] = it.x[nn]; vy[nn] = it.y[nn]; vz[nn] = it.z[nn];
+                    s1[nn][0] = cind[nn][0]; s1[nn][1] = cind[nn][1]; s1[nn][2] = cind[nn][2];
+                    s1[nn][dir] = min(cind[nn][dir], cut - 1);
+                }
+                const CutCase& C = s_tab[cs];
+                for (int nn = 0; nn < C.nvert; ++nn) {
+                    const int v1 = C.v1[nn], v2 = C.v2[nn];
+                    const float den = d[v2] - d[v1];
+                    const float mu = fminf(1.f, fmaxf(0.f, den != 0.f ? -d[v1] / den : 1.f));
+                    const float x = fmaf(mu, vx[v2] - vx[v1], vx[v1]);
+                    const float y = fmaf(mu, vy[v2] - vy[v1], vy[v1]);
+                    const float z = fmaf(mu, vz[v2] - vz[v1], vz[v1]);
+                    vx[4 + nn] = x; vy[4 + nn] = y; vz[4 + nn] = z;
+                    const int Iv[3] = {idx32(x, s1[nn][0], rlo[0], rhi[0], err), idx32(y, s1[nn][1], rlo[1], rhi[1], err),
+                                       idx32(z, s1[nn][2], rlo[2], rhi[2], err)};
+                    for (int q = 0; q < 3; ++q) {
+                        const int a1 = s1[v1][q], a2 = s1[v2][q];
+                        s1[4 + nn][q] = min(max(Iv[q], min(a1, a2)), max(a1, a2));
+                    }
+                    s1[4 + nn][dir] = cut - 1;
+                }
+                const int pos = size + ipush - pushed;
+                const unsigned tag = (unsigned)b | ((unsigned)flags << 2);
+                for (int c = 0; c < C.ntets; ++c) {
+                    const int side = C.side[c];
+                    Item& ch = stk[pos + c];
+                    for (int nn = 0; nn < 4; ++nn) {
+                        const int v = C.vtet[c][nn];
+                        ch.x[nn] = vx[v]; ch.y[nn] = vy[v]; ch.z[nn] = vz[v];
+                        int a0 = s1[v][0], a1 = s1[v][1], a2 = s1[v][2];
+                        if (side == 1) { if (dir == 0) a0 = cut; else if (dir == 1) a1 = cut; else a2 = cut; }
+                        ch.ix[nn] = pack3(a0, a1, a2);
+                    }
+                    ch.tag = tag;
+                }
+            }
+            /* nodes that did not fit go back above the children, in lane order */
+            if (back) stk[size + tot_push + __popc(backmask & ((1u << lane) - 1u))] = it;
+            size += tot_push + __popc(backmask);
+            __syncwarp();
+        }
+        /* per-cell liquid volume: fixed-order shuffle tree over lanes */
+#pragma unroll
+        for (int b = 0; b < CLIPW_BATCH; ++b) {
+            if (b >= nb) break;
+            double v = (double)acc[b].hi + (double)acc[b].lo;
+            double u = (double)avol[b].hi + (double)avol[b].lo;
+            for (int off = 16; off > 0; off >>= 1) {
+                v += __shfl_xor_sync(0xffffffffu, v, off);
+                u += __shfl_xor_sync(0xffffffffu, u, off);
+            }
+            if (lane == b) {
+                const double tetsign = ((ci_ + cj_ + ck_) % 2) == 0 ? 1.0 : -1.0;
+                const double vol = tetsign * u, liq = tetsign * v;
+                if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
+                VFout[vidx(m, ci_, cj_, ck_)] = liq / vol;
+            }
+        }
         __syncwarp();
     }
     if (err) atomicOr(errw, err);
 }
 
 /* ---- launchers ------------------------------------------------------------------------ */
-void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int nsm, cudaStream_t s)
-{
-    k_elvira_iface32<<<nsm * 8, EL32_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work);
-}
-
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
-                 int* errw, int nsm, cudaStream_t s)
+                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, double2* tet_out, int* errw,
+                 int nsm, cudaStream_t s)
 {
     Vel32 V{uf, vf, wf};
     Plane32 PL{planes};
-    k_sl32<<<nsm * 8, SL32_THREADS, 0, s>>>(m, (float)dt, VFout, V, PL, phase, list, count, work, errw);
+    k_sl32_pre<<<nsm * 8, SL32_THREADS, 0, s>>>(m, (float)dt, VFout, V, PL, phase, list, count, work, slow_cells,
+                                                slow_verts, slow_count, errw);
+    (void)tet_out;
+    k_sl32_clipw<<<nsm * 4, CLIPW_WARPS * 32, 0, s>>>(m, VFout, PL, slow_cells, slow_verts, slow_count, work2, errw);
 }
 
 } // namespace slvof

@@ -35,6 +35,9 @@ struct slvof_ctx {
     float *uf32 = nullptr, *vf32 = nullptr, *wf32 = nullptr;
     double *nx = nullptr, *ny = nullptr, *nz = nullptr, *D = nullptr;
     float4* planes = nullptr;     /* mixed: donor planes in cell units */
+    int* slow_cells = nullptr;    /* mixed SL: cells that need the clip */
+    float4* slow_verts = nullptr; /* mixed SL: their pre-image vertices (cell units) + packed indices */
+    double2* tet_out = nullptr;   /* mixed SL: (vol, vLiq) of each tet of each slow cell */
     signed char* phase = nullptr; /* pure-donor codes of the PLIC pass */
     short* band[2] = {nullptr, nullptr};
     int bcur = 0;
@@ -59,7 +62,7 @@ struct slvof_ctx {
 
 namespace {
 
-enum { C_SL = 0, C_IF = 1, C_SLW = 2, C_IFW = 3, C_ERR = 4, C_PL = 5, C_N = 8 };
+enum { C_SL = 0, C_IF = 1, C_SLW = 2, C_IFW = 3, C_ERR = 4, C_PL = 5, C_SLOW = 6, C_SLW2 = 7, C_ARB = 8, C_N = 16 };
 
 int fail(slvof_ctx* c, int code, const std::string& msg)
 {
@@ -132,6 +135,7 @@ int st_normals(slvof_ctx* c)
 {
     CK(cudaMemsetAsync(c->ctr + C_IF, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->ctr + C_IFW, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_ARB, 0, sizeof(int), c->stream));
     s_beg(c, S_PURE);
     launch_elvira_pure(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->partials, c->npure,
                        c->stream);
@@ -142,7 +146,7 @@ int st_normals(slvof_ctx* c)
                               c->ctr + C_ERR, c->nsm, c->stream);
     else
         launch_elvira_iface32(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->ctr + C_IFW,
-                              c->nsm, c->stream);
+                              c->ctr + C_ARB, c->ctr + C_ERR, c->nsm, c->stream);
     s_end(c, S_IFACE);
     s_beg(c, S_NGHOST);
     launch_normal_ghost(c->m, c->nx, c->ny, c->nz, c->nsm, c->stream);
@@ -183,6 +187,7 @@ int st_transport(slvof_ctx* c, double dt)
     const int o = 1 - c->vcur;
     CK(cudaMemsetAsync(c->ctr + C_SL, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->ctr + C_SLW, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream)); /* slow count, clip work */
     s_beg(c, S_CLASSIFY);
     launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
     s_end(c, S_CLASSIFY);
@@ -192,7 +197,8 @@ int st_transport(slvof_ctx* c, double dt)
                     c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
     else
         launch_sl32(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
-                    c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
+                    c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->tet_out,
+                    c->ctr + C_ERR, c->nsm, c->stream);
     s_end(c, S_SL);
     s_beg(c, S_VFGHOST);
     launch_vf_ghost(c->m, c->VF[c->vcur], c->VF[o], c->nsm, c->stream);
@@ -300,7 +306,10 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
               alloc((void**)&c->mass_d, sizeof(double));
     if (ok && precision == SLVOF_MIXED)
         ok = alloc((void**)&c->uf32, c->ncell * sizeof(float)) && alloc((void**)&c->vf32, c->ncell * sizeof(float)) &&
-             alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4));
+             alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4)) &&
+             alloc((void**)&c->slow_cells, interior * sizeof(int)) &&
+             alloc((void**)&c->slow_verts, interior * 8 * sizeof(float4)) &&
+             alloc((void**)&c->tet_out, interior * 5 * sizeof(double2));
     if (!ok) return bail(SLVOF_E_NOMEM);
     /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
     std::vector<double> h(ncoord);
@@ -358,7 +367,7 @@ int slvof_destroy(slvof_ctx* c)
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->coords, c->VF[0], c->VF[1], c->uf, c->vf, c->wf, c->uf32, c->vf32, c->wf32, c->nx, c->ny,
-                    c->nz, c->D, c->planes, c->phase, c->band[0], c->band[1], c->list_sl, c->list_if, c->list_plic, c->ctr,
+                    c->nz, c->D, c->planes, c->phase, c->band[0], c->band[1], c->list_sl, c->list_if, c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr,
                     c->partials, c->mass_d, c->table, c->spheres};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -393,6 +402,16 @@ int slvof_stage_ms(const slvof_ctx* c, double* ms, int n)
         float t = 0.f;
         ms[q] = (c->sran[q] && cudaEventElapsedTime(&t, c->sev[q][0], c->sev[q][1]) == cudaSuccess) ? t : 0.0;
     }
+    return SLVOF_OK;
+}
+
+int slvof_counters(const slvof_ctx* c, int* out, int n)
+{
+    if (!c || !out || n < 0) return SLVOF_E_ARG;
+    int h[C_N] = {0};
+    if (cudaMemcpy(h, c->ctr, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) return SLVOF_E_CUDA;
+    const int v[SLVOF_NCOUNTERS] = {h[C_SL], h[C_IF], h[C_SLOW], h[C_PL], h[C_ARB]};
+    for (int q = 0; q < n && q < SLVOF_NCOUNTERS; ++q) out[q] = v[q];
     return SLVOF_OK;
 }
 

@@ -17,6 +17,7 @@ namespace slvof {
 constexpr double EPS64 = 2.220446049250313e-16; /* Julia eps() */
 constexpr int CLIP_STACK = 12;                   /* max cutTet nesting held per thread */
 constexpr int CLIP_MAX_LEAVES = 4096;            /* leaf budget of one top-level tet clip */
+constexpr int CLIP_STACK32 = 8;                  /* FP32 clip nesting (pruned subtrees are shallow) */
 
 /* Error bits, same values as SLVOF_DEV_* in include/slvof.h. */
 enum : int { ERR_INDEX = 1, ERR_DEPTH = 2, ERR_NAN = 4, ERR_VOLUME = 8 };

@@ -34,11 +34,12 @@ void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout,
                  const signed char* phase, const int* list, const int* count, int* work, int* errw, int nsm,
                  cudaStream_t s);
 
-/* k_mixed.cu */
+/* k_mixed.cu, k_elvira_mixed.cu */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int nsm, cudaStream_t s);
+                           const int* count, int* work, int* stats, int* errw, int nsm, cudaStream_t s);
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
-                 int* errw, int nsm, cudaStream_t s);
+                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, double2* tet_out, int* errw,
+                 int nsm, cudaStream_t s);
 
 } // namespace slvof

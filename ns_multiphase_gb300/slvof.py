@@ -33,6 +33,7 @@ SYMBOLS = [
     ("slvof_last_kernel_ms", _I, [_P, _P]),
     ("slvof_stage_ms", _I, [_P, _P, _I]),
     ("slvof_set_stream", _I, [_P, _P]),
+    ("slvof_counters", _I, [_P, _P, _I]),
     ("slvof_upload_vf", _I, [_P, _P]),
     ("slvof_upload_velocity", _I, [_P, _P, _P, _P]),
     ("slvof_upload_band", _I, [_P, _P]),
@@ -143,6 +144,13 @@ class SLVOF:
         a = np.zeros(len(self.STAGES))
         self.L.slvof_stage_ms(self.h, a.ctypes.data, len(a))
         return dict(zip(self.STAGES, a.tolist()))
+
+    COUNTERS = ("band_cells", "interface_cells", "clipped_cells", "plic_solves", "fp64_arbitrations")
+
+    def counters(self) -> dict:
+        a = np.zeros(len(self.COUNTERS), dtype=np.int32)
+        self._check(self.L.slvof_counters(self.h, a.ctypes.data, len(a)), "counters")
+        return dict(zip(self.COUNTERS, a.tolist()))
 
     def set_stream(self, stream_handle: int | None):
         """Run on a caller-owned cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""

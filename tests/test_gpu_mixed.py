@@ -2,9 +2,15 @@
 volume sums and mass) against the FP64 path and against exact planar transport.
 
 Tolerances: a plane carried by a uniform velocity must come out within 2e-6 of the exact
-fraction (FP32 geometry in cell units); over short deformation runs the total volume must
-agree with the FP64 path to 1e-9 relative and per-cell VF to 5e-3 (cells where FP32 errors
-pick a different ELVIRA candidate than FP64 differ by the two planes' donated volumes).
+fraction (FP32 geometry in cell units).  ELVIRA's FP32 candidate errors are arbitrated in FP64
+wherever two candidates are within rounding of each other, so the chosen normals must equal
+the FP64 path's in at least 99.5% of interface cells.  Over short deformation runs every cell
+must stay within 5e-3 of the FP64 path, and 99% of the interface cells within 1e-5 except for
+the sphere centred at (0.35,0.35,0.35): on a uniform grid its three mirror planes hold exact
+FP64 ties between mirror candidates, which the ~1e-7 VF differences of the FP32 transport can
+break the other way.  The total volume must agree within
+1e-6 * cell volume * sqrt(steps * interface cells) (FP32 vertex positions carry ~1e-7 of a
+cell, with independent signs from cell to cell).
 """
 import numpy as np
 import pytest
@@ -62,8 +68,7 @@ def test_mixed_uniform_translation_of_plane():
     assert worst <= 2e-6, worst
 
 
-@pytest.mark.parametrize("shape", ["sphere3d", "spheres3d", "vortex2d"])
-def test_mixed_tracks_fp64(shape):
+def case(shape):
     if shape == "vortex2d":
         m = Mesh(Nx=48, Ny=48, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / 48, CFL=0.5, zper=True)
         VF = cases.vf_spheres(m, [[0.5, 0.75, 0.0]], [0.15], nF=10, dims=2)
@@ -78,16 +83,45 @@ def test_mixed_tracks_fp64(shape):
             VF = cases.vf_spheres(m, c, 2.5 * r, nF=8)
         vel = lambda t: cases.deformation3d_faces(m, t, 3.0)
         dt = 0.5 * m.dx / 2.0
+    return m, VF, vel, dt
+
+
+@pytest.mark.parametrize("shape", ["sphere3d", "spheres3d", "vortex2d"])
+def test_mixed_normals_match_fp64(shape):
+    m, VF, vel, dt = case(shape)
+    g64, g32 = make(m, VF, "fp64"), make(m, VF, "mixed")
+    a, b = g64.download_normals(), g32.download_normals()
+    V = m.interior(g64.download_vf())
+    iface = (V >= 1e-10) & (V <= 1 - 1e-10)
+    same = np.ones(iface.shape, bool)
+    for p, q in zip(a, b):
+        same &= m.interior(p) == m.interior(q)
+    frac = same[iface].mean()
+    assert frac >= 0.995, frac
+
+
+@pytest.mark.parametrize("shape", ["sphere3d", "spheres3d", "vortex2d"])
+def test_mixed_tracks_fp64(shape):
+    m, VF, vel, dt = case(shape)
     g64, g32 = make(m, VF, "fp64"), make(m, VF, "mixed")
     t = 0.0
-    for s in range(10):
+    n_if = 0
+    steps = 10
+    for s in range(steps):
         uf, vf, wf = vel(t + 0.5 * dt)
         g64.upload_velocity(uf, vf, wf)
         g32.upload_velocity(uf, vf, wf)
         M64 = g64.step(dt)
         M32 = g32.step(dt)
         t += dt
+        V = m.interior(g64.download_vf())
+        n_if += int(((V >= 1e-10) & (V <= 1 - 1e-10)).sum())
     V64, V32 = m.interior(g64.download_vf()), m.interior(g32.download_vf())
-    assert abs(M32 - M64) <= 1e-9 * M64, (M32, M64)
-    assert np.max(np.abs(V64 - V32)) <= 5e-3
+    cv = m.dx * m.dy * m.dz
+    d = np.abs(V64 - V32)
+    iface = (V64 >= 1e-10) & (V64 <= 1 - 1e-10)
+    assert abs(M32 - M64) <= 1e-6 * cv * np.sqrt(n_if), (M32, M64, abs(M32 - M64) / M64)
+    if shape != "sphere3d":
+        assert float(np.percentile(d[iface], 99)) <= 1e-5, float(np.percentile(d[iface], 99))
+    assert float(d.max()) <= 5e-3, float(d.max())
     assert V32.min() >= -1e-6 and V32.max() <= 1 + 1e-6
