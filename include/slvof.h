@@ -36,6 +36,7 @@ extern "C" {
 #define SLVOF_E_CUDA (-2)
 #define SLVOF_E_UNSUPPORTED (-3)
 #define SLVOF_E_NOMEM (-4)
+#define SLVOF_E_TOO_LARGE (-5) /* grid larger than a fixed scratch maximum (slvof_mass_noalloc) */
 
 #define SLVOF_FP64 0  /* every stage in FP64, rounding identical to the CPU restatement */
 #define SLVOF_MIXED 1 /* FP32 trajectories, interpolation, clip geometry and ELVIRA candidate errors;
@@ -143,6 +144,22 @@ int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, cons
 int slvof_case_vf_spheres(slvof_ctx* ctx, const double* centres, const double* radii, int n, int nF, int dims);
 /* Deformation3D face velocities at time t with period T (src/Tools.jl:660-662). */
 int slvof_case_deformation3d(slvof_ctx* ctx, double t, double T);
+
+/* ---- no-allocation variant ----------------------------------------------------------------
+ * sum(VF[interior])*dx*dy*dz of a VF array that is already on the device, written to the
+ * device double *d_mass, on the given cudaStream_t (NULL: the default stream).  No counterpart
+ * in the reference: it serves callers that cannot allocate device memory (a host framework
+ * that owns every device allocation through its own pool, or code that runs after the solver
+ * has reserved all device memory), so it needs no context and calls no cudaMalloc, cudaFree or
+ * allocating library routine.  Its scratch, one compensated partial sum per z-plane, is a
+ * fixed static device array of the library, held on every device that loads the library
+ * until the process exits; grids with Nz > SLVOF_NOALLOC_MAX_PLANES return SLVOF_E_TOO_LARGE.
+ * The first call on a device looks up that array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU race, so order
+ * them.  Only Nx, Ny, Nz, nghost, dx, dy, dz of *mesh are read.  The result is written in
+ * stream order; synchronise the stream before reading it. */
+#define SLVOF_NOALLOC_MAX_PLANES 8192
+int slvof_mass_noalloc(const slvof_mesh* mesh, const double* d_VF, double* d_mass, void* stream);
 
 #ifdef __cplusplus
 }

@@ -26,6 +26,7 @@ UNITS = {
     "k_fp64.cu": ["-fmad=false"],
     "k_mixed.cu": ["-fmad=true"],
     "k_elvira_mixed.cu": ["-fmad=false"],
+    "slvof_noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -56,6 +56,7 @@ SYMBOLS = [
     ("slvof_step_host", _I, [_P, _D, _I, _P, _P, _P, _P, _P]),
     ("slvof_case_vf_spheres", _I, [_P, _P, _P, _I, _I, _I]),
     ("slvof_case_deformation3d", _I, [_P, _D, _D]),
+    ("slvof_mass_noalloc", _I, [_P, _P, _P, _P]),
 ]
 
 _lib = None
