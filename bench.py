@@ -236,6 +236,7 @@ def main():
     with Clocks(local) as ck:
         ms, stage = timed_steps(g, dt, args.steps, torch)
     clocks = ck.summary()
+    counters = g.counters()
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
@@ -310,13 +311,16 @@ def main():
             pass
         hbm = peaks.get("hbm_gbs", 6800.0)
         dom = max(stage, key=stage.get)
-        alg = algorithmic_bytes(m, dom)
+        alg = algorithmic_bytes(m, dom, counters)
         achieved = alg / (stage[dom] / 1e3) / 1e9 if stage[dom] > 0 else 0.0
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": profiled_traffic(dom),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "algorithmic_bytes": alg, "kernel_ms": stage[dom],
-                "note": "ALU-bound (FP32 pipe); HBM fraction is reported per the contract"}
+                "note": "sl_update = k_sl32_pre + k_sl32_clipw; branch- and latency-bound (see profiles/), "
+                        "the HBM fraction is reported per the contract",
+                "step": {"algorithmic_bytes": 28 * cells, "achieved_gbs": 28 * cells / (ms_step / 1e3) / 1e9,
+                         "frac": 28 * cells / (ms_step / 1e3) / 1e9 / hbm}}
         out = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
@@ -328,7 +332,7 @@ def main():
                         "stages_ms": stage64},
                "accuracy": {"steps": args.drift_steps, "mass_rel_diff_mixed_vs_fp64": drift_vs_fp64,
                             "max_abs_dVF_mixed_vs_fp64": dVF, "mass_rel_change_fp64": abs(m64 - M0) / M0},
-               "stages_ms": stage, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+               "stages_ms": stage, "work_lists": counters, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": launches_per_step(m) * args.steps}
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -336,18 +340,21 @@ def main():
         tdist.destroy_process_group()
 
 
-def algorithmic_bytes(m, stage):
-    """Minimum unique HBM bytes of one launch of a stage (mixed precision storage)."""
+def algorithmic_bytes(m, stage, ctr):
+    """Minimum unique HBM bytes of one launch of a stage (mixed-precision storage), from the
+    work-list sizes of the step: each band cell of the SL update reads its FP32 face velocities
+    (12 B) and donor plane (16 B) and writes VF (8 B); each ELVIRA interface cell reads VF and
+    writes three normals (32 B)."""
     interior = m.Nx * m.Ny * m.Nz
     ncell = int(np.prod(m.cell_shape))
     table = {
         "sl_classify": interior * (2 + 8 + 8),
-        "sl_update": interior * (12 + 16 + 8),      # FP32 velocities + donor planes + VF, upper bound
+        "sl_update": ctr.get("band_cells", interior) * (12 + 16 + 8),
         "vf_ghost": (int(np.prod(m.vf_shape)) - interior) * 16,
         "elvira_pure": interior * (8 + 24),
-        "elvira_candidates": interior * (8 + 24),   # upper bound: VF block + normals of listed cells
+        "elvira_candidates": ctr.get("interface_cells", interior) * (8 + 24),
         "normal_ghost": (ncell - interior) * 24,
-        "plic": ncell * (8 * 5 + 16 + 1),
+        "plic": ncell * (8 * 4 + 8 + 16 + 1),
         "band": interior * (8 + 2 * 2 * 2),
         "mass": 8 * 1024,
     }
