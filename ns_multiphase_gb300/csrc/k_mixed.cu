@@ -445,37 +445,89 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
  * Stage 2: warp-cooperative clip.  The clip of one tet is a tree (cutTet's recursion); run
  * thread per cell its depth varies so much that a warp idles most lanes.  Here a warp takes a
  * batch of cells and keeps their pending sub-tets in a LIFO stack in shared memory: each round
- * every lane pops one node and either finishes it (pruned or PLIC leaf: its volume and liquid
- * volume are added to the lane's running sums for that cell) or cuts it by the next mesh plane
- * and pushes the children (warp prefix sum).  Cutters whose children do not fit put their node
- * back; if no cutter fits, the first one finishes its node with the private-stack clip.  Lanes'
- * partial sums are combined per cell by a fixed shuffle tree, so results are deterministic.
- * vol and vLiq are sums over the same pieces, so a pre-image that is all liquid gives VF = 1
- * exactly, as in the reference.
+ * every lane pops one node and classifies it —
+ *   pruned: strictly on one side of every donor plane of its index box (one leaf, no cuts),
+ *   leaf:   one donor cell left, cut by that donor's PLIC plane,
+ *   cut:    split by the next mesh plane, children pushed (warp prefix sum) —
+ * and all three then run one code path: distances to a plane, d2case, new vertices on the
+ * cut edges, then per child tet either its volume (leaf; liquid when on the plane's negative
+ * side) or a push.  A pruned node is the one-tet case 1 (all liquid) or 16 (all gas).
+ * Cutters whose children do not fit put their node back; if no cutter fits, the first one
+ * finishes its node with the private-stack clip.  Lanes' partial sums are combined per cell
+ * by a fixed shuffle tree, so results are deterministic.  vol and vLiq are sums over the same
+ * pieces, so a pre-image that is all liquid gives VF = 1 exactly, as in the reference.
+ *
+ * Shared memory per warp: the node stack as four arrays of float4 (x, y, z, packed donor
+ * indices), one per vertex, so a warp's pops and pushes hit consecutive 16-byte words; the
+ * eight vertices of each lane's current cut (vertex-major, lane fastest); and the donor
+ * planes of the 3x3x3 neighbourhood of each batch cell, which covers every donor a pre-image
+ * reaches at CFL <= 0.5 (farther donors are read from global memory).
  * ==================================================================================== */
 constexpr int CLIPW_WARPS = 4;
-constexpr int CLIPW_CAP = 160; /* stack items per warp */
-constexpr int CLIPW_BATCH = 4; /* cells per warp batch */
+constexpr int CLIPW_CAP = 112;  /* stack nodes per warp */
+constexpr int CLIPW_BATCH = 4;  /* cells per warp batch */
+constexpr int CLIPW_NBR = 27;   /* cached donor planes per batch cell */
 
 /* acc[b] += x with a compile-time index (keeps the accumulators in registers) */
 __device__ __forceinline__ void acc_add(FF* acc, int b, float x)
 {
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < CLIPW_BATCH; ++q)
         if (q == b) ff_add(acc[q], x);
 }
 __device__ __forceinline__ void acc_add(FF* acc, int b, const FF& x)
 {
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < CLIPW_BATCH; ++q)
         if (q == b) ff_add(acc[q], x);
 }
 
-struct Item {
-    float x[4], y[4], z[4];
-    unsigned ix[4];
-    unsigned tag; /* cell in batch (bits 0-1) | done flags (bits 2-4) */
+struct ClipShared {
+    CutCase tab[16];
+    float4 stk[CLIPW_WARPS][4][CLIPW_CAP];
+    float4 scr[8][CLIPW_WARPS * 32];
+    float4 pl[CLIPW_WARPS][CLIPW_BATCH][CLIPW_NBR];
 };
+
+__device__ __forceinline__ unsigned wbits(const float4& v) { return (unsigned)__float_as_int(v.w); }
+__device__ __forceinline__ float sel4(float a, float b, float c, float d, int i)
+{
+    return i == 0 ? a : (i == 1 ? b : (i == 2 ? c : d));
+}
+
+/* Donor plane at index offset (a, b, c) from the batch cell (i0, j0, k0). */
+__device__ __forceinline__ float4 nbr_plane(const DevMesh& m, const Plane32& PL, const float4* cache, int i0, int j0,
+                                            int k0, int a, int b, int c)
+{
+    if ((unsigned)(a + 1) <= 2u && (unsigned)(b + 1) <= 2u && (unsigned)(c + 1) <= 2u)
+        return cache[(c + 1) * 9 + (b + 1) * 3 + (a + 1)];
+    return __ldg(PL.P + cidx(m, i0 + a, j0 + b, k0 + c));
+}
+
+/* box_plane_side for a node's four vertices, donor planes from the cache. */
+__device__ __forceinline__ int node_side(const DevMesh& m, const Plane32& PL, const float4* cache, int i0, int j0,
+                                         int k0, const int* lo, const int* hi, const float4* v)
+{
+    if (hi[0] - lo[0] > 1 || hi[1] - lo[1] > 1 || hi[2] - lo[2] > 1) return 0;
+    int side = 2;
+    for (int c = lo[2]; c <= hi[2]; ++c)
+        for (int b = lo[1]; b <= hi[1]; ++b)
+            for (int a = lo[0]; a <= hi[0]; ++a) {
+                const float4 p = nbr_plane(m, PL, cache, i0, j0, k0, a, b, c);
+                const float Dt = p.w + p.x * (float)a + p.y * (float)b + p.z * (float)c;
+                bool neg = true, pos = true;
+#pragma unroll
+                for (int n = 0; n < 4; ++n) {
+                    const float d = fmaf(p.x, v[n].x, fmaf(p.y, v[n].y, fmaf(p.z, v[n].z, -Dt)));
+                    neg = neg && d < 0.f;
+                    pos = pos && d > 0.f;
+                }
+                const int sd = neg ? 1 : (pos ? -1 : 0);
+                if (sd == 0 || (side != 2 && sd != side)) return 0;
+                side = sd;
+            }
+    return side;
+}
 
 __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, double* __restrict__ VFout, Plane32 PL,
                                                                   const int* __restrict__ slow_cells,
@@ -483,13 +535,13 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
                                                                   const int* __restrict__ slow_count, int* work,
                                                                   int* errw)
 {
-    __shared__ CutCase s_tab[16];
-    __shared__ Item s_stack[CLIPW_WARPS][CLIPW_CAP];
+    extern __shared__ __align__(16) unsigned char clip_smem[];
+    ClipShared& S = *reinterpret_cast<ClipShared*>(clip_smem);
     for (int t = threadIdx.x; t < 16 * (int)sizeof(CutCase); t += blockDim.x)
-        reinterpret_cast<char*>(s_tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
+        reinterpret_cast<char*>(S.tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
     __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    Item* stk = s_stack[w];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+    const unsigned lanemask_lt = (1u << lane) - 1u;
     const int n_cells = *slow_count;
     int err = 0;
     for (;;) {
@@ -501,18 +553,29 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
         /* cell geometry of the batch (lane b holds cell b) */
         int ci_ = 0, cj_ = 0, ck_ = 0;
         if (lane < nb) cell_of(m, slow_cells[base + lane], ci_, cj_, ck_);
-        /* seed: lane q < 5*nb pushes tet q%5 of cell q/5; unclipped tet volume = vol */
+        /* donor planes of each batch cell's 3x3x3 neighbourhood */
+        for (int t0 = 0; t0 < CLIPW_BATCH * CLIPW_NBR; t0 += 32) {
+            const int t = t0 + lane;
+            const int b = min(t / CLIPW_NBR, CLIPW_BATCH - 1);
+            const int ii = __shfl_sync(0xffffffffu, ci_, b), jj = __shfl_sync(0xffffffffu, cj_, b),
+                      kk = __shfl_sync(0xffffffffu, ck_, b);
+            if (t < nb * CLIPW_NBR) {
+                const int r = t - b * CLIPW_NBR;
+                S.pl[w][b][r] = __ldg(PL.P + cidx(m, ii + r % 3 - 1, jj + (r / 3) % 3 - 1, kk + r / 9 - 1));
+            }
+        }
+        /* seed: lane q < 5*nb pushes tet q%5 of cell q/5, its tag (cell in batch) in vertex 0 */
         FF acc[CLIPW_BATCH], avol[CLIPW_BATCH];
+#pragma unroll
         for (int b = 0; b < CLIPW_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; }
         if (lane < 5 * nb) {
             const int b = lane / 5, t = lane - 5 * b;
-            Item& it = stk[lane];
+#pragma unroll
             for (int n = 0; n < 4; ++n) {
-                const float4 q = __ldg(slow_verts + (long)(base + b) * 8 + tet5(t, n));
-                it.x[n] = q.x; it.y[n] = q.y; it.z[n] = q.z;
-                it.ix[n] = (unsigned)__float_as_int(q.w);
+                float4 q = __ldg(slow_verts + (long)(base + b) * 8 + tet5(t, n));
+                if (n == 0) q.w = __int_as_float((int)(wbits(q) | ((unsigned)b << 24)));
+                S.stk[w][n][lane] = q;
             }
-            it.tag = (unsigned)b;
         }
         int size = 5 * nb;
         __syncwarp();
@@ -522,136 +585,182 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
             /* phase 1: pop up to 32 nodes and classify them */
             const int n = min(32, size);
             const int top = size - n;
-            Item it;
             const bool act = lane < n;
-            if (act) it = stk[top + lane];
+            float4 v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = act ? S.stk[w][q][top + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
             __syncwarp();
             size = top;
-            const int bsel = act ? (int)(it.tag & 3) : 0;
-            const int i0 = __shfl_sync(0xffffffffu, ci_, bsel), j0 = __shfl_sync(0xffffffffu, cj_, bsel),
-                      k0 = __shfl_sync(0xffffffffu, ck_, bsel);
-            const int b = bsel;
-            int kind = 0; /* 0 idle, 1 pruned, 2 leaf, 3 cut */
-            int bp = 0, cs = 0, dir = -1, cut = 0, flags = 0, nchild = 0;
+            const unsigned tag = wbits(v[0]) >> 24;
+            const int b = (int)(tag & 3u);
+            int flags = (int)((tag >> 2) & 7u);
+            const int i0 = __shfl_sync(0xffffffffu, ci_, b), j0 = __shfl_sync(0xffffffffu, cj_, b),
+                      k0 = __shfl_sync(0xffffffffu, ck_, b);
+            const float4* cache = S.pl[w][b];
+            int mode = 0; /* 0 idle, 1 leaf (pruned or PLIC), 2 cut */
+            int cs = 0, dir = -1, cut = 0, nchild = 0;
             int rlo[3], rhi[3];
             int cind[4][3];
-            float d[4];
+            float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
             if (act) {
-                flags = (it.tag >> 2) & 7;
                 rlo[0] = max(m.lo - i0, -REL); rlo[1] = max(m.lo - j0, -REL); rlo[2] = max(m.lo - k0, -REL);
                 rhi[0] = min(m.hi[0] - i0, REL); rhi[1] = min(m.hi[1] - j0, REL); rhi[2] = min(m.hi[2] - k0, REL);
+#pragma unroll
                 for (int nn = 0; nn < 4; ++nn)
-                    for (int q = 0; q < 3; ++q) cind[nn][q] = unpack(it.ix[nn], q);
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) cind[nn][q] = unpack(wbits(v[nn]), q);
                 int lo[3], hi[3];
+#pragma unroll
                 for (int q = 0; q < 3; ++q) {
                     lo[q] = min(min(cind[0][q], cind[1][q]), min(cind[2][q], cind[3][q]));
                     hi[q] = max(max(cind[0][q], cind[1][q]), max(cind[2][q], cind[3][q]));
                 }
-                bp = m.fast_pure ? box_plane_side<4>(m, PL, i0, j0, k0, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], it.x,
-                                                     it.y, it.z) : 0;
+                const int bp = m.fast_pure ? node_side(m, PL, cache, i0, j0, k0, lo, hi, v) : 0;
                 if (bp != 0) {
-                    kind = 1;
+                    mode = 1;
+                    cs = bp > 0 ? 0 : 15;
                 } else {
+#pragma unroll
                     for (int q = 0; q < 3; ++q) {
-                        if (flags & (1 << q)) continue;
-                        if (hi[q] > lo[q]) { dir = q; cut = hi[q]; break; }
-                        flags |= 1 << q;
+                        if (dir >= 0 || (flags & (1 << q))) continue;
+                        if (hi[q] > lo[q]) { dir = q; cut = hi[q]; }
+                        else flags |= 1 << q;
                     }
                     if (dir < 0) {
-                        kind = 2;
+                        /* PLIC leaf (src/VFgeom.jl:760-830): the donor is the cell of vertex 0 */
+                        mode = 1;
+                        const int di = cind[0][0], dj = cind[0][1], dk = cind[0][2];
+                        const float4 p = nbr_plane(m, PL, cache, i0, j0, k0, di, dj, dk);
+                        const float Dt = p.w + p.x * (float)di + p.y * (float)dj + p.z * (float)dk;
+                        d0 = p.x * v[0].x + p.y * v[0].y + p.z * v[0].z - Dt;
+                        d1 = p.x * v[1].x + p.y * v[1].y + p.z * v[1].z - Dt;
+                        d2 = p.x * v[2].x + p.y * v[2].y + p.z * v[2].z - Dt;
+                        d3 = p.x * v[3].x + p.y * v[3].y + p.z * v[3].z - Dt;
                     } else {
-                        kind = 3;
+                        /* mesh-plane cut (src/VFgeom.jl:832-899) */
+                        mode = 2;
                         const float pl = (float)cut;
-                        const float* cd = dir == 0 ? it.x : (dir == 1 ? it.y : it.z);
-                        for (int nn = 0; nn < 4; ++nn) d[nn] = cd[nn] - pl;
-                        float c0 = d[0], c1 = d[1], c2 = d[2], c3 = d[3];
-                        cs = d2case(c0, c1, c2, c3, 1e-30f, err);
-                        nchild = s_tab[cs].ntets;
+                        d0 = (dir == 0 ? v[0].x : (dir == 1 ? v[0].y : v[0].z)) - pl;
+                        d1 = (dir == 0 ? v[1].x : (dir == 1 ? v[1].y : v[1].z)) - pl;
+                        d2 = (dir == 0 ? v[2].x : (dir == 1 ? v[2].y : v[2].z)) - pl;
+                        d3 = (dir == 0 ? v[3].x : (dir == 1 ? v[3].y : v[3].z)) - pl;
                     }
+                    cs = d2case(d0, d1, d2, d3, 1e-30f, err);
+                    if (mode == 2) nchild = S.tab[cs].ntets;
                 }
             }
             /* children placement: cutters in lane order while they fit, keeping n slots free for
-             * the nodes that have to go back; if none fits, lane 0 finishes its node privately */
+             * the nodes that have to go back; if none fits, the first cutter finishes its node
+             * privately */
             int incl = nchild;
+#pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, incl, off);
                 if (lane >= off) incl += y;
             }
-            bool fits = kind == 3 && size + incl <= CLIPW_CAP - n;
+            const bool fits = mode == 2 && size + incl <= CLIPW_CAP - n;
             const unsigned fitmask = __ballot_sync(0xffffffffu, fits);
-            const unsigned cutmask = __ballot_sync(0xffffffffu, kind == 3);
-            bool back = kind == 3 && !fits;
+            const unsigned cutmask = __ballot_sync(0xffffffffu, mode == 2);
+            bool back = mode == 2 && !fits;
             bool priv = false;
             if (!fitmask && cutmask && lane == __ffs(cutmask) - 1) { back = false; priv = true; }
             const int pushed = fits ? nchild : 0;
             int ipush = pushed;
+#pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, ipush, off);
                 if (lane >= off) ipush += y;
             }
             const int tot_push = __shfl_sync(0xffffffffu, ipush, 31);
             const unsigned backmask = __ballot_sync(0xffffffffu, back);
-            /* phase 2 */
-            if (kind == 1) {
-                const float tv = tet_vol<float>(it.x[0], it.y[0], it.z[0], it.x[1], it.y[1], it.z[1], it.x[2], it.y[2],
-                                                it.z[2], it.x[3], it.y[3], it.z[3]);
-                acc_add(avol, b, tv);
-                if (bp > 0) acc_add(acc, b, tv);
-            } else if (kind == 2) {
-                FF rv, rl;
-                leaf32(m, s_tab, PL, i0, j0, k0, it.x, it.y, it.z, cind[0][0], cind[0][1], cind[0][2], rv, rl, err);
-                acc_add(avol, b, rv);
-                acc_add(acc, b, rl);
+            /* phase 2: leaves and fitting cuts share the plane-cut code */
+            if (mode == 1 || fits) {
+                const CutCase& C = S.tab[cs];
+                unsigned s1p[4];
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn) {
+                    int a0 = cind[nn][0], a1 = cind[nn][1], a2 = cind[nn][2];
+                    if (mode == 2) {
+                        if (dir == 0) a0 = min(a0, cut - 1);
+                        else if (dir == 1) a1 = min(a1, cut - 1);
+                        else a2 = min(a2, cut - 1);
+                    }
+                    s1p[nn] = pack3(a0, a1, a2);
+                    S.scr[nn][tid] = make_float4(v[nn].x, v[nn].y, v[nn].z, __int_as_float((int)s1p[nn]));
+                }
+                const int nvert = C.nvert;
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn) {
+                    if (nn >= nvert) break;
+                    const int e1 = C.v1[nn], e2 = C.v2[nn];
+                    const float4 A = S.scr[e1][tid], B = S.scr[e2][tid];
+                    const float da = sel4(d0, d1, d2, d3, e1), db = sel4(d0, d1, d2, d3, e2);
+                    const float den = db - da;
+                    const float mu = fminf(1.f, fmaxf(0.f, den != 0.f ? -da / den : 1.f));
+                    const float x = fmaf(mu, B.x - A.x, A.x);
+                    const float y = fmaf(mu, B.y - A.y, A.y);
+                    const float z = fmaf(mu, B.z - A.z, A.z);
+                    unsigned pk = 0u;
+                    if (mode == 2) {
+                        /* pt2index! seeded with vertex nn's indices, bracketed by the edge's ends */
+                        const unsigned pa = wbits(A), pb = wbits(B);
+                        int nv[3];
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const float u = q == 0 ? x : (q == 1 ? y : z);
+                            const int Iv = idx32(u, unpack(s1p[nn], q), rlo[q], rhi[q], err);
+                            const int a1 = unpack(pa, q), a2 = unpack(pb, q);
+                            nv[q] = min(max(Iv, min(a1, a2)), max(a1, a2));
+                        }
+                        if (dir == 0) nv[0] = cut - 1;
+                        else if (dir == 1) nv[1] = cut - 1;
+                        else nv[2] = cut - 1;
+                        pk = pack3(nv[0], nv[1], nv[2]);
+                    }
+                    S.scr[4 + nn][tid] = make_float4(x, y, z, __int_as_float((int)pk));
+                }
+                const int nt = C.ntets;
+                if (mode == 1) {
+                    for (int c = 0; c < nt; ++c) {
+                        const float4 P0 = S.scr[C.vtet[c][0]][tid], P1 = S.scr[C.vtet[c][1]][tid];
+                        const float4 P2 = S.scr[C.vtet[c][2]][tid], P3 = S.scr[C.vtet[c][3]][tid];
+                        const float tv = tet_vol<float>(P0.x, P0.y, P0.z, P1.x, P1.y, P1.z, P2.x, P2.y, P2.z, P3.x,
+                                                        P3.y, P3.z);
+                        acc_add(avol, b, tv);
+                        if (C.side[c] == 0) acc_add(acc, b, tv);
+                    }
+                } else {
+                    const int pos = size + ipush - pushed;
+                    const unsigned tagc = ((unsigned)b | ((unsigned)flags << 2)) << 24;
+                    const int sh = 8 * dir;
+                    for (int c = 0; c < nt; ++c) {
+                        const bool up = C.side[c] == 1;
+#pragma unroll
+                        for (int nn = 0; nn < 4; ++nn) {
+                            float4 q = S.scr[C.vtet[c][nn]][tid];
+                            unsigned pk = wbits(q);
+                            if (up) pk = (pk & ~(255u << sh)) | ((unsigned)(cut + 128) << sh);
+                            if (nn == 0) pk |= tagc;
+                            q.w = __int_as_float((int)pk);
+                            S.stk[w][nn][pos + c] = q;
+                        }
+                    }
+                }
             } else if (priv) {
                 FF rv, rl;
                 float cx[4], cy[4], cz[4];
-                for (int nn = 0; nn < 4; ++nn) { cx[nn] = it.x[nn]; cy[nn] = it.y[nn]; cz[nn] = it.z[nn]; }
-                clip32(m, s_tab, PL, nullptr, i0, j0, k0, rlo, rhi, cx, cy, cz, cind, rv, rl, err);
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn) { cx[nn] = v[nn].x; cy[nn] = v[nn].y; cz[nn] = v[nn].z; }
+                clip32(m, S.tab, PL, nullptr, i0, j0, k0, rlo, rhi, cx, cy, cz, cind, rv, rl, err);
                 acc_add(avol, b, rv);
                 acc_add(acc, b, rl);
-            } else if (fits) {
-                /* cut by the mesh plane (src/VFgeom.jl:832-899) and push the children */
-                float vx[8], vy[8], vz[8];
-                int s1[8][3];
-                for (int nn = 0; nn < 4; ++nn) {
-                    vx[nn] = it.x[nn]; vy[nn] = it.y[nn]; vz[nn] = it.z[nn];
-                    s1[nn][0] = cind[nn][0]; s1[nn][1] = cind[nn][1]; s1[nn][2] = cind[nn][2];
-                    s1[nn][dir] = min(cind[nn][dir], cut - 1);
-                }
-                const CutCase& C = s_tab[cs];
-                for (int nn = 0; nn < C.nvert; ++nn) {
-                    const int v1 = C.v1[nn], v2 = C.v2[nn];
-                    const float den = d[v2] - d[v1];
-                    const float mu = fminf(1.f, fmaxf(0.f, den != 0.f ? -d[v1] / den : 1.f));
-                    const float x = fmaf(mu, vx[v2] - vx[v1], vx[v1]);
-                    const float y = fmaf(mu, vy[v2] - vy[v1], vy[v1]);
-                    const float z = fmaf(mu, vz[v2] - vz[v1], vz[v1]);
-                    vx[4 + nn] = x; vy[4 + nn] = y; vz[4 + nn] = z;
-                    const int Iv[3] = {idx32(x, s1[nn][0], rlo[0], rhi[0], err), idx32(y, s1[nn][1], rlo[1], rhi[1], err),
-                                       idx32(z, s1[nn][2], rlo[2], rhi[2], err)};
-                    for (int q = 0; q < 3; ++q) {
-                        const int a1 = s1[v1][q], a2 = s1[v2][q];
-                        s1[4 + nn][q] = min(max(Iv[q], min(a1, a2)), max(a1, a2));
-                    }
-                    s1[4 + nn][dir] = cut - 1;
-                }
-                const int pos = size + ipush - pushed;
-                const unsigned tag = (unsigned)b | ((unsigned)flags << 2);
-                for (int c = 0; c < C.ntets; ++c) {
-                    const int side = C.side[c];
-                    Item& ch = stk[pos + c];
-                    for (int nn = 0; nn < 4; ++nn) {
-                        const int v = C.vtet[c][nn];
-                        ch.x[nn] = vx[v]; ch.y[nn] = vy[v]; ch.z[nn] = vz[v];
-                        int a0 = s1[v][0], a1 = s1[v][1], a2 = s1[v][2];
-                        if (side == 1) { if (dir == 0) a0 = cut; else if (dir == 1) a1 = cut; else a2 = cut; }
-                        ch.ix[nn] = pack3(a0, a1, a2);
-                    }
-                    ch.tag = tag;
-                }
             }
             /* nodes that did not fit go back above the children, in lane order */
-            if (back) stk[size + tot_push + __popc(backmask & ((1u << lane) - 1u))] = it;
+            if (back) {
+                const int p = size + tot_push + __popc(backmask & lanemask_lt);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) S.stk[w][q][p] = v[q];
+            }
             size += tot_push + __popc(backmask);
             __syncwarp();
         }
@@ -659,15 +768,15 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
 #pragma unroll
         for (int b = 0; b < CLIPW_BATCH; ++b) {
             if (b >= nb) break;
-            double v = (double)acc[b].hi + (double)acc[b].lo;
+            double vl = (double)acc[b].hi + (double)acc[b].lo;
             double u = (double)avol[b].hi + (double)avol[b].lo;
             for (int off = 16; off > 0; off >>= 1) {
-                v += __shfl_xor_sync(0xffffffffu, v, off);
+                vl += __shfl_xor_sync(0xffffffffu, vl, off);
                 u += __shfl_xor_sync(0xffffffffu, u, off);
             }
             if (lane == b) {
                 const double tetsign = ((ci_ + cj_ + ck_) % 2) == 0 ? 1.0 : -1.0;
-                const double vol = tetsign * u, liq = tetsign * v;
+                const double vol = tetsign * u, liq = tetsign * vl;
                 if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
                 VFout[vidx(m, ci_, cj_, ck_)] = liq / vol;
             }
@@ -688,7 +797,11 @@ void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, co
     k_sl32_pre<<<nsm * 8, SL32_THREADS, 0, s>>>(m, (float)dt, VFout, V, PL, phase, list, count, work, slow_cells,
                                                 slow_verts, slow_count, errw);
     (void)tet_out;
-    k_sl32_clipw<<<nsm * 4, CLIPW_WARPS * 32, 0, s>>>(m, VFout, PL, slow_cells, slow_verts, slow_count, work2, errw);
+    /* 51.4 KB of dynamic shared memory per block: above the 48 KB default, four blocks per SM */
+    const int smem = (int)sizeof(ClipShared);
+    cudaFuncSetAttribute(k_sl32_clipw, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_sl32_clipw<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, VFout, PL, slow_cells, slow_verts, slow_count, work2,
+                                                          errw);
 }
 
 } // namespace slvof
