@@ -292,7 +292,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     const long interior = N[0] * N[1] * N[2];
     c->npure = c->nsm * 8;
     auto alloc = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess && cudaMemset(*p, 0, bytes) == cudaSuccess; };
-    const long ncoord = 2 * (n0 + n1 + n2) + 3;
+    const long ncoord = mesh_coords(mesh, nullptr);
     bool ok = alloc((void**)&c->coords, ncoord * sizeof(double)) && alloc((void**)&c->VF[0], c->nvf * sizeof(double)) &&
               alloc((void**)&c->VF[1], c->nvf * sizeof(double)) && alloc((void**)&c->uf, c->ncell * sizeof(double)) &&
               alloc((void**)&c->vf, c->ncell * sizeof(double)) && alloc((void**)&c->wf, c->ncell * sizeof(double)) &&
@@ -313,20 +313,9 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     if (!ok) return bail(SLVOF_E_NOMEM);
     /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
     std::vector<double> h(ncoord);
-    double* p = h.data();
+    mesh_coords(mesh, h.data());
     const double* fsrc[3] = {mesh->x, mesh->y, mesh->z};
-    const double* csrc[3] = {mesh->xm, mesh->ym, mesh->zm};
     const long nn[3] = {n0, n1, n2};
-    long off_f[3], off_c[3], o = 0;
-    double maxabs = 0.0;
-    for (int q = 0; q < 3; ++q) {
-        off_f[q] = o;
-        for (long t = 0; t <= nn[q]; ++t) { p[o++] = fsrc[q][t]; maxabs = std::max(maxabs, std::fabs(fsrc[q][t])); }
-    }
-    for (int q = 0; q < 3; ++q) {
-        off_c[q] = o;
-        for (long t = 0; t < nn[q]; ++t) p[o++] = csrc[q][t];
-    }
     if (precision == SLVOF_MIXED) {
         /* the FP32 geometry works in cell units and needs a uniform mesh (src/Mesh.jl:83-100) */
         const double dd[3] = {mesh->dx, mesh->dy, mesh->dz};
@@ -336,27 +325,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     }
     if (cudaMemcpy(c->coords, h.data(), ncoord * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(SLVOF_E_CUDA);
-    DevMesh& m = c->m;
-    for (int q = 0; q < 3; ++q) {
-        m.N[q] = (int)N[q];
-        m.hi[q] = (int)(N[q] + g);
-        m.f[q] = c->coords + off_f[q];
-        m.c[q] = c->coords + off_c[q];
-    }
-    m.g = (int)g;
-    m.nband = mesh->nband;
-    m.projection = mesh->projection;
-    m.per[0] = mesh->xper != 0; m.per[1] = mesh->yper != 0; m.per[2] = mesh->zper != 0;
-    m.lo = 1 - (int)g;
-    m.vlo = m.lo - 3;
-    m.d[0] = mesh->dx; m.d[1] = mesh->dy; m.d[2] = mesh->dz;
-    m.VFlo = mesh->VFlo;
-    m.VFhi = mesh->VFhi;
-    m.Lsum = (mesh->Lx + mesh->Ly) + mesh->Lz;
-    m.cellvol = (mesh->dx * mesh->dy) * mesh->dz;
-    m.fast_pure = maxabs < m.Lsum * (1.0 - 1e-9);
-    m.cs1 = n0; m.cs2 = n0 * n1;
-    m.vs1 = n0 + 6; m.vs2 = (n0 + 6) * (n1 + 6);
+    mesh_fill(mesh, c->coords, c->m);
     *out = c;
     return SLVOF_OK;
 }

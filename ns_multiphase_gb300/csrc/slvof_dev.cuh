@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "detmath.h"
+#include "mesh_view.h"
 
 namespace slvof {
 
@@ -22,26 +23,6 @@ constexpr int CLIP_STACK32 = 8;                  /* FP32 clip nesting (pruned su
 /* Error bits, same values as SLVOF_DEV_* in include/slvof.h. */
 enum : int { ERR_INDEX = 1, ERR_DEPTH = 2, ERR_NAN = 4, ERR_VOLUME = 8 };
 
-struct DevMesh {
-    int N[3];
-    int g;
-    int nband;
-    int projection;
-    int per[3];
-    int lo;  /* 1 - g, first cell index in every direction */
-    int vlo; /* lo - 3, first VF index */
-    int hi[3];
-    int fast_pure; /* pure-donor shortcut valid (|coordinates| < Lx+Ly+Lz everywhere) */
-    double d[3];
-    double VFlo, VFhi;
-    double Lsum;    /* (Lx+Ly)+Lz, |D| of pure cells (src/VF.jl:116-120) */
-    double cellvol; /* (dx*dy)*dz */
-    const double* f[3]; /* face coordinates, f[q][i - lo] */
-    const double* c[3]; /* centre coordinates */
-    long cs1, cs2;      /* cell-array strides (j, k) */
-    long vs1, vs2;      /* VF strides */
-};
-
 __device__ __forceinline__ long cidx(const DevMesh& m, int i, int j, int k)
 {
     return (long)(i - m.lo) + (long)(j - m.lo) * m.cs1 + (long)(k - m.lo) * m.cs2;
@@ -52,24 +33,6 @@ __device__ __forceinline__ long vidx(const DevMesh& m, int i, int j, int k)
 }
 __device__ __forceinline__ double fco(const DevMesh& m, int q, int i) { return __ldg(m.f[q] + (i - m.lo)); }
 __device__ __forceinline__ double cco(const DevMesh& m, int q, int i) { return __ldg(m.c[q] + (i - m.lo)); }
-
-/* Single-rank ghost fill as a source map.  Neumann! (x-,x+,y-,y+,z-,z+) followed by
- * update_borders! (x, y, z; two self-Sendrecv! copies per periodic direction) is a sequence
- * of slab copies, each reading the state before it.  Walking the copies backwards gives, for
- * every cell, the cell whose pre-fill value it ends with.  The copies of one direction only
- * move that direction's index, so the map is separable. */
-__host__ __device__ __forceinline__ int ghost_src_1d(int p, int N, int g, bool periodic, bool neumann)
-{
-    if (periodic) {
-        if (p >= 1 - g && p <= 0) p += N;     /* A[mino_:min_-1] <- A[max_-g+1:max_] (second copy) */
-        if (p >= N + 1 && p <= N + g) p -= N; /* A[max_+1:maxo_] <- A[min_:min_+g-1] (first copy) */
-    }
-    if (neumann) {
-        if (p == N + 1) p = N; /* A[max_+1] <- A[max_] */
-        if (p == 0) p = 1;     /* A[min_-1] <- A[min_] */
-    }
-    return p;
-}
 
 /* Julia max/min on Float64 (NaN-propagating, max(-0.0, 0.0) == 0.0). */
 template <class R>
@@ -90,80 +53,11 @@ __device__ __forceinline__ double sdiv(double a, double b) { return fabs(b) <= E
 /* mu = min(1, max(0, -d1 /^ (d2-d1))), src/VFgeom.jl:787 */
 __device__ __forceinline__ double clamp_mu(double q) { return jmin(1.0, jmax(0.0, q)); }
 
-/* ---- cut tables, src/VFgeom.jl:55-165, 0-based ---------------------------------------
- * For each cut case (0..15, = reference case - 1): number of new vertices on the plane, the
- * edges they lie on (v1, v2), number of tets, first liquid (negative-side) tet, the tets'
- * vertices (0..3 original, 4..7 new) and the side (0 negative, 1 positive) of each tet. */
-struct CutCase {
-    int8_t nvert, ntets, nntet, pad;
-    int8_t v1[4], v2[4];
-    int8_t vtet[6][4];
-    int8_t side[6];
-    int8_t pad2[2];
-};
-
+/* cut tables (src/VFgeom.jl:55-165) in constant memory */
 #define X_ -1
-static __constant__ CutCase c_cut[16] = {
-    {0, 1, 1, 0, {X_, X_, X_, X_}, {X_, X_, X_, X_},
-     {{0, 1, 2, 3}, {X_, X_, X_, X_}, {X_, X_, X_, X_}, {X_, X_, X_, X_}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {0, X_, X_, X_, X_, X_}, {0, 0}},
-    {3, 4, 2, 0, {0, 0, 0, X_}, {1, 2, 3, X_},
-     {{4, 6, 5, 0}, {5, 1, 2, 3}, {3, 1, 4, 5}, {4, 5, 6, 3}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 0, 0, 0, X_, X_}, {0, 0}},
-    {3, 4, 2, 0, {1, 1, 1, X_}, {2, 3, 0, X_},
-     {{6, 4, 5, 1}, {0, 2, 3, 5}, {0, 4, 2, 5}, {4, 6, 5, 0}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 0, 0, 0, X_, X_}, {0, 0}},
-    {4, 6, 4, 0, {0, 1, 0, 1}, {3, 3, 2, 2},
-     {{4, 7, 5, 1}, {4, 6, 7, 0}, {4, 0, 7, 1}, {4, 5, 7, 3}, {4, 7, 6, 2}, {4, 7, 2, 3}},
-     {1, 1, 1, 0, 0, 0}, {0, 0}},
-    {3, 4, 2, 0, {2, 2, 2, X_}, {3, 0, 1, X_},
-     {{5, 4, 6, 2}, {1, 0, 3, 5}, {5, 4, 3, 1}, {5, 6, 4, 1}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 0, 0, 0, X_, X_}, {0, 0}},
-    {4, 6, 4, 0, {0, 2, 0, 2}, {3, 3, 1, 1},
-     {{4, 5, 7, 2}, {4, 7, 6, 0}, {4, 7, 0, 2}, {4, 7, 5, 3}, {4, 6, 7, 1}, {4, 7, 3, 1}},
-     {1, 1, 1, 0, 0, 0}, {0, 0}},
-    {4, 6, 4, 0, {1, 2, 1, 2}, {3, 3, 0, 0},
-     {{7, 5, 4, 2}, {4, 6, 7, 1}, {7, 4, 1, 2}, {7, 4, 5, 3}, {4, 7, 6, 0}, {4, 7, 0, 3}},
-     {1, 1, 1, 0, 0, 0}, {0, 0}},
-    {3, 4, 4, 0, {3, 3, 3, X_}, {0, 1, 2, X_},
-     {{0, 1, 2, 6}, {0, 1, 6, 5}, {4, 6, 5, 0}, {4, 5, 6, 3}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 1, 1, 0, X_, X_}, {0, 0}},
-    {3, 4, 2, 0, {3, 3, 3, X_}, {0, 1, 2, X_},
-     {{4, 5, 6, 3}, {0, 1, 2, 5}, {4, 0, 2, 5}, {4, 6, 5, 2}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 0, 0, 0, X_, X_}, {0, 0}},
-    {4, 6, 4, 0, {0, 3, 0, 3}, {2, 2, 1, 1},
-     {{4, 7, 5, 3}, {4, 6, 7, 0}, {4, 7, 3, 0}, {4, 5, 7, 2}, {4, 7, 6, 1}, {4, 7, 1, 2}},
-     {1, 1, 1, 0, 0, 0}, {0, 0}},
-    {4, 6, 4, 0, {1, 3, 1, 3}, {2, 2, 0, 0},
-     {{7, 4, 5, 3}, {4, 7, 6, 1}, {7, 1, 4, 3}, {7, 5, 4, 2}, {4, 6, 7, 0}, {4, 7, 2, 0}},
-     {1, 1, 1, 0, 0, 0}, {0, 0}},
-    {3, 4, 4, 0, {2, 2, 2, X_}, {3, 0, 1, X_},
-     {{0, 3, 1, 6}, {3, 0, 5, 6}, {5, 6, 4, 3}, {5, 4, 6, 2}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 1, 1, 0, X_, X_}, {0, 0}},
-    {4, 6, 4, 0, {2, 3, 2, 3}, {1, 1, 0, 0},
-     {{7, 5, 4, 3}, {4, 6, 7, 2}, {7, 3, 4, 2}, {7, 4, 5, 1}, {4, 7, 6, 0}, {4, 7, 0, 1}},
-     {1, 1, 1, 0, 0, 0}, {0, 0}},
-    {3, 4, 4, 0, {1, 1, 1, X_}, {2, 3, 0, X_},
-     {{2, 3, 0, 6}, {6, 5, 2, 3}, {6, 5, 4, 2}, {6, 4, 5, 1}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 1, 1, 0, X_, X_}, {0, 0}},
-    {3, 4, 4, 0, {0, 0, 0, X_}, {1, 2, 3, X_},
-     {{6, 3, 1, 2}, {1, 2, 5, 6}, {4, 5, 6, 1}, {4, 6, 5, 0}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, 1, 1, 0, X_, X_}, {0, 0}},
-    {0, 1, 2, 0, {X_, X_, X_, X_}, {X_, X_, X_, X_},
-     {{0, 1, 2, 3}, {X_, X_, X_, X_}, {X_, X_, X_, X_}, {X_, X_, X_, X_}, {X_, X_, X_, X_}, {X_, X_, X_, X_}},
-     {1, X_, X_, X_, X_, X_}, {0, 0}},
-};
+static __constant__ CutCase c_cut[16] = SLVOF_CUT_TABLE;
 #undef X_
 
-/* 5-tet split of the 8 cell vertices (src/VFgeom.jl:235-256), 0-based. */
-__host__ __device__ constexpr int tet5(int t, int n)
-{
-    return (t == 0) ? (n == 0 ? 0 : n == 1 ? 1 : n == 2 ? 3 : 5)
-         : (t == 1) ? (n == 0 ? 0 : n == 1 ? 3 : n == 2 ? 2 : 6)
-         : (t == 2) ? (n == 0 ? 0 : n == 1 ? 4 : n == 2 ? 5 : 6)
-         : (t == 3) ? (n == 0 ? 3 : n == 1 ? 6 : n == 2 ? 5 : 7)
-                    : (n == 0 ? 0 : n == 1 ? 3 : n == 2 ? 6 : 5);
-}
 
 /* tet_vol, src/VFgeom.jl:669-681: -1/6 * det(v1-v4, v2-v4, v3-v4) in the reference's
  * expansion order. */
