@@ -137,6 +137,36 @@ int slvof_transportSL(slvof_ctx* ctx, double dt, double* VF, const double* uf, c
 int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, const double* vf, const double* wf,
                     double* VF, double* mass);
 
+/* ---- state save/restore and the reverse pass ------------------------------------------------
+ * Reverse-mode derivative of the FP64 step (the hand-written adjoint; the reference has no
+ * counterpart, its Julia callers would wrap it as a ChainRules rrule).  It treats the step as
+ * the smooth function it is between switches of its discrete choices (ELVIRA candidate, band,
+ * cut cases, donor cells) and is exact there.  The derivative runs in FP64 for both
+ * precisions: a mixed-precision context reverses with the same FP64 geometry. */
+/* Neumann! + VF borders, computeNormal!, computePLIC!, computeBand! on the current VF: the
+ * state a step starts from (run_solver, src/NavierStokes_Parallel.jl:73-98). */
+int slvof_prepare(slvof_ctx* ctx);
+/* Copy the current VF (VF-array shaped) to / from a device buffer of the caller, for
+ * checkpoints that stay on the device.  After loading, call slvof_prepare before stepping. */
+int slvof_copy_vf_device(slvof_ctx* ctx, double* d_dst);
+int slvof_load_vf_device(slvof_ctx* ctx, const double* d_src);
+/* The context's VF-derivative buffer (VF-array shaped, ghosts included; NULL sets zero) and
+ * its face-velocity derivative buffers (cell-array shaped).  Any NULL output is skipped. */
+int slvof_adjoint_set_vf(slvof_ctx* ctx, const double* gVF);
+int slvof_adjoint_get(slvof_ctx* ctx, double* gVF, double* guf, double* gvf, double* gwf);
+int slvof_adjoint_zero_velocity(slvof_ctx* ctx);
+/* Reverse of one slvof_step(ctx, dt, SLVOF_STEP_BAND, .) from the current state.  Before the
+ * call the context holds the VF the step started from with its normals, PLIC planes and band
+ * (as slvof_step or slvof_prepare leave them), the step's face velocities, and dL/dVF of the
+ * step's result in the VF-derivative buffer.  After it the buffer holds dL/dVF of the
+ * starting VF (ghost entries: derivatives with respect to the ghost values) and dL/d(face
+ * velocities) of the step has been added to the velocity buffers.  The state is unchanged. */
+int slvof_adjoint_step(slvof_ctx* ctx, double dt);
+/* Fold the VF-derivative buffer's ghost entries onto the interior cells they are copies of
+ * (the reverse of Neumann! + VF borders): the derivative with respect to the interior of a
+ * VF whose ghosts were filled from it, e.g. the initial condition after IC!. */
+int slvof_adjoint_fold(slvof_ctx* ctx);
+
 /* ---- synthetic inputs (not part of the reference path) -----------------------------------
  * VF of a union of spheres by VFsphere's sub-sampling rule (src/Tools.jl:907-922), nF points
  * per direction, written to every cell of imino_:imaxo_ (extra VF layers zero); dims=2 uses

@@ -27,6 +27,7 @@ UNITS = {
     "k_mixed.cu": ["-fmad=true"],
     "k_elvira_mixed.cu": ["-fmad=false"],
     "slvof_noalloc.cu": ["-fmad=false"],
+    "k_adj64.cu": ["-fmad=false"],
 }
 
 

@@ -725,7 +725,7 @@ SLVOF_HD void elvira_reverse(const DevMesh& m, const double* VF, double* gVF, in
 }
 
 /* ---- ghost fills ----------------------------------------------------------------------- */
-constexpr int MAXPRE = 40;
+constexpr int MAXPRE = 16;
 /* Indices p of [lo, hi] (one direction) whose ghost-fill source is q; at most MAXPRE. */
 SLVOF_HD int preimage_1d(int q, int N, int g, bool per, bool neu, int lo, int hi, int* out)
 {

@@ -1,0 +1,180 @@
+/*
+ * k_adj64.cu — reverse pass of one FP64 SL-VOF step on the GPU.  Built with -fmad=false: the
+ * forward recomputation inside (pre-image, clip tree) rounds as the FP64 forward path does,
+ * so it walks the same tree.  The per-cell mathematics is adj64.cuh; the kernels here order
+ * the reverse of the step (src/Transport.jl:108-184, src/VF.jl:94-103):
+ *
+ *   fold VF    the step ends with Neumann!/update_VF_borders! (src/Transport.jl:180-181):
+ *              derivatives of ghost copies go to their sources;
+ *   SL         cells outside the band copy VF (derivative passes through); band cells run
+ *              the clip tree backwards, thread per cell, to the face velocities and to the
+ *              donor planes (n, D);
+ *   fold D     computePLIC!'s update_borders!(D) (src/VF.jl:102);
+ *   PLIC       computeDist's derivative at every cell (ghosts included) to n and VF;
+ *   fold n     ELVIRA!'s update_borders! of the normals (src/ELVIRA.jl:49-51);
+ *   ELVIRA     interface cells: the chosen candidate's derivative to the VF block.
+ */
+#include "slvof_kernels.h"
+#include "slvof_dev.cuh"
+#include "adj64.cuh"
+
+namespace slvof {
+
+namespace {
+
+constexpr int ADJ_SL_THREADS = 64;
+
+__device__ __forceinline__ void load_cut_table(CutCase* s_tab)
+{
+    for (int t = threadIdx.x; t < 16 * (int)sizeof(CutCase); t += blockDim.x)
+        reinterpret_cast<char*>(s_tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
+    __syncthreads();
+}
+
+/* out[q] = sum of in[p] over the cells p whose ghost-fill source is q (separable map), over
+ * the VF array (vf = 1, Neumann + borders) or a cell array (vf = 0, borders only). */
+__global__ void k_adj_fold(DevMesh m, const double* __restrict__ in, double* __restrict__ out, int vf, int neumann)
+{
+    const int lo = vf ? m.vlo : m.lo;
+    const int ext = vf ? 3 : 0;
+    const int hi[3] = {m.hi[0] + ext, m.hi[1] + ext, m.hi[2] + ext};
+    const long n0 = hi[0] - lo + 1, n1 = hi[1] - lo + 1, n2 = hi[2] - lo + 1;
+    const long total = n0 * n1 * n2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = lo + (int)(t % n0), j = lo + (int)((t / n0) % n1), k = lo + (int)(t / (n0 * n1));
+        int pa[adj::MAXPRE], pb[adj::MAXPRE], pc[adj::MAXPRE];
+        const int na = adj::preimage_1d(i, m.N[0], m.g, m.per[0], neumann, lo, hi[0], pa);
+        const int nb = adj::preimage_1d(j, m.N[1], m.g, m.per[1], neumann, lo, hi[1], pb);
+        const int nc = adj::preimage_1d(k, m.N[2], m.g, m.per[2], neumann, lo, hi[2], pc);
+        double s = 0.0;
+        for (int c = 0; c < nc; ++c)
+            for (int b = 0; b < nb; ++b)
+                for (int a = 0; a < na; ++a)
+                    s += in[(long)(pa[a] - lo) + (long)(pb[b] - lo) * n0 + (long)(pc[c] - lo) * n0 * n1];
+        out[t] = s;
+    }
+}
+
+/* Cells outside the band: VFnew = VF, the derivative passes through.  Band cells with a
+ * nonzero incoming derivative go to the list. */
+__global__ void k_adj_split(DevMesh m, const short* __restrict__ band, const double* __restrict__ gfold,
+                            double* __restrict__ gout, int* list, int* count)
+{
+    const long total = (long)m.N[0] * m.N[1] * m.N[2];
+    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+        const long v = vidx(m, i, j, k);
+        const double g = gfold[v];
+        const int b = band[cidx(m, i, j, k)];
+        const bool sl = (b < 0 ? -b : b) <= m.nband;
+        if (!sl) gout[v] = g;
+        warp_append(sl && g != 0.0, (int)L, list, count);
+    }
+}
+
+/* Band cells: the SL update backwards (adj::sl_cell), one thread per cell. */
+__global__ void __launch_bounds__(ADJ_SL_THREADS) k_adj_sl(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV,
+                                                           adj::Plic P, const double* __restrict__ gfold,
+                                                           const int* __restrict__ list, const int* __restrict__ count,
+                                                           int* work, int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    load_cut_table(s_tab);
+    adj::Frame st[adj::STACK];
+    const int n = *count;
+    int err = 0;
+    for (;;) {
+        int item = 0;
+        const int lane = threadIdx.x & 31;
+        if (lane == 0) item = atomicAdd(work, 32);
+        item = __shfl_sync(0xffffffffu, item, 0) + lane;
+        if (item - lane >= n) break;
+        if (item < n) {
+            const int L = list[item];
+            const int i = 1 + L % m.N[0], j = 1 + (L / m.N[0]) % m.N[1], k = 1 + L / (m.N[0] * m.N[1]);
+            const double g = gfold[vidx(m, i, j, k)];
+            adj::sl_cell(m, s_tab, V, GV, P, dt, i, j, k, g, st, err);
+        }
+    }
+    if (err) atomicOr(errw, err);
+}
+
+/* computeDist backwards at every cell (ghosts included): gDf -> gn (+=) and gout. */
+__global__ void k_adj_dist(DevMesh m, const double* __restrict__ VF, const double* __restrict__ nx,
+                           const double* __restrict__ ny, const double* __restrict__ nz, const double* __restrict__ D,
+                           const double* __restrict__ gDf, double* gnx, double* gny, double* gnz, double* gout,
+                           int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    load_cut_table(s_tab);
+    const long n0 = m.hi[0] - m.lo + 1, n1 = m.hi[1] - m.lo + 1, n2 = m.hi[2] - m.lo + 1;
+    const long total = n0 * n1 * n2;
+    int err = 0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const double g = gDf[t];
+        if (g == 0.0) continue;
+        const int i = m.lo + (int)(t % n0), j = m.lo + (int)((t / n0) % n1), k = m.lo + (int)(t / (n0 * n1));
+        const long v = vidx(m, i, j, k);
+        const double vf = VF[v];
+        if (!(vf >= m.VFlo && vf <= m.VFhi)) continue; /* pure: D = +-(Lx+Ly+Lz) */
+        double dn[3], dv;
+        if (!adj::dist_partials(m, s_tab, i, j, k, nx[t], ny[t], nz[t], D[t], dn, dv, err)) continue;
+        gnx[t] += dn[0] * g;
+        gny[t] += dn[1] * g;
+        gnz[t] += dn[2] * g;
+        gout[v] += dv * g;
+    }
+    if (err) atomicOr(errw, err);
+}
+
+/* ELVIRA backwards at interior interface cells with a chosen candidate. */
+__global__ void k_adj_elvira(DevMesh m, const double* __restrict__ VF, const signed char* __restrict__ cand,
+                             const double* __restrict__ gnx, const double* __restrict__ gny,
+                             const double* __restrict__ gnz, double* gout)
+{
+    const long total = (long)m.N[0] * m.N[1] * m.N[2];
+    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+        const long c = cidx(m, i, j, k);
+        const double gn[3] = {gnx[c], gny[c], gnz[c]};
+        if (gn[0] == 0.0 && gn[1] == 0.0 && gn[2] == 0.0) continue;
+        const double vf = VF[vidx(m, i, j, k)];
+        if (!(vf >= m.VFlo && vf <= m.VFhi)) continue; /* pure cells carry fixed axis normals */
+        const int lane = cand[c];
+        if (lane < 0) continue;
+        adj::elvira_reverse(m, VF, gout, i, j, k, lane, gn);
+    }
+}
+
+} // namespace
+
+void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s)
+{
+    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, gin, gout, 1, 1);
+}
+
+void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
+                         const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                         const short* band, const signed char* cand, const AdjBuffers& b, int* list, int* count,
+                         int* work, int* errw, int nsm, cudaStream_t s)
+{
+    const long vbytes = (long)(m.N[0] + 2 * m.g + 6) * (m.N[1] + 2 * m.g + 6) * (m.N[2] + 2 * m.g + 6) * sizeof(double);
+    const long cbytes = (long)(m.N[0] + 2 * m.g) * (m.N[1] + 2 * m.g) * (m.N[2] + 2 * m.g) * sizeof(double);
+    cudaMemsetAsync(b.gout, 0, vbytes, s);
+    for (int q = 0; q < 3; ++q) cudaMemsetAsync(b.gn[q], 0, cbytes, s);
+    cudaMemsetAsync(b.gD, 0, cbytes, s);
+    cudaMemsetAsync(count, 0, sizeof(int), s);
+    cudaMemsetAsync(work, 0, sizeof(int), s);
+    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gin, b.gfold, 1, 1);
+    k_adj_split<<<nsm * 8, 256, 0, s>>>(m, band, b.gfold, b.gout, list, count);
+    adj::Vel V{uf, vf, wf};
+    adj::VelGrad GV{b.guf, b.gvf, b.gwf};
+    adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD};
+    k_adj_sl<<<nsm * 8, ADJ_SL_THREADS, 0, s>>>(m, dt, V, GV, P, b.gfold, list, count, work, errw);
+    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gD, b.gDf, 0, 0);
+    k_adj_dist<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, D, b.gDf, b.gn[0], b.gn[1], b.gn[2], b.gout, errw);
+    for (int q = 0; q < 3; ++q) k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gn[q], b.gnf[q], 0, 0);
+    k_adj_elvira<<<nsm * 8, 256, 0, s>>>(m, VF, cand, b.gnf[0], b.gnf[1], b.gnf[2], b.gout);
+}
+
+} // namespace slvof

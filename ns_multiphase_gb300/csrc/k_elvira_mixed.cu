@@ -193,7 +193,8 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
                                                                     double* __restrict__ nz,
                                                                     const int* __restrict__ list,
                                                                     const int* __restrict__ count, int* work,
-                                                                    int* stats, int* errw)
+                                                                    int* stats, signed char* __restrict__ cand,
+                                                                    int* errw)
 {
     __shared__ CutCase s_tab[16];
     __shared__ double s_vd[EL32_WARPS][27];
@@ -307,6 +308,7 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
             const long o = cidx(m, i, j, k);
             nx[o] = cx; ny[o] = cy; nz[o] = cz;
         }
+        if (cand && lane == 0) cand[cidx(m, i, j, k)] = (signed char)(winner < 32 ? winner : -1);
         __syncwarp();
     }
     if (lane == 0 && n_arb) atomicAdd(stats, n_arb);
@@ -314,9 +316,10 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
 }
 
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int* stats, int* errw, int nsm, cudaStream_t s)
+                           const int* count, int* work, int* stats, signed char* cand, int* errw, int nsm,
+                           cudaStream_t s)
 {
-    k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, stats, errw);
+    k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, stats, cand, errw);
 }
 
 } // namespace slvof

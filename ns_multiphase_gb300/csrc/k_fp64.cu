@@ -26,7 +26,8 @@ constexpr int EL_WARPS = 4;
 __global__ void __launch_bounds__(EL_WARPS * 32) k_elvira_iface64(DevMesh m, const double* __restrict__ VF,
                                                                   double* __restrict__ nx, double* __restrict__ ny,
                                                                   double* __restrict__ nz, const int* __restrict__ list,
-                                                                  const int* __restrict__ count, int* work, int* errw)
+                                                                  const int* __restrict__ count, int* work,
+                                                                  signed char* __restrict__ cand, int* errw)
 {
     __shared__ CutCase s_tab[16];
     __shared__ double s_term[EL_WARPS][27][5];
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(EL_WARPS * 32) k_elvira_iface64(DevMesh m, con
             const long c = cidx(m, i, j, k);
             nx[c] = cx; ny[c] = cy; nz[c] = cz;
         }
+        if (cand && lane == 0) cand[cidx(m, i, j, k)] = (signed char)(bl < 32 ? bl : -1);
         __syncwarp();
     }
     if (err) atomicOr(errw, err);
@@ -550,9 +552,9 @@ __global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const
 
 /* ---- launchers ------------------------------------------------------------------------ */
 void launch_elvira_iface64(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int* errw, int nsm, cudaStream_t s)
+                           const int* count, int* work, signed char* cand, int* errw, int nsm, cudaStream_t s)
 {
-    k_elvira_iface64<<<nsm * 8, EL_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, errw);
+    k_elvira_iface64<<<nsm * 8, EL_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, cand, errw);
 }
 
 void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz, double* D,

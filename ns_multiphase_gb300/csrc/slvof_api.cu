@@ -39,6 +39,14 @@ struct slvof_ctx {
     float4* slow_verts = nullptr; /* mixed SL: their pre-image vertices (cell units) + packed indices */
     double2* tet_out = nullptr;   /* mixed SL: (vol, vLiq) of each tet of each slow cell */
     signed char* phase = nullptr; /* pure-donor codes of the PLIC pass */
+    signed char* cand = nullptr;  /* ELVIRA: chosen candidate lane of each interface cell */
+    /* reverse pass (allocated on first use) */
+    double* gvf[2] = {nullptr, nullptr}; /* dL/dVF (current, scratch) */
+    double* gfold = nullptr;
+    double *gn[3] = {nullptr, nullptr, nullptr}, *gD = nullptr;
+    double *gnf[3] = {nullptr, nullptr, nullptr}, *gDf = nullptr;
+    double *guf = nullptr, *gvf_ = nullptr, *gwf = nullptr;
+    int* list_adj = nullptr;
     short* band[2] = {nullptr, nullptr};
     int bcur = 0;
     int* list_sl = nullptr;
@@ -62,7 +70,8 @@ struct slvof_ctx {
 
 namespace {
 
-enum { C_SL = 0, C_IF = 1, C_SLW = 2, C_IFW = 3, C_ERR = 4, C_PL = 5, C_SLOW = 6, C_SLW2 = 7, C_ARB = 8, C_N = 16 };
+enum { C_SL = 0, C_IF = 1, C_SLW = 2, C_IFW = 3, C_ERR = 4, C_PL = 5, C_SLOW = 6, C_SLW2 = 7, C_ARB = 8, C_ADJ = 9,
+       C_ADJW = 10, C_N = 16 };
 
 int fail(slvof_ctx* c, int code, const std::string& msg)
 {
@@ -143,10 +152,10 @@ int st_normals(slvof_ctx* c)
     s_beg(c, S_IFACE);
     if (c->precision == SLVOF_FP64)
         launch_elvira_iface64(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->ctr + C_IFW,
-                              c->ctr + C_ERR, c->nsm, c->stream);
+                              c->cand, c->ctr + C_ERR, c->nsm, c->stream);
     else
         launch_elvira_iface32(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->ctr + C_IFW,
-                              c->ctr + C_ARB, c->ctr + C_ERR, c->nsm, c->stream);
+                              c->ctr + C_ARB, c->cand, c->ctr + C_ERR, c->nsm, c->stream);
     s_end(c, S_IFACE);
     s_beg(c, S_NGHOST);
     launch_normal_ghost(c->m, c->nx, c->ny, c->nz, c->nsm, c->stream);
@@ -299,6 +308,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
               alloc((void**)&c->nx, c->ncell * sizeof(double)) && alloc((void**)&c->ny, c->ncell * sizeof(double)) &&
               alloc((void**)&c->nz, c->ncell * sizeof(double)) && alloc((void**)&c->D, c->ncell * sizeof(double)) &&
               alloc((void**)&c->phase, c->ncell * sizeof(signed char)) &&
+              alloc((void**)&c->cand, c->ncell * sizeof(signed char)) &&
               alloc((void**)&c->band[0], c->ncell * sizeof(short)) && alloc((void**)&c->band[1], c->ncell * sizeof(short)) &&
               alloc((void**)&c->list_sl, interior * sizeof(int)) && alloc((void**)&c->list_if, interior * sizeof(int)) &&
               alloc((void**)&c->list_plic, c->ncell * sizeof(int)) &&
@@ -336,8 +346,10 @@ int slvof_destroy(slvof_ctx* c)
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->coords, c->VF[0], c->VF[1], c->uf, c->vf, c->wf, c->uf32, c->vf32, c->wf32, c->nx, c->ny,
-                    c->nz, c->D, c->planes, c->phase, c->band[0], c->band[1], c->list_sl, c->list_if, c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr,
-                    c->partials, c->mass_d, c->table, c->spheres};
+                    c->nz, c->D, c->planes, c->phase, c->cand, c->band[0], c->band[1], c->list_sl, c->list_if,
+                    c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
+                    c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
+                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -637,6 +649,117 @@ int slvof_case_deformation3d(slvof_ctx* c, double t, double T)
     launch_case_deformation3d(c->m, t, T, c->uf, c->vf, c->wf, c->nsm, c->stream);
     to_float_velocity(c);
     return finish(c, false);
+}
+
+/* ---- reverse pass ----------------------------------------------------------------------- */
+namespace {
+int adj_alloc(slvof_ctx* c)
+{
+    if (c->gvf[0]) return 0;
+    auto alloc = [&](double** p, long n) {
+        return cudaMalloc((void**)p, n * sizeof(double)) == cudaSuccess &&
+               cudaMemset(*p, 0, n * sizeof(double)) == cudaSuccess;
+    };
+    const long interior = (long)c->m.N[0] * c->m.N[1] * c->m.N[2];
+    bool ok = alloc(&c->gvf[0], c->nvf) && alloc(&c->gvf[1], c->nvf) && alloc(&c->gfold, c->nvf) &&
+              alloc(&c->gD, c->ncell) && alloc(&c->gDf, c->ncell) && alloc(&c->guf, c->ncell) &&
+              alloc(&c->gvf_, c->ncell) && alloc(&c->gwf, c->ncell);
+    for (int q = 0; q < 3 && ok; ++q) ok = alloc(&c->gn[q], c->ncell) && alloc(&c->gnf[q], c->ncell);
+    ok = ok && cudaMalloc((void**)&c->list_adj, interior * sizeof(int)) == cudaSuccess;
+    if (!ok) return fail(c, SLVOF_E_NOMEM, "reverse-pass buffers");
+    return 0;
+}
+} // namespace
+
+int slvof_prepare(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(clear_err(c));
+    TRY(st_vf_ghost_inplace(c));
+    TRY(st_normals(c));
+    TRY(st_plic(c));
+    TRY(st_band(c));
+    return finish(c);
+}
+
+int slvof_copy_vf_device(slvof_ctx* c, double* d_dst)
+{
+    TRY(begin(c));
+    if (!d_dst) return fail(c, SLVOF_E_ARG, "null device pointer");
+    CK(cudaMemcpyAsync(d_dst, c->VF[c->vcur], c->nvf * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    return finish(c, false);
+}
+
+int slvof_load_vf_device(slvof_ctx* c, const double* d_src)
+{
+    TRY(begin(c));
+    if (!d_src) return fail(c, SLVOF_E_ARG, "null device pointer");
+    CK(cudaMemcpyAsync(c->VF[c->vcur], d_src, c->nvf * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    c->normals_valid = false;
+    return finish(c, false);
+}
+
+int slvof_adjoint_set_vf(slvof_ctx* c, const double* gVF)
+{
+    TRY(begin(c));
+    TRY(adj_alloc(c));
+    if (gVF) TRY(h2d(c, c->gvf[0], gVF, c->nvf * sizeof(double)));
+    else CK(cudaMemsetAsync(c->gvf[0], 0, c->nvf * sizeof(double), c->stream));
+    return finish(c, false);
+}
+
+int slvof_adjoint_get(slvof_ctx* c, double* gVF, double* guf, double* gvf, double* gwf)
+{
+    TRY(begin(c));
+    TRY(adj_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    if (gVF) TRY(d2h(c, gVF, c->gvf[0], c->nvf * sizeof(double)));
+    if (guf) TRY(d2h(c, guf, c->guf, b));
+    if (gvf) TRY(d2h(c, gvf, c->gvf_, b));
+    if (gwf) TRY(d2h(c, gwf, c->gwf, b));
+    return finish(c, false);
+}
+
+int slvof_adjoint_zero_velocity(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(adj_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    CK(cudaMemsetAsync(c->guf, 0, b, c->stream));
+    CK(cudaMemsetAsync(c->gvf_, 0, b, c->stream));
+    CK(cudaMemsetAsync(c->gwf, 0, b, c->stream));
+    return finish(c, false);
+}
+
+int slvof_adjoint_fold(slvof_ctx* c)
+{
+    TRY(begin(c));
+    TRY(adj_alloc(c));
+    launch_adjoint_fold_vf(c->m, c->gvf[0], c->gvf[1], c->nsm, c->stream);
+    std::swap(c->gvf[0], c->gvf[1]);
+    return finish(c, false);
+}
+
+int slvof_adjoint_step(slvof_ctx* c, double dt)
+{
+    TRY(begin(c));
+    TRY(adj_alloc(c));
+    if (!c->normals_valid) return fail(c, SLVOF_E_ARG, "normals/PLIC/band of the current VF are not computed (slvof_prepare)");
+    TRY(clear_err(c));
+    AdjBuffers b{};
+    b.gin = c->gvf[0];
+    b.gfold = c->gfold;
+    b.gout = c->gvf[1];
+    for (int q = 0; q < 3; ++q) { b.gn[q] = c->gn[q]; b.gnf[q] = c->gnf[q]; }
+    b.gD = c->gD;
+    b.gDf = c->gDf;
+    b.guf = c->guf;
+    b.gvf = c->gvf_;
+    b.gwf = c->gwf;
+    launch_adjoint_step(c->m, dt, c->VF[c->vcur], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->band[c->bcur],
+                        c->cand, b, c->list_adj, c->ctr + C_ADJ, c->ctr + C_ADJW, c->ctr + C_ERR, c->nsm, c->stream);
+    std::swap(c->gvf[0], c->gvf[1]);
+    return finish(c);
 }
 
 } // extern "C"

@@ -26,7 +26,7 @@ void launch_case_deformation3d(const DevMesh& m, double t, double T, double* uf,
 
 /* k_fp64.cu */
 void launch_elvira_iface64(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int* errw, int nsm, cudaStream_t s);
+                           const int* count, int* work, signed char* cand, int* errw, int nsm, cudaStream_t s);
 void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz, double* D,
                    float4* planes, signed char* phase, int* list, int* count, int nsm, cudaStream_t s);
 void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout, const double* uf, const double* vf,
@@ -36,7 +36,23 @@ void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout,
 
 /* k_mixed.cu, k_elvira_mixed.cu */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int* stats, int* errw, int nsm, cudaStream_t s);
+                           const int* count, int* work, int* stats, signed char* cand, int* errw, int nsm,
+                           cudaStream_t s);
+
+/* k_adj64.cu: reverse pass of one FP64 step (see adj64.cuh) */
+struct AdjBuffers {
+    const double* gin;  /* dL/dVF^{n+1}, VF array */
+    double* gfold;      /* gin with ghost copies folded onto their sources */
+    double* gout;       /* dL/dVF^n, VF array */
+    double *gn[3], *gD; /* dL/d(border-updated normal, D) */
+    double *gnf[3], *gDf; /* the same folded onto the border copies' sources */
+    double *guf, *gvf, *gwf; /* dL/d(face velocities), accumulated */
+};
+void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
+                         const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                         const short* band, const signed char* cand, const AdjBuffers& b, int* list, int* count,
+                         int* work, int* errw, int nsm, cudaStream_t s);
+void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s);
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
                  int* work2, int* slow_cells, float4* slow_verts, int* slow_count, double2* tet_out, int* errw,

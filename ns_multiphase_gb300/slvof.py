@@ -57,6 +57,14 @@ SYMBOLS = [
     ("slvof_case_vf_spheres", _I, [_P, _P, _P, _I, _I, _I]),
     ("slvof_case_deformation3d", _I, [_P, _D, _D]),
     ("slvof_mass_noalloc", _I, [_P, _P, _P, _P]),
+    ("slvof_prepare", _I, [_P]),
+    ("slvof_copy_vf_device", _I, [_P, _P]),
+    ("slvof_load_vf_device", _I, [_P, _P]),
+    ("slvof_adjoint_set_vf", _I, [_P, _P]),
+    ("slvof_adjoint_get", _I, [_P, _P, _P, _P, _P]),
+    ("slvof_adjoint_zero_velocity", _I, [_P]),
+    ("slvof_adjoint_step", _I, [_P, _D]),
+    ("slvof_adjoint_fold", _I, [_P]),
 ]
 
 _lib = None
@@ -237,6 +245,44 @@ class SLVOF:
             self.compute_band()
         self.compute_normal()
         self.compute_plic()
+
+    def prepare(self):
+        """Ghost fill, normals, PLIC and band of the current VF: the state a step starts from."""
+        self._check(self.L.slvof_prepare(self.h), "prepare")
+
+    def copy_vf_device(self, d_ptr: int):
+        """Copy the current VF to a caller's device buffer (VF-array sized, float64)."""
+        self._check(self.L.slvof_copy_vf_device(self.h, d_ptr), "copy_vf_device")
+
+    def load_vf_device(self, d_ptr: int):
+        """Make a caller's device buffer the current VF (then prepare() before stepping)."""
+        self._check(self.L.slvof_load_vf_device(self.h, d_ptr), "load_vf_device")
+
+    # ---- reverse pass ----------------------------------------------------------------------
+    def adjoint_set_vf(self, gVF=None):
+        """dL/dVF of the current result (VF-array shaped); None sets zero."""
+        p = None if gVF is None else _ptr(gVF, np.float64, self.mesh.vf_shape)
+        self._check(self.L.slvof_adjoint_set_vf(self.h, p), "adjoint_set_vf")
+
+    def adjoint_get(self):
+        """(dL/dVF, dL/duf, dL/dvf, dL/dwf) held by the context."""
+        m = self.mesh
+        g = m.vf_array()
+        gu, gv, gw = m.cell_array(), m.cell_array(), m.cell_array()
+        self._check(self.L.slvof_adjoint_get(self.h, g.ctypes.data, gu.ctypes.data, gv.ctypes.data, gw.ctypes.data),
+                    "adjoint_get")
+        return g, gu, gv, gw
+
+    def adjoint_zero_velocity(self):
+        self._check(self.L.slvof_adjoint_zero_velocity(self.h), "adjoint_zero_velocity")
+
+    def adjoint_step(self, dt: float):
+        """Reverse of one step(dt, band=True) from the current (prepared) state."""
+        self._check(self.L.slvof_adjoint_step(self.h, dt), "adjoint_step")
+
+    def adjoint_fold(self):
+        """Fold ghost derivatives onto the interior cells they copy."""
+        self._check(self.L.slvof_adjoint_fold(self.h), "adjoint_fold")
 
     # ---- host-buffer drop-ins (reference signatures) -------------------------------------
     def computeNormal(self, nx, ny, nz, VF):

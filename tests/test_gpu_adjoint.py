@@ -1,0 +1,210 @@
+"""The adjoint on the GPU against central finite differences of the CPU restatement.
+
+Loss L = sum_c w_c VF_c over the interior after the rollout, seeded weights w.  The GPU
+reverse pass (slvof_adjoint_step through ns_multiphase_gb300.adjoint.Rollout) gives dL/d(face
+velocities) and dL/d(initial VF); each sampled entry is compared with (L(x+h) - L(x-h))/2h,
+h = 1e-6, of the restatement's FP64 step (the reference's CPU path restated).  Velocities
+carry seeded noise on every face, as the adjoint configurations do.  Tolerance: 1e-6 relative
+to the largest sampled derivative.
+"""
+import numpy as np
+import pytest
+
+from ns_multiphase_gb300 import cases
+from ns_multiphase_gb300.mesh import Mesh
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-6
+RTOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def built():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import __graft_entry__
+    __graft_entry__.build()
+    return True
+
+
+def oracle_rollout(m, VF0, vel, dt, steps, w):
+    """L after `steps` FP64 steps of the restatement from VF0 (ghosts filled here)."""
+    o = Oracle(m)
+    VF = VF0.copy(order="F")
+    band, nx, ny, nz, D = o.init_state(VF)
+    for n in range(steps):
+        uf, vf, wf = vel(n)
+        f = o.step(dt, VF, uf, vf, wf, nx, ny, nz, D, band, True)
+        assert f == 0
+    return float(np.sum(m.interior(VF) * w))
+
+
+def gpu_gradients(m, VF0, vel, dt, steps, w, every, precision="fp64"):
+    from ns_multiphase_gb300.adjoint import Rollout
+    from ns_multiphase_gb300.slvof import SLVOF
+    g = SLVOF(m, precision)
+    g.upload_vf(VF0)
+    g.vf_ghost_fill()
+    R = Rollout(g, dt, steps, vel, every=every)
+    VFT = R.forward()
+    gT = m.vf_array()
+    m.interior(gT)[...] = w
+    gVF0, (gu, gv, gw) = R.backward(gT)
+    L = float(np.sum(m.interior(VFT) * w))
+    g.close()
+    return L, gVF0, gu, gv, gw
+
+
+def noisy(m, base, sigma, seed):
+    rng = np.random.default_rng(seed)
+    noise = [sigma * rng.standard_normal(m.cell_shape) for _ in range(3)]
+    if m.Nz == 1:
+        noise[2][...] = 0.0
+
+    def vel(n):
+        uf, vf, wf = base(n)
+        return tuple(np.asfortranarray(a + e) for a, e in zip((uf, vf, wf), noise))
+    return vel, noise
+
+
+def sample_faces(grads, count, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for q, g in enumerate(grads):
+        idx = np.argwhere(np.abs(g) > 0)
+        if len(idx) == 0:
+            continue
+        order = np.argsort(-np.abs(g[tuple(idx.T)]))
+        for p in list(order[:count // 2]) + list(rng.choice(len(idx), size=min(count // 2, len(idx)), replace=False)):
+            out.append((q, tuple(idx[p])))
+    return out
+
+
+def fd_velocity(m, VF0, noise, base, dt, steps, w, q, idx):
+    vals = []
+    for sgn in (1.0, -1.0):
+        pert = [a.copy(order="F") for a in noise]
+        pert[q][idx] += sgn * H
+
+        def vel(n):
+            uf, vf, wf = base(n)
+            return tuple(np.asfortranarray(a + e) for a, e in zip((uf, vf, wf), pert))
+        vals.append(oracle_rollout(m, VF0, vel, dt, steps, w))
+    return (vals[0] - vals[1]) / (2 * H)
+
+
+def check_velocity(m, VF0, base, noise, dt, steps, w, grads, count=12):
+    worst, scale, n = 0.0, 0.0, 0
+    picks = sample_faces(grads, count, 7)
+    fds = []
+    for q, idx in picks:
+        fds.append(fd_velocity(m, VF0, noise, base, dt, steps, w, q, idx))
+    scale = max(abs(f) for f in fds)
+    for (q, idx), fd in zip(picks, fds):
+        worst = max(worst, abs(fd - grads[q][idx]) / scale)
+        n += 1
+    return worst, n
+
+
+def sphere3d(N=12):
+    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    VF0 = cases.vf_spheres(m, np.array([[0.45, 0.52, 0.55]]), np.array([0.27]), nF=8)
+    return m, VF0
+
+
+def test_single_step_3d_velocity_gradient(built):
+    m, VF0 = sphere3d()
+    dt = 0.5 * m.dx / 2.0
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
+    vel, noise = noisy(m, base, 0.05, 31)
+    w = np.random.default_rng(2).standard_normal((m.Nx, m.Ny, m.Nz))
+    L_gpu, gVF0, gu, gv, gw = gpu_gradients(m, VF0, vel, dt, 1, w, every=1)
+    L_cpu = oracle_rollout(m, VF0, vel, dt, 1, w)
+    assert abs(L_gpu - L_cpu) <= 1e-12 * max(1.0, abs(L_cpu))
+    worst, n = check_velocity(m, VF0, base, noise, dt, 1, w, (gu, gv, gw))
+    assert n >= 12
+    assert worst <= RTOL, worst
+
+
+def test_single_step_3d_initial_vf_gradient(built):
+    m, VF0 = sphere3d()
+    # The sub-sampled sphere holds VF in multiples of 1/512, so neighbours often tie exactly:
+    # ELVIRA's +-1 components compare neighbours and its candidate errors then tie, discrete
+    # choices that a step of h flips.  Seeded jitter on the interface cells removes the ties.
+    inner = m.interior(VF0)
+    mixed = (inner > 0.02) & (inner < 0.98)
+    inner[mixed] += np.random.default_rng(8).uniform(-0.01, 0.01, size=int(mixed.sum()))
+    dt = 0.5 * m.dx / 2.0
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
+    vel, noise = noisy(m, base, 0.05, 31)
+    w = np.random.default_rng(2).standard_normal((m.Nx, m.Ny, m.Nz))
+    _, gVF0, _, _, _ = gpu_gradients(m, VF0, vel, dt, 1, w, every=1)
+    # interface cells only: a pure cell moved by h becomes an interface cell (band and ELVIRA
+    # switch), where the step is not differentiable
+    inner = m.interior(VF0)
+    cand = np.argwhere((inner > 1e-3) & (inner < 1 - 1e-3))
+    rng = np.random.default_rng(4)
+    picks = cand[rng.choice(len(cand), size=10, replace=False)]
+    fds, adj = [], []
+    for (a, b, c) in picks:
+        idx = m.vidx(a + 1, b + 1, c + 1)
+        vals = []
+        for sgn in (1.0, -1.0):
+            V = VF0.copy(order="F")
+            V[idx] += sgn * H
+            vals.append(oracle_rollout(m, V, vel, dt, 1, w))
+        fds.append((vals[0] - vals[1]) / (2 * H))
+        adj.append(gVF0[idx])
+    fds, adj = np.array(fds), np.array(adj)
+    assert np.max(np.abs(fds - adj)) <= RTOL * np.max(np.abs(fds)), (fds, adj)
+
+
+def test_rollout_2d_vortex_with_checkpoints(built):
+    """The 2D single-vortex adjoint configuration at reduced size: 32x32, circle r = 0.15 at
+    (0.5, 0.75), noise 0.05 on every face, 6 steps, VF checkpoint every 3 steps."""
+    N = 32
+    m = Mesh(Nx=N, Ny=N, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / N, CFL=0.5, zper=True)
+    VF0 = cases.vf_spheres(m, np.array([[0.5, 0.75, 0.0]]), np.array([0.15]), nF=10, dims=2)
+    dt = 0.5 * m.dx
+    base = lambda n: cases.deformation2d_faces(m, (n + 0.5) * dt, 8.0)
+    vel, noise = noisy(m, base, 0.05, 17)
+    steps = 6
+    w = np.random.default_rng(9).standard_normal((m.Nx, m.Ny, m.Nz))
+    L_gpu, gVF0, gu, gv, gw = gpu_gradients(m, VF0, vel, dt, steps, w, every=3)
+    L_cpu = oracle_rollout(m, VF0, vel, dt, steps, w)
+    assert abs(L_gpu - L_cpu) <= 1e-12 * max(1.0, abs(L_cpu))
+    worst, n = check_velocity(m, VF0, base, noise, dt, steps, w, (gu, gv, gw), count=16)
+    assert n >= 16
+    assert worst <= RTOL, worst
+
+
+def test_checkpoint_interval_does_not_change_the_gradient(built):
+    N = 24
+    m = Mesh(Nx=N, Ny=N, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / N, CFL=0.5, zper=True)
+    VF0 = cases.vf_spheres(m, np.array([[0.5, 0.6, 0.0]]), np.array([0.2]), nF=10, dims=2)
+    dt = 0.5 * m.dx
+    base = lambda n: cases.deformation2d_faces(m, (n + 0.5) * dt, 8.0)
+    vel, _ = noisy(m, base, 0.05, 5)
+    w = np.random.default_rng(1).standard_normal((m.Nx, m.Ny, m.Nz))
+    a = gpu_gradients(m, VF0, vel, dt, 5, w, every=5)
+    b = gpu_gradients(m, VF0, vel, dt, 5, w, every=2)
+    for x, y in zip(a[1:], b[1:]):
+        assert np.allclose(x, y, rtol=1e-12, atol=1e-12 * np.max(np.abs(x)))
+
+
+def test_mixed_context_runs_the_fp64_reverse(built):
+    """A mixed-precision context reverses with FP64 geometry around its own states; its
+    velocity derivative stays close to the FP64 context's."""
+    m, VF0 = sphere3d(16)
+    dt = 0.5 * m.dx / 2.0
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
+    vel, _ = noisy(m, base, 0.05, 3)
+    w = np.random.default_rng(6).standard_normal((m.Nx, m.Ny, m.Nz))
+    a = gpu_gradients(m, VF0, vel, dt, 2, w, every=1, precision="fp64")
+    b = gpu_gradients(m, VF0, vel, dt, 2, w, every=1, precision="mixed")
+    ga = np.concatenate([x.ravel() for x in a[2:]])
+    gb = np.concatenate([x.ravel() for x in b[2:]])
+    assert np.linalg.norm(ga - gb) <= 1e-2 * np.linalg.norm(ga)
