@@ -49,6 +49,7 @@ def parse():
     p.add_argument("--fp64-steps", type=int, default=3)
     p.add_argument("--drift-steps", type=int, default=8)
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--adj-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
@@ -70,10 +71,16 @@ def workload(n):
     return m, centres, radii, dt
 
 
-def make_ctx(m, centres, radii, precision, t):
+def make_ctx(m, centres, radii, precision, t, VF0=None):
+    """Context holding the workload's state: the sphere union generated on the device, or a
+    copy of an already generated VF0 (host array)."""
     from ns_multiphase_gb300.slvof import SLVOF
     g = SLVOF(m, precision)
-    g.case_vf_spheres(centres, radii, nF=20, dims=3)
+    if VF0 is None:
+        g.case_vf_spheres(centres, radii, nF=20, dims=3)
+    else:
+        g.upload_vf(VF0)
+        g.vf_ghost_fill()
     g.init_state(band=True)
     g.case_deformation3d(t, 3.0)
     return g
@@ -147,6 +154,33 @@ def timed_steps(g, dt, steps, torch):
     torch.cuda.synchronize()
     g.set_stream(None)
     return e0.elapsed_time(e1), {k: v / steps for k, v in stage.items()}
+
+
+def adjoint_timing(g, m, dt, steps, torch, fwd64_ms, fwd_mixed_ms):
+    """Reverse of one step (slvof_adjoint_step, FP64) from the context's current state, seeded
+    with dL/dVF = seeded normal weights on the interior; CUDA events on the launching stream,
+    one untimed call first.  Compared with the FP64 and the mixed forward step."""
+    gT = m.vf_array()
+    m.interior(gT)[...] = np.random.default_rng(SEED).standard_normal((m.Nx, m.Ny, m.Nz))
+    g.adjoint_set_vf(gT)
+    g.adjoint_zero_velocity()
+    g.adjoint_step(dt)
+    stream = torch.cuda.current_stream()
+    g.set_stream(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        g.adjoint_step(dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    g.set_stream(None)
+    adj = e0.elapsed_time(e1) / steps
+    return {"workload": f"{m.Nx}^3 benchmark state after the FP64 arm's steps, FP64 reverse of one step "
+                        "(recorded candidate lanes, recomputed pre-images and clip trees)",
+            "adj_ms_per_step": adj, "fwd_fp64_ms_per_step": fwd64_ms, "fwd_mixed_ms_per_step": fwd_mixed_ms,
+            "adj_over_fwd_fp64": adj / fwd64_ms, "adj_over_fwd_mixed": adj / fwd_mixed_ms,
+            "fd_check": "tests/test_gpu_adjoint.py: central differences (h=1e-6) of the CPU restatement, 1e-6 relative"}
 
 
 def cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, budget_s):
@@ -229,6 +263,7 @@ def main():
 
     # ---- mixed precision, resident (value) -----------------------------------------------
     g = make_ctx(m, centres, radii, "mixed", 0.5 * dt)
+    VF0 = g.download_vf() if rank == 0 else None
     for _ in range(args.warmup):
         g.step(dt, band=True, mass=True)
     if ws > 1:
@@ -248,8 +283,8 @@ def main():
     out = None
     if rank == 0:
         # ---- FP64 arm and mixed-vs-FP64 accuracy on the same state ------------------------
-        g64 = make_ctx(m, centres, radii, "fp64", 0.5 * dt)
-        g32 = make_ctx(m, centres, radii, "mixed", 0.5 * dt)
+        g64 = make_ctx(m, centres, radii, "fp64", 0.5 * dt, VF0)
+        g32 = make_ctx(m, centres, radii, "mixed", 0.5 * dt, VF0)
         M0 = g64.mass()
         for s in range(args.drift_steps):
             m64 = g64.step(dt)
@@ -260,6 +295,7 @@ def main():
         ms64, stage64 = timed_steps(g64, dt, args.fp64_steps, torch)
         value64 = cells * args.fp64_steps / (ms64 / 1e3)
         g32.close()
+        adjoint = adjoint_timing(g64, m, dt, args.adj_steps, torch, ms64 / args.fp64_steps, ms_step)
         VF = g64.download_vf()
         nx, ny, nz = g64.download_normals()
         D = g64.download_plic()
@@ -281,7 +317,7 @@ def main():
         tv, hvf = pinned(vf, shp)
         tw, hwf = pinned(wf, shp)
         tV, hVF = pinned(None, tuple(reversed(m.vf_shape)))
-        ge = make_ctx(m, centres, radii, "mixed", 0.5 * dt)
+        ge = make_ctx(m, centres, radii, "mixed", 0.5 * dt, VF0)
         ge.step_host(dt, huf, hvf, hwf, hVF)  # warm
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -332,6 +368,7 @@ def main():
                         "stages_ms": stage64},
                "accuracy": {"steps": args.drift_steps, "mass_rel_diff_mixed_vs_fp64": drift_vs_fp64,
                             "max_abs_dVF_mixed_vs_fp64": dVF, "mass_rel_change_fp64": abs(m64 - M0) / M0},
+               "adjoint": adjoint,
                "stages_ms": stage, "work_lists": counters, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": launches_per_step(m) * args.steps}
         print(json.dumps(out), flush=True)

@@ -18,7 +18,7 @@
  *          pi - 2 asin(sqrt((1+x)/2)) outside; pi and pi/2 carried as two-double sums.
  *   sin, cos : reduction by the nearest multiple of pi/2 (two-constant split), then the
  *          Maclaurin series of sin and cos on |r| <= pi/4 (terms through r^19 / r^18).
- * Accuracy against libm (a few ulp at most) is checked by tests/test_detmath.py.
+ * Accuracy against libm (a few ulp at most) is checked by tests/test_oracle_pins.py.
  */
 #pragma once
 
