@@ -394,6 +394,7 @@ SLVOF_HD void leaf(const CutCase* tab, const double v[4][3], double nx, double n
 struct Plic {
     const double *nx, *ny, *nz, *D;  /* donor planes (border-updated, every cell) */
     double *gnx, *gny, *gnz, *gD;    /* their derivatives, accumulated */
+    const signed char* phase;        /* +1/-1: the plane puts the whole domain on one side; may be null */
 };
 
 /* One cut level: parent vertices 0-3 and the new vertices 4-7 on the mesh plane, the
@@ -422,11 +423,89 @@ SLVOF_HD void form_child(const CutCase* tab, const Frame& F, int c, double cv[4]
     }
 }
 
+/* +1 when every one of the np points is strictly on the liquid side of the PLIC plane of
+ * every donor cell of the index box [lo, hi] (at most 2x2x2 cells), -1 when strictly on the gas
+ * side of every one, 0 otherwise.  Every cutTet leaf of a (sub-)tet with such points is then
+ * the one-tet case 1 (or 16), whatever the mesh cuts: its liquid volume is its own volume (or
+ * 0) for every nearby position of the points. */
+SLVOF_HD int points_side(const DevMesh& m, const Plic& P, const double (*v)[3], int np, const int* lo, const int* hi)
+{
+    for (int q = 0; q < 3; ++q)
+        if (hi[q] - lo[q] > 1) return 0;
+    int side = 2;
+    for (int c = lo[2]; c <= hi[2]; ++c)
+        for (int b = lo[1]; b <= hi[1]; ++b)
+            for (int a = lo[0]; a <= hi[0]; ++a) {
+                const long o = ci(m, a, b, c);
+                const double nx = ld(P.nx + o), ny = ld(P.ny + o), nz = ld(P.nz + o), D = ld(P.D + o);
+                bool neg = true, pos = true;
+                for (int n = 0; n < np; ++n) {
+                    const double d = ((nx * v[n][0] + ny * v[n][1]) + nz * v[n][2]) - D;
+                    neg = neg && d < 0.0;
+                    pos = pos && d > 0.0;
+                }
+                const int sd = neg ? 1 : (pos ? -1 : 0);
+                if (sd == 0 || (side != 2 && sd != side)) return 0;
+                side = sd;
+            }
+    return side;
+}
+
+/* The same decision from the donors' phase codes alone (pure donors whose plane puts every
+ * point of the domain on one side): +1 / -1 when every donor of the node's index box (at most
+ * 2x2x2) is pure of that phase, 0 otherwise.  Cheap (byte loads), so it is tried at every
+ * node of the clip tree. */
+SLVOF_HD int node_phase(const DevMesh& m, const Plic& P, const int ind[4][3])
+{
+    if (!P.phase || !m.fast_pure) return 0;
+    int lo[3], hi[3];
+    for (int q = 0; q < 3; ++q) {
+        lo[q] = hi[q] = ind[0][q];
+        for (int n = 1; n < 4; ++n) {
+            lo[q] = ind[n][q] < lo[q] ? ind[n][q] : lo[q];
+            hi[q] = ind[n][q] > hi[q] ? ind[n][q] : hi[q];
+        }
+        if (hi[q] - lo[q] > 1) return 0;
+    }
+    int ph = 2;
+    for (int c = lo[2]; c <= hi[2]; ++c)
+        for (int b = lo[1]; b <= hi[1]; ++b)
+            for (int a = lo[0]; a <= hi[0]; ++a) {
+                const int p = P.phase[ci(m, a, b, c)];
+                if (p == 0 || (ph != 2 && p != ph)) return 0;
+                ph = p;
+            }
+    return ph;
+}
+
+/* Whole pre-image (8 vertices, their cells) one-sided: VF is 1 (or 0) for every nearby input
+ * and the derivative of the cell's update is zero. */
+SLVOF_HD bool preimage_one_sided(const DevMesh& m, const Plic& P, const double vt[8][3], const int vind[8][3])
+{
+    if (!m.fast_pure) return false;
+    int lo[3], hi[3];
+    for (int q = 0; q < 3; ++q) {
+        lo[q] = hi[q] = vind[0][q];
+        for (int n = 1; n < 8; ++n) {
+            lo[q] = vind[n][q] < lo[q] ? vind[n][q] : lo[q];
+            hi[q] = vind[n][q] > hi[q] ? vind[n][q] : hi[q];
+        }
+    }
+    return points_side(m, P, vt, 8, lo, hi) != 0;
+}
+
+/* Leaf kinds seen by a clip, OR-ed into `kinds`: liquid and gas one-sided nodes, and PLIC
+ * leaves.  A pre-image whose leaves are all one-sided of one phase has VF = 1 (or 0) for every
+ * nearby input: its derivative is zero. */
+enum : int { LEAF_LIQ = 1, LEAF_GAS = 2, LEAF_CUT = 4 };
+
 /* cutTet (src/VFgeom.jl:713-900) of one top-level tet of a pre-image, then its reverse:
  * returns the tet's vol and vLiq, adds s * d(vLiq)/d(tet vertices) to gtet and
- * s * d(vLiq)/d(donor planes) to the plane derivatives. */
+ * s * d(vLiq)/d(donor planes) to the plane derivatives.  Nodes whose donors are all pure of
+ * one phase (node_phase) are single leaves; the summation tree therefore differs from the
+ * forward's, the value only by rounding and the derivative not at all. */
 SLVOF_HD void clip(const DevMesh& m, const CutCase* tab, const Plic& P, const double tet[4][3], const int ind[4][3],
-                   double s, Frame* st, double& vol_out, double& liq_out, double gtet[4][3], int& err)
+                   double s, Frame* st, double& vol_out, double& liq_out, double gtet[4][3], int& kinds, int& err)
 {
     double cv[4][3];
     int cind[4][3];
@@ -435,19 +514,37 @@ SLVOF_HD void clip(const DevMesh& m, const CutCase* tab, const Plic& P, const do
     int flags = 0, depth = 0, leaves = 0;
     double rvol = 0.0, rliq = 0.0, rg[4][3];
     for (;;) {
-        int dir = -1, cut = 0;
-        for (int q = 0; q < 3; ++q) {
-            if (flags & (1 << q)) continue;
-            int mx = cind[0][q], mn = cind[0][q];
-            for (int n = 1; n < 4; ++n) {
-                mx = cind[n][q] > mx ? cind[n][q] : mx;
-                mn = cind[n][q] < mn ? cind[n][q] : mn;
+        const int side = node_phase(m, P, cind);
+        if (side != 0) {
+            if (++leaves > MAX_LEAVES) {
+                err |= E_DEPTH;
+                vol_out = liq_out = 0.0;
+                for (int n = 0; n < 4; ++n) gtet[n][0] = gtet[n][1] = gtet[n][2] = 0.0;
+                return;
             }
-            if (mx > mn) { dir = q; cut = mx; break; }
-            flags |= 1 << q;
+            for (int n = 0; n < 4; ++n) rg[n][0] = rg[n][1] = rg[n][2] = 0.0;
+            rvol = tet_vol(cv[0], cv[1], cv[2], cv[3]);
+            rliq = side > 0 ? rvol : 0.0;
+            if (side > 0 && s != 0.0) tet_vol_grad(cv[0], cv[1], cv[2], cv[3], s, rg[0], rg[1], rg[2], rg[3]);
+            kinds |= side > 0 ? LEAF_LIQ : LEAF_GAS;
         }
-        if (dir >= 0 && depth == STACK) { err |= E_DEPTH; dir = -1; }
-        if (dir < 0) {
+        int dir = -1, cut = 0;
+        if (side == 0) {
+            for (int q = 0; q < 3; ++q) {
+                if (flags & (1 << q)) continue;
+                int mx = cind[0][q], mn = cind[0][q];
+                for (int n = 1; n < 4; ++n) {
+                    mx = cind[n][q] > mx ? cind[n][q] : mx;
+                    mn = cind[n][q] < mn ? cind[n][q] : mn;
+                }
+                if (mx > mn) { dir = q; cut = mx; break; }
+                flags |= 1 << q;
+            }
+            if (dir >= 0 && depth == STACK) { err |= E_DEPTH; dir = -1; }
+        }
+        if (side != 0) {
+            /* one-sided node: finished above */
+        } else if (dir < 0) {
             for (int n = 0; n < 4; ++n) rg[n][0] = rg[n][1] = rg[n][2] = 0.0;
             if (++leaves > MAX_LEAVES) {
                 err |= E_DEPTH;
@@ -458,6 +555,7 @@ SLVOF_HD void clip(const DevMesh& m, const CutCase* tab, const Plic& P, const do
             const long c = ci(m, cind[0][0], cind[0][1], cind[0][2]);
             double gpl[4] = {0.0, 0.0, 0.0, 0.0};
             leaf(tab, cv, ld(P.nx + c), ld(P.ny + c), ld(P.nz + c), ld(P.D + c), s, rvol, rliq, rg, gpl, err);
+            kinds |= LEAF_CUT;
             if (gpl[0] != 0.0) acc(P.gnx + c, gpl[0]);
             if (gpl[1] != 0.0) acc(P.gny + c, gpl[1]);
             if (gpl[2] != 0.0) acc(P.gnz + c, gpl[2]);
@@ -566,6 +664,9 @@ SLVOF_HD double sl_vertices(const DevMesh& m, const CutCase* tab, const Plic& P,
         volu += tetsign * tet_vol(vt[tet5(t, 0)], vt[tet5(t, 1)], vt[tet5(t, 2)], vt[tet5(t, 3)]);
     const double s = (g != 0.0 && volu != 0.0) ? tetsign * g / volu : 0.0;
     double vol = 0.0, vLiq = 0.0;
+    double gsum[8][3];
+    for (int n = 0; n < 8; ++n) gsum[n][0] = gsum[n][1] = gsum[n][2] = 0.0;
+    int kinds = 0;
     for (int t = 0; t < 5; ++t) {
         double tet[4][3], gtet[4][3];
         int ind[4][3];
@@ -575,15 +676,18 @@ SLVOF_HD double sl_vertices(const DevMesh& m, const CutCase* tab, const Plic& P,
                 ind[n][p] = vind[tet5(t, n)][p];
             }
         double rv, rl;
-        clip(m, tab, P, tet, ind, s, st, rv, rl, gtet, err);
+        clip(m, tab, P, tet, ind, s, st, rv, rl, gtet, kinds, err);
         vol += tetsign * rv;
         vLiq += tetsign * rl;
         for (int n = 0; n < 4; ++n)
-            for (int p = 0; p < 3; ++p) gvt[tet5(t, n)][p] += gtet[n][p];
+            for (int p = 0; p < 3; ++p) gsum[tet5(t, n)][p] += gtet[n][p];
     }
     if (!(vol > 0.0) || !std::isfinite(vol)) err |= E_VOLUME;
     const double VF = vLiq / vol;
-    if (s == 0.0) return VF;
+    /* all leaves one-sided of one phase: VF is 1 (or 0) around this input, derivative zero */
+    if (s == 0.0 || kinds == LEAF_LIQ || kinds == LEAF_GAS) return VF;
+    for (int n = 0; n < 8; ++n)
+        for (int p = 0; p < 3; ++p) gvt[n][p] += gsum[n][p];
     /* d(VF)/d(vol) part: -g VF / vol times d(vol)/d(vertices) */
     const double w = -g * VF / vol;
     for (int t = 0; t < 5; ++t) {
@@ -610,7 +714,9 @@ SLVOF_HD double sl_cell(const DevMesh& m, const CutCase* tab, const Vel& V, cons
     }
     const double VF = sl_vertices(m, tab, P, tetsign, vt, vind, g, st, gvt, err);
     if (g == 0.0) return VF;
-    for (int n = 0; n < 8; ++n) project_reverse(m, V, GV, p0[n], i, j, k, dt, gvt[n]);
+    for (int n = 0; n < 8; ++n)
+        if (gvt[n][0] != 0.0 || gvt[n][1] != 0.0 || gvt[n][2] != 0.0)
+            project_reverse(m, V, GV, p0[n], i, j, k, dt, gvt[n]);
     return VF;
 }
 

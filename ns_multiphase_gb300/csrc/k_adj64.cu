@@ -72,6 +72,37 @@ __global__ void k_adj_split(DevMesh m, const short* __restrict__ band, const dou
     }
 }
 
+/* Band cells with a nonzero incoming derivative: the FP64 pre-image (as the forward computes
+ * it); cells whose whole pre-image is strictly on one side of every donor plane it reaches have
+ * VF = 1 (or 0) around this input, hence a zero derivative, and are dropped.  The others go to
+ * the reverse kernel's list, so its warps hold only cells that clip. */
+__global__ void k_adj_pre(DevMesh m, double dt, adj::Vel V, adj::Plic P, const int* __restrict__ list,
+                          const int* __restrict__ count, int* list2, int* count2, int* errw)
+{
+    const int n = *count;
+    int err = 0;
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item - (int)(threadIdx.x & 31) < n;
+         item += gridDim.x * blockDim.x) {
+        bool keep = false;
+        int L = 0;
+        if (item < n) {
+            L = list[item];
+            const int i = 1 + L % m.N[0], j = 1 + (L / m.N[0]) % m.N[1], k = 1 + L / (m.N[0] * m.N[1]);
+            double vt[8][3];
+            int vind[8][3];
+            adj::cell_verts(m, i, j, k, vt);
+            for (int v = 0; v < 8; ++v) {
+                double x[3][3];
+                adj::project(m, V, vt[v], i, j, k, dt, x);
+                adj::pt2index(m, vind[v], vt[v], i, j, k, err);
+            }
+            keep = !adj::preimage_one_sided(m, P, vt, vind);
+        }
+        warp_append(keep, L, list2, count2);
+    }
+    if (err) atomicOr(errw, err);
+}
+
 /* Band cells: the SL update backwards (adj::sl_cell), one thread per cell. */
 __global__ void __launch_bounds__(ADJ_SL_THREADS) k_adj_sl(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV,
                                                            adj::Plic P, const double* __restrict__ gfold,
@@ -155,8 +186,8 @@ void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, i
 
 void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
-                         const short* band, const signed char* cand, const AdjBuffers& b, int* list, int* count,
-                         int* work, int* errw, int nsm, cudaStream_t s)
+                         const short* band, const signed char* cand, const signed char* phase, const AdjBuffers& b,
+                         int* list, int* count, int* list2, int* count2, int* work, int* errw, int nsm, cudaStream_t s)
 {
     const long vbytes = (long)(m.N[0] + 2 * m.g + 6) * (m.N[1] + 2 * m.g + 6) * (m.N[2] + 2 * m.g + 6) * sizeof(double);
     const long cbytes = (long)(m.N[0] + 2 * m.g) * (m.N[1] + 2 * m.g) * (m.N[2] + 2 * m.g) * sizeof(double);
@@ -164,13 +195,15 @@ void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const do
     for (int q = 0; q < 3; ++q) cudaMemsetAsync(b.gn[q], 0, cbytes, s);
     cudaMemsetAsync(b.gD, 0, cbytes, s);
     cudaMemsetAsync(count, 0, sizeof(int), s);
+    cudaMemsetAsync(count2, 0, sizeof(int), s);
     cudaMemsetAsync(work, 0, sizeof(int), s);
     k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gin, b.gfold, 1, 1);
     k_adj_split<<<nsm * 8, 256, 0, s>>>(m, band, b.gfold, b.gout, list, count);
     adj::Vel V{uf, vf, wf};
     adj::VelGrad GV{b.guf, b.gvf, b.gwf};
-    adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD};
-    k_adj_sl<<<nsm * 8, ADJ_SL_THREADS, 0, s>>>(m, dt, V, GV, P, b.gfold, list, count, work, errw);
+    adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD, phase};
+    k_adj_pre<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, list, count, list2, count2, errw);
+    k_adj_sl<<<nsm * 8, ADJ_SL_THREADS, 0, s>>>(m, dt, V, GV, P, b.gfold, list2, count2, work, errw);
     k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gD, b.gDf, 0, 0);
     k_adj_dist<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, D, b.gDf, b.gn[0], b.gn[1], b.gn[2], b.gout, errw);
     for (int q = 0; q < 3; ++q) k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gn[q], b.gnf[q], 0, 0);

@@ -47,6 +47,7 @@ struct slvof_ctx {
     double *gnf[3] = {nullptr, nullptr, nullptr}, *gDf = nullptr;
     double *guf = nullptr, *gvf_ = nullptr, *gwf = nullptr;
     int* list_adj = nullptr;
+    int* list_adj2 = nullptr;
     short* band[2] = {nullptr, nullptr};
     int bcur = 0;
     int* list_sl = nullptr;
@@ -71,7 +72,7 @@ struct slvof_ctx {
 namespace {
 
 enum { C_SL = 0, C_IF = 1, C_SLW = 2, C_IFW = 3, C_ERR = 4, C_PL = 5, C_SLOW = 6, C_SLW2 = 7, C_ARB = 8, C_ADJ = 9,
-       C_ADJW = 10, C_N = 16 };
+       C_ADJW = 10, C_ADJ2 = 11, C_N = 16 };
 
 int fail(slvof_ctx* c, int code, const std::string& msg)
 {
@@ -349,7 +350,7 @@ int slvof_destroy(slvof_ctx* c)
                     c->nz, c->D, c->planes, c->phase, c->cand, c->band[0], c->band[1], c->list_sl, c->list_if,
                     c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
-                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj};
+                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->list_adj2};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -665,7 +666,8 @@ int adj_alloc(slvof_ctx* c)
               alloc(&c->gD, c->ncell) && alloc(&c->gDf, c->ncell) && alloc(&c->guf, c->ncell) &&
               alloc(&c->gvf_, c->ncell) && alloc(&c->gwf, c->ncell);
     for (int q = 0; q < 3 && ok; ++q) ok = alloc(&c->gn[q], c->ncell) && alloc(&c->gnf[q], c->ncell);
-    ok = ok && cudaMalloc((void**)&c->list_adj, interior * sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&c->list_adj, interior * sizeof(int)) == cudaSuccess &&
+         cudaMalloc((void**)&c->list_adj2, interior * sizeof(int)) == cudaSuccess;
     if (!ok) return fail(c, SLVOF_E_NOMEM, "reverse-pass buffers");
     return 0;
 }
@@ -757,7 +759,8 @@ int slvof_adjoint_step(slvof_ctx* c, double dt)
     b.gvf = c->gvf_;
     b.gwf = c->gwf;
     launch_adjoint_step(c->m, dt, c->VF[c->vcur], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->band[c->bcur],
-                        c->cand, b, c->list_adj, c->ctr + C_ADJ, c->ctr + C_ADJW, c->ctr + C_ERR, c->nsm, c->stream);
+                        c->cand, c->phase, b, c->list_adj, c->ctr + C_ADJ, c->list_adj2, c->ctr + C_ADJ2,
+                        c->ctr + C_ADJW, c->ctr + C_ERR, c->nsm, c->stream);
     std::swap(c->gvf[0], c->gvf[1]);
     return finish(c);
 }

@@ -50,8 +50,8 @@ struct AdjBuffers {
 };
 void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
-                         const short* band, const signed char* cand, const AdjBuffers& b, int* list, int* count,
-                         int* work, int* errw, int nsm, cudaStream_t s);
+                         const short* band, const signed char* cand, const signed char* phase, const AdjBuffers& b,
+                         int* list, int* count, int* list2, int* count2, int* work, int* errw, int nsm, cudaStream_t s);
 void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s);
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,

@@ -38,7 +38,14 @@ double adjh_sl_cell(const slvof_mesh* M, double dt, int i, int j, int k, const d
     HostMesh H(M);
     adj::Vel V{uf, vf, wf};
     adj::VelGrad G{guf, gvf, gwf};
-    adj::Plic P{nx, ny, nz, D, gnx, gny, gnz, gD};
+    /* phase codes as the PLIC pass writes them: +-1 where |n|_1 <= 1 and D = +-(Lx+Ly+Lz) */
+    const long nc = H.m.cs2 * (H.m.N[2] + 2 * H.m.g);
+    std::vector<signed char> phase(nc);
+    for (long t = 0; t < nc; ++t) {
+        const double l1 = std::fabs(nx[t]) + std::fabs(ny[t]) + std::fabs(nz[t]);
+        phase[t] = (l1 <= 1.0 && D[t] == H.m.Lsum) ? 1 : ((l1 <= 1.0 && D[t] == -H.m.Lsum) ? -1 : 0);
+    }
+    adj::Plic P{nx, ny, nz, D, gnx, gny, gnz, gD, phase.data()};
     std::vector<adj::Frame> st(adj::STACK);
     int e = 0;
     const double r = adj::sl_cell(H.m, TAB, V, G, P, dt, i, j, k, g, st.data(), e);
@@ -86,9 +93,9 @@ double adjh_clip(const slvof_mesh* M, const double* tet, const int* ind, const d
     std::vector<double> sink(4 * nc, 0.0);
     adj::Plic P{nx, ny, nz, D, sink.data(), sink.data() + nc, sink.data() + 2 * nc, sink.data() + 3 * nc};
     std::vector<adj::Frame> st(adj::STACK);
-    int e = 0;
+    int e = 0, kinds = 0;
     double rv, rl;
-    adj::clip(H.m, TAB, P, t, I, s, st.data(), rv, rl, g, e);
+    adj::clip(H.m, TAB, P, t, I, s, st.data(), rv, rl, g, kinds, e);
     for (int n = 0; n < 4; ++n)
         for (int p = 0; p < 3; ++p) gtet[3 * n + p] = g[n][p];
     if (vol) *vol = rv;

@@ -102,7 +102,9 @@ def harness_grads(hlib, m, st, cell, g=1.0):
     return r, grads, err.value
 
 
-def test_sl_cell_forward_matches_restatement_bitwise(hlib, state):
+def test_sl_cell_forward_matches_restatement(hlib, state):
+    """Same pre-image and clip tree as the restatement; one-sided sub-trees are single leaves
+    in the reverse pass, so the value agrees to rounding."""
     m, o = state[0], state[1]
     _, _, VF, band, nx, ny, nz, D, uf, vf, wf, dt = state
     cells = interface_preimage_cells(m, o, state, 12)
@@ -111,7 +113,7 @@ def test_sl_cell_forward_matches_restatement_bitwise(hlib, state):
         r, _, err = harness_grads(hlib, m, state, c)
         ref, _, flags = o.sl_cell(dt, *c, uf, vf, wf, nx, ny, nz, D)
         assert err == 0 and flags == 0
-        assert r == ref, (c, r, ref)
+        assert abs(r - ref) <= 1e-14, (c, r, ref)
 
 
 def fd_sl(o, st, cell, arr, idx):
