@@ -1,0 +1,205 @@
+"""The two adjoint configurations of the SL-VOF path, with their finite-difference checks.
+
+    python -m ns_multiphase_gb300.adjoint_configs 2d [--fd 64]      # 256^2, 40 steps
+    python -m ns_multiphase_gb300.adjoint_configs 3d [--fd 16] [--precision mixed]
+
+2d: single-vortex deformation on 256x256 (Nz = 1, z periodic), circle r = 0.15 at
+    (0.5, 0.75) by 10x10 sub-sampling, stream-function face velocities (period T = 8) at
+    t_n + dt/2 plus seeded N(0, 0.05^2) noise on every face (the same noise every step), FP64,
+    40 steps with a VF checkpoint every 10.  Loss 1/2 ||VF_40 - VF_target||^2, the target from
+    the noise-free field.  The gradient is with respect to every face velocity (the noise).
+3d: Deformation3D (T = 3) on 128^3, sphere r = 0.15 at (0.35, 0.35, 0.35), plus the curl of a
+    vector potential with 8x8x8 sine modes per component (3 x 512 coefficients, N(0, 0.02^2),
+    seeded; ``cases.FourierPotential``), 30 steps with a checkpoint every 10.  Loss as above,
+    gradient with respect to the 3 x 512 coefficients (FP64 accumulation; the forward runs in
+    FP64 or mixed precision).
+
+The gradient comes from the library's reverse pass (``adjoint.Rollout``).  Finite
+differences are central, h = 1e-6, of the FP64 forward: the CPU restatement, or the FP64 GPU
+path, whose results are bit-identical to it.  The check reports the largest deviation relative
+to the largest finite difference of the checked entries.  Entries are drawn at random among
+those with a nonzero derivative (the rest are exactly zero on both sides).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import cases
+from .mesh import Mesh
+
+SEED = 20261203
+H = 1e-6
+
+
+class Config:
+    """A rollout with parameters p: vel(n, p) -> face velocities of step n."""
+
+    def __init__(self, name, mesh, VF0, dt, steps, every, base, perturb, p0, grad_of_faces):
+        self.name, self.mesh, self.VF0, self.dt = name, mesh, VF0, dt
+        self.steps, self.every = steps, every
+        self.base, self.perturb, self.p0, self.grad_of_faces = base, perturb, p0, grad_of_faces
+        self.target = None
+
+    def vel(self, n, p):
+        d = self.perturb(p)
+        return tuple(np.asfortranarray(a + e) for a, e in zip(self.base(n), d))
+
+
+def config2d(N=256, steps=40, every=10, sigma=0.05, seed=SEED):
+    m = Mesh(Nx=N, Ny=N, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / N, CFL=0.5, zper=True)
+    VF0 = cases.vf_spheres(m, np.array([[0.5, 0.75, 0.0]]), np.array([0.15]), nF=10, dims=2)
+    dt = 0.5 * m.dx  # CFL 0.5 on the vortex field (max |u| = 1)
+    base = lambda n: cases.deformation2d_faces(m, (n + 0.5) * dt, 8.0)
+    rng = np.random.default_rng(seed)
+    noise = np.stack([sigma * rng.standard_normal(m.cell_shape), sigma * rng.standard_normal(m.cell_shape),
+                      np.zeros(m.cell_shape)])
+
+    def perturb(p):
+        return p[0], p[1], p[2]
+    return Config("2d", m, VF0, dt, steps, every, base, perturb, noise, lambda gu, gv, gw: np.stack([gu, gv, gw]))
+
+
+def config3d(N=128, steps=30, every=10, sigma=0.02, modes=8, seed=SEED):
+    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    VF0 = cases.vf_spheres(m, np.array([[0.35, 0.35, 0.35]]), np.array([0.15]), nF=20)
+    F = cases.FourierPotential(m, modes)
+    C = sigma * np.random.default_rng(seed).standard_normal((3, modes, modes, modes))
+    pert = F.faces(C)
+    umax = max(np.max(np.abs(a + b)) for a, b in zip(cases.deformation3d_faces(m, 0.0, 3.0), pert))
+    dt = 0.5 * m.dx / umax  # CFL 0.5 on the perturbed field
+    base = lambda n: cases.deformation3d_faces(m, (n + 0.5) * dt, 3.0)
+    return Config("3d", m, VF0, dt, steps, every, base, F.faces, C, F.grad)
+
+
+# ---- forward evaluations -----------------------------------------------------------------
+def rollout_cpu(cfg, p):
+    """VF after the rollout by the CPU restatement (FP64)."""
+    from oracle.oracle import Oracle
+    o = Oracle(cfg.mesh)
+    VF = cfg.VF0.copy(order="F")
+    band, nx, ny, nz, D = o.init_state(VF)
+    for n in range(cfg.steps):
+        f = o.step(cfg.dt, VF, *cfg.vel(n, p), nx, ny, nz, D, band, True)
+        if f:
+            raise RuntimeError(f"restatement step {n}: error bits {f}")
+    return VF
+
+
+def rollout_gpu(cfg, p, precision="fp64"):
+    from .slvof import SLVOF
+    g = SLVOF(cfg.mesh, precision)
+    g.upload_vf(cfg.VF0)
+    g.vf_ghost_fill()
+    g.prepare()
+    for n in range(cfg.steps):
+        g.upload_velocity(*cfg.vel(n, p))
+        g.step(cfg.dt, band=True, mass=False)
+    VF = g.download_vf()
+    g.close()
+    return VF
+
+
+def loss(cfg, VF):
+    r = cfg.mesh.interior(VF) - cfg.mesh.interior(cfg.target)
+    return 0.5 * float(np.sum(r * r))
+
+
+def gradient(cfg, precision="fp64"):
+    """(loss, dL/dp, timings) by the library's reverse pass."""
+    from .adjoint import Rollout
+    from .slvof import SLVOF
+    m = cfg.mesh
+    g = SLVOF(m, precision)
+    g.upload_vf(cfg.VF0)
+    g.vf_ghost_fill()
+    R = Rollout(g, cfg.dt, cfg.steps, lambda n: cfg.vel(n, cfg.p0), every=cfg.every)
+    VFT = R.forward()
+    gT = m.vf_array()
+    m.interior(gT)[...] = m.interior(VFT) - m.interior(cfg.target)
+    _, (gu, gv, gw) = R.backward(gT)
+    g.close()
+    times = {"forward_ms": R.fwd_ms, "backward_ms": R.bwd_ms,
+             "fwd_step_ms": float(np.mean(R.fwd_step_ms)), "adj_step_ms": float(np.mean(R.adj_step_ms))}
+    return loss(cfg, VFT), cfg.grad_of_faces(gu, gv, gw), times
+
+
+def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=()):
+    """Gradient by the reverse pass against central differences on `count` entries.  `also`
+    lists further forward precisions whose gradients are compared on the same entries."""
+    evaluate = rollout_cpu if fd_backend == "cpu" else rollout_gpu
+    cfg.target = evaluate(cfg, np.zeros_like(cfg.p0))
+    L, G, times = gradient(cfg, precision)
+    others = {pr: gradient(cfg, pr) for pr in also}
+    rng = np.random.default_rng(seed)
+    support = np.argwhere(np.abs(G) > 0)
+    picks = [tuple(support[k]) for k in rng.choice(len(support), size=min(count, len(support)), replace=False)]
+    def fd_at(idx, h):
+        vals = []
+        for sgn in (1.0, -1.0):
+            p = cfg.p0.copy()
+            p[idx] += sgn * h
+            vals.append(loss(cfg, evaluate(cfg, p)))
+        return (vals[0] - vals[1]) / (2 * h)
+
+    rows = []
+    t0 = time.perf_counter()
+    for idx in picks:
+        rows.append((float(G[idx]), fd_at(idx, H)))
+    adj = np.array([r[0] for r in rows])
+    fd = np.array([r[1] for r in rows])
+    scale = float(np.max(np.abs(fd)))
+    # Entries off by more than 1e-6 of the scale: central differences again with h/8.  Where the
+    # two differ by more than the tolerance themselves, the loss is not smooth within +-h of the
+    # input (a discrete choice of the step switches there) and neither estimate is a derivative.
+    sweep = {}
+    for q, idx in enumerate(picks):
+        if scale > 0 and abs(adj[q] - fd[q]) > 1e-6 * scale:
+            sweep[q] = fd_at(idx, H / 8)
+    fd_s = time.perf_counter() - t0
+    smooth = [q for q in range(len(picks)) if q not in sweep or abs(sweep[q] - fd[q]) <= 1e-6 * scale]
+    rough = [q for q in range(len(picks)) if q not in smooth]
+    extra = {}
+    for pr, (Lp, Gp, tp) in others.items():
+        ap = np.array([float(Gp[idx]) for idx in picks])
+        extra[pr] = {"loss": Lp, "max_abs_err_over_max_fd": float(np.max(np.abs(ap - fd)) / scale) if scale > 0 else None,
+                     "rel_l2_vs_" + precision: float(np.linalg.norm(Gp - G) / np.linalg.norm(G)), "timings": tp}
+    return {"config": cfg.name, "also": extra, "grid": list(cfg.mesh.cell_shape), "steps": cfg.steps, "checkpoint_every": cfg.every,
+            "precision_forward": precision, "fd_backend": fd_backend, "h": H, "loss": L,
+            "params": int(cfg.p0.size), "support": int(len(support)), "checked": len(rows),
+            "max_abs_err_over_max_fd": float(np.max(np.abs(adj - fd)) / scale) if scale > 0 else None,
+            "smooth_entries": len(smooth),
+            "max_abs_err_over_max_fd_smooth": float(np.max(np.abs(adj[smooth] - fd[smooth])) / scale)
+            if scale > 0 and smooth else None,
+            "not_smooth": [{"index": [int(x) for x in picks[q]], "adjoint": float(adj[q]), "fd_h": float(fd[q]),
+                            "fd_h_over_8": float(sweep[q])} for q in rough],
+            "max_fd": scale, "fd_seconds": fd_s, "timings": times,
+            "entries": [{"index": [int(x) for x in idx], "adjoint": a, "fd": f, "fd_h_over_8": sweep.get(q)}
+                        for q, (idx, (a, f)) in enumerate(zip(picks, rows))]}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("config", choices=["2d", "3d"])
+    ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--every", type=int, default=10)
+    ap.add_argument("--fd", type=int, default=None)
+    ap.add_argument("--fd-backend", choices=["cpu", "gpu"], default=None)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--also", choices=["fp64", "mixed"], nargs="*", default=[])
+    a = ap.parse_args()
+    if a.config == "2d":
+        cfg = config2d(N=a.n or 256, steps=a.steps or 40, every=a.every)
+        out = check(cfg, a.fd or 64, a.fd_backend or "cpu", a.precision, also=a.also)
+    else:
+        cfg = config3d(N=a.n or 128, steps=a.steps or 30, every=a.every)
+        out = check(cfg, a.fd or 16, a.fd_backend or "gpu", a.precision, also=a.also)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -156,3 +156,75 @@ def config_spheres(n_spheres: int = 200, seed: int = 20261203):
     centres = rng.uniform(0.1, 0.9, size=(n_spheres, 3))
     radii = rng.uniform(0.02, 0.08, size=n_spheres)
     return centres, radii
+
+
+class FourierPotential:
+    """Divergence-free face velocities from the curl of a vector potential.
+
+    A_q(x, y, z) = sum_{a,b,c < M} C[q, a, b, c] / |k_abc| sin(pi (a+1) x/Lx) sin(pi (b+1) y/Ly)
+    sin(pi (c+1) z/Lz), q = x, y, z (M = 8: 3 x 512 coefficients), |k_abc| = pi sqrt((a+1)^2 +
+    (b+1)^2 + (c+1)^2): each mode scaled so that a unit coefficient gives a velocity of order
+    one (curl multiplies a mode by its wavenumber).  A vanishes on the domain
+    boundary, so curl A has no normal component there.  Each face's velocity is its flux of
+    curl A, i.e. by Stokes the circulation of A around the face's four edges (line integrals
+    of the sines, exact), over the face area: the face fluxes of every cell then sum to zero
+    exactly (each edge enters two faces with opposite signs), a discretely divergence-free
+    field.  Faces in the ghost layers use the same formula at their coordinates.
+
+    The map C -> (uf, vf, wf) is linear and separable; ``grad`` is its transpose, taking
+    dL/d(face velocities) to dL/dC.
+    """
+
+    def __init__(self, mesh: Mesh, modes: int = 8):
+        self.m = mesh
+        self.M = modes
+        L = (mesh.Lx, mesh.Ly, mesh.Lz)
+        faces = (mesh.x, mesh.y, mesh.z)
+        k = PI * np.arange(1, modes + 1)
+        # node values S[d][a, i] = sin(k_a p_i / L) at faces p_i (cell-array index i), and the
+        # edge integrals I[d][a, i] = int_{p_i}^{p_{i+1}} sin(k_a p / L) dp
+        self.S, self.I = [], []
+        for d in range(3):
+            p = np.asarray(faces[d])
+            ka = k[:, None] / L[d]
+            self.S.append(np.sin(ka * p[None, :-1]))
+            self.I.append((np.cos(ka * p[None, :-1]) - np.cos(ka * p[None, 1:])) / ka)
+        self.area = (mesh.dy * mesh.dz, mesh.dx * mesh.dz, mesh.dx * mesh.dy)
+        n = np.arange(1, modes + 1, dtype=np.float64)
+        self.W = 1.0 / (PI * np.sqrt(n[:, None, None] ** 2 + n[None, :, None] ** 2 + n[None, None, :] ** 2))
+
+    def _edge(self, C, q):
+        """Line integrals of A_q along the q-directed edges: E[i, j, k] over the cell-array
+        index ranges (the edge from node (i, j, k) one cell along q)."""
+        f = [self.I[d] if d == q else self.S[d] for d in range(3)]
+        return np.einsum("abc,ai,bj,ck->ijk", C[q] * self.W, f[0], f[1], f[2], optimize=True)
+
+    def faces(self, C):
+        """(uf, vf, wf) cell arrays (Fortran order) of curl A."""
+        Ex, Ey, Ez = (self._edge(C, q) for q in range(3))
+        sh = self.m.cell_shape
+        uf, vf, wf = np.zeros(sh), np.zeros(sh), np.zeros(sh)
+        # x-face (i, j, k): +Ey(k) - Ey(k+1) + Ez(j+1) - Ez(j)
+        uf[:, :-1, :-1] = (Ey[:, :-1, :-1] - Ey[:, :-1, 1:]) + (Ez[:, 1:, :-1] - Ez[:, :-1, :-1])
+        # y-face (i, j, k): +Ez(i) - Ez(i+1) + Ex(k+1) - Ex(k)
+        vf[:-1, :, :-1] = (Ez[:-1, :, :-1] - Ez[1:, :, :-1]) + (Ex[:-1, :, 1:] - Ex[:-1, :, :-1])
+        # z-face (i, j, k): +Ex(j) - Ex(j+1) + Ey(i+1) - Ey(i)
+        wf[:-1, :-1, :] = (Ex[:-1, :-1, :] - Ex[:-1, 1:, :]) + (Ey[1:, :-1, :] - Ey[:-1, :-1, :])
+        return tuple(np.asfortranarray(a / ar) for a, ar in zip((uf, vf, wf), self.area))
+
+    def grad(self, gu, gv, gw):
+        """dL/dC (3, M, M, M) from dL/d(uf, vf, wf): the transpose of faces()."""
+        gu, gv, gw = gu / self.area[0], gv / self.area[1], gw / self.area[2]
+        sh = self.m.cell_shape
+        gEx, gEy, gEz = np.zeros(sh), np.zeros(sh), np.zeros(sh)
+        a = gu[:, :-1, :-1]
+        gEy[:, :-1, :-1] += a; gEy[:, :-1, 1:] -= a; gEz[:, 1:, :-1] += a; gEz[:, :-1, :-1] -= a
+        b = gv[:-1, :, :-1]
+        gEz[:-1, :, :-1] += b; gEz[1:, :, :-1] -= b; gEx[:-1, :, 1:] += b; gEx[:-1, :, :-1] -= b
+        c = gw[:-1, :-1, :]
+        gEx[:-1, :-1, :] += c; gEx[:-1, 1:, :] -= c; gEy[1:, :-1, :] += c; gEy[:-1, :-1, :] -= c
+        out = np.zeros((3, self.M, self.M, self.M))
+        for q, gE in enumerate((gEx, gEy, gEz)):
+            f = [self.I[d] if d == q else self.S[d] for d in range(3)]
+            out[q] = np.einsum("ijk,ai,bj,ck->abc", gE, f[0], f[1], f[2], optimize=True) * self.W
+        return out

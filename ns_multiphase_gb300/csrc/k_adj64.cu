@@ -72,60 +72,118 @@ __global__ void k_adj_split(DevMesh m, const short* __restrict__ band, const dou
     }
 }
 
-/* Band cells with a nonzero incoming derivative: the FP64 pre-image (as the forward computes
- * it); cells whose whole pre-image is strictly on one side of every donor plane it reaches have
- * VF = 1 (or 0) around this input, hence a zero derivative, and are dropped.  The others go to
- * the reverse kernel's list, so its warps hold only cells that clip. */
+/* ---- SL reverse in three kernels ------------------------------------------------------
+ * A cell's reverse is 8 RK reverses and 5 independent tet clips; one thread per cell runs
+ * them in series and a warp waits for its slowest cell.  Instead:
+ *   k_adj_pre   thread per band cell: FP64 pre-image (as the forward computes it) and the
+ *               uncut pre-image volume; cells whose whole pre-image is strictly on one side of
+ *               every donor plane it reaches (VF = 1 or 0 around this input, zero derivative)
+ *               are dropped, the others are compacted with their vertices;
+ *   k_adj_tet   thread per (cell, tet): the tet's clip and its reverse (adj::clip), seeded with
+ *               tetsign * g / vol; results per (cell, tet);
+ *   k_adj_vert  thread per (cell, vertex): the vertex's derivative gathered from its tets in
+ *               a fixed order, the d(vol) term, and the RK reverse to the face velocities.
+ * The buffers are sized from the list counts by the host. */
 __global__ void k_adj_pre(DevMesh m, double dt, adj::Vel V, adj::Plic P, const int* __restrict__ list,
-                          const int* __restrict__ count, int* list2, int* count2, int* errw)
+                          const int* __restrict__ count, const double* __restrict__ gfold, AdjCell* cells,
+                          int* count2, int* errw)
 {
     const int n = *count;
     int err = 0;
     for (int item = blockIdx.x * blockDim.x + threadIdx.x; item - (int)(threadIdx.x & 31) < n;
          item += gridDim.x * blockDim.x) {
         bool keep = false;
-        int L = 0;
+        AdjCell r;
         if (item < n) {
-            L = list[item];
-            const int i = 1 + L % m.N[0], j = 1 + (L / m.N[0]) % m.N[1], k = 1 + L / (m.N[0] * m.N[1]);
-            double vt[8][3];
-            int vind[8][3];
-            adj::cell_verts(m, i, j, k, vt);
+            r.L = list[item];
+            const int i = 1 + r.L % m.N[0], j = 1 + (r.L / m.N[0]) % m.N[1], k = 1 + r.L / (m.N[0] * m.N[1]);
+            r.tetsign = adj::cell_verts(m, i, j, k, r.vt);
             for (int v = 0; v < 8; ++v) {
                 double x[3][3];
-                adj::project(m, V, vt[v], i, j, k, dt, x);
-                adj::pt2index(m, vind[v], vt[v], i, j, k, err);
+                adj::project(m, V, r.vt[v], i, j, k, dt, x);
+                adj::pt2index(m, r.vind[v], r.vt[v], i, j, k, err);
             }
-            keep = !adj::preimage_one_sided(m, P, vt, vind);
+            r.volu = 0.0;
+            for (int t = 0; t < 5; ++t)
+                r.volu += r.tetsign * adj::tet_vol(r.vt[tet5(t, 0)], r.vt[tet5(t, 1)], r.vt[tet5(t, 2)], r.vt[tet5(t, 3)]);
+            r.g = gfold[vidx(m, i, j, k)];
+            keep = r.volu != 0.0 && !adj::preimage_one_sided(m, P, r.vt, r.vind);
         }
-        warp_append(keep, L, list2, count2);
+        /* warp-aggregated slot in the compacted list */
+        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0 && ballot) base = atomicAdd(count2, __popc(ballot));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (keep) cells[base + __popc(ballot & ((1u << lane) - 1u))] = r;
     }
     if (err) atomicOr(errw, err);
 }
 
-/* Band cells: the SL update backwards (adj::sl_cell), one thread per cell. */
-__global__ void __launch_bounds__(ADJ_SL_THREADS) k_adj_sl(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV,
-                                                           adj::Plic P, const double* __restrict__ gfold,
-                                                           const int* __restrict__ list, const int* __restrict__ count,
-                                                           int* work, int* errw)
+__global__ void __launch_bounds__(ADJ_SL_THREADS) k_adj_tet(DevMesh m, adj::Plic P, const AdjCell* __restrict__ cells,
+                                                            const int* __restrict__ count2, AdjTet* tets, int* errw)
 {
     __shared__ CutCase s_tab[16];
     load_cut_table(s_tab);
     adj::Frame st[adj::STACK];
-    const int n = *count;
+    const long n = 5L * *count2;
     int err = 0;
-    for (;;) {
-        int item = 0;
-        const int lane = threadIdx.x & 31;
-        if (lane == 0) item = atomicAdd(work, 32);
-        item = __shfl_sync(0xffffffffu, item, 0) + lane;
-        if (item - lane >= n) break;
-        if (item < n) {
-            const int L = list[item];
-            const int i = 1 + L % m.N[0], j = 1 + (L / m.N[0]) % m.N[1], k = 1 + L / (m.N[0] * m.N[1]);
-            const double g = gfold[vidx(m, i, j, k)];
-            adj::sl_cell(m, s_tab, V, GV, P, dt, i, j, k, g, st, err);
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const AdjCell& r = cells[q / 5];
+        const int t = (int)(q % 5);
+        double tet[4][3];
+        int ind[4][3];
+        for (int v = 0; v < 4; ++v)
+            for (int p = 0; p < 3; ++p) {
+                tet[v][p] = r.vt[tet5(t, v)][p];
+                ind[v][p] = r.vind[tet5(t, v)][p];
+            }
+        const double s = r.tetsign * r.g / r.volu;
+        AdjTet o;
+        o.kinds = 0;
+        adj::clip(m, s_tab, P, tet, ind, s, st, o.rv, o.rl, o.g, o.kinds, err);
+        tets[q] = o;
+    }
+    if (err) atomicOr(errw, err);
+}
+
+__global__ void k_adj_vert(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV, const AdjCell* __restrict__ cells,
+                           const AdjTet* __restrict__ tets, const int* __restrict__ count2, int* errw)
+{
+    const long n = 8L * *count2;
+    int err = 0;
+    for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+        const long c = q / 8;
+        const int vtx = (int)(q % 8);
+        const AdjCell& r = cells[c];
+        const AdjTet* T = tets + 5 * c;
+        double vol = 0.0, vLiq = 0.0;
+        int kinds = 0;
+        for (int t = 0; t < 5; ++t) {
+            vol += r.tetsign * T[t].rv;
+            vLiq += r.tetsign * T[t].rl;
+            kinds |= T[t].kinds;
         }
+        if (!(vol > 0.0) || !isfinite(vol)) err |= adj::E_VOLUME;
+        /* all leaves one-sided of one phase: VF is 1 (or 0) around this input */
+        if (kinds == adj::LEAF_LIQ || kinds == adj::LEAF_GAS) continue;
+        const double VF = vLiq / vol;
+        const double w = -r.g * VF / vol;
+        double gp[3] = {0.0, 0.0, 0.0};
+        for (int t = 0; t < 5; ++t)
+            for (int v = 0; v < 4; ++v) {
+                if (tet5(t, v) != vtx) continue;
+                double g4[4][3] = {};
+                adj::tet_vol_grad(r.vt[tet5(t, 0)], r.vt[tet5(t, 1)], r.vt[tet5(t, 2)], r.vt[tet5(t, 3)],
+                                  w * r.tetsign, g4[0], g4[1], g4[2], g4[3]);
+                for (int p = 0; p < 3; ++p) gp[p] += T[t].g[v][p] + g4[v][p];
+            }
+        if (gp[0] == 0.0 && gp[1] == 0.0 && gp[2] == 0.0) continue;
+        const int L = r.L;
+        const int i = 1 + L % m.N[0], j = 1 + (L / m.N[0]) % m.N[1], k = 1 + L / (m.N[0] * m.N[1]);
+        double p0[8][3];
+        adj::cell_verts(m, i, j, k, p0);
+        adj::project_reverse(m, V, GV, p0[vtx], i, j, k, dt, gp);
     }
     if (err) atomicOr(errw, err);
 }
@@ -184,10 +242,8 @@ void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, i
     k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, gin, gout, 1, 1);
 }
 
-void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
-                         const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
-                         const short* band, const signed char* cand, const signed char* phase, const AdjBuffers& b,
-                         int* list, int* count, int* list2, int* count2, int* work, int* errw, int nsm, cudaStream_t s)
+void launch_adjoint_head(const DevMesh& m, const short* band, const AdjBuffers& b, int* list, int* count, int* count2,
+                         int nsm, cudaStream_t s)
 {
     const long vbytes = (long)(m.N[0] + 2 * m.g + 6) * (m.N[1] + 2 * m.g + 6) * (m.N[2] + 2 * m.g + 6) * sizeof(double);
     const long cbytes = (long)(m.N[0] + 2 * m.g) * (m.N[1] + 2 * m.g) * (m.N[2] + 2 * m.g) * sizeof(double);
@@ -196,14 +252,30 @@ void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const do
     cudaMemsetAsync(b.gD, 0, cbytes, s);
     cudaMemsetAsync(count, 0, sizeof(int), s);
     cudaMemsetAsync(count2, 0, sizeof(int), s);
-    cudaMemsetAsync(work, 0, sizeof(int), s);
     k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gin, b.gfold, 1, 1);
     k_adj_split<<<nsm * 8, 256, 0, s>>>(m, band, b.gfold, b.gout, list, count);
+}
+
+void launch_adjoint_pre(const DevMesh& m, double dt, const double* uf, const double* vf, const double* wf,
+                        const double* nx, const double* ny, const double* nz, const double* D, const signed char* phase,
+                        const AdjBuffers& b, const int* list, const int* count, int* count2, int* errw, int nsm,
+                        cudaStream_t s)
+{
+    adj::Vel V{uf, vf, wf};
+    adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD, phase};
+    k_adj_pre<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, list, count, b.gfold, b.cells, count2, errw);
+}
+
+void launch_adjoint_tail(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
+                         const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                         const signed char* cand, const signed char* phase, const AdjBuffers& b, const int* count2,
+                         int* errw, int nsm, cudaStream_t s)
+{
     adj::Vel V{uf, vf, wf};
     adj::VelGrad GV{b.guf, b.gvf, b.gwf};
     adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD, phase};
-    k_adj_pre<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, list, count, list2, count2, errw);
-    k_adj_sl<<<nsm * 8, ADJ_SL_THREADS, 0, s>>>(m, dt, V, GV, P, b.gfold, list2, count2, work, errw);
+    k_adj_tet<<<nsm * 16, ADJ_SL_THREADS, 0, s>>>(m, P, b.cells, count2, b.tets, errw);
+    k_adj_vert<<<nsm * 8, 128, 0, s>>>(m, dt, V, GV, b.cells, b.tets, count2, errw);
     k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gD, b.gDf, 0, 0);
     k_adj_dist<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, D, b.gDf, b.gn[0], b.gn[1], b.gn[2], b.gout, errw);
     for (int q = 0; q < 3; ++q) k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gn[q], b.gnf[q], 0, 0);

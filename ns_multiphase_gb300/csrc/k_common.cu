@@ -97,12 +97,19 @@ __global__ void __launch_bounds__(PURE_THREADS) k_elvira_pure(DevMesh m, const d
     }
 }
 
+/* One warp: lane l merges blocks l, l+32, ... in order, then a fixed shuffle tree (the same
+ * order every call). */
 __global__ void k_mass_final(const double* __restrict__ partials, int nblocks, double cellvol, double* out)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
     Comp a{0.0, 0.0};
-    for (int b = 0; b < nblocks; ++b) comp_merge(a, Comp{partials[2 * b], partials[2 * b + 1]});
-    out[0] = (a.s + a.c) * cellvol;
+    for (int b = lane; b < nblocks; b += 32) comp_merge(a, Comp{partials[2 * b], partials[2 * b + 1]});
+    for (int off = 16; off > 0; off >>= 1) {
+        const Comp o{__shfl_down_sync(0xffffffffu, a.s, off), __shfl_down_sync(0xffffffffu, a.c, off)};
+        comp_merge(a, o);
+    }
+    if (lane == 0) out[0] = (a.s + a.c) * cellvol;
 }
 
 /* update_borders!(nx/ny/nz) after ELVIRA! zeroed the whole arrays (src/ELVIRA.jl:11-13,50-52):
@@ -129,30 +136,78 @@ __global__ void k_normal_ghost(DevMesh m, double* nx, double* ny, double* nz)
 /* computeBand! (src/VF.jl:16-74).  The first pass marks pure cells touching the opposite
  * pure phase (Julia's combined for-loop break leaves all three loops: band 0 if any of the
  * 27 cells qualifies). */
-__global__ void k_band_first(DevMesh m, const double* __restrict__ VF, short* __restrict__ bout)
+/* Band kernels as a 3D stencil: a block owns a BX x BY tile of an x-y plane and marches up a
+ * chunk of BZ planes.  Each plane of the tile plus a one-cell halo is classified once into
+ * bits (bit 0: VF >= VFhi, bit 1: VF <= VFlo for the first pass; bit 0: |band| == n-1 for a
+ * sweep), OR-ed over its 3x3 x-y neighbourhood in shared memory, and kept for three planes;
+ * a cell's 3x3x3 test is then the OR of the three dilated planes.  Every cell value is read
+ * once per plane (plus the halo), coalesced along x. */
+constexpr int BX = 32, BY = 8, BZ = 16;
+
+/* bits of one (tile + halo) plane k into shared memory, then its x-y dilation */
+template <class Classify>
+__device__ __forceinline__ void band_plane(int i0, int j0, int k, unsigned char (*raw)[BX + 2],
+                                          unsigned char (*dil)[BX], Classify cls)
 {
-    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
-    const long total = N0 * N1 * N2;
-    const short nb1 = (short)(m.nband + 1);
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
-        const double c = VF[vidx(m, i, j, k)];
-        short b = 0;
-        if (c < m.VFlo) {
-            bool hit = false;
-            for (int kk = -1; kk <= 1; ++kk)
-                for (int jj = -1; jj <= 1; ++jj)
-                    for (int ii = -1; ii <= 1; ++ii) hit |= VF[vidx(m, i + ii, j + jj, k + kk)] >= m.VFhi;
-            b = hit ? (short)0 : (short)-nb1;
-        } else if (c > m.VFhi) {
-            bool hit = false;
-            for (int kk = -1; kk <= 1; ++kk)
-                for (int jj = -1; jj <= 1; ++jj)
-                    for (int ii = -1; ii <= 1; ++ii) hit |= VF[vidx(m, i + ii, j + jj, k + kk)] <= m.VFlo;
-            b = hit ? (short)0 : nb1;
-        }
-        bout[cidx(m, i, j, k)] = b;
+    for (int t = threadIdx.y * BX + threadIdx.x; t < (BX + 2) * (BY + 2); t += BX * BY) {
+        const int a = t % (BX + 2), b = t / (BX + 2);
+        raw[b][a] = cls(i0 - 1 + a, j0 - 1 + b, k);
     }
+    __syncthreads();
+    const int x = threadIdx.x + 1, y = threadIdx.y + 1;
+    unsigned char d = 0;
+#pragma unroll
+    for (int b = -1; b <= 1; ++b)
+#pragma unroll
+        for (int a = -1; a <= 1; ++a) d |= raw[y + b][x + a];
+    dil[threadIdx.y][threadIdx.x] = d;
+}
+
+template <class Classify, class Finish>
+__device__ __forceinline__ void band_march(const DevMesh& m, Classify cls, Finish fin)
+{
+    __shared__ unsigned char raw[BY + 2][BX + 2];
+    __shared__ unsigned char dil[3][BY][BX];
+    const int i0 = 1 + blockIdx.x * BX, j0 = 1 + blockIdx.y * BY;
+    const int kbeg = 1 + blockIdx.z * BZ, kend = min(kbeg + BZ - 1, m.N[2]);
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    /* planes kbeg-1 and kbeg */
+    band_plane(i0, j0, kbeg - 1, raw, dil[0], cls);
+    __syncthreads();
+    band_plane(i0, j0, kbeg, raw, dil[1], cls);
+    __syncthreads();
+    for (int k = kbeg; k <= kend; ++k) {
+        const int s0 = (k - kbeg) % 3, s1 = (k - kbeg + 1) % 3, s2 = (k - kbeg + 2) % 3;
+        band_plane(i0, j0, k + 1, raw, dil[s2], cls);
+        __syncthreads();
+        const unsigned char any = dil[s0][threadIdx.y][threadIdx.x] | dil[s1][threadIdx.y][threadIdx.x] |
+                                  dil[s2][threadIdx.y][threadIdx.x];
+        if (i <= m.N[0] && j <= m.N[1]) fin(i, j, k, any);
+        __syncthreads();
+    }
+}
+
+/* computeBand! first pass (src/VF.jl:16-45): pure cells next to the opposite phase (3x3x3
+ * block, the cell itself included) get 0, other pure cells +-(nband+1), interface cells 0. */
+__global__ void __launch_bounds__(BX * BY) k_band_first(DevMesh m, const double* __restrict__ VF,
+                                                       short* __restrict__ bout)
+{
+    const short nb1 = (short)(m.nband + 1);
+    auto cls = [&](int a, int b, int c) -> unsigned char {
+        /* the halo reaches index 0 and N+1 (ghost cells); beyond the tile's cells of a partial
+         * tile it stays inside the ghost layers (g >= 3) */
+        const int aa = min(a, m.N[0] + 1), bb = min(b, m.N[1] + 1);
+        const double v = __ldg(VF + vidx(m, aa, bb, c));
+        return (unsigned char)((v >= m.VFhi ? 1 : 0) | (v <= m.VFlo ? 2 : 0));
+    };
+    auto fin = [&](int i, int j, int k, unsigned char any) {
+        const double c = __ldg(VF + vidx(m, i, j, k));
+        short b = 0;
+        if (c < m.VFlo) b = (any & 1) ? (short)0 : (short)-nb1;
+        else if (c > m.VFhi) b = (any & 2) ? (short)0 : nb1;
+        bout[cidx(m, i, j, k)] = b;
+    };
+    band_march(m, cls, fin);
 }
 
 /* Neumann!(band) + update_borders!(band) (neumann=true) or update_borders!(band) alone. */
@@ -173,23 +228,20 @@ __global__ void k_band_ghost(DevMesh m, const short* __restrict__ bin, short* __
 
 /* One band sweep: |band| > n next to |band| == n-1 becomes n*sign(band).  The result does
  * not depend on the update order, so the sweep reads one buffer and writes the other. */
-__global__ void k_band_sweep(DevMesh m, const short* __restrict__ bin, short* __restrict__ bout, int n)
+__global__ void __launch_bounds__(BX * BY) k_band_sweep(DevMesh m, const short* __restrict__ bin,
+                                                       short* __restrict__ bout, int n)
 {
-    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
-    const long total = N0 * N1 * N2;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
-        const long c = cidx(m, i, j, k);
-        short b = bin[c];
-        if (abs((int)b) > n) {
-            bool hit = false;
-            for (int kk = -1; kk <= 1; ++kk)
-                for (int jj = -1; jj <= 1; ++jj)
-                    for (int ii = -1; ii <= 1; ++ii) hit |= abs((int)bin[cidx(m, i + ii, j + jj, k + kk)]) == n - 1;
-            if (hit) b = (short)(b > 0 ? n : -n);
-        }
-        bout[c] = b;
-    }
+    auto cls = [&](int a, int b, int c) -> unsigned char {
+        const int aa = min(a, m.N[0] + 1), bb = min(b, m.N[1] + 1);
+        return (unsigned char)(abs((int)bin[cidx(m, aa, bb, c)]) == n - 1 ? 1 : 0);
+    };
+    auto fin = [&](int i, int j, int k, unsigned char any) {
+        const long o = cidx(m, i, j, k);
+        short b = bin[o];
+        if (abs((int)b) > n && (any & 1)) b = (short)(b > 0 ? n : -n);
+        bout[o] = b;
+    };
+    band_march(m, cls, fin);
 }
 
 /* transport! band gate (src/Transport.jl:111,153): band cells go to the SL list, the rest
@@ -325,7 +377,8 @@ void launch_mass_final(const double* partials, int nblocks, double cellvol, doub
 }
 void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s)
 {
-    k_band_first<<<nsm * 8, 256, 0, s>>>(m, VF, bout);
+    const dim3 grid((m.N[0] + BX - 1) / BX, (m.N[1] + BY - 1) / BY, (m.N[2] + BZ - 1) / BZ);
+    k_band_first<<<grid, dim3(BX, BY), 0, s>>>(m, VF, bout);
 }
 void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neumann, int nsm, cudaStream_t s)
 {
@@ -333,7 +386,8 @@ void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neu
 }
 void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, int nsm, cudaStream_t s)
 {
-    k_band_sweep<<<nsm * 8, 256, 0, s>>>(m, bin, bout, n);
+    const dim3 grid((m.N[0] + BX - 1) / BX, (m.N[1] + BY - 1) / BY, (m.N[2] + BZ - 1) / BZ);
+    k_band_sweep<<<grid, dim3(BX, BY), 0, s>>>(m, bin, bout, n);
 }
 void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin, double* VFout, int* list, int* count,
                         int nsm, cudaStream_t s)

@@ -302,17 +302,39 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
                 if (e2 < bestE) { bestE = e2; winner = c; }
             }
         }
-        if (winner < 32 && lane == winner) {
-            double cx, cy, cz;
-            candidate64(m, s_vd[w], fam_on, winner, i, j, k, cx, cy, cz);
-            const long o = cidx(m, i, j, k);
-            nx[o] = cx; ny[o] = cy; nz[o] = cz;
-        }
-        if (cand && lane == 0) cand[cidx(m, i, j, k)] = (signed char)(winner < 32 ? winner : -1);
+        /* the winner's FP64 normal is formed by k_elvira_winner64, all lanes busy */
+        if (lane == 0) cand[cidx(m, i, j, k)] = (signed char)(winner < 32 ? winner : -1);
         __syncwarp();
     }
     if (lane == 0 && n_arb) atomicAdd(stats, n_arb);
     if (err) atomicOr(errw, err);
+}
+
+/* The chosen candidate of every interface cell re-formed from its VF block and normalised
+ * in FP64 exactly as the FP64 path forms it (src/ELVIRA.jl:72-98,112-115), one thread per
+ * cell: on GB300 the FP64 pipe is charged per warp instruction, so this runs 32 cells per
+ * instruction instead of one lane of a per-cell warp. */
+__global__ void k_elvira_winner64(DevMesh m, const double* __restrict__ VF, double* __restrict__ nx,
+                                  double* __restrict__ ny, double* __restrict__ nz, const int* __restrict__ list,
+                                  const int* __restrict__ count, const signed char* __restrict__ cand)
+{
+    const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
+    const int n = *count;
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
+        const int L = list[item];
+        const int i = 1 + L % m.N[0];
+        const int j = 1 + (L / m.N[0]) % m.N[1];
+        const int k = 1 + L / (m.N[0] * m.N[1]);
+        const long o = cidx(m, i, j, k);
+        const int c = cand[o];
+        if (c < 0) continue;
+        double sv[27];
+#pragma unroll
+        for (int q = 0; q < 27; ++q) sv[q] = __ldg(VF + vidx(m, i - 1 + q % 3, j - 1 + (q / 3) % 3, k - 1 + q / 9));
+        double cx, cy, cz;
+        candidate64(m, sv, fam_on, c, i, j, k, cx, cy, cz);
+        nx[o] = cx; ny[o] = cy; nz[o] = cz;
+    }
 }
 
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
@@ -320,6 +342,7 @@ void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, doubl
                            cudaStream_t s)
 {
     k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, stats, cand, errw);
+    k_elvira_winner64<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, list, count, cand);
 }
 
 } // namespace slvof

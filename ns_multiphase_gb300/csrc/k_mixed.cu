@@ -649,18 +649,21 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
                     if (mode == 2) nchild = S.tab[cs].ntets;
                 }
             }
-            /* children placement: cutters in lane order while they fit, keeping n slots free for
-             * the nodes that have to go back; if none fits, the first cutter finishes its node
-             * privately */
+            /* children placement: cutters in lane order while they fit.  Cutter q fits when the
+             * children of the cutters up to q, plus one slot for each later cutter (which may
+             * have to go back), fit above the remaining stack; the fitting cutters are a prefix
+             * (each cutter adds nchild - 1 >= 0 to the need), so all placements fit.  If none
+             * fits, the first cutter finishes its node privately. */
             int incl = nchild;
 #pragma unroll
             for (int off = 1; off < 32; off <<= 1) {
                 const int y = __shfl_up_sync(0xffffffffu, incl, off);
                 if (lane >= off) incl += y;
             }
-            const bool fits = mode == 2 && size + incl <= CLIPW_CAP - n;
-            const unsigned fitmask = __ballot_sync(0xffffffffu, fits);
             const unsigned cutmask = __ballot_sync(0xffffffffu, mode == 2);
+            const int later_cuts = __popc(cutmask) - __popc(cutmask & (lanemask_lt | (1u << lane)));
+            const bool fits = mode == 2 && size + incl + later_cuts <= CLIPW_CAP;
+            const unsigned fitmask = __ballot_sync(0xffffffffu, fits);
             bool back = mode == 2 && !fits;
             bool priv = false;
             if (!fitmask && cutmask && lane == __ffs(cutmask) - 1) { back = false; priv = true; }

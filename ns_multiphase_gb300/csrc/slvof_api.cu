@@ -47,7 +47,9 @@ struct slvof_ctx {
     double *gnf[3] = {nullptr, nullptr, nullptr}, *gDf = nullptr;
     double *guf = nullptr, *gvf_ = nullptr, *gwf = nullptr;
     int* list_adj = nullptr;
-    int* list_adj2 = nullptr;
+    AdjCell* adj_cells = nullptr;
+    AdjTet* adj_tets = nullptr;
+    long adj_cells_cap = 0, adj_tets_cap = 0;
     short* band[2] = {nullptr, nullptr};
     int bcur = 0;
     int* list_sl = nullptr;
@@ -350,7 +352,7 @@ int slvof_destroy(slvof_ctx* c)
                     c->nz, c->D, c->planes, c->phase, c->cand, c->band[0], c->band[1], c->list_sl, c->list_if,
                     c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
-                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->list_adj2};
+                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -666,8 +668,7 @@ int adj_alloc(slvof_ctx* c)
               alloc(&c->gD, c->ncell) && alloc(&c->gDf, c->ncell) && alloc(&c->guf, c->ncell) &&
               alloc(&c->gvf_, c->ncell) && alloc(&c->gwf, c->ncell);
     for (int q = 0; q < 3 && ok; ++q) ok = alloc(&c->gn[q], c->ncell) && alloc(&c->gnf[q], c->ncell);
-    ok = ok && cudaMalloc((void**)&c->list_adj, interior * sizeof(int)) == cudaSuccess &&
-         cudaMalloc((void**)&c->list_adj2, interior * sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&c->list_adj, interior * sizeof(int)) == cudaSuccess;
     if (!ok) return fail(c, SLVOF_E_NOMEM, "reverse-pass buffers");
     return 0;
 }
@@ -758,9 +759,36 @@ int slvof_adjoint_step(slvof_ctx* c, double dt)
     b.guf = c->guf;
     b.gvf = c->gvf_;
     b.gwf = c->gwf;
-    launch_adjoint_step(c->m, dt, c->VF[c->vcur], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->band[c->bcur],
-                        c->cand, c->phase, b, c->list_adj, c->ctr + C_ADJ, c->list_adj2, c->ctr + C_ADJ2,
-                        c->ctr + C_ADJW, c->ctr + C_ERR, c->nsm, c->stream);
+    /* head: fold, pass-through of cells outside the band, band list; its count sizes the
+     * pre-image records, the pre-pass's count the per-tet records */
+    launch_adjoint_head(c->m, c->band[c->bcur], b, c->list_adj, c->ctr + C_ADJ, c->ctr + C_ADJ2, c->nsm, c->stream);
+    int n1 = 0, n2 = 0;
+    CK(cudaMemcpyAsync(&n1, c->ctr + C_ADJ, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (n1 > c->adj_cells_cap) {
+        if (c->adj_cells) cudaFree(c->adj_cells);
+        c->adj_cells = nullptr;
+        c->adj_cells_cap = 0;
+        const long cap = n1 + n1 / 4 + 1024;
+        CK(cudaMalloc((void**)&c->adj_cells, cap * sizeof(AdjCell)));
+        c->adj_cells_cap = cap;
+    }
+    b.cells = c->adj_cells;
+    launch_adjoint_pre(c->m, dt, c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->phase, b, c->list_adj,
+                       c->ctr + C_ADJ, c->ctr + C_ADJ2, c->ctr + C_ERR, c->nsm, c->stream);
+    CK(cudaMemcpyAsync(&n2, c->ctr + C_ADJ2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (5L * n2 > c->adj_tets_cap) {
+        if (c->adj_tets) cudaFree(c->adj_tets);
+        c->adj_tets = nullptr;
+        c->adj_tets_cap = 0;
+        const long cap = 5L * (n2 + n2 / 4 + 1024);
+        CK(cudaMalloc((void**)&c->adj_tets, cap * sizeof(AdjTet)));
+        c->adj_tets_cap = cap;
+    }
+    b.tets = c->adj_tets;
+    launch_adjoint_tail(c->m, dt, c->VF[c->vcur], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->cand, c->phase, b,
+                        c->ctr + C_ADJ2, c->ctr + C_ERR, c->nsm, c->stream);
     std::swap(c->gvf[0], c->gvf[1]);
     return finish(c);
 }

@@ -40,6 +40,17 @@ void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, doubl
                            cudaStream_t s);
 
 /* k_adj64.cu: reverse pass of one FP64 step (see adj64.cuh) */
+struct AdjCell {  /* a band cell whose pre-image clips: pre-image and seed */
+    double vt[8][3];
+    int vind[8][3];
+    double tetsign, volu, g;
+    int L;
+};
+struct AdjTet {   /* one tet's clip: vol, vLiq, s * d(vLiq)/d(vertices), leaf kinds */
+    double rv, rl;
+    double g[4][3];
+    int kinds;
+};
 struct AdjBuffers {
     const double* gin;  /* dL/dVF^{n+1}, VF array */
     double* gfold;      /* gin with ghost copies folded onto their sources */
@@ -47,11 +58,21 @@ struct AdjBuffers {
     double *gn[3], *gD; /* dL/d(border-updated normal, D) */
     double *gnf[3], *gDf; /* the same folded onto the border copies' sources */
     double *guf, *gvf, *gwf; /* dL/d(face velocities), accumulated */
+    AdjCell* cells;          /* capacity: the band count of the step (head's count) */
+    AdjTet* tets;            /* capacity: 5 x the clip count (pre's count2) */
 };
-void launch_adjoint_step(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
+/* The reverse of one step in three launches; the host reads `count` after the head and
+ * `count2` after the pre-pass to size cells and tets. */
+void launch_adjoint_head(const DevMesh& m, const short* band, const AdjBuffers& b, int* list, int* count, int* count2,
+                         int nsm, cudaStream_t s);
+void launch_adjoint_pre(const DevMesh& m, double dt, const double* uf, const double* vf, const double* wf,
+                        const double* nx, const double* ny, const double* nz, const double* D, const signed char* phase,
+                        const AdjBuffers& b, const int* list, const int* count, int* count2, int* errw, int nsm,
+                        cudaStream_t s);
+void launch_adjoint_tail(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
-                         const short* band, const signed char* cand, const signed char* phase, const AdjBuffers& b,
-                         int* list, int* count, int* list2, int* count2, int* work, int* errw, int nsm, cudaStream_t s);
+                         const signed char* cand, const signed char* phase, const AdjBuffers& b, const int* count2,
+                         int* errw, int nsm, cudaStream_t s);
 void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s);
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,

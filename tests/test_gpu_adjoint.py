@@ -208,3 +208,20 @@ def test_mixed_context_runs_the_fp64_reverse(built):
     ga = np.concatenate([x.ravel() for x in a[2:]])
     gb = np.concatenate([x.ravel() for x in b[2:]])
     assert np.linalg.norm(ga - gb) <= 1e-2 * np.linalg.norm(ga)
+
+
+@pytest.mark.parametrize("which", ["2d", "3d"])
+def test_adjoint_configurations_at_reduced_size(built, which):
+    """The two adjoint configurations (ns_multiphase_gb300.adjoint_configs) at reduced size,
+    checked against central differences of the CPU restatement on random entries of the
+    derivative's support: 2D 32^2 vortex + noise on every face (8 steps, checkpoint every 3),
+    3D 16^3 deformation + curl of the 3 x 512-coefficient potential (4 steps, every 2)."""
+    from ns_multiphase_gb300 import adjoint_configs as A
+    if which == "2d":
+        cfg = A.config2d(N=32, steps=8, every=3)
+        out = A.check(cfg, 12, "cpu")
+    else:
+        cfg = A.config3d(N=16, steps=4, every=2)
+        out = A.check(cfg, 8, "cpu")
+    assert out["checked"] >= 8
+    assert out["max_abs_err_over_max_fd"] <= RTOL, out
