@@ -127,7 +127,7 @@ def gradient(cfg, precision="fp64"):
     return loss(cfg, VFT), cfg.grad_of_faces(gu, gv, gw), times
 
 
-def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=()):
+def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=(), sweep_all=False):
     """Gradient by the reverse pass against central differences on `count` entries.  `also`
     lists further forward precisions whose gradients are compared on the same entries."""
     evaluate = rollout_cpu if fd_backend == "cpu" else rollout_gpu
@@ -157,7 +157,7 @@ def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=()):
     # input (a discrete choice of the step switches there) and neither estimate is a derivative.
     sweep = {}
     for q, idx in enumerate(picks):
-        if scale > 0 and abs(adj[q] - fd[q]) > 1e-6 * scale:
+        if sweep_all or (scale > 0 and abs(adj[q] - fd[q]) > 1e-6 * scale):
             sweep[q] = fd_at(idx, H / 8)
     fd_s = time.perf_counter() - t0
     smooth = [q for q in range(len(picks)) if q not in sweep or abs(sweep[q] - fd[q]) <= 1e-6 * scale]
@@ -176,6 +176,8 @@ def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=()):
             if scale > 0 and smooth else None,
             "not_smooth": [{"index": [int(x) for x in picks[q]], "adjoint": float(adj[q]), "fd_h": float(fd[q]),
                             "fd_h_over_8": float(sweep[q])} for q in rough],
+            "max_abs_err_over_max_fd_h_over_8": float(max(abs(adj[q] - sweep[q]) for q in sweep) / scale)
+            if sweep and scale > 0 else None,
             "max_fd": scale, "fd_seconds": fd_s, "timings": times,
             "entries": [{"index": [int(x) for x in idx], "adjoint": a, "fd": f, "fd_h_over_8": sweep.get(q)}
                         for q, (idx, (a, f)) in enumerate(zip(picks, rows))]}
@@ -191,13 +193,14 @@ def main():
     ap.add_argument("--fd-backend", choices=["cpu", "gpu"], default=None)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--also", choices=["fp64", "mixed"], nargs="*", default=[])
+    ap.add_argument("--sweep-all", action="store_true", help="central differences with h/8 for every entry")
     a = ap.parse_args()
     if a.config == "2d":
         cfg = config2d(N=a.n or 256, steps=a.steps or 40, every=a.every)
-        out = check(cfg, a.fd or 64, a.fd_backend or "cpu", a.precision, also=a.also)
+        out = check(cfg, a.fd or 64, a.fd_backend or "cpu", a.precision, also=a.also, sweep_all=a.sweep_all)
     else:
         cfg = config3d(N=a.n or 128, steps=a.steps or 30, every=a.every)
-        out = check(cfg, a.fd or 16, a.fd_backend or "gpu", a.precision, also=a.also)
+        out = check(cfg, a.fd or 16, a.fd_backend or "gpu", a.precision, also=a.also, sweep_all=a.sweep_all)
     print(json.dumps(out))
 
 

@@ -123,6 +123,121 @@ __device__ __forceinline__ float cube_alpha(const Cube& q, float V)
     return a;
 }
 
+/* The same plane/cube volume and its derivative in FP64, for the plane-constant root of the
+ * mixed path: the FP32 inverse above starts FP64 Newton steps on this function. */
+struct Cube64 {
+    double m1, m2, m3, m12, i6m23, i2m3, im1;
+};
+
+__device__ __forceinline__ Cube64 make_cube64(double a, double b, double c)
+{
+    double t;
+    if (a > b) { t = a; a = b; b = t; }
+    if (b > c) { t = b; b = c; c = t; }
+    if (a > b) { t = a; a = b; b = t; }
+    Cube64 q;
+    q.m1 = a; q.m2 = b; q.m3 = c; q.m12 = a + b;
+    q.i6m23 = (b > 0.0) ? 1.0 / (6.0 * b * c) : 0.0;
+    q.i2m3 = c > 0.0 ? 0.5 / c : 0.0;
+    q.im1 = (a > 0.0) ? 1.0 / a : 0.0;
+    return q;
+}
+
+__device__ __forceinline__ void cube_lower64(const Cube64& q, double a, double& V, double& dV)
+{
+    if (a < q.m1) {
+        V = a * a * a * q.im1 * q.i6m23;
+        dV = 3.0 * a * a * q.im1 * q.i6m23;
+        return;
+    }
+    V = (3.0 * a * (a - q.m1) + q.m1 * q.m1) * q.i6m23;
+    dV = (6.0 * a - 3.0 * q.m1) * q.i6m23;
+    if (a < q.m2) return;
+    if (a < q.m12 && a < q.m3) {
+        const double b = a - q.m2;
+        V -= (b * q.im1) * b * b * q.i6m23;
+        dV -= 3.0 * (b * q.im1) * b * q.i6m23;
+        return;
+    }
+    if (q.m3 < q.m12) {
+        const double b = a - q.m2, c = a - q.m3;
+        V -= ((b * q.im1) * b * b + (c * q.im1) * c * c) * q.i6m23;
+        dV -= 3.0 * ((b * q.im1) * b + (c * q.im1) * c) * q.i6m23;
+        return;
+    }
+    V = (2.0 * a - q.m12) * q.i2m3;
+    dV = 2.0 * q.i2m3;
+}
+
+/* computeDist (src/VF.jl:109-156) with computeAlpha's inverse (src/VF.jl:164-214) taken as the
+ * FP32 closed-form inverse plus FP64 Newton steps on the exact volume: the same plane
+ * constant to within a few units of FP64 rounding, without the trigonometric branch. */
+__device__ __forceinline__ double compute_dist_newton(const DevMesh& m, int i, int j, int k, double nx, double ny,
+                                                      double nz, double VF)
+{
+    if (VF < m.VFlo) return -m.Lsum;
+    if (VF > m.VFhi) return +m.Lsum;
+    double m0 = nx * m.d[0], m1 = ny * m.d[1], m2 = nz * m.d[2];
+    const double norm = ((fabs(m0) + fabs(m1)) + fabs(m2)) + EPS64;
+    m0 = m0 / norm; m1 = m1 / norm; m2 = m2 / norm;
+    double factor = 0.0;
+    if (m0 < 0.0) factor += m0;
+    if (m1 < 0.0) factor += m1;
+    if (m2 < 0.0) factor += m2;
+    const double VFo = VF > 0.5 ? 1.0 - VF : VF;
+    const Cube64 q = make_cube64(fabs(m0), fabs(m1), fabs(m2));
+    double alpha;
+    if (q.m3 <= 0.0) {
+        alpha = 0.0; /* n = 0: computeAlpha's quadratic branch gives 0 */
+    } else if (q.m2 <= 0.0) {
+        alpha = VFo; /* plane parallel to a face: V(a) = a */
+    } else {
+        alpha = (double)cube_alpha(make_cube((float)q.m1, (float)q.m2, (float)q.m3), (float)VFo);
+        for (int it = 0; it < 3; ++it) {
+            double V, dV;
+            cube_lower64(q, alpha, V, dV);
+            if (!(dV > 0.0)) break;
+            const double step = (V - VFo) / dV;
+            alpha -= step;
+            if (fabs(step) <= 1e-17) break;
+        }
+        alpha = fmin(fmax(alpha, 0.0), 0.5);
+    }
+    alpha = VF > 0.5 ? 1.0 - alpha : alpha;
+    alpha += factor;
+    alpha -= 0.5 * ((m0 + m1) + m2);
+    double dist = alpha * norm;
+    dist += (nx * cco(m, 0, i) + ny * cco(m, 1, j)) + nz * cco(m, 2, k);
+    return dist;
+}
+
+__global__ void k_plic_iface_newton(DevMesh m, const double* __restrict__ VF, const double* __restrict__ nx,
+                                    const double* __restrict__ ny, const double* __restrict__ nz,
+                                    double* __restrict__ D, float4* __restrict__ planes,
+                                    signed char* __restrict__ phase, const int* __restrict__ list,
+                                    const int* __restrict__ count)
+{
+    const long n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g;
+    const int n = *count;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int t = list[q];
+        const int ip = (int)(t % n0) + m.lo, jp = (int)((t / n0) % n1) + m.lo, kp = (int)(t / (n0 * n1)) + m.lo;
+        const int i = ghost_src_1d(ip, m.N[0], m.g, m.per[0], false);
+        const int j = ghost_src_1d(jp, m.N[1], m.g, m.per[1], false);
+        const int k = ghost_src_1d(kp, m.N[2], m.g, m.per[2], false);
+        const long c = cidx(m, i, j, k);
+        const double dist = compute_dist_newton(m, i, j, k, nx[c], ny[c], nz[c], VF[vidx(m, i, j, k)]);
+        plic_outputs(m, t, ip, jp, kp, dist, nx, ny, nz, D, planes, phase);
+    }
+}
+
+void launch_plic_iface_newton(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz,
+                              double* D, float4* planes, signed char* phase, const int* list, const int* count,
+                              int nsm, cudaStream_t s)
+{
+    k_plic_iface_newton<<<nsm * 4, 128, 0, s>>>(m, VF, nx, ny, nz, D, planes, phase, list, count);
+}
+
 /* Candidate normal of lane (family f, outer a, inner b) from a 3x3x3 VF block; R = float
  * for the error pass, double to form candidates exactly as the FP64 path does. */
 template <class R>

@@ -88,4 +88,22 @@ __device__ __forceinline__ double plic2vf64(const CutCase* tab, const NbrGeom& G
     return VF;
 }
 
+/* The plane each cell donates with: its own border-updated normal and D.  Phase +1/-1 marks
+ * |D| = Lx+Ly+Lz with a zero or axis normal: every point of the domain and its ghosts is then
+ * strictly on one side, so a clip against the plane is all liquid (+1) or all gas (-1). */
+static __device__ __forceinline__ void plic_outputs(const DevMesh& m, long t, int ip, int jp, int kp, double dist,
+                                             const double* __restrict__ nx, const double* __restrict__ ny,
+                                             const double* __restrict__ nz, double* __restrict__ D,
+                                             float4* __restrict__ planes, signed char* __restrict__ phase)
+{
+    D[t] = dist;
+    const double a = nx[t], b = ny[t], e = nz[t];
+    const double l1 = fabs(a) + fabs(b) + fabs(e);
+    phase[t] = (l1 <= 1.0 && dist == m.Lsum) ? 1 : ((l1 <= 1.0 && dist == -m.Lsum) ? -1 : 0);
+    if (planes) {
+        const double Dl = dist - ((a * fco(m, 0, ip) + b * fco(m, 1, jp)) + e * fco(m, 2, kp));
+        planes[t] = make_float4((float)(a * m.d[0]), (float)(b * m.d[1]), (float)(e * m.d[2]), (float)Dl);
+    }
+}
+
 } // namespace slvof

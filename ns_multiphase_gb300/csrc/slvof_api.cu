@@ -172,7 +172,7 @@ int st_plic(slvof_ctx* c)
     s_beg(c, S_PLIC);
     CK(cudaMemsetAsync(c->ctr + C_PL, 0, sizeof(int), c->stream));
     launch_plic64(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->D, c->planes, c->phase, c->list_plic, c->ctr + C_PL,
-                  c->nsm, c->stream);
+                  c->precision == SLVOF_MIXED, c->nsm, c->stream);
     s_end(c, S_PLIC);
     return 0;
 }

@@ -27,8 +27,13 @@ void launch_case_deformation3d(const DevMesh& m, double t, double T, double* uf,
 /* k_fp64.cu */
 void launch_elvira_iface64(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
                            const int* count, int* work, signed char* cand, int* errw, int nsm, cudaStream_t s);
+/* newton_root: the mixed path's plane constants (FP32 inverse + FP64 Newton, k_elvira_mixed.cu);
+ * otherwise computeAlpha's closed form, bit-identical to the CPU restatement */
 void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz, double* D,
-                   float4* planes, signed char* phase, int* list, int* count, int nsm, cudaStream_t s);
+                   float4* planes, signed char* phase, int* list, int* count, bool newton_root, int nsm, cudaStream_t s);
+void launch_plic_iface_newton(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz,
+                              double* D, float4* planes, signed char* phase, const int* list, const int* count,
+                              int nsm, cudaStream_t s);
 void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout, const double* uf, const double* vf,
                  const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
                  const signed char* phase, const int* list, const int* count, int* work, int* errw, int nsm,
