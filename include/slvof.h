@@ -59,6 +59,9 @@ typedef struct slvof_mesh {
     double VFlo, VFhi, rho_liq, rho_gas;
     const double *x, *y, *z;
     const double *xm, *ym, *zm;
+    int32_t tesselation; /* param.tesselation (src/Parameters.jl:77): 5 "5_tets" (also 0), 6 "6_tets",
+                            24 "24_tets" (src/VFgeom.jl:229-332) */
+    int32_t reserved;
 } slvof_mesh;
 
 typedef struct slvof_ctx slvof_ctx;

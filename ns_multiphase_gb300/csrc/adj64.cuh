@@ -139,10 +139,11 @@ SLVOF_HD void tet_vol_grad(const double* p0, const double* p1, const double* p2,
     }
 }
 
-/* oddEvenCell + cell2verts! (src/VFgeom.jl:171-216), 5_tets; returns tetsign. */
-SLVOF_HD double cell_verts(const DevMesh& m, int i, int j, int k, double v[8][3])
+/* oddEvenCell + cell2verts! (src/VFgeom.jl:171-216); returns tetsign (odd cells are
+ * mirrored only by 5_tets). */
+SLVOF_HD double cell_verts(const DevMesh& m, int i, int j, int k, double (*v)[3])
 {
-    const bool even = ((i + j + k) % 2) == 0;
+    const bool even = tess_even(m.tess, i, j, k);
     const int ia = even ? i : i + 1, ib = even ? i + 1 : i;
     const double xs[2] = {fc(m, 0, ia), fc(m, 0, ib)};
     const double ys[2] = {fc(m, 1, j), fc(m, 1, j + 1)};
@@ -653,47 +654,69 @@ SLVOF_HD void clip(const DevMesh& m, const CutCase* tab, const Plic& P, const do
 }
 
 /* ---- one SL cell ----------------------------------------------------------------------- */
-/* VFnew of a cell from its pre-image vertices vt (cell2tets! order) and their cells, and
- * g * d(VFnew)/d(vt) added to gvt (when g != 0) plus g * d(VFnew)/d(donor planes). */
-SLVOF_HD double sl_vertices(const DevMesh& m, const CutCase* tab, const Plic& P, double tetsign, const double vt[8][3],
-                            const int vind[8][3], double g, Frame* st, double gvt[8][3], int& err)
+/* Weight of point `id` of a cell's tessellation in vertex v (0..7): 1 for the vertex itself,
+ * 1/8 for the cell's mean point, 1/4 for the mean point of a face that holds v (24_tets). */
+SLVOF_HD double point_weight(int id, int v)
 {
+    if (id == v) return 1.0;
+    if (id == 8) return 0.125;
+    if (id >= 9) {
+        const int f = id - 9;
+        for (int n = 0; n < 4; ++n)
+            if (face24(f, n) == v) return 0.25;
+    }
+    return 0.0;
+}
+
+/* VFnew of a cell from its pre-image points p (tessellation order: vertices, then for 24_tets
+ * the mean points computed from them) and their cells, and g * d(VFnew)/d(vertices) added to
+ * gvt[8] (the mean points' derivatives distributed to the vertices they average), plus
+ * g * d(VFnew)/d(donor planes). */
+SLVOF_HD double sl_vertices(const DevMesh& m, const CutCase* tab, const Plic& P, double tetsign, const double (*p)[3],
+                            const int (*pind)[3], double g, Frame* st, double gvt[8][3], int& err)
+{
+    const int tess = m.tess, nt = tess_ntets(tess);
     /* pre-image volume from the uncut tets (the pieces add up to it) */
     double volu = 0.0;
-    for (int t = 0; t < 5; ++t)
-        volu += tetsign * tet_vol(vt[tet5(t, 0)], vt[tet5(t, 1)], vt[tet5(t, 2)], vt[tet5(t, 3)]);
+    for (int t = 0; t < nt; ++t)
+        volu += tetsign * tet_vol(p[tess_tet(tess, t, 0)], p[tess_tet(tess, t, 1)], p[tess_tet(tess, t, 2)],
+                                  p[tess_tet(tess, t, 3)]);
     const double s = (g != 0.0 && volu != 0.0) ? tetsign * g / volu : 0.0;
     double vol = 0.0, vLiq = 0.0;
-    double gsum[8][3];
-    for (int n = 0; n < 8; ++n) gsum[n][0] = gsum[n][1] = gsum[n][2] = 0.0;
+    double gsum[15][3];
+    for (int n = 0; n < 15; ++n) gsum[n][0] = gsum[n][1] = gsum[n][2] = 0.0;
     int kinds = 0;
-    for (int t = 0; t < 5; ++t) {
+    for (int t = 0; t < nt; ++t) {
         double tet[4][3], gtet[4][3];
         int ind[4][3];
         for (int n = 0; n < 4; ++n)
-            for (int p = 0; p < 3; ++p) {
-                tet[n][p] = vt[tet5(t, n)][p];
-                ind[n][p] = vind[tet5(t, n)][p];
+            for (int q = 0; q < 3; ++q) {
+                tet[n][q] = p[tess_tet(tess, t, n)][q];
+                ind[n][q] = pind[tess_tet(tess, t, n)][q];
             }
         double rv, rl;
         clip(m, tab, P, tet, ind, s, st, rv, rl, gtet, kinds, err);
         vol += tetsign * rv;
         vLiq += tetsign * rl;
         for (int n = 0; n < 4; ++n)
-            for (int p = 0; p < 3; ++p) gsum[tet5(t, n)][p] += gtet[n][p];
+            for (int q = 0; q < 3; ++q) gsum[tess_tet(tess, t, n)][q] += gtet[n][q];
     }
     if (!(vol > 0.0) || !std::isfinite(vol)) err |= E_VOLUME;
     const double VF = vLiq / vol;
     /* all leaves one-sided of one phase: VF is 1 (or 0) around this input, derivative zero */
     if (s == 0.0 || kinds == LEAF_LIQ || kinds == LEAF_GAS) return VF;
-    for (int n = 0; n < 8; ++n)
-        for (int p = 0; p < 3; ++p) gvt[n][p] += gsum[n][p];
-    /* d(VF)/d(vol) part: -g VF / vol times d(vol)/d(vertices) */
+    /* d(VF)/d(vol) part: -g VF / vol times d(vol)/d(points) */
     const double w = -g * VF / vol;
-    for (int t = 0; t < 5; ++t) {
-        const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), e = tet5(t, 3);
-        tet_vol_grad(vt[a], vt[b], vt[c], vt[e], w * tetsign, gvt[a], gvt[b], gvt[c], gvt[e]);
+    for (int t = 0; t < nt; ++t) {
+        const int a = tess_tet(tess, t, 0), b = tess_tet(tess, t, 1), c = tess_tet(tess, t, 2), e = tess_tet(tess, t, 3);
+        tet_vol_grad(p[a], p[b], p[c], p[e], w * tetsign, gsum[a], gsum[b], gsum[c], gsum[e]);
     }
+    for (int id = 0; id < tess_npoints(tess); ++id)
+        for (int v = 0; v < 8; ++v) {
+            const double wgt = point_weight(id, v);
+            if (wgt != 0.0)
+                for (int q = 0; q < 3; ++q) gvt[v][q] += wgt * gsum[id][q];
+        }
     return VF;
 }
 
@@ -703,16 +726,17 @@ SLVOF_HD double sl_vertices(const DevMesh& m, const CutCase* tab, const Plic& P,
 SLVOF_HD double sl_cell(const DevMesh& m, const CutCase* tab, const Vel& V, const VelGrad& GV, const Plic& P, double dt,
                         int i, int j, int k, double g, Frame* st, int& err)
 {
-    double p0[8][3], vt[8][3], gvt[8][3];
+    double p0[8][3], p[15][3], gvt[8][3];
     const double tetsign = cell_verts(m, i, j, k, p0);
-    int vind[8][3];
+    int pind[15][3];
     for (int n = 0; n < 8; ++n) {
         double x[3][3];
-        for (int p = 0; p < 3; ++p) { vt[n][p] = p0[n][p]; gvt[n][p] = 0.0; }
-        project(m, V, vt[n], i, j, k, dt, x);
-        pt2index(m, vind[n], vt[n], i, j, k, err);
+        for (int q = 0; q < 3; ++q) { p[n][q] = p0[n][q]; gvt[n][q] = 0.0; }
+        project(m, V, p[n], i, j, k, dt, x);
     }
-    const double VF = sl_vertices(m, tab, P, tetsign, vt, vind, g, st, gvt, err);
+    tess_means<double>(m.tess, p);
+    for (int n = 0; n < tess_npoints(m.tess); ++n) pt2index(m, pind[n], p[n], i, j, k, err);
+    const double VF = sl_vertices(m, tab, P, tetsign, p, pind, g, st, gvt, err);
     if (g == 0.0) return VF;
     for (int n = 0; n < 8; ++n)
         if (gvt[n][0] != 0.0 || gvt[n][1] != 0.0 || gvt[n][2] != 0.0)
@@ -728,8 +752,20 @@ SLVOF_HD double sl_cell(const DevMesh& m, const CutCase* tab, const Vel& V, cons
 SLVOF_HD bool dist_partials(const DevMesh& m, const CutCase* tab, int i, int j, int k, double nx, double ny, double nz,
                             double D, double* dDdn, double& dDdVF, int& err)
 {
+    /* the cut-cell fraction is the exact plane/box volume whatever the tessellation: take
+     * the five tets of the cell in its 5_tets vertex order */
     double v[8][3];
-    const double tetsign = cell_verts(m, i, j, k, v);
+    const bool even = ((i + j + k) % 2) == 0;
+    {
+        const int ia = even ? i : i + 1, ib = even ? i + 1 : i;
+        for (int c = 0; c < 2; ++c)
+            for (int b = 0; b < 2; ++b)
+                for (int a = 0; a < 2; ++a) {
+                    double* q = v[a + 2 * b + 4 * c];
+                    q[0] = fc(m, 0, a ? ib : ia); q[1] = fc(m, 1, j + b); q[2] = fc(m, 2, k + c);
+                }
+    }
+    const double tetsign = even ? 1.0 : -1.0;
     const double w = tetsign / m.cellvol;
     double gpl[4] = {0.0, 0.0, 0.0, 0.0};
     for (int t = 0; t < 5; ++t) {

@@ -101,11 +101,13 @@ __global__ void k_adj_pre(DevMesh m, double dt, adj::Vel V, adj::Plic P, const i
             for (int v = 0; v < 8; ++v) {
                 double x[3][3];
                 adj::project(m, V, r.vt[v], i, j, k, dt, x);
-                adj::pt2index(m, r.vind[v], r.vt[v], i, j, k, err);
             }
+            tess_means<double>(m.tess, r.vt);
+            for (int v = 0; v < tess_npoints(m.tess); ++v) adj::pt2index(m, r.vind[v], r.vt[v], i, j, k, err);
             r.volu = 0.0;
-            for (int t = 0; t < 5; ++t)
-                r.volu += r.tetsign * adj::tet_vol(r.vt[tet5(t, 0)], r.vt[tet5(t, 1)], r.vt[tet5(t, 2)], r.vt[tet5(t, 3)]);
+            for (int t = 0; t < tess_ntets(m.tess); ++t)
+                r.volu += r.tetsign * adj::tet_vol(r.vt[tess_tet(m.tess, t, 0)], r.vt[tess_tet(m.tess, t, 1)],
+                                                   r.vt[tess_tet(m.tess, t, 2)], r.vt[tess_tet(m.tess, t, 3)]);
             r.g = gfold[vidx(m, i, j, k)];
             keep = r.volu != 0.0 && !adj::preimage_one_sided(m, P, r.vt, r.vind);
         }
@@ -126,17 +128,18 @@ __global__ void __launch_bounds__(ADJ_SL_THREADS) k_adj_tet(DevMesh m, adj::Plic
     __shared__ CutCase s_tab[16];
     load_cut_table(s_tab);
     adj::Frame st[adj::STACK];
-    const long n = 5L * *count2;
+    const int nt = tess_ntets(m.tess);
+    const long n = (long)nt * *count2;
     int err = 0;
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
-        const AdjCell& r = cells[q / 5];
-        const int t = (int)(q % 5);
+        const AdjCell& r = cells[q / nt];
+        const int t = (int)(q % nt);
         double tet[4][3];
         int ind[4][3];
         for (int v = 0; v < 4; ++v)
             for (int p = 0; p < 3; ++p) {
-                tet[v][p] = r.vt[tet5(t, v)][p];
-                ind[v][p] = r.vind[tet5(t, v)][p];
+                tet[v][p] = r.vt[tess_tet(m.tess, t, v)][p];
+                ind[v][p] = r.vind[tess_tet(m.tess, t, v)][p];
             }
         const double s = r.tetsign * r.g / r.volu;
         AdjTet o;
@@ -156,10 +159,11 @@ __global__ void k_adj_vert(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV, co
         const long c = q / 8;
         const int vtx = (int)(q % 8);
         const AdjCell& r = cells[c];
-        const AdjTet* T = tets + 5 * c;
+        const int nt = tess_ntets(m.tess);
+        const AdjTet* T = tets + (long)nt * c;
         double vol = 0.0, vLiq = 0.0;
         int kinds = 0;
-        for (int t = 0; t < 5; ++t) {
+        for (int t = 0; t < nt; ++t) {
             vol += r.tetsign * T[t].rv;
             vLiq += r.tetsign * T[t].rl;
             kinds |= T[t].kinds;
@@ -169,14 +173,19 @@ __global__ void k_adj_vert(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV, co
         if (kinds == adj::LEAF_LIQ || kinds == adj::LEAF_GAS) continue;
         const double VF = vLiq / vol;
         const double w = -r.g * VF / vol;
+        /* this vertex's derivative: from the tets that hold it, and (24_tets) a share of the
+         * derivatives of the mean points that average it */
         double gp[3] = {0.0, 0.0, 0.0};
-        for (int t = 0; t < 5; ++t)
+        for (int t = 0; t < nt; ++t)
             for (int v = 0; v < 4; ++v) {
-                if (tet5(t, v) != vtx) continue;
+                const int id = tess_tet(m.tess, t, v);
+                const double wgt = adj::point_weight(id, vtx);
+                if (wgt == 0.0) continue;
                 double g4[4][3] = {};
-                adj::tet_vol_grad(r.vt[tet5(t, 0)], r.vt[tet5(t, 1)], r.vt[tet5(t, 2)], r.vt[tet5(t, 3)],
-                                  w * r.tetsign, g4[0], g4[1], g4[2], g4[3]);
-                for (int p = 0; p < 3; ++p) gp[p] += T[t].g[v][p] + g4[v][p];
+                adj::tet_vol_grad(r.vt[tess_tet(m.tess, t, 0)], r.vt[tess_tet(m.tess, t, 1)],
+                                  r.vt[tess_tet(m.tess, t, 2)], r.vt[tess_tet(m.tess, t, 3)], w * r.tetsign, g4[0],
+                                  g4[1], g4[2], g4[3]);
+                for (int p = 0; p < 3; ++p) gp[p] += wgt * (T[t].g[v][p] + g4[v][p]);
             }
         if (gp[0] == 0.0 && gp[1] == 0.0 && gp[2] == 0.0) continue;
         const int L = r.L;

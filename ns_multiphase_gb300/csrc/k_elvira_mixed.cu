@@ -409,7 +409,10 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
                 double cx, cy, cz;
                 candidate64(m, s_vd[w], fam_on, c, i, j, k, cx, cy, cz);
                 const double dist = compute_dist64(m, i, j, k, cx, cy, cz, s_vd[w][13]);
-                const double v_ = plic2vf64(s_tab, G, s_term[w][ql], s_full[w][ql], cx, cy, cz, dist, m.cellvol, err);
+                const double v_ = m.tess == 5
+                                      ? plic2vf64(s_tab, G, s_term[w][ql], s_full[w][ql], cx, cy, cz, dist, m.cellvol, err)
+                                      : plic2vf64_gen(s_tab, m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, cx,
+                                                      cy, cz, dist, err);
                 const double r = s_vd[w][ql] - v_;
                 const double r2 = r * r;
                 double e2 = 0.0;

@@ -107,9 +107,15 @@ __global__ void __launch_bounds__(EL_WARPS * 32) k_elvira_iface64(DevMesh m, con
             const double dist = compute_dist64(m, i, j, k, cx, cy, cz, V3(0, 0, 0));
             double e2 = 0.0;
             for (int c = 0; c < 27; ++c) {
-                NbrGeom G;
-                nbr_geom(m, i - 1 + c % 3, j - 1 + (c / 3) % 3, k - 1 + c / 9, G);
-                const double v_ = plic2vf64(s_tab, G, s_term[w][c], s_full[w][c], cx, cy, cz, dist, m.cellvol, err);
+                double v_;
+                if (m.tess == 5) {
+                    NbrGeom G;
+                    nbr_geom(m, i - 1 + c % 3, j - 1 + (c / 3) % 3, k - 1 + c / 9, G);
+                    v_ = plic2vf64(s_tab, G, s_term[w][c], s_full[w][c], cx, cy, cz, dist, m.cellvol, err);
+                } else {
+                    v_ = plic2vf64_gen(s_tab, m, i - 1 + c % 3, j - 1 + (c / 3) % 3, k - 1 + c / 9, cx, cy, cz, dist,
+                                       err);
+                }
                 const double r = sv[c] - v_;
                 e2 += r * r;
             }
@@ -452,8 +458,9 @@ __device__ __forceinline__ int pure_phase(const DevMesh& m, const signed char* _
 constexpr int SL_THREADS = 128;
 
 /* SL update of one band cell: cell2tets!(project_verts=true, compute_indices=true)
- * (src/VFgeom.jl:345-420), then cutTet on the five tets and VFnew = vLiq/vol
- * (src/Transport.jl:116-145). */
+ * (src/VFgeom.jl:345-420), then cutTet on the cell's tets and VFnew = vLiq/vol
+ * (src/Transport.jl:116-145).  For 24_tets the mean points come from the projected vertices
+ * and their cells from pt2index! seeded at the cell, as verts2tets! does. */
 __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, double dt,
                                           const signed char* __restrict__ phase, double* __restrict__ VFout,
                                           const Vel64& V, const Plic64& P, int L, int& err)
@@ -461,26 +468,32 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
     const int i = 1 + L % m.N[0];
     const int j = 1 + (L / m.N[0]) % m.N[1];
     const int k = 1 + L / (m.N[0] * m.N[1]);
-    const bool even = ((i + j + k) % 2) == 0;
+    const int tess = m.tess;
+    const bool even = tess_even(tess, i, j, k);
     const double tetsign = even ? 1.0 : -1.0;
     const double X[2] = {fco(m, 0, even ? i : i + 1), fco(m, 0, even ? i + 1 : i)};
     const double Y[2] = {fco(m, 1, j), fco(m, 1, j + 1)};
     const double Z[2] = {fco(m, 2, k), fco(m, 2, k + 1)};
-    double px[8], py[8], pz[8];
-    int vi[8][3];
+    double p[15][3];
+    int vi[15][3];
 #pragma unroll 1
     for (int v = 0; v < 8; ++v) {
         double x = X[v & 1], y = Y[(v >> 1) & 1], z = Z[v >> 2];
         project64(m, V, x, y, z, i, j, k, dt);
-        px[v] = x; py[v] = y; pz[v] = z;
-        vi[v][0] = pt2index1(m, 0, x, i, err);
-        vi[v][1] = pt2index1(m, 1, y, j, err);
-        vi[v][2] = pt2index1(m, 2, z, k, err);
+        p[v][0] = x; p[v][1] = y; p[v][2] = z;
+    }
+    tess_means<double>(tess, p);
+    const int np = tess_npoints(tess), nt = tess_ntets(tess);
+#pragma unroll 1
+    for (int v = 0; v < np; ++v) {
+        vi[v][0] = pt2index1(m, 0, p[v][0], i, err);
+        vi[v][1] = pt2index1(m, 1, p[v][1], j, err);
+        vi[v][2] = pt2index1(m, 2, p[v][2], k, err);
     }
     const long out = vidx(m, i, j, k);
     if (m.fast_pure) {
         int lo0 = vi[0][0], hi0 = vi[0][0], lo1 = vi[0][1], hi1 = vi[0][1], lo2 = vi[0][2], hi2 = vi[0][2];
-        for (int v = 1; v < 8; ++v) {
+        for (int v = 1; v < np; ++v) {
             lo0 = min(lo0, vi[v][0]); hi0 = max(hi0, vi[v][0]);
             lo1 = min(lo1, vi[v][1]); hi1 = max(hi1, vi[v][1]);
             lo2 = min(lo2, vi[v][2]); hi2 = max(hi2, vi[v][2]);
@@ -488,10 +501,11 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
         const int ph = pure_phase(m, phase, lo0, hi0, lo1, hi1, lo2, hi2);
         if (ph != 0) {
             double vol = 0.0;
-            for (int t = 0; t < 5; ++t) {
-                const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), e = tet5(t, 3);
-                vol += tetsign * tet_vol(px[a], py[a], pz[a], px[b], py[b], pz[b], px[c], py[c], pz[c], px[e], py[e],
-                                         pz[e]);
+            for (int t = 0; t < nt; ++t) {
+                const int a = tess_tet(tess, t, 0), b = tess_tet(tess, t, 1), c = tess_tet(tess, t, 2),
+                          e = tess_tet(tess, t, 3);
+                vol += tetsign * tet_vol(p[a][0], p[a][1], p[a][2], p[b][0], p[b][1], p[b][2], p[c][0], p[c][1],
+                                         p[c][2], p[e][0], p[e][1], p[e][2]);
             }
             if (vol > 0.25 * m.cellvol && vol < 4.0 * m.cellvol) {
                 VFout[out] = ph > 0 ? 1.0 : 0.0;
@@ -501,12 +515,12 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
     }
     double vol = 0.0, liq = 0.0;
 #pragma unroll 1
-    for (int t = 0; t < 5; ++t) {
+    for (int t = 0; t < nt; ++t) {
         double cx[4], cy[4], cz[4];
         int ci[4][3];
         for (int n = 0; n < 4; ++n) {
-            const int v = tet5(t, n);
-            cx[n] = px[v]; cy[n] = py[v]; cz[n] = pz[v];
+            const int v = tess_tet(tess, t, n);
+            cx[n] = p[v][0]; cy[n] = p[v][1]; cz[n] = p[v][2];
             ci[n][0] = vi[v][0]; ci[n][1] = vi[v][1]; ci[n][2] = vi[v][2];
         }
         double tv, tl;

@@ -395,7 +395,7 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
             L = list[item];
             int i, j, k;
             cell_of(m, L, i, j, k);
-            const bool even = ((i + j + k) % 2) == 0;
+            const bool even = tess_even(m.tess, i, j, k);
             int rlo[3], rhi[3];
             rel_bounds(m, i, j, k, rlo, rhi);
 #pragma unroll 1
@@ -432,9 +432,31 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
         const int slot = warp_slot(slow, slow_count);
         if (slot >= 0) {
             slow_cells[slot] = L;
+            const int stride = m.tess == 24 ? 16 : 8;
             for (int v = 0; v < 8; ++v) {
                 const unsigned pk = pack3(vi[v][0], vi[v][1], vi[v][2]);
-                slow_verts[(long)slot * 8 + v] = make_float4(px[v], py[v], pz[v], __int_as_float((int)pk));
+                slow_verts[(long)slot * stride + v] = make_float4(px[v], py[v], pz[v], __int_as_float((int)pk));
+            }
+            if (m.tess == 24) {
+                /* mean points of the projected vertices (verts2tets!, src/VFgeom.jl:283-330),
+                 * their cells seeded at the cell */
+                int i, j, k, rlo[3], rhi[3];
+                cell_of(m, L, i, j, k);
+                rel_bounds(m, i, j, k, rlo, rhi);
+                for (int f = -1; f < 6; ++f) {
+                    const int nv = f < 0 ? 8 : 4;
+                    float x = 0.f, y = 0.f, z = 0.f;
+                    for (int n = 0; n < nv; ++n) {
+                        const int v = f < 0 ? n : face24(f, n);
+                        x = n == 0 ? px[v] : x + px[v];
+                        y = n == 0 ? py[v] : y + py[v];
+                        z = n == 0 ? pz[v] : z + pz[v];
+                    }
+                    x /= (float)nv; y /= (float)nv; z /= (float)nv;
+                    const unsigned pk = pack3(idx32(x, 0, rlo[0], rhi[0], err), idx32(y, 0, rlo[1], rhi[1], err),
+                                              idx32(z, 0, rlo[2], rhi[2], err));
+                    slow_verts[(long)slot * 16 + 9 + f] = make_float4(x, y, z, __int_as_float((int)pk));
+                }
             }
         }
     }
@@ -546,10 +568,12 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
     int err = 0;
     for (;;) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(work, CLIPW_BATCH);
+        /* cells per batch: every tet of the batch is seeded in one round (<= 32 lanes) */
+        const int B = m.tess == 24 ? 1 : CLIPW_BATCH;
+        if (lane == 0) base = atomicAdd(work, B);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_cells) break;
-        const int nb = min(CLIPW_BATCH, n_cells - base);
+        const int nb = min(B, n_cells - base);
         /* cell geometry of the batch (lane b holds cell b) */
         int ci_ = 0, cj_ = 0, ck_ = 0;
         if (lane < nb) cell_of(m, slow_cells[base + lane], ci_, cj_, ck_);
@@ -568,16 +592,17 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
         FF acc[CLIPW_BATCH], avol[CLIPW_BATCH];
 #pragma unroll
         for (int b = 0; b < CLIPW_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; }
-        if (lane < 5 * nb) {
-            const int b = lane / 5, t = lane - 5 * b;
+        const int ntet = tess_ntets(m.tess), stride = m.tess == 24 ? 16 : 8;
+        if (lane < ntet * nb) {
+            const int b = lane / ntet, t = lane - ntet * b;
 #pragma unroll
             for (int n = 0; n < 4; ++n) {
-                float4 q = __ldg(slow_verts + (long)(base + b) * 8 + tet5(t, n));
+                float4 q = __ldg(slow_verts + (long)(base + b) * stride + tess_tet(m.tess, t, n));
                 if (n == 0) q.w = __int_as_float((int)(wbits(q) | ((unsigned)b << 24)));
                 S.stk[w][n][lane] = q;
             }
         }
-        int size = 5 * nb;
+        int size = ntet * nb;
         __syncwarp();
         int guard = 0;
         while (size > 0) {
@@ -778,7 +803,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
                 u += __shfl_xor_sync(0xffffffffu, u, off);
             }
             if (lane == b) {
-                const double tetsign = ((ci_ + cj_ + ck_) % 2) == 0 ? 1.0 : -1.0;
+                const double tetsign = tess_even(m.tess, ci_, cj_, ck_) ? 1.0 : -1.0;
                 const double vol = tetsign * u, liq = tetsign * vl;
                 if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
                 VFout[vidx(m, ci_, cj_, ck_)] = liq / vol;

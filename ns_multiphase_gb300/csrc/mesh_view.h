@@ -32,6 +32,7 @@ struct DevMesh {
     int vlo; /* lo - 3, first VF index */
     int hi[3];
     int fast_pure; /* pure-donor shortcut valid (|coordinates| < Lx+Ly+Lz everywhere) */
+    int tess;      /* tets per cell: 5, 6 or 24 (src/VFgeom.jl:229-332) */
     double d[3];
     double VFlo, VFhi;
     double Lsum;    /* (Lx+Ly)+Lz, |D| of pure cells (src/VF.jl:116-120) */
@@ -97,6 +98,7 @@ inline void mesh_fill(const slvof_mesh* mesh, const double* coords, DevMesh& m)
     m.Lsum = (mesh->Lx + mesh->Ly) + mesh->Lz;
     m.cellvol = (mesh->dx * mesh->dy) * mesh->dz;
     m.fast_pure = maxabs < m.Lsum * (1.0 - 1e-9);
+    m.tess = mesh->tesselation == 0 ? 5 : mesh->tesselation;
     m.cs1 = nn[0]; m.cs2 = nn[0] * nn[1];
     m.vs1 = nn[0] + 6; m.vs2 = (nn[0] + 6) * (nn[1] + 6);
 }
@@ -193,6 +195,61 @@ SLVOF_HD constexpr int tet5(int t, int n)
          : (t == 2) ? (n == 0 ? 0 : n == 1 ? 4 : n == 2 ? 5 : 6)
          : (t == 3) ? (n == 0 ? 3 : n == 1 ? 6 : n == 2 ? 5 : 7)
                     : (n == 0 ? 0 : n == 1 ? 3 : n == 2 ? 6 : 5);
+}
+
+
+/* ---- tessellations (src/VFgeom.jl:171-184,229-332) --------------------------------------
+ * A cell's points, 0-based: 0..7 its vertices in cell2verts! order, 8 the mean of the
+ * vertices and 9..14 the means of its six faces (24_tets only).  Only 5_tets mirrors odd
+ * cells (oddEvenCell); 6_tets and 24_tets use the even order and tet sign +1 everywhere. */
+SLVOF_HD constexpr int tess_ntets(int tess) { return tess == 6 ? 6 : (tess == 24 ? 24 : 5); }
+SLVOF_HD constexpr int tess_npoints(int tess) { return tess == 24 ? 15 : 8; }
+SLVOF_HD constexpr bool tess_even(int tess, int i, int j, int k) { return tess != 5 || ((i + j + k) % 2) == 0; }
+
+/* face f of 24_tets as vertex ids in the order of `vts` (src/VFgeom.jl:297-302), 0-based */
+SLVOF_HD constexpr int face24(int f, int n)
+{
+    return f == 0 ? (n == 0 ? 0 : n == 1 ? 2 : n == 2 ? 6 : 4)
+         : f == 1 ? (n == 0 ? 1 : n == 1 ? 5 : n == 2 ? 7 : 3)
+         : f == 2 ? (n == 0 ? 0 : n == 1 ? 4 : n == 2 ? 5 : 1)
+         : f == 3 ? (n == 0 ? 2 : n == 1 ? 3 : n == 2 ? 7 : 6)
+         : f == 4 ? (n == 0 ? 0 : n == 1 ? 1 : n == 2 ? 3 : 2)
+                  : (n == 0 ? 4 : n == 1 ? 6 : n == 2 ? 7 : 5);
+}
+
+/* point id of vertex n of tet t */
+SLVOF_HD constexpr int tess_tet(int tess, int t, int n)
+{
+    return tess == 5 ? tet5(t, n)
+         : tess == 6 ? ((t == 0) ? (n == 0 ? 4 : n == 1 ? 5 : n == 2 ? 3 : 7)
+                      : (t == 1) ? (n == 0 ? 4 : n == 1 ? 5 : n == 2 ? 1 : 3)
+                      : (t == 2) ? (n == 0 ? 4 : n == 1 ? 1 : n == 2 ? 0 : 3)
+                      : (t == 3) ? (n == 0 ? 6 : n == 1 ? 7 : n == 2 ? 4 : 3)
+                      : (t == 4) ? (n == 0 ? 2 : n == 1 ? 3 : n == 2 ? 6 : 4)
+                                 : (n == 0 ? 0 : n == 1 ? 3 : n == 2 ? 2 : 4))
+         /* 24_tets: face f = t/4, tets (v4,v1,f,m), (v1,v2,f,m), (v2,v3,f,m), (v3,v4,f,m) */
+         : (n == 0 ? face24(t / 4, (t % 4 + 3) % 4)
+            : n == 1 ? face24(t / 4, t % 4)
+            : n == 2 ? 9 + t / 4 : 8);
+}
+
+/* Mean points of 24_tets from the vertices p[0..7], as Julia's Statistics.mean(eachcol(...))
+ * computes them: the vectors summed in order, then divided by their count. */
+template <class R>
+SLVOF_HD void tess_means(int tess, R (*p)[3])
+{
+    if (tess != 24) return;
+    for (int q = 0; q < 3; ++q) {
+        R s = p[0][q];
+        for (int n = 1; n < 8; ++n) s = s + p[n][q];
+        p[8][q] = s / R(8);
+    }
+    for (int f = 0; f < 6; ++f)
+        for (int q = 0; q < 3; ++q) {
+            R s = p[face24(f, 0)][q];
+            for (int n = 1; n < 4; ++n) s = s + p[face24(f, n)][q];
+            p[9 + f][q] = s / R(4);
+        }
 }
 
 } // namespace slvof

@@ -88,6 +88,48 @@ __device__ __forceinline__ double plic2vf64(const CutCase* tab, const NbrGeom& G
     return VF;
 }
 
+/* computePLIC2VF (src/VF.jl:219-278) for any tessellation, as the reference loops: the
+ * cell's tets (cell2tets!, means for 24_tets), d2case in place, interpolated vertices from
+ * the fixed-up distances, liquid tets from the last one down, VF += tetsign*tet_vol/cellvol.
+ * The 5_tets case has the cached form plic2vf64 above. */
+static __device__ __noinline__ double plic2vf64_gen(const CutCase* tab, const DevMesh& m, int i, int j, int k,
+                                                    double nx, double ny, double nz, double dist, int& err)
+{
+    const int tess = m.tess;
+    const bool even = tess_even(tess, i, j, k);
+    const double tetsign = even ? 1.0 : -1.0;
+    const double X[2] = {fco(m, 0, even ? i : i + 1), fco(m, 0, even ? i + 1 : i)};
+    const double Y[2] = {fco(m, 1, j), fco(m, 1, j + 1)};
+    const double Z[2] = {fco(m, 2, k), fco(m, 2, k + 1)};
+    double p[15][3];
+    for (int v = 0; v < 8; ++v) { p[v][0] = X[v & 1]; p[v][1] = Y[(v >> 1) & 1]; p[v][2] = Z[v >> 2]; }
+    tess_means<double>(tess, p);
+    double VF = 0.0;
+    for (int t = 0; t < tess_ntets(tess); ++t) {
+        double vx[8], vy[8], vz[8], d[4];
+        for (int n = 0; n < 4; ++n) {
+            const int v = tess_tet(tess, t, n);
+            vx[n] = p[v][0]; vy[n] = p[v][1]; vz[n] = p[v][2];
+            d[n] = ((nx * vx[n] + ny * vy[n]) + nz * vz[n]) - dist;
+        }
+        const int cs = d2case(d[0], d[1], d[2], d[3], EPS64, err);
+        const CutCase& C = tab[cs];
+        for (int n = 0; n < C.nvert; ++n) {
+            const int v1 = C.v1[n], v2 = C.v2[n];
+            const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
+            vx[4 + n] = (1.0 - mu) * vx[v1] + mu * vx[v2];
+            vy[4 + n] = (1.0 - mu) * vy[v1] + mu * vy[v2];
+            vz[4 + n] = (1.0 - mu) * vz[v1] + mu * vz[v2];
+        }
+        for (int n = C.ntets - 1; n >= C.nntet - 1; --n) {
+            const int a = C.vtet[n][0], b = C.vtet[n][1], c = C.vtet[n][2], e = C.vtet[n][3];
+            const double tv = tet_vol(vx[a], vy[a], vz[a], vx[b], vy[b], vz[b], vx[c], vy[c], vz[c], vx[e], vy[e], vz[e]);
+            VF += tetsign * tv / m.cellvol;
+        }
+    }
+    return VF;
+}
+
 /* The plane each cell donates with: its own border-updated normal and D.  Phase +1/-1 marks
  * |D| = Lx+Ly+Lz with a zero or axis normal: every point of the domain and its ghosts is then
  * strictly on one side, so a clip against the plane is all liquid (+1) or all gas (-1). */

@@ -280,6 +280,8 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     if (precision != SLVOF_FP64 && precision != SLVOF_MIXED) return SLVOF_E_ARG;
     if (mesh->Nx < 1 || mesh->Ny < 1 || mesh->Nz < 1 || mesh->nghost < 3) return SLVOF_E_ARG;
     if (mesh->projection < 0 || mesh->projection > 2 || mesh->nband < 0) return SLVOF_E_ARG;
+    if (mesh->tesselation != 0 && mesh->tesselation != 5 && mesh->tesselation != 6 && mesh->tesselation != 24)
+        return SLVOF_E_ARG;
     if (!mesh->x || !mesh->y || !mesh->z || !mesh->xm || !mesh->ym || !mesh->zm) return SLVOF_E_ARG;
     const long g = mesh->nghost;
     const long N[3] = {mesh->Nx, mesh->Ny, mesh->Nz};
@@ -321,7 +323,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
         ok = alloc((void**)&c->uf32, c->ncell * sizeof(float)) && alloc((void**)&c->vf32, c->ncell * sizeof(float)) &&
              alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4)) &&
              alloc((void**)&c->slow_cells, interior * sizeof(int)) &&
-             alloc((void**)&c->slow_verts, interior * 8 * sizeof(float4)) &&
+             alloc((void**)&c->slow_verts, interior * (mesh->tesselation == 24 ? 16 : 8) * sizeof(float4)) &&
              alloc((void**)&c->tet_out, interior * 5 * sizeof(double2));
     if (!ok) return bail(SLVOF_E_NOMEM);
     /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
@@ -778,11 +780,12 @@ int slvof_adjoint_step(slvof_ctx* c, double dt)
                        c->ctr + C_ADJ, c->ctr + C_ADJ2, c->ctr + C_ERR, c->nsm, c->stream);
     CK(cudaMemcpyAsync(&n2, c->ctr + C_ADJ2, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
-    if (5L * n2 > c->adj_tets_cap) {
+    const long ntet = tess_ntets(c->m.tess);
+    if (ntet * n2 > c->adj_tets_cap) {
         if (c->adj_tets) cudaFree(c->adj_tets);
         c->adj_tets = nullptr;
         c->adj_tets_cap = 0;
-        const long cap = 5L * (n2 + n2 / 4 + 1024);
+        const long cap = ntet * (n2 + n2 / 4 + 1024);
         CK(cudaMalloc((void**)&c->adj_tets, cap * sizeof(AdjTet)));
         c->adj_tets_cap = cap;
     }

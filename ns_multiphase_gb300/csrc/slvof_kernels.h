@@ -45,9 +45,9 @@ void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, doubl
                            cudaStream_t s);
 
 /* k_adj64.cu: reverse pass of one FP64 step (see adj64.cuh) */
-struct AdjCell {  /* a band cell whose pre-image clips: pre-image and seed */
-    double vt[8][3];
-    int vind[8][3];
+struct AdjCell {  /* a band cell whose pre-image clips: pre-image points and seed */
+    double vt[15][3]; /* vertices, then the mean points of 24_tets */
+    int vind[15][3];
     double tetsign, volu, g;
     int L;
 };
@@ -64,7 +64,7 @@ struct AdjBuffers {
     double *gnf[3], *gDf; /* the same folded onto the border copies' sources */
     double *guf, *gvf, *gwf; /* dL/d(face velocities), accumulated */
     AdjCell* cells;          /* capacity: the band count of the step (head's count) */
-    AdjTet* tets;            /* capacity: 5 x the clip count (pre's count2) */
+    AdjTet* tets;            /* capacity: tets per cell x the clip count (pre's count2) */
 };
 /* The reverse of one step in three launches; the host reads `count` after the head and
  * `count2` after the pre-pass to size cells and tets. */

@@ -56,7 +56,11 @@ class MeshDesc(ctypes.Structure):
         ("x", ctypes.POINTER(ctypes.c_double)), ("y", ctypes.POINTER(ctypes.c_double)),
         ("z", ctypes.POINTER(ctypes.c_double)), ("xm", ctypes.POINTER(ctypes.c_double)),
         ("ym", ctypes.POINTER(ctypes.c_double)), ("zm", ctypes.POINTER(ctypes.c_double)),
+        ("tesselation", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
+
+
+TESSELATION = {"5_tets": 5, "6_tets": 6, "24_tets": 24}
 
 
 @dataclass
@@ -78,6 +82,7 @@ class Mesh:
     VFhi: float | None = None
     nband: int | None = None
     projection: str = "RK4"
+    tesselation: str = "5_tets"
     rho_liq: float = 1.0
     rho_gas: float = 1.0
     nghost: int = field(init=False)
@@ -151,5 +156,6 @@ class Mesh:
                 PROJECTION[self.projection], int(self.xper), int(self.yper), int(self.zper),
                 self.Lx, self.Ly, self.Lz, self.dx, self.dy, self.dz,
                 self.VFlo, self.VFhi, self.rho_liq, self.rho_gas,
-                p(self.x), p(self.y), p(self.z), p(self.xm), p(self.ym), p(self.zm))
+                p(self.x), p(self.y), p(self.z), p(self.xm), p(self.ym), p(self.zm),
+                TESSELATION[self.tesselation], 0)
         return self._desc

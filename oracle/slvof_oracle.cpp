@@ -44,6 +44,8 @@ typedef struct orc_mesh {
     double VFlo, VFhi, rho_liq, rho_gas;
     const double *x, *y, *z;    /* faces, index 1-g .. N+g+1 */
     const double *xm, *ym, *zm; /* centres, index 1-g .. N+g */
+    int32_t tesselation;        /* 5, 6 or 24 (0 means 5): param.tesselation, src/Parameters.jl:77 */
+    int32_t reserved;
 } orc_mesh;
 }
 
@@ -64,8 +66,10 @@ struct Grid {
     int lo[3], hi[3];   /* cell arrays imino_..imaxo_ */
     int vlo[3], vhi[3]; /* VF array */
     long n[3], vn[3];
+    int tess;
     explicit Grid(const orc_mesh* mm) : m(mm)
     {
+        tess = mm->tesselation == 0 ? 5 : mm->tesselation;
         g = mm->nghost;
         N[0] = mm->Nx; N[1] = mm->Ny; N[2] = mm->Nz;
         for (int d = 0; d < 3; ++d) {
@@ -125,6 +129,48 @@ const int T_SIDE[16][6] = {
 
 /* 5-tet decomposition of the 8 cell vertices, src/VFgeom.jl:235-256 (1-based vertex ids). */
 const int TET5[5][4] = {{1, 2, 4, 6}, {1, 4, 3, 7}, {1, 5, 6, 7}, {4, 7, 6, 8}, {1, 4, 7, 6}};
+/* 6_tets, src/VFgeom.jl:257-282 (1-based vertex ids). */
+const int TET6[6][4] = {{5, 6, 4, 8}, {5, 6, 2, 4}, {5, 2, 1, 4}, {7, 8, 5, 4}, {3, 4, 7, 5}, {1, 4, 3, 5}};
+/* 24_tets, src/VFgeom.jl:283-330: per face (vertex ids in the order of `vts`, 1-based), four
+ * tets (v4, v1, f, m), (v1, v2, f, m), (v2, v3, f, m), (v3, v4, f, m) with f the face's mean
+ * point and m the cell's mean point. */
+const int FACE24[6][4] = {{1, 3, 7, 5}, {2, 6, 8, 4}, {1, 5, 6, 2}, {3, 4, 8, 7}, {1, 2, 4, 3}, {5, 7, 8, 6}};
+
+/* Points of a cell's tessellation, 0-based: 0..7 the vertices (cell2verts! order), 8 the mean
+ * of the vertices, 9..14 the means of the six faces (24_tets only).  Tet t of a tessellation
+ * as four point ids. */
+inline int tess_ntets(int tess) { return tess == 6 ? 6 : (tess == 24 ? 24 : 5); }
+inline void tess_tet(int tess, int t, int out[4])
+{
+    if (tess == 6) {
+        for (int n = 0; n < 4; ++n) out[n] = TET6[t][n] - 1;
+    } else if (tess == 24) {
+        const int f = t / 4, q = t % 4;
+        const int* v = FACE24[f];
+        const int a = q == 0 ? v[3] : v[q - 1], b = q == 0 ? v[0] : v[q];
+        out[0] = a - 1; out[1] = b - 1; out[2] = 9 + f; out[3] = 8;
+    } else {
+        for (int n = 0; n < 4; ++n) out[n] = TET5[t][n] - 1;
+    }
+}
+/* mean(eachcol(p)) as Julia's Statistics.mean computes it: the vectors summed in order, then
+ * divided by their count. */
+inline void tess_points(int tess, double pts[15][3])
+{
+    if (tess != 24) return;
+    for (int p = 0; p < 3; ++p) {
+        double s = pts[0][p];
+        for (int n = 1; n < 8; ++n) s = s + pts[n][p];
+        pts[8][p] = s / 8.0;
+    }
+    for (int f = 0; f < 6; ++f)
+        for (int p = 0; p < 3; ++p) {
+            double s = pts[FACE24[f][0] - 1][p];
+            for (int n = 1; n < 4; ++n) s = s + pts[FACE24[f][n] - 1][p];
+            pts[9 + f][p] = s / 4.0;
+        }
+}
+inline int tess_npoints(int tess) { return tess == 24 ? 15 : 8; }
 
 struct Err { int flags = 0; };
 enum { E_INDEX = 1, E_DEPTH = 2, E_NAN = 4, E_VOLUME = 8 };
@@ -155,10 +201,11 @@ inline int d2case(double d[4], Err* err)
 
 inline double clamp_mu(double q) { return jmin(1.0, jmax(0.0, q)); }
 
-/* oddEvenCell + cell2verts!, src/VFgeom.jl:171-216 (5_tets). verts[vertex][coord]. */
-double cell2verts(const Grid& G, int i, int j, int k, double verts[8][3])
+/* oddEvenCell + cell2verts!, src/VFgeom.jl:171-216: only 5_tets mirrors odd cells.
+ * verts[vertex][coord]. */
+double cell2verts(const Grid& G, int i, int j, int k, double verts[][3])
 {
-    const bool even = ((i + j + k) % 2) == 0;
+    const bool even = G.tess != 5 || ((i + j + k) % 2) == 0;
     const int ia = even ? i : i + 1, ib = even ? i + 1 : i;
     const double xs[2] = {G.x(ia), G.x(ib)};
     const double ys[2] = {G.y(j), G.y(j + 1)};
@@ -245,13 +292,16 @@ double compute_dist(const Grid& G, int i, int j, int k, double nx, double ny, do
 double compute_plic2vf(const Grid& G, int i, int j, int k, double nx, double ny, double nz, double dist, Err* err)
 {
     const orc_mesh* M = G.m;
-    double verts[8][3];
+    double verts[15][3];
     const double tetsign = cell2verts(G, i, j, k, verts);
+    tess_points(G.tess, verts);
     double VF = 0.0;
-    for (int t = 0; t < 5; ++t) {
+    for (int t = 0; t < tess_ntets(G.tess); ++t) {
         double vert[8][3];
+        int tv[4];
+        tess_tet(G.tess, t, tv);
         for (int n = 0; n < 4; ++n)
-            for (int p = 0; p < 3; ++p) vert[n][p] = verts[TET5[t][n] - 1][p];
+            for (int p = 0; p < 3; ++p) vert[n][p] = verts[tv[n]][p];
         double d[4];
         for (int n = 0; n < 4; ++n) d[n] = ((nx * vert[n][0] + ny * vert[n][1]) + nz * vert[n][2]) - dist;
         const int cs = d2case(d, err) - 1;
@@ -627,19 +677,24 @@ CutOut cut_tet(const Grid& G, const Plic& P, double tet[4][3], int ind[4][3], bo
  * compute_indices=true) (src/VFgeom.jl:345-420). Returns VFnew. */
 double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out)
 {
-    double verts[8][3];
+    double verts[15][3];
     const double tetsign = cell2verts(G, i, j, k, verts);
     for (int n = 0; n < 8; ++n) project(G, V, verts[n], i, j, k, dt);
-    int vInds[8][3];
-    for (int n = 0; n < 8; ++n) pt2index(G, vInds[n], verts[n], i, j, k, e);
+    /* 24_tets: mean points of the projected vertices, their cells seeded at the cell
+     * (verts2tets! inside cell2tets!, src/VFgeom.jl:283-330,402-406) */
+    tess_points(G.tess, verts);
+    int vInds[15][3];
+    for (int n = 0; n < tess_npoints(G.tess); ++n) pt2index(G, vInds[n], verts[n], i, j, k, e);
     double vol = 0.0, vLiq = 0.0;
-    for (int t = 0; t < 5; ++t) {
+    for (int t = 0; t < tess_ntets(G.tess); ++t) {
         double tet[4][3];
         int ind[4][3];
+        int tv[4];
+        tess_tet(G.tess, t, tv);
         for (int n = 0; n < 4; ++n)
             for (int p = 0; p < 3; ++p) {
-                tet[n][p] = verts[TET5[t][n] - 1][p];
-                ind[n][p] = vInds[TET5[t][n] - 1][p];
+                tet[n][p] = verts[tv[n]][p];
+                ind[n][p] = vInds[tv[n]][p];
             }
         const CutOut r = cut_tet(G, P, tet, ind, false, false, false, 1, e);
         vol += tetsign * r.vol;

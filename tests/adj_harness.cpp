@@ -59,14 +59,14 @@ double adjh_sl_vertices(const slvof_mesh* M, int i, int j, int k, const double* 
                         const double* nz, const double* D, double g, double* gvt, int* err)
 {
     HostMesh H(M);
-    double p0[8][3], v[8][3], gv[8][3];
+    double p0[8][3], v[15][3], gv[8][3];
     const double tetsign = adj::cell_verts(H.m, i, j, k, p0);
-    int vind[8][3];
+    int vind[15][3];
     int e = 0;
-    for (int n = 0; n < 8; ++n) {
+    for (int n = 0; n < 8; ++n)
         for (int p = 0; p < 3; ++p) { v[n][p] = vt[3 * n + p]; gv[n][p] = 0.0; }
-        adj::pt2index(H.m, vind[n], v[n], i, j, k, e);
-    }
+    tess_means<double>(H.m.tess, v);
+    for (int n = 0; n < tess_npoints(H.m.tess); ++n) adj::pt2index(H.m, vind[n], v[n], i, j, k, e);
     adj::Plic P{nx, ny, nz, D, nullptr, nullptr, nullptr, nullptr};
     std::vector<adj::Frame> st(adj::STACK);
     std::vector<double> sink(4 * H.m.cs2 * (H.m.N[2] + 2 * H.m.g), 0.0);

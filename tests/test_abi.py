@@ -3,6 +3,7 @@ no compute calls), and the host-side layout helpers match the reference's extent
 import ctypes
 import os
 import re
+import subprocess
 
 import numpy as np
 import pytest
@@ -35,11 +36,18 @@ def test_library_exports_every_declared_symbol(lib):
     assert sorted(n for n, _, _ in slvof.SYMBOLS) == syms
 
 
-def test_descriptor_layout_matches_header():
-    # slvof_mesh: 9 int32 (36 B) + pad to 40, 10 doubles, 6 pointers
-    assert ctypes.sizeof(MeshDesc) == 40 + 10 * 8 + 6 * ctypes.sizeof(ctypes.c_void_p)
-    assert MeshDesc.Lx.offset == 40
-    assert MeshDesc.x.offset == 120
+def test_descriptor_layout_matches_header(tmp_path):
+    """ctypes' MeshDesc against the C compiler's layout of slvof_mesh (include/slvof.h)."""
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "slvof.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(slvof_mesh), offsetof(slvof_mesh, Lx), '
+                   'offsetof(slvof_mesh, x), offsetof(slvof_mesh, zm), offsetof(slvof_mesh, tesselation)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    size, lx, x, zm, tess = (int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                              check=True).stdout.split())
+    assert ctypes.sizeof(MeshDesc) == size
+    assert (MeshDesc.Lx.offset, MeshDesc.x.offset, MeshDesc.zm.offset, MeshDesc.tesselation.offset) == (lx, x, zm, tess)
 
 
 def test_extents_follow_initArrays():

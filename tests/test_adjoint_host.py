@@ -54,8 +54,8 @@ def ptr(a):
     return a.ctypes.data
 
 
-def sphere_state(N=10, centre=(0.45, 0.52, 0.55), r=0.27, t=0.4):
-    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+def sphere_state(N=10, centre=(0.45, 0.52, 0.55), r=0.27, t=0.4, tess="5_tets"):
+    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess)
     o = Oracle(m)
     VF = cases.vf_spheres(m, np.array([centre]), np.array([r]), nF=8)
     band, nx, ny, nz, D = o.init_state(VF)
@@ -70,9 +70,9 @@ def sphere_state(N=10, centre=(0.45, 0.52, 0.55), r=0.27, t=0.4):
     return m, o, VF, band, nx, ny, nz, D, uf, vf, wf, dt
 
 
-@pytest.fixture(scope="module")
-def state():
-    return sphere_state()
+@pytest.fixture(scope="module", params=["5_tets", "6_tets", "24_tets"])
+def state(request):
+    return sphere_state(tess=request.param)
 
 
 def interface_preimage_cells(m, o, st, count):

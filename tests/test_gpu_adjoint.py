@@ -225,3 +225,21 @@ def test_adjoint_configurations_at_reduced_size(built, which):
         out = A.check(cfg, 8, "cpu")
     assert out["checked"] >= 8
     assert out["max_abs_err_over_max_fd"] <= RTOL, out
+
+
+@pytest.mark.parametrize("tess", ["6_tets", "24_tets"])
+def test_single_step_other_tessellations(built, tess):
+    """The reverse pass over 6_tets and 24_tets (mean points' derivatives shared out to the
+    vertices they average) against central differences of the restatement."""
+    m = Mesh(Nx=12, Ny=12, Nz=12, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess)
+    VF0 = cases.vf_spheres(m, np.array([[0.45, 0.52, 0.55]]), np.array([0.27]), nF=8)
+    dt = 0.5 * m.dx / 2.0
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
+    vel, noise = noisy(m, base, 0.05, 31)
+    w = np.random.default_rng(2).standard_normal((m.Nx, m.Ny, m.Nz))
+    L_gpu, gVF0, gu, gv, gw = gpu_gradients(m, VF0, vel, dt, 1, w, every=1)
+    L_cpu = oracle_rollout(m, VF0, vel, dt, 1, w)
+    assert abs(L_gpu - L_cpu) <= 1e-12 * max(1.0, abs(L_cpu))
+    worst, n = check_velocity(m, VF0, base, noise, dt, 1, w, (gu, gv, gw))
+    assert n >= 12
+    assert worst <= RTOL, worst

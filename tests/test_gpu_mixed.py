@@ -125,3 +125,51 @@ def test_mixed_tracks_fp64(shape):
         assert float(np.percentile(d[iface], 99)) <= 1e-5, float(np.percentile(d[iface], 99))
     assert float(d.max()) <= 5e-3, float(d.max())
     assert V32.min() >= -1e-6 and V32.max() <= 1 + 1e-6
+
+
+@pytest.mark.parametrize("tess", ["6_tets", "24_tets"])
+def test_mixed_other_tessellations_track_fp64(tess):
+    """6_tets and 24_tets in the mixed path (tets seeded from the tessellation, 24_tets with
+    FP32 mean points): a plane carried by a uniform velocity comes out exact to 2e-6, and a
+    deforming sphere stays with the FP64 path of the same tessellation."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from planevol import box_fraction
+    from test_oracle_pins import plane_vf
+    m = Mesh(Nx=10, Ny=10, Nz=10, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess)
+    n0 = np.array([0.25, 0.1, 1.0])
+    n0 /= np.linalg.norm(n0)
+    c = float(np.dot(n0, [0.5, 0.5, 0.48]))
+    g = make(m, plane_vf(m, n0, c), "mixed")
+    g.upload_band(m.cell_array(np.int16))
+    u = (0.31, -0.27, 0.43)
+    g.upload_velocity(*cases.uniform_faces(m, *u))
+    dt = 0.5 * m.dx / 0.43
+    g.transport(dt)
+    out = g.download_vf()
+    shift = dt * float(np.dot(n0, u))
+    worst = 0.0
+    for k in range(3, 9):
+        for j in range(3, 9):
+            for i in range(3, 9):
+                ci = m.cidx(i, j, k)
+                lo = (m.x[ci[0]], m.y[ci[1]], m.z[ci[2]])
+                hi = (m.x[ci[0] + 1], m.y[ci[1] + 1], m.z[ci[2] + 1])
+                worst = max(worst, abs(out[m.vidx(i, j, k)] - box_fraction(n0, c + shift, lo, hi)))
+    assert worst <= 2e-6, worst
+
+    m = Mesh(Nx=20, Ny=20, Nz=20, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess)
+    VF = cases.vf_spheres(m, [[0.42, 0.47, 0.4]], [0.21], nF=10)
+    g64, g32 = make(m, VF, "fp64"), make(m, VF, "mixed")
+    dt = 0.5 * m.dx / 2.0
+    for s in range(6):
+        uf, vf, wf = cases.deformation3d_faces(m, 0.2 + (s + 0.5) * dt, 3.0)
+        g64.upload_velocity(uf, vf, wf)
+        g32.upload_velocity(uf, vf, wf)
+        M64, M32 = g64.step(dt), g32.step(dt)
+    V64, V32 = m.interior(g64.download_vf()), m.interior(g32.download_vf())
+    iface = (V64 >= 1e-10) & (V64 <= 1 - 1e-10)
+    d = np.abs(V64 - V32)
+    assert float(np.percentile(d[iface], 99)) <= 1e-5
+    assert float(d.max()) <= 5e-3
+    assert abs(M32 - M64) <= 1e-6 * m.dx * m.dy * m.dz * np.sqrt(6 * iface.sum())

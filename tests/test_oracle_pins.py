@@ -61,9 +61,11 @@ def random_cases(n, seed):
     return out
 
 
-def test_plic_round_trip_1000():
-    # test/runtests.jl:32-45 -> test/test_PLIC_dist_cutting.jl:141-149
-    m = plic_test_mesh()
+@pytest.mark.parametrize("tess", ["5_tets", "6_tets", "24_tets"])
+def test_plic_round_trip_1000(tess):
+    # test/runtests.jl:32-45 -> test/test_PLIC_dist_cutting.jl:141-149 (the reference runs it
+    # with its default tessellation; computeDist does not depend on it, computePLIC2VF does)
+    m = Mesh(Nx=10, Ny=10, Nz=1, Lx=3.0, Ly=1.0, Lz=1.0, CFL=0.1, tesselation=tess)
     o = Oracle(m)
     worst = 0.0
     for nx, ny, nz, VF in random_cases(1000, 20261203):
@@ -170,10 +172,23 @@ def test_elvira_reconstructs_planes_exactly():
     assert checked >= 10
 
 
-def test_uniform_translation_of_plane_is_exact():
+@pytest.mark.parametrize("tess", ["5_tets", "6_tets", "24_tets"])
+def test_full_cell_volume_of_every_tessellation(tess):
+    """The tets of each tessellation tile the cell with positive orientation: a plane that
+    leaves the whole cell liquid gives VF = 1, on odd and even cells."""
+    m = Mesh(Nx=4, Ny=4, Nz=4, Lx=1.0, Ly=0.7, Lz=1.3, tesselation=tess)
+    o = Oracle(m)
+    for (i, j, k) in [(1, 1, 1), (2, 1, 1), (3, 4, 2), (4, 4, 4)]:
+        v = o.computePLIC2VF(i, j, k, 0.3, -0.5, 0.8, 10.0)
+        assert abs(v - 1.0) <= 1e-14, (tess, i, j, k, v)
+        assert o.computePLIC2VF(i, j, k, 0.3, -0.5, 0.8, -10.0) == 0.0
+
+
+@pytest.mark.parametrize("tess", ["5_tets", "6_tets", "24_tets"])
+def test_uniform_translation_of_plane_is_exact(tess):
     """A uniform velocity carries a plane exactly: the pre-image is the translated cell, and
     every donor's PLIC plane is the exact plane, so VFnew is the exact shifted fraction."""
-    m = Mesh(Nx=10, Ny=10, Nz=10, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    m = Mesh(Nx=10, Ny=10, Nz=10, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess)
     o = Oracle(m)
     n0 = np.array([0.25, 0.1, 1.0])
     n0 /= np.linalg.norm(n0)
@@ -202,8 +217,9 @@ def test_uniform_translation_of_plane_is_exact():
     assert checked > 20
 
 
-def test_pre_image_volume_uniform_flow():
-    m = Mesh(Nx=6, Ny=6, Nz=6, Lx=1.0, Ly=1.0, Lz=1.0)
+@pytest.mark.parametrize("tess", ["5_tets", "6_tets", "24_tets"])
+def test_pre_image_volume_uniform_flow(tess):
+    m = Mesh(Nx=6, Ny=6, Nz=6, Lx=1.0, Ly=1.0, Lz=1.0, tesselation=tess)
     o = Oracle(m)
     uf, vf, wf = cases.uniform_faces(m, 0.2, -0.1, 0.3)
     VF = m.vf_array()
