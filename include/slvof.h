@@ -53,7 +53,8 @@ typedef struct slvof_mesh {
     int32_t Nx, Ny, Nz;
     int32_t nghost;     /* 3 + max(0, ceil(CFL)-2), src/Mesh.jl:66 */
     int32_t nband;      /* ceil(CFL), src/Parameters.jl:70 */
-    int32_t projection; /* 0 Euler, 1 Midpoint, 2 RK4 (src/Tools.jl:392-418) */
+    int32_t projection; /* 0 Euler, 1 Midpoint, 2 RK4 (src/Tools.jl:392-418); 3 the exact rotation of
+                           test_case "Zalesak" (src/Tools.jl:396-399) */
     int32_t xper, yper, zper;
     double Lx, Ly, Lz, dx, dy, dz;
     double VFlo, VFhi, rho_liq, rho_gas;

@@ -32,6 +32,7 @@
 
 #include <cmath>
 
+#include "detmath.h"
 #include "mesh_view.h"
 
 namespace slvof {
@@ -262,6 +263,15 @@ SLVOF_HD void velocity_reverse(const DevMesh& m, const Vel& V, const VelGrad& G,
 SLVOF_HD void project(const DevMesh& m, const Vel& V, double* pt, int i, int j, int k, double dt, double x[3][3])
 {
     double v1[3], v2[3], v3[3], v4[3];
+    if (m.projection == 3) {
+        /* test_case == "Zalesak": exact rotation about (0.5, 0.5), src/Tools.jl:396-399 */
+        const double a = 6.283185307179586 * dt;
+        const double c = detm_cos(a), s = detm_sin(a);
+        const double x0 = pt[0], y0 = pt[1];
+        pt[0] = (0.5 + c * (x0 - 0.5)) + s * (y0 - 0.5);
+        pt[1] = (0.5 - s * (x0 - 0.5)) + c * (y0 - 0.5);
+        return;
+    }
     if (m.projection == 2) {
         velocity(m, V, pt, i, j, k, v1);
         for (int d = 0; d < 3; ++d) x[0][d] = pt[d] - 0.5 * dt * v1[d];
@@ -286,6 +296,7 @@ SLVOF_HD void project(const DevMesh& m, const Vel& V, double* pt, int i, int j, 
 SLVOF_HD void project_reverse(const DevMesh& m, const Vel& V, const VelGrad& G, const double* p0, int i, int j, int k,
                               double dt, const double* gp)
 {
+    if (m.projection == 3) return; /* the rotation does not depend on the velocities */
     double pt[3] = {p0[0], p0[1], p0[2]};
     double x[3][3];
     project(m, V, pt, i, j, k, dt, x);

@@ -252,6 +252,15 @@ __device__ __forceinline__ void velocity64(const DevMesh& m, const Vel64& V, dou
 __device__ __forceinline__ void project64(const DevMesh& m, const Vel64& V, double& px, double& py, double& pz, int i,
                                           int j, int k, double dt)
 {
+    if (m.projection == 3) {
+        /* test_case == "Zalesak": exact rotation about (0.5, 0.5), src/Tools.jl:396-399 */
+        const double a = 6.283185307179586 * dt;
+        const double c = detm_cos(a), s = detm_sin(a);
+        const double x0 = px, y0 = py;
+        px = (0.5 + c * (x0 - 0.5)) + s * (y0 - 0.5);
+        py = (0.5 - s * (x0 - 0.5)) + c * (y0 - 0.5);
+        return;
+    }
     double u1, v1, w1;
     velocity64(m, V, px, py, pz, i, j, k, u1, v1, w1);
     if (m.projection == 2) {

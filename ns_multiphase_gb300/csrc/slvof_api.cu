@@ -279,7 +279,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     *out = nullptr;
     if (precision != SLVOF_FP64 && precision != SLVOF_MIXED) return SLVOF_E_ARG;
     if (mesh->Nx < 1 || mesh->Ny < 1 || mesh->Nz < 1 || mesh->nghost < 3) return SLVOF_E_ARG;
-    if (mesh->projection < 0 || mesh->projection > 2 || mesh->nband < 0) return SLVOF_E_ARG;
+    if (mesh->projection < 0 || mesh->projection > 3 || mesh->nband < 0) return SLVOF_E_ARG;
     if (mesh->tesselation != 0 && mesh->tesselation != 5 && mesh->tesselation != 6 && mesh->tesselation != 24)
         return SLVOF_E_ARG;
     if (!mesh->x || !mesh->y || !mesh->z || !mesh->xm || !mesh->ym || !mesh->zm) return SLVOF_E_ARG;

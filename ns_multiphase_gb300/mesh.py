@@ -20,7 +20,7 @@ from fractions import Fraction
 
 import numpy as np
 
-PROJECTION = {"Euler": 0, "Midpoint": 1, "RK4": 2}
+PROJECTION = {"Euler": 0, "Midpoint": 1, "RK4": 2, "Zalesak": 3}  # Zalesak: test_case, src/Tools.jl:396-399
 
 
 def _axis(N: int, L: float, g: int):

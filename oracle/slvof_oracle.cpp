@@ -523,6 +523,16 @@ void velocity(const Grid& G, const Vel& V, const double pt[3], int i, int j, int
 void project(const Grid& G, const Vel& V, double pt[3], int i, int j, int k, double dt)
 {
     const int method = G.m->projection;
+    if (method == 3) {
+        /* test_case == "Zalesak": exact rotation about (0.5, 0.5), src/Tools.jl:396-399;
+         * 2*pi in Float64 is 2.0*pi exactly */
+        const double a = 6.283185307179586 * dt;
+        const double c = detm_cos(a), s = detm_sin(a);
+        const double x0 = pt[0], y0 = pt[1];
+        pt[0] = (0.5 + c * (x0 - 0.5)) + s * (y0 - 0.5);
+        pt[1] = (0.5 - s * (x0 - 0.5)) + c * (y0 - 0.5);
+        return;
+    }
     if (method == 2) {
         double v1[3], v2[3], v3[3], v4[3], p[3];
         velocity(G, V, pt, i, j, k, v1);

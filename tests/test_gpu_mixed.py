@@ -173,3 +173,21 @@ def test_mixed_other_tessellations_track_fp64(tess):
     assert float(np.percentile(d[iface], 99)) <= 1e-5
     assert float(d.max()) <= 5e-3
     assert abs(M32 - M64) <= 1e-6 * m.dx * m.dy * m.dz * np.sqrt(6 * iface.sum())
+
+
+def test_mixed_zalesak_rotation_tracks_fp64():
+    m = Mesh(Nx=40, Ny=40, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / 40, CFL=0.5, zper=True, projection="Zalesak")
+    VF = cases.vf_spheres(m, [[0.5, 0.75, 0.0]], [0.15], nF=10, dims=2)
+    g64, g32 = make(m, VF, "fp64"), make(m, VF, "mixed")
+    zero = m.cell_array()
+    for g in (g64, g32):
+        g.upload_velocity(zero, zero, zero)
+    dt = 0.5 * m.dx / (2 * np.pi * 0.5)
+    for s in range(8):
+        M64, M32 = g64.step(dt), g32.step(dt)
+    V64, V32 = m.interior(g64.download_vf()), m.interior(g32.download_vf())
+    iface = (V64 >= 1e-10) & (V64 <= 1 - 1e-10)
+    d = np.abs(V64 - V32)
+    assert float(np.percentile(d[iface], 99)) <= 1e-5
+    assert float(d.max()) <= 5e-3
+    assert abs(M32 - M64) <= 1e-6 * m.dx * m.dy * m.dz * np.sqrt(8 * iface.sum())

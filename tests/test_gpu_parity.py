@@ -214,3 +214,21 @@ def test_2d_vortex_other_tessellations(tess):
         g.step(dt)
         assert o.step(dt, VFo, uf, vf, wf, nx, ny, nz, D, band) == 0
     assert_same(g.download_vf(), VFo, "VF")
+
+
+def test_zalesak_rotation_projection():
+    """test_case "Zalesak" (src/Tools.jl:396-399): the pre-image is the exact rotation about
+    (0.5, 0.5), no velocity interpolation; FP64 path bit for bit against the restatement."""
+    m = Mesh(Nx=40, Ny=40, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / 40, CFL=0.5, zper=True, projection="Zalesak")
+    VF = cases.vf_spheres(m, [[0.5, 0.75, 0.0]], [0.15], nF=10, dims=2)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    dt = 0.5 * m.dx / (2 * np.pi * 0.5)
+    zero = m.cell_array()
+    g.upload_velocity(zero, zero, zero)
+    for s in range(8):
+        g.step(dt)
+        assert o.step(dt, VFo, zero, zero, zero, nx, ny, nz, D, band) == 0
+    assert_same(g.download_vf(), VFo, "VF")
+    gx, gy, gz = g.download_normals()
+    assert_same(gx, nx, "nx")
+    assert_same(g.download_plic(), D, "D")
