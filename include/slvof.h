@@ -124,6 +124,18 @@ int slvof_step(slvof_ctx* ctx, double dt, int flags, double* mass);
 /* sum(VF[interior])*dx*dy*dz, compensated FP64 (src/WriteData.jl:33). */
 int slvof_mass(slvof_ctx* ctx, double* mass);
 
+/* ---- momentum of transport! (FP64 context) -------------------------------------------------
+ * With the cell-centred velocities u, v, w (cell arrays), the SL update also gives us, vs, ws
+ * of every interior cell (src/Transport.jl:34-166 with pressure_scheme "semi-lagrangian"):
+ * band cells from the clipped pre-image (vrhoU/vrho with rho_liq/rho_gas on each side of the
+ * donors' planes), the others from the face fluxes (finite-difference flux, no flux between
+ * two band cells, the semi-Lagrangian flux volume SLfluxVol at band edges).  A mixed-precision
+ * context returns SLVOF_E_UNSUPPORTED. */
+int slvof_upload_cell_velocity(slvof_ctx* ctx, const double* u, const double* v, const double* w);
+int slvof_download_momentum(slvof_ctx* ctx, double* us, double* vs, double* ws);
+/* the SL section of transport! with its momentum, on the resident state */
+int slvof_transport_momentum(slvof_ctx* ctx, double dt);
+
 /* ---- host-buffer drop-ins: one call per reference function, arrays in host memory --------
  * Each copies its inputs to the device, runs the operation and copies the outputs back.  */
 /* computeNormal!(nx,ny,nz,VF,param,mesh,par_env), src/VF.jl:79 */
@@ -136,6 +148,12 @@ int slvof_computeBand(slvof_ctx* ctx, int16_t* band, const double* VF);
 /* SL section of transport!(...): src/Transport.jl:108-151,179-181.  VF is updated in place. */
 int slvof_transportSL(slvof_ctx* ctx, double dt, double* VF, const double* uf, const double* vf, const double* wf,
                       const double* nx, const double* ny, const double* nz, const double* D, const int16_t* band);
+/* SL and momentum sections of transport! (src/Transport.jl:34-181): VF updated in place,
+ * us, vs, ws written (cell arrays; interior cells). */
+int slvof_transportSL_momentum(slvof_ctx* ctx, double dt, double* VF, const double* uf, const double* vf,
+                               const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                               const int16_t* band, const double* u, const double* v, const double* w, double* us,
+                               double* vs, double* ws);
 /* Per-step drop-in for run_solver's loop with the state resident between calls: uploads
  * this step's face velocities, runs slvof_step and downloads VF (and the mass). */
 int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, const double* vf, const double* wf,

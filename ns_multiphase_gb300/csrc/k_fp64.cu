@@ -304,9 +304,13 @@ __device__ __forceinline__ int pt2index1(const DevMesh& m, int q, double p, int 
  * case and the running (vol, vLiq) of its children, so partial sums are added in exactly
  * the reference's tree order.
  * ==================================================================================== */
+/* One cutTet level: parent vertices 0-3, new vertices 4-7, their cells, the children's running
+ * sums (vol, vLiq, and with MOM vrhoU, vrhoV, vrhoW, vrho) and the level's case, next child,
+ * cut direction and index. */
+template <bool MOM>
 struct Frame64 {
     double x[8], y[8], z[8];
-    double acc_v, acc_l;
+    double acc[MOM ? 6 : 2];
     short ind[8][3]; /* side-1 indices; side 2 differs only in the cut direction (= cut) */
     signed char cs, next, dir, flags;
     int cut;
@@ -314,12 +318,15 @@ struct Frame64 {
 
 struct Plic64 {
     const double *nx, *ny, *nz, *D;
+    const double *u, *v, *w; /* cell-centred velocities for the momentum sums (MOM only) */
+    double rho_liq, rho_gas;
 };
 
-/* Leaf: clip by the donor cell's PLIC plane (src/VFgeom.jl:757-830). */
+/* Leaf: clip by the donor cell's PLIC plane (src/VFgeom.jl:757-830): r = (vol, vLiq) and with
+ * MOM (vrhoU, vrhoV, vrhoW, vrho) with the donor's velocity and each side's density. */
+template <bool MOM>
 __device__ __forceinline__ void leaf64(const DevMesh& m, const CutCase* tab, const Plic64& P, const double* cx,
-                                       const double* cy, const double* cz, int di, int dj, int dk, double& rv,
-                                       double& rl, int& err)
+                                       const double* cy, const double* cz, int di, int dj, int dk, double* r, int& err)
 {
     const long c = cidx(m, di, dj, dk);
     const double a = __ldg(P.nx + c), b = __ldg(P.ny + c), e = __ldg(P.nz + c), Dd = __ldg(P.D + c);
@@ -338,22 +345,39 @@ __device__ __forceinline__ void leaf64(const DevMesh& m, const CutCase* tab, con
         vy[4 + n] = (1.0 - mu) * vy[v1] + mu * vy[v2];
         vz[4 + n] = (1.0 - mu) * vz[v1] + mu * vz[v2];
     }
-    double vol = 0.0, liq = 0.0;
+    double vol = 0.0, liq = 0.0, ru = 0.0, rv = 0.0, rw = 0.0, rho = 0.0;
+    double uc = 0.0, vc = 0.0, wc = 0.0;
+    if (MOM) { uc = __ldg(P.u + c); vc = __ldg(P.v + c); wc = __ldg(P.w + c); }
     for (int n = C.ntets - 1; n >= C.nntet - 1; --n) {
-        const int p = C.vtet[n][0], q = C.vtet[n][1], r = C.vtet[n][2], s = C.vtet[n][3];
-        const double tv = tet_vol(vx[p], vy[p], vz[p], vx[q], vy[q], vz[q], vx[r], vy[r], vz[r], vx[s], vy[s], vz[s]);
+        const int p = C.vtet[n][0], q = C.vtet[n][1], t = C.vtet[n][2], s = C.vtet[n][3];
+        const double tv = tet_vol(vx[p], vy[p], vz[p], vx[q], vy[q], vz[q], vx[t], vy[t], vz[t], vx[s], vy[s], vz[s]);
         vol += tv;
         liq += tv;
+        if (MOM) {
+            ru += tv * uc * P.rho_liq;
+            rv += tv * vc * P.rho_liq;
+            rw += tv * wc * P.rho_liq;
+            rho += tv * P.rho_liq;
+        }
     }
     for (int n = 0; n < C.nntet - 1; ++n) {
-        const int p = C.vtet[n][0], q = C.vtet[n][1], r = C.vtet[n][2], s = C.vtet[n][3];
-        vol += tet_vol(vx[p], vy[p], vz[p], vx[q], vy[q], vz[q], vx[r], vy[r], vz[r], vx[s], vy[s], vz[s]);
+        const int p = C.vtet[n][0], q = C.vtet[n][1], t = C.vtet[n][2], s = C.vtet[n][3];
+        const double tv = tet_vol(vx[p], vy[p], vz[p], vx[q], vy[q], vz[q], vx[t], vy[t], vz[t], vx[s], vy[s], vz[s]);
+        vol += tv;
+        if (MOM) {
+            ru += tv * uc * P.rho_gas;
+            rv += tv * vc * P.rho_gas;
+            rw += tv * wc * P.rho_gas;
+            rho += tv * P.rho_gas;
+        }
     }
-    rv = vol;
-    rl = liq;
+    r[0] = vol;
+    r[1] = liq;
+    if (MOM) { r[2] = ru; r[3] = rv; r[4] = rw; r[5] = rho; }
 }
 
-__device__ __forceinline__ void form_child64(const Frame64& F, const CutCase* tab, int n, double* cx, double* cy,
+template <bool MOM>
+__device__ __forceinline__ void form_child64(const Frame64<MOM>& F, const CutCase* tab, int n, double* cx, double* cy,
                                              double* cz, int (*ci)[3])
 {
     const CutCase& C = tab[F.cs];
@@ -366,10 +390,14 @@ __device__ __forceinline__ void form_child64(const Frame64& F, const CutCase* ta
     }
 }
 
+/* cutTet (src/VFgeom.jl:713-900) with an explicit stack; the children's sums are added in the
+ * reference's order.  out = (vol, vLiq[, vrhoU, vrhoV, vrhoW, vrho]). */
+template <bool MOM>
 __device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P, double* cx, double* cy, double* cz,
-                           int (*ci)[3], double& out_v, double& out_l, int& err)
+                           int (*ci)[3], double* out, int& err)
 {
-    Frame64 st[CLIP_STACK];
+    constexpr int NA = MOM ? 6 : 2;
+    Frame64<MOM> st[CLIP_STACK];
     int depth = 0, flags = 0, leaves = 0;
     for (;;) {
         int dir = -1, cut = 0;
@@ -380,17 +408,17 @@ __device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P
             if (mx > mn) { dir = q; cut = mx; break; }
             flags |= 1 << q;
         }
-        double rv, rl;
+        double r[NA];
         if (dir >= 0 && depth == CLIP_STACK) { err |= ERR_DEPTH; dir = -1; }
         if (dir < 0) {
             if (++leaves > CLIP_MAX_LEAVES) { /* bounded work even for clamped, far-away pre-images */
                 err |= ERR_DEPTH;
-                out_v = 0.0; out_l = 0.0;
+                for (int q = 0; q < NA; ++q) out[q] = 0.0;
                 return;
             }
-            leaf64(m, tab, P, cx, cy, cz, ci[0][0], ci[0][1], ci[0][2], rv, rl, err);
+            leaf64<MOM>(m, tab, P, cx, cy, cz, ci[0][0], ci[0][1], ci[0][2], r, err);
         } else {
-            Frame64& F = st[depth];
+            Frame64<MOM>& F = st[depth];
             const double pl = fco(m, dir, cut);
             const double* cd = dir == 0 ? cx : (dir == 1 ? cy : cz);
             double d[4];
@@ -424,23 +452,26 @@ __device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P
                 F.ind[4 + n][dir] = (short)(cut - 1);
             }
             F.cs = (signed char)cs; F.dir = (signed char)dir; F.cut = cut; F.flags = (signed char)flags;
-            F.acc_v = 0.0; F.acc_l = 0.0; F.next = 1;
+            for (int q = 0; q < NA; ++q) F.acc[q] = 0.0;
+            F.next = 1;
             ++depth;
-            form_child64(F, tab, 0, cx, cy, cz, ci);
+            form_child64<MOM>(F, tab, 0, cx, cy, cz, ci);
             continue;
         }
         for (;;) {
-            if (depth == 0) { out_v = rv; out_l = rl; return; }
-            Frame64& F = st[depth - 1];
-            F.acc_v += rv;
-            F.acc_l += rl;
+            if (depth == 0) {
+                for (int q = 0; q < NA; ++q) out[q] = r[q];
+                return;
+            }
+            Frame64<MOM>& F = st[depth - 1];
+            for (int q = 0; q < NA; ++q) F.acc[q] += r[q];
             if (F.next < tab[F.cs].ntets) {
-                form_child64(F, tab, F.next, cx, cy, cz, ci);
+                form_child64<MOM>(F, tab, F.next, cx, cy, cz, ci);
                 F.next += 1;
                 flags = F.flags;
                 break;
             }
-            rv = F.acc_v; rl = F.acc_l;
+            for (int q = 0; q < NA; ++q) r[q] = F.acc[q];
             --depth;
         }
     }
@@ -469,10 +500,13 @@ constexpr int SL_THREADS = 128;
 /* SL update of one band cell: cell2tets!(project_verts=true, compute_indices=true)
  * (src/VFgeom.jl:345-420), then cutTet on the cell's tets and VFnew = vLiq/vol
  * (src/Transport.jl:116-145).  For 24_tets the mean points come from the projected vertices
- * and their cells from pt2index! seeded at the cell, as verts2tets! does. */
+ * and their cells from pt2index! seeded at the cell, as verts2tets! does.  With MOM also
+ * us, vs, ws = vrhoU/vrho, ... (src/Transport.jl:146-148). */
+template <bool MOM>
 __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, double dt,
                                           const signed char* __restrict__ phase, double* __restrict__ VFout,
-                                          const Vel64& V, const Plic64& P, int L, int& err)
+                                          const Vel64& V, const Plic64& P, int L, double* us, double* vs, double* ws,
+                                          int& err)
 {
     const int i = 1 + L % m.N[0];
     const int j = 1 + (L / m.N[0]) % m.N[1];
@@ -500,7 +534,8 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
         vi[v][2] = pt2index1(m, 2, p[v][2], k, err);
     }
     const long out = vidx(m, i, j, k);
-    if (m.fast_pure) {
+    /* pure-donor shortcut (VF only: the momentum sums depend on each donor's share) */
+    if (!MOM && m.fast_pure) {
         int lo0 = vi[0][0], hi0 = vi[0][0], lo1 = vi[0][1], hi1 = vi[0][1], lo2 = vi[0][2], hi2 = vi[0][2];
         for (int v = 1; v < np; ++v) {
             lo0 = min(lo0, vi[v][0]); hi0 = max(hi0, vi[v][0]);
@@ -522,7 +557,9 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
             }
         }
     }
-    double vol = 0.0, liq = 0.0;
+    constexpr int NA = MOM ? 6 : 2;
+    double sum[NA];
+    for (int q = 0; q < NA; ++q) sum[q] = 0.0;
 #pragma unroll 1
     for (int t = 0; t < nt; ++t) {
         double cx[4], cy[4], cz[4];
@@ -532,19 +569,25 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
             cx[n] = p[v][0]; cy[n] = p[v][1]; cz[n] = p[v][2];
             ci[n][0] = vi[v][0]; ci[n][1] = vi[v][1]; ci[n][2] = vi[v][2];
         }
-        double tv, tl;
-        clip_tet64(m, tab, P, cx, cy, cz, ci, tv, tl, err);
-        vol += tetsign * tv;
-        liq += tetsign * tl;
+        double r[NA];
+        clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err);
+        for (int q = 0; q < NA; ++q) sum[q] += tetsign * r[q];
     }
-    if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
-    VFout[out] = liq / vol;
+    if (!(sum[0] > 0.0) || !isfinite(sum[0])) err |= ERR_VOLUME;
+    VFout[out] = sum[1] / sum[0];
+    if (MOM) {
+        const long c = cidx(m, i, j, k);
+        us[c] = sum[2] / sum[5];
+        vs[c] = sum[3] / sum[5];
+        ws[c] = sum[4] / sum[5];
+    }
 }
 
+template <bool MOM>
 __global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const signed char* __restrict__ phase,
                                                      double* __restrict__ VFout, Vel64 V, Plic64 P,
                                                      const int* __restrict__ list, const int* __restrict__ count,
-                                                     int* work, int* errw)
+                                                     int* work, double* us, double* vs, double* ws, int* errw)
 {
     __shared__ CutCase s_tab[16];
     load_table(s_tab);
@@ -557,10 +600,110 @@ __global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_items) break;
         const int item = base + lane;
-        if (item < n_items) sl_cell64(m, s_tab, dt, phase, VFout, V, P, list[item], err);
+        if (item < n_items) sl_cell64<MOM>(m, s_tab, dt, phase, VFout, V, P, list[item], us, vs, ws, err);
         __syncwarp();
     }
     if (err) atomicOr(errw, err);
+}
+
+/* ======================================================================================
+ * Momentum of the cells outside the band (src/Transport.jl:34-104,150-166, pressure_scheme
+ * "semi-lagrangian"): us = u + dt/(dx dy dz) * sum of face-flux differences.  A face between
+ * two band cells carries no flux, a face with one band cell the semi-Lagrangian flux volume
+ * (SLfluxVol, src/VFgeom.jl:428-509), every other face the finite-difference flux.
+ * ==================================================================================== */
+/* vertices of the flux volume of face `dir`: index offsets and projection flag, even and odd */
+__constant__ signed char c_fluxv[3][2][8][4] = {
+    {{{0, 0, 0, 1}, {0, 0, 0, 0}, {0, 1, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 1}, {0, 0, 1, 0}, {0, 1, 1, 1}, {0, 1, 1, 0}},
+     {{0, 0, 0, 0}, {0, 0, 0, 1}, {0, 1, 0, 0}, {0, 1, 0, 1}, {0, 0, 1, 0}, {0, 0, 1, 1}, {0, 1, 1, 0}, {0, 1, 1, 1}}},
+    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 0, 1, 1}, {1, 0, 1, 1}, {0, 0, 1, 0}, {1, 0, 1, 0}},
+     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 0, 1, 1}, {0, 0, 1, 1}, {1, 0, 1, 0}, {0, 0, 1, 0}}},
+    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {1, 1, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {1, 1, 0, 0}},
+     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 0, 1}, {0, 1, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 1, 0, 0}, {0, 1, 0, 0}}}};
+
+__device__ double sl_flux_vol64(const DevMesh& m, const Vel64& V, int dir, int i, int j, int k, double dt)
+{
+    const bool even = tess_even(m.tess, i, j, k);
+    const double tetsign = even ? 1.0 : -1.0;
+    double p[15][3];
+    for (int n = 0; n < 8; ++n) {
+        const signed char* f = c_fluxv[dir][even ? 0 : 1][n];
+        double x = fco(m, 0, i + f[0]), y = fco(m, 1, j + f[1]), z = fco(m, 2, k + f[2]);
+        if (f[3]) project64(m, V, x, y, z, i, j, k, dt);
+        p[n][0] = x; p[n][1] = y; p[n][2] = z;
+    }
+    tess_means<double>(m.tess, p);
+    double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+    for (int t = 0; t < tess_ntets(m.tess); ++t) {
+        const int a = tess_tet(m.tess, t, 0), b = tess_tet(m.tess, t, 1), c = tess_tet(m.tess, t, 2),
+                  e = tess_tet(m.tess, t, 3);
+        vol += tet_vol(p[a][0], p[a][1], p[a][2], p[b][0], p[b][1], p[b][2], p[c][0], p[c][1], p[c][2], p[e][0],
+                       p[e][1], p[e][2]);
+    }
+    return vol * tetsign;
+}
+
+__device__ void face_flux64(const DevMesh& m, const Vel64& V, const Plic64& P, const short* __restrict__ band, int dir,
+                            int i, int j, int k, double dt, double* F)
+{
+    const int li = i - (dir == 0), lj = j - (dir == 1), lk = k - (dir == 2);
+    const long c = cidx(m, i, j, k), l = cidx(m, li, lj, lk);
+    const double uface = 0.5 * (__ldg(P.u + l) + __ldg(P.u + c));
+    const double vface = 0.5 * (__ldg(P.v + l) + __ldg(P.v + c));
+    const double wface = 0.5 * (__ldg(P.w + l) + __ldg(P.w + c));
+    const bool bl = abs((int)band[l]) <= m.nband, bc = abs((int)band[c]) <= m.nband;
+    if (bl && bc) {
+        F[0] = 0.0; F[1] = 0.0; F[2] = 0.0;
+    } else if (bl || bc) {
+        const double vol = sl_flux_vol64(m, V, dir, i, j, k, dt) / dt;
+        F[0] = -uface * vol; F[1] = -vface * vol; F[2] = -wface * vol;
+    } else {
+        const double a = dir == 0 ? m.d[1] : m.d[0], b = dir == 2 ? m.d[1] : m.d[2];
+        const double q = __ldg((dir == 0 ? V.uf : (dir == 1 ? V.vf : V.wf)) + c);
+        F[0] = -uface * a * b * q; F[1] = -vface * a * b * q; F[2] = -wface * a * b * q;
+    }
+}
+
+__global__ void k_mom_flux64(DevMesh m, double dt, Vel64 V, Plic64 P, const short* __restrict__ band,
+                             double* __restrict__ us, double* __restrict__ vs, double* __restrict__ ws)
+{
+    const long total = (long)m.N[0] * m.N[1] * m.N[2];
+    const double f = dt / m.cellvol;
+    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+        const long c = cidx(m, i, j, k);
+        if (abs((int)band[c]) <= m.nband) continue; /* band cell: written by the SL update */
+        double Fx0[3], Fx1[3], Fy0[3], Fy1[3], Fz0[3], Fz1[3];
+        face_flux64(m, V, P, band, 0, i, j, k, dt, Fx0);
+        face_flux64(m, V, P, band, 0, i + 1, j, k, dt, Fx1);
+        face_flux64(m, V, P, band, 1, i, j, k, dt, Fy0);
+        face_flux64(m, V, P, band, 1, i, j + 1, k, dt, Fy1);
+        face_flux64(m, V, P, band, 2, i, j, k, dt, Fz0);
+        face_flux64(m, V, P, band, 2, i, j, k + 1, dt, Fz1);
+        us[c] = __ldg(P.u + c) + f * (((((Fx1[0] - Fx0[0]) + Fy1[0]) - Fy0[0]) + Fz1[0]) - Fz0[0]);
+        vs[c] = __ldg(P.v + c) + f * (((((Fx1[1] - Fx0[1]) + Fy1[1]) - Fy0[1]) + Fz1[1]) - Fz0[1]);
+        ws[c] = __ldg(P.w + c) + f * (((((Fx1[2] - Fx0[2]) + Fy1[2]) - Fy0[2]) + Fz1[2]) - Fz0[2]);
+    }
+}
+
+/* Phase codes (and mixed-path planes) of planes that were uploaded rather than computed:
+ * the same outputs as the PLIC pass derives from its own D. */
+__global__ void k_plic_phase(DevMesh m, const double* __restrict__ nx, const double* __restrict__ ny,
+                             const double* __restrict__ nz, double* D, float4* __restrict__ planes,
+                             signed char* __restrict__ phase)
+{
+    const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = (long)n0 * n1 * n2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int ip = (int)(t % n0) + m.lo, jp = (int)((t / n0) % n1) + m.lo, kp = (int)(t / ((long)n0 * n1)) + m.lo;
+        plic_outputs(m, t, ip, jp, kp, D[t], nx, ny, nz, D, planes, phase);
+    }
+}
+
+void launch_plic_phase(const DevMesh& m, const double* nx, const double* ny, const double* nz, double* D,
+                       float4* planes, signed char* phase, int nsm, cudaStream_t s)
+{
+    k_plic_phase<<<nsm * 8, 256, 0, s>>>(m, nx, ny, nz, D, planes, phase);
 }
 
 /* ---- launchers ------------------------------------------------------------------------ */
@@ -588,8 +731,21 @@ void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout,
 {
     (void)VFin;
     Vel64 V{uf, vf, wf};
-    Plic64 P{nx, ny, nz, D};
-    k_sl64<<<nsm * 8, SL_THREADS, 0, s>>>(m, dt, phase, VFout, V, P, list, count, work, errw);
+    Plic64 P{nx, ny, nz, D, nullptr, nullptr, nullptr, 0.0, 0.0};
+    k_sl64<false><<<nsm * 8, SL_THREADS, 0, s>>>(m, dt, phase, VFout, V, P, list, count, work, nullptr, nullptr,
+                                                 nullptr, errw);
+}
+
+void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const double* uf, const double* vf,
+                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                          const signed char* phase, const short* band, const double* u, const double* v,
+                          const double* w, double rho_liq, double rho_gas, double* us, double* vs, double* ws,
+                          const int* list, const int* count, int* work, int* errw, int nsm, cudaStream_t s)
+{
+    Vel64 V{uf, vf, wf};
+    Plic64 P{nx, ny, nz, D, u, v, w, rho_liq, rho_gas};
+    k_sl64<true><<<nsm * 8, SL_THREADS, 0, s>>>(m, dt, phase, VFout, V, P, list, count, work, us, vs, ws, errw);
+    k_mom_flux64<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, band, us, vs, ws);
 }
 
 } // namespace slvof

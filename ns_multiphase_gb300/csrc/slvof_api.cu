@@ -47,6 +47,8 @@ struct slvof_ctx {
     double *gnf[3] = {nullptr, nullptr, nullptr}, *gDf = nullptr;
     double *guf = nullptr, *gvf_ = nullptr, *gwf = nullptr;
     int* list_adj = nullptr;
+    /* momentum of transport! (allocated on first use): cell-centred velocities in, us/vs/ws out */
+    double *cu = nullptr, *cv = nullptr, *cw = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
     AdjCell* adj_cells = nullptr;
     AdjTet* adj_tets = nullptr;
     long adj_cells_cap = 0, adj_tets_cap = 0;
@@ -64,6 +66,7 @@ struct slvof_ctx {
     double* spheres = nullptr;
     int spheres_n = 0;
     bool normals_valid = false;
+    double rho_liq = 1.0, rho_gas = 1.0;
     double last_ms = 0.0;
     cudaStream_t own_stream = nullptr;
     cudaEvent_t sev[SLVOF_NSTAGES][2] = {};
@@ -220,6 +223,41 @@ int st_transport(slvof_ctx* c, double dt)
     return 0;
 }
 
+int mom_alloc(slvof_ctx* c)
+{
+    if (c->cu) return 0;
+    double** bufs[6] = {&c->cu, &c->cv, &c->cw, &c->us, &c->vs, &c->ws};
+    for (double** b : bufs) {
+        if (cudaMalloc((void**)b, c->ncell * sizeof(double)) != cudaSuccess ||
+            cudaMemset(*b, 0, c->ncell * sizeof(double)) != cudaSuccess)
+            return fail(c, SLVOF_E_NOMEM, "momentum buffers");
+    }
+    return 0;
+}
+
+/* transport!'s SL section with its momentum (src/Transport.jl:34-181, pressure_scheme
+ * "semi-lagrangian"), FP64. */
+int st_transport_mom(slvof_ctx* c, double dt)
+{
+    const int o = 1 - c->vcur;
+    CK(cudaMemsetAsync(c->ctr + C_SL, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_SLW, 0, sizeof(int), c->stream));
+    s_beg(c, S_CLASSIFY);
+    launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
+    s_end(c, S_CLASSIFY);
+    s_beg(c, S_SL);
+    launch_sl64_momentum(c->m, dt, c->VF[o], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->phase,
+                         c->band[c->bcur], c->cu, c->cv, c->cw, c->rho_liq, c->rho_gas, c->us, c->vs, c->ws,
+                         c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
+    s_end(c, S_SL);
+    s_beg(c, S_VFGHOST);
+    launch_vf_ghost(c->m, c->VF[c->vcur], c->VF[o], c->nsm, c->stream);
+    s_end(c, S_VFGHOST);
+    c->vcur = o;
+    c->normals_valid = false;
+    return 0;
+}
+
 int st_mass(slvof_ctx* c, double* mass, bool partials_ready)
 {
     s_beg(c, S_MASS);
@@ -341,6 +379,8 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     if (cudaMemcpy(c->coords, h.data(), ncoord * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(SLVOF_E_CUDA);
     mesh_fill(mesh, c->coords, c->m);
+    c->rho_liq = mesh->rho_liq;
+    c->rho_gas = mesh->rho_gas;
     *out = c;
     return SLVOF_OK;
 }
@@ -354,7 +394,8 @@ int slvof_destroy(slvof_ctx* c)
                     c->nz, c->D, c->planes, c->phase, c->cand, c->band[0], c->band[1], c->list_sl, c->list_if,
                     c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
-                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets};
+                    c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
+                    c->cu, c->cv, c->cw, c->us, c->vs, c->ws};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -440,6 +481,7 @@ int slvof_upload_plic(slvof_ctx* c, const double* nx, const double* ny, const do
     TRY(h2d(c, c->ny, ny, b));
     TRY(h2d(c, c->nz, nz, b));
     TRY(h2d(c, c->D, D, b));
+    launch_plic_phase(c->m, c->nx, c->ny, c->nz, c->D, c->planes, c->phase, c->nsm, c->stream);
     c->normals_valid = true;
     return finish(c, false);
 }
@@ -589,6 +631,7 @@ int slvof_transportSL(slvof_ctx* c, double dt, double* VF, const double* uf, con
     TRY(h2d(c, c->nz, nz, b));
     TRY(h2d(c, c->D, D, b));
     TRY(h2d(c, c->band[c->bcur], band, c->ncell * sizeof(short)));
+    launch_plic_phase(c->m, c->nx, c->ny, c->nz, c->D, c->planes, c->phase, c->nsm, c->stream);
     TRY(st_transport(c, dt));
     TRY(d2h(c, VF, c->VF[c->vcur], c->nvf * sizeof(double)));
     return finish(c);
@@ -654,6 +697,73 @@ int slvof_case_deformation3d(slvof_ctx* c, double t, double T)
     launch_case_deformation3d(c->m, t, T, c->uf, c->vf, c->wf, c->nsm, c->stream);
     to_float_velocity(c);
     return finish(c, false);
+}
+
+/* ---- momentum ---------------------------------------------------------------------------- */
+int slvof_upload_cell_velocity(slvof_ctx* c, const double* u, const double* v, const double* w)
+{
+    TRY(begin(c));
+    TRY(mom_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(h2d(c, c->cu, u, b));
+    TRY(h2d(c, c->cv, v, b));
+    TRY(h2d(c, c->cw, w, b));
+    return finish(c, false);
+}
+
+int slvof_download_momentum(slvof_ctx* c, double* us, double* vs, double* ws)
+{
+    TRY(begin(c));
+    TRY(mom_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(d2h(c, us, c->us, b));
+    TRY(d2h(c, vs, c->vs, b));
+    TRY(d2h(c, ws, c->ws, b));
+    return finish(c, false);
+}
+
+int slvof_transport_momentum(slvof_ctx* c, double dt)
+{
+    TRY(begin(c));
+    if (c->precision != SLVOF_FP64)
+        return fail(c, SLVOF_E_UNSUPPORTED, "the momentum of transport! runs in an FP64 context");
+    TRY(mom_alloc(c));
+    TRY(clear_err(c));
+    TRY(st_transport_mom(c, dt));
+    return finish(c);
+}
+
+int slvof_transportSL_momentum(slvof_ctx* c, double dt, double* VF, const double* uf, const double* vf,
+                               const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                               const int16_t* band, const double* u, const double* v, const double* w, double* us,
+                               double* vs, double* ws)
+{
+    TRY(begin(c));
+    if (c->precision != SLVOF_FP64)
+        return fail(c, SLVOF_E_UNSUPPORTED, "the momentum of transport! runs in an FP64 context");
+    TRY(mom_alloc(c));
+    TRY(clear_err(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(h2d(c, c->VF[c->vcur], VF, c->nvf * sizeof(double)));
+    TRY(h2d(c, c->uf, uf, b));
+    TRY(h2d(c, c->vf, vf, b));
+    TRY(h2d(c, c->wf, wf, b));
+    TRY(h2d(c, c->nx, nx, b));
+    TRY(h2d(c, c->ny, ny, b));
+    TRY(h2d(c, c->nz, nz, b));
+    TRY(h2d(c, c->D, D, b));
+    TRY(h2d(c, c->band[c->bcur], band, c->ncell * sizeof(short)));
+    TRY(h2d(c, c->cu, u, b));
+    TRY(h2d(c, c->cv, v, b));
+    TRY(h2d(c, c->cw, w, b));
+    /* phase codes of the uploaded planes */
+    launch_plic_phase(c->m, c->nx, c->ny, c->nz, c->D, c->planes, c->phase, c->nsm, c->stream);
+    TRY(st_transport_mom(c, dt));
+    TRY(d2h(c, VF, c->VF[c->vcur], c->nvf * sizeof(double)));
+    TRY(d2h(c, us, c->us, b));
+    TRY(d2h(c, vs, c->vs, b));
+    TRY(d2h(c, ws, c->ws, b));
+    return finish(c);
 }
 
 /* ---- reverse pass ----------------------------------------------------------------------- */

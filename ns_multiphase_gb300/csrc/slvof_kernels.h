@@ -39,6 +39,16 @@ void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout,
                  const signed char* phase, const int* list, const int* count, int* work, int* errw, int nsm,
                  cudaStream_t s);
 
+/* phase codes and mixed-path planes of uploaded normals and D */
+void launch_plic_phase(const DevMesh& m, const double* nx, const double* ny, const double* nz, double* D,
+                       float4* planes, signed char* phase, int nsm, cudaStream_t s);
+/* SL update with the momentum of transport! (us, vs, ws of every interior cell) */
+void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const double* uf, const double* vf,
+                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                          const signed char* phase, const short* band, const double* u, const double* v,
+                          const double* w, double rho_liq, double rho_gas, double* us, double* vs, double* ws,
+                          const int* list, const int* count, int* work, int* errw, int nsm, cudaStream_t s);
+
 /* k_mixed.cu, k_elvira_mixed.cu */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
                            const int* count, int* work, int* stats, signed char* cand, int* errw, int nsm,

@@ -57,6 +57,10 @@ SYMBOLS = [
     ("slvof_case_vf_spheres", _I, [_P, _P, _P, _I, _I, _I]),
     ("slvof_case_deformation3d", _I, [_P, _D, _D]),
     ("slvof_mass_noalloc", _I, [_P, _P, _P, _P]),
+    ("slvof_upload_cell_velocity", _I, [_P, _P, _P, _P]),
+    ("slvof_download_momentum", _I, [_P, _P, _P, _P]),
+    ("slvof_transport_momentum", _I, [_P, _D]),
+    ("slvof_transportSL_momentum", _I, [_P, _D] + [_P] * 15),
     ("slvof_prepare", _I, [_P]),
     ("slvof_copy_vf_device", _I, [_P, _P]),
     ("slvof_load_vf_device", _I, [_P, _P]),
@@ -245,6 +249,32 @@ class SLVOF:
             self.compute_band()
         self.compute_normal()
         self.compute_plic()
+
+    # ---- momentum of transport! -----------------------------------------------------------
+    def upload_cell_velocity(self, u, v, w):
+        s = self.mesh.cell_shape
+        self._check(self.L.slvof_upload_cell_velocity(self.h, _ptr(u, np.float64, s), _ptr(v, np.float64, s),
+                                                      _ptr(w, np.float64, s)), "upload_cell_velocity")
+
+    def download_momentum(self):
+        m = self.mesh
+        us, vs, ws = m.cell_array(), m.cell_array(), m.cell_array()
+        self._check(self.L.slvof_download_momentum(self.h, us.ctypes.data, vs.ctypes.data, ws.ctypes.data),
+                    "download_momentum")
+        return us, vs, ws
+
+    def transport_momentum(self, dt: float):
+        self._check(self.L.slvof_transport_momentum(self.h, dt), "transport_momentum")
+
+    def transportSL_momentum(self, dt, VF, uf, vf, wf, nx, ny, nz, D, band, u, v, w):
+        """SL + momentum sections of transport! (src/Transport.jl:34-181); returns us, vs, ws."""
+        m, s = self.mesh, self.mesh.cell_shape
+        us, vs, ws = m.cell_array(), m.cell_array(), m.cell_array()
+        args = [_ptr(VF, np.float64, m.vf_shape)] + [_ptr(a, np.float64, s) for a in (uf, vf, wf, nx, ny, nz, D)]
+        args += [_ptr(band, np.int16, s)] + [_ptr(a, np.float64, s) for a in (u, v, w)]
+        args += [us.ctypes.data, vs.ctypes.data, ws.ctypes.data]
+        self._check(self.L.slvof_transportSL_momentum(self.h, dt, *args), "transportSL_momentum")
+        return us, vs, ws
 
     def prepare(self):
         """Ghost fill, normals, PLIC and band of the current VF: the state a step starts from."""

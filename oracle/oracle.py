@@ -53,6 +53,10 @@ def lib():
         L.orc_tet_vol.argtypes = [p]
         L.orc_elvira.restype = i
         L.orc_elvira.argtypes = [p, p, p, p, p, i, i]
+        L.orc_transport_mom.restype = i
+        L.orc_transport_mom.argtypes = [p, d] + [p] * 16
+        L.orc_sl_flux_vol.restype = d
+        L.orc_sl_flux_vol.argtypes = [p, i, i, i, i, p, p, p, d]
         L.orc_compute_plic.restype = i
         L.orc_compute_plic.argtypes = [p, p, p, p, p, p]
         L.orc_compute_band.restype = i
@@ -129,6 +133,20 @@ class Oracle:
         flags = self.L.orc_transport(_m(self.mesh), dt, _p(VF), _p(VFnew), _p(uf), _p(vf), _p(wf),
                                      _p(nx), _p(ny), _p(nz), _p(D), _p(band), klo, khi)
         return flags, VFnew
+
+    def transport_mom(self, dt, VF, uf, vf, wf, nx, ny, nz, D, band, u, v, w):
+        """transport!'s SL loop with its momentum (pressure_scheme "semi-lagrangian"): VF is
+        updated in place; returns (flags, us, vs, ws)."""
+        m = self.mesh
+        VFnew = m.vf_array()
+        us, vs, ws = m.cell_array(), m.cell_array(), m.cell_array()
+        flags = self.L.orc_transport_mom(_m(m), dt, _p(VF), _p(VFnew), _p(uf), _p(vf), _p(wf), _p(nx), _p(ny),
+                                         _p(nz), _p(D), _p(band), _p(u), _p(v), _p(w), _p(us), _p(vs), _p(ws))
+        return flags, us, vs, ws
+
+    def sl_flux_vol(self, direction, i, j, k, uf, vf, wf, dt):
+        """SLfluxVol (src/VFgeom.jl:428-509); direction 0, 1, 2 for x, y, z."""
+        return self.L.orc_sl_flux_vol(_m(self.mesh), direction, i, j, k, _p(uf), _p(vf), _p(wf), dt)
 
     def sl_cell(self, dt, i, j, k, uf, vf, wf, nx, ny, nz, D):
         vol = ctypes.c_double()

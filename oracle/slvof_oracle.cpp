@@ -577,13 +577,15 @@ void pt2index(const Grid& G, int I[3], const double pt[3], int i, int j, int k, 
  * cutTet, src/VFgeom.jl:713-900, kept recursive as in the reference.
  * ------------------------------------------------------------------------------------- */
 struct Plic { const double *nx, *ny, *nz, *D; };
+/* cell-centred velocities and densities for the momentum sums of transport! (may be absent) */
+struct Mom { const double *u, *v, *w; double rho_liq, rho_gas; };
 
-struct CutOut { double vol, vLiq; };
+struct CutOut { double vol, vLiq, vrhoU, vrhoV, vrhoW, vrho; };
 
-CutOut cut_tet(const Grid& G, const Plic& P, double tet[4][3], int ind[4][3], bool xdone, bool ydone, bool zdone,
-               int lvl, Err* e)
+CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int ind[4][3], bool xdone, bool ydone,
+               bool zdone, int lvl, Err* e)
 {
-    if (lvl > 64) { e->flags |= E_DEPTH; return {0.0, 0.0}; }
+    if (lvl > 64) { e->flags |= E_DEPTH; return {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}; }
     int dir = -1, cut_ind = 0;
     double d[4];
     for (;;) {
@@ -616,22 +618,36 @@ CutOut cut_tet(const Grid& G, const Plic& P, double tet[4][3], int ind[4][3], bo
             const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
             for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
         }
-        double vol = 0.0, vLiq = 0.0;
+        CutOut r{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        const double uc = M ? M->u[c] : 0.0, vc = M ? M->v[c] : 0.0, wc = M ? M->w[c] : 0.0;
         for (int n = T_NTETS[cs]; n >= T_NNTET[cs]; --n) {
             double nt[4][3];
             for (int t = 0; t < 4; ++t)
                 for (int p = 0; p < 3; ++p) nt[t][p] = vert[T_VTET[cs][n - 1][t] - 1][p];
             const double tv = tet_vol(nt);
-            vol += tv;
-            vLiq += tv;
+            r.vol += tv;
+            r.vLiq += tv;
+            if (M) {
+                r.vrhoU += tv * uc * M->rho_liq;
+                r.vrhoV += tv * vc * M->rho_liq;
+                r.vrhoW += tv * wc * M->rho_liq;
+                r.vrho += tv * M->rho_liq;
+            }
         }
         for (int n = 1; n <= T_NNTET[cs] - 1; ++n) {
             double nt[4][3];
             for (int t = 0; t < 4; ++t)
                 for (int p = 0; p < 3; ++p) nt[t][p] = vert[T_VTET[cs][n - 1][t] - 1][p];
-            vol += tet_vol(nt);
+            const double tv = tet_vol(nt);
+            r.vol += tv;
+            if (M) {
+                r.vrhoU += tv * uc * M->rho_gas;
+                r.vrhoV += tv * vc * M->rho_gas;
+                r.vrhoW += tv * wc * M->rho_gas;
+                r.vrho += tv * M->rho_gas;
+            }
         }
-        return {vol, vLiq};
+        return r;
     }
     /* Cut by the mesh plane (src/VFgeom.jl:832-899). */
     double dc[4] = {d[0], d[1], d[2], d[3]};
@@ -664,7 +680,7 @@ CutOut cut_tet(const Grid& G, const Plic& P, double tet[4][3], int ind[4][3], bo
         vind[4 + n][dir][0] = cut_ind - 1;
         vind[4 + n][dir][1] = cut_ind;
     }
-    double vol = 0.0, vLiq = 0.0;
+    CutOut acc{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int n = 0; n < T_NTETS[cs]; ++n) {
         double ct[4][3];
         int ci[4][3];
@@ -676,16 +692,21 @@ CutOut cut_tet(const Grid& G, const Plic& P, double tet[4][3], int ind[4][3], bo
                 ci[nn][p] = vind[vt][p][side];
             }
         }
-        const CutOut r = cut_tet(G, P, ct, ci, xdone, ydone, zdone, lvl + 1, e);
-        vol += r.vol;
-        vLiq += r.vLiq;
+        const CutOut r = cut_tet(G, P, M, ct, ci, xdone, ydone, zdone, lvl + 1, e);
+        acc.vol += r.vol;
+        acc.vLiq += r.vLiq;
+        acc.vrhoU += r.vrhoU;
+        acc.vrhoV += r.vrhoV;
+        acc.vrhoW += r.vrhoW;
+        acc.vrho += r.vrho;
     }
-    return {vol, vLiq};
+    return acc;
 }
 
 /* SL update of one cell, src/Transport.jl:111-148 with cell2tets!(project_verts=true,
  * compute_indices=true) (src/VFgeom.jl:345-420). Returns VFnew. */
-double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out)
+double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out,
+               const Mom* M = nullptr, double* mom_out = nullptr)
 {
     double verts[15][3];
     const double tetsign = cell2verts(G, i, j, k, verts);
@@ -695,7 +716,7 @@ double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int
     tess_points(G.tess, verts);
     int vInds[15][3];
     for (int n = 0; n < tess_npoints(G.tess); ++n) pt2index(G, vInds[n], verts[n], i, j, k, e);
-    double vol = 0.0, vLiq = 0.0;
+    double vol = 0.0, vLiq = 0.0, vrhoU = 0.0, vrhoV = 0.0, vrhoW = 0.0, vrho = 0.0;
     for (int t = 0; t < tess_ntets(G.tess); ++t) {
         double tet[4][3];
         int ind[4][3];
@@ -706,13 +727,82 @@ double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int
                 tet[n][p] = verts[tv[n]][p];
                 ind[n][p] = vInds[tv[n]][p];
             }
-        const CutOut r = cut_tet(G, P, tet, ind, false, false, false, 1, e);
+        const CutOut r = cut_tet(G, P, M, tet, ind, false, false, false, 1, e);
         vol += tetsign * r.vol;
         vLiq += tetsign * r.vLiq;
+        vrhoU += tetsign * r.vrhoU;
+        vrhoV += tetsign * r.vrhoV;
+        vrhoW += tetsign * r.vrhoW;
+        vrho += tetsign * r.vrho;
     }
     if (!(vol > 0.0) || !std::isfinite(vol)) e->flags |= E_VOLUME;
     if (vol_out) *vol_out = vol;
+    /* us, vs, ws of the cell (src/Transport.jl:146-148) */
+    if (mom_out) { mom_out[0] = vrhoU / vrho; mom_out[1] = vrhoV / vrho; mom_out[2] = vrhoW / vrho; }
     return vLiq / vol;
+}
+
+/* ---------------------------------------------------------------------------------------
+ * Momentum of transport! (src/Transport.jl:34-104,146-166): face fluxes, SLfluxVol.
+ * ------------------------------------------------------------------------------------- */
+/* Vertices of the flux volume of face `dir` of cell (i,j,k) (src/VFgeom.jl:428-509): index
+ * offsets (di, dj, dk) and whether the point is projected, for even and odd cells. */
+const int FLUXV[3][2][8][4] = {
+    {{{0, 0, 0, 1}, {0, 0, 0, 0}, {0, 1, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 1}, {0, 0, 1, 0}, {0, 1, 1, 1}, {0, 1, 1, 0}},
+     {{0, 0, 0, 0}, {0, 0, 0, 1}, {0, 1, 0, 0}, {0, 1, 0, 1}, {0, 0, 1, 0}, {0, 0, 1, 1}, {0, 1, 1, 0}, {0, 1, 1, 1}}},
+    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 0, 1, 1}, {1, 0, 1, 1}, {0, 0, 1, 0}, {1, 0, 1, 0}},
+     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 0, 1, 1}, {0, 0, 1, 1}, {1, 0, 1, 0}, {0, 0, 1, 0}}},
+    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {1, 1, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {1, 1, 0, 0}},
+     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 0, 1}, {0, 1, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 1, 0, 0}, {0, 1, 0, 0}}}};
+
+double sl_flux_vol(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt)
+{
+    const bool even = G.tess != 5 || ((i + j + k) % 2) == 0;
+    const double tetsign = even ? 1.0 : -1.0;
+    double verts[15][3];
+    for (int n = 0; n < 8; ++n) {
+        const int* f = FLUXV[dir][even ? 0 : 1][n];
+        verts[n][0] = G.x(i + f[0]);
+        verts[n][1] = G.y(j + f[1]);
+        verts[n][2] = G.z(k + f[2]);
+        if (f[3]) project(G, V, verts[n], i, j, k, dt);
+    }
+    tess_points(G.tess, verts);
+    double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+    for (int t = 0; t < tess_ntets(G.tess); ++t) {
+        int tv[4];
+        tess_tet(G.tess, t, tv);
+        double tet[4][3];
+        for (int n = 0; n < 4; ++n)
+            for (int p = 0; p < 3; ++p) tet[n][p] = verts[tv[n]][p];
+        vol += tet_vol(tet);
+    }
+    return vol * tetsign;
+}
+
+/* Convective fluxes through face `dir` (0 x, 1 y, 2 z) at the low side of cell (i,j,k),
+ * src/Transport.jl:34-104 with pressure_scheme "semi-lagrangian". */
+void face_flux(const Grid& G, const Vel& V, const Mom& M, const int16_t* band, int dir, int i, int j, int k, double dt,
+               double F[3])
+{
+    const int li = i - (dir == 0), lj = j - (dir == 1), lk = k - (dir == 2);
+    const long c = G.c(i, j, k), l = G.c(li, lj, lk);
+    const double uface = 0.5 * (M.u[l] + M.u[c]);
+    const double vface = 0.5 * (M.v[l] + M.v[c]);
+    const double wface = 0.5 * (M.w[l] + M.w[c]);
+    const int nb = G.m->nband;
+    const bool bl = std::abs((int)band[l]) <= nb, bc = std::abs((int)band[c]) <= nb;
+    if (bl && bc) {
+        F[0] = 0.0; F[1] = 0.0; F[2] = 0.0;
+    } else if (bl || bc) {
+        const double vol = sl_flux_vol(G, V, dir, i, j, k, dt) / dt;
+        F[0] = -uface * vol; F[1] = -vface * vol; F[2] = -wface * vol;
+    } else {
+        const orc_mesh* Mm = G.m;
+        const double a = dir == 0 ? Mm->dy : Mm->dx, b = dir == 2 ? Mm->dy : Mm->dz;
+        const double q = dir == 0 ? V.uf[c] : (dir == 1 ? V.vf[c] : V.wf[c]);
+        F[0] = -uface * a * b * q; F[1] = -vface * a * b * q; F[2] = -wface * a * b * q;
+    }
 }
 
 } // namespace
@@ -879,6 +969,64 @@ int orc_transport(const orc_mesh* M, double dt, double* VF, double* VFnew, const
             for (int i = 1; i <= G.N[0]; ++i) VF[G.v(i, j, k)] = VFnew[G.v(i, j, k)];
     orc_vf_ghost_fill(M, VF);
     return flags;
+}
+
+/* transport!'s SL cell loop with its momentum (src/Transport.jl:34-166, pressure_scheme
+ * "semi-lagrangian"): VFnew as orc_transport, and us, vs, ws for every interior cell -- band
+ * cells from the clipped pre-image (vrhoU/vrho, ...), the others from the face fluxes.  VF is
+ * updated in place and its ghosts filled, as orc_transport does. */
+int orc_transport_mom(const orc_mesh* M, double dt, double* VF, double* VFnew, const double* uf, const double* vf,
+                      const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                      const int16_t* band, const double* u, const double* v, const double* w, double* us, double* vs,
+                      double* ws)
+{
+    Grid G(M);
+    Vel V{uf, vf, wf};
+    Plic P{nx, ny, nz, D};
+    Mom Mo{u, v, w, M->rho_liq, M->rho_gas};
+    int flags = 0;
+    const double cv = (M->dx * M->dy) * M->dz;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : flags)
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j) {
+            Err e;
+            for (int i = 1; i <= G.N[0]; ++i) {
+                const long c = G.c(i, j, k);
+                const long vv = G.v(i, j, k);
+                if (std::abs((int)band[c]) <= M->nband) {
+                    double mom[3];
+                    VFnew[vv] = sl_cell(G, V, P, dt, i, j, k, &e, nullptr, &Mo, mom);
+                    us[c] = mom[0]; vs[c] = mom[1]; ws[c] = mom[2];
+                } else {
+                    VFnew[vv] = VF[vv];
+                    double Fx0[3], Fx1[3], Fy0[3], Fy1[3], Fz0[3], Fz1[3];
+                    face_flux(G, V, Mo, band, 0, i, j, k, dt, Fx0);
+                    face_flux(G, V, Mo, band, 0, i + 1, j, k, dt, Fx1);
+                    face_flux(G, V, Mo, band, 1, i, j, k, dt, Fy0);
+                    face_flux(G, V, Mo, band, 1, i, j + 1, k, dt, Fy1);
+                    face_flux(G, V, Mo, band, 2, i, j, k, dt, Fz0);
+                    face_flux(G, V, Mo, band, 2, i, j, k + 1, dt, Fz1);
+                    const double f = dt / cv;
+                    us[c] = u[c] + f * (((((Fx1[0] - Fx0[0]) + Fy1[0]) - Fy0[0]) + Fz1[0]) - Fz0[0]);
+                    vs[c] = v[c] + f * (((((Fx1[1] - Fx0[1]) + Fy1[1]) - Fy0[1]) + Fz1[1]) - Fz0[1]);
+                    ws[c] = w[c] + f * (((((Fx1[2] - Fx0[2]) + Fy1[2]) - Fy0[2]) + Fz1[2]) - Fz0[2]);
+                }
+            }
+            flags |= e.flags;
+        }
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i) VF[G.v(i, j, k)] = VFnew[G.v(i, j, k)];
+    orc_vf_ghost_fill(M, VF);
+    return flags;
+}
+
+double orc_sl_flux_vol(const orc_mesh* M, int dir, int i, int j, int k, const double* uf, const double* vf,
+                       const double* wf, double dt)
+{
+    Grid G(M);
+    Vel V{uf, vf, wf};
+    return sl_flux_vol(G, V, dir, i, j, k, dt);
 }
 
 /* Pre-image of one cell: projected vertices and indices + the SL result, for unit tests. */

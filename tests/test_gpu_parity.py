@@ -232,3 +232,66 @@ def test_zalesak_rotation_projection():
     gx, gy, gz = g.download_normals()
     assert_same(gx, nx, "nx")
     assert_same(g.download_plic(), D, "D")
+
+
+def momentum_state(tess):
+    m = Mesh(Nx=18, Ny=16, Nz=14, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess, rho_liq=1000.0, rho_gas=1.2)
+    VF = cases.vf_spheres(m, [[0.45, 0.5, 0.48]], [0.23], nF=8)
+    o = Oracle(m)
+    VFo = VF.copy(order="F")
+    band, nx, ny, nz, D = o.init_state(VFo)
+    uf, vf, wf = cases.deformation3d_faces(m, 0.25, 3.0)
+    # cell-centred velocities: face averages plus a smooth perturbation
+    u = np.asfortranarray(0.5 * (uf + np.roll(uf, -1, axis=0)) + 0.1 * np.sin(3 * m.xm)[:, None, None])
+    v = np.asfortranarray(0.5 * (vf + np.roll(vf, -1, axis=1)) - 0.07 * np.cos(2 * m.ym)[None, :, None])
+    w = np.asfortranarray(0.5 * (wf + np.roll(wf, -1, axis=2)) + 0.05)
+    dt = 0.5 * m.dx / 2.0
+    return m, o, VFo, band, nx, ny, nz, D, uf, vf, wf, u, v, w, dt
+
+
+@pytest.mark.parametrize("tess", ["5_tets", "24_tets"])
+def test_transport_momentum_matches_restatement(tess):
+    """transport!'s momentum (src/Transport.jl:34-166): us, vs, ws of every interior cell, band
+    cells from the clip with rho_liq/rho_gas, the others from FD fluxes and SL flux volumes at
+    the band edges; bit for bit against the restatement, host drop-in and resident call."""
+    m, o, VFo, band, nx, ny, nz, D, uf, vf, wf, u, v, w, dt = momentum_state(tess)
+    g = ctx(m)
+    VFg = VFo.copy(order="F")
+    us, vs, ws = g.transportSL_momentum(dt, VFg, uf, vf, wf, nx, ny, nz, D, band, u, v, w)
+    flags, uso, vso, wso = o.transport_mom(dt, VFo, uf, vf, wf, nx, ny, nz, D, band, u, v, w)
+    assert flags == 0
+    assert_same(VFg, VFo, "VF")
+    for a, b, name in ((us, uso, "us"), (vs, vso, "vs"), (ws, wso, "ws")):
+        assert_same(m.interior(a), m.interior(b), name)
+    inner = np.abs(m.interior(band).astype(int))
+    assert (inner <= m.nband).any() and (inner > m.nband).any()
+    # resident: state, velocities and the momentum call
+    m2, o2, VF2, band2, nx2, ny2, nz2, D2, uf2, vf2, wf2, u2, v2, w2, dt2 = momentum_state(tess)
+    g2 = ctx(m2)
+    g2.upload_vf(VF2)
+    g2.vf_ghost_fill()
+    g2.init_state()
+    g2.upload_velocity(uf2, vf2, wf2)
+    g2.upload_cell_velocity(u2, v2, w2)
+    g2.transport_momentum(dt2)
+    r = g2.download_momentum()
+    for a, b, name in zip(r, (uso, vso, wso), ("us", "vs", "ws")):
+        assert_same(m2.interior(a), m2.interior(b), "resident " + name)
+
+
+def test_host_transport_refreshes_phase_codes_of_uploaded_planes():
+    """A drop-in call on a context that last held another state: the pure-donor codes come
+    from the uploaded planes, not from the previous state."""
+    m, VF = spheres_mesh(N=16, seed=3)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    m2, VFb = spheres_mesh(N=16, seed=11)
+    o2 = Oracle(m2)
+    VFb = VFb.copy(order="F")
+    band_b, nxb, nyb, nzb, Db = o2.init_state(VFb)
+    uf, vf, wf = cases.deformation3d_faces(m2, 0.4, 3.0)
+    dt = 0.5 * m2.dx / 2.0
+    VFg = VFb.copy(order="F")
+    g.transportSL(dt, VFg, uf, vf, wf, nxb, nyb, nzb, Db, band_b)
+    flags, _ = o2.transport(dt, VFb, uf, vf, wf, nxb, nyb, nzb, Db, band_b)
+    assert flags == 0
+    assert_same(VFg, VFb, "VF")
