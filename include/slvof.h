@@ -57,7 +57,8 @@ typedef struct slvof_mesh {
                            test_case "Zalesak" (src/Tools.jl:396-399) */
     int32_t xper, yper, zper;
     double Lx, Ly, Lz, dx, dy, dz;
-    double VFlo, VFhi, rho_liq, rho_gas;
+    double VFlo, VFhi, rho_liq, rho_gas; /* VFlo, VFhi > 0 and finite (src/Parameters.jl:68-69 default
+                                            1e-10 and 1 - VFlo); others give SLVOF_E_UNSUPPORTED */
     const double *x, *y, *z;
     const double *xm, *ym, *zm;
     int32_t tesselation; /* param.tesselation (src/Parameters.jl:77): 5 "5_tets" (also 0), 6 "6_tets",

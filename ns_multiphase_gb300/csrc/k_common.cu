@@ -32,84 +32,92 @@ __global__ void k_vf_ghost(DevMesh m, const double* __restrict__ VFin, double* _
     }
 }
 
-/* ELVIRA! pure cells (src/ELVIRA.jl:19-46), the interface-cell list for the candidate
- * kernel, and per-block compensated partial sums of the interior VF. */
-constexpr int PURE_THREADS = 256;
+constexpr int PURE_BX = 32, PURE_BY = 8; /* pure-cell tile: 32 i x 8 j of one k plane */
 
-__global__ void __launch_bounds__(PURE_THREADS) k_elvira_pure(DevMesh m, const double* __restrict__ VF,
-                                                              double* __restrict__ nx, double* __restrict__ ny,
-                                                              double* __restrict__ nz, int* list, int* count,
-                                                              double* partials)
+/* ELVIRA! for pure cells (src/ELVIRA.jl:19-46): the axis normal from the first face
+ * neighbour of the opposite phase (x-, x+, y-, y+, z-, z+), zero otherwise; interface cells
+ * go to the candidate list.  The interior VF is also summed for the mass, exactly: each value
+ * in 62-bit fixed point, 128-bit integer sums, one partial per block.  A thread per cell,
+ * (i, j) from the block's tile and k from the grid, and threshold tests on the bit patterns,
+ * so the pass runs on the integer pipes. */
+__global__ void __launch_bounds__(PURE_BX * PURE_BY) k_elvira_pure(DevMesh m, const double* __restrict__ VF,
+                                                                   double* __restrict__ nx, double* __restrict__ ny,
+                                                                   double* __restrict__ nz, int* list, int* count,
+                                                                   long long* partials)
 {
-    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
-    const long total = N0 * N1 * N2;
-    const double lo = m.VFlo, hi = m.VFhi;
+    const int i = 1 + blockIdx.x * PURE_BX + threadIdx.x, j = 1 + blockIdx.y * PURE_BY + threadIdx.y;
+    const int k = 1 + blockIdx.z;
+    const long long lo = dbits(m.VFlo), hi = dbits(m.VFhi);
     const long sj = m.vs1, sk = m.vs2;
-    Comp acc{0.0, 0.0};
-    const long stride = (long)gridDim.x * blockDim.x;
-    for (long base = blockIdx.x * (long)blockDim.x; base < total; base += stride) {
-        const long t = base + threadIdx.x;
-        bool iface = false;
-        if (t < total) {
-            const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
-            const long v = vidx(m, i, j, k);
-            const double c = VF[v];
-            comp_add(acc, c);
-            double ax = 0.0, ay = 0.0, az = 0.0;
-            if (c >= lo && c <= hi) {
-                iface = true;
-            } else if (c < lo) {
-                if (VF[v - 1] > hi) ax = 1.0;
-                else if (VF[v + 1] > hi) ax = -1.0;
-                else if (VF[v - sj] > hi) ay = 1.0;
-                else if (VF[v + sj] > hi) ay = -1.0;
-                else if (VF[v - sk] > hi) az = 1.0;
-                else if (VF[v + sk] > hi) az = -1.0;
-            } else if (c > hi) {
-                if (VF[v - 1] < lo) ax = -1.0;
-                else if (VF[v + 1] < lo) ax = 1.0;
-                else if (VF[v - sj] < lo) ay = -1.0;
-                else if (VF[v + sj] < lo) ay = 1.0;
-                else if (VF[v - sk] < lo) az = -1.0;
-                else if (VF[v + sk] < lo) az = 1.0;
-            }
-            if (nx) {
-                const long o = cidx(m, i, j, k);
-                nx[o] = ax; ny[o] = ay; nz[o] = az;
-            }
+    __int128 acc = 0;
+    bool iface = false;
+    int L = 0;
+    if (i <= m.N[0] && j <= m.N[1]) {
+        L = (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1];
+        const long v = vidx(m, i, j, k);
+        const double c = VF[v];
+        const long long cb = dbits(c);
+        acc = fx62(c);
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        if (bits_below(cb, lo)) {
+            if (bits_above(dbits(VF[v - 1]), hi)) ax = 1.0;
+            else if (bits_above(dbits(VF[v + 1]), hi)) ax = -1.0;
+            else if (bits_above(dbits(VF[v - sj]), hi)) ay = 1.0;
+            else if (bits_above(dbits(VF[v + sj]), hi)) ay = -1.0;
+            else if (bits_above(dbits(VF[v - sk]), hi)) az = 1.0;
+            else if (bits_above(dbits(VF[v + sk]), hi)) az = -1.0;
+        } else if (bits_above(cb, hi)) {
+            if (bits_below(dbits(VF[v - 1]), lo)) ax = -1.0;
+            else if (bits_below(dbits(VF[v + 1]), lo)) ax = 1.0;
+            else if (bits_below(dbits(VF[v - sj]), lo)) ay = -1.0;
+            else if (bits_below(dbits(VF[v + sj]), lo)) ay = 1.0;
+            else if (bits_below(dbits(VF[v - sk]), lo)) az = -1.0;
+            else if (bits_below(dbits(VF[v + sk]), lo)) az = 1.0;
+        } else {
+            iface = true; /* VFlo <= VF <= VFhi (or NaN, as the reference's compares) */
         }
-        if (list) warp_append(iface, (int)t, list, count);
+        if (nx) {
+            const long o = cidx(m, i, j, k);
+            nx[o] = ax; ny[o] = ay; nz[o] = az;
+        }
     }
-    /* block reduction of the compensated pair */
-    for (int off = 16; off > 0; off >>= 1) {
-        Comp o{__shfl_down_sync(0xffffffffu, acc.s, off), __shfl_down_sync(0xffffffffu, acc.c, off)};
-        comp_merge(acc, o);
-    }
-    __shared__ double ss[PURE_THREADS / 32], sc[PURE_THREADS / 32];
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { ss[w] = acc.s; sc[w] = acc.c; }
+    if (list) warp_append(iface, L, list, count);
+    /* block sum: exact, so its order does not matter */
+    for (int off = 16; off > 0; off >>= 1) acc += i128_shfl_down(acc, off);
+    __shared__ long long sh_hi[PURE_BX * PURE_BY / 32];
+    __shared__ unsigned long long sh_lo[PURE_BX * PURE_BY / 32];
+    const int t = threadIdx.y * PURE_BX + threadIdx.x, w = t >> 5;
+    if ((t & 31) == 0) { sh_hi[w] = (long long)(acc >> 64); sh_lo[w] = (unsigned long long)acc; }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        Comp b{ss[0], sc[0]};
-        for (int q = 1; q < PURE_THREADS / 32; ++q) comp_merge(b, Comp{ss[q], sc[q]});
-        partials[2 * blockIdx.x] = b.s;
-        partials[2 * blockIdx.x + 1] = b.c;
+    if (t == 0) {
+        __int128 b = 0;
+        for (int q = 0; q < PURE_BX * PURE_BY / 32; ++q) b += i128_from(sh_hi[q], sh_lo[q]);
+        const long blk = blockIdx.x + (long)gridDim.x * (blockIdx.y + (long)gridDim.y * blockIdx.z);
+        partials[2 * blk] = (long long)(b >> 64);
+        partials[2 * blk + 1] = (long long)(unsigned long long)b;
     }
 }
 
-/* One warp: lane l merges blocks l, l+32, ... in order, then a fixed shuffle tree (the same
- * order every call). */
-__global__ void k_mass_final(const double* __restrict__ partials, int nblocks, double cellvol, double* out)
+/* Sum of the exact partials, scaled: mass = sum(VF) * dx*dy*dz (src/WriteData.jl:33).  One
+ * block of MASS_THREADS; integer sums, so the order is free. */
+constexpr int MASS_THREADS = 1024;
+__global__ void __launch_bounds__(MASS_THREADS) k_mass_final(const long long* __restrict__ partials, long nblocks,
+                                                             double cellvol, double* out)
 {
-    if (blockIdx.x != 0 || threadIdx.x >= 32) return;
-    const int lane = threadIdx.x;
-    Comp a{0.0, 0.0};
-    for (int b = lane; b < nblocks; b += 32) comp_merge(a, Comp{partials[2 * b], partials[2 * b + 1]});
-    for (int off = 16; off > 0; off >>= 1) {
-        const Comp o{__shfl_down_sync(0xffffffffu, a.s, off), __shfl_down_sync(0xffffffffu, a.c, off)};
-        comp_merge(a, o);
+    __int128 a = 0;
+    for (long b = threadIdx.x; b < nblocks; b += MASS_THREADS)
+        a += i128_from(partials[2 * b], (unsigned long long)partials[2 * b + 1]);
+    for (int off = 16; off > 0; off >>= 1) a += i128_shfl_down(a, off);
+    __shared__ long long sh_hi[MASS_THREADS / 32];
+    __shared__ unsigned long long sh_lo[MASS_THREADS / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) { sh_hi[w] = (long long)(a >> 64); sh_lo[w] = (unsigned long long)a; }
+    __syncthreads();
+    if (w == 0) {
+        a = i128_from(sh_hi[lane], sh_lo[lane]);
+        for (int off = 16; off > 0; off >>= 1) a += i128_shfl_down(a, off);
+        if (lane == 0) out[0] = ldexp(i128_to_double(a), -62) * cellvol;
     }
-    if (lane == 0) out[0] = (a.s + a.c) * cellvol;
 }
 
 /* update_borders!(nx/ny/nz) after ELVIRA! zeroed the whole arrays (src/ELVIRA.jl:11-13,50-52):
@@ -193,18 +201,19 @@ __global__ void __launch_bounds__(BX * BY) k_band_first(DevMesh m, const double*
                                                        short* __restrict__ bout)
 {
     const short nb1 = (short)(m.nband + 1);
+    const long long lob = dbits(m.VFlo), hib = dbits(m.VFhi);
     auto cls = [&](int a, int b, int c) -> unsigned char {
         /* the halo reaches index 0 and N+1 (ghost cells); beyond the tile's cells of a partial
          * tile it stays inside the ghost layers (g >= 3) */
         const int aa = min(a, m.N[0] + 1), bb = min(b, m.N[1] + 1);
-        const double v = __ldg(VF + vidx(m, aa, bb, c));
-        return (unsigned char)((v >= m.VFhi ? 1 : 0) | (v <= m.VFlo ? 2 : 0));
+        const long long v = dbits(__ldg(VF + vidx(m, aa, bb, c)));
+        return (unsigned char)((!bits_below(v, hib) ? 1 : 0) | (!bits_above(v, lob) ? 2 : 0));
     };
     auto fin = [&](int i, int j, int k, unsigned char any) {
-        const double c = __ldg(VF + vidx(m, i, j, k));
+        const long long c = dbits(__ldg(VF + vidx(m, i, j, k)));
         short b = 0;
-        if (c < m.VFlo) b = (any & 1) ? (short)0 : (short)-nb1;
-        else if (c > m.VFhi) b = (any & 2) ? (short)0 : nb1;
+        if (bits_below(c, lob)) b = (any & 1) ? (short)0 : (short)-nb1;
+        else if (bits_above(c, hib)) b = (any & 2) ? (short)0 : nb1;
         bout[cidx(m, i, j, k)] = b;
     };
     band_march(m, cls, fin);
@@ -362,18 +371,23 @@ void launch_vf_ghost(const DevMesh& m, const double* VFin, double* VFout, int ns
 {
     k_vf_ghost<<<nsm * 8, 256, 0, s>>>(m, VFin, VFout);
 }
-void launch_elvira_pure(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, int* list, int* count,
-                        double* partials, int nblocks, cudaStream_t s)
+long pure_blocks(long nx, long ny, long nz)
 {
-    k_elvira_pure<<<nblocks, PURE_THREADS, 0, s>>>(m, VF, nx, ny, nz, list, count, partials);
+    return ((nx + PURE_BX - 1) / PURE_BX) * ((ny + PURE_BY - 1) / PURE_BY) * nz;
+}
+void launch_elvira_pure(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, int* list, int* count,
+                        long long* partials, cudaStream_t s)
+{
+    const dim3 grid((m.N[0] + PURE_BX - 1) / PURE_BX, (m.N[1] + PURE_BY - 1) / PURE_BY, m.N[2]);
+    k_elvira_pure<<<grid, dim3(PURE_BX, PURE_BY), 0, s>>>(m, VF, nx, ny, nz, list, count, partials);
 }
 void launch_normal_ghost(const DevMesh& m, double* nx, double* ny, double* nz, int nsm, cudaStream_t s)
 {
     k_normal_ghost<<<nsm * 8, 256, 0, s>>>(m, nx, ny, nz);
 }
-void launch_mass_final(const double* partials, int nblocks, double cellvol, double* out, cudaStream_t s)
+void launch_mass_final(const long long* partials, long nblocks, double cellvol, double* out, cudaStream_t s)
 {
-    k_mass_final<<<1, 32, 0, s>>>(partials, nblocks, cellvol, out);
+    k_mass_final<<<1, MASS_THREADS, 0, s>>>(partials, nblocks, cellvol, out);
 }
 void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s)
 {

@@ -153,8 +153,11 @@ __global__ void __launch_bounds__(EL_WARPS * 32) k_elvira_iface64(DevMesh m, con
  * arithmetic is done for the 97% of cells that are pure.  Threads map to (i, j) of a plane
  * and blocks to k, so no index divides. */
 __global__ void k_plic_pure(DevMesh m, const double* __restrict__ VF, double* __restrict__ D,
-                            float4* __restrict__ planes, signed char* __restrict__ phase, int* list, int* count)
+                            float4* __restrict__ planes, signed char* __restrict__ phase, int* list, int* count,
+                            float Lsum_f)
 {
+    /* the thresholds are tested on the bit patterns (integer pipe), the outputs are copies */
+    const long long lob = dbits(m.VFlo), hib = dbits(m.VFhi);
     const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g;
     const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y * blockDim.y + threadIdx.y;
     const int c = blockIdx.z;
@@ -166,12 +169,12 @@ __global__ void k_plic_pure(DevMesh m, const double* __restrict__ VF, double* __
         const int i = ghost_src_1d(ip, m.N[0], m.g, m.per[0], false);
         const int j = ghost_src_1d(jp, m.N[1], m.g, m.per[1], false);
         const int k = ghost_src_1d(kp, m.N[2], m.g, m.per[2], false);
-        const double v = VF[vidx(m, i, j, k)];
-        if (v < m.VFlo || v > m.VFhi) {
-            const double dist = v < m.VFlo ? -m.Lsum : m.Lsum;
-            D[t] = dist;
-            phase[t] = v < m.VFlo ? -1 : 1;
-            if (planes) planes[t] = make_float4(0.f, 0.f, 0.f, (float)dist);
+        const long long v = dbits(VF[vidx(m, i, j, k)]);
+        const bool gas = bits_below(v, lob);
+        if (gas || bits_above(v, hib)) {
+            D[t] = gas ? -m.Lsum : m.Lsum;
+            phase[t] = gas ? -1 : 1;
+            if (planes) planes[t] = make_float4(0.f, 0.f, 0.f, gas ? -Lsum_f : Lsum_f);
         } else {
             defer = true; /* interface (or NaN) source */
         }
@@ -717,7 +720,7 @@ void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const d
                    float4* planes, signed char* phase, int* list, int* count, bool newton_root, int nsm, cudaStream_t s)
 {
     const dim3 grid((m.N[0] + 2 * m.g + 31) / 32, (m.N[1] + 2 * m.g + 7) / 8, m.N[2] + 2 * m.g);
-    k_plic_pure<<<grid, dim3(32, 8), 0, s>>>(m, VF, D, planes, phase, list, count);
+    k_plic_pure<<<grid, dim3(32, 8), 0, s>>>(m, VF, D, planes, phase, list, count, (float)m.Lsum);
     if (newton_root)
         launch_plic_iface_newton(m, VF, nx, ny, nz, D, planes, phase, list, count, nsm, s);
     else

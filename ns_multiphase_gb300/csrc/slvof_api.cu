@@ -58,8 +58,8 @@ struct slvof_ctx {
     int* list_if = nullptr;
     int* list_plic = nullptr; /* cells whose PLIC solve is deferred to full warps */
     int* ctr = nullptr; /* 0 sl count, 1 if count, 2 sl work, 3 if work, 4 error bits */
-    double* partials = nullptr;
-    int npure = 0;
+    long long* partials = nullptr; /* exact mass partials, (high, low) words of a 128-bit sum per block */
+    long npure = 0;
     double* mass_d = nullptr;
     double* table = nullptr; /* case generator scratch */
     int table_n = 0;
@@ -152,8 +152,7 @@ int st_normals(slvof_ctx* c)
     CK(cudaMemsetAsync(c->ctr + C_IFW, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->ctr + C_ARB, 0, sizeof(int), c->stream));
     s_beg(c, S_PURE);
-    launch_elvira_pure(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->partials, c->npure,
-                       c->stream);
+    launch_elvira_pure(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->partials, c->stream);
     s_end(c, S_PURE);
     s_beg(c, S_IFACE);
     if (c->precision == SLVOF_FP64)
@@ -262,8 +261,7 @@ int st_mass(slvof_ctx* c, double* mass, bool partials_ready)
 {
     s_beg(c, S_MASS);
     if (!partials_ready)
-        launch_elvira_pure(c->m, c->VF[c->vcur], nullptr, nullptr, nullptr, nullptr, nullptr, c->partials, c->npure,
-                           c->stream);
+        launch_elvira_pure(c->m, c->VF[c->vcur], nullptr, nullptr, nullptr, nullptr, nullptr, c->partials, c->stream);
     launch_mass_final(c->partials, c->npure, c->m.cellvol, c->mass_d, c->stream);
     s_end(c, S_MASS);
     CK(cudaMemcpyAsync(mass, c->mass_d, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -321,6 +319,9 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     if (mesh->tesselation != 0 && mesh->tesselation != 5 && mesh->tesselation != 6 && mesh->tesselation != 24)
         return SLVOF_E_ARG;
     if (!mesh->x || !mesh->y || !mesh->z || !mesh->xm || !mesh->ym || !mesh->zm) return SLVOF_E_ARG;
+    /* the pure/interface thresholds are compared as bit patterns, which orders doubles like the
+     * floating-point compare only against positive finite thresholds */
+    if (!(mesh->VFlo > 0.0 && mesh->VFhi > 0.0 && mesh->VFlo < 1e300 && mesh->VFhi < 1e300)) return SLVOF_E_UNSUPPORTED;
     const long g = mesh->nghost;
     const long N[3] = {mesh->Nx, mesh->Ny, mesh->Nz};
     const long n0 = N[0] + 2 * g, n1 = N[1] + 2 * g, n2 = N[2] + 2 * g;
@@ -342,7 +343,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     c->ncell = n0 * n1 * n2;
     c->nvf = (n0 + 6) * (n1 + 6) * (n2 + 6);
     const long interior = N[0] * N[1] * N[2];
-    c->npure = c->nsm * 8;
+    c->npure = pure_blocks(N[0], N[1], N[2]);
     auto alloc = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess && cudaMemset(*p, 0, bytes) == cudaSuccess; };
     const long ncoord = mesh_coords(mesh, nullptr);
     bool ok = alloc((void**)&c->coords, ncoord * sizeof(double)) && alloc((void**)&c->VF[0], c->nvf * sizeof(double)) &&
@@ -355,7 +356,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
               alloc((void**)&c->band[0], c->ncell * sizeof(short)) && alloc((void**)&c->band[1], c->ncell * sizeof(short)) &&
               alloc((void**)&c->list_sl, interior * sizeof(int)) && alloc((void**)&c->list_if, interior * sizeof(int)) &&
               alloc((void**)&c->list_plic, c->ncell * sizeof(int)) &&
-              alloc((void**)&c->ctr, C_N * sizeof(int)) && alloc((void**)&c->partials, 2 * c->npure * sizeof(double)) &&
+              alloc((void**)&c->ctr, C_N * sizeof(int)) && alloc((void**)&c->partials, 2 * c->npure * sizeof(long long)) &&
               alloc((void**)&c->mass_d, sizeof(double));
     if (ok && precision == SLVOF_MIXED)
         ok = alloc((void**)&c->uf32, c->ncell * sizeof(float)) && alloc((void**)&c->vf32, c->ncell * sizeof(float)) &&

@@ -174,6 +174,53 @@ __device__ __forceinline__ void warp_append(bool flag, int item, int* list, int*
     if (flag) list[base + __popc(ballot & ((1u << lane) - 1))] = item;
 }
 
+/* ---- VF thresholds and sums on the integer pipe ------------------------------------------
+ * GB300 issues double compares and adds on its narrow FP64 pipe.  For a positive threshold t
+ * and any double x, x < t exactly when the bit pattern of x, read as a signed 64-bit integer,
+ * is below that of t (negative x have the sign bit set); NaN is neither below nor above, as
+ * in the floating-point compare. */
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ bool bits_nan(long long b) { return (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL; }
+__device__ __forceinline__ bool bits_below(long long b, long long t) { return b < t && !bits_nan(b); }
+__device__ __forceinline__ bool bits_above(long long b, long long t) { return b > t && !bits_nan(b); }
+
+/* round(x * 2^62) for |x| < 2, from the bit pattern (zero for subnormals, saturated for
+ * |x| >= 2 and non-finite values).  Volume fractions summed in this fixed point with 128-bit
+ * integers give an exact, order-independent sum. */
+__device__ __forceinline__ long long fx62(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return 0;
+    const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    const int sh = e - 1023 + 10; /* x * 2^62 = mant * 2^(e - 1023 - 52 + 62) */
+    long long r;
+    if (sh >= 11) r = 0x7FFFFFFFFFFFFFFFLL;
+    else if (sh >= 0) r = (long long)(mant << sh);
+    else if (sh > -60) r = (long long)((mant + (1ull << (-sh - 1))) >> (-sh));
+    else r = 0;
+    return (b >> 63) ? -r : r;
+}
+
+/* 128-bit integer in two 64-bit words, for warp shuffles and storage */
+__device__ __forceinline__ __int128 i128_from(long long hi, unsigned long long lo)
+{
+    return (__int128)(((unsigned __int128)(unsigned long long)hi << 64) | lo);
+}
+__device__ __forceinline__ __int128 i128_shfl_down(__int128 x, int off)
+{
+    const long long hi = (long long)(x >> 64);
+    const unsigned long long lo = (unsigned long long)x;
+    return i128_from(__shfl_down_sync(0xffffffffu, hi, off), __shfl_down_sync(0xffffffffu, lo, off));
+}
+__device__ __forceinline__ double i128_to_double(__int128 x)
+{
+    const bool neg = x < 0;
+    const unsigned __int128 u = neg ? (unsigned __int128)(-x) : (unsigned __int128)x;
+    const double r = (double)(unsigned long long)(u >> 64) * 18446744073709551616.0 + (double)(unsigned long long)u;
+    return neg ? -r : r;
+}
+
 /* Neumaier-compensated pair (sum, correction). */
 struct Comp {
     double s, c;

@@ -9,10 +9,12 @@ namespace slvof {
 
 /* k_common.cu */
 void launch_vf_ghost(const DevMesh& m, const double* VFin, double* VFout, int nsm, cudaStream_t s);
+/* pure-cell normals, interface list and exact mass partials: pure_blocks(m) pairs of int64 */
+long pure_blocks(long nx, long ny, long nz);
 void launch_elvira_pure(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, int* list, int* count,
-                        double* partials, int nblocks, cudaStream_t s);
+                        long long* partials, cudaStream_t s);
 void launch_normal_ghost(const DevMesh& m, double* nx, double* ny, double* nz, int nsm, cudaStream_t s);
-void launch_mass_final(const double* partials, int nblocks, double cellvol, double* out, cudaStream_t s);
+void launch_mass_final(const long long* partials, long nblocks, double cellvol, double* out, cudaStream_t s);
 void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s);
 void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neumann, int nsm, cudaStream_t s);
 void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, int nsm, cudaStream_t s);
