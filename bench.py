@@ -156,31 +156,43 @@ def timed_steps(g, dt, steps, torch):
     return e0.elapsed_time(e1), {k: v / steps for k, v in stage.items()}
 
 
-def adjoint_timing(g, m, dt, steps, torch, fwd64_ms, fwd_mixed_ms):
-    """Reverse of one step (slvof_adjoint_step, FP64) from the context's current state, seeded
-    with dL/dVF = seeded normal weights on the interior; CUDA events on the launching stream,
-    one untimed call first.  Compared with the FP64 and the mixed forward step."""
+def adjoint_timing(g, m, dt, steps, torch, next_ptr=None):
+    """Mean time of the reverse of one step (slvof_adjoint_step, or slvof_adjoint_step_next with
+    the step's result on the device) from the context's current state, seeded with dL/dVF =
+    seeded normal weights on the interior; CUDA events on the launching stream, one untimed
+    call first."""
     gT = m.vf_array()
     m.interior(gT)[...] = np.random.default_rng(SEED).standard_normal((m.Nx, m.Ny, m.Nz))
     g.adjoint_set_vf(gT)
     g.adjoint_zero_velocity()
-    g.adjoint_step(dt)
+    g.adjoint_step(dt, next_ptr)
     stream = torch.cuda.current_stream()
     g.set_stream(stream.cuda_stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(steps):
-        g.adjoint_step(dt)
+        g.adjoint_step(dt, next_ptr)
     e1.record(stream)
     torch.cuda.synchronize()
     g.set_stream(None)
-    adj = e0.elapsed_time(e1) / steps
-    return {"workload": f"{m.Nx}^3 benchmark state after the FP64 arm's steps, FP64 reverse of one step "
-                        "(recorded candidate lanes, recomputed pre-images and clip trees)",
-            "adj_ms_per_step": adj, "fwd_fp64_ms_per_step": fwd64_ms, "fwd_mixed_ms_per_step": fwd_mixed_ms,
-            "adj_over_fwd_fp64": adj / fwd64_ms, "adj_over_fwd_mixed": adj / fwd_mixed_ms,
-            "fd_check": "tests/test_gpu_adjoint.py: central differences (h=1e-6) of the CPU restatement, 1e-6 relative"}
+    return e0.elapsed_time(e1) / steps
+
+
+def adjoint_mixed(g, m, dt, steps, torch):
+    """The mixed context's reverse of one step from its current state, given the step's result
+    (as a rollout's reverse pass has it) and recomputing it."""
+    nvf = int(np.prod(m.vf_shape))
+    s0 = torch.empty(nvf, dtype=torch.float64, device="cuda")
+    s1 = torch.empty_like(s0)
+    g.copy_vf_device(s0.data_ptr())
+    g.step(dt, band=True, mass=False)
+    g.copy_vf_device(s1.data_ptr())
+    g.load_vf_device(s0.data_ptr())
+    g.prepare()
+    given = adjoint_timing(g, m, dt, steps, torch, s1.data_ptr())
+    recompute = adjoint_timing(g, m, dt, steps, torch, None)
+    return given, recompute
 
 
 def cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, budget_s):
@@ -294,8 +306,21 @@ def main():
         drift_vs_fp64 = abs(m32 - m64) / abs(m64)
         ms64, stage64 = timed_steps(g64, dt, args.fp64_steps, torch)
         value64 = cells * args.fp64_steps / (ms64 / 1e3)
+        adj32, adj32_re = adjoint_mixed(g32, m, dt, args.adj_steps, torch)
         g32.close()
-        adjoint = adjoint_timing(g64, m, dt, args.adj_steps, torch, ms64 / args.fp64_steps, ms_step)
+        adj64 = adjoint_timing(g64, m, dt, args.adj_steps, torch)
+        adjoint = {"workload": f"{m.Nx}^3 benchmark state after the accuracy steps, reverse of one step seeded with "
+                               "normal weights on every interior cell",
+                   "adj_ms_per_step": adj32, "fwd_mixed_ms_per_step": ms_step, "adj_over_fwd_mixed": adj32 / ms_step,
+                   "mixed": "boundary-form reverse (FP32 cell-local geometry, FP64 accumulation), the step's "
+                            "result given as a rollout holds it (slvof_adjoint_step_next)",
+                   "adj_recompute_ms_per_step": adj32_re,
+                   "adj_recompute_over_fwd_mixed": adj32_re / ms_step,
+                   "adj_fp64_ms_per_step": adj64, "fwd_fp64_ms_per_step": ms64 / args.fp64_steps,
+                   "adj_over_fwd_fp64": adj64 / (ms64 / args.fp64_steps),
+                   "fp64": "clip trees run backwards in FP64 (recorded candidate lanes, recomputed pre-images)",
+                   "fd_check": "tests/test_gpu_adjoint.py: central differences (h=1e-6) of the CPU restatement, "
+                               "1e-6 relative to the largest sampled derivative, FP64 and mixed contexts"}
         VF = g64.download_vf()
         nx, ny, nz = g64.download_normals()
         D = g64.download_plic()

@@ -164,8 +164,10 @@ int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, cons
  * Reverse-mode derivative of the FP64 step (the hand-written adjoint; the reference has no
  * counterpart, its Julia callers would wrap it as a ChainRules rrule).  It treats the step as
  * the smooth function it is between switches of its discrete choices (ELVIRA candidate, band,
- * cut cases, donor cells) and is exact there.  The derivative runs in FP64 for both
- * precisions: a mixed-precision context reverses with the same FP64 geometry. */
+ * cut cases, donor cells) and is exact there.  An FP64 context runs the clip trees backwards
+ * in FP64 geometry; a mixed-precision context takes the clipped volumes' derivatives from the
+ * pre-images' boundaries (liquid moments of their faces, PLIC polygons) in FP32 cell-local
+ * geometry, accumulated in FP64. */
 /* Neumann! + VF borders, computeNormal!, computePLIC!, computeBand! on the current VF: the
  * state a step starts from (run_solver, src/NavierStokes_Parallel.jl:73-98). */
 int slvof_prepare(slvof_ctx* ctx);
@@ -185,6 +187,11 @@ int slvof_adjoint_zero_velocity(slvof_ctx* ctx);
  * starting VF (ghost entries: derivatives with respect to the ghost values) and dL/d(face
  * velocities) of the step has been added to the velocity buffers.  The state is unchanged. */
 int slvof_adjoint_step(slvof_ctx* ctx, double dt);
+/* The same with the step's result given: d_VFnext is the VF (VF-array shaped, device) that
+ * slvof_step(ctx, dt, SLVOF_STEP_BAND, .) produces from the current state, e.g. the next
+ * checkpoint of a rollout.  A mixed-precision context then skips recomputing the clipped
+ * volumes; an FP64 context ignores it.  NULL recomputes, as slvof_adjoint_step. */
+int slvof_adjoint_step_next(slvof_ctx* ctx, double dt, const double* d_VFnext);
 /* Fold the VF-derivative buffer's ghost entries onto the interior cells they are copies of
  * (the reverse of Neumann! + VF borders): the derivative with respect to the interior of a
  * VF whose ghosts were filled from it, e.g. the initial condition after IC!. */

@@ -4,7 +4,8 @@ A rollout is ``steps`` calls of the step, each with its own face velocities.  Th
 pass keeps VF on the device every ``every`` steps (the checkpoints); the reverse pass walks
 the segments backwards, recomputes each segment's states from its checkpoint (pre-images,
 normals, PLIC planes and band are recomputed, not stored), and runs the step's reverse
-(``slvof_adjoint_step``) from the last state to the first.  This is the pullback a Julia
+(``slvof_adjoint_step_next``, given the step's result from the stored states) from the last
+state to the first.  This is the pullback a Julia
 caller would register as a ChainRules ``rrule`` around its loop over ``transport!``; here it
 is the Python analogue of a ``torch.autograd.Function`` over the whole rollout.
 
@@ -31,7 +32,8 @@ class Rollout:
     called; forward() prepares it.
     """
 
-    def __init__(self, solver: SLVOF, dt: float, steps: int, velocity: Callable[[int], tuple], every: int = 10):
+    def __init__(self, solver: SLVOF, dt: float, steps: int, velocity: Callable[[int], tuple], every: int = 10,
+                 give_next: bool = True):
         import torch
 
         if steps < 1 or every < 1:
@@ -41,6 +43,8 @@ class Rollout:
         self.steps = int(steps)
         self.every = int(every)
         self.velocity = velocity
+        self.give_next = bool(give_next)  # hand each reverse step its step's result
+        self.final = None
         self.torch = torch
         self.nvf = int(np.prod(solver.mesh.vf_shape))
         self.ckpt: dict[int, object] = {}
@@ -72,6 +76,7 @@ class Rollout:
             self.s.upload_velocity(*self.velocity(n))
             self.s.step(self.dt, band=True, mass=False)
             self.fwd_step_ms.append(self.s.last_kernel_ms())
+        self.final = self._save()
         out = self.s.download_vf()
         self.fwd_ms = (time.perf_counter() - t0) * 1e3
         return out
@@ -101,7 +106,8 @@ class Rollout:
             for n in range(k1 - 1, k0 - 1, -1):
                 self._load(states[n])
                 s.upload_velocity(*self.velocity(n))
-                s.adjoint_step(self.dt)
+                nxt = states.get(n + 1, self.ckpt.get(n + 1, self.final if n + 1 == self.steps else None))
+                s.adjoint_step(self.dt, nxt.data_ptr() if (self.give_next and nxt is not None) else None)
                 self.adj_step_ms.append(s.last_kernel_ms())
                 if per_step:
                     _, gu, gv, gw = s.adjoint_get()

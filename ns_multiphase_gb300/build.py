@@ -28,6 +28,7 @@ UNITS = {
     "k_elvira_mixed.cu": ["-fmad=false"],
     "slvof_noalloc.cu": ["-fmad=false"],
     "k_adj64.cu": ["-fmad=false"],
+    "k_adj32.cu": ["-fmad=true"],
 }
 
 

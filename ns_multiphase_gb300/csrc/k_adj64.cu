@@ -251,6 +251,17 @@ void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, i
     k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, gin, gout, 1, 1);
 }
 
+void launch_adjoint_fold_cell(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s)
+{
+    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, gin, gout, 0, 0);
+}
+
+void launch_adjoint_elvira(const DevMesh& m, const double* VF, const signed char* cand, const AdjBuffers& b, int nsm,
+                           cudaStream_t s)
+{
+    k_adj_elvira<<<nsm * 8, 256, 0, s>>>(m, VF, cand, b.gnf[0], b.gnf[1], b.gnf[2], b.gout);
+}
+
 void launch_adjoint_head(const DevMesh& m, const short* band, const AdjBuffers& b, int* list, int* count, int* count2,
                          int nsm, cudaStream_t s)
 {

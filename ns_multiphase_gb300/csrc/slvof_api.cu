@@ -47,6 +47,8 @@ struct slvof_ctx {
     double *gnf[3] = {nullptr, nullptr, nullptr}, *gDf = nullptr;
     double *guf = nullptr, *gvf_ = nullptr, *gwf = nullptr;
     int* list_adj = nullptr;
+    double* gvtx[3] = {nullptr, nullptr, nullptr}; /* mixed: dL/d(traced grid vertices), cell units */
+    float2* cinfo = nullptr;                       /* mixed: per clip cell g * tetsign / vol and VFnew */
     /* momentum of transport! (allocated on first use): cell-centred velocities in, us/vs/ws out */
     double *cu = nullptr, *cv = nullptr, *cw = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
     AdjCell* adj_cells = nullptr;
@@ -396,6 +398,7 @@ int slvof_destroy(slvof_ctx* c)
                     c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
                     c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
+                    c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo,
                     c->cu, c->cv, c->cw, c->us, c->vs, c->ws};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -782,6 +785,10 @@ int adj_alloc(slvof_ctx* c)
               alloc(&c->gvf_, c->ncell) && alloc(&c->gwf, c->ncell);
     for (int q = 0; q < 3 && ok; ++q) ok = alloc(&c->gn[q], c->ncell) && alloc(&c->gnf[q], c->ncell);
     ok = ok && cudaMalloc((void**)&c->list_adj, interior * sizeof(int)) == cudaSuccess;
+    if (c->precision == SLVOF_MIXED) {
+        for (int q = 0; q < 3 && ok; ++q) ok = alloc(&c->gvtx[q], c->ncell);
+        ok = ok && cudaMalloc((void**)&c->cinfo, interior * sizeof(float2)) == cudaSuccess;
+    }
     if (!ok) return fail(c, SLVOF_E_NOMEM, "reverse-pass buffers");
     return 0;
 }
@@ -856,7 +863,36 @@ int slvof_adjoint_fold(slvof_ctx* c)
     return finish(c, false);
 }
 
-int slvof_adjoint_step(slvof_ctx* c, double dt)
+namespace {
+/* Reverse of the mixed-precision step: pre-images of the band cells again (k_sl32_pre, which
+ * also lists the cells the clip needs), VFnew given or recomputed by the clip, then the
+ * boundary-form SL reverse, computeDist's reverse from the plane polygons, and the FP64 folds
+ * and ELVIRA reverse shared with the FP64 path. */
+int adjoint_step32(slvof_ctx* c, double dt, const double* d_next, AdjBuffers& b)
+{
+    const int o = 1 - c->vcur;
+    CK(cudaMemsetAsync(c->ctr + C_SL, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_SLW, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream)); /* clip count, clip work */
+    launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
+    launch_sl32_pre(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
+                    c->ctr + C_SLW, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR, c->nsm, c->stream);
+    if (!d_next) {
+        launch_sl32_clip(c->m, c->VF[o], c->planes, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW,
+                         c->ctr + C_ERR, c->nsm, c->stream);
+        d_next = c->VF[o];
+    }
+    launch_adjoint32_sl(c->m, dt, d_next, c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->slow_cells,
+                        c->slow_verts, c->ctr + C_SLOW, c->cinfo, c->gvtx[0], c->gvtx[1], c->gvtx[2], b,
+                        c->ctr + C_ERR, c->nsm, c->stream);
+    launch_adjoint_fold_cell(c->m, b.gD, b.gDf, c->nsm, c->stream);
+    launch_adjoint32_dist(c->m, c->VF[c->vcur], c->planes, b, c->nsm, c->stream);
+    for (int q = 0; q < 3; ++q) launch_adjoint_fold_cell(c->m, b.gn[q], b.gnf[q], c->nsm, c->stream);
+    launch_adjoint_elvira(c->m, c->VF[c->vcur], c->cand, b, c->nsm, c->stream);
+    return 0;
+}
+
+int adjoint_step(slvof_ctx* c, double dt, const double* d_next)
 {
     TRY(begin(c));
     TRY(adj_alloc(c));
@@ -875,6 +911,11 @@ int slvof_adjoint_step(slvof_ctx* c, double dt)
     /* head: fold, pass-through of cells outside the band, band list; its count sizes the
      * pre-image records, the pre-pass's count the per-tet records */
     launch_adjoint_head(c->m, c->band[c->bcur], b, c->list_adj, c->ctr + C_ADJ, c->ctr + C_ADJ2, c->nsm, c->stream);
+    if (c->precision == SLVOF_MIXED) {
+        TRY(adjoint_step32(c, dt, d_next, b));
+        std::swap(c->gvf[0], c->gvf[1]);
+        return finish(c);
+    }
     int n1 = 0, n2 = 0;
     CK(cudaMemcpyAsync(&n1, c->ctr + C_ADJ, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
@@ -906,5 +947,10 @@ int slvof_adjoint_step(slvof_ctx* c, double dt)
     std::swap(c->gvf[0], c->gvf[1]);
     return finish(c);
 }
+} // namespace
+
+int slvof_adjoint_step(slvof_ctx* c, double dt) { return adjoint_step(c, dt, nullptr); }
+
+int slvof_adjoint_step_next(slvof_ctx* c, double dt, const double* d_VFnext) { return adjoint_step(c, dt, d_VFnext); }
 
 } // extern "C"

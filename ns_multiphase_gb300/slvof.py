@@ -68,6 +68,7 @@ SYMBOLS = [
     ("slvof_adjoint_get", _I, [_P, _P, _P, _P, _P]),
     ("slvof_adjoint_zero_velocity", _I, [_P]),
     ("slvof_adjoint_step", _I, [_P, _D]),
+    ("slvof_adjoint_step_next", _I, [_P, _D, _P]),
     ("slvof_adjoint_fold", _I, [_P]),
 ]
 
@@ -306,9 +307,14 @@ class SLVOF:
     def adjoint_zero_velocity(self):
         self._check(self.L.slvof_adjoint_zero_velocity(self.h), "adjoint_zero_velocity")
 
-    def adjoint_step(self, dt: float):
-        """Reverse of one step(dt, band=True) from the current (prepared) state."""
-        self._check(self.L.slvof_adjoint_step(self.h, dt), "adjoint_step")
+    def adjoint_step(self, dt: float, vf_next_ptr: int | None = None):
+        """Reverse of one step(dt, band=True) from the current (prepared) state.  vf_next_ptr
+        may give the step's result (a device VF buffer, as copy_vf_device writes it), which a
+        mixed-precision context then does not recompute."""
+        if vf_next_ptr is None:
+            self._check(self.L.slvof_adjoint_step(self.h, dt), "adjoint_step")
+        else:
+            self._check(self.L.slvof_adjoint_step_next(self.h, dt, vf_next_ptr), "adjoint_step")
 
     def adjoint_fold(self):
         """Fold ghost derivatives onto the interior cells they copy."""

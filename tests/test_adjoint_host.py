@@ -30,7 +30,7 @@ def hlib():
     src = os.path.join(HERE, "adj_harness.cpp")
     out = os.path.join(HERE, "_build", "libadjh.so")
     os.makedirs(os.path.dirname(out), exist_ok=True)
-    deps = [src] + [os.path.join(ROOT, "ns_multiphase_gb300", "csrc", f) for f in ("adj64.cuh", "mesh_view.h")]
+    deps = [src] + [os.path.join(ROOT, "ns_multiphase_gb300", "csrc", f) for f in ("adj64.cuh", "adj32.cuh", "mesh_view.h")]
     if not os.path.exists(out) or any(os.path.getmtime(d) > os.path.getmtime(out) for d in deps):
         subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
                         "-I", ROOT, src, "-o", out + ".tmp"], check=True)
@@ -47,6 +47,14 @@ def hlib():
     L.adjh_elvira_reverse.argtypes = [p, p, p, i, i, i, i, p]
     L.adjh_preimage.restype = i
     L.adjh_preimage.argtypes = [i, i, i, i, i, i, i, p]
+    L.adjh_preimage_vertices.restype = None
+    L.adjh_preimage_vertices.argtypes = [p, d, i, i, i, p, p, p, p]
+    L.adjh_sl_vertices_pl.restype = d
+    L.adjh_sl_vertices_pl.argtypes = [p, i, i, i, p, p, p, p, p, d, p, p, p]
+    L.adjh_sd_vertices.restype = None
+    L.adjh_sd_vertices.argtypes = [p, i, i, i, i, p, p, p, p, p, d, d, p, p]
+    L.adjh_sd_dist.restype = i
+    L.adjh_sd_dist.argtypes = [p, i, i, i, i, d, d, d, d, p]
     return L
 
 
@@ -304,3 +312,54 @@ def test_ghost_preimage_inverts_the_source_map(hlib, per, neu):
         got = sorted(buf[:n].tolist())
         want = sorted(p for p in range(lo, hi + 1) if src_of[p] == q)
         assert got == want, (q, got, want)
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-10), (1, 1e-5)])
+def test_boundary_form_matches_clip_tree_reverse(hlib, state, prec, tol):
+    """The mixed path's reverse takes the clipped volume's derivatives from the pre-image's
+    boundary (adj32.cuh): liquid moments of its boundary triangles for the vertices, the PLIC
+    polygons inside each tet and donor cell for the planes.  Against the FP64 reverse of the
+    cutTet tree on the same pre-images: to rounding in double, to FP32 rounding in float."""
+    m, o = state[0], state[1]
+    _, _, VF, band, nx, ny, nz, D, uf, vf, wf, dt = state
+    desc = m.desc()
+    nc = int(np.prod(m.cell_shape))
+    cells = interface_preimage_cells(m, o, state, 12)
+    assert len(cells) >= 8
+    for c in cells:
+        vt = np.zeros(24)
+        hlib.adjh_preimage_vertices(ctypes.byref(desc), dt, *c, ptr(uf), ptr(vf), ptr(wf), ptr(vt))
+        g0, p0 = np.zeros(24), np.zeros(4 * nc)
+        err = ctypes.c_int()
+        r = hlib.adjh_sl_vertices_pl(ctypes.byref(desc), *c, ptr(vt), ptr(nx), ptr(ny), ptr(nz), ptr(D), 1.0,
+                                     ptr(g0), ptr(p0), ctypes.addressof(err))
+        assert err.value == 0
+        g1, p1 = np.zeros(24), np.zeros(4 * nc)
+        hlib.adjh_sd_vertices(ctypes.byref(desc), prec, *c, ptr(vt), ptr(nx), ptr(ny), ptr(nz), ptr(D), r, 1.0,
+                              ptr(g1), ptr(p1))
+        assert np.max(np.abs(g1 - g0)) <= tol * np.max(np.abs(g0)), c
+        assert np.max(np.abs(p1 - p0)) <= tol * np.max(np.abs(p0)), c
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-10), (1, 1e-5)])
+def test_plane_polygon_gives_computeDist_partials(hlib, state, prec, tol):
+    """computeDist's derivatives from the plane's polygon in the cell (dD/dVF = |grad d| / A,
+    dD/dn = centroid) against the implicit derivative of the five-tet cut-cell fraction."""
+    m, o = state[0], state[1]
+    _, _, VF, band, nx, ny, nz, D, uf, vf, wf, dt = state
+    desc = m.desc()
+    n = 0
+    for k in range(1, m.Nz + 1):
+        for j in range(1, m.Ny + 1):
+            for i in range(1, m.Nx + 1):
+                t = m.cidx(i, j, k)
+                v = VF[m.vidx(i, j, k)]
+                if not (m.VFlo <= v <= m.VFhi) or v < 1e-3 or v > 1 - 1e-3:
+                    continue
+                a, b = np.zeros(4), np.zeros(4)
+                if not hlib.adjh_dist_partials(ctypes.byref(desc), i, j, k, nx[t], ny[t], nz[t], D[t], ptr(a)):
+                    continue
+                assert hlib.adjh_sd_dist(ctypes.byref(desc), prec, i, j, k, nx[t], ny[t], nz[t], D[t], ptr(b))
+                assert np.all(np.abs(b - a) <= tol * np.maximum(np.abs(a), 1.0)), ((i, j, k), a, b)
+                n += 1
+    assert n >= 20
