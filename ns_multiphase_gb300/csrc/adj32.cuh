@@ -104,7 +104,8 @@ SLVOF_HD void moments2(const Poly2<R>& P, R& A, R& M1, R& M2)
  * ph, px, py, pz, Dt) gives the phase code of donor (a, b, c) and, for ph == 0, its plane
  * px*x + py*y + pz*z - Dt in this frame (liquid below). */
 template <class R, class Donor>
-SLVOF_HD void face_moments(const R (&p)[3][3], const int (&ind)[3][3], const Donor& donor, R (&m)[3])
+SLVOF_HD void face_moments(const R (&p)[3][3], const int (&ind)[3][3], const Donor& donor, R (&m)[3],
+                           Poly2<R>* buf /* 7 polygons of workspace */)
 {
     int lo[3], hi[3];
     R e1[3], e2[3];
@@ -114,7 +115,6 @@ SLVOF_HD void face_moments(const R (&p)[3][3], const int (&ind)[3][3], const Don
         e1[q] = p[1][q] - p[0][q];
         e2[q] = p[2][q] - p[0][q];
     }
-    Poly2<R> buf[7];
     Poly2<R>& X = buf[0]; /* remaining part below the current x plane */
     X.n = 3;
     X.a[0] = R(0); X.b[0] = R(0);
@@ -167,6 +167,13 @@ SLVOF_HD void face_moments(const R (&p)[3][3], const int (&ind)[3][3], const Don
     m[1] = M1 / R(3);
     m[2] = M2 / R(3);
     m[0] = A - (M1 + M2) / R(3);
+}
+
+template <class R, class Donor>
+SLVOF_HD void face_moments(const R (&p)[3][3], const int (&ind)[3][3], const Donor& donor, R (&m)[3])
+{
+    Poly2<R> buf[7];
+    face_moments(p, ind, donor, m, buf);
 }
 
 /* Oriented area vector S_b = -3 dV/dv_b of the face opposite slot b of tet t (V the
@@ -272,13 +279,12 @@ SLVOF_HD bool plane_tet(const R (&t)[4][3], R px, R py, R pz, R Dt, Poly3<R>& P)
     return true;
 }
 
-/* Keep the part of a convex 3D polygon with g = nx*x + ny*y + nz*z - off <= 0 (in place). */
+/* The part of a convex 3D polygon P with g = nx*x + ny*y + nz*z - off <= 0, into Q. */
 template <class R>
-SLVOF_HD void clip3(Poly3<R>& P, R nx, R ny, R nz, R off)
+SLVOF_HD void clip3(const Poly3<R>& P, Poly3<R>& Q, R nx, R ny, R nz, R off)
 {
-    if (P.n < 3) { P.n = 0; return; }
-    Poly3<R> Q;
     Q.n = 0;
+    if (P.n < 3) return;
     int ip = P.n - 1;
     R gp = nx * P.x[ip] + ny * P.y[ip] + nz * P.z[ip] - off;
     for (int q = 0; q < P.n; ++q) {
@@ -294,7 +300,6 @@ SLVOF_HD void clip3(Poly3<R>& P, R nx, R ny, R nz, R off)
         gp = gq;
         ip = q;
     }
-    P = Q;
 }
 
 /* Area (along the unit normal u) and first moment of a planar polygon, by a fan from its
@@ -320,21 +325,28 @@ SLVOF_HD void poly_area(const Poly3<R>& P, R ux, R uy, R uz, R& A, R (&M)[3])
  * cut: beyond the box's ends the donor extends, as cutTet assigns it. */
 template <class R>
 SLVOF_HD bool plane_piece(const R (&t)[4][3], const int (&lo)[3], const int (&hi)[3], int a, int b, int c, R px,
-                          R py, R pz, R Dt, R& A, R (&C)[3])
+                          R py, R pz, R Dt, R& A, R (&C)[3], Poly3<R>* ws /* 2 polygons of workspace */)
 {
-    Poly3<R> P;
-    if (!plane_tet(t, px, py, pz, Dt, P)) return false;
+    Poly3<R>* P = &ws[0];
+    Poly3<R>* Q = &ws[1];
+    if (!plane_tet(t, px, py, pz, Dt, *P)) return false;
     const int off[3] = {a, b, c};
     for (int q = 0; q < 3; ++q) {
         const R e0 = q == 0 ? R(1) : R(0), e1 = q == 1 ? R(1) : R(0), e2 = q == 2 ? R(1) : R(0);
-        if (off[q] > lo[q]) clip3(P, -e0, -e1, -e2, -R(off[q]));
-        if (off[q] < hi[q]) clip3(P, e0, e1, e2, R(off[q] + 1));
+        if (off[q] > lo[q]) {
+            clip3(*P, *Q, -e0, -e1, -e2, -R(off[q]));
+            Poly3<R>* x = P; P = Q; Q = x;
+        }
+        if (off[q] < hi[q]) {
+            clip3(*P, *Q, e0, e1, e2, R(off[q] + 1));
+            Poly3<R>* x = P; P = Q; Q = x;
+        }
     }
-    if (P.n < 3) return false;
+    if (P->n < 3) return false;
     const R len = sqrt_of(px * px + py * py + pz * pz);
     if (!(len > R(0))) return false;
     R M[3];
-    poly_area(P, px / len, py / len, pz / len, A, M);
+    poly_area(*P, px / len, py / len, pz / len, A, M);
     if (A == R(0)) return false;
     for (int q = 0; q < 3; ++q) C[q] = M[q] / A;
     A = A < R(0) ? -A : A;

@@ -107,7 +107,10 @@ __device__ __forceinline__ void scatter_point(const DevMesh& m, int i, int j, in
     }
 }
 
-__global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_faces(DevMesh m, const float4* __restrict__ planes,
+constexpr int FACES_THREADS = 64; /* 7 polygons of workspace per thread in shared memory: 37.6 KB a block */
+constexpr int PLANES_THREADS = 128; /* 2 polygons per thread: 31.7 KB a block */
+
+__global__ void __launch_bounds__(FACES_THREADS) k_adj32_faces(DevMesh m, const float4* __restrict__ planes,
                                                                const signed char* __restrict__ phase,
                                                                const int* __restrict__ cells,
                                                                const float4* __restrict__ verts,
@@ -115,6 +118,9 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_faces(DevMesh m, const 
                                                                const int* __restrict__ count, sd::BFaces F,
                                                                double* gx, double* gy, double* gz)
 {
+    /* the polygon workspace lives in shared memory: in local memory it spilled to DRAM */
+    __shared__ sd::Poly2<float> s_ws[FACES_THREADS * 7];
+    sd::Poly2<float>* ws = s_ws + threadIdx.x * 7;
     const long n = (long)F.n * *count;
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
         const long s = q / F.n;
@@ -146,7 +152,7 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_faces(DevMesh m, const 
             px = pl.x; py = pl.y; pz = pl.z;
             Dt = pl.w + pl.x * (float)a + pl.y * (float)bb + pl.z * (float)c;
         };
-        sd::face_moments(p3, i3, donor, mm);
+        sd::face_moments(p3, i3, donor, mm, ws);
         const bool even = tess_even(m.tess, i, j, k);
         const float third = ci.y * (1.f / 3.f);
         for (int sl = 0; sl < 3; ++sl) {
@@ -158,7 +164,7 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_faces(DevMesh m, const 
     }
 }
 
-__global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_planes(DevMesh m, const float4* __restrict__ planes,
+__global__ void __launch_bounds__(PLANES_THREADS) k_adj32_planes(DevMesh m, const float4* __restrict__ planes,
                                                                 const signed char* __restrict__ phase,
                                                                 const int* __restrict__ cells,
                                                                 const float4* __restrict__ verts,
@@ -166,6 +172,8 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_planes(DevMesh m, const
                                                                 const int* __restrict__ count, double* gnx,
                                                                 double* gny, double* gnz, double* gD)
 {
+    __shared__ sd::Poly3<float> s_ws[PLANES_THREADS * 2];
+    sd::Poly3<float>* ws = s_ws + threadIdx.x * 2;
     const int nt = tess_ntets(m.tess);
     const long n = (long)nt * *count;
     for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
@@ -195,7 +203,7 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_planes(DevMesh m, const
                     const float4 pl = __ldg(planes + d);
                     const float Dt = pl.w + pl.x * (float)a + pl.y * (float)b + pl.z * (float)c;
                     float A, C[3];
-                    if (!sd::plane_piece(tv, lo, hi, a, b, c, pl.x, pl.y, pl.z, Dt, A, C)) continue;
+                    if (!sd::plane_piece(tv, lo, hi, a, b, c, pl.x, pl.y, pl.z, Dt, A, C, ws)) continue;
                     const float len = sqrtf(pl.x * pl.x + pl.y * pl.y + pl.z * pl.z);
                     const double c2 = (double)(cs * A / len);
                     atomicAdd(gD + d, c2);
@@ -207,11 +215,12 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_planes(DevMesh m, const
 }
 
 /* ---- RK reverse ------------------------------------------------------------------------ */
-/* Reverse of tri32: adds gval * d(value)/d(node) * scale to the eight nodes of gf and returns
+/* Reverse of tri32: adds gval * d(value)/d(node) to the eight nodes of gf (FP32, one step's
+ * sums; the step's totals go to the FP64 velocity derivatives afterwards) and returns
  * gval * d(value)/d(wx, wy, wz). */
-__device__ __forceinline__ void tri32_rev(const DevMesh& m, const float* __restrict__ f, double* gf, double scale,
-                                          int I, int J, int K, float wx, float wy, float wz, float gval, float& dx,
-                                          float& dy, float& dz)
+__device__ __forceinline__ void tri32_rev(const DevMesh& m, const float* __restrict__ f, float* gf, int I, int J,
+                                          int K, float wx, float wy, float wz, float gval, float& dx, float& dy,
+                                          float& dz)
 {
     dx = dy = dz = 0.f;
     if (gval == 0.f) return;
@@ -227,24 +236,24 @@ __device__ __forceinline__ void tri32_rev(const DevMesh& m, const float* __restr
     dz = gval * (y1 - y0);
     dy = gval * (uz * (x10 - x00) + wz * (x11 - x01));
     dx = gval * (uz * (uy * (f100 - f000) + wy * (f110 - f010)) + wz * (uy * (f101 - f001) + wy * (f111 - f011)));
-    const double gs = (double)gval * scale;
-    atomicAdd(gf + b, gs * (double)(ux * uy * uz));
-    atomicAdd(gf + b + 1, gs * (double)(wx * uy * uz));
-    atomicAdd(gf + b + sj, gs * (double)(ux * wy * uz));
-    atomicAdd(gf + b + 1 + sj, gs * (double)(wx * wy * uz));
-    atomicAdd(gf + b + sk, gs * (double)(ux * uy * wz));
-    atomicAdd(gf + b + 1 + sk, gs * (double)(wx * uy * wz));
-    atomicAdd(gf + b + sj + sk, gs * (double)(ux * wy * wz));
-    atomicAdd(gf + b + 1 + sj + sk, gs * (double)(wx * wy * wz));
+    const float a0 = gval * uz, a1 = gval * wz;
+    atomicAdd(gf + b, a0 * (ux * uy));
+    atomicAdd(gf + b + 1, a0 * (wx * uy));
+    atomicAdd(gf + b + sj, a0 * (ux * wy));
+    atomicAdd(gf + b + 1 + sj, a0 * (wx * wy));
+    atomicAdd(gf + b + sk, a1 * (ux * uy));
+    atomicAdd(gf + b + 1 + sk, a1 * (wx * uy));
+    atomicAdd(gf + b + sj + sk, a1 * (ux * wy));
+    atomicAdd(gf + b + 1 + sj + sk, a1 * (wx * wy));
 }
 
-struct VelGrad64 {
-    double *gu, *gv, *gw;
+struct VelGrad32 {
+    float *gu, *gv, *gw; /* one step's dL/d(face velocity in cells per unit time) */
 };
 
 /* Reverse of vel32 at (x, y, z): face-velocity derivatives of the cotangent (cu, cv, cw) of
  * the interpolated velocity (cells per unit time), and its pull-back to the point in g. */
-__device__ __forceinline__ void vel32_rev(const DevMesh& m, const Vel32& V, const VelGrad64& G, int i0, int j0,
+__device__ __forceinline__ void vel32_rev(const DevMesh& m, const Vel32& V, const VelGrad32& G, int i0, int j0,
                                           int k0, float x, float y, float z, float cu, float cv, float cw, float (&g)[3])
 {
     const float B = 1.0e6f;
@@ -259,17 +268,17 @@ __device__ __forceinline__ void vel32_rev(const DevMesh& m, const Vel32& V, cons
     const float wfz = z - (float)(Fz - k0), wcz = z - ((float)(Cz - k0) + 0.5f);
     float a, b, c;
     g[0] = g[1] = g[2] = 0.f;
-    tri32_rev(m, V.uf, G.gu, 1.0 / m.d[0], Fx, Cy, Cz, wfx, wcy, wcz, cu, a, b, c);
+    tri32_rev(m, V.uf, G.gu, Fx, Cy, Cz, wfx, wcy, wcz, cu, a, b, c);
     g[0] += a; g[1] += b; g[2] += c;
-    tri32_rev(m, V.vf, G.gv, 1.0 / m.d[1], Cx, Fy, Cz, wcx, wfy, wcz, cv, a, b, c);
+    tri32_rev(m, V.vf, G.gv, Cx, Fy, Cz, wcx, wfy, wcz, cv, a, b, c);
     g[0] += a; g[1] += b; g[2] += c;
-    tri32_rev(m, V.wf, G.gw, 1.0 / m.d[2], Cx, Cy, Fz, wcx, wcy, wfz, cw, a, b, c);
+    tri32_rev(m, V.wf, G.gw, Cx, Cy, Fz, wcx, wcy, wfz, cw, a, b, c);
     g[0] += a; g[1] += b; g[2] += c;
 }
 
 /* Reverse of project32 for the trajectory of the grid vertex (I, J, K) (the origin of its
  * cell frame): g = dL/d(end point) in cell units. */
-__device__ void project32_rev(const DevMesh& m, const Vel32& V, const VelGrad64& G, int I, int J, int K, float dt,
+__device__ void project32_rev(const DevMesh& m, const Vel32& V, const VelGrad32& G, int I, int J, int K, float dt,
                               const float (&g)[3])
 {
     if (m.projection == 3) return; /* Zalesak rotation: no velocity */
@@ -309,7 +318,7 @@ __device__ void project32_rev(const DevMesh& m, const Vel32& V, const VelGrad64&
     vel32_rev(m, V, G, I, J, K, 0.f, 0.f, 0.f, c1[0], c1[1], c1[2], t);
 }
 
-__global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_vert(DevMesh m, float dt, Vel32 V, VelGrad64 G, double* gx,
+__global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_vert(DevMesh m, float dt, Vel32 V, VelGrad32 G, double* gx,
                                                               double* gy, double* gz)
 {
     const long n0 = m.N[0] + 1, n1 = m.N[1] + 1, n2 = m.N[2] + 1;
@@ -322,6 +331,101 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_vert(DevMesh m, float d
         gx[t] = 0.0; gy[t] = 0.0; gz[t] = 0.0;
         const float g[3] = {(float)a, (float)b, (float)c};
         project32_rev(m, V, G, I, J, K, dt, g);
+    }
+}
+
+/* The step's face-velocity derivatives (cells per unit time, FP32) into the FP64 totals of
+ * dL/d(face velocity): divided by the spacing, since the mixed path's velocities are u / d.
+ * The FP32 sums are cleared for the next step. */
+__global__ void k_adj32_vel_flush(long n, float* __restrict__ su, float* __restrict__ sv, float* __restrict__ sw,
+                                  double* gu, double* gv, double* gw, double rx, double ry, double rz)
+{
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const float a = su[t], b = sv[t], c = sw[t];
+        if (a != 0.f) { gu[t] += rx * (double)a; su[t] = 0.f; }
+        if (b != 0.f) { gv[t] += ry * (double)b; sv[t] = 0.f; }
+        if (c != 0.f) { gw[t] += rz * (double)c; sw[t] = 0.f; }
+    }
+}
+
+/* ELVIRA backwards at interior interface cells with a chosen candidate, in FP32 (the normal
+ * is c/|c| with c linear in the 3x3x3 VF block, check_normal! and ELVIRA_calc!,
+ * src/ELVIRA.jl:62-115; the same algebra as the FP64 reverse). */
+__device__ void elvira_reverse32(const DevMesh& m, const double* __restrict__ VF, double* gVF, int i, int j, int k,
+                                 int lane, const float (&gn)[3])
+{
+    const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
+    const int fam = lane / 9, oa = (lane % 9) / 3, ob = lane % 3;
+    int f = 0;
+    for (int q = 0, seen = 0; q < 3; ++q)
+        if (fam_on[q]) {
+            if (seen == fam) { f = q; break; }
+            ++seen;
+        }
+    const int lo_b = oa == 2 ? 0 : -1, hi_b = oa == 0 ? 0 : 1;
+    const int lo_a = ob == 2 ? 0 : -1, hi_a = ob == 0 ? 0 : 1;
+    const int ta = f == 2 ? 1 : 0, tb = f == 0 ? 1 : 2, tn = f == 0 ? 2 : (f == 1 ? 1 : 0);
+    const float hs = (float)m.d[tn];
+    const int base[3] = {i, j, k};
+    auto V_ = [&](const int* e) { return (float)__ldg(VF + vidx(m, i + e[0], j + e[1], k + e[2])); };
+    int e[3];
+    float c[3], s2 = 0.f, s1 = 0.f;
+    for (int r = -1; r <= 1; ++r) {
+        e[ta] = hi_a; e[tb] = 0; e[tn] = r;
+        s2 += V_(e) * hs;
+        e[ta] = lo_a;
+        s1 += V_(e) * hs;
+    }
+    const float dca = (float)(cco(m, ta, base[ta] + hi_a) - cco(m, ta, base[ta] + lo_a));
+    c[ta] = -(s2 - s1) / dca;
+    s2 = 0.f;
+    s1 = 0.f;
+    for (int r = -1; r <= 1; ++r) {
+        e[tb] = hi_b; e[ta] = 0; e[tn] = r;
+        s2 += V_(e) * hs;
+        e[tb] = lo_b;
+        s1 += V_(e) * hs;
+    }
+    const float dcb = (float)(cco(m, tb, base[tb] + hi_b) - cco(m, tb, base[tb] + lo_b));
+    c[tb] = -(s2 - s1) / dcb;
+    int up[3] = {0, 0, 0}, dn[3] = {0, 0, 0};
+    up[tn] = 1;
+    dn[tn] = -1;
+    c[tn] = V_(up) > V_(dn) ? -1.f : 1.f;
+    const float norm = sqrtf(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    const float n[3] = {c[0] / norm, c[1] / norm, c[2] / norm};
+    const float dot = n[0] * gn[0] + n[1] * gn[1] + n[2] * gn[2];
+    const double wa = (double)((gn[ta] - n[ta] * dot) / norm * hs / dca);
+    const double wb = (double)((gn[tb] - n[tb] * dot) / norm * hs / dcb);
+    for (int r = -1; r <= 1; ++r) {
+        e[ta] = hi_a; e[tb] = 0; e[tn] = r;
+        atomicAdd(gVF + vidx(m, i + e[0], j + e[1], k + e[2]), -wa);
+        e[ta] = lo_a;
+        atomicAdd(gVF + vidx(m, i + e[0], j + e[1], k + e[2]), wa);
+        e[tb] = hi_b; e[ta] = 0; e[tn] = r;
+        atomicAdd(gVF + vidx(m, i + e[0], j + e[1], k + e[2]), -wb);
+        e[tb] = lo_b;
+        atomicAdd(gVF + vidx(m, i + e[0], j + e[1], k + e[2]), wb);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_adj32_elvira(DevMesh m, const double* __restrict__ VF,
+                                                      const signed char* __restrict__ cand,
+                                                      const double* __restrict__ gnx, const double* __restrict__ gny,
+                                                      const double* __restrict__ gnz, double* gout)
+{
+    const long total = (long)m.N[0] * m.N[1] * m.N[2];
+    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+        const long c = cidx(m, i, j, k);
+        const double a = gnx[c], b = gny[c], d = gnz[c];
+        if (a == 0.0 && b == 0.0 && d == 0.0) continue;
+        const double vf = VF[vidx(m, i, j, k)];
+        if (!(vf >= m.VFlo && vf <= m.VFhi)) continue; /* pure cells carry fixed axis normals */
+        const int lane = cand[c];
+        if (lane < 0) continue;
+        const float gn[3] = {(float)a, (float)b, (float)d};
+        elvira_reverse32(m, VF, gout, i, j, k, lane, gn);
     }
 }
 
@@ -358,16 +462,25 @@ __global__ void __launch_bounds__(ADJ32_THREADS) k_adj32_dist(DevMesh m, const d
 void launch_adjoint32_sl(const DevMesh& m, double dt, const double* VFnext, const float* uf32, const float* vf32,
                          const float* wf32, const float4* planes, const signed char* phase, const int* cells,
                          const float4* verts, const int* count, float2* cinfo, double* gvx, double* gvy, double* gvz,
-                         const AdjBuffers& b, int* errw, int nsm, cudaStream_t s)
+                         float* const* gvel32, const AdjBuffers& b, int* errw, int nsm, cudaStream_t s)
 {
     const sd::BFaces F = sd::boundary_faces(m.tess);
     k_adj32_cell<<<nsm * 8, ADJ32_THREADS, 0, s>>>(m, cells, verts, count, b.gfold, VFnext, cinfo, errw);
-    k_adj32_faces<<<nsm * 16, ADJ32_THREADS, 0, s>>>(m, planes, phase, cells, verts, cinfo, count, F, gvx, gvy, gvz);
-    k_adj32_planes<<<nsm * 16, ADJ32_THREADS, 0, s>>>(m, planes, phase, cells, verts, cinfo, count, b.gn[0], b.gn[1],
-                                                      b.gn[2], b.gD);
+    k_adj32_faces<<<nsm * 24, FACES_THREADS, 0, s>>>(m, planes, phase, cells, verts, cinfo, count, F, gvx, gvy, gvz);
+    k_adj32_planes<<<nsm * 12, PLANES_THREADS, 0, s>>>(m, planes, phase, cells, verts, cinfo, count, b.gn[0],
+                                                       b.gn[1], b.gn[2], b.gD);
     Vel32 V{uf32, vf32, wf32};
-    VelGrad64 G{b.guf, b.gvf, b.gwf};
+    VelGrad32 G{gvel32[0], gvel32[1], gvel32[2]};
     k_adj32_vert<<<nsm * 8, ADJ32_THREADS, 0, s>>>(m, (float)dt, V, G, gvx, gvy, gvz);
+    const long n = (long)(m.N[0] + 2 * m.g) * (m.N[1] + 2 * m.g) * (m.N[2] + 2 * m.g);
+    k_adj32_vel_flush<<<nsm * 8, 256, 0, s>>>(n, gvel32[0], gvel32[1], gvel32[2], b.guf, b.gvf, b.gwf, 1.0 / m.d[0],
+                                              1.0 / m.d[1], 1.0 / m.d[2]);
+}
+
+void launch_adjoint32_elvira(const DevMesh& m, const double* VF, const signed char* cand, const AdjBuffers& b,
+                             int nsm, cudaStream_t s)
+{
+    k_adj32_elvira<<<nsm * 8, 256, 0, s>>>(m, VF, cand, b.gnf[0], b.gnf[1], b.gnf[2], b.gout);
 }
 
 void launch_adjoint32_dist(const DevMesh& m, const double* VF, const float4* planes, const AdjBuffers& b, int nsm,

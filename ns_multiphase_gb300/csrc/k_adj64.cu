@@ -42,6 +42,11 @@ __global__ void k_adj_fold(DevMesh m, const double* __restrict__ in, double* __r
     const long total = n0 * n1 * n2;
     for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
         const int i = lo + (int)(t % n0), j = lo + (int)((t / n0) % n1), k = lo + (int)(t / (n0 * n1));
+        /* farther than g from every end no ghost copies the cell: it is its own only preimage */
+        if (i > m.g && i <= m.N[0] - m.g && j > m.g && j <= m.N[1] - m.g && k > m.g && k <= m.N[2] - m.g) {
+            out[t] = in[t];
+            continue;
+        }
         int pa[adj::MAXPRE], pb[adj::MAXPRE], pc[adj::MAXPRE];
         const int na = adj::preimage_1d(i, m.N[0], m.g, m.per[0], neumann, lo, hi[0], pa);
         const int nb = adj::preimage_1d(j, m.N[1], m.g, m.per[1], neumann, lo, hi[1], pb);

@@ -49,6 +49,7 @@ struct slvof_ctx {
     int* list_adj = nullptr;
     double* gvtx[3] = {nullptr, nullptr, nullptr}; /* mixed: dL/d(traced grid vertices), cell units */
     float2* cinfo = nullptr;                       /* mixed: per clip cell g * tetsign / vol and VFnew */
+    float* gvel32[3] = {nullptr, nullptr, nullptr}; /* mixed: one step's face-velocity derivatives */
     /* momentum of transport! (allocated on first use): cell-centred velocities in, us/vs/ws out */
     double *cu = nullptr, *cv = nullptr, *cw = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
     AdjCell* adj_cells = nullptr;
@@ -398,7 +399,7 @@ int slvof_destroy(slvof_ctx* c)
                     c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
                     c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
-                    c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo,
+                    c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo, c->gvel32[0], c->gvel32[1], c->gvel32[2],
                     c->cu, c->cv, c->cw, c->us, c->vs, c->ws};
     for (void* b : bufs)
         if (b) cudaFree(b);
@@ -788,6 +789,9 @@ int adj_alloc(slvof_ctx* c)
     if (c->precision == SLVOF_MIXED) {
         for (int q = 0; q < 3 && ok; ++q) ok = alloc(&c->gvtx[q], c->ncell);
         ok = ok && cudaMalloc((void**)&c->cinfo, interior * sizeof(float2)) == cudaSuccess;
+        for (int q = 0; q < 3 && ok; ++q)
+            ok = cudaMalloc((void**)&c->gvel32[q], c->ncell * sizeof(float)) == cudaSuccess &&
+                 cudaMemset(c->gvel32[q], 0, c->ncell * sizeof(float)) == cudaSuccess;
     }
     if (!ok) return fail(c, SLVOF_E_NOMEM, "reverse-pass buffers");
     return 0;
@@ -883,12 +887,12 @@ int adjoint_step32(slvof_ctx* c, double dt, const double* d_next, AdjBuffers& b)
         d_next = c->VF[o];
     }
     launch_adjoint32_sl(c->m, dt, d_next, c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->slow_cells,
-                        c->slow_verts, c->ctr + C_SLOW, c->cinfo, c->gvtx[0], c->gvtx[1], c->gvtx[2], b,
+                        c->slow_verts, c->ctr + C_SLOW, c->cinfo, c->gvtx[0], c->gvtx[1], c->gvtx[2], c->gvel32, b,
                         c->ctr + C_ERR, c->nsm, c->stream);
     launch_adjoint_fold_cell(c->m, b.gD, b.gDf, c->nsm, c->stream);
     launch_adjoint32_dist(c->m, c->VF[c->vcur], c->planes, b, c->nsm, c->stream);
     for (int q = 0; q < 3; ++q) launch_adjoint_fold_cell(c->m, b.gn[q], b.gnf[q], c->nsm, c->stream);
-    launch_adjoint_elvira(c->m, c->VF[c->vcur], c->cand, b, c->nsm, c->stream);
+    launch_adjoint32_elvira(c->m, c->VF[c->vcur], c->cand, b, c->nsm, c->stream);
     return 0;
 }
 

@@ -95,11 +95,14 @@ void launch_adjoint_fold_cell(const DevMesh& m, const double* gin, double* gout,
 void launch_adjoint_elvira(const DevMesh& m, const double* VF, const signed char* cand, const AdjBuffers& b, int nsm,
                            cudaStream_t s);
 /* Reverse of the mixed-precision SL update (k_adj32.cu): the clip list and pre-image vertices
- * of k_sl32_pre, VFnew of the step, dL/d(grid vertices) scratch (zero on entry, left zero). */
+ * of k_sl32_pre, VFnew of the step, dL/d(grid vertices) and per-step face-velocity sums (FP32)
+ * as scratch (zero on entry, left zero). */
 void launch_adjoint32_sl(const DevMesh& m, double dt, const double* VFnext, const float* uf32, const float* vf32,
                          const float* wf32, const float4* planes, const signed char* phase, const int* cells,
                          const float4* verts, const int* count, float2* cinfo, double* gvx, double* gvy, double* gvz,
-                         const AdjBuffers& b, int* errw, int nsm, cudaStream_t s);
+                         float* const* gvel32, const AdjBuffers& b, int* errw, int nsm, cudaStream_t s);
+void launch_adjoint32_elvira(const DevMesh& m, const double* VF, const signed char* cand, const AdjBuffers& b,
+                             int nsm, cudaStream_t s);
 void launch_adjoint32_dist(const DevMesh& m, const double* VF, const float4* planes, const AdjBuffers& b, int nsm,
                            cudaStream_t s);
 void launch_sl32_pre(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,

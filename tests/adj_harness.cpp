@@ -275,7 +275,8 @@ void sd_cell(const DevMesh& m, int i, int j, int k, const double* vt, const doub
                     R px, py, pz, Dt, A, C[3];
                     donor(a, b, c, ph, px, py, pz, Dt);
                     if (ph != 0) continue;
-                    if (!sd::plane_piece(tv, lo, hi, a, b, c, px, py, pz, Dt, A, C)) continue;
+                    sd::Poly3<R> ws[2];
+                    if (!sd::plane_piece(tv, lo, hi, a, b, c, px, py, pz, Dt, A, C, ws)) continue;
                     const double len = std::sqrt((double)px * px + (double)py * py + (double)pz * pz);
                     const double c2 = (double)(coef * sgn) * (double)A / len;
                     const long td = adj::ci(m, i + a, j + b, k + c);
