@@ -160,6 +160,33 @@ int slvof_transportSL_momentum(slvof_ctx* ctx, double dt, double* VF, const doub
 int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, const double* vf, const double* wf,
                     double* VF, double* mass);
 
+/* ---- divergence and the pressure operator ---------------------------------------------------
+ * FP64 in the reference's operation order, in either context precision (they are the pressure
+ * solver's operators, not part of the interface step).  scheme: 1 pressure_scheme
+ * "semi-lagrangian", 0 "finite-difference".  Cell arrays (N+2g)^3; band Int16.  Each call stands
+ * alone: the context's transport state is not read or changed.  For a multigrid level, use a
+ * context created on that level's mesh. */
+/* divergence! (src/Velocity.jl:59-68) with divg_cell (src/Velocity.jl:71-122): divg = 0 on every
+ * cell, the divergence of (uf, vf, wf) over dt on the interior.  A band cell's is
+ * (dx*dy*dz - v1)/(dx*dy*dz)/dt with v1 the volume of the cell projected back through the face
+ * velocities; any other cell's comes from face fluxes (SLfluxVol/dt through a face next to a
+ * band cell).  Host arrays. */
+int slvof_divergence(slvof_ctx* ctx, double dt, int scheme, double* divg, const double* uf, const double* vf,
+                     const double* wf, const int16_t* band);
+/* The same on device arrays of the caller, on the context's stream. */
+int slvof_divergence_device(slvof_ctx* ctx, double dt, int scheme, double* d_divg, const double* d_uf,
+                            const double* d_vf, const double* d_wf, const int16_t* d_band);
+/* A! (src/Pressure.jl:83-115), the left-hand side of the pressure equation: Neumann! +
+ * update_borders! of P in place, the corrected face velocities uf - dt/denx * dP/dx (and y, z)
+ * over the reference's index ranges, and LHS = 0 on every cell, divg_cell of the corrected
+ * velocities on the interior.  Host arrays (P is read and its ghosts written back). */
+int slvof_A(slvof_ctx* ctx, double dt, int scheme, double* LHS, double* P, const double* uf, const double* vf,
+            const double* wf, const double* denx, const double* deny, const double* denz, const int16_t* band);
+/* The same on device arrays of the caller (the corrected velocities are context scratch). */
+int slvof_A_device(slvof_ctx* ctx, double dt, int scheme, double* d_LHS, double* d_P, const double* d_uf,
+                   const double* d_vf, const double* d_wf, const double* d_denx, const double* d_deny,
+                   const double* d_denz, const int16_t* d_band);
+
 /* ---- state save/restore and the reverse pass ------------------------------------------------
  * Reverse-mode derivative of the FP64 step (the hand-written adjoint; the reference has no
  * counterpart, its Julia callers would wrap it as a ChainRules rrule).  It treats the step as

@@ -689,6 +689,120 @@ __global__ void k_mom_flux64(DevMesh m, double dt, Vel64 V, Plic64 P, const shor
     }
 }
 
+/* ======================================================================================
+ * divg_cell / divergence! (src/Velocity.jl:59-122) and A! (src/Pressure.jl:83-115), FP64 in
+ * the reference's operation order.  sl: pressure_scheme == "semi-lagrangian".  A band cell's
+ * divergence is (v2 - v1)/v2/dt with v1 the volume of its projected cell; any other cell sums
+ * face fluxes: SLfluxVol/dt through a face whose neighbour is a band cell, the
+ * finite-difference flux otherwise.
+ * ==================================================================================== */
+__device__ double divg_cell64(const DevMesh& m, const Vel64& V, const short* __restrict__ band, bool sl, int i, int j,
+                              int k, double dt)
+{
+    auto inband = [&](int a, int b, int c) { return sl && abs((int)__ldg(band + cidx(m, a, b, c))) <= m.nband; };
+    if (inband(i, j, k)) {
+        const int tess = m.tess;
+        const bool even = tess_even(tess, i, j, k);
+        const double tetsign = even ? 1.0 : -1.0;
+        const double X[2] = {fco(m, 0, even ? i : i + 1), fco(m, 0, even ? i + 1 : i)};
+        const double Y[2] = {fco(m, 1, j), fco(m, 1, j + 1)};
+        const double Z[2] = {fco(m, 2, k), fco(m, 2, k + 1)};
+        double p[15][3];
+#pragma unroll 1
+        for (int v = 0; v < 8; ++v) {
+            double x = X[v & 1], y = Y[(v >> 1) & 1], z = Z[v >> 2];
+            project64(m, V, x, y, z, i, j, k, dt);
+            p[v][0] = x; p[v][1] = y; p[v][2] = z;
+        }
+        tess_means<double>(tess, p);
+        double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+        for (int t = 0; t < tess_ntets(tess); ++t) {
+            const int a = tess_tet(tess, t, 0), b = tess_tet(tess, t, 1), c = tess_tet(tess, t, 2),
+                      e = tess_tet(tess, t, 3);
+            vol += tet_vol(p[a][0], p[a][1], p[a][2], p[b][0], p[b][1], p[b][2], p[c][0], p[c][1], p[c][2], p[e][0],
+                           p[e][1], p[e][2]);
+        }
+        const double v2 = m.cellvol, v1 = tetsign * vol;
+        return (v2 - v1) / v2 / dt;
+    }
+    auto flux = [&](int dir, int a, int b, int c, int na, int nb, int nc) {
+        if (inband(na, nb, nc)) return sl_flux_vol64(m, V, dir, a, b, c, dt) / dt;
+        const long t = cidx(m, a, b, c);
+        if (dir == 0) return (m.d[1] * m.d[2]) * __ldg(V.uf + t);
+        if (dir == 1) return (m.d[0] * m.d[2]) * __ldg(V.vf + t);
+        return (m.d[0] * m.d[1]) * __ldg(V.wf + t);
+    };
+    const double Fxm = flux(0, i, j, k, i - 1, j, k), Fxp = flux(0, i + 1, j, k, i + 1, j, k);
+    const double Fym = flux(1, i, j, k, i, j - 1, k), Fyp = flux(1, i, j + 1, k, i, j + 1, k);
+    const double Fzm = flux(2, i, j, k, i, j, k - 1), Fzp = flux(2, i, j, k + 1, i, j, k + 1);
+    return (((((Fxp - Fxm) + Fyp) - Fym) + Fzp) - Fzm) / m.cellvol;
+}
+
+__global__ void k_divg64(DevMesh m, double dt, Vel64 V, const short* __restrict__ band, int sl,
+                         double* __restrict__ divg)
+{
+    const long total = (long)m.N[0] * m.N[1] * m.N[2];
+    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+        divg[cidx(m, i, j, k)] = divg_cell64(m, V, band, sl != 0, i, j, k, dt);
+    }
+}
+
+/* Neumann! + update_borders! of a cell array in place: every ghost takes its separable source
+ * (sources are fixed points of the map, so no copy reads a written cell). */
+__global__ void k_cell_ghost64(DevMesh m, double* A)
+{
+    const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = (long)n0 * n1 * n2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int ip = (int)(t % n0) + m.lo, jp = (int)((t / n0) % n1) + m.lo, kp = (int)(t / ((long)n0 * n1)) + m.lo;
+        const int si = ghost_src_1d(ip, m.N[0], m.g, m.per[0], true);
+        const int sj = ghost_src_1d(jp, m.N[1], m.g, m.per[1], true);
+        const int sk = ghost_src_1d(kp, m.N[2], m.g, m.per[2], true);
+        if (si != ip || sj != jp || sk != kp) A[t] = A[cidx(m, si, sj, sk)];
+    }
+}
+
+/* A!'s pressure-corrected face velocities over the reference's ranges (src/Pressure.jl:
+ * 92-105), 0 elsewhere: gradx with plain divides, grady and gradz with the safe divide. */
+__global__ void k_pgrad64(DevMesh m, double dt, const double* __restrict__ P, const double* __restrict__ uf,
+                          const double* __restrict__ vf, const double* __restrict__ wf,
+                          const double* __restrict__ denx, const double* __restrict__ deny,
+                          const double* __restrict__ denz, double* __restrict__ gx, double* __restrict__ gy,
+                          double* __restrict__ gz)
+{
+    const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = (long)n0 * n1 * n2;
+    const long sj = m.cs1, sk = m.cs2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int ii = (int)(t % n0) + m.lo, jj = (int)((t / n0) % n1) + m.lo, kk = (int)(t / ((long)n0 * n1)) + m.lo;
+        const bool in0 = ii >= 0 && ii <= m.N[0] + 1, in1 = jj >= 0 && jj <= m.N[1] + 1, in2 = kk >= 0 && kk <= m.N[2] + 1;
+        const bool x0 = ii >= 0 && ii <= m.N[0] + 2, y0 = jj >= 0 && jj <= m.N[1] + 2, z0 = kk >= 0 && kk <= m.N[2] + 2;
+        gx[t] = (x0 && in1 && in2) ? uf[t] - dt / denx[t] * (P[t] - P[t - 1]) / m.d[0] : 0.0;
+        gy[t] = (in0 && y0 && in2) ? vf[t] - sdiv(sdiv(dt, deny[t]) * (P[t] - P[t - sj]), m.d[1]) : 0.0;
+        gz[t] = (in0 && in1 && z0) ? wf[t] - sdiv(sdiv(dt, denz[t]) * (P[t] - P[t - sk]), m.d[2]) : 0.0;
+    }
+}
+
+void launch_divergence64(const DevMesh& m, double dt, int sl, const double* uf, const double* vf, const double* wf,
+                         const short* band, double* divg, int nsm, cudaStream_t s)
+{
+    const long nc = (long)(m.N[0] + 2 * m.g) * (m.N[1] + 2 * m.g) * (m.N[2] + 2 * m.g);
+    cudaMemsetAsync(divg, 0, nc * sizeof(double), s);
+    Vel64 V{uf, vf, wf};
+    k_divg64<<<nsm * 8, 128, 0, s>>>(m, dt, V, band, sl, divg);
+}
+
+void launch_pressure_A64(const DevMesh& m, double dt, int sl, double* LHS, double* P, const double* uf,
+                         const double* vf, const double* wf, const double* denx, const double* deny,
+                         const double* denz, const short* band, double* gx, double* gy, double* gz, int nsm,
+                         cudaStream_t s)
+{
+    k_cell_ghost64<<<nsm * 8, 256, 0, s>>>(m, P);
+    k_pgrad64<<<nsm * 8, 256, 0, s>>>(m, dt, P, uf, vf, wf, denx, deny, denz, gx, gy, gz);
+    launch_divergence64(m, dt, sl, gx, gy, gz, band, LHS, nsm, s);
+}
+
 /* Phase codes (and mixed-path planes) of planes that were uploaded rather than computed:
  * the same outputs as the PLIC pass derives from its own D. */
 __global__ void k_plic_phase(DevMesh m, const double* __restrict__ nx, const double* __restrict__ ny,

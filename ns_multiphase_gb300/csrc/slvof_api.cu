@@ -52,6 +52,10 @@ struct slvof_ctx {
     float* gvel32[3] = {nullptr, nullptr, nullptr}; /* mixed: one step's face-velocity derivatives */
     /* momentum of transport! (allocated on first use): cell-centred velocities in, us/vs/ws out */
     double *cu = nullptr, *cv = nullptr, *cw = nullptr, *us = nullptr, *vs = nullptr, *ws = nullptr;
+    /* divergence and A! with host arrays (allocated on first use): face velocities, P,
+     * densities, corrected velocities, the result, and the band */
+    double* pr[11] = {};
+    short* pr_band = nullptr;
     AdjCell* adj_cells = nullptr;
     AdjTet* adj_tets = nullptr;
     long adj_cells_cap = 0, adj_tets_cap = 0;
@@ -400,7 +404,8 @@ int slvof_destroy(slvof_ctx* c)
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
                     c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
                     c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo, c->gvel32[0], c->gvel32[1], c->gvel32[2],
-                    c->cu, c->cv, c->cw, c->us, c->vs, c->ws};
+                    c->cu, c->cv, c->cw, c->us, c->vs, c->ws, c->pr[0], c->pr[1], c->pr[2], c->pr[3],
+                    c->pr[4], c->pr[5], c->pr[6], c->pr[7], c->pr[8], c->pr[9], c->pr[10], c->pr_band};
     for (void* b : bufs)
         if (b) cudaFree(b);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -769,6 +774,87 @@ int slvof_transportSL_momentum(slvof_ctx* c, double dt, double* VF, const double
     TRY(d2h(c, vs, c->vs, b));
     TRY(d2h(c, ws, c->ws, b));
     return finish(c);
+}
+
+/* ---- divergence and the pressure operator ----------------------------------------------- */
+namespace {
+enum { PR_U = 0, PR_V, PR_W, PR_P, PR_DX, PR_DY, PR_DZ, PR_GX, PR_GY, PR_GZ, PR_OUT };
+
+int pr_alloc(slvof_ctx* c)
+{
+    if (c->pr_band) return 0;
+    for (double*& b : c->pr)
+        if (cudaMalloc((void**)&b, c->ncell * sizeof(double)) != cudaSuccess ||
+            cudaMemset(b, 0, c->ncell * sizeof(double)) != cudaSuccess)
+            return fail(c, SLVOF_E_NOMEM, "divergence buffers");
+    if (cudaMalloc((void**)&c->pr_band, c->ncell * sizeof(short)) != cudaSuccess)
+        return fail(c, SLVOF_E_NOMEM, "divergence buffers");
+    return 0;
+}
+
+int scheme_ok(slvof_ctx* c, int scheme)
+{
+    return (scheme == 0 || scheme == 1) ? 0 : fail(c, SLVOF_E_ARG, "scheme: 0 finite-difference, 1 semi-lagrangian");
+}
+} // namespace
+
+int slvof_divergence(slvof_ctx* c, double dt, int scheme, double* divg, const double* uf, const double* vf,
+                     const double* wf, const int16_t* band)
+{
+    TRY(begin(c));
+    TRY(scheme_ok(c, scheme));
+    TRY(pr_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    TRY(h2d(c, c->pr[PR_U], uf, b));
+    TRY(h2d(c, c->pr[PR_V], vf, b));
+    TRY(h2d(c, c->pr[PR_W], wf, b));
+    TRY(h2d(c, c->pr_band, band, c->ncell * sizeof(short)));
+    launch_divergence64(c->m, dt, scheme, c->pr[PR_U], c->pr[PR_V], c->pr[PR_W], c->pr_band, c->pr[PR_OUT], c->nsm,
+                        c->stream);
+    TRY(d2h(c, divg, c->pr[PR_OUT], b));
+    return finish(c, false);
+}
+
+int slvof_divergence_device(slvof_ctx* c, double dt, int scheme, double* d_divg, const double* d_uf,
+                            const double* d_vf, const double* d_wf, const int16_t* d_band)
+{
+    TRY(begin(c));
+    TRY(scheme_ok(c, scheme));
+    if (!d_divg || !d_uf || !d_vf || !d_wf || !d_band) return fail(c, SLVOF_E_ARG, "null device pointer");
+    launch_divergence64(c->m, dt, scheme, d_uf, d_vf, d_wf, (const short*)d_band, d_divg, c->nsm, c->stream);
+    return finish(c, false);
+}
+
+int slvof_A(slvof_ctx* c, double dt, int scheme, double* LHS, double* P, const double* uf, const double* vf,
+            const double* wf, const double* denx, const double* deny, const double* denz, const int16_t* band)
+{
+    TRY(begin(c));
+    TRY(scheme_ok(c, scheme));
+    TRY(pr_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    const double* in[7] = {uf, vf, wf, P, denx, deny, denz};
+    for (int q = 0; q < 7; ++q) TRY(h2d(c, c->pr[q], in[q], b));
+    TRY(h2d(c, c->pr_band, band, c->ncell * sizeof(short)));
+    launch_pressure_A64(c->m, dt, scheme, c->pr[PR_OUT], c->pr[PR_P], c->pr[PR_U], c->pr[PR_V], c->pr[PR_W],
+                        c->pr[PR_DX], c->pr[PR_DY], c->pr[PR_DZ], c->pr_band, c->pr[PR_GX], c->pr[PR_GY],
+                        c->pr[PR_GZ], c->nsm, c->stream);
+    TRY(d2h(c, LHS, c->pr[PR_OUT], b));
+    TRY(d2h(c, P, c->pr[PR_P], b));
+    return finish(c, false);
+}
+
+int slvof_A_device(slvof_ctx* c, double dt, int scheme, double* d_LHS, double* d_P, const double* d_uf,
+                   const double* d_vf, const double* d_wf, const double* d_denx, const double* d_deny,
+                   const double* d_denz, const int16_t* d_band)
+{
+    TRY(begin(c));
+    TRY(scheme_ok(c, scheme));
+    if (!d_LHS || !d_P || !d_uf || !d_vf || !d_wf || !d_denx || !d_deny || !d_denz || !d_band)
+        return fail(c, SLVOF_E_ARG, "null device pointer");
+    TRY(pr_alloc(c));
+    launch_pressure_A64(c->m, dt, scheme, d_LHS, d_P, d_uf, d_vf, d_wf, d_denx, d_deny, d_denz,
+                        (const short*)d_band, c->pr[PR_GX], c->pr[PR_GY], c->pr[PR_GZ], c->nsm, c->stream);
+    return finish(c, false);
 }
 
 /* ---- reverse pass ----------------------------------------------------------------------- */

@@ -105,6 +105,14 @@ void launch_adjoint32_elvira(const DevMesh& m, const double* VF, const signed ch
                              int nsm, cudaStream_t s);
 void launch_adjoint32_dist(const DevMesh& m, const double* VF, const float4* planes, const AdjBuffers& b, int nsm,
                            cudaStream_t s);
+/* divergence! / divg_cell and A! (k_fp64.cu); sl: pressure_scheme "semi-lagrangian".  A!
+ * fills P's ghosts in place and uses gx, gy, gz as its corrected face velocities. */
+void launch_divergence64(const DevMesh& m, double dt, int sl, const double* uf, const double* vf, const double* wf,
+                         const short* band, double* divg, int nsm, cudaStream_t s);
+void launch_pressure_A64(const DevMesh& m, double dt, int sl, double* LHS, double* P, const double* uf,
+                         const double* vf, const double* wf, const double* denx, const double* deny,
+                         const double* denz, const short* band, double* gx, double* gy, double* gz, int nsm,
+                         cudaStream_t s);
 void launch_sl32_pre(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                      const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
                      int* slow_cells, float4* slow_verts, int* slow_count, int* errw, int nsm, cudaStream_t s);

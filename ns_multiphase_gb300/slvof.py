@@ -67,6 +67,10 @@ SYMBOLS = [
     ("slvof_adjoint_set_vf", _I, [_P, _P]),
     ("slvof_adjoint_get", _I, [_P, _P, _P, _P, _P]),
     ("slvof_adjoint_zero_velocity", _I, [_P]),
+    ("slvof_divergence", _I, [_P, _D, _I, _P, _P, _P, _P, _P]),
+    ("slvof_divergence_device", _I, [_P, _D, _I, _P, _P, _P, _P, _P]),
+    ("slvof_A", _I, [_P, _D, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("slvof_A_device", _I, [_P, _D, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("slvof_adjoint_step", _I, [_P, _D]),
     ("slvof_adjoint_step_next", _I, [_P, _D, _P]),
     ("slvof_adjoint_fold", _I, [_P]),
@@ -288,6 +292,37 @@ class SLVOF:
     def load_vf_device(self, d_ptr: int):
         """Make a caller's device buffer the current VF (then prepare() before stepping)."""
         self._check(self.L.slvof_load_vf_device(self.h, d_ptr), "load_vf_device")
+
+    # ---- divergence and the pressure operator (FP64, either precision) -------------------
+    SCHEME = {"finite-difference": 0, "semi-lagrangian": 1}
+
+    def divergence(self, dt, uf, vf, wf, band, scheme="semi-lagrangian"):
+        """divergence! with divg_cell (src/Velocity.jl:59-122) of host face velocities."""
+        s = self.mesh.cell_shape
+        divg = self.mesh.cell_array()
+        self._check(self.L.slvof_divergence(self.h, dt, self.SCHEME[scheme], divg.ctypes.data,
+                                            _ptr(uf, np.float64, s), _ptr(vf, np.float64, s),
+                                            _ptr(wf, np.float64, s), _ptr(band, np.int16, s)), "divergence")
+        return divg
+
+    def divergence_device(self, dt, d_divg, d_uf, d_vf, d_wf, d_band, scheme="semi-lagrangian"):
+        self._check(self.L.slvof_divergence_device(self.h, dt, self.SCHEME[scheme], d_divg, d_uf, d_vf, d_wf,
+                                                   d_band), "divergence_device")
+
+    def A(self, dt, P, uf, vf, wf, denx, deny, denz, band, scheme="semi-lagrangian"):
+        """A! (src/Pressure.jl:83-115): returns LHS; P's ghosts are filled in place."""
+        s = self.mesh.cell_shape
+        LHS = self.mesh.cell_array()
+        self._check(self.L.slvof_A(self.h, dt, self.SCHEME[scheme], LHS.ctypes.data, _ptr(P, np.float64, s),
+                                   _ptr(uf, np.float64, s), _ptr(vf, np.float64, s), _ptr(wf, np.float64, s),
+                                   _ptr(denx, np.float64, s), _ptr(deny, np.float64, s),
+                                   _ptr(denz, np.float64, s), _ptr(band, np.int16, s)), "A")
+        return LHS
+
+    def A_device(self, dt, d_LHS, d_P, d_uf, d_vf, d_wf, d_denx, d_deny, d_denz, d_band,
+                 scheme="semi-lagrangian"):
+        self._check(self.L.slvof_A_device(self.h, dt, self.SCHEME[scheme], d_LHS, d_P, d_uf, d_vf, d_wf, d_denx,
+                                          d_deny, d_denz, d_band), "A_device")
 
     # ---- reverse pass ----------------------------------------------------------------------
     def adjoint_set_vf(self, gVF=None):

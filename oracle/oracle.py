@@ -57,6 +57,10 @@ def lib():
         L.orc_transport_mom.argtypes = [p, d] + [p] * 16
         L.orc_sl_flux_vol.restype = d
         L.orc_sl_flux_vol.argtypes = [p, i, i, i, i, p, p, p, d]
+        L.orc_divergence.restype = i
+        L.orc_divergence.argtypes = [p, d, i, p, p, p, p, p]
+        L.orc_A.restype = i
+        L.orc_A.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p, p]
         L.orc_compute_plic.restype = i
         L.orc_compute_plic.argtypes = [p, p, p, p, p, p]
         L.orc_compute_band.restype = i
@@ -143,6 +147,23 @@ class Oracle:
         flags = self.L.orc_transport_mom(_m(m), dt, _p(VF), _p(VFnew), _p(uf), _p(vf), _p(wf), _p(nx), _p(ny),
                                          _p(nz), _p(D), _p(band), _p(u), _p(v), _p(w), _p(us), _p(vs), _p(ws))
         return flags, us, vs, ws
+
+    def divergence(self, dt, uf, vf, wf, band, scheme=1):
+        """divergence! (src/Velocity.jl:59-68) with divg_cell; scheme 1 "semi-lagrangian",
+        0 "finite-difference".  Returns divg (cell array, 0 outside the interior)."""
+        m = self.mesh
+        divg = m.cell_array()
+        self.L.orc_divergence(_m(m), dt, scheme, _p(divg), _p(uf), _p(vf), _p(wf), _p(band))
+        return divg
+
+    def A(self, dt, P, uf, vf, wf, denx, deny, denz, band, scheme=1):
+        """A! (src/Pressure.jl:83-115): P's ghosts are filled in place; returns (LHS, gradx,
+        grady, gradz)."""
+        m = self.mesh
+        LHS, gx, gy, gz = m.cell_array(), m.cell_array(), m.cell_array(), m.cell_array()
+        self.L.orc_A(_m(m), dt, scheme, _p(LHS), _p(P), _p(uf), _p(vf), _p(wf), _p(denx), _p(deny), _p(denz),
+                     _p(band), _p(gx), _p(gy), _p(gz))
+        return LHS, gx, gy, gz
 
     def sl_flux_vol(self, direction, i, j, k, uf, vf, wf, dt):
         """SLfluxVol (src/VFgeom.jl:428-509); direction 0, 1, 2 for x, y, z."""

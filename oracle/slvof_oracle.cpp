@@ -805,6 +805,48 @@ void face_flux(const Grid& G, const Vel& V, const Mom& M, const int16_t* band, i
     }
 }
 
+/* ---------------------------------------------------------------------------------------
+ * Divergence and the pressure operator (src/Velocity.jl:59-122, src/Pressure.jl:83-115).
+ * ------------------------------------------------------------------------------------- */
+/* divg_cell, src/Velocity.jl:71-122.  sl: pressure_scheme == "semi-lagrangian".  A band cell
+ * gives (v2 - v1)/v2/dt with v1 the volume of its projected cell (cell2tets! with
+ * project_verts, tets_vol) and v2 = dx*dy*dz; any other cell the face fluxes, SLfluxVol/dt
+ * through a face whose neighbour is a band cell, the finite-difference flux otherwise. */
+double divg_cell(const Grid& G, const Vel& V, const int16_t* band, bool sl, int i, int j, int k, double dt)
+{
+    const orc_mesh* M = G.m;
+    auto inband = [&](int a, int b, int c) { return sl && std::abs((int)band[G.c(a, b, c)]) <= M->nband; };
+    if (inband(i, j, k)) {
+        double verts[15][3];
+        const double tetsign = cell2verts(G, i, j, k, verts);
+        for (int n = 0; n < 8; ++n) project(G, V, verts[n], i, j, k, dt);
+        tess_points(G.tess, verts);
+        double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+        for (int t = 0; t < tess_ntets(G.tess); ++t) {
+            int tv[4];
+            tess_tet(G.tess, t, tv);
+            double tet[4][3];
+            for (int n = 0; n < 4; ++n)
+                for (int p = 0; p < 3; ++p) tet[n][p] = verts[tv[n]][p];
+            vol += tet_vol(tet);
+        }
+        const double v2 = (M->dx * M->dy) * M->dz;
+        const double v1 = tetsign * vol;
+        return (v2 - v1) / v2 / dt;
+    }
+    auto flux = [&](int dir, int a, int b, int c, int na, int nb, int nc) {
+        if (inband(na, nb, nc)) return sl_flux_vol(G, V, dir, a, b, c, dt) / dt;
+        const long t = G.c(a, b, c);
+        if (dir == 0) return (M->dy * M->dz) * V.uf[t];
+        if (dir == 1) return (M->dx * M->dz) * V.vf[t];
+        return (M->dx * M->dy) * V.wf[t];
+    };
+    const double Fxm = flux(0, i, j, k, i - 1, j, k), Fxp = flux(0, i + 1, j, k, i + 1, j, k);
+    const double Fym = flux(1, i, j, k, i, j - 1, k), Fyp = flux(1, i, j + 1, k, i, j + 1, k);
+    const double Fzm = flux(2, i, j, k, i, j, k - 1), Fzp = flux(2, i, j, k + 1, i, j, k + 1);
+    return (((((Fxp - Fxm) + Fyp) - Fym) + Fzp) - Fzm) / ((M->dx * M->dy) * M->dz);
+}
+
 } // namespace
 
 /* =========================================================================================
@@ -1019,6 +1061,63 @@ int orc_transport_mom(const orc_mesh* M, double dt, double* VF, double* VFnew, c
             for (int i = 1; i <= G.N[0]; ++i) VF[G.v(i, j, k)] = VFnew[G.v(i, j, k)];
     orc_vf_ghost_fill(M, VF);
     return flags;
+}
+
+/* divergence!, src/Velocity.jl:59-68: divg = 0 on every cell, divg_cell on the interior.
+ * scheme 1 "semi-lagrangian", 0 "finite-difference". */
+int orc_divergence(const orc_mesh* M, double dt, int scheme, double* divg, const double* uf, const double* vf,
+                   const double* wf, const int16_t* band)
+{
+    Grid G(M);
+    Vel V{uf, vf, wf};
+    const long nc = G.n[0] * G.n[1] * G.n[2];
+    for (long t = 0; t < nc; ++t) divg[t] = 0.0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1)
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i) divg[G.c(i, j, k)] = divg_cell(G, V, band, scheme != 0, i, j, k, dt);
+    return 0;
+}
+
+/* A!, src/Pressure.jl:83-115: Neumann!(P) + update_borders!(P) in place; the pressure-corrected
+ * face velocities gradx = uf - dt/denx*(P - P[i-1])/dx (grady, gradz with the safe divide)
+ * over the reference's index ranges, 0 elsewhere; LHS = 0 on every cell and divg_cell of the
+ * corrected velocities on the interior. */
+int orc_A(const orc_mesh* M, double dt, int scheme, double* LHS, double* P, const double* uf, const double* vf,
+          const double* wf, const double* denx, const double* deny, const double* denz, const int16_t* band,
+          double* gradx, double* grady, double* gradz)
+{
+    Grid G(M);
+    Arr3<double> A(P, G.lo, G.hi);
+    neumann(G, A);
+    update_borders(G, A);
+    const long nc = G.n[0] * G.n[1] * G.n[2];
+    for (long t = 0; t < nc; ++t) { gradx[t] = 0.0; grady[t] = 0.0; gradz[t] = 0.0; LHS[t] = 0.0; }
+    const int* N = G.N;
+    for (int kk = 0; kk <= N[2] + 1; ++kk)
+        for (int jj = 0; jj <= N[1] + 1; ++jj)
+            for (int ii = 0; ii <= N[0] + 2; ++ii) {
+                const long t = G.c(ii, jj, kk);
+                gradx[t] = uf[t] - dt / denx[t] * (P[t] - P[G.c(ii - 1, jj, kk)]) / M->dx;
+            }
+    for (int kk = 0; kk <= N[2] + 1; ++kk)
+        for (int jj = 0; jj <= N[1] + 2; ++jj)
+            for (int ii = 0; ii <= N[0] + 1; ++ii) {
+                const long t = G.c(ii, jj, kk);
+                grady[t] = vf[t] - sdiv(sdiv(dt, deny[t]) * (P[t] - P[G.c(ii, jj - 1, kk)]), M->dy);
+            }
+    for (int kk = 0; kk <= N[2] + 2; ++kk)
+        for (int jj = 0; jj <= N[1] + 1; ++jj)
+            for (int ii = 0; ii <= N[0] + 1; ++ii) {
+                const long t = G.c(ii, jj, kk);
+                gradz[t] = wf[t] - sdiv(sdiv(dt, denz[t]) * (P[t] - P[G.c(ii, jj, kk - 1)]), M->dz);
+            }
+    Vel V{gradx, grady, gradz};
+#pragma omp parallel for collapse(2) schedule(dynamic, 1)
+    for (int k = 1; k <= N[2]; ++k)
+        for (int j = 1; j <= N[1]; ++j)
+            for (int i = 1; i <= N[0]; ++i) LHS[G.c(i, j, k)] = divg_cell(G, V, band, scheme != 0, i, j, k, dt);
+    return 0;
 }
 
 double orc_sl_flux_vol(const orc_mesh* M, int dir, int i, int j, int k, const double* uf, const double* vf,
