@@ -187,6 +187,23 @@ int slvof_A_device(slvof_ctx* ctx, double dt, int scheme, double* d_LHS, double*
                    const double* d_vf, const double* d_wf, const double* d_denx, const double* d_deny,
                    const double* d_denz, const int16_t* d_band);
 
+/* ---- curvature and face properties (FP64 in either precision) ------------------------------
+ * The curvature section of transport! (src/Transport.jl:187-191): Curve = 0 on every cell, then
+ * compute_curvature! (src/ELVIRA.jl:141-184) on the interior: heights of 7 cells along the
+ * normal's strictly dominant axis over the 3x3 columns, central differences, the height
+ * function's curvature; no strictly dominant component leaves 0.  x^(3/2) is x*sqrt(x).  Host
+ * arrays: VF (N+2g+6)^3, normals and Curve (N+2g)^3. */
+int slvof_computeCurvature(slvof_ctx* ctx, double* Curve, const double* VF, const double* nx, const double* ny,
+                           const double* nz);
+/* The same from the context's current VF and normals (after slvof_step or slvof_prepare), into a
+ * device array of the caller. */
+int slvof_compute_curvature_device(slvof_ctx* ctx, double* d_Curve);
+/* compute_props! (src/Tools.jl:1186-1210) on every cell: face VF clamp((VF + VF[-1])/2, 0, 1),
+ * density rho_liq*vf + rho_gas*(1 - vf) and viscosity vf*mu_liq + (1 - vf)*mu_gas per face
+ * direction.  Null viscosity arrays give compute_dens! (src/Tools.jl:1212-1231). */
+int slvof_computeProps(slvof_ctx* ctx, double rho_liq, double rho_gas, double mu_liq, double mu_gas, double* denx,
+                       double* deny, double* denz, double* viscx, double* viscy, double* viscz, const double* VF);
+
 /* ---- state save/restore and the reverse pass ------------------------------------------------
  * Reverse-mode derivative of the FP64 step (the hand-written adjoint; the reference has no
  * counterpart, its Julia callers would wrap it as a ChainRules rrule).  It treats the step as

@@ -366,7 +366,86 @@ __global__ void k_case_deformation3d(DevMesh m, double t, double T, double* uf, 
     }
 }
 
+/* ---- height-function curvature and face properties --------------------------------------
+ * compute_curvature! (src/ELVIRA.jl:141-184) on the interior, in the reference's operation
+ * order: 7-cell heights along the normal's strictly dominant axis in the 3x3 columns, times the
+ * spacing; central differences; the height function's curvature.  x^(3/2) is x*sqrt(x) (IEEE
+ * sqrt, one rounded product).  No strictly dominant component: Curve = 0. */
+__device__ __forceinline__ double pow32(double x) { return x * sqrt(x); }
+
+__global__ void k_curvature64(DevMesh m, const double* __restrict__ VF, const double* __restrict__ nx,
+                              const double* __restrict__ ny, const double* __restrict__ nz, double* __restrict__ Curve)
+{
+    const long total = (long)m.N[0] * m.N[1] * m.N[2];
+    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
+        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+        const long c = cidx(m, i, j, k);
+        const double ax = fabs(nx[c]), ay = fabs(ny[c]), az = fabs(nz[c]);
+        /* dominant axis q, tangential axes (a, b) in the reference's hf index order */
+        int q, a, b;
+        if (ax > ay && ax > az) { q = 0; a = 1; b = 2; }
+        else if (ay > ax && ay > az) { q = 1; a = 2; b = 0; }
+        else if (az > ay && az > ax) { q = 2; a = 0; b = 1; }
+        else { Curve[c] = 0.0; continue; }
+        const long st[3] = {1, m.vs1, m.vs2};
+        const long v0 = vidx(m, i, j, k);
+        double h[3][3];
+        for (int ob = -1; ob <= 1; ++ob)
+            for (int oa = -1; oa <= 1; ++oa) {
+                const long base = v0 + oa * st[a] + ob * st[b];
+                double s = 0.0;
+                for (int r = -3; r <= 3; ++r) s += __ldg(VF + base + r * st[q]);
+                h[oa + 1][ob + 1] = s * m.d[q];
+            }
+        const double da = m.d[a], db = m.d[b];
+        const double ha = (h[2][1] - h[0][1]) / (2 * da), hb = (h[1][2] - h[1][0]) / (2 * db);
+        const double haa = ((h[2][1] - 2 * h[1][1]) + h[0][1]) / (da * da);
+        const double hbb = ((h[1][2] - 2 * h[1][1]) + h[1][0]) / (db * db);
+        double hab;
+        if (q == 0) hab = (((h[2][2] - h[0][2]) - h[2][0]) + h[0][0]) / ((4 * da) * db);
+        else hab = (((h[2][2] - h[2][0]) - h[0][2]) + h[0][0]) / (q == 1 ? (4 * da) * db : (4 * db) * da);
+        Curve[c] = ((((haa + hbb) + haa * (hb * hb)) + hbb * (ha * ha)) - ((2 * hab) * ha) * hb) /
+                   pow32((1 + ha * ha) + hb * hb);
+    }
+}
+
+/* compute_props! (src/Tools.jl:1186-1210) on every cell: face VF clamp((VF + VF[-1])/2, 0, 1),
+ * density and (when visc[0] is not null) viscosity; compute_dens! without viscosities. */
+__global__ void k_props64(DevMesh m, const double* __restrict__ VF, double rho_liq, double rho_gas, double mu_liq,
+                          double mu_gas, double* denx, double* deny, double* denz, double* viscx, double* viscy,
+                          double* viscz)
+{
+    const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
+    const long total = (long)n0 * n1 * n2;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(t % n0) + m.lo, j = (int)((t / n0) % n1) + m.lo, k = (int)(t / ((long)n0 * n1)) + m.lo;
+        const long v = vidx(m, i, j, k);
+        const double c = VF[v];
+        const double f[3] = {jmin(1.0, jmax(0.0, (c + VF[v - 1]) / 2)), jmin(1.0, jmax(0.0, (c + VF[v - m.vs1]) / 2)),
+                             jmin(1.0, jmax(0.0, (c + VF[v - m.vs2]) / 2))};
+        double* den[3] = {denx, deny, denz};
+        double* visc[3] = {viscx, viscy, viscz};
+        for (int d = 0; d < 3; ++d) {
+            den[d][t] = rho_liq * f[d] + rho_gas * (1 - f[d]);
+            if (visc[0]) visc[d][t] = f[d] * mu_liq + (1 - f[d]) * mu_gas;
+        }
+    }
+}
+
 /* ---- launchers ------------------------------------------------------------------------ */
+void launch_curvature64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz,
+                        double* Curve, int nsm, cudaStream_t s)
+{
+    const long nc = (long)(m.N[0] + 2 * m.g) * (m.N[1] + 2 * m.g) * (m.N[2] + 2 * m.g);
+    cudaMemsetAsync(Curve, 0, nc * sizeof(double), s);
+    k_curvature64<<<nsm * 8, 256, 0, s>>>(m, VF, nx, ny, nz, Curve);
+}
+void launch_props64(const DevMesh& m, const double* VF, double rho_liq, double rho_gas, double mu_liq, double mu_gas,
+                    double* denx, double* deny, double* denz, double* viscx, double* viscy, double* viscz, int nsm,
+                    cudaStream_t s)
+{
+    k_props64<<<nsm * 8, 256, 0, s>>>(m, VF, rho_liq, rho_gas, mu_liq, mu_gas, denx, deny, denz, viscx, viscy, viscz);
+}
 void launch_vf_ghost(const DevMesh& m, const double* VFin, double* VFout, int nsm, cudaStream_t s)
 {
     k_vf_ghost<<<nsm * 8, 256, 0, s>>>(m, VFin, VFout);

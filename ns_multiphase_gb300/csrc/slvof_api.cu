@@ -857,6 +857,50 @@ int slvof_A_device(slvof_ctx* c, double dt, int scheme, double* d_LHS, double* d
     return finish(c, false);
 }
 
+/* ---- curvature and face properties ------------------------------------------------------- */
+int slvof_computeCurvature(slvof_ctx* c, double* Curve, const double* VF, const double* nx, const double* ny,
+                           const double* nz)
+{
+    TRY(begin(c));
+    TRY(pr_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    double* vf = c->VF[1 - c->vcur]; /* the step's scratch copy */
+    TRY(h2d(c, vf, VF, c->nvf * sizeof(double)));
+    TRY(h2d(c, c->pr[0], nx, b));
+    TRY(h2d(c, c->pr[1], ny, b));
+    TRY(h2d(c, c->pr[2], nz, b));
+    launch_curvature64(c->m, vf, c->pr[0], c->pr[1], c->pr[2], c->pr[PR_OUT], c->nsm, c->stream);
+    TRY(d2h(c, Curve, c->pr[PR_OUT], b));
+    return finish(c, false);
+}
+
+int slvof_compute_curvature_device(slvof_ctx* c, double* d_Curve)
+{
+    TRY(begin(c));
+    if (!d_Curve) return fail(c, SLVOF_E_ARG, "null device pointer");
+    if (!c->normals_valid) return fail(c, SLVOF_E_ARG, "normals of the current VF are not computed (slvof_prepare)");
+    launch_curvature64(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, d_Curve, c->nsm, c->stream);
+    return finish(c, false);
+}
+
+int slvof_computeProps(slvof_ctx* c, double rho_liq, double rho_gas, double mu_liq, double mu_gas, double* denx,
+                       double* deny, double* denz, double* viscx, double* viscy, double* viscz, const double* VF)
+{
+    TRY(begin(c));
+    const bool visc = viscx != nullptr;
+    if (!denx || !deny || !denz || (visc && (!viscy || !viscz)) || (!visc && (viscy || viscz)))
+        return fail(c, SLVOF_E_ARG, "density arrays, and all three or none of the viscosity arrays");
+    TRY(pr_alloc(c));
+    const size_t b = c->ncell * sizeof(double);
+    double* vf = c->VF[1 - c->vcur];
+    TRY(h2d(c, vf, VF, c->nvf * sizeof(double)));
+    launch_props64(c->m, vf, rho_liq, rho_gas, mu_liq, mu_gas, c->pr[0], c->pr[1], c->pr[2], visc ? c->pr[3] : nullptr,
+                   visc ? c->pr[4] : nullptr, visc ? c->pr[5] : nullptr, c->nsm, c->stream);
+    double* out[6] = {denx, deny, denz, viscx, viscy, viscz};
+    for (int q = 0; q < (visc ? 6 : 3); ++q) TRY(d2h(c, out[q], c->pr[q], b));
+    return finish(c, false);
+}
+
 /* ---- reverse pass ----------------------------------------------------------------------- */
 namespace {
 int adj_alloc(slvof_ctx* c)

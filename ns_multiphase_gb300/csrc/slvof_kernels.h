@@ -105,6 +105,13 @@ void launch_adjoint32_elvira(const DevMesh& m, const double* VF, const signed ch
                              int nsm, cudaStream_t s);
 void launch_adjoint32_dist(const DevMesh& m, const double* VF, const float4* planes, const AdjBuffers& b, int nsm,
                            cudaStream_t s);
+/* compute_curvature! on the interior (Curve zeroed first) and compute_props! / compute_dens!
+ * (visc* null) on every cell (k_common.cu). */
+void launch_curvature64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz,
+                        double* Curve, int nsm, cudaStream_t s);
+void launch_props64(const DevMesh& m, const double* VF, double rho_liq, double rho_gas, double mu_liq, double mu_gas,
+                    double* denx, double* deny, double* denz, double* viscx, double* viscy, double* viscz, int nsm,
+                    cudaStream_t s);
 /* divergence! / divg_cell and A! (k_fp64.cu); sl: pressure_scheme "semi-lagrangian".  A!
  * fills P's ghosts in place and uses gx, gy, gz as its corrected face velocities. */
 void launch_divergence64(const DevMesh& m, double dt, int sl, const double* uf, const double* vf, const double* wf,

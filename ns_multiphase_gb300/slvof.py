@@ -71,6 +71,9 @@ SYMBOLS = [
     ("slvof_divergence_device", _I, [_P, _D, _I, _P, _P, _P, _P, _P]),
     ("slvof_A", _I, [_P, _D, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     ("slvof_A_device", _I, [_P, _D, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("slvof_computeCurvature", _I, [_P, _P, _P, _P, _P, _P]),
+    ("slvof_compute_curvature_device", _I, [_P, _P]),
+    ("slvof_computeProps", _I, [_P, _D, _D, _D, _D, _P, _P, _P, _P, _P, _P, _P]),
     ("slvof_adjoint_step", _I, [_P, _D]),
     ("slvof_adjoint_step_next", _I, [_P, _D, _P]),
     ("slvof_adjoint_fold", _I, [_P]),
@@ -323,6 +326,29 @@ class SLVOF:
                  scheme="semi-lagrangian"):
         self._check(self.L.slvof_A_device(self.h, dt, self.SCHEME[scheme], d_LHS, d_P, d_uf, d_vf, d_wf, d_denx,
                                           d_deny, d_denz, d_band), "A_device")
+
+    # ---- curvature and face properties (FP64, either precision) --------------------------
+    def computeCurvature(self, VF, nx, ny, nz):
+        """transport!'s curvature section (compute_curvature!, src/ELVIRA.jl:141-184)."""
+        s = self.mesh.cell_shape
+        Curve = self.mesh.cell_array()
+        self._check(self.L.slvof_computeCurvature(self.h, Curve.ctypes.data, _ptr(VF, np.float64, self.mesh.vf_shape),
+                                                  _ptr(nx, np.float64, s), _ptr(ny, np.float64, s),
+                                                  _ptr(nz, np.float64, s)), "computeCurvature")
+        return Curve
+
+    def compute_curvature_device(self, d_curve: int):
+        self._check(self.L.slvof_compute_curvature_device(self.h, d_curve), "compute_curvature_device")
+
+    def computeProps(self, VF, rho_liq, rho_gas, mu_liq=None, mu_gas=None):
+        """compute_props! (compute_dens! without viscosities): (denx, deny, denz[, viscx, viscy, viscz])."""
+        m = self.mesh
+        den = [m.cell_array() for _ in range(3)]
+        visc = [m.cell_array() for _ in range(3)] if mu_liq is not None else None
+        ptrs = [a.ctypes.data for a in den] + ([a.ctypes.data for a in visc] if visc else [None, None, None])
+        self._check(self.L.slvof_computeProps(self.h, rho_liq, rho_gas, mu_liq or 0.0, mu_gas or 0.0, *ptrs,
+                                              _ptr(VF, np.float64, m.vf_shape)), "computeProps")
+        return tuple(den) + (tuple(visc) if visc else ())
 
     # ---- reverse pass ----------------------------------------------------------------------
     def adjoint_set_vf(self, gVF=None):

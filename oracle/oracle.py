@@ -59,6 +59,10 @@ def lib():
         L.orc_sl_flux_vol.argtypes = [p, i, i, i, i, p, p, p, d]
         L.orc_divergence.restype = i
         L.orc_divergence.argtypes = [p, d, i, p, p, p, p, p]
+        L.orc_curvature.restype = i
+        L.orc_curvature.argtypes = [p, p, p, p, p, p]
+        L.orc_props.restype = i
+        L.orc_props.argtypes = [p, p, d, d, d, d, p, p, p, p, p, p]
         L.orc_A.restype = i
         L.orc_A.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p, p]
         L.orc_compute_plic.restype = i
@@ -164,6 +168,22 @@ class Oracle:
         self.L.orc_A(_m(m), dt, scheme, _p(LHS), _p(P), _p(uf), _p(vf), _p(wf), _p(denx), _p(deny), _p(denz),
                      _p(band), _p(gx), _p(gy), _p(gz))
         return LHS, gx, gy, gz
+
+    def curvature(self, VF, nx, ny, nz):
+        """transport!'s curvature section (src/Transport.jl:187-191, compute_curvature!)."""
+        Curve = self.mesh.cell_array()
+        self.L.orc_curvature(_m(self.mesh), _p(Curve), _p(VF), _p(nx), _p(ny), _p(nz))
+        return Curve
+
+    def props(self, VF, rho_liq, rho_gas, mu_liq=None, mu_gas=None):
+        """compute_props! (or compute_dens! without viscosities): (denx, deny, denz[, viscx,
+        viscy, viscz])."""
+        m = self.mesh
+        den = [m.cell_array() for _ in range(3)]
+        visc = [m.cell_array() for _ in range(3)] if mu_liq is not None else [None] * 3
+        self.L.orc_props(_m(m), _p(VF), rho_liq, rho_gas, mu_liq or 0.0, mu_gas or 0.0,
+                         *[_p(a) for a in den], *[_p(a) if a is not None else None for a in visc])
+        return tuple(den) + (tuple(visc) if mu_liq is not None else ())
 
     def sl_flux_vol(self, direction, i, j, k, uf, vf, wf, dt):
         """SLfluxVol (src/VFgeom.jl:428-509); direction 0, 1, 2 for x, y, z."""

@@ -847,6 +847,74 @@ double divg_cell(const Grid& G, const Vel& V, const int16_t* band, bool sl, int 
     return (((((Fxp - Fxm) + Fyp) - Fym) + Fzp) - Fzm) / ((M->dx * M->dy) * M->dz);
 }
 
+/* ---------------------------------------------------------------------------------------
+ * Height-function curvature (src/ELVIRA.jl:141-184) and the face properties
+ * (compute_props!, src/Tools.jl:1186-1210).
+ * ------------------------------------------------------------------------------------- */
+/* x^(3/2) as x*sqrt(x): IEEE sqrt and one rounded product, within two ulp of a correctly
+ * rounded power (the reference's Julia ^ is not vendored). */
+inline double pow32(double x) { return x * std::sqrt(x); }
+
+/* compute_curvature!: heights of 7 cells along the normal's dominant axis (strictly larger
+ * component) in the 3x3 columns around the cell, scaled by the spacing; central differences of
+ * the heights; the curvature of the height function.  A cell without a strictly dominant
+ * component keeps Curve = 0. */
+double curvature_cell(const Grid& G, const double* VF, double nx, double ny, double nz, int i, int j, int k)
+{
+    const orc_mesh* M = G.m;
+    const double ax = std::fabs(nx), ay = std::fabs(ny), az = std::fabs(nz);
+    double h[3][3]; /* h[a][b]: a, b the two tangential offsets + 1 in the branch's hf order */
+    if (ax > ay && ax > az) {
+        for (int kk = -1; kk <= 1; ++kk)
+            for (int jj = -1; jj <= 1; ++jj) {
+                double s = 0.0;
+                for (int ii = -3; ii <= 3; ++ii) s += VF[G.v(i + ii, j + jj, k + kk)];
+                h[jj + 1][kk + 1] = s;
+            }
+        for (auto& r : h) for (double& x : r) x *= M->dx;
+        const double dy = M->dy, dz = M->dz;
+        const double hfy = (h[2][1] - h[0][1]) / (2 * dy), hfz = (h[1][2] - h[1][0]) / (2 * dz);
+        const double hfyy = ((h[2][1] - 2 * h[1][1]) + h[0][1]) / (dy * dy);
+        const double hfzz = ((h[1][2] - 2 * h[1][1]) + h[1][0]) / (dz * dz);
+        const double hfyz = (((h[2][2] - h[0][2]) - h[2][0]) + h[0][0]) / ((4 * dy) * dz);
+        return ((((hfyy + hfzz) + hfyy * (hfz * hfz)) + hfzz * (hfy * hfy)) - ((2 * hfyz) * hfy) * hfz) /
+               pow32((1 + hfy * hfy) + hfz * hfz);
+    }
+    if (ay > ax && ay > az) {
+        for (int ii = -1; ii <= 1; ++ii)
+            for (int kk = -1; kk <= 1; ++kk) {
+                double s = 0.0;
+                for (int jj = -3; jj <= 3; ++jj) s += VF[G.v(i + ii, j + jj, k + kk)];
+                h[kk + 1][ii + 1] = s;
+            }
+        for (auto& r : h) for (double& x : r) x *= M->dy;
+        const double dx = M->dx, dz = M->dz;
+        const double hfz = (h[2][1] - h[0][1]) / (2 * dz), hfx = (h[1][2] - h[1][0]) / (2 * dx);
+        const double hfzz = ((h[2][1] - 2 * h[1][1]) + h[0][1]) / (dz * dz);
+        const double hfxx = ((h[1][2] - 2 * h[1][1]) + h[1][0]) / (dx * dx);
+        const double hfxz = (((h[2][2] - h[2][0]) - h[0][2]) + h[0][0]) / ((4 * dz) * dx);
+        return ((((hfzz + hfxx) + hfzz * (hfx * hfx)) + hfxx * (hfz * hfz)) - ((2 * hfxz) * hfz) * hfx) /
+               pow32((1 + hfz * hfz) + hfx * hfx);
+    }
+    if (az > ay && az > ax) {
+        for (int jj = -1; jj <= 1; ++jj)
+            for (int ii = -1; ii <= 1; ++ii) {
+                double s = 0.0;
+                for (int kk = -3; kk <= 3; ++kk) s += VF[G.v(i + ii, j + jj, k + kk)];
+                h[ii + 1][jj + 1] = s;
+            }
+        for (auto& r : h) for (double& x : r) x *= M->dz;
+        const double dx = M->dx, dy = M->dy;
+        const double hfx = (h[2][1] - h[0][1]) / (2 * dx), hfy = (h[1][2] - h[1][0]) / (2 * dy);
+        const double hfxx = ((h[2][1] - 2 * h[1][1]) + h[0][1]) / (dx * dx);
+        const double hfyy = ((h[1][2] - 2 * h[1][1]) + h[1][0]) / (dy * dy);
+        const double hfxy = (((h[2][2] - h[2][0]) - h[0][2]) + h[0][0]) / ((4 * dy) * dx);
+        return ((((hfxx + hfyy) + hfxx * (hfy * hfy)) + hfyy * (hfx * hfx)) - ((2 * hfxy) * hfx) * hfy) /
+               pow32((1 + hfx * hfx) + hfy * hfy);
+    }
+    return 0.0;
+}
+
 } // namespace
 
 /* =========================================================================================
@@ -1117,6 +1185,46 @@ int orc_A(const orc_mesh* M, double dt, int scheme, double* LHS, double* P, cons
     for (int k = 1; k <= N[2]; ++k)
         for (int j = 1; j <= N[1]; ++j)
             for (int i = 1; i <= N[0]; ++i) LHS[G.c(i, j, k)] = divg_cell(G, V, band, scheme != 0, i, j, k, dt);
+    return 0;
+}
+
+/* The curvature section of transport! (src/Transport.jl:187-191): Curve = 0, then
+ * compute_curvature! on the interior. */
+int orc_curvature(const orc_mesh* M, double* Curve, const double* VF, const double* nx, const double* ny,
+                  const double* nz)
+{
+    Grid G(M);
+    const long nc = G.n[0] * G.n[1] * G.n[2];
+    for (long t = 0; t < nc; ++t) Curve[t] = 0.0;
+#pragma omp parallel for collapse(2)
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i) {
+                const long c = G.c(i, j, k);
+                Curve[c] = curvature_cell(G, VF, nx[c], ny[c], nz[c], i, j, k);
+            }
+    return 0;
+}
+
+/* compute_props! (src/Tools.jl:1186-1210) on every cell of the cell arrays: face VF
+ * clamp((VF + VF[-1])/2, 0, 1), density rho_liq*vf + rho_gas*(1 - vf), viscosity
+ * vf*mu_liq + (1 - vf)*mu_gas.  Null viscosity arrays give compute_dens! (:1212-1231). */
+int orc_props(const orc_mesh* M, const double* VF, double rho_liq, double rho_gas, double mu_liq, double mu_gas,
+              double* denx, double* deny, double* denz, double* viscx, double* viscy, double* viscz)
+{
+    Grid G(M);
+    double* den[3] = {denx, deny, denz};
+    double* visc[3] = {viscx, viscy, viscz};
+    for (int d = 0; d < 3; ++d)
+        for (int k = G.lo[2]; k <= G.hi[2]; ++k)
+            for (int j = G.lo[1]; j <= G.hi[1]; ++j)
+                for (int i = G.lo[0]; i <= G.hi[0]; ++i) {
+                    const int a = i - (d == 0), b = j - (d == 1), c = k - (d == 2);
+                    const double vf = jmin(1.0, jmax(0.0, (VF[G.v(i, j, k)] + VF[G.v(a, b, c)]) / 2));
+                    const long t = G.c(i, j, k);
+                    den[d][t] = rho_liq * vf + rho_gas * (1 - vf);
+                    if (visc[d]) visc[d][t] = vf * mu_liq + (1 - vf) * mu_gas;
+                }
     return 0;
 }
 
