@@ -63,8 +63,14 @@ typedef struct slvof_mesh {
     const double *xm, *ym, *zm;
     int32_t tesselation; /* param.tesselation (src/Parameters.jl:77): 5 "5_tets" (also 0), 6 "6_tets",
                             24 "24_tets" (src/VFgeom.jl:229-332) */
-    int32_t reserved;
+    int32_t pressure_scheme; /* param.pressure_scheme (src/Parameters.jl:60): SLVOF_PRESSURE_SEMI_LAGRANGIAN
+                                (0, the default) or SLVOF_PRESSURE_FINITE_DIFFERENCE (1), whose band cells
+                                add the flux-correction tets (src/Transport.jl:121-124; 5_tets, FP64
+                                context) and whose band-edge momentum fluxes are finite differences */
 } slvof_mesh;
+
+#define SLVOF_PRESSURE_SEMI_LAGRANGIAN 0
+#define SLVOF_PRESSURE_FINITE_DIFFERENCE 1
 
 typedef struct slvof_ctx slvof_ctx;
 
@@ -162,8 +168,8 @@ int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, cons
 
 /* ---- divergence and the pressure operator ---------------------------------------------------
  * FP64 in the reference's operation order, in either context precision (they are the pressure
- * solver's operators, not part of the interface step).  scheme: 1 pressure_scheme
- * "semi-lagrangian", 0 "finite-difference".  Cell arrays (N+2g)^3; band Int16.  Each call stands
+ * solver's operators, not part of the interface step).  scheme: SLVOF_PRESSURE_SEMI_LAGRANGIAN or
+ * SLVOF_PRESSURE_FINITE_DIFFERENCE (param.pressure_scheme).  Cell arrays (N+2g)^3; band Int16.  Each call stands
  * alone: the context's transport state is not read or changed.  For a multigrid level, use a
  * context created on that level's mesh. */
 /* divergence! (src/Velocity.jl:59-68) with divg_cell (src/Velocity.jl:71-122): divg = 0 on every

@@ -505,6 +505,84 @@ constexpr int SL_THREADS = 128;
  * (src/Transport.jl:116-145).  For 24_tets the mean points come from the projected vertices
  * and their cells from pt2index! seeded at the cell, as verts2tets! does.  With MOM also
  * us, vs, ws = vrhoU/vrho, ... (src/Transport.jl:146-148). */
+/* vertices of the flux volume of face `dir`: index offsets and projection flag, even and odd */
+__constant__ signed char c_fluxv[3][2][8][4] = {
+    {{{0, 0, 0, 1}, {0, 0, 0, 0}, {0, 1, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 1}, {0, 0, 1, 0}, {0, 1, 1, 1}, {0, 1, 1, 0}},
+     {{0, 0, 0, 0}, {0, 0, 0, 1}, {0, 1, 0, 0}, {0, 1, 0, 1}, {0, 0, 1, 0}, {0, 0, 1, 1}, {0, 1, 1, 0}, {0, 1, 1, 1}}},
+    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 0, 1, 1}, {1, 0, 1, 1}, {0, 0, 1, 0}, {1, 0, 1, 0}},
+     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 0, 1, 1}, {0, 0, 1, 1}, {1, 0, 1, 0}, {0, 0, 1, 0}}},
+    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {1, 1, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {1, 1, 0, 0}},
+     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 0, 1}, {0, 1, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 1, 0, 0}, {0, 1, 0, 0}}}};
+
+/* SLfluxVol (src/VFgeom.jl:428-509): the flux volume's vertices (tessellation order, mean
+ * points for 24_tets) and its signed volume. */
+__device__ double flux_verts64(const DevMesh& m, const Vel64& V, int dir, int i, int j, int k, double dt,
+                               double (*p)[3])
+{
+    const bool even = tess_even(m.tess, i, j, k);
+    const double tetsign = even ? 1.0 : -1.0;
+    for (int n = 0; n < 8; ++n) {
+        const signed char* f = c_fluxv[dir][even ? 0 : 1][n];
+        double x = fco(m, 0, i + f[0]), y = fco(m, 1, j + f[1]), z = fco(m, 2, k + f[2]);
+        if (f[3]) project64(m, V, x, y, z, i, j, k, dt);
+        p[n][0] = x; p[n][1] = y; p[n][2] = z;
+    }
+    tess_means<double>(m.tess, p);
+    double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+    for (int t = 0; t < tess_ntets(m.tess); ++t) {
+        const int a = tess_tet(m.tess, t, 0), b = tess_tet(m.tess, t, 1), c = tess_tet(m.tess, t, 2),
+                  e = tess_tet(m.tess, t, 3);
+        vol += tet_vol(p[a][0], p[a][1], p[a][2], p[b][0], p[b][1], p[b][2], p[c][0], p[c][1], p[c][2], p[e][0],
+                       p[e][1], p[e][2]);
+    }
+    return vol * tetsign;
+}
+
+__device__ double sl_flux_vol64(const DevMesh& m, const Vel64& V, int dir, int i, int j, int k, double dt)
+{
+    double p[15][3];
+    return flux_verts64(m, V, dir, i, j, k, dt, p);
+}
+
+/* add_correction_tets (src/VFgeom.jl:514-664), pressure_scheme "finite-difference", 5_tets:
+ * two tets (a,b,d,e), (b,c,d,e) on each face (x-, x+, y-, y+, z-, z+) over the quad a,b,c,d of
+ * the face's SLfluxVol vertices, with the apex e at the quad's mean except for the face-normal
+ * coordinate, which makes their volume the difference between the finite-difference flux
+ * volume dt * area * face velocity and the SL one.  Both volumes are affine in e with gradient
+ * (a x b + d x a + b x c + c x d)/6, so that coordinate moves by 6 (vol - V(mean)) / its
+ * component. */
+__device__ void correction_tet64(const DevMesh& m, const Vel64& V, int i, int j, int k, double dt, int f,
+                                 double (*tet)[3])
+{
+    const int dir = f >> 2, up = (f >> 1) & 1, second = f & 1; /* f = 4 dir + 2 up + second tet */
+    const int fi = i + (dir == 0 ? up : 0), fj = j + (dir == 1 ? up : 0), fk = k + (dir == 2 ? up : 0);
+    double fv[15][3];
+    const double flux_vol = flux_verts64(m, V, dir, fi, fj, fk, dt, fv);
+    const long t = cidx(m, fi, fj, fk);
+    const double divg_vol = dir == 0 ? ((dt * m.d[1]) * m.d[2]) * V.uf[t]
+                                     : (dir == 1 ? ((dt * m.d[0]) * m.d[2]) * V.vf[t] : ((dt * m.d[0]) * m.d[1]) * V.wf[t]);
+    const bool even = tess_even(m.tess, fi, fj, fk);
+    const double vol = even ? (divg_vol - flux_vol) : -(divg_vol - flux_vol);
+    int q[4];
+    if (dir == 0) {
+        if (even) { q[0] = 4; q[1] = 6; q[2] = 2; q[3] = 0; }
+        else { q[0] = 7; q[1] = 5; q[2] = 1; q[3] = 3; }
+    } else if (dir == 1) { q[0] = 1; q[1] = 5; q[2] = 4; q[3] = 0; }
+    else { q[0] = 1; q[1] = 0; q[2] = 2; q[3] = 3; }
+    const double *a = fv[q[0]], *b = fv[q[1]], *c = fv[q[2]], *d = fv[q[3]];
+    double e[3];
+    for (int p = 0; p < 3; ++p) e[p] = 0.25 * (((a[p] + b[p]) + c[p]) + d[p]);
+    const double v0 = tet_vol(a[0], a[1], a[2], b[0], b[1], b[2], d[0], d[1], d[2], e[0], e[1], e[2]) +
+                      tet_vol(b[0], b[1], b[2], c[0], c[1], c[2], d[0], d[1], d[2], e[0], e[1], e[2]);
+    const int p1 = (dir + 1) % 3, p2 = (dir + 2) % 3;
+    auto cr = [&](const double* u, const double* w) { return u[p1] * w[p2] - u[p2] * w[p1]; };
+    const double N = ((cr(a, b) + cr(d, a)) + cr(b, c)) + cr(c, d);
+    e[dir] += 6.0 * (vol - v0) / N;
+    const double* v4[4] = {second ? b : a, second ? c : b, d, e};
+    for (int n = 0; n < 4; ++n)
+        for (int p = 0; p < 3; ++p) tet[n][p] = v4[n][p];
+}
+
 template <bool MOM>
 __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, double dt,
                                           const signed char* __restrict__ phase, double* __restrict__ VFout,
@@ -538,7 +616,7 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
     }
     const long out = vidx(m, i, j, k);
     /* pure-donor shortcut (VF only: the momentum sums depend on each donor's share) */
-    if (!MOM && m.fast_pure) {
+    if (!MOM && m.fast_pure && !m.fd) {
         int lo0 = vi[0][0], hi0 = vi[0][0], lo1 = vi[0][1], hi1 = vi[0][1], lo2 = vi[0][2], hi2 = vi[0][2];
         for (int v = 1; v < np; ++v) {
             lo0 = min(lo0, vi[v][0]); hi0 = max(hi0, vi[v][0]);
@@ -575,6 +653,25 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
         double r[NA];
         clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err);
         for (int q = 0; q < NA; ++q) sum[q] += tetsign * r[q];
+    }
+    if (m.fd) {
+        /* pressure_scheme "finite-difference": the flux-correction tets, their vertices' cells
+         * by pt2index! seeded at the cell (src/Transport.jl:121-124, src/VFgeom.jl:654-661) */
+#pragma unroll 1
+        for (int f = 0; f < 12; ++f) {
+            double tet[4][3], cx[4], cy[4], cz[4];
+            int ci[4][3];
+            correction_tet64(m, V, i, j, k, dt, f, tet);
+            for (int n = 0; n < 4; ++n) {
+                cx[n] = tet[n][0]; cy[n] = tet[n][1]; cz[n] = tet[n][2];
+                ci[n][0] = pt2index1(m, 0, cx[n], i, err);
+                ci[n][1] = pt2index1(m, 1, cy[n], j, err);
+                ci[n][2] = pt2index1(m, 2, cz[n], k, err);
+            }
+            double r[NA];
+            clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err);
+            for (int q = 0; q < NA; ++q) sum[q] += tetsign * r[q];
+        }
     }
     if (!(sum[0] > 0.0) || !isfinite(sum[0])) err |= ERR_VOLUME;
     VFout[out] = sum[1] / sum[0];
@@ -615,37 +712,6 @@ __global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const
  * two band cells carries no flux, a face with one band cell the semi-Lagrangian flux volume
  * (SLfluxVol, src/VFgeom.jl:428-509), every other face the finite-difference flux.
  * ==================================================================================== */
-/* vertices of the flux volume of face `dir`: index offsets and projection flag, even and odd */
-__constant__ signed char c_fluxv[3][2][8][4] = {
-    {{{0, 0, 0, 1}, {0, 0, 0, 0}, {0, 1, 0, 1}, {0, 1, 0, 0}, {0, 0, 1, 1}, {0, 0, 1, 0}, {0, 1, 1, 1}, {0, 1, 1, 0}},
-     {{0, 0, 0, 0}, {0, 0, 0, 1}, {0, 1, 0, 0}, {0, 1, 0, 1}, {0, 0, 1, 0}, {0, 0, 1, 1}, {0, 1, 1, 0}, {0, 1, 1, 1}}},
-    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 0, 1, 1}, {1, 0, 1, 1}, {0, 0, 1, 0}, {1, 0, 1, 0}},
-     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 0, 1, 1}, {0, 0, 1, 1}, {1, 0, 1, 0}, {0, 0, 1, 0}}},
-    {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {1, 1, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {1, 1, 0, 0}},
-     {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 0, 1}, {0, 1, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 1, 0, 0}, {0, 1, 0, 0}}}};
-
-__device__ double sl_flux_vol64(const DevMesh& m, const Vel64& V, int dir, int i, int j, int k, double dt)
-{
-    const bool even = tess_even(m.tess, i, j, k);
-    const double tetsign = even ? 1.0 : -1.0;
-    double p[15][3];
-    for (int n = 0; n < 8; ++n) {
-        const signed char* f = c_fluxv[dir][even ? 0 : 1][n];
-        double x = fco(m, 0, i + f[0]), y = fco(m, 1, j + f[1]), z = fco(m, 2, k + f[2]);
-        if (f[3]) project64(m, V, x, y, z, i, j, k, dt);
-        p[n][0] = x; p[n][1] = y; p[n][2] = z;
-    }
-    tess_means<double>(m.tess, p);
-    double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
-    for (int t = 0; t < tess_ntets(m.tess); ++t) {
-        const int a = tess_tet(m.tess, t, 0), b = tess_tet(m.tess, t, 1), c = tess_tet(m.tess, t, 2),
-                  e = tess_tet(m.tess, t, 3);
-        vol += tet_vol(p[a][0], p[a][1], p[a][2], p[b][0], p[b][1], p[b][2], p[c][0], p[c][1], p[c][2], p[e][0],
-                       p[e][1], p[e][2]);
-    }
-    return vol * tetsign;
-}
-
 __device__ void face_flux64(const DevMesh& m, const Vel64& V, const Plic64& P, const short* __restrict__ band, int dir,
                             int i, int j, int k, double dt, double* F)
 {
@@ -657,7 +723,7 @@ __device__ void face_flux64(const DevMesh& m, const Vel64& V, const Plic64& P, c
     const bool bl = abs((int)band[l]) <= m.nband, bc = abs((int)band[c]) <= m.nband;
     if (bl && bc) {
         F[0] = 0.0; F[1] = 0.0; F[2] = 0.0;
-    } else if (bl || bc) {
+    } else if ((bl || bc) && !m.fd) {
         const double vol = sl_flux_vol64(m, V, dir, i, j, k, dt) / dt;
         F[0] = -uface * vol; F[1] = -vface * vol; F[2] = -wface * vol;
     } else {

@@ -33,6 +33,7 @@ struct DevMesh {
     int hi[3];
     int fast_pure; /* pure-donor shortcut valid (|coordinates| < Lx+Ly+Lz everywhere) */
     int tess;      /* tets per cell: 5, 6 or 24 (src/VFgeom.jl:229-332) */
+    int fd;        /* pressure_scheme "finite-difference": band cells add the flux-correction tets */
     double d[3];
     double VFlo, VFhi;
     double Lsum;    /* (Lx+Ly)+Lz, |D| of pure cells (src/VF.jl:116-120) */
@@ -99,6 +100,7 @@ inline void mesh_fill(const slvof_mesh* mesh, const double* coords, DevMesh& m)
     m.cellvol = (mesh->dx * mesh->dy) * mesh->dz;
     m.fast_pure = maxabs < m.Lsum * (1.0 - 1e-9);
     m.tess = mesh->tesselation == 0 ? 5 : mesh->tesselation;
+    m.fd = mesh->pressure_scheme == 1;
     m.cs1 = nn[0]; m.cs2 = nn[0] * nn[1];
     m.vs1 = nn[0] + 6; m.vs2 = (nn[0] + 6) * (nn[1] + 6);
 }

@@ -326,6 +326,13 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     if (mesh->tesselation != 0 && mesh->tesselation != 5 && mesh->tesselation != 6 && mesh->tesselation != 24)
         return SLVOF_E_ARG;
     if (!mesh->x || !mesh->y || !mesh->z || !mesh->xm || !mesh->ym || !mesh->zm) return SLVOF_E_ARG;
+    if (mesh->pressure_scheme != SLVOF_PRESSURE_SEMI_LAGRANGIAN && mesh->pressure_scheme != SLVOF_PRESSURE_FINITE_DIFFERENCE)
+        return SLVOF_E_ARG;
+    /* the flux-correction tets of the finite-difference scheme exist for 5_tets in the
+     * reference (add_correction_tets keeps the first five tets), and run in FP64 here */
+    if (mesh->pressure_scheme == SLVOF_PRESSURE_FINITE_DIFFERENCE &&
+        (precision != SLVOF_FP64 || (mesh->tesselation != 0 && mesh->tesselation != 5)))
+        return SLVOF_E_UNSUPPORTED;
     /* the pure/interface thresholds are compared as bit patterns, which orders doubles like the
      * floating-point compare only against positive finite thresholds */
     if (!(mesh->VFlo > 0.0 && mesh->VFhi > 0.0 && mesh->VFlo < 1e300 && mesh->VFhi < 1e300)) return SLVOF_E_UNSUPPORTED;
@@ -794,7 +801,9 @@ int pr_alloc(slvof_ctx* c)
 
 int scheme_ok(slvof_ctx* c, int scheme)
 {
-    return (scheme == 0 || scheme == 1) ? 0 : fail(c, SLVOF_E_ARG, "scheme: 0 finite-difference, 1 semi-lagrangian");
+    return (scheme == SLVOF_PRESSURE_SEMI_LAGRANGIAN || scheme == SLVOF_PRESSURE_FINITE_DIFFERENCE)
+               ? 0
+               : fail(c, SLVOF_E_ARG, "scheme: SLVOF_PRESSURE_SEMI_LAGRANGIAN or SLVOF_PRESSURE_FINITE_DIFFERENCE");
 }
 } // namespace
 
@@ -809,7 +818,7 @@ int slvof_divergence(slvof_ctx* c, double dt, int scheme, double* divg, const do
     TRY(h2d(c, c->pr[PR_V], vf, b));
     TRY(h2d(c, c->pr[PR_W], wf, b));
     TRY(h2d(c, c->pr_band, band, c->ncell * sizeof(short)));
-    launch_divergence64(c->m, dt, scheme, c->pr[PR_U], c->pr[PR_V], c->pr[PR_W], c->pr_band, c->pr[PR_OUT], c->nsm,
+    launch_divergence64(c->m, dt, scheme == SLVOF_PRESSURE_SEMI_LAGRANGIAN, c->pr[PR_U], c->pr[PR_V], c->pr[PR_W], c->pr_band, c->pr[PR_OUT], c->nsm,
                         c->stream);
     TRY(d2h(c, divg, c->pr[PR_OUT], b));
     return finish(c, false);
@@ -821,7 +830,7 @@ int slvof_divergence_device(slvof_ctx* c, double dt, int scheme, double* d_divg,
     TRY(begin(c));
     TRY(scheme_ok(c, scheme));
     if (!d_divg || !d_uf || !d_vf || !d_wf || !d_band) return fail(c, SLVOF_E_ARG, "null device pointer");
-    launch_divergence64(c->m, dt, scheme, d_uf, d_vf, d_wf, (const short*)d_band, d_divg, c->nsm, c->stream);
+    launch_divergence64(c->m, dt, scheme == SLVOF_PRESSURE_SEMI_LAGRANGIAN, d_uf, d_vf, d_wf, (const short*)d_band, d_divg, c->nsm, c->stream);
     return finish(c, false);
 }
 
@@ -835,7 +844,7 @@ int slvof_A(slvof_ctx* c, double dt, int scheme, double* LHS, double* P, const d
     const double* in[7] = {uf, vf, wf, P, denx, deny, denz};
     for (int q = 0; q < 7; ++q) TRY(h2d(c, c->pr[q], in[q], b));
     TRY(h2d(c, c->pr_band, band, c->ncell * sizeof(short)));
-    launch_pressure_A64(c->m, dt, scheme, c->pr[PR_OUT], c->pr[PR_P], c->pr[PR_U], c->pr[PR_V], c->pr[PR_W],
+    launch_pressure_A64(c->m, dt, scheme == SLVOF_PRESSURE_SEMI_LAGRANGIAN, c->pr[PR_OUT], c->pr[PR_P], c->pr[PR_U], c->pr[PR_V], c->pr[PR_W],
                         c->pr[PR_DX], c->pr[PR_DY], c->pr[PR_DZ], c->pr_band, c->pr[PR_GX], c->pr[PR_GY],
                         c->pr[PR_GZ], c->nsm, c->stream);
     TRY(d2h(c, LHS, c->pr[PR_OUT], b));
@@ -852,7 +861,7 @@ int slvof_A_device(slvof_ctx* c, double dt, int scheme, double* d_LHS, double* d
     if (!d_LHS || !d_P || !d_uf || !d_vf || !d_wf || !d_denx || !d_deny || !d_denz || !d_band)
         return fail(c, SLVOF_E_ARG, "null device pointer");
     TRY(pr_alloc(c));
-    launch_pressure_A64(c->m, dt, scheme, d_LHS, d_P, d_uf, d_vf, d_wf, d_denx, d_deny, d_denz,
+    launch_pressure_A64(c->m, dt, scheme == SLVOF_PRESSURE_SEMI_LAGRANGIAN, d_LHS, d_P, d_uf, d_vf, d_wf, d_denx, d_deny, d_denz,
                         (const short*)d_band, c->pr[PR_GX], c->pr[PR_GY], c->pr[PR_GZ], c->nsm, c->stream);
     return finish(c, false);
 }
@@ -1031,6 +1040,7 @@ int adjoint_step(slvof_ctx* c, double dt, const double* d_next)
     TRY(begin(c));
     TRY(adj_alloc(c));
     if (!c->normals_valid) return fail(c, SLVOF_E_ARG, "normals/PLIC/band of the current VF are not computed (slvof_prepare)");
+    if (c->m.fd) return fail(c, SLVOF_E_UNSUPPORTED, "the reverse pass of the flux-correction tets is not built");
     TRY(clear_err(c));
     AdjBuffers b{};
     b.gin = c->gvf[0];

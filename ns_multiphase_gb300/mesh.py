@@ -56,11 +56,12 @@ class MeshDesc(ctypes.Structure):
         ("x", ctypes.POINTER(ctypes.c_double)), ("y", ctypes.POINTER(ctypes.c_double)),
         ("z", ctypes.POINTER(ctypes.c_double)), ("xm", ctypes.POINTER(ctypes.c_double)),
         ("ym", ctypes.POINTER(ctypes.c_double)), ("zm", ctypes.POINTER(ctypes.c_double)),
-        ("tesselation", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("tesselation", ctypes.c_int32), ("pressure_scheme", ctypes.c_int32),
     ]
 
 
 TESSELATION = {"5_tets": 5, "6_tets": 6, "24_tets": 24}
+PRESSURE_SCHEME = {"semi-lagrangian": 0, "finite-difference": 1}  # src/Parameters.jl:60
 
 
 @dataclass
@@ -83,6 +84,7 @@ class Mesh:
     nband: int | None = None
     projection: str = "RK4"
     tesselation: str = "5_tets"
+    pressure_scheme: str = "semi-lagrangian"
     rho_liq: float = 1.0
     rho_gas: float = 1.0
     nghost: int = field(init=False)
@@ -157,5 +159,5 @@ class Mesh:
                 self.Lx, self.Ly, self.Lz, self.dx, self.dy, self.dz,
                 self.VFlo, self.VFhi, self.rho_liq, self.rho_gas,
                 p(self.x), p(self.y), p(self.z), p(self.xm), p(self.ym), p(self.zm),
-                TESSELATION[self.tesselation], 0)
+                TESSELATION[self.tesselation], PRESSURE_SCHEME[self.pressure_scheme])
         return self._desc

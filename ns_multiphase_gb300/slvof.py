@@ -297,7 +297,7 @@ class SLVOF:
         self._check(self.L.slvof_load_vf_device(self.h, d_ptr), "load_vf_device")
 
     # ---- divergence and the pressure operator (FP64, either precision) -------------------
-    SCHEME = {"finite-difference": 0, "semi-lagrangian": 1}
+    SCHEME = {"semi-lagrangian": 0, "finite-difference": 1}
 
     def divergence(self, dt, uf, vf, wf, band, scheme="semi-lagrangian"):
         """divergence! with divg_cell (src/Velocity.jl:59-122) of host face velocities."""

@@ -152,15 +152,15 @@ class Oracle:
                                          _p(nz), _p(D), _p(band), _p(u), _p(v), _p(w), _p(us), _p(vs), _p(ws))
         return flags, us, vs, ws
 
-    def divergence(self, dt, uf, vf, wf, band, scheme=1):
-        """divergence! (src/Velocity.jl:59-68) with divg_cell; scheme 1 "semi-lagrangian",
-        0 "finite-difference".  Returns divg (cell array, 0 outside the interior)."""
+    def divergence(self, dt, uf, vf, wf, band, scheme=0):
+        """divergence! (src/Velocity.jl:59-68) with divg_cell; scheme 0 "semi-lagrangian",
+        1 "finite-difference".  Returns divg (cell array, 0 outside the interior)."""
         m = self.mesh
         divg = m.cell_array()
         self.L.orc_divergence(_m(m), dt, scheme, _p(divg), _p(uf), _p(vf), _p(wf), _p(band))
         return divg
 
-    def A(self, dt, P, uf, vf, wf, denx, deny, denz, band, scheme=1):
+    def A(self, dt, P, uf, vf, wf, denx, deny, denz, band, scheme=0):
         """A! (src/Pressure.jl:83-115): P's ghosts are filled in place; returns (LHS, gradx,
         grady, gradz)."""
         m = self.mesh

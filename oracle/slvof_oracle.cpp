@@ -45,7 +45,7 @@ typedef struct orc_mesh {
     const double *x, *y, *z;    /* faces, index 1-g .. N+g+1 */
     const double *xm, *ym, *zm; /* centres, index 1-g .. N+g */
     int32_t tesselation;        /* 5, 6 or 24 (0 means 5): param.tesselation, src/Parameters.jl:77 */
-    int32_t reserved;
+    int32_t pressure_scheme;    /* 0 "semi-lagrangian", 1 "finite-difference": param.pressure_scheme */
 } orc_mesh;
 }
 
@@ -703,6 +703,8 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
     return acc;
 }
 
+void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt, double tets[12][4][3]);
+
 /* SL update of one cell, src/Transport.jl:111-148 with cell2tets!(project_verts=true,
  * compute_indices=true) (src/VFgeom.jl:345-420). Returns VFnew. */
 double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out,
@@ -735,6 +737,23 @@ double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int
         vrhoW += tetsign * r.vrhoW;
         vrho += tetsign * r.vrho;
     }
+    if (G.m->pressure_scheme == 1) {
+        /* pressure_scheme "finite-difference": the flux-correction tets, their vertices' cells
+         * by pt2index! seeded at the cell (src/Transport.jl:121-124, src/VFgeom.jl:654-661) */
+        double ct[12][4][3];
+        correction_tets(G, V, i, j, k, dt, ct);
+        for (int t = 0; t < 12; ++t) {
+            int ind[4][3];
+            for (int n = 0; n < 4; ++n) pt2index(G, ind[n], ct[t][n], i, j, k, e);
+            const CutOut r = cut_tet(G, P, M, ct[t], ind, false, false, false, 1, e);
+            vol += tetsign * r.vol;
+            vLiq += tetsign * r.vLiq;
+            vrhoU += tetsign * r.vrhoU;
+            vrhoV += tetsign * r.vrhoV;
+            vrhoW += tetsign * r.vrhoW;
+            vrho += tetsign * r.vrho;
+        }
+    }
     if (!(vol > 0.0) || !std::isfinite(vol)) e->flags |= E_VOLUME;
     if (vol_out) *vol_out = vol;
     /* us, vs, ws of the cell (src/Transport.jl:146-148) */
@@ -755,11 +774,11 @@ const int FLUXV[3][2][8][4] = {
     {{{0, 0, 0, 1}, {1, 0, 0, 1}, {0, 1, 0, 1}, {1, 1, 0, 1}, {0, 0, 0, 0}, {1, 0, 0, 0}, {0, 1, 0, 0}, {1, 1, 0, 0}},
      {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 0, 1}, {0, 1, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 1, 0, 0}, {0, 1, 0, 0}}}};
 
-double sl_flux_vol(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt)
+/* SLfluxVol's vertices (tessellation order, mean points for 24_tets) and signed volume. */
+double sl_flux_verts(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt, double verts[15][3])
 {
     const bool even = G.tess != 5 || ((i + j + k) % 2) == 0;
     const double tetsign = even ? 1.0 : -1.0;
-    double verts[15][3];
     for (int n = 0; n < 8; ++n) {
         const int* f = FLUXV[dir][even ? 0 : 1][n];
         verts[n][0] = G.x(i + f[0]);
@@ -780,6 +799,63 @@ double sl_flux_vol(const Grid& G, const Vel& V, int dir, int i, int j, int k, do
     return vol * tetsign;
 }
 
+double sl_flux_vol(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt)
+{
+    double verts[15][3];
+    return sl_flux_verts(G, V, dir, i, j, k, dt, verts);
+}
+
+/* Apex of add_correction_tets' tets (a,b,d,e) and (b,c,d,e) over a face quad a,b,c,d
+ * (src/VFgeom.jl:590-646): e starts at the quad's mean 0.25*(a+b+c+d) and its `axis`
+ * coordinate moves until V(a,b,d,e) + V(b,c,d,e) = vol.  Both volumes are affine in e with
+ * gradient (a x b + d x a + b x c + c x d)/6, so the coordinate moves by
+ * 6 (vol - V(mean)) / that gradient's component.  (The reference writes the same solution as
+ * one expanded polynomial, which rounds differently.) */
+void correction_apex(int axis, const double* a, const double* b, const double* c, const double* d, double vol,
+                     double e[3])
+{
+    for (int p = 0; p < 3; ++p) e[p] = 0.25 * (((a[p] + b[p]) + c[p]) + d[p]);
+    double t1[4][3], t2[4][3];
+    for (int p = 0; p < 3; ++p) {
+        t1[0][p] = a[p]; t1[1][p] = b[p]; t1[2][p] = d[p]; t1[3][p] = e[p];
+        t2[0][p] = b[p]; t2[1][p] = c[p]; t2[2][p] = d[p]; t2[3][p] = e[p];
+    }
+    const double v0 = tet_vol(t1) + tet_vol(t2);
+    const int p = (axis + 1) % 3, q = (axis + 2) % 3; /* (u x w)_axis = u_p w_q - u_q w_p */
+    auto cr = [&](const double* u, const double* w) { return u[p] * w[q] - u[q] * w[p]; };
+    const double N = ((cr(a, b) + cr(d, a)) + cr(b, c)) + cr(c, d);
+    e[axis] += 6.0 * (vol - v0) / N;
+}
+
+/* add_correction_tets (src/VFgeom.jl:514-664), 5_tets: two tets on each face of cell (i,j,k),
+ * faces x-, x+, y-, y+, z-, z+, built on the face's SLfluxVol vertices so that the face's flux
+ * volume becomes the finite-difference one, dt * area * face velocity. */
+void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt, double tets[12][4][3])
+{
+    const orc_mesh* M = G.m;
+    static const int QUAD[3][2][4] = {{{4, 6, 2, 0}, {7, 5, 1, 3}}, {{1, 5, 4, 0}, {1, 5, 4, 0}}, {{1, 0, 2, 3}, {1, 0, 2, 3}}};
+    for (int f = 0; f < 6; ++f) {
+        const int dir = f / 2, up = f & 1;
+        const int fi = i + (dir == 0 ? up : 0), fj = j + (dir == 1 ? up : 0), fk = k + (dir == 2 ? up : 0);
+        double fv[15][3];
+        const double flux_vol = sl_flux_verts(G, V, dir, fi, fj, fk, dt, fv);
+        const long t = G.c(fi, fj, fk);
+        const double divg_vol = dir == 0 ? ((dt * M->dy) * M->dz) * V.uf[t]
+                                         : (dir == 1 ? ((dt * M->dx) * M->dz) * V.vf[t] : ((dt * M->dx) * M->dy) * V.wf[t]);
+        const bool even = G.tess != 5 || ((fi + fj + fk) % 2) == 0; /* oddEvenCell of the face's cell */
+        const double vol = even ? (divg_vol - flux_vol) : -(divg_vol - flux_vol);
+        const int* qd = QUAD[dir][even ? 0 : 1];
+        const double *a = fv[qd[0]], *b = fv[qd[1]], *c = fv[qd[2]], *d = fv[qd[3]];
+        double e[3];
+        correction_apex(dir, a, b, c, d, vol, e);
+        for (int p = 0; p < 3; ++p) {
+            tets[2 * f][0][p] = a[p]; tets[2 * f][1][p] = b[p]; tets[2 * f][2][p] = d[p]; tets[2 * f][3][p] = e[p];
+            tets[2 * f + 1][0][p] = b[p]; tets[2 * f + 1][1][p] = c[p]; tets[2 * f + 1][2][p] = d[p];
+            tets[2 * f + 1][3][p] = e[p];
+        }
+    }
+}
+
 /* Convective fluxes through face `dir` (0 x, 1 y, 2 z) at the low side of cell (i,j,k),
  * src/Transport.jl:34-104 with pressure_scheme "semi-lagrangian". */
 void face_flux(const Grid& G, const Vel& V, const Mom& M, const int16_t* band, int dir, int i, int j, int k, double dt,
@@ -794,7 +870,7 @@ void face_flux(const Grid& G, const Vel& V, const Mom& M, const int16_t* band, i
     const bool bl = std::abs((int)band[l]) <= nb, bc = std::abs((int)band[c]) <= nb;
     if (bl && bc) {
         F[0] = 0.0; F[1] = 0.0; F[2] = 0.0;
-    } else if (bl || bc) {
+    } else if ((bl || bc) && G.m->pressure_scheme == 0) {
         const double vol = sl_flux_vol(G, V, dir, i, j, k, dt) / dt;
         F[0] = -uface * vol; F[1] = -vface * vol; F[2] = -wface * vol;
     } else {
@@ -1132,7 +1208,7 @@ int orc_transport_mom(const orc_mesh* M, double dt, double* VF, double* VFnew, c
 }
 
 /* divergence!, src/Velocity.jl:59-68: divg = 0 on every cell, divg_cell on the interior.
- * scheme 1 "semi-lagrangian", 0 "finite-difference". */
+ * scheme 0 "semi-lagrangian", 1 "finite-difference". */
 int orc_divergence(const orc_mesh* M, double dt, int scheme, double* divg, const double* uf, const double* vf,
                    const double* wf, const int16_t* band)
 {
@@ -1143,7 +1219,7 @@ int orc_divergence(const orc_mesh* M, double dt, int scheme, double* divg, const
 #pragma omp parallel for collapse(2) schedule(dynamic, 1)
     for (int k = 1; k <= G.N[2]; ++k)
         for (int j = 1; j <= G.N[1]; ++j)
-            for (int i = 1; i <= G.N[0]; ++i) divg[G.c(i, j, k)] = divg_cell(G, V, band, scheme != 0, i, j, k, dt);
+            for (int i = 1; i <= G.N[0]; ++i) divg[G.c(i, j, k)] = divg_cell(G, V, band, scheme == 0, i, j, k, dt);
     return 0;
 }
 
@@ -1184,7 +1260,7 @@ int orc_A(const orc_mesh* M, double dt, int scheme, double* LHS, double* P, cons
 #pragma omp parallel for collapse(2) schedule(dynamic, 1)
     for (int k = 1; k <= N[2]; ++k)
         for (int j = 1; j <= N[1]; ++j)
-            for (int i = 1; i <= N[0]; ++i) LHS[G.c(i, j, k)] = divg_cell(G, V, band, scheme != 0, i, j, k, dt);
+            for (int i = 1; i <= N[0]; ++i) LHS[G.c(i, j, k)] = divg_cell(G, V, band, scheme == 0, i, j, k, dt);
     return 0;
 }
 

@@ -83,7 +83,7 @@ def test_zalesak_rotation_divergence(built):
     g = SLVOF(m, "fp64")
     got = g.divergence(dt, uf, vf, wf, band)
     g.close()
-    assert np.array_equal(got, o.divergence(dt, uf, vf, wf, band, 1))
+    assert np.array_equal(got, o.divergence(dt, uf, vf, wf, band, 0))
     inband = np.abs(m.interior(band)) <= m.nband
     assert np.max(np.abs(m.interior(got)[inband])) <= 1e-9
 

@@ -295,3 +295,49 @@ def test_host_transport_refreshes_phase_codes_of_uploaded_planes():
     flags, _ = o2.transport(dt, VFb, uf, vf, wf, nxb, nyb, nzb, Db, band_b)
     assert flags == 0
     assert_same(VFg, VFb, "VF")
+
+
+def test_finite_difference_scheme_correction_tets():
+    """pressure_scheme "finite-difference": band cells add the flux-correction tets
+    (add_correction_tets, src/VFgeom.jl:514-664) and band-edge momentum fluxes are finite
+    differences; VF over several steps and the momentum, bit for bit against the restatement."""
+    m = Mesh(Nx=20, Ny=20, Nz=20, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, pressure_scheme="finite-difference")
+    VF = cases.vf_spheres(m, [[0.45, 0.52, 0.5]], [0.22], nF=10)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF)
+    dt = 0.5 * m.dx / 2.0
+    rng = np.random.default_rng(8)
+    noise = [0.05 * rng.standard_normal(m.cell_shape) for _ in range(3)]
+    for s in range(4):
+        uf, vf, wf = (a + e for a, e in zip(cases.deformation3d_faces(m, 0.2 + (s + 0.5) * dt, 3.0), noise))
+        uf, vf, wf = (np.asfortranarray(x) for x in (uf, vf, wf))
+        g.upload_velocity(uf, vf, wf)
+        mass = g.step(dt)
+        assert o.step(dt, VFo, uf, vf, wf, nx, ny, nz, D, band) == 0
+    assert_same(g.download_vf(), VFo, "VF")
+    mo = o.mass(VFo)
+    assert abs(mass - mo) <= 1e-13 * abs(mo)
+    g.close()
+    # momentum with the finite-difference scheme's fluxes
+    mm = Mesh(Nx=18, Ny=16, Nz=14, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, rho_liq=1000.0, rho_gas=1.2,
+              pressure_scheme="finite-difference")
+    _, _, VF2, band2, nx2, ny2, nz2, D2, uf2, vf2, wf2, u2, v2, w2, dt2 = momentum_state("5_tets")
+    o2 = Oracle(mm)
+    g2 = ctx(mm)
+    VFg = VF2.copy(order="F")
+    r = g2.transportSL_momentum(dt2, VFg, uf2, vf2, wf2, nx2, ny2, nz2, D2, band2, u2, v2, w2)
+    flags, *ro = o2.transport_mom(dt2, VF2, uf2, vf2, wf2, nx2, ny2, nz2, D2, band2, u2, v2, w2)
+    assert flags == 0
+    assert_same(VFg, VF2, "VF (momentum call)")
+    for a, b, name in zip(r, ro, ("us", "vs", "ws")):
+        assert_same(mm.interior(a), mm.interior(b), name)
+    g2.close()
+
+
+@pytest.mark.parametrize("precision,tess", [("mixed", "5_tets"), ("fp64", "24_tets")])
+def test_finite_difference_scheme_unsupported_combinations(precision, tess):
+    """The correction tets are defined for 5_tets (the reference keeps the first five tets) and
+    built for FP64 contexts; other combinations are refused at creation."""
+    from ns_multiphase_gb300.slvof import SLVOF
+    m = Mesh(Nx=8, Ny=8, Nz=8, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess, pressure_scheme="finite-difference")
+    with pytest.raises(RuntimeError):
+        SLVOF(m, precision)

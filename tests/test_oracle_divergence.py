@@ -37,7 +37,7 @@ def test_uniform_flow_has_no_divergence(tess):
     vf[...] = -0.3
     wf[...] = 0.2
     dt = 0.5 * m.dx
-    for scheme in (0, 1):
+    for scheme in (0, 1):  # semi-lagrangian, finite-difference
         divg = o.divergence(dt, uf, vf, wf, band, scheme)
         assert np.max(np.abs(m.interior(divg))) <= 1e-10, scheme
     assert np.count_nonzero(np.abs(m.interior(band)) <= m.nband) > 100
@@ -49,9 +49,9 @@ def test_linear_flow_divergence(tess):
     a = 0.8
     uf, vf, wf = linear_faces(m, a)
     dt = 0.5 * m.dx
-    fd = m.interior(o.divergence(dt, uf, vf, wf, band, 0))
+    fd = m.interior(o.divergence(dt, uf, vf, wf, band, 1))
     assert np.max(np.abs(fd - a)) <= 1e-12
-    sl = m.interior(o.divergence(dt, uf, vf, wf, band, 1))
+    sl = m.interior(o.divergence(dt, uf, vf, wf, band, 0))
     inband = np.abs(m.interior(band)) <= m.nband
     assert inband.sum() > 100
     # the projected cell's volume is exp(-a dt) of the cell's, up to RK4's (a dt)^5/120
@@ -91,7 +91,7 @@ def test_A_pressure_gradient_terms():
     P = m.cell_array()
     P[...] = (np.arange(m.cell_shape[0]) * 0.5)[:, None, None]   # dP/dx = 0.5 / dx per cell
     rho = np.ones(m.cell_shape, order="F")
-    LHS, gx, gy, gz = o.A(dt, P, uf, vf, wf, rho, rho, rho, band, 0)
+    LHS, gx, gy, gz = o.A(dt, P, uf, vf, wf, rho, rho, rho, band, 1)
     # Neumann! copies P[1] to P[0] and P[N] to P[N+1], so the end faces see no gradient; the
     # others -dt*0.5/dx
     g = m.nghost
