@@ -48,47 +48,42 @@ __device__ __forceinline__ Cube make_cube(float a, float b, float c)
     return q;
 }
 
-__device__ __forceinline__ float cube_lower(const Cube& q, float a)
+/* The volume below a in [0, 1/2], every interval's expression evaluated and the right one
+ * selected, so a warp whose lanes score different candidate planes (in different intervals)
+ * does not diverge; where b = a - m2 <= 0 or c = a - m3 <= 0 that cubic correction vanishes. */
+__device__ __forceinline__ float cube_lower_sel(const Cube& q, float a)
 {
-    if (a < q.m1) return a * a * a * q.im1 * q.i6m23;
+    const float t1 = a * a * a * q.im1 * q.i6m23;
     const float base = fmaf(3.f * a, a - q.m1, q.m1 * q.m1) * q.i6m23;
-    if (a < q.m2) return base;
-    if (a < q.m12 && a < q.m3) {
-        const float b = a - q.m2;
-        return fmaf(-(b * q.im1) * b * b, q.i6m23, base);
-    }
-    if (q.m3 < q.m12) {
-        const float b = a - q.m2, c = a - q.m3;
-        return fmaf(-fmaf((b * q.im1) * b, b, (c * q.im1) * c * c), q.i6m23, base);
-    }
-    return fmaf(2.f, a, -q.m12) * q.i2m3;
+    const float b = fmaxf(a - q.m2, 0.f), c = fmaxf(a - q.m3, 0.f);
+    const float corr = fmaf((b * q.im1) * b, b, (c * q.im1) * c * c);
+    const float cub = fmaf(-corr, q.i6m23, base);
+    const float lin = fmaf(2.f, a, -q.m12) * q.i2m3;
+    const float r = (q.m3 >= q.m12 && a >= q.m12) ? lin : cub;
+    return a < q.m1 ? t1 : r;
 }
 
+/* d/da of cube_lower_sel (the cut area), for the Newton inverse, the same way. */
+__device__ __forceinline__ float cube_area_sel(const Cube& q, float a)
+{
+    const float t1 = 3.f * a * a * q.im1 * q.i6m23;
+    const float base = (6.f * a - 3.f * q.m1) * q.i6m23;
+    const float b = fmaxf(a - q.m2, 0.f), c = fmaxf(a - q.m3, 0.f);
+    const float cub = base - 3.f * ((b * q.im1) * b + (c * q.im1) * c) * q.i6m23;
+    const float r = (q.m3 >= q.m12 && a >= q.m12) ? 2.f * q.i2m3 : cub;
+    return a < q.m1 ? t1 : r;
+}
+
+/* The fraction for any a: 0 below the cube, 1 above, V(a) = 1 - V(1 - a) above 1/2. */
 __device__ __forceinline__ float cube_frac(const Cube& q, float a)
 {
-    if (a <= 0.f) return 0.f;
-    if (a >= 1.f) return 1.f;
-    return a <= 0.5f ? cube_lower(q, a) : 1.f - cube_lower(q, 1.f - a);
+    const bool upper = a > 0.5f;
+    const float aa = fminf(fmaxf(upper ? 1.f - a : a, 0.f), 0.5f);
+    const float r = cube_lower_sel(q, aa);
+    return upper ? 1.f - r : r;
 }
 
-/* d/da of cube_lower (cut area), for the Newton inverse. */
-__device__ __forceinline__ float cube_area(const Cube& q, float a)
-{
-    if (a < q.m1) return 3.f * a * a * q.im1 * q.i6m23;
-    const float base = (6.f * a - 3.f * q.m1) * q.i6m23;
-    if (a < q.m2) return base;
-    if (a < q.m12 && a < q.m3) {
-        const float b = a - q.m2;
-        return base - 3.f * (b * q.im1) * b * q.i6m23;
-    }
-    if (q.m3 < q.m12) {
-        const float b = a - q.m2, c = a - q.m3;
-        return base - 3.f * ((b * q.im1) * b + (c * q.im1) * c) * q.i6m23;
-    }
-    return 2.f * q.i2m3;
-}
-
-/* alpha with cube_lower(alpha) = V for V in [0, 1/2] (computeAlpha's role, src/VF.jl:164-214).
+/* alpha with cube_lower_sel(alpha) = V for V in [0, 1/2] (computeAlpha's role, src/VF.jl:164-214).
  * The first two intervals and the linear one are inverted in closed form (cbrt, the
  * quadratic root, a line); on the cubic interval the bracket end points are known, so a
  * linear start and bracketed Newton converge to FP32 rounding in a few steps. */
@@ -105,17 +100,17 @@ __device__ __forceinline__ float cube_alpha(const Cube& q, float V)
         if (V >= q.m12 * q.i2m3) return fmaf(V, q.m3, 0.5f * q.m12);
         lo = q.m2; hi = q.m12;
     } else {
-        if (V < cube_lower(q, q.m3)) { lo = q.m2; hi = q.m3; }
+        if (V < cube_lower_sel(q, q.m3)) { lo = q.m2; hi = q.m3; }
         else { lo = q.m3; hi = 0.5f; }
     }
-    const float vl = cube_lower(q, lo), vh = cube_lower(q, hi);
+    const float vl = cube_lower_sel(q, lo), vh = cube_lower_sel(q, hi);
     float a = vh > vl ? fmaf((V - vl) / (vh - vl), hi - lo, lo) : 0.5f * (lo + hi);
 #pragma unroll 1
     for (int it = 0; it < 5; ++it) {
-        const float f = cube_lower(q, a) - V;
+        const float f = cube_lower_sel(q, a) - V;
         if (f > 0.f) hi = a;
         else lo = a;
-        const float s = cube_area(q, a);
+        const float s = cube_area_sel(q, a);
         float an = s > 0.f ? a - f / s : 0.5f * (lo + hi);
         if (!(an >= lo && an <= hi)) an = 0.5f * (lo + hi);
         a = an;
@@ -304,25 +299,17 @@ __device__ __forceinline__ void candidate64(const DevMesh& m, const double* sv, 
 }
 
 __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, const double* __restrict__ VF,
-                                                                    double* __restrict__ nx, double* __restrict__ ny,
-                                                                    double* __restrict__ nz,
                                                                     const int* __restrict__ list,
                                                                     const int* __restrict__ count, int* work,
-                                                                    int* stats, signed char* __restrict__ cand,
-                                                                    int* errw)
+                                                                    int* n_arb, int2* __restrict__ arb,
+                                                                    signed char* __restrict__ cand)
 {
-    __shared__ CutCase s_tab[16];
-    __shared__ double s_vd[EL32_WARPS][27];
     __shared__ float s_vf[EL32_WARPS][27];
-    __shared__ double s_term[EL32_WARPS][27][5];
-    __shared__ double s_full[EL32_WARPS][27];
-    load_table(s_tab);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n_items = *count;
     const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
     const int ncand = 9 * (fam_on[0] + fam_on[1] + fam_on[2]);
     const float dx = (float)m.d[0], dy = (float)m.d[1], dz = (float)m.d[2];
-    int err = 0, n_arb = 0;
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(work, 1);
@@ -332,11 +319,7 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
         const int i = 1 + L % m.N[0];
         const int j = 1 + (L / m.N[0]) % m.N[1];
         const int k = 1 + L / (m.N[0] * m.N[1]);
-        if (lane < 27) {
-            const double v = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
-            s_vd[w][lane] = v;
-            s_vf[w][lane] = (float)v;
-        }
+        if (lane < 27) s_vf[w][lane] = (float)VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
         __syncwarp();
         const float* sv = s_vf[w];
         float err_ = INFINITY, tol = 0.f;
@@ -377,54 +360,85 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) hi = fminf(hi, __shfl_xor_sync(0xffffffffu, hi, off));
         const unsigned contend = __ballot_sync(0xffffffffu, fin && err_ - tol <= hi);
-        int winner = 32;
-        if (__popc(contend) == 1) {
-            winner = __ffs(contend) - 1;
-        } else if (contend) {
-            /* FP64 arbitration, exactly as check_normal! scores candidates in the FP64 path */
-            ++n_arb;
-            if (lane < 27) {
-                NbrGeom G;
-                nbr_geom(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9, G);
-                double full = 0.0;
-#pragma unroll
-                for (int t = 0; t < 5; ++t) {
-                    const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), e = tet5(t, 3);
-                    const double tv = tet_vol(G.X[a & 1], G.Y[(a >> 1) & 1], G.Z[a >> 2], G.X[b & 1],
-                                              G.Y[(b >> 1) & 1], G.Z[b >> 2], G.X[c & 1], G.Y[(c >> 1) & 1],
-                                              G.Z[c >> 2], G.X[e & 1], G.Y[(e >> 1) & 1], G.Z[e >> 2]);
-                    const double term = G.tetsign * tv / m.cellvol;
-                    s_term[w][lane][t] = term;
-                    full += term;
-                }
-                s_full[w][lane] = full;
-            }
-            __syncwarp();
-            NbrGeom G;
-            const int ql = lane < 27 ? lane : 26;
-            nbr_geom(m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, G);
-            double bestE = INFINITY;
-            for (unsigned mask = contend; mask; mask &= mask - 1) {
-                const int c = __ffs(mask) - 1;
-                double cx, cy, cz;
-                candidate64(m, s_vd[w], fam_on, c, i, j, k, cx, cy, cz);
-                const double dist = compute_dist64(m, i, j, k, cx, cy, cz, s_vd[w][13]);
-                const double v_ = m.tess == 5
-                                      ? plic2vf64(s_tab, G, s_term[w][ql], s_full[w][ql], cx, cy, cz, dist, m.cellvol, err)
-                                      : plic2vf64_gen(s_tab, m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, cx,
-                                                      cy, cz, dist, err);
-                const double r = s_vd[w][ql] - v_;
-                const double r2 = r * r;
-                double e2 = 0.0;
-                for (int q = 0; q < 27; ++q) e2 += __shfl_sync(0xffffffffu, r2, q);
-                if (e2 < bestE) { bestE = e2; winner = c; }
+        if (lane == 0) {
+            if (__popc(contend) <= 1) {
+                cand[cidx(m, i, j, k)] = (signed char)(contend ? __ffs(contend) - 1 : -1);
+            } else {
+                /* near-tie: the FP64 scoring pass decides */
+                const int slot = atomicAdd(n_arb, 1);
+                arb[slot] = make_int2(L, (int)contend);
             }
         }
-        /* the winner's FP64 normal is formed by k_elvira_winner64, all lanes busy */
-        if (lane == 0) cand[cidx(m, i, j, k)] = (signed char)(winner < 32 ? winner : -1);
         __syncwarp();
     }
-    if (lane == 0 && n_arb) atomicAdd(stats, n_arb);
+}
+
+/* FP64 arbitration of the near-ties, warp per cell: the contending candidates scored exactly as
+ * check_normal! scores them in the FP64 path (5-tet clips, lanes = neighbours, errors summed in
+ * neighbour order), the first strict minimum wins.  A separate pass keeps this FP64 code and
+ * its registers out of the FP32 scoring kernel, where it cost occupancy on every cell. */
+__global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_arb64(DevMesh m, const double* __restrict__ VF,
+                                                                  const int* __restrict__ n_arb,
+                                                                  const int2* __restrict__ arb,
+                                                                  signed char* __restrict__ cand, int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    __shared__ double s_vd[EL32_WARPS][27];
+    __shared__ double s_term[EL32_WARPS][27][5];
+    __shared__ double s_full[EL32_WARPS][27];
+    load_table(s_tab);
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
+    const int n = *n_arb;
+    int err = 0;
+    for (int item = blockIdx.x * EL32_WARPS + w; item < n; item += gridDim.x * EL32_WARPS) {
+        const int2 e = arb[item];
+        const int L = e.x;
+        const unsigned contend = (unsigned)e.y;
+        const int i = 1 + L % m.N[0];
+        const int j = 1 + (L / m.N[0]) % m.N[1];
+        const int k = 1 + L / (m.N[0] * m.N[1]);
+        if (lane < 27) {
+            s_vd[w][lane] = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
+            NbrGeom G;
+            nbr_geom(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9, G);
+            double full = 0.0;
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+                const int a = tet5(t, 0), b = tet5(t, 1), c = tet5(t, 2), ee = tet5(t, 3);
+                const double tv = tet_vol(G.X[a & 1], G.Y[(a >> 1) & 1], G.Z[a >> 2], G.X[b & 1], G.Y[(b >> 1) & 1],
+                                          G.Z[b >> 2], G.X[c & 1], G.Y[(c >> 1) & 1], G.Z[c >> 2], G.X[ee & 1],
+                                          G.Y[(ee >> 1) & 1], G.Z[ee >> 2]);
+                const double term = G.tetsign * tv / m.cellvol;
+                s_term[w][lane][t] = term;
+                full += term;
+            }
+            s_full[w][lane] = full;
+        }
+        __syncwarp();
+        NbrGeom G;
+        const int ql = lane < 27 ? lane : 26;
+        nbr_geom(m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, G);
+        double bestE = INFINITY;
+        int winner = -1;
+        for (unsigned mask = contend; mask; mask &= mask - 1) {
+            const int c = __ffs(mask) - 1;
+            double cx, cy, cz;
+            candidate64(m, s_vd[w], fam_on, c, i, j, k, cx, cy, cz);
+            const double dist = compute_dist64(m, i, j, k, cx, cy, cz, s_vd[w][13]);
+            const double v_ = m.tess == 5
+                                  ? plic2vf64(s_tab, G, s_term[w][ql], s_full[w][ql], cx, cy, cz, dist, m.cellvol, err)
+                                  : plic2vf64_gen(s_tab, m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, cx,
+                                                  cy, cz, dist, err);
+            const double r = s_vd[w][ql] - v_;
+            const double r2 = r * r;
+            double e2 = 0.0;
+            for (int q = 0; q < 27; ++q) e2 += __shfl_sync(0xffffffffu, r2, q);
+            if (e2 < bestE) { bestE = e2; winner = c; }
+        }
+        if (lane == 0) cand[cidx(m, i, j, k)] = (signed char)winner;
+        __syncwarp();
+    }
     if (err) atomicOr(errw, err);
 }
 
@@ -456,10 +470,11 @@ __global__ void k_elvira_winner64(DevMesh m, const double* __restrict__ VF, doub
 }
 
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int* stats, signed char* cand, int* errw, int nsm,
+                           const int* count, int* work, int* n_arb, int2* arb, signed char* cand, int* errw, int nsm,
                            cudaStream_t s)
 {
-    k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, nx, ny, nz, list, count, work, stats, cand, errw);
+    k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, list, count, work, n_arb, arb, cand);
+    k_elvira_arb64<<<nsm, EL32_WARPS * 32, 0, s>>>(m, VF, n_arb, arb, cand, errw);
     k_elvira_winner64<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, list, count, cand);
 }
 

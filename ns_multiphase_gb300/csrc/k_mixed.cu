@@ -737,10 +737,9 @@ void launch_sl32_clip(const DevMesh& m, double* VFout, const float4* planes, int
 
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
-                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, double2* tet_out, int* errw,
+                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, int* errw,
                  int nsm, cudaStream_t s)
 {
-    (void)tet_out;
     launch_sl32_pre(m, dt, VFout, uf, vf, wf, planes, phase, list, count, work, slow_cells, slow_verts, slow_count,
                     errw, nsm, s);
     launch_sl32_clip(m, VFout, planes, work2, slow_cells, slow_verts, slow_count, errw, nsm, s);

@@ -35,9 +35,9 @@ struct slvof_ctx {
     float *uf32 = nullptr, *vf32 = nullptr, *wf32 = nullptr;
     double *nx = nullptr, *ny = nullptr, *nz = nullptr, *D = nullptr;
     float4* planes = nullptr;     /* mixed: donor planes in cell units */
+    int2* arb = nullptr;          /* mixed ELVIRA: near-tie cells (cell, contending lanes) for FP64 scoring */
     int* slow_cells = nullptr;    /* mixed SL: cells that need the clip */
     float4* slow_verts = nullptr; /* mixed SL: their pre-image vertices (cell units) + packed indices */
-    double2* tet_out = nullptr;   /* mixed SL: (vol, vLiq) of each tet of each slow cell */
     signed char* phase = nullptr; /* pure-donor codes of the PLIC pass */
     signed char* cand = nullptr;  /* ELVIRA: chosen candidate lane of each interface cell */
     /* reverse pass (allocated on first use) */
@@ -167,7 +167,7 @@ int st_normals(slvof_ctx* c)
                               c->cand, c->ctr + C_ERR, c->nsm, c->stream);
     else
         launch_elvira_iface32(c->m, c->VF[c->vcur], c->nx, c->ny, c->nz, c->list_if, c->ctr + C_IF, c->ctr + C_IFW,
-                              c->ctr + C_ARB, c->cand, c->ctr + C_ERR, c->nsm, c->stream);
+                              c->ctr + C_ARB, c->arb, c->cand, c->ctr + C_ERR, c->nsm, c->stream);
     s_end(c, S_IFACE);
     s_beg(c, S_NGHOST);
     launch_normal_ghost(c->m, c->nx, c->ny, c->nz, c->nsm, c->stream);
@@ -218,7 +218,7 @@ int st_transport(slvof_ctx* c, double dt)
                     c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
     else
         launch_sl32(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
-                    c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->tet_out,
+                    c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW,
                     c->ctr + C_ERR, c->nsm, c->stream);
     s_end(c, S_SL);
     s_beg(c, S_VFGHOST);
@@ -377,7 +377,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
              alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4)) &&
              alloc((void**)&c->slow_cells, interior * sizeof(int)) &&
              alloc((void**)&c->slow_verts, interior * (mesh->tesselation == 24 ? 16 : 8) * sizeof(float4)) &&
-             alloc((void**)&c->tet_out, interior * 5 * sizeof(double2));
+             alloc((void**)&c->arb, interior * sizeof(int2));
     if (!ok) return bail(SLVOF_E_NOMEM);
     /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
     std::vector<double> h(ncoord);
@@ -407,7 +407,7 @@ int slvof_destroy(slvof_ctx* c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* bufs[] = {c->coords, c->VF[0], c->VF[1], c->uf, c->vf, c->wf, c->uf32, c->vf32, c->wf32, c->nx, c->ny,
                     c->nz, c->D, c->planes, c->phase, c->cand, c->band[0], c->band[1], c->list_sl, c->list_if,
-                    c->list_plic, c->slow_cells, c->slow_verts, c->tet_out, c->ctr, c->partials, c->mass_d, c->table,
+                    c->list_plic, c->slow_cells, c->slow_verts, c->arb, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
                     c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
                     c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo, c->gvel32[0], c->gvel32[1], c->gvel32[2],

@@ -52,8 +52,10 @@ void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const doub
                           const int* list, const int* count, int* work, int* errw, int nsm, cudaStream_t s);
 
 /* k_mixed.cu, k_elvira_mixed.cu */
+/* mixed ELVIRA: FP32 scoring (warp per cell), FP64 arbitration of the near-ties listed in arb
+ * (n_arb zeroed by the caller; capacity: the interface count), FP64 winner normals */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
-                           const int* count, int* work, int* stats, signed char* cand, int* errw, int nsm,
+                           const int* count, int* work, int* n_arb, int2* arb, signed char* cand, int* errw, int nsm,
                            cudaStream_t s);
 
 /* k_adj64.cu: reverse pass of one FP64 step (see adj64.cuh) */
@@ -127,7 +129,7 @@ void launch_sl32_clip(const DevMesh& m, double* VFout, const float4* planes, int
                       const float4* slow_verts, const int* slow_count, int* errw, int nsm, cudaStream_t s);
 void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                  const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
-                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, double2* tet_out, int* errw,
+                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, int* errw,
                  int nsm, cudaStream_t s);
 
 } // namespace slvof
