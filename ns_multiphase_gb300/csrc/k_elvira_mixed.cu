@@ -373,35 +373,41 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
     }
 }
 
-/* FP64 arbitration of the near-ties, warp per cell: the contending candidates scored exactly as
- * check_normal! scores them in the FP64 path (5-tet clips, lanes = neighbours, errors summed in
- * neighbour order), the first strict minimum wins.  A separate pass keeps this FP64 code and
- * its registers out of the FP32 scoring kernel, where it cost occupancy on every cell. */
-__global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_arb64(DevMesh m, const double* __restrict__ VF,
-                                                                  const int* __restrict__ n_arb,
-                                                                  const int2* __restrict__ arb,
-                                                                  signed char* __restrict__ cand, int* errw)
+/* FP64 arbitration of the near-ties: the contending candidates scored exactly as
+ * check_normal! scores them in the FP64 path (computeDist, 5-tet clips of the 27 neighbours,
+ * squared errors summed in neighbour order), the first strict minimum wins.  A block per cell,
+ * a thread per (candidate, neighbour) pair: the scoring's long FP64 chains run side by side
+ * instead of one contender after another in one warp.  A separate pass keeps this FP64 code and
+ * its registers out of the FP32 scoring kernel. */
+constexpr int ARB_THREADS = 256;
+
+__global__ void __launch_bounds__(ARB_THREADS) k_elvira_arb64(DevMesh m, const double* __restrict__ VF,
+                                                              const int* __restrict__ n_arb,
+                                                              const int2* __restrict__ arb,
+                                                              signed char* __restrict__ cand, int* errw)
 {
     __shared__ CutCase s_tab[16];
-    __shared__ double s_vd[EL32_WARPS][27];
-    __shared__ double s_term[EL32_WARPS][27][5];
-    __shared__ double s_full[EL32_WARPS][27];
+    __shared__ double s_vd[27], s_full[27], s_term[27][5];
+    __shared__ double s_n[27][3], s_dist[27];
+    __shared__ double s_r2[27][27];
+    __shared__ int s_c[27];
     load_table(s_tab);
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tid = threadIdx.x;
     const int fam_on[3] = {m.N[2] > 1, m.N[1] > 1, m.N[0] > 1};
     const int n = *n_arb;
     int err = 0;
-    for (int item = blockIdx.x * EL32_WARPS + w; item < n; item += gridDim.x * EL32_WARPS) {
+    for (int item = blockIdx.x; item < n; item += gridDim.x) {
         const int2 e = arb[item];
         const int L = e.x;
         const unsigned contend = (unsigned)e.y;
+        const int nc = __popc(contend);
         const int i = 1 + L % m.N[0];
         const int j = 1 + (L / m.N[0]) % m.N[1];
         const int k = 1 + L / (m.N[0] * m.N[1]);
-        if (lane < 27) {
-            s_vd[w][lane] = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
+        if (tid < 27) {
+            s_vd[tid] = VF[vidx(m, i - 1 + tid % 3, j - 1 + (tid / 3) % 3, k - 1 + tid / 9)];
             NbrGeom G;
-            nbr_geom(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9, G);
+            nbr_geom(m, i - 1 + tid % 3, j - 1 + (tid / 3) % 3, k - 1 + tid / 9, G);
             double full = 0.0;
 #pragma unroll
             for (int t = 0; t < 5; ++t) {
@@ -410,34 +416,50 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_arb64(DevMesh m, con
                                           G.Z[b >> 2], G.X[c & 1], G.Y[(c >> 1) & 1], G.Z[c >> 2], G.X[ee & 1],
                                           G.Y[(ee >> 1) & 1], G.Z[ee >> 2]);
                 const double term = G.tetsign * tv / m.cellvol;
-                s_term[w][lane][t] = term;
+                s_term[tid][t] = term;
                 full += term;
             }
-            s_full[w][lane] = full;
+            s_full[tid] = full;
+            /* the q-th contending lane, in lane order */
+            unsigned mask = contend;
+            for (int q = 0; q < tid && mask; ++q) mask &= mask - 1;
+            s_c[tid] = mask ? __ffs(mask) - 1 : -1;
         }
-        __syncwarp();
-        NbrGeom G;
-        const int ql = lane < 27 ? lane : 26;
-        nbr_geom(m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, G);
-        double bestE = INFINITY;
-        int winner = -1;
-        for (unsigned mask = contend; mask; mask &= mask - 1) {
-            const int c = __ffs(mask) - 1;
+        __syncthreads();
+        if (tid < nc) {
             double cx, cy, cz;
-            candidate64(m, s_vd[w], fam_on, c, i, j, k, cx, cy, cz);
-            const double dist = compute_dist64(m, i, j, k, cx, cy, cz, s_vd[w][13]);
-            const double v_ = m.tess == 5
-                                  ? plic2vf64(s_tab, G, s_term[w][ql], s_full[w][ql], cx, cy, cz, dist, m.cellvol, err)
-                                  : plic2vf64_gen(s_tab, m, i - 1 + ql % 3, j - 1 + (ql / 3) % 3, k - 1 + ql / 9, cx,
-                                                  cy, cz, dist, err);
-            const double r = s_vd[w][ql] - v_;
-            const double r2 = r * r;
-            double e2 = 0.0;
-            for (int q = 0; q < 27; ++q) e2 += __shfl_sync(0xffffffffu, r2, q);
-            if (e2 < bestE) { bestE = e2; winner = c; }
+            candidate64(m, s_vd, fam_on, s_c[tid], i, j, k, cx, cy, cz);
+            s_n[tid][0] = cx; s_n[tid][1] = cy; s_n[tid][2] = cz;
+            s_dist[tid] = compute_dist64(m, i, j, k, cx, cy, cz, s_vd[13]);
         }
-        if (lane == 0) cand[cidx(m, i, j, k)] = (signed char)winner;
-        __syncwarp();
+        __syncthreads();
+        for (int pq = tid; pq < nc * 27; pq += ARB_THREADS) {
+            const int c = pq / 27, q = pq - 27 * c;
+            const int ii = i - 1 + q % 3, jj = j - 1 + (q / 3) % 3, kk = k - 1 + q / 9;
+            double v_;
+            if (m.tess == 5) {
+                NbrGeom G;
+                nbr_geom(m, ii, jj, kk, G);
+                v_ = plic2vf64(s_tab, G, s_term[q], s_full[q], s_n[c][0], s_n[c][1], s_n[c][2], s_dist[c], m.cellvol,
+                               err);
+            } else {
+                v_ = plic2vf64_gen(s_tab, m, ii, jj, kk, s_n[c][0], s_n[c][1], s_n[c][2], s_dist[c], err);
+            }
+            const double r = s_vd[q] - v_;
+            s_r2[c][q] = r * r;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double bestE = INFINITY;
+            int winner = -1;
+            for (int c = 0; c < nc; ++c) {
+                double e2 = 0.0;
+                for (int q = 0; q < 27; ++q) e2 += s_r2[c][q];
+                if (e2 < bestE) { bestE = e2; winner = s_c[c]; }
+            }
+            cand[cidx(m, i, j, k)] = (signed char)winner;
+        }
+        __syncthreads();
     }
     if (err) atomicOr(errw, err);
 }
@@ -474,7 +496,7 @@ void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, doubl
                            cudaStream_t s)
 {
     k_elvira_iface32<<<nsm * 4, EL32_WARPS * 32, 0, s>>>(m, VF, list, count, work, n_arb, arb, cand);
-    k_elvira_arb64<<<nsm, EL32_WARPS * 32, 0, s>>>(m, VF, n_arb, arb, cand, errw);
+    k_elvira_arb64<<<nsm * 8, ARB_THREADS, 0, s>>>(m, VF, n_arb, arb, cand, errw);
     k_elvira_winner64<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, list, count, cand);
 }
 
