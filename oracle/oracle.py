@@ -59,6 +59,10 @@ def lib():
         L.orc_sl_flux_vol.argtypes = [p, i, i, i, i, p, p, p, d]
         L.orc_divergence.restype = i
         L.orc_divergence.argtypes = [p, d, i, p, p, p, p, p]
+        L.orc_ndual.restype = i
+        L.orc_ndual.argtypes = []
+        L.orc_sl_forward.restype = i
+        L.orc_sl_forward.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p, p, p]
         L.orc_curvature.restype = i
         L.orc_curvature.argtypes = [p, p, p, p, p, p]
         L.orc_props.restype = i
@@ -168,6 +172,28 @@ class Oracle:
         self.L.orc_A(_m(m), dt, scheme, _p(LHS), _p(P), _p(uf), _p(vf), _p(wf), _p(denx), _p(deny), _p(denz),
                      _p(band), _p(gx), _p(gy), _p(gz))
         return LHS, gx, gy, gz
+
+    def sl_forward(self, dt, cells, uf, vf, wf, seeds, nx, ny, nz, D):
+        """Forward-mode derivatives of the SL update (Dual numbers through the restatement):
+        cells is a list of (i, j, k); seeds a list of up to ndual() (array 0/1/2, parent index)
+        face entries.  Returns (VFnew per cell, d VFnew / d seed, shape (cells, seeds))."""
+        m = self.mesh
+        K = self.L.orc_ndual()
+        assert len(seeds) <= K
+        slots = [np.full(m.cell_shape, -1, dtype=np.int32, order="F") for _ in range(3)]
+        for s, (a, idx) in enumerate(seeds):
+            slots[a][idx] = s
+        cl = np.ascontiguousarray(np.asarray(cells, dtype=np.int32).reshape(-1, 3))
+        out = np.zeros(len(cl))
+        grad = np.zeros((len(cl), K))
+        f = self.L.orc_sl_forward(_m(m), dt, len(cl), cl.ctypes.data, _p(uf), _p(vf), _p(wf), *[_p(x) for x in slots],
+                                  _p(nx), _p(ny), _p(nz), _p(D), out.ctypes.data, grad.ctypes.data)
+        if f:
+            raise RuntimeError(f"restatement flags {f}")
+        return out, grad[:, :len(seeds)]
+
+    def ndual(self):
+        return self.L.orc_ndual()
 
     def curvature(self, VF, nx, ny, nz):
         """transport!'s curvature section (src/Transport.jl:187-191, compute_curvature!)."""

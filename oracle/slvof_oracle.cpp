@@ -53,12 +53,53 @@ namespace {
 
 const double EPS = 2.220446049250313e-16; /* Julia eps() */
 
+/* Forward-mode dual numbers for the derivative checks: the SL path below is written for a
+ * generic scalar, instantiated with double (the restatement) and with Dual (value plus K
+ * directional derivatives, the CPU analogue of ForwardDiff.jl's Dual).  Branches and
+ * comparisons use the value; the double instantiation is the plain restatement. */
+constexpr int NDUAL = 16;
+struct Dual {
+    double v = 0.0;
+    double d[NDUAL] = {};
+    Dual() = default;
+    Dual(double x) : v(x) {}
+};
+inline Dual operator+(const Dual& a, const Dual& b) { Dual r(a.v + b.v); for (int q = 0; q < NDUAL; ++q) r.d[q] = a.d[q] + b.d[q]; return r; }
+inline Dual operator-(const Dual& a, const Dual& b) { Dual r(a.v - b.v); for (int q = 0; q < NDUAL; ++q) r.d[q] = a.d[q] - b.d[q]; return r; }
+inline Dual operator-(const Dual& a) { Dual r(-a.v); for (int q = 0; q < NDUAL; ++q) r.d[q] = -a.d[q]; return r; }
+inline Dual operator*(const Dual& a, const Dual& b)
+{
+    Dual r(a.v * b.v);
+    for (int q = 0; q < NDUAL; ++q) r.d[q] = a.d[q] * b.v + a.v * b.d[q];
+    return r;
+}
+inline Dual operator/(const Dual& a, const Dual& b)
+{
+    Dual r(a.v / b.v);
+    for (int q = 0; q < NDUAL; ++q) r.d[q] = (a.d[q] * b.v - a.v * b.d[q]) / (b.v * b.v);
+    return r;
+}
+inline Dual& operator+=(Dual& a, const Dual& b) { a = a + b; return a; }
+inline double val(double x) { return x; }
+inline double val(const Dual& x) { return x.v; }
+
 /* Julia min/max on Float64: NaN-propagating. */
-inline double jmax(double a, double b) { return (a != a || b != b) ? NAN : (a > b ? a : (b > a ? b : (std::signbit(a) ? b : a))); }
-inline double jmin(double a, double b) { return (a != a || b != b) ? NAN : (a < b ? a : (b < a ? b : (std::signbit(a) ? a : b))); }
+template <class R>
+inline R jmax(const R& a, const R& b)
+{
+    const double x = val(a), y = val(b);
+    return (x != x || y != y) ? R(NAN) : (x > y ? a : (y > x ? b : (std::signbit(x) ? b : a)));
+}
+template <class R>
+inline R jmin(const R& a, const R& b)
+{
+    const double x = val(a), y = val(b);
+    return (x != x || y != y) ? R(NAN) : (x < y ? a : (y < x ? b : (std::signbit(x) ? a : b)));
+}
 
 /* /̂  (src/Tools.jl:375-377) */
-inline double sdiv(double a, double b) { return std::fabs(b) <= EPS ? INFINITY : a / b; }
+template <class R>
+inline R sdiv(const R& a, const R& b) { return std::fabs(val(b)) <= EPS ? R(INFINITY) : a / b; }
 
 struct Grid {
     const orc_mesh* m;
@@ -155,17 +196,18 @@ inline void tess_tet(int tess, int t, int out[4])
 }
 /* mean(eachcol(p)) as Julia's Statistics.mean computes it: the vectors summed in order, then
  * divided by their count. */
-inline void tess_points(int tess, double pts[15][3])
+template <class R>
+inline void tess_points(int tess, R pts[15][3])
 {
     if (tess != 24) return;
     for (int p = 0; p < 3; ++p) {
-        double s = pts[0][p];
+        R s = pts[0][p];
         for (int n = 1; n < 8; ++n) s = s + pts[n][p];
         pts[8][p] = s / 8.0;
     }
     for (int f = 0; f < 6; ++f)
         for (int p = 0; p < 3; ++p) {
-            double s = pts[FACE24[f][0] - 1][p];
+            R s = pts[FACE24[f][0] - 1][p];
             for (int n = 1; n < 4; ++n) s = s + pts[FACE24[f][n] - 1][p];
             pts[9 + f][p] = s / 4.0;
         }
@@ -176,12 +218,13 @@ struct Err { int flags = 0; };
 enum { E_INDEX = 1, E_DEPTH = 2, E_NAN = 4, E_VOLUME = 8 };
 
 /* tet_vol, src/VFgeom.jl:669-681.  v[vertex][coord]. */
-inline double tet_vol(const double v[4][3])
+template <class R>
+inline R tet_vol(const R v[4][3])
 {
-    const double a1 = v[0][0] - v[3][0], a2 = v[0][1] - v[3][1], a3 = v[0][2] - v[3][2];
-    const double b1 = v[1][0] - v[3][0], b2 = v[1][1] - v[3][1], b3 = v[1][2] - v[3][2];
-    const double c1 = v[2][0] - v[3][0], c2 = v[2][1] - v[3][1], c3 = v[2][2] - v[3][2];
-    return -1.0 / 6.0 * ((a1 * (b2 * c3 - c2 * b3) - a2 * (b1 * c3 - c1 * b3)) + a3 * (b1 * c2 - c1 * b2));
+    const R a1 = v[0][0] - v[3][0], a2 = v[0][1] - v[3][1], a3 = v[0][2] - v[3][2];
+    const R b1 = v[1][0] - v[3][0], b2 = v[1][1] - v[3][1], b3 = v[1][2] - v[3][2];
+    const R c1 = v[2][0] - v[3][0], c2 = v[2][1] - v[3][1], c3 = v[2][2] - v[3][2];
+    return R(-1.0 / 6.0) * ((a1 * (b2 * c3 - c2 * b3) - a2 * (b1 * c3 - c1 * b3)) + a3 * (b1 * c2 - c1 * b2));
 }
 
 /* d2case, src/VFgeom.jl:693-708.  Modifies d (callers pass a copy where the reference does). */
@@ -199,7 +242,8 @@ inline int d2case(double d[4], Err* err)
     return c;
 }
 
-inline double clamp_mu(double q) { return jmin(1.0, jmax(0.0, q)); }
+template <class R>
+inline R clamp_mu(const R& q) { return jmin(R(1.0), jmax(R(0.0), q)); }
 
 /* oddEvenCell + cell2verts!, src/VFgeom.jl:171-216: only 5_tets mirrors odd cells.
  * verts[vertex][coord]. */
@@ -488,39 +532,57 @@ void elvira_cell(const Grid& G, const Fields& F, double* nx, double* ny, double*
 /* ---------------------------------------------------------------------------------------
  * Velocity interpolation and projection, src/Tools.jl:392-641.
  * ------------------------------------------------------------------------------------- */
-struct Vel { const double *uf, *vf, *wf; };
+struct Vel {
+    const double *uf, *vf, *wf;
+    const int *su = nullptr, *sv = nullptr, *sw = nullptr; /* Dual: derivative slot of each face value, -1 none */
+};
+
+template <class R>
+inline R fetch(const double* f, const int* seed, long t);
+template <>
+inline double fetch<double>(const double* f, const int*, long t) { return f[t]; }
+template <>
+inline Dual fetch<Dual>(const double* f, const int* seed, long t)
+{
+    Dual r(f[t]);
+    if (seed && seed[t] >= 0) r.d[seed[t]] = 1.0;
+    return r;
+}
 
 /* get_velocity_{u,v,w}face: stag = which direction uses face coordinates. */
-double interp_face(const Grid& G, const double* f, int stag, const double pt[3], int i, int j, int k)
+template <class R>
+R interp_face(const Grid& G, const double* f, const int* seed, int stag, const R pt[3], int i, int j, int k)
 {
     int I[3] = {i, j, k};
     for (int d = 0; d < 3; ++d) {
         auto co = [&](int q) { return d == stag ? G.fc(d, q) : (d == 0 ? G.xm(q) : (d == 1 ? G.ym(q) : G.zm(q))); };
-        while (pt[d] - co(I[d]) < 0.0 && I[d] > G.lo[d]) I[d] = I[d] - 1;
-        while (pt[d] - co(I[d] + 1) >= 0.0 && I[d] + 1 < G.hi[d]) I[d] = I[d] + 1;
+        while (val(pt[d]) - co(I[d]) < 0.0 && I[d] > G.lo[d]) I[d] = I[d] - 1;
+        while (val(pt[d]) - co(I[d] + 1) >= 0.0 && I[d] + 1 < G.hi[d]) I[d] = I[d] + 1;
     }
-    double w1[3], w2[3];
+    R w1[3], w2[3];
     for (int d = 0; d < 3; ++d) {
         auto co = [&](int q) { return d == stag ? G.fc(d, q) : (d == 0 ? G.xm(q) : (d == 1 ? G.ym(q) : G.zm(q))); };
-        w1[d] = sdiv(pt[d] - co(I[d]), co(I[d] + 1) - co(I[d]));
-        w2[d] = 1.0 - w1[d];
+        w1[d] = sdiv<R>(pt[d] - co(I[d]), R(co(I[d] + 1) - co(I[d])));
+        w2[d] = R(1.0) - w1[d];
     }
     const int a = I[0], b = I[1], c = I[2];
-    auto F = [&](int ii, int jj, int kk) { return f[G.c(ii, jj, kk)]; };
+    auto F = [&](int ii, int jj, int kk) { return fetch<R>(f, seed, G.c(ii, jj, kk)); };
     return w1[2] * (w1[1] * (w1[0] * F(a + 1, b + 1, c + 1) + w2[0] * F(a, b + 1, c + 1)) +
                     w2[1] * (w1[0] * F(a + 1, b, c + 1) + w2[0] * F(a, b, c + 1))) +
            w2[2] * (w1[1] * (w1[0] * F(a + 1, b + 1, c) + w2[0] * F(a, b + 1, c)) +
                     w2[1] * (w1[0] * F(a + 1, b, c) + w2[0] * F(a, b, c)));
 }
 
-void velocity(const Grid& G, const Vel& V, const double pt[3], int i, int j, int k, double out[3])
+template <class R>
+void velocity(const Grid& G, const Vel& V, const R pt[3], int i, int j, int k, R out[3])
 {
-    out[0] = interp_face(G, V.uf, 0, pt, i, j, k);
-    out[1] = interp_face(G, V.vf, 1, pt, i, j, k);
-    out[2] = interp_face(G, V.wf, 2, pt, i, j, k);
+    out[0] = interp_face<R>(G, V.uf, V.su, 0, pt, i, j, k);
+    out[1] = interp_face<R>(G, V.vf, V.sv, 1, pt, i, j, k);
+    out[2] = interp_face<R>(G, V.wf, V.sw, 2, pt, i, j, k);
 }
 
-void project(const Grid& G, const Vel& V, double pt[3], int i, int j, int k, double dt)
+template <class R>
+void project(const Grid& G, const Vel& V, R pt[3], int i, int j, int k, double dt)
 {
     const int method = G.m->projection;
     if (method == 3) {
@@ -528,13 +590,13 @@ void project(const Grid& G, const Vel& V, double pt[3], int i, int j, int k, dou
          * 2*pi in Float64 is 2.0*pi exactly */
         const double a = 6.283185307179586 * dt;
         const double c = detm_cos(a), s = detm_sin(a);
-        const double x0 = pt[0], y0 = pt[1];
+        const R x0 = pt[0], y0 = pt[1];
         pt[0] = (0.5 + c * (x0 - 0.5)) + s * (y0 - 0.5);
         pt[1] = (0.5 - s * (x0 - 0.5)) + c * (y0 - 0.5);
         return;
     }
     if (method == 2) {
-        double v1[3], v2[3], v3[3], v4[3], p[3];
+        R v1[3], v2[3], v3[3], v4[3], p[3];
         velocity(G, V, pt, i, j, k, v1);
         for (int d = 0; d < 3; ++d) p[d] = pt[d] - 0.5 * dt * v1[d];
         velocity(G, V, p, i, j, k, v2);
@@ -544,11 +606,11 @@ void project(const Grid& G, const Vel& V, double pt[3], int i, int j, int k, dou
         velocity(G, V, p, i, j, k, v4);
         for (int d = 0; d < 3; ++d) pt[d] = pt[d] + (-dt) / 6.0 * (((v1[d] + 2.0 * v2[d]) + 2.0 * v3[d]) + v4[d]);
     } else if (method == 0) {
-        double v1[3];
+        R v1[3];
         velocity(G, V, pt, i, j, k, v1);
         for (int d = 0; d < 3; ++d) pt[d] = pt[d] + (-dt) * v1[d];
     } else {
-        double v1[3], v2[3], p[3];
+        R v1[3], v2[3], p[3];
         velocity(G, V, pt, i, j, k, v1);
         for (int d = 0; d < 3; ++d) p[d] = pt[d] - 0.5 * dt * v1[d];
         velocity(G, V, p, i, j, k, v2);
@@ -573,6 +635,12 @@ void pt2index(const Grid& G, int I[3], const double pt[3], int i, int j, int k, 
     }
 }
 
+inline void pt2index(const Grid& G, int I[3], const Dual pt[3], int i, int j, int k, Err* e)
+{
+    const double p[3] = {pt[0].v, pt[1].v, pt[2].v};
+    pt2index(G, I, p, i, j, k, e);
+}
+
 /* ---------------------------------------------------------------------------------------
  * cutTet, src/VFgeom.jl:713-900, kept recursive as in the reference.
  * ------------------------------------------------------------------------------------- */
@@ -580,14 +648,17 @@ struct Plic { const double *nx, *ny, *nz, *D; };
 /* cell-centred velocities and densities for the momentum sums of transport! (may be absent) */
 struct Mom { const double *u, *v, *w; double rho_liq, rho_gas; };
 
-struct CutOut { double vol, vLiq, vrhoU, vrhoV, vrhoW, vrho; };
+template <class R>
+struct CutOutT { R vol, vLiq, vrhoU, vrhoV, vrhoW, vrho; };
+using CutOut = CutOutT<double>;
 
-CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int ind[4][3], bool xdone, bool ydone,
+template <class R>
+CutOutT<R> cut_tet(const Grid& G, const Plic& P, const Mom* M, R tet[4][3], int ind[4][3], bool xdone, bool ydone,
                bool zdone, int lvl, Err* e)
 {
-    if (lvl > 64) { e->flags |= E_DEPTH; return {0.0, 0.0, 0.0, 0.0, 0.0, 0.0}; }
+    if (lvl > 64) { e->flags |= E_DEPTH; return {R(0.0), R(0.0), R(0.0), R(0.0), R(0.0), R(0.0)}; }
     int dir = -1, cut_ind = 0;
-    double d[4];
+    R d[4];
     for (;;) {
         bool* done[3] = {&xdone, &ydone, &zdone};
         int q = -1;
@@ -605,26 +676,26 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
     }
     if (dir < 0) {
         /* Leaf: clip by the donor cell's PLIC plane (src/VFgeom.jl:757-830). */
-        double vert[8][3];
+        R vert[8][3];
         for (int n = 0; n < 4; ++n)
             for (int p = 0; p < 3; ++p) vert[n][p] = tet[n][p];
         const int i = ind[0][0], j = ind[0][1], k = ind[0][2];
         const long c = G.c(i, j, k);
         for (int n = 0; n < 4; ++n) d[n] = ((P.nx[c] * vert[n][0] + P.ny[c] * vert[n][1]) + P.nz[c] * vert[n][2]) - P.D[c];
-        double dc[4] = {d[0], d[1], d[2], d[3]};
+        double dc[4] = {val(d[0]), val(d[1]), val(d[2]), val(d[3])};
         const int cs = d2case(dc, e) - 1;
         for (int n = 0; n < T_NVERT[cs]; ++n) {
             const int v1 = T_V1[cs][n] - 1, v2 = T_V2[cs][n] - 1;
-            const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
-            for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
+            const R mu = clamp_mu(sdiv<R>(-d[v1], d[v2] - d[v1]));
+            for (int p = 0; p < 3; ++p) vert[4 + n][p] = (R(1.0) - mu) * vert[v1][p] + mu * vert[v2][p];
         }
-        CutOut r{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        CutOutT<R> r{R(0.0), R(0.0), R(0.0), R(0.0), R(0.0), R(0.0)};
         const double uc = M ? M->u[c] : 0.0, vc = M ? M->v[c] : 0.0, wc = M ? M->w[c] : 0.0;
         for (int n = T_NTETS[cs]; n >= T_NNTET[cs]; --n) {
-            double nt[4][3];
+            R nt[4][3];
             for (int t = 0; t < 4; ++t)
                 for (int p = 0; p < 3; ++p) nt[t][p] = vert[T_VTET[cs][n - 1][t] - 1][p];
-            const double tv = tet_vol(nt);
+            const R tv = tet_vol(nt);
             r.vol += tv;
             r.vLiq += tv;
             if (M) {
@@ -635,10 +706,10 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
             }
         }
         for (int n = 1; n <= T_NNTET[cs] - 1; ++n) {
-            double nt[4][3];
+            R nt[4][3];
             for (int t = 0; t < 4; ++t)
                 for (int p = 0; p < 3; ++p) nt[t][p] = vert[T_VTET[cs][n - 1][t] - 1][p];
-            const double tv = tet_vol(nt);
+            const R tv = tet_vol(nt);
             r.vol += tv;
             if (M) {
                 r.vrhoU += tv * uc * M->rho_gas;
@@ -650,9 +721,9 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
         return r;
     }
     /* Cut by the mesh plane (src/VFgeom.jl:832-899). */
-    double dc[4] = {d[0], d[1], d[2], d[3]};
+    double dc[4] = {val(d[0]), val(d[1]), val(d[2]), val(d[3])};
     const int cs = d2case(dc, e) - 1;
-    double vert[8][3];
+    R vert[8][3];
     int vind[8][3][2];
     for (int n = 0; n < 4; ++n) {
         for (int p = 0; p < 3; ++p) {
@@ -665,8 +736,8 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
     }
     for (int n = 0; n < T_NVERT[cs]; ++n) {
         const int v1 = T_V1[cs][n] - 1, v2 = T_V2[cs][n] - 1;
-        const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
-        for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
+        const R mu = clamp_mu(sdiv<R>(-d[v1], d[v2] - d[v1]));
+        for (int p = 0; p < 3; ++p) vert[4 + n][p] = (R(1.0) - mu) * vert[v1][p] + mu * vert[v2][p];
         /* seed: side-1 index of vertex n (src/VFgeom.jl:854-857) */
         int I[3];
         pt2index(G, I, vert[4 + n], vind[n][0][0], vind[n][1][0], vind[n][2][0], e);
@@ -680,9 +751,9 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
         vind[4 + n][dir][0] = cut_ind - 1;
         vind[4 + n][dir][1] = cut_ind;
     }
-    CutOut acc{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    CutOutT<R> acc{R(0.0), R(0.0), R(0.0), R(0.0), R(0.0), R(0.0)};
     for (int n = 0; n < T_NTETS[cs]; ++n) {
-        double ct[4][3];
+        R ct[4][3];
         int ci[4][3];
         const int side = T_SIDE[cs][n] - 1;
         for (int nn = 0; nn < 4; ++nn) {
@@ -692,7 +763,7 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
                 ci[nn][p] = vind[vt][p][side];
             }
         }
-        const CutOut r = cut_tet(G, P, M, ct, ci, xdone, ydone, zdone, lvl + 1, e);
+        const CutOutT<R> r = cut_tet<R>(G, P, M, ct, ci, xdone, ydone, zdone, lvl + 1, e);
         acc.vol += r.vol;
         acc.vLiq += r.vLiq;
         acc.vrhoU += r.vrhoU;
@@ -703,24 +774,29 @@ CutOut cut_tet(const Grid& G, const Plic& P, const Mom* M, double tet[4][3], int
     return acc;
 }
 
-void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt, double tets[12][4][3]);
+template <class R>
+void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt, R tets[12][4][3]);
 
 /* SL update of one cell, src/Transport.jl:111-148 with cell2tets!(project_verts=true,
  * compute_indices=true) (src/VFgeom.jl:345-420). Returns VFnew. */
-double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out,
-               const Mom* M = nullptr, double* mom_out = nullptr)
+template <class R = double>
+R sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out,
+          const Mom* M = nullptr, double* mom_out = nullptr)
 {
-    double verts[15][3];
-    const double tetsign = cell2verts(G, i, j, k, verts);
+    double v0[15][3];
+    const double tetsign = cell2verts(G, i, j, k, v0);
+    R verts[15][3];
+    for (int n = 0; n < 8; ++n)
+        for (int p = 0; p < 3; ++p) verts[n][p] = v0[n][p];
     for (int n = 0; n < 8; ++n) project(G, V, verts[n], i, j, k, dt);
     /* 24_tets: mean points of the projected vertices, their cells seeded at the cell
      * (verts2tets! inside cell2tets!, src/VFgeom.jl:283-330,402-406) */
     tess_points(G.tess, verts);
     int vInds[15][3];
     for (int n = 0; n < tess_npoints(G.tess); ++n) pt2index(G, vInds[n], verts[n], i, j, k, e);
-    double vol = 0.0, vLiq = 0.0, vrhoU = 0.0, vrhoV = 0.0, vrhoW = 0.0, vrho = 0.0;
+    R vol(0.0), vLiq(0.0), vrhoU(0.0), vrhoV(0.0), vrhoW(0.0), vrho(0.0);
     for (int t = 0; t < tess_ntets(G.tess); ++t) {
-        double tet[4][3];
+        R tet[4][3];
         int ind[4][3];
         int tv[4];
         tess_tet(G.tess, t, tv);
@@ -729,7 +805,7 @@ double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int
                 tet[n][p] = verts[tv[n]][p];
                 ind[n][p] = vInds[tv[n]][p];
             }
-        const CutOut r = cut_tet(G, P, M, tet, ind, false, false, false, 1, e);
+        const CutOutT<R> r = cut_tet<R>(G, P, M, tet, ind, false, false, false, 1, e);
         vol += tetsign * r.vol;
         vLiq += tetsign * r.vLiq;
         vrhoU += tetsign * r.vrhoU;
@@ -740,12 +816,12 @@ double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int
     if (G.m->pressure_scheme == 1) {
         /* pressure_scheme "finite-difference": the flux-correction tets, their vertices' cells
          * by pt2index! seeded at the cell (src/Transport.jl:121-124, src/VFgeom.jl:654-661) */
-        double ct[12][4][3];
-        correction_tets(G, V, i, j, k, dt, ct);
+        R ct[12][4][3];
+        correction_tets<R>(G, V, i, j, k, dt, ct);
         for (int t = 0; t < 12; ++t) {
             int ind[4][3];
             for (int n = 0; n < 4; ++n) pt2index(G, ind[n], ct[t][n], i, j, k, e);
-            const CutOut r = cut_tet(G, P, M, ct[t], ind, false, false, false, 1, e);
+            const CutOutT<R> r = cut_tet<R>(G, P, M, ct[t], ind, false, false, false, 1, e);
             vol += tetsign * r.vol;
             vLiq += tetsign * r.vLiq;
             vrhoU += tetsign * r.vrhoU;
@@ -754,10 +830,14 @@ double sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int
             vrho += tetsign * r.vrho;
         }
     }
-    if (!(vol > 0.0) || !std::isfinite(vol)) e->flags |= E_VOLUME;
-    if (vol_out) *vol_out = vol;
+    if (!(val(vol) > 0.0) || !std::isfinite(val(vol))) e->flags |= E_VOLUME;
+    if (vol_out) *vol_out = val(vol);
     /* us, vs, ws of the cell (src/Transport.jl:146-148) */
-    if (mom_out) { mom_out[0] = vrhoU / vrho; mom_out[1] = vrhoV / vrho; mom_out[2] = vrhoW / vrho; }
+    if (mom_out) {
+        mom_out[0] = val(vrhoU / vrho);
+        mom_out[1] = val(vrhoV / vrho);
+        mom_out[2] = val(vrhoW / vrho);
+    }
     return vLiq / vol;
 }
 
@@ -775,7 +855,8 @@ const int FLUXV[3][2][8][4] = {
      {{1, 0, 0, 1}, {0, 0, 0, 1}, {1, 1, 0, 1}, {0, 1, 0, 1}, {1, 0, 0, 0}, {0, 0, 0, 0}, {1, 1, 0, 0}, {0, 1, 0, 0}}}};
 
 /* SLfluxVol's vertices (tessellation order, mean points for 24_tets) and signed volume. */
-double sl_flux_verts(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt, double verts[15][3])
+template <class R>
+R sl_flux_verts(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt, R verts[15][3])
 {
     const bool even = G.tess != 5 || ((i + j + k) % 2) == 0;
     const double tetsign = even ? 1.0 : -1.0;
@@ -784,25 +865,25 @@ double sl_flux_verts(const Grid& G, const Vel& V, int dir, int i, int j, int k, 
         verts[n][0] = G.x(i + f[0]);
         verts[n][1] = G.y(j + f[1]);
         verts[n][2] = G.z(k + f[2]);
-        if (f[3]) project(G, V, verts[n], i, j, k, dt);
+        if (f[3]) project<R>(G, V, verts[n], i, j, k, dt);
     }
     tess_points(G.tess, verts);
-    double vol = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+    R vol(0.0); /* tets_vol, src/VFgeom.jl:683-689 */
     for (int t = 0; t < tess_ntets(G.tess); ++t) {
         int tv[4];
         tess_tet(G.tess, t, tv);
-        double tet[4][3];
+        R tet[4][3];
         for (int n = 0; n < 4; ++n)
             for (int p = 0; p < 3; ++p) tet[n][p] = verts[tv[n]][p];
         vol += tet_vol(tet);
     }
-    return vol * tetsign;
+    return vol * R(tetsign);
 }
 
 double sl_flux_vol(const Grid& G, const Vel& V, int dir, int i, int j, int k, double dt)
 {
     double verts[15][3];
-    return sl_flux_verts(G, V, dir, i, j, k, dt, verts);
+    return sl_flux_verts<double>(G, V, dir, i, j, k, dt, verts);
 }
 
 /* Apex of add_correction_tets' tets (a,b,d,e) and (b,c,d,e) over a face quad a,b,c,d
@@ -811,43 +892,45 @@ double sl_flux_vol(const Grid& G, const Vel& V, int dir, int i, int j, int k, do
  * gradient (a x b + d x a + b x c + c x d)/6, so the coordinate moves by
  * 6 (vol - V(mean)) / that gradient's component.  (The reference writes the same solution as
  * one expanded polynomial, which rounds differently.) */
-void correction_apex(int axis, const double* a, const double* b, const double* c, const double* d, double vol,
-                     double e[3])
+template <class R>
+void correction_apex(int axis, const R* a, const R* b, const R* c, const R* d, const R& vol, R e[3])
 {
-    for (int p = 0; p < 3; ++p) e[p] = 0.25 * (((a[p] + b[p]) + c[p]) + d[p]);
-    double t1[4][3], t2[4][3];
+    for (int p = 0; p < 3; ++p) e[p] = R(0.25) * (((a[p] + b[p]) + c[p]) + d[p]);
+    R t1[4][3], t2[4][3];
     for (int p = 0; p < 3; ++p) {
         t1[0][p] = a[p]; t1[1][p] = b[p]; t1[2][p] = d[p]; t1[3][p] = e[p];
         t2[0][p] = b[p]; t2[1][p] = c[p]; t2[2][p] = d[p]; t2[3][p] = e[p];
     }
-    const double v0 = tet_vol(t1) + tet_vol(t2);
+    const R v0 = tet_vol(t1) + tet_vol(t2);
     const int p = (axis + 1) % 3, q = (axis + 2) % 3; /* (u x w)_axis = u_p w_q - u_q w_p */
-    auto cr = [&](const double* u, const double* w) { return u[p] * w[q] - u[q] * w[p]; };
-    const double N = ((cr(a, b) + cr(d, a)) + cr(b, c)) + cr(c, d);
-    e[axis] += 6.0 * (vol - v0) / N;
+    auto cr = [&](const R* u, const R* w) { return u[p] * w[q] - u[q] * w[p]; };
+    const R N = ((cr(a, b) + cr(d, a)) + cr(b, c)) + cr(c, d);
+    e[axis] = e[axis] + R(6.0) * (vol - v0) / N;
 }
 
 /* add_correction_tets (src/VFgeom.jl:514-664), 5_tets: two tets on each face of cell (i,j,k),
  * faces x-, x+, y-, y+, z-, z+, built on the face's SLfluxVol vertices so that the face's flux
  * volume becomes the finite-difference one, dt * area * face velocity. */
-void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt, double tets[12][4][3])
+template <class R>
+void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt, R tets[12][4][3])
 {
     const orc_mesh* M = G.m;
     static const int QUAD[3][2][4] = {{{4, 6, 2, 0}, {7, 5, 1, 3}}, {{1, 5, 4, 0}, {1, 5, 4, 0}}, {{1, 0, 2, 3}, {1, 0, 2, 3}}};
     for (int f = 0; f < 6; ++f) {
         const int dir = f / 2, up = f & 1;
         const int fi = i + (dir == 0 ? up : 0), fj = j + (dir == 1 ? up : 0), fk = k + (dir == 2 ? up : 0);
-        double fv[15][3];
-        const double flux_vol = sl_flux_verts(G, V, dir, fi, fj, fk, dt, fv);
+        R fv[15][3];
+        const R flux_vol = sl_flux_verts<R>(G, V, dir, fi, fj, fk, dt, fv);
         const long t = G.c(fi, fj, fk);
-        const double divg_vol = dir == 0 ? ((dt * M->dy) * M->dz) * V.uf[t]
-                                         : (dir == 1 ? ((dt * M->dx) * M->dz) * V.vf[t] : ((dt * M->dx) * M->dy) * V.wf[t]);
+        const R divg_vol = dir == 0 ? R((dt * M->dy) * M->dz) * fetch<R>(V.uf, V.su, t)
+                                    : (dir == 1 ? R((dt * M->dx) * M->dz) * fetch<R>(V.vf, V.sv, t)
+                                                : R((dt * M->dx) * M->dy) * fetch<R>(V.wf, V.sw, t));
         const bool even = G.tess != 5 || ((fi + fj + fk) % 2) == 0; /* oddEvenCell of the face's cell */
-        const double vol = even ? (divg_vol - flux_vol) : -(divg_vol - flux_vol);
+        const R vol = even ? (divg_vol - flux_vol) : -(divg_vol - flux_vol);
         const int* qd = QUAD[dir][even ? 0 : 1];
-        const double *a = fv[qd[0]], *b = fv[qd[1]], *c = fv[qd[2]], *d = fv[qd[3]];
-        double e[3];
-        correction_apex(dir, a, b, c, d, vol, e);
+        const R *a = fv[qd[0]], *b = fv[qd[1]], *c = fv[qd[2]], *d = fv[qd[3]];
+        R e[3];
+        correction_apex<R>(dir, a, b, c, d, vol, e);
         for (int p = 0; p < 3; ++p) {
             tets[2 * f][0][p] = a[p]; tets[2 * f][1][p] = b[p]; tets[2 * f][2][p] = d[p]; tets[2 * f][3][p] = e[p];
             tets[2 * f + 1][0][p] = b[p]; tets[2 * f + 1][1][p] = c[p]; tets[2 * f + 1][2][p] = d[p];
@@ -1302,6 +1385,31 @@ int orc_props(const orc_mesh* M, const double* VF, double rho_liq, double rho_ga
                     if (visc[d]) visc[d][t] = vf * mu_liq + (1 - vf) * mu_gas;
                 }
     return 0;
+}
+
+/* Forward-mode derivatives of transport!'s SL update (the CPU analogue of ForwardDiff.jl's
+ * Dual numbers): for each listed cell (i, j, k triples), VFnew and its derivatives with respect
+ * to up to orc_ndual() face velocities, selected by the slot arrays su, sv, sw (cell-array
+ * shaped: the derivative slot of each face value, -1 for none).  grad is ncells x orc_ndual(). */
+int orc_ndual() { return NDUAL; }
+
+int orc_sl_forward(const orc_mesh* M, double dt, int ncells, const int* cells, const double* uf, const double* vf,
+                   const double* wf, const int* su, const int* sv, const int* sw, const double* nx, const double* ny,
+                   const double* nz, const double* D, double* vf_out, double* grad)
+{
+    Grid G(M);
+    Vel V{uf, vf, wf, su, sv, sw};
+    Plic P{nx, ny, nz, D};
+    int flags = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : flags)
+    for (int q = 0; q < ncells; ++q) {
+        Err e;
+        const Dual r = sl_cell<Dual>(G, V, P, dt, cells[3 * q], cells[3 * q + 1], cells[3 * q + 2], &e, nullptr);
+        vf_out[q] = r.v;
+        for (int s = 0; s < NDUAL; ++s) grad[(long)q * NDUAL + s] = r.d[s];
+        flags |= e.flags;
+    }
+    return flags;
 }
 
 double orc_sl_flux_vol(const orc_mesh* M, int dir, int i, int j, int k, const double* uf, const double* vf,

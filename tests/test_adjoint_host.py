@@ -363,3 +363,35 @@ def test_plane_polygon_gives_computeDist_partials(hlib, state, prec, tol):
                 assert np.all(np.abs(b - a) <= tol * np.maximum(np.abs(a), 1.0)), ((i, j, k), a, b)
                 n += 1
     assert n >= 20
+
+
+def forward_mode_grads(o, st, cells, weights, entries):
+    """dL/d(face value) for L = sum_c w_c VFnew_c, by forward-mode Dual numbers through the
+    restatement, entries (array 0/1/2, parent index) in chunks of ndual()."""
+    _, _, VF, band, nx, ny, nz, D, uf, vf, wf, dt = st
+    K = o.ndual()
+    out = np.zeros(len(entries))
+    for c0 in range(0, len(entries), K):
+        chunk = entries[c0:c0 + K]
+        _, g = o.sl_forward(dt, cells, uf, vf, wf, chunk, nx, ny, nz, D)
+        out[c0:c0 + len(chunk)] = weights @ g
+    return out
+
+
+def test_forward_mode_matches_reverse_pass(hlib, state):
+    """The hand-written reverse of one cell's SL update against forward-mode derivatives of the
+    restatement (Dual numbers, the CPU analogue of a ForwardDiff.jl gradient): every face value
+    the cell's update reads, to rounding."""
+    m, o = state[0], state[1]
+    cells = interface_preimage_cells(m, o, state, 8)
+    assert len(cells) >= 6
+    worst = 0.0
+    for c in cells:
+        _, grads, err = harness_grads(hlib, m, state, c)
+        assert err == 0
+        entries = [(a, tuple(int(x) for x in idx)) for a in range(3) for idx in np.argwhere(grads[a] != 0.0)]
+        assert len(entries) > 10
+        fwd = forward_mode_grads(o, state, [c], np.ones(1), entries)
+        rev = np.array([grads[a][idx] for a, idx in entries])
+        worst = max(worst, float(np.max(np.abs(fwd - rev)) / np.max(np.abs(rev))))
+    assert worst <= 1e-11, worst

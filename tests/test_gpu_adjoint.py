@@ -303,3 +303,35 @@ def test_single_step_other_tessellations(built, tess):
     worst, n = check_velocity(m, VF0, base, noise, dt, 1, w, (gu, gv, gw))
     assert n >= 12
     assert worst <= RTOL, worst
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-6)])
+def test_against_forward_mode_on_a_small_grid(built, precision, tol):
+    """One step on 12^3: the GPU reverse pass's dL/d(face velocities) against forward-mode
+    derivatives of the FP64 restatement (Dual numbers through the CPU path, the analogue of a
+    ForwardDiff.jl gradient), on every face the reverse pass reaches.  The FP64 reverse agrees to
+    rounding; the mixed one (FP32 geometry around its own states) to FP32 accuracy."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_adjoint_host import forward_mode_grads
+    m, VF0 = sphere3d(12)
+    dt = 0.5 * m.dx / 2.0
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
+    vel, noise = noisy(m, base, 0.05, 17)
+    w = np.random.default_rng(5).standard_normal((m.Nx, m.Ny, m.Nz))
+    L, gVF0, gu, gv, gw = gpu_gradients(m, VF0, vel, dt, 1, w, every=1, precision=precision)
+    o = Oracle(m)
+    VF = VF0.copy(order="F")
+    band, nx, ny, nz, D = o.init_state(VF)
+    uf, vf, wf = vel(0)
+    cells = [(i, j, k) for k in range(1, m.Nz + 1) for j in range(1, m.Ny + 1) for i in range(1, m.Nx + 1)
+             if abs(int(band[m.cidx(i, j, k)])) <= m.nband]
+    weights = np.array([w[i - 1, j - 1, k - 1] for i, j, k in cells])
+    grads = (gu, gv, gw)
+    entries = [(a, tuple(int(x) for x in idx)) for a in range(3) for idx in np.argwhere(grads[a] != 0.0)]
+    assert len(entries) > 100
+    st = (m, o, VF, band, nx, ny, nz, D, uf, vf, wf, dt)
+    fwd = forward_mode_grads(o, st, cells, weights, entries)
+    rev = np.array([grads[a][idx] for a, idx in entries])
+    assert np.max(np.abs(fwd - rev)) <= tol * np.max(np.abs(fwd))
