@@ -131,13 +131,14 @@ int slvof_step(slvof_ctx* ctx, double dt, int flags, double* mass);
 /* sum(VF[interior])*dx*dy*dz, compensated FP64 (src/WriteData.jl:33). */
 int slvof_mass(slvof_ctx* ctx, double* mass);
 
-/* ---- momentum of transport! (FP64 context) -------------------------------------------------
+/* ---- momentum of transport! (FP64 in either precision) ---------------------------------------
  * With the cell-centred velocities u, v, w (cell arrays), the SL update also gives us, vs, ws
  * of every interior cell (src/Transport.jl:34-166 with pressure_scheme "semi-lagrangian"):
  * band cells from the clipped pre-image (vrhoU/vrho with rho_liq/rho_gas on each side of the
  * donors' planes), the others from the face fluxes (finite-difference flux, no flux between
- * two band cells, the semi-Lagrangian flux volume SLfluxVol at band edges).  A mixed-precision
- * context returns SLVOF_E_UNSUPPORTED. */
+ * two band cells, the semi-Lagrangian flux volume SLfluxVol at band edges).  The clipped
+ * momentum sums need each donor's share of a pre-image, so these calls run the FP64 clip in a
+ * mixed-precision context too (its VF update is then the FP64 one). */
 int slvof_upload_cell_velocity(slvof_ctx* ctx, const double* u, const double* v, const double* w);
 int slvof_download_momentum(slvof_ctx* ctx, double* us, double* vs, double* ws);
 /* the SL section of transport! with its momentum, on the resident state */

@@ -742,8 +742,6 @@ int slvof_download_momentum(slvof_ctx* c, double* us, double* vs, double* ws)
 int slvof_transport_momentum(slvof_ctx* c, double dt)
 {
     TRY(begin(c));
-    if (c->precision != SLVOF_FP64)
-        return fail(c, SLVOF_E_UNSUPPORTED, "the momentum of transport! runs in an FP64 context");
     TRY(mom_alloc(c));
     TRY(clear_err(c));
     TRY(st_transport_mom(c, dt));
@@ -756,8 +754,6 @@ int slvof_transportSL_momentum(slvof_ctx* c, double dt, double* VF, const double
                                double* vs, double* ws)
 {
     TRY(begin(c));
-    if (c->precision != SLVOF_FP64)
-        return fail(c, SLVOF_E_UNSUPPORTED, "the momentum of transport! runs in an FP64 context");
     TRY(mom_alloc(c));
     TRY(clear_err(c));
     const size_t b = c->ncell * sizeof(double);

@@ -341,3 +341,18 @@ def test_finite_difference_scheme_unsupported_combinations(precision, tess):
     m = Mesh(Nx=8, Ny=8, Nz=8, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess, pressure_scheme="finite-difference")
     with pytest.raises(RuntimeError):
         SLVOF(m, precision)
+
+
+def test_momentum_in_a_mixed_context_runs_the_fp64_path():
+    """A mixed-precision context's momentum call runs the FP64 clip: the same VF and us, vs, ws
+    as an FP64 context on the same inputs."""
+    m, o, VFo, band, nx, ny, nz, D, uf, vf, wf, u, v, w, dt = momentum_state("5_tets")
+    out = []
+    for prec in ("fp64", "mixed"):
+        g = ctx(m, prec)
+        VFg = VFo.copy(order="F")
+        r = g.transportSL_momentum(dt, VFg, uf, vf, wf, nx, ny, nz, D, band, u, v, w)
+        out.append((VFg, *r))
+        g.close()
+    for a, b, name in zip(out[0], out[1], ("VF", "us", "vs", "ws")):
+        assert_same(a, b, name)
