@@ -375,7 +375,8 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
  * side) or a push.  A pruned node is the one-tet case 1 (all liquid) or 16 (all gas).
  * Cutters whose children do not fit put their node back; if no cutter fits, the first one
  * finishes its node with the private-stack clip.  Lanes' partial sums are combined per cell
- * by a fixed shuffle tree, so results are deterministic.  vol and vLiq are sums over the same
+ * by a fixed shuffle tree; which lane takes which piece depends on the batch, so the last
+ * bits of VF depend on how cells are batched.  vol and vLiq are sums over the same
  * pieces, so a pre-image that is all liquid gives VF = 1 exactly, as in the reference.
  *
  * Shared memory per warp: the node stack as four arrays of float4 (x, y, z, packed donor
@@ -385,8 +386,14 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
  * reaches at CFL <= 0.5 (farther donors are read from global memory).
  * ==================================================================================== */
 constexpr int CLIPW_WARPS = 4;
-constexpr int CLIPW_CAP = 112;  /* stack nodes per warp */
-constexpr int CLIPW_BATCH = 4;  /* cells per warp batch */
+/* Sizes: 2 cells per batch (10 seed tets for 5_tets) and 140 stack nodes per warp take
+ * 55.1 KB of shared memory per block, the most that keeps four blocks (16 warps) on an SM.
+ * Measured at 256^3: 4 cells and 112 nodes took 9.5 ms; a deeper stack puts fewer cutters
+ * back (112 nodes: 11 of 31 cuts per step went back) and a smaller batch frees the plane
+ * cache's share and halves the accumulator selects; 8.7 ms here.  Past 4 blocks per SM
+ * (3 blocks, 12 warps) the clip is slower at any depth. */
+constexpr int CLIPW_CAP = 140;  /* stack nodes per warp */
+constexpr int CLIPW_BATCH = 2;  /* cells per warp batch */
 constexpr int CLIPW_NBR = 27;   /* cached donor planes per batch cell */
 
 /* acc[b] += x with a compile-time index (keeps the accumulators in registers) */
@@ -728,7 +735,7 @@ void launch_sl32_clip(const DevMesh& m, double* VFout, const float4* planes, int
                       const float4* slow_verts, const int* slow_count, int* errw, int nsm, cudaStream_t s)
 {
     Plane32 PL{planes};
-    /* 51.4 KB of dynamic shared memory per block: above the 48 KB default, four blocks per SM */
+    /* 55.1 KB of dynamic shared memory per block: above the 48 KB default, four blocks per SM */
     const int smem = (int)sizeof(ClipShared);
     cudaFuncSetAttribute(k_sl32_clipw, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_sl32_clipw<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, VFout, PL, slow_cells, slow_verts, slow_count, work2,
