@@ -58,21 +58,26 @@ __global__ void __launch_bounds__(PURE_BX * PURE_BY) k_elvira_pure(DevMesh m, co
         const double c = VF[v];
         const long long cb = dbits(c);
         acc = fx62(c);
+        /* the six face neighbours are loaded together (one latency, not six in a chain) and
+         * tested in the reference's order */
+        const long long xm = dbits(VF[v - 1]), xp = dbits(VF[v + 1]);
+        const long long ym = dbits(VF[v - sj]), yp = dbits(VF[v + sj]);
+        const long long zm = dbits(VF[v - sk]), zp = dbits(VF[v + sk]);
         double ax = 0.0, ay = 0.0, az = 0.0;
         if (bits_below(cb, lo)) {
-            if (bits_above(dbits(VF[v - 1]), hi)) ax = 1.0;
-            else if (bits_above(dbits(VF[v + 1]), hi)) ax = -1.0;
-            else if (bits_above(dbits(VF[v - sj]), hi)) ay = 1.0;
-            else if (bits_above(dbits(VF[v + sj]), hi)) ay = -1.0;
-            else if (bits_above(dbits(VF[v - sk]), hi)) az = 1.0;
-            else if (bits_above(dbits(VF[v + sk]), hi)) az = -1.0;
+            if (bits_above(xm, hi)) ax = 1.0;
+            else if (bits_above(xp, hi)) ax = -1.0;
+            else if (bits_above(ym, hi)) ay = 1.0;
+            else if (bits_above(yp, hi)) ay = -1.0;
+            else if (bits_above(zm, hi)) az = 1.0;
+            else if (bits_above(zp, hi)) az = -1.0;
         } else if (bits_above(cb, hi)) {
-            if (bits_below(dbits(VF[v - 1]), lo)) ax = -1.0;
-            else if (bits_below(dbits(VF[v + 1]), lo)) ax = 1.0;
-            else if (bits_below(dbits(VF[v - sj]), lo)) ay = -1.0;
-            else if (bits_below(dbits(VF[v + sj]), lo)) ay = 1.0;
-            else if (bits_below(dbits(VF[v - sk]), lo)) az = -1.0;
-            else if (bits_below(dbits(VF[v + sk]), lo)) az = 1.0;
+            if (bits_below(xm, lo)) ax = -1.0;
+            else if (bits_below(xp, lo)) ax = 1.0;
+            else if (bits_below(ym, lo)) ay = -1.0;
+            else if (bits_below(yp, lo)) ay = 1.0;
+            else if (bits_below(zm, lo)) az = -1.0;
+            else if (bits_below(zp, lo)) az = 1.0;
         } else {
             iface = true; /* VFlo <= VF <= VFhi (or NaN, as the reference's compares) */
         }
@@ -254,26 +259,27 @@ __global__ void __launch_bounds__(BX * BY) k_band_sweep(DevMesh m, const short* 
 }
 
 /* transport! band gate (src/Transport.jl:111,153): band cells go to the SL list, the rest
- * keep VF. */
-__global__ void k_sl_classify(DevMesh m, const short* __restrict__ band, const double* __restrict__ VFin,
-                              double* __restrict__ VFout, int* list, int* count)
+ * keep VF.  Thread per interior cell on the pure-cell tiles ((i, j) from the block, k from the
+ * grid), so no index divides: a warp reads one row of 32 band entries and copies one row of
+ * VF. */
+__global__ void __launch_bounds__(PURE_BX * PURE_BY) k_sl_classify(DevMesh m, const short* __restrict__ band,
+                                                                   const double* __restrict__ VFin,
+                                                                   double* __restrict__ VFout, int* list,
+                                                                   int* count)
 {
-    const long N0 = m.N[0], N1 = m.N[1], N2 = m.N[2];
-    const long total = N0 * N1 * N2;
-    const long stride = (long)gridDim.x * blockDim.x;
-    for (long base = blockIdx.x * (long)blockDim.x; base < total; base += stride) {
-        const long t = base + threadIdx.x;
-        bool sl = false;
-        if (t < total) {
-            const int i = 1 + (int)(t % N0), j = 1 + (int)((t / N0) % N1), k = 1 + (int)(t / (N0 * N1));
-            sl = abs((int)band[cidx(m, i, j, k)]) <= m.nband;
-            if (!sl) {
-                const long v = vidx(m, i, j, k);
-                VFout[v] = VFin[v];
-            }
+    const int i = 1 + blockIdx.x * PURE_BX + threadIdx.x, j = 1 + blockIdx.y * PURE_BY + threadIdx.y;
+    const int k = 1 + blockIdx.z;
+    bool sl = false;
+    int L = 0;
+    if (i <= m.N[0] && j <= m.N[1]) {
+        L = (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1];
+        sl = abs((int)band[cidx(m, i, j, k)]) <= m.nband;
+        if (!sl) {
+            const long v = vidx(m, i, j, k);
+            VFout[v] = VFin[v];
         }
-        warp_append(sl, (int)t, list, count);
     }
+    warp_append(sl, L, list, count);
 }
 
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, long n, double scale)
@@ -485,7 +491,9 @@ void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, i
 void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin, double* VFout, int* list, int* count,
                         int nsm, cudaStream_t s)
 {
-    k_sl_classify<<<nsm * 8, 256, 0, s>>>(m, band, VFin, VFout, list, count);
+    (void)nsm;
+    const dim3 grid((m.N[0] + PURE_BX - 1) / PURE_BX, (m.N[1] + PURE_BY - 1) / PURE_BY, m.N[2]);
+    k_sl_classify<<<grid, dim3(PURE_BX, PURE_BY), 0, s>>>(m, band, VFin, VFout, list, count);
 }
 void launch_to_float(const double* a, float* b, long n, double scale, int nsm, cudaStream_t s)
 {
