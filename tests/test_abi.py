@@ -69,3 +69,38 @@ def test_create_rejects_bad_descriptor_without_gpu(lib):
     assert lib.slvof_create(None, 0, ctypes.byref(h)) == -1
     m = Mesh(Nx=4, Ny=4, Nz=4, Lx=1.0, Ly=1.0, Lz=1.0)
     assert lib.slvof_create(ctypes.byref(m.desc()), 7, ctypes.byref(h)) == -1
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("Nx", 0, -1), ("nghost", 2, -1), ("projection", 4, -1), ("nband", -1, -1), ("tesselation", 7, -1),
+    ("pressure_scheme", 2, -1), ("x", None, -1),
+    # thresholds are compared as bit patterns: positive finite only
+    ("VFlo", 0.0, -3), ("VFlo", -1e-10, -3), ("VFhi", float("nan"), -3), ("VFhi", float("inf"), -3),
+])
+def test_create_rejects_each_bad_field_without_gpu(lib, field, value, code):
+    m = Mesh(Nx=4, Ny=4, Nz=4, Lx=1.0, Ly=1.0, Lz=1.0)
+    d = m.desc()
+    setattr(d, field, value)
+    h = ctypes.c_void_p()
+    lib.slvof_create.restype = ctypes.c_int
+    for precision in (0, 1):
+        assert lib.slvof_create(ctypes.byref(d), precision, ctypes.byref(h)) == code
+        assert h.value is None
+
+
+@pytest.mark.parametrize("precision,tess,code", [(1, 5, -3), (0, 6, -3), (0, 24, -3), (1, 24, -3)])
+def test_create_refuses_finite_difference_outside_fp64_5_tets(lib, precision, tess, code):
+    m = Mesh(Nx=4, Ny=4, Nz=4, Lx=1.0, Ly=1.0, Lz=1.0, tesselation=f"{tess}_tets",
+             pressure_scheme="finite-difference")
+    h = ctypes.c_void_p()
+    lib.slvof_create.restype = ctypes.c_int
+    assert lib.slvof_create(ctypes.byref(m.desc()), precision, ctypes.byref(h)) == code
+
+
+@pytest.mark.parametrize("shape", [(1300, 1300, 1300), (40000, 4, 4), (4, 40000, 4), (4, 4, 40000)])
+def test_create_refuses_grids_past_32_bit_cell_indices(lib, shape):
+    # cell lists hold 32-bit linear indices of the (N + 2 nghost)^3 cell arrays
+    m = Mesh(Nx=shape[0], Ny=shape[1], Nz=shape[2], Lx=1.0, Ly=1.0, Lz=1.0)
+    h = ctypes.c_void_p()
+    lib.slvof_create.restype = ctypes.c_int
+    assert lib.slvof_create(ctypes.byref(m.desc()), 1, ctypes.byref(h)) == -3
