@@ -163,7 +163,9 @@ int slvof_transportSL_momentum(slvof_ctx* ctx, double dt, double* VF, const doub
                                const int16_t* band, const double* u, const double* v, const double* w, double* us,
                                double* vs, double* ws);
 /* Per-step drop-in for run_solver's loop with the state resident between calls: uploads
- * this step's face velocities, runs slvof_step and downloads VF (and the mass). */
+ * this step's face velocities, runs slvof_step and downloads VF (and the mass).  VF is
+ * downloaded on a second stream while the new state's normals, PLIC, band and mass are built;
+ * the call returns when both are done.  VF must not be null. */
 int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, const double* vf, const double* wf,
                     double* VF, double* mass);
 

@@ -76,6 +76,9 @@ struct slvof_ctx {
     double rho_liq = 1.0, rho_gas = 1.0;
     double last_ms = 0.0;
     cudaStream_t own_stream = nullptr;
+    /* slvof_step_host copies VF out on copy_stream while the next state's geometry is built */
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_state = nullptr, ev_copied = nullptr;
     cudaEvent_t sev[SLVOF_NSTAGES][2] = {};
     bool sran[SLVOF_NSTAGES] = {};
     std::string err;
@@ -351,6 +354,10 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return bail(SLVOF_E_CUDA);
     c->stream = c->own_stream;
     if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return bail(SLVOF_E_CUDA);
+    if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_state, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess)
+        return bail(SLVOF_E_CUDA);
     for (int q = 0; q < SLVOF_NSTAGES; ++q)
         if (cudaEventCreate(&c->sev[q][0]) != cudaSuccess || cudaEventCreate(&c->sev[q][1]) != cudaSuccess)
             return bail(SLVOF_E_CUDA);
@@ -420,6 +427,9 @@ int slvof_destroy(slvof_ctx* c)
     for (int q = 0; q < SLVOF_NSTAGES; ++q)
         for (int e = 0; e < 2; ++e)
             if (c->sev[q][e]) cudaEventDestroy(c->sev[q][e]);
+    if (c->ev_state) cudaEventDestroy(c->ev_state);
+    if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SLVOF_OK;
@@ -659,6 +669,7 @@ int slvof_step_host(slvof_ctx* c, double dt, int flags, const double* uf, const 
 {
     TRY(begin(c));
     if ((flags & SLVOF_STEP_MASS) && !mass) return fail(c, SLVOF_E_ARG, "mass requested with a null pointer");
+    if (!VF) return fail(c, SLVOF_E_ARG, "null host pointer");
     TRY(clear_err(c));
     TRY(up_velocity(c, uf, vf, wf));
     if (!c->normals_valid) {
@@ -666,11 +677,25 @@ int slvof_step_host(slvof_ctx* c, double dt, int flags, const double* uf, const 
         TRY(st_plic(c));
     }
     TRY(st_transport(c, dt));
-    TRY(st_normals(c));
-    TRY(st_plic(c));
-    if (flags & SLVOF_STEP_BAND) TRY(st_band(c));
-    if (flags & SLVOF_STEP_MASS) TRY(st_mass(c, mass, true));
-    TRY(d2h(c, VF, c->VF[c->vcur], c->nvf * sizeof(double)));
+    /* the new VF is final here (normals, PLIC, band and mass only read it): it goes to the host
+     * on the copy stream while they run */
+    CK(cudaEventRecord(c->ev_state, c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->ev_state, 0));
+    cudaError_t ce = cudaMemcpyAsync(VF, c->VF[c->vcur], c->nvf * sizeof(double), cudaMemcpyDeviceToHost,
+                                     c->copy_stream);
+    if (ce == cudaSuccess) ce = cudaEventRecord(c->ev_copied, c->copy_stream);
+    int r = 0;
+    if (ce == cudaSuccess) {
+        r = st_normals(c);
+        if (r >= 0) r = st_plic(c);
+        if (r >= 0 && (flags & SLVOF_STEP_BAND)) r = st_band(c);
+        if (r >= 0 && (flags & SLVOF_STEP_MASS)) r = st_mass(c, mass, true);
+        ce = cudaStreamWaitEvent(c->stream, c->ev_copied, 0);
+    }
+    if (r < 0 || ce != cudaSuccess) {
+        cudaStreamSynchronize(c->copy_stream); /* the host buffer is the caller's again on return */
+        return r < 0 ? r : fail(c, SLVOF_E_CUDA, std::string("VF download: ") + cudaGetErrorString(ce));
+    }
     return finish(c);
 }
 
