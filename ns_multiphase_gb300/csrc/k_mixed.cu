@@ -383,11 +383,13 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
  * indices), one per vertex, so a warp's pops and pushes hit consecutive 16-byte words; the
  * eight vertices of each lane's current cut (vertex-major, lane fastest); and the donor
  * planes of the 3x3x3 neighbourhood of each batch cell, which covers every donor a pre-image
- * reaches at CFL <= 0.5 (farther donors are read from global memory).
+ * reaches at CFL <= 0.5 (farther donors are read from global memory), with their constants
+ * moved to the batch cell's frame and two 27-bit masks of its pure liquid and pure gas donors,
+ * so that the pruning test evaluates planes only for the interface donors of a node's box.
  * ==================================================================================== */
 constexpr int CLIPW_WARPS = 4;
 /* Sizes: 2 cells per batch (10 seed tets for 5_tets) and 140 stack nodes per warp take
- * 55.1 KB of shared memory per block, the most that keeps four blocks (16 warps) on an SM.
+ * 55.2 KB of shared memory per block, the most that keeps four blocks (16 warps) on an SM.
  * Measured at 256^3: 4 cells and 112 nodes took 9.5 ms; a deeper stack puts fewer cutters
  * back (112 nodes: 11 of 31 cuts per step went back) and a smaller batch frees the plane
  * cache's share and halves the accumulator selects; 8.7 ms here.  Past 4 blocks per SM
@@ -415,6 +417,7 @@ struct ClipShared {
     float4 stk[CLIPW_WARPS][4][CLIPW_CAP];
     float4 scr[8][CLIPW_WARPS * 32];
     float4 pl[CLIPW_WARPS][CLIPW_BATCH][CLIPW_NBR];
+    uint2 msk[CLIPW_WARPS][CLIPW_BATCH];
 };
 
 __device__ __forceinline__ unsigned wbits(const float4& v) { return (unsigned)__float_as_int(v.w); }
@@ -423,34 +426,70 @@ __device__ __forceinline__ float sel4(float a, float b, float c, float d, int i)
     return i == 0 ? a : (i == 1 ? b : (i == 2 ? c : d));
 }
 
-/* Donor plane at index offset (a, b, c) from the batch cell (i0, j0, k0). */
+/* A donor plane's constant moved from the donor's frame to the frame of the cell at index
+ * offset -(a, b, c) from it: w + n.(a, b, c). */
+__device__ __forceinline__ float rel_dt(const float4& p, int a, int b, int c)
+{
+    return p.w + p.x * (float)a + p.y * (float)b + p.z * (float)c;
+}
+
+/* Donor plane at index offset (a, b, c) from the batch cell (i0, j0, k0), in the batch cell's
+ * frame: the cache holds the 3x3x3 neighbourhood already moved. */
 __device__ __forceinline__ float4 nbr_plane(const DevMesh& m, const Plane32& PL, const float4* cache, int i0, int j0,
                                             int k0, int a, int b, int c)
 {
     if ((unsigned)(a + 1) <= 2u && (unsigned)(b + 1) <= 2u && (unsigned)(c + 1) <= 2u)
         return cache[(c + 1) * 9 + (b + 1) * 3 + (a + 1)];
-    return __ldg(PL.P + cidx(m, i0 + a, j0 + b, k0 + c));
+    float4 p = __ldg(PL.P + cidx(m, i0 + a, j0 + b, k0 + c));
+    p.w = rel_dt(p, a, b, c);
+    return p;
 }
 
-/* box_plane_side for a node's four vertices, donor planes from the cache. */
-__device__ __forceinline__ int node_side(const DevMesh& m, const Plane32& PL, const float4* cache, int i0, int j0,
-                                         int k0, const int* lo, const int* hi, const float4* v)
+/* Side of a node's four vertices against one donor plane (in the batch cell's frame): 1 all
+ * strictly liquid, -1 all strictly gas, 0 otherwise. */
+__device__ __forceinline__ int plane_side4(const float4& p, const float4* v)
+{
+    bool neg = true, pos = true;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        const float d = fmaf(p.x, v[n].x, fmaf(p.y, v[n].y, fmaf(p.z, v[n].z, -p.w)));
+        neg = neg && d < 0.f;
+        pos = pos && d > 0.f;
+    }
+    return neg ? 1 : (pos ? -1 : 0);
+}
+
+/* box_plane_side for a node: the common side of its four vertices against every donor plane
+ * of its index box (at most 2x2x2), 0 when there is none.  LM and GM mark the pure liquid and
+ * pure gas donors of the cached neighbourhood (bit (c+1)*9 + (b+1)*3 + (a+1)). */
+__device__ __forceinline__ int node_side(const DevMesh& m, const Plane32& PL, const float4* cache, unsigned LM,
+                                         unsigned GM, int i0, int j0, int k0, const int* lo, const int* hi,
+                                         const float4* v)
 {
     if (hi[0] - lo[0] > 1 || hi[1] - lo[1] > 1 || hi[2] - lo[2] > 1) return 0;
+    if (lo[0] >= -1 && lo[1] >= -1 && lo[2] >= -1 && hi[0] <= 1 && hi[1] <= 1 && hi[2] <= 1) {
+        /* box inside the cached neighbourhood: pure donors from the phase masks, planes only
+         * for the interface donors */
+        const unsigned row = (hi[0] > lo[0] ? 3u : 1u) << (lo[0] + 1);
+        unsigned pln = row << (3 * (lo[1] + 1));
+        if (hi[1] > lo[1]) pln |= row << (3 * (hi[1] + 1));
+        unsigned box = pln << (9 * (lo[2] + 1));
+        if (hi[2] > lo[2]) box |= pln << (9 * (hi[2] + 1));
+        const bool liq = (box & LM) != 0u, gas = (box & GM) != 0u;
+        if (liq && gas) return 0;
+        int sd_all = liq ? 1 : (gas ? -1 : 2);
+        for (unsigned im = box & ~(LM | GM); im != 0u; im &= im - 1u) {
+            const int sd = plane_side4(cache[__ffs((int)im) - 1], v);
+            if (sd == 0 || (sd_all != 2 && sd != sd_all)) return 0;
+            sd_all = sd;
+        }
+        return sd_all == 2 ? 0 : sd_all;
+    }
     int side = 2;
     for (int c = lo[2]; c <= hi[2]; ++c)
         for (int b = lo[1]; b <= hi[1]; ++b)
             for (int a = lo[0]; a <= hi[0]; ++a) {
-                const float4 p = nbr_plane(m, PL, cache, i0, j0, k0, a, b, c);
-                const float Dt = p.w + p.x * (float)a + p.y * (float)b + p.z * (float)c;
-                bool neg = true, pos = true;
-#pragma unroll
-                for (int n = 0; n < 4; ++n) {
-                    const float d = fmaf(p.x, v[n].x, fmaf(p.y, v[n].y, fmaf(p.z, v[n].z, -Dt)));
-                    neg = neg && d < 0.f;
-                    pos = pos && d > 0.f;
-                }
-                const int sd = neg ? 1 : (pos ? -1 : 0);
+                const int sd = plane_side4(nbr_plane(m, PL, cache, i0, j0, k0, a, b, c), v);
                 if (sd == 0 || (side != 2 && sd != side)) return 0;
                 side = sd;
             }
@@ -491,9 +530,25 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
                       kk = __shfl_sync(0xffffffffu, ck_, b);
             if (t < nb * CLIPW_NBR) {
                 const int r = t - b * CLIPW_NBR;
-                S.pl[w][b][r] = __ldg(PL.P + cidx(m, ii + r % 3 - 1, jj + (r / 3) % 3 - 1, kk + r / 9 - 1));
+                const int a = r % 3 - 1, bq = (r / 3) % 3 - 1, c = r / 9 - 1;
+                float4 p = __ldg(PL.P + cidx(m, ii + a, jj + bq, kk + c));
+                p.w = rel_dt(p, a, bq, c);
+                S.pl[w][b][r] = p;
             }
         }
+        __syncwarp();
+        /* phase masks of the cached neighbourhoods: bit r set for a pure liquid (lm) or pure
+         * gas (gm) donor; a pure cell's plane is (0, 0, 0, +-Lsum) */
+#pragma unroll
+        for (int bb = 0; bb < CLIPW_BATCH; ++bb) {
+            float4 p = make_float4(1.f, 0.f, 0.f, 0.f);
+            if (bb < nb && lane < CLIPW_NBR) p = S.pl[w][bb][lane];
+            const bool pure = p.x == 0.f && p.y == 0.f && p.z == 0.f;
+            const unsigned l_ = __ballot_sync(0xffffffffu, pure && p.w > 0.f);
+            const unsigned g_ = __ballot_sync(0xffffffffu, pure && p.w < 0.f);
+            if (lane == 0) S.msk[w][bb] = make_uint2(l_, g_);
+        }
+        __syncwarp();
         /* seed: lane q < 5*nb pushes tet q%5 of cell q/5, its tag (cell in batch) in vertex 0 */
         FF acc[CLIPW_BATCH], avol[CLIPW_BATCH];
 #pragma unroll
@@ -546,7 +601,9 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
                     lo[q] = min(min(cind[0][q], cind[1][q]), min(cind[2][q], cind[3][q]));
                     hi[q] = max(max(cind[0][q], cind[1][q]), max(cind[2][q], cind[3][q]));
                 }
-                const int bp = m.fast_pure ? node_side(m, PL, cache, i0, j0, k0, lo, hi, v) : 0;
+                const uint2 mk = S.msk[w][b];
+                const unsigned LM = mk.x, GM = mk.y;
+                const int bp = m.fast_pure ? node_side(m, PL, cache, LM, GM, i0, j0, k0, lo, hi, v) : 0;
                 if (bp != 0) {
                     mode = 1;
                     cs = bp > 0 ? 0 : 15;
@@ -562,7 +619,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
                         mode = 1;
                         const int di = cind[0][0], dj = cind[0][1], dk = cind[0][2];
                         const float4 p = nbr_plane(m, PL, cache, i0, j0, k0, di, dj, dk);
-                        const float Dt = p.w + p.x * (float)di + p.y * (float)dj + p.z * (float)dk;
+                        const float Dt = p.w;
                         d0 = p.x * v[0].x + p.y * v[0].y + p.z * v[0].z - Dt;
                         d1 = p.x * v[1].x + p.y * v[1].y + p.z * v[1].z - Dt;
                         d2 = p.x * v[2].x + p.y * v[2].y + p.z * v[2].z - Dt;
@@ -735,7 +792,7 @@ void launch_sl32_clip(const DevMesh& m, double* VFout, const float4* planes, int
                       const float4* slow_verts, const int* slow_count, int* errw, int nsm, cudaStream_t s)
 {
     Plane32 PL{planes};
-    /* 55.1 KB of dynamic shared memory per block: above the 48 KB default, four blocks per SM */
+    /* 55.2 KB of dynamic shared memory per block: above the 48 KB default, four blocks per SM */
     const int smem = (int)sizeof(ClipShared);
     cudaFuncSetAttribute(k_sl32_clipw, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_sl32_clipw<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, VFout, PL, slow_cells, slow_verts, slow_count, work2,
