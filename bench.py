@@ -18,6 +18,12 @@ Arms:
              step, D2H of VF and the mass;
   cpu_baseline / --impl reference: the CPU restatement of the reference (C++, OpenMP on
              all host cores) on a bounded z-slab of the same state.
+
+Rooflines: "roofline" is the HBM roofline of the dominant stage (algorithmic bytes over its
+CUDA-event time, against the measured copy bandwidth); "roofline.compute" counts the
+reference algorithm's operations on a sample of the state (the restatement run with a
+counting scalar, in the CPU leg: absent with --no-cpu) and sets them against the CUDA
+cores' nominal FP32 rate (mixed) and FP64 rate (the FP64 arm).
 """
 from __future__ import annotations
 
@@ -52,6 +58,9 @@ def parse():
     p.add_argument("--adj-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--count-sample", type=int, default=1500,
+                   help="interface cells sampled for the operation count of the CPU leg (twice as many band "
+                        "cells); 0 skips it")
     return p.parse_args()
 
 
@@ -215,6 +224,35 @@ def cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, budget_s):
     return m.Nx * m.Ny * nk / sec, nk, sec
 
 
+def op_counts(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, counters, n_if):
+    """Algorithmic operations of one step: the restatement's ELVIRA, plane-constant and SL
+    paths run with a counting scalar (each +, -, *, / and each sqrt, cbrt, acos, sin, cos) on a
+    seeded sample of this state's interface cells and band cells, scaled to the step by its own
+    work-list sizes.  Pure cells do no arithmetic (axis normals, constant plane distances)."""
+    from oracle.oracle import Oracle, build
+    build()
+    g = m.nghost
+    vfi = m.interior(VF)
+    iface = np.flatnonzero(((vfi >= m.VFlo) & (vfi <= m.VFhi)).ravel(order="F"))
+    bnd = np.flatnonzero((np.abs(band[g:g + m.Nx, g:g + m.Ny, g:g + m.Nz]) <= m.nband).ravel(order="F"))
+    rng = np.random.default_rng(SEED)
+    si = np.sort(rng.choice(iface, min(n_if, len(iface)), replace=False))
+    sb = np.sort(rng.choice(bnd, min(2 * n_if, len(bnd)), replace=False))
+    t0 = time.perf_counter()
+    c = Oracle(m).count_ops(dt, VF, uf, vf, wf, nx, ny, nz, D, si, sb)
+    sec = time.perf_counter() - t0
+    per = {"elvira_per_interface_cell": c["elvira"] / len(si), "plic_per_interface_cell": c["plic"] / len(si),
+           "sl_per_band_cell": c["sl"] / len(sb)}
+    n_if_step, n_band_step = counters["interface_cells"], counters["band_cells"]
+    parts = {"elvira": per["elvira_per_interface_cell"] * n_if_step,
+             "plic": per["plic_per_interface_cell"] * n_if_step,
+             "sl": per["sl_per_band_cell"] * n_band_step}
+    return {"ops_per_step": sum(parts.values()), "parts": parts, "per_cell": per,
+            "sample": f"{len(si)} interface and {len(sb)} band cells of the FP64 state after the accuracy steps "
+                      f"(seed {SEED}), counted on one host thread in {sec:.1f} s; scaled by this step's "
+                      f"{n_if_step} interface and {n_band_step} band cells"}
+
+
 def reference_arm(args, rank):
     """--impl reference: the CPU restatement (the Julia reference cannot run here)."""
     import torch
@@ -356,7 +394,11 @@ def main():
 
         # ---- CPU restatement on a bounded slab ---------------------------------------------
         cpu = None
+        ops = None
         if not args.no_cpu:
+            # the CPU leg also counts the reference algorithm's operations on a sample
+            if args.count_sample > 0:
+                ops = op_counts(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, counters, args.count_sample)
             from oracle.oracle import build
             build()
             v, layers, sec = cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, args.cpu_seconds)
@@ -382,6 +424,31 @@ def main():
                         "the HBM fraction is reported per the contract",
                 "step": {"algorithmic_bytes": 28 * cells, "achieved_gbs": 28 * cells / (ms_step / 1e3) / 1e9,
                          "frac": 28 * cells / (ms_step / 1e3) / 1e9 / hbm}}
+        if ops is not None:
+            # CUDA-core peaks from the SM count and the measured maximum SM clock: 128 FP32 lanes
+            # per SM, an FMA counting two operations; GB300's FP64 rate is 1/64 of that
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            mhz = peaks.get("sm_max_mhz", 2070.0)
+            fp32 = sms * 128 * 2 * mhz * 1e6 / 1e12
+            fp64 = fp32 / 64
+            ms64_step = ms64 / args.fp64_steps
+
+            def rate(n, ms_):
+                return n / (ms_ / 1e3) / 1e12
+            roof["compute"] = {
+                "unit": "TFLOP/s", "ops_per_step": ops["ops_per_step"], "per_cell": ops["per_cell"],
+                "sample": ops["sample"],
+                "peak_fp32": fp32, "peak_fp64": fp64,
+                "peak_source": f"nominal: {sms} SMs x 128 lanes x 2 x {mhz:.0f} MHz (FP32), FP64 at 1/64",
+                "kernel": {"stage": dom, "ops": ops["parts"]["sl"], "achieved": rate(ops["parts"]["sl"], stage[dom]),
+                           "frac_fp32": rate(ops["parts"]["sl"], stage[dom]) / fp32},
+                "step_mixed": {"achieved": rate(ops["ops_per_step"], ms_step),
+                               "frac_fp32": rate(ops["ops_per_step"], ms_step) / fp32},
+                "step_fp64": {"achieved": rate(ops["ops_per_step"], ms64_step),
+                              "frac_fp64": rate(ops["ops_per_step"], ms64_step) / fp64},
+                "note": "operations of the reference's algorithm (the restatement with a counting scalar); the "
+                        "mixed ELVIRA scores candidates with a closed-form plane/cube volume instead of five tet "
+                        "clips, so its share of the mixed step's rate is an effective rate"}
         out = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",

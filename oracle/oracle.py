@@ -63,6 +63,8 @@ def lib():
         L.orc_ndual.argtypes = []
         L.orc_sl_forward.restype = i
         L.orc_sl_forward.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p, p, p]
+        L.orc_count_ops.restype = i
+        L.orc_count_ops.argtypes = [p, d, p, p, p, p, p, p, p, p, i, p, i, p, p, p]
         L.orc_curvature.restype = i
         L.orc_curvature.argtypes = [p, p, p, p, p, p]
         L.orc_props.restype = i
@@ -194,6 +196,29 @@ class Oracle:
 
     def ndual(self):
         return self.L.orc_ndual()
+
+    def count_ops(self, dt, VF, uf, vf, wf, nx, ny, nz, D, if_cells, band_cells, values=False):
+        """Algorithmic operation counts of a step's per-cell parts (each +, -, *, / and each
+        sqrt, cbrt, acos, sin, cos of the restatement), summed over the given interior cells
+        (linear indices (i-1) + Nx*((j-1) + Ny*(k-1))), on one thread.  Returns
+        {"elvira": .., "plic": .., "sl": ..} (interface cells, interface cells, band cells),
+        and with values=True also the values the counted paths computed (normals (n, 3), D,
+        VFnew), which equal the double paths' bit for bit."""
+        m = self.mesh
+        ic = np.ascontiguousarray(np.asarray(if_cells, dtype=np.int32).ravel())
+        bc = np.ascontiguousarray(np.asarray(band_cells, dtype=np.int32).ravel())
+        out = (ctypes.c_ulonglong * 3)()
+        vals = np.zeros(4 * len(ic) + len(bc)) if values else None
+        f = self.L.orc_count_ops(_m(m), dt, _p(VF), _p(nx), _p(ny), _p(nz), _p(D), _p(uf), _p(vf), _p(wf), len(ic),
+                                 ic.ctypes.data, len(bc), bc.ctypes.data, out,
+                                 vals.ctypes.data if values else None)
+        if f:
+            raise RuntimeError(f"restatement flags {f}")
+        counts = {"elvira": int(out[0]), "plic": int(out[1]), "sl": int(out[2])}
+        if not values:
+            return counts
+        n = len(ic)
+        return counts, vals[:3 * n].reshape(n, 3), vals[3 * n:4 * n], vals[4 * n:]
 
     def curvature(self, VF, nx, ny, nz):
         """transport!'s curvature section (src/Transport.jl:187-191, compute_curvature!)."""

@@ -83,6 +83,44 @@ inline Dual& operator+=(Dual& a, const Dual& b) { a = a + b; return a; }
 inline double val(double x) { return x; }
 inline double val(const Dual& x) { return x.v; }
 
+/* Operation counter for the algorithmic FLOP count of a step: the ELVIRA, plane-constant and
+ * SL paths below are also instantiated with Cnt, a double that counts each +, -, *, / and
+ * each sqrt, cbrt, acos, sin, cos it takes part in.  Negation, comparisons, min/max and fabs
+ * are not counted, nor are expressions of mesh constants alone (they stay double).  The
+ * counter is global: count on one thread. */
+unsigned long long g_nops = 0;
+struct Cnt {
+    double v;
+    Cnt() : v(0.0) {}
+    Cnt(double x) : v(x) {}
+};
+inline Cnt operator+(const Cnt& a, const Cnt& b) { ++g_nops; return Cnt(a.v + b.v); }
+inline Cnt operator-(const Cnt& a, const Cnt& b) { ++g_nops; return Cnt(a.v - b.v); }
+inline Cnt operator*(const Cnt& a, const Cnt& b) { ++g_nops; return Cnt(a.v * b.v); }
+inline Cnt operator/(const Cnt& a, const Cnt& b) { ++g_nops; return Cnt(a.v / b.v); }
+inline Cnt operator-(const Cnt& a) { return Cnt(-a.v); }
+inline Cnt& operator+=(Cnt& a, const Cnt& b) { a = a + b; return a; }
+inline Cnt& operator-=(Cnt& a, const Cnt& b) { a = a - b; return a; }
+inline bool operator<(const Cnt& a, const Cnt& b) { return a.v < b.v; }
+inline bool operator>(const Cnt& a, const Cnt& b) { return a.v > b.v; }
+inline bool operator<=(const Cnt& a, const Cnt& b) { return a.v <= b.v; }
+inline bool operator>=(const Cnt& a, const Cnt& b) { return a.v >= b.v; }
+inline double val(const Cnt& x) { return x.v; }
+
+/* Math functions of the generic paths: the restatement's own for double, counted for Cnt. */
+inline double f_sqrt(double x) { return std::sqrt(x); }
+inline double f_cbrt(double x) { return detm_cbrt(x); }
+inline double f_acos(double x) { return detm_acos(x); }
+inline double f_sin(double x) { return detm_sin(x); }
+inline double f_cos(double x) { return detm_cos(x); }
+inline double f_abs(double x) { return std::fabs(x); }
+inline Cnt f_sqrt(const Cnt& x) { ++g_nops; return Cnt(std::sqrt(x.v)); }
+inline Cnt f_cbrt(const Cnt& x) { ++g_nops; return Cnt(detm_cbrt(x.v)); }
+inline Cnt f_acos(const Cnt& x) { ++g_nops; return Cnt(detm_acos(x.v)); }
+inline Cnt f_sin(const Cnt& x) { ++g_nops; return Cnt(detm_sin(x.v)); }
+inline Cnt f_cos(const Cnt& x) { ++g_nops; return Cnt(detm_cos(x.v)); }
+inline Cnt f_abs(const Cnt& x) { return Cnt(std::fabs(x.v)); }
+
 /* Julia min/max on Float64: NaN-propagating. */
 template <class R>
 inline R jmax(const R& a, const R& b)
@@ -264,101 +302,108 @@ double cell2verts(const Grid& G, int i, int j, int k, double verts[][3])
 }
 
 /* computeAlpha, src/VF.jl:164-214. */
-double compute_alpha(const double min[3], double VF)
+template <class R>
+R compute_alpha(const R min[3], R VF)
 {
-    double m[3] = {min[0], min[1], min[2]};
-    std::sort(m, m + 3);
-    const double m1 = m[0], m2 = m[1], m3 = m[2];
-    const double m12 = m[0] + m[1];
-    const double V1 = m[0] * m[0] / jmax(6.0 * m[1] * m[2], EPS);
-    const double V2 = V1 + sdiv(0.5 * (m[1] - m[0]), m3);
-    double V3;
-    if (m12 <= m[2]) V3 = sdiv(0.5 * m12, m3);
-    else V3 = sdiv((m3 * m3 * (3.0 * m12 - m3) + m1 * m1 * (m1 - 3.0 * m3)) + m2 * m2 * (m2 - 3.0 * m3), 6.0 * m1 * m2 * m3);
-    double alpha;
-    if (0.0 <= VF && VF < V1) {
-        alpha = detm_cbrt(6.0 * m1 * m2 * m3 * VF);
+    R m[3] = {min[0], min[1], min[2]};
+    std::sort(m, m + 3, [](const R& a, const R& b) { return val(a) < val(b); });
+    const R m1 = m[0], m2 = m[1], m3 = m[2];
+    const R m12 = m[0] + m[1];
+    const R V1 = m[0] * m[0] / jmax(R(6.0) * m[1] * m[2], R(EPS));
+    const R V2 = V1 + sdiv(R(0.5) * (m[1] - m[0]), m3);
+    R V3;
+    if (m12 <= m[2]) V3 = sdiv(R(0.5) * m12, m3);
+    else V3 = sdiv((m3 * m3 * (R(3.0) * m12 - m3) + m1 * m1 * (m1 - R(3.0) * m3)) + m2 * m2 * (m2 - R(3.0) * m3),
+                   R(6.0) * m1 * m2 * m3);
+    R alpha;
+    if (R(0.0) <= VF && VF < V1) {
+        alpha = f_cbrt(R(6.0) * m1 * m2 * m3 * VF);
     } else if (V1 <= VF && VF < V2) {
-        alpha = 0.5 * (m1 + std::sqrt(m1 * m1 + 8.0 * m2 * m3 * (VF - V1)));
+        alpha = R(0.5) * (m1 + f_sqrt(m1 * m1 + R(8.0) * m2 * m3 * (VF - V1)));
     } else if (V2 <= VF && VF < V3) {
-        double a0 = (m1 * m1 * m1 + m2 * m2 * m2) - 6.0 * m1 * m2 * m3 * VF;
-        double a1 = -3.0 * (m1 * m1 + m2 * m2);
-        double a2 = 3.0 * m12;
-        double a3 = -1.0;
+        R a0 = (m1 * m1 * m1 + m2 * m2 * m2) - R(6.0) * m1 * m2 * m3 * VF;
+        R a1 = R(-3.0) * (m1 * m1 + m2 * m2);
+        R a2 = R(3.0) * m12;
+        R a3 = R(-1.0);
         a0 = a0 / a3; a1 = a1 / a3; a2 = a2 / a3; a3 = a3 / a3;
-        const double p0 = a1 / 3.0 - a2 * a2 / 9.0;
-        const double q0 = (a1 * a2 - 3.0 * a0) / 6.0 - a2 * a2 * a2 / 27.0;
-        const double theta = detm_acos(jmin(1.0, jmax(-1.0, q0 / std::sqrt(-1.0 * (p0 * p0 * p0))))) / 3.0;
-        alpha = std::sqrt(-p0) * (std::sqrt(3.0) * detm_sin(theta) - detm_cos(theta)) - a2 / 3.0;
+        const R p0 = a1 / R(3.0) - a2 * a2 / R(9.0);
+        const R q0 = (a1 * a2 - R(3.0) * a0) / R(6.0) - a2 * a2 * a2 / R(27.0);
+        const R theta = f_acos(jmin(R(1.0), jmax(R(-1.0), q0 / f_sqrt(R(-1.0) * (p0 * p0 * p0))))) / R(3.0);
+        alpha = f_sqrt(-p0) * (R(std::sqrt(3.0)) * f_sin(theta) - f_cos(theta)) - a2 / R(3.0);
     } else {
         if (m12 <= m3) {
-            alpha = m3 * VF + 0.5 * m12;
+            alpha = m3 * VF + R(0.5) * m12;
         } else {
-            double a0 = ((m1 * m1 * m1 + m2 * m2 * m2) + m3 * m3 * m3) - 6.0 * m1 * m2 * m3 * VF;
-            double a1 = -3.0 * ((m1 * m1 + m2 * m2) + m3 * m3);
-            double a2 = 3.0;
-            double a3 = -2.0;
+            R a0 = ((m1 * m1 * m1 + m2 * m2 * m2) + m3 * m3 * m3) - R(6.0) * m1 * m2 * m3 * VF;
+            R a1 = R(-3.0) * ((m1 * m1 + m2 * m2) + m3 * m3);
+            R a2 = R(3.0);
+            R a3 = R(-2.0);
             a0 = a0 / a3; a1 = a1 / a3; a2 = a2 / a3; a3 = a3 / a3;
-            const double p0 = a1 / 3.0 - a2 * a2 / 9.0;
-            const double q0 = (a1 * a2 - 3.0 * a0) / 6.0 - a2 * a2 * a2 / 27.0;
-            const double theta = detm_acos(jmin(1.0, jmax(-1.0, q0 / std::sqrt(-(p0 * p0 * p0))))) / 3.0;
-            alpha = std::sqrt(-p0) * (std::sqrt(3.0) * detm_sin(theta) - detm_cos(theta)) - a2 / 3.0;
+            const R p0 = a1 / R(3.0) - a2 * a2 / R(9.0);
+            const R q0 = (a1 * a2 - R(3.0) * a0) / R(6.0) - a2 * a2 * a2 / R(27.0);
+            const R theta = f_acos(jmin(R(1.0), jmax(R(-1.0), q0 / f_sqrt(-(p0 * p0 * p0))))) / R(3.0);
+            alpha = f_sqrt(-p0) * (R(std::sqrt(3.0)) * f_sin(theta) - f_cos(theta)) - a2 / R(3.0);
         }
     }
     return alpha;
 }
 
 /* computeDist, src/VF.jl:109-156. */
-double compute_dist(const Grid& G, int i, int j, int k, double nx, double ny, double nz, double VF)
+template <class R>
+R compute_dist(const Grid& G, int i, int j, int k, R nx, R ny, R nz, R VF)
 {
     const orc_mesh* M = G.m;
-    if (VF < M->VFlo) return -((M->Lx + M->Ly) + M->Lz);
-    if (VF > M->VFhi) return +((M->Lx + M->Ly) + M->Lz);
-    double mm[3] = {nx * M->dx, ny * M->dy, nz * M->dz};
-    const double norm = ((std::fabs(mm[0]) + std::fabs(mm[1])) + std::fabs(mm[2])) + EPS;
+    if (VF < M->VFlo) return R(-((M->Lx + M->Ly) + M->Lz));
+    if (VF > M->VFhi) return R(+((M->Lx + M->Ly) + M->Lz));
+    R mm[3] = {nx * M->dx, ny * M->dy, nz * M->dz};
+    const R norm = ((f_abs(mm[0]) + f_abs(mm[1])) + f_abs(mm[2])) + R(EPS);
     mm[0] = mm[0] / norm; mm[1] = mm[1] / norm; mm[2] = mm[2] / norm;
-    double factor = 0.0;
+    R factor(0.0);
     if (mm[0] < 0.0) factor += mm[0];
     if (mm[1] < 0.0) factor += mm[1];
     if (mm[2] < 0.0) factor += mm[2];
-    const double VFo = VF > 0.5 ? 1.0 - VF : VF;
-    const double am[3] = {std::fabs(mm[0]), std::fabs(mm[1]), std::fabs(mm[2])};
-    double alpha = compute_alpha(am, VFo);
-    alpha = VF > 0.5 ? 1.0 - alpha : alpha;
+    const R VFo = VF > 0.5 ? R(1.0) - VF : VF;
+    const R am[3] = {f_abs(mm[0]), f_abs(mm[1]), f_abs(mm[2])};
+    R alpha = compute_alpha(am, VFo);
+    alpha = VF > 0.5 ? R(1.0) - alpha : alpha;
     alpha += factor;
-    alpha -= 0.5 * ((mm[0] + mm[1]) + mm[2]);
-    double dist = alpha * norm;
+    alpha -= R(0.5) * ((mm[0] + mm[1]) + mm[2]);
+    R dist = alpha * norm;
     dist += (nx * G.xm(i) + ny * G.ym(j)) + nz * G.zm(k);
     return dist;
 }
 
 /* computePLIC2VF, src/VF.jl:219-278 (5_tets).  d2case modifies d in place here. */
-double compute_plic2vf(const Grid& G, int i, int j, int k, double nx, double ny, double nz, double dist, Err* err)
+template <class R>
+R compute_plic2vf(const Grid& G, int i, int j, int k, R nx, R ny, R nz, R dist, Err* err)
 {
     const orc_mesh* M = G.m;
     double verts[15][3];
     const double tetsign = cell2verts(G, i, j, k, verts);
     tess_points(G.tess, verts);
-    double VF = 0.0;
+    R VF(0.0);
     for (int t = 0; t < tess_ntets(G.tess); ++t) {
-        double vert[8][3];
+        R vert[8][3];
         int tv[4];
         tess_tet(G.tess, t, tv);
         for (int n = 0; n < 4; ++n)
             for (int p = 0; p < 3; ++p) vert[n][p] = verts[tv[n]][p];
-        double d[4];
+        R d[4];
         for (int n = 0; n < 4; ++n) d[n] = ((nx * vert[n][0] + ny * vert[n][1]) + nz * vert[n][2]) - dist;
-        const int cs = d2case(d, err) - 1;
+        double dc[4] = {val(d[0]), val(d[1]), val(d[2]), val(d[3])};
+        const int cs = d2case(dc, err) - 1;
+        for (int n = 0; n < 4; ++n)
+            if (!(dc[n] == val(d[n]))) d[n] = R(dc[n]);
         for (int n = 0; n < T_NVERT[cs]; ++n) {
             const int v1 = T_V1[cs][n] - 1, v2 = T_V2[cs][n] - 1;
-            const double mu = clamp_mu(sdiv(-d[v1], d[v2] - d[v1]));
-            for (int p = 0; p < 3; ++p) vert[4 + n][p] = (1.0 - mu) * vert[v1][p] + mu * vert[v2][p];
+            const R mu = clamp_mu(sdiv<R>(-d[v1], d[v2] - d[v1]));
+            for (int p = 0; p < 3; ++p) vert[4 + n][p] = (R(1.0) - mu) * vert[v1][p] + mu * vert[v2][p];
         }
         for (int n = T_NTETS[cs]; n >= T_NNTET[cs]; --n) {
-            double tet[4][3];
+            R tet[4][3];
             for (int tt = 0; tt < 4; ++tt)
                 for (int p = 0; p < 3; ++p) tet[tt][p] = vert[T_VTET[cs][n - 1][tt] - 1][p];
-            VF += tetsign * tet_vol(tet) / (M->dx * M->dy * M->dz);
+            VF += R(tetsign) * tet_vol(tet) / R(M->dx * M->dy * M->dz);
         }
     }
     return VF;
@@ -434,72 +479,75 @@ struct Fields {
     double VFat(int i, int j, int k) const { return VF[G->v(i, j, k)]; }
 };
 
-void check_normal(const Grid& G, const Fields& F, double& err, double nx_, double ny_, double nz_,
-                  double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
+template <class R>
+void check_normal(const Grid& G, const Fields& F, R& err, R nx_, R ny_, R nz_, double* nx, double* ny, double* nz,
+                  int i, int j, int k, Err* e)
 {
-    double err_ = 0.0;
-    const double norm = std::sqrt((nx_ * nx_ + ny_ * ny_) + nz_ * nz_);
+    R err_(0.0);
+    const R norm = f_sqrt((nx_ * nx_ + ny_ * ny_) + nz_ * nz_);
     nx_ = nx_ / norm; ny_ = ny_ / norm; nz_ = nz_ / norm;
-    const double dist = compute_dist(G, i, j, k, nx_, ny_, nz_, F.VFat(i, j, k));
+    const R dist = compute_dist<R>(G, i, j, k, nx_, ny_, nz_, R(F.VFat(i, j, k)));
     for (int kk = k - 1; kk <= k + 1; ++kk)
         for (int jj = j - 1; jj <= j + 1; ++jj)
             for (int ii = i - 1; ii <= i + 1; ++ii) {
-                const double VF_ = compute_plic2vf(G, ii, jj, kk, nx_, ny_, nz_, dist, e);
-                const double r = F.VFat(ii, jj, kk) - VF_;
+                const R VF_ = compute_plic2vf<R>(G, ii, jj, kk, nx_, ny_, nz_, dist, e);
+                const R r = R(F.VFat(ii, jj, kk)) - VF_;
                 err_ += r * r;
             }
     if (err_ < err) {
         err = err_;
         const long c = G.c(i, j, k);
-        nx[c] = nx_; ny[c] = ny_; nz[c] = nz_;
+        nx[c] = val(nx_); ny[c] = val(ny_); nz[c] = val(nz_);
     }
 }
 
+template <class R = double>
 void elvira_calc(const Grid& G, const Fields& F, double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
 {
     const orc_mesh* M = G.m;
-    double err = INFINITY;
+    R err(INFINITY);
+    auto V = [&](int a, int b, int c) { return R(F.VFat(a, b, c)); };
     const int P[3][2] = {{-1, 0}, {-1, 1}, {0, 1}};
     if (M->Nz > 1) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
                 const int jj1 = j + P[a][0], jj2 = j + P[a][1], ii1 = i + P[b][0], ii2 = i + P[b][1];
-                const double s2x = (F.VFat(ii2, j, k - 1) * M->dz + F.VFat(ii2, j, k) * M->dz) + F.VFat(ii2, j, k + 1) * M->dz;
-                const double s1x = (F.VFat(ii1, j, k - 1) * M->dz + F.VFat(ii1, j, k) * M->dz) + F.VFat(ii1, j, k + 1) * M->dz;
-                const double nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
-                const double s2y = (F.VFat(i, jj2, k - 1) * M->dz + F.VFat(i, jj2, k) * M->dz) + F.VFat(i, jj2, k + 1) * M->dz;
-                const double s1y = (F.VFat(i, jj1, k - 1) * M->dz + F.VFat(i, jj1, k) * M->dz) + F.VFat(i, jj1, k + 1) * M->dz;
-                const double ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
-                const double nz_ = F.VFat(i, j, k + 1) > F.VFat(i, j, k - 1) ? -1.0 : 1.0;
-                check_normal(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+                const R s2x = (V(ii2, j, k - 1) * M->dz + V(ii2, j, k) * M->dz) + V(ii2, j, k + 1) * M->dz;
+                const R s1x = (V(ii1, j, k - 1) * M->dz + V(ii1, j, k) * M->dz) + V(ii1, j, k + 1) * M->dz;
+                const R nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
+                const R s2y = (V(i, jj2, k - 1) * M->dz + V(i, jj2, k) * M->dz) + V(i, jj2, k + 1) * M->dz;
+                const R s1y = (V(i, jj1, k - 1) * M->dz + V(i, jj1, k) * M->dz) + V(i, jj1, k + 1) * M->dz;
+                const R ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
+                const R nz_ = V(i, j, k + 1) > V(i, j, k - 1) ? R(-1.0) : R(1.0);
+                check_normal<R>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
             }
     }
     if (M->Ny > 1) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
                 const int kk1 = k + P[a][0], kk2 = k + P[a][1], ii1 = i + P[b][0], ii2 = i + P[b][1];
-                const double s2x = (F.VFat(ii2, j - 1, k) * M->dy + F.VFat(ii2, j, k) * M->dy) + F.VFat(ii2, j + 1, k) * M->dy;
-                const double s1x = (F.VFat(ii1, j - 1, k) * M->dy + F.VFat(ii1, j, k) * M->dy) + F.VFat(ii1, j + 1, k) * M->dy;
-                const double nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
-                const double ny_ = F.VFat(i, j + 1, k) > F.VFat(i, j - 1, k) ? -1.0 : 1.0;
-                const double s2z = (F.VFat(i, j - 1, kk2) * M->dy + F.VFat(i, j, kk2) * M->dy) + F.VFat(i, j + 1, kk2) * M->dy;
-                const double s1z = (F.VFat(i, j - 1, kk1) * M->dy + F.VFat(i, j, kk1) * M->dy) + F.VFat(i, j + 1, kk1) * M->dy;
-                const double nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
-                check_normal(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+                const R s2x = (V(ii2, j - 1, k) * M->dy + V(ii2, j, k) * M->dy) + V(ii2, j + 1, k) * M->dy;
+                const R s1x = (V(ii1, j - 1, k) * M->dy + V(ii1, j, k) * M->dy) + V(ii1, j + 1, k) * M->dy;
+                const R nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
+                const R ny_ = V(i, j + 1, k) > V(i, j - 1, k) ? R(-1.0) : R(1.0);
+                const R s2z = (V(i, j - 1, kk2) * M->dy + V(i, j, kk2) * M->dy) + V(i, j + 1, kk2) * M->dy;
+                const R s1z = (V(i, j - 1, kk1) * M->dy + V(i, j, kk1) * M->dy) + V(i, j + 1, kk1) * M->dy;
+                const R nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
+                check_normal<R>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
             }
     }
     if (M->Nx > 1) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
                 const int kk1 = k + P[a][0], kk2 = k + P[a][1], jj1 = j + P[b][0], jj2 = j + P[b][1];
-                const double nx_ = F.VFat(i + 1, j, k) > F.VFat(i - 1, j, k) ? -1.0 : 1.0;
-                const double s2y = (F.VFat(i - 1, jj2, k) * M->dx + F.VFat(i, jj2, k) * M->dx) + F.VFat(i + 1, jj2, k) * M->dx;
-                const double s1y = (F.VFat(i - 1, jj1, k) * M->dx + F.VFat(i, jj1, k) * M->dx) + F.VFat(i + 1, jj1, k) * M->dx;
-                const double ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
-                const double s2z = (F.VFat(i - 1, j, kk2) * M->dx + F.VFat(i, j, kk2) * M->dx) + F.VFat(i + 1, j, kk2) * M->dx;
-                const double s1z = (F.VFat(i - 1, j, kk1) * M->dx + F.VFat(i, j, kk1) * M->dx) + F.VFat(i + 1, j, kk1) * M->dx;
-                const double nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
-                check_normal(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+                const R nx_ = V(i + 1, j, k) > V(i - 1, j, k) ? R(-1.0) : R(1.0);
+                const R s2y = (V(i - 1, jj2, k) * M->dx + V(i, jj2, k) * M->dx) + V(i + 1, jj2, k) * M->dx;
+                const R s1y = (V(i - 1, jj1, k) * M->dx + V(i, jj1, k) * M->dx) + V(i + 1, jj1, k) * M->dx;
+                const R ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
+                const R s2z = (V(i - 1, j, kk2) * M->dx + V(i, j, kk2) * M->dx) + V(i + 1, j, kk2) * M->dx;
+                const R s1z = (V(i - 1, j, kk1) * M->dx + V(i, j, kk1) * M->dx) + V(i + 1, j, kk1) * M->dx;
+                const R nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
+                check_normal<R>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
             }
     }
 }
@@ -541,6 +589,8 @@ template <class R>
 inline R fetch(const double* f, const int* seed, long t);
 template <>
 inline double fetch<double>(const double* f, const int*, long t) { return f[t]; }
+template <>
+inline Cnt fetch<Cnt>(const double* f, const int*, long t) { return Cnt(f[t]); }
 template <>
 inline Dual fetch<Dual>(const double* f, const int* seed, long t)
 {
@@ -633,6 +683,12 @@ void pt2index(const Grid& G, int I[3], const double pt[3], int i, int j, int k, 
             I[d] -= 1;
         }
     }
+}
+
+inline void pt2index(const Grid& G, int I[3], const Cnt pt[3], int i, int j, int k, Err* e)
+{
+    const double p[3] = {pt[0].v, pt[1].v, pt[2].v};
+    pt2index(G, I, p, i, j, k, e);
 }
 
 inline void pt2index(const Grid& G, int I[3], const Dual pt[3], int i, int j, int k, Err* e)
@@ -1392,6 +1448,63 @@ int orc_props(const orc_mesh* M, const double* VF, double rho_liq, double rho_ga
  * to up to orc_ndual() face velocities, selected by the slot arrays su, sv, sw (cell-array
  * shaped: the derivative slot of each face value, -1 for none).  grad is ncells x orc_ndual(). */
 int orc_ndual() { return NDUAL; }
+
+/* Algorithmic operation counts (see Cnt) of one step's per-cell parts, summed over the given
+ * cells (interior cells as linear indices (i-1) + Nx*((j-1) + Ny*(k-1))), on one thread:
+ *   out[0]  ELVIRA at the interface cells: elvira_calc, 27 (2D: 18) candidates, each
+ *           normalised, computeDist, and computePLIC2VF of the 27 neighbours;
+ *   out[1]  the plane constant at the interface cells (computeDist with the given normals);
+ *   out[2]  the SL update at the band cells (sl_cell: the projected vertices and the clip).
+ * vals, when given, receives the values the counted paths compute (3 normal components per
+ * interface cell, then D per interface cell, then VFnew per band cell), which equal the
+ * double paths' bit for bit. */
+int orc_count_ops(const orc_mesh* M, double dt, const double* VF, const double* nx, const double* ny,
+                  const double* nz, const double* D, const double* uf, const double* vf, const double* wf, int n_if,
+                  const int* if_cells, int n_band, const int* band_cells, unsigned long long out[3], double* vals)
+{
+    Grid G(M);
+    Fields F{&G, VF};
+    Err e;
+    const long ncell = (long)G.n[0] * G.n[1] * G.n[2];
+    std::vector<double> sx(ncell, 0.0), sy(ncell, 0.0), sz(ncell, 0.0);
+    auto ijk = [&](int L, int& i, int& j, int& k) {
+        i = 1 + L % M->Nx;
+        j = 1 + (L / M->Nx) % M->Ny;
+        k = 1 + L / (M->Nx * M->Ny);
+    };
+    g_nops = 0;
+    for (int q = 0; q < n_if; ++q) {
+        int i, j, k;
+        ijk(if_cells[q], i, j, k);
+        elvira_calc<Cnt>(G, F, sx.data(), sy.data(), sz.data(), i, j, k, &e);
+        if (vals) {
+            const long c = G.c(i, j, k);
+            vals[3 * q] = sx[c]; vals[3 * q + 1] = sy[c]; vals[3 * q + 2] = sz[c];
+        }
+    }
+    out[0] = g_nops;
+    g_nops = 0;
+    for (int q = 0; q < n_if; ++q) {
+        int i, j, k;
+        ijk(if_cells[q], i, j, k);
+        const long c = G.c(i, j, k);
+        const Cnt d = compute_dist<Cnt>(G, i, j, k, Cnt(nx[c]), Cnt(ny[c]), Cnt(nz[c]), Cnt(VF[G.v(i, j, k)]));
+        if (vals) vals[3 * n_if + q] = d.v;
+    }
+    out[1] = g_nops;
+    g_nops = 0;
+    Vel V{uf, vf, wf};
+    Plic P{nx, ny, nz, D};
+    for (int q = 0; q < n_band; ++q) {
+        int i, j, k;
+        ijk(band_cells[q], i, j, k);
+        const Cnt r = sl_cell<Cnt>(G, V, P, dt, i, j, k, &e, nullptr);
+        if (vals) vals[4 * n_if + q] = r.v;
+    }
+    out[2] = g_nops;
+    g_nops = 0;
+    return e.flags;
+}
 
 int orc_sl_forward(const orc_mesh* M, double dt, int ncells, const int* cells, const double* uf, const double* vf,
                    const double* wf, const int* su, const int* sv, const int* sw, const double* nx, const double* ny,
