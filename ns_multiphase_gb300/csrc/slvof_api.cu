@@ -76,9 +76,10 @@ struct slvof_ctx {
     double rho_liq = 1.0, rho_gas = 1.0;
     double last_ms = 0.0;
     cudaStream_t own_stream = nullptr;
-    /* slvof_step_host copies VF out on copy_stream while the next state's geometry is built */
-    cudaStream_t copy_stream = nullptr;
-    cudaEvent_t ev_state = nullptr, ev_copied = nullptr;
+    /* slvof_step_host copies VF out on copy_stream while the next state's geometry is built;
+     * the steps build the band on band_stream beside the normals and PLIC */
+    cudaStream_t copy_stream = nullptr, band_stream = nullptr;
+    cudaEvent_t ev_state = nullptr, ev_copied = nullptr, ev_band = nullptr;
     cudaEvent_t sev[SLVOF_NSTAGES][2] = {};
     bool sran[SLVOF_NSTAGES] = {};
     std::string err;
@@ -112,13 +113,13 @@ int begin(slvof_ctx* c)
     return 0;
 }
 
-/* stage markers: events around each launch group */
-void s_beg(slvof_ctx* c, int s)
+/* stage markers: events around each launch group (on the stream the group runs on) */
+void s_beg(slvof_ctx* c, int s, cudaStream_t st = nullptr)
 {
-    cudaEventRecord(c->sev[s][0], c->stream);
+    cudaEventRecord(c->sev[s][0], st ? st : c->stream);
     c->sran[s] = true;
 }
-void s_end(slvof_ctx* c, int s) { cudaEventRecord(c->sev[s][1], c->stream); }
+void s_end(slvof_ctx* c, int s, cudaStream_t st = nullptr) { cudaEventRecord(c->sev[s][1], st ? st : c->stream); }
 
 /* Synchronise, time the call and fold the device error word into the status. */
 int finish(slvof_ctx* c, bool read_err = true)
@@ -189,20 +190,45 @@ int st_plic(slvof_ctx* c)
     return 0;
 }
 
-int st_band(slvof_ctx* c)
+int st_band(slvof_ctx* c, cudaStream_t st = nullptr)
 {
+    cudaStream_t s = st ? st : c->stream;
     int b = c->bcur;
-    s_beg(c, S_BAND);
-    launch_band_first(c->m, c->VF[c->vcur], c->band[1 - b], c->nsm, c->stream);
-    launch_band_ghost(c->m, c->band[b], c->band[1 - b], true, c->nsm, c->stream);
+    s_beg(c, S_BAND, s);
+    launch_band_first(c->m, c->VF[c->vcur], c->band[1 - b], c->nsm, s);
+    launch_band_ghost(c->m, c->band[b], c->band[1 - b], true, c->nsm, s);
     b = 1 - b;
     for (int n = 1; n <= c->m.nband; ++n) {
-        launch_band_sweep(c->m, c->band[b], c->band[1 - b], n, c->nsm, c->stream);
-        launch_band_ghost(c->m, c->band[b], c->band[1 - b], false, c->nsm, c->stream);
+        launch_band_sweep(c->m, c->band[b], c->band[1 - b], n, c->nsm, s);
+        launch_band_ghost(c->m, c->band[b], c->band[1 - b], false, c->nsm, s);
         b = 1 - b;
     }
     c->bcur = b;
-    s_end(c, S_BAND);
+    s_end(c, S_BAND, s);
+    return 0;
+}
+
+/* The band of the new state reads only VF, which the normals, PLIC and mass only read, and
+ * they do not touch the band: after the transport it is built on band_stream beside them, and
+ * the call's stream waits for ev_band before the call ends (join_band). */
+int st_band_side(slvof_ctx* c)
+{
+    CK(cudaEventRecord(c->ev_state, c->stream));
+    CK(cudaStreamWaitEvent(c->band_stream, c->ev_state, 0));
+    st_band(c, c->band_stream);
+    CK(cudaEventRecord(c->ev_band, c->band_stream));
+    return 0;
+}
+
+/* The call's stream waits for the side band; after an error the band stream is drained so
+ * that no band kernel outlives the call. */
+int join_band(slvof_ctx* c, int r)
+{
+    const cudaError_t e = cudaStreamWaitEvent(c->stream, c->ev_band, 0);
+    if (r < 0 || e != cudaSuccess) {
+        cudaStreamSynchronize(c->band_stream);
+        return r < 0 ? r : fail(c, SLVOF_E_CUDA, std::string("band join: ") + cudaGetErrorString(e));
+    }
     return 0;
 }
 
@@ -355,8 +381,10 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     c->stream = c->own_stream;
     if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return bail(SLVOF_E_CUDA);
     if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->band_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_state, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_band, cudaEventDisableTiming) != cudaSuccess)
         return bail(SLVOF_E_CUDA);
     for (int q = 0; q < SLVOF_NSTAGES; ++q)
         if (cudaEventCreate(&c->sev[q][0]) != cudaSuccess || cudaEventCreate(&c->sev[q][1]) != cudaSuccess)
@@ -429,7 +457,9 @@ int slvof_destroy(slvof_ctx* c)
             if (c->sev[q][e]) cudaEventDestroy(c->sev[q][e]);
     if (c->ev_state) cudaEventDestroy(c->ev_state);
     if (c->ev_copied) cudaEventDestroy(c->ev_copied);
+    if (c->ev_band) cudaEventDestroy(c->ev_band);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->band_stream) cudaStreamDestroy(c->band_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SLVOF_OK;
@@ -592,10 +622,13 @@ int slvof_step(slvof_ctx* c, double dt, int flags, double* mass)
         TRY(st_plic(c));
     }
     TRY(st_transport(c, dt));
-    TRY(st_normals(c));
-    TRY(st_plic(c));
-    if (flags & SLVOF_STEP_BAND) TRY(st_band(c));
-    if (flags & SLVOF_STEP_MASS) TRY(st_mass(c, mass, true));
+    const bool band = (flags & SLVOF_STEP_BAND) != 0;
+    int r = band ? st_band_side(c) : 0;
+    if (r >= 0) r = st_normals(c);
+    if (r >= 0) r = st_plic(c);
+    if (r >= 0 && (flags & SLVOF_STEP_MASS)) r = st_mass(c, mass, true);
+    if (band) r = join_band(c, r);
+    if (r < 0) return r;
     return finish(c);
 }
 
@@ -685,11 +718,13 @@ int slvof_step_host(slvof_ctx* c, double dt, int flags, const double* uf, const 
                                      c->copy_stream);
     if (ce == cudaSuccess) ce = cudaEventRecord(c->ev_copied, c->copy_stream);
     int r = 0;
+    const bool band = (flags & SLVOF_STEP_BAND) != 0;
     if (ce == cudaSuccess) {
-        r = st_normals(c);
+        r = band ? st_band_side(c) : 0;
+        if (r >= 0) r = st_normals(c);
         if (r >= 0) r = st_plic(c);
-        if (r >= 0 && (flags & SLVOF_STEP_BAND)) r = st_band(c);
         if (r >= 0 && (flags & SLVOF_STEP_MASS)) r = st_mass(c, mass, true);
+        if (band) r = join_band(c, r);
         ce = cudaStreamWaitEvent(c->stream, c->ev_copied, 0);
     }
     if (r < 0 || ce != cudaSuccess) {
