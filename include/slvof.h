@@ -90,7 +90,10 @@ int slvof_last_kernel_ms(const slvof_ctx* ctx, double* ms);
 #define SLVOF_NSTAGES 9
 int slvof_stage_ms(const slvof_ctx* ctx, double* ms, int n);
 /* Run the context's work on a caller-owned cudaStream_t (NULL: back to the private stream),
- * e.g. the stream of a Julia CUDA.jl task.  No counterpart in the reference (CPU only). */
+ * e.g. the stream of a Julia CUDA.jl task.  slvof_step and slvof_step_host also use two
+ * streams of their own (the band and the VF download), ordered after the caller's stream by
+ * events; the caller's stream waits for both before the call returns.  No counterpart in the
+ * reference (CPU only). */
 int slvof_set_stream(slvof_ctx* ctx, void* stream);
 /* Work-list sizes of the last step: [0] band cells updated by the SL clip pipeline,
  * [1] interface cells given ELVIRA candidates, [2] band cells that needed the full clip (mixed
