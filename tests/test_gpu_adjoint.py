@@ -311,11 +311,25 @@ def test_against_forward_mode_on_a_small_grid(built, precision, tol):
     derivatives of the FP64 restatement (Dual numbers through the CPU path, the analogue of a
     ForwardDiff.jl gradient), on every face the reverse pass reaches.  The FP64 reverse agrees to
     rounding; the mixed one (FP32 geometry around its own states) to FP32 accuracy."""
+    forward_mode_check(sphere3d(12), precision, tol)
+
+
+@pytest.mark.parametrize("projection", ["Euler", "Midpoint"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 2e-6)])
+def test_other_projections_against_forward_mode(built, projection, precision, tol):
+    """The reverse of project!'s Euler and Midpoint stages (src/Tools.jl:392-418), as the RK4
+    case above."""
+    m = Mesh(Nx=12, Ny=12, Nz=12, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, projection=projection)
+    VF0 = cases.vf_spheres(m, np.array([[0.45, 0.52, 0.55]]), np.array([0.27]), nF=8)
+    forward_mode_check((m, VF0), precision, tol)
+
+
+def forward_mode_check(mesh_vf, precision, tol):
     import sys
     import os
     sys.path.insert(0, os.path.dirname(__file__))
     from test_adjoint_host import forward_mode_grads
-    m, VF0 = sphere3d(12)
+    m, VF0 = mesh_vf
     dt = 0.5 * m.dx / 2.0
     base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
     vel, noise = noisy(m, base, 0.05, 17)
