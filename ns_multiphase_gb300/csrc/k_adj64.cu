@@ -33,48 +33,66 @@ __device__ __forceinline__ void load_cut_table(CutCase* s_tab)
 
 /* out[q] = sum of in[p] over the cells p whose ghost-fill source is q (separable map), over
  * the VF array (vf = 1, Neumann + borders) or a cell array (vf = 0, borders only). */
-__global__ void k_adj_fold(DevMesh m, const double* __restrict__ in, double* __restrict__ out, int vf, int neumann)
+constexpr int FOLD_BX = 32, FOLD_BY = 8; /* fold tile: 32 x 8 entries of one k plane */
+
+__global__ void __launch_bounds__(FOLD_BX * FOLD_BY) k_adj_fold(DevMesh m, const double* __restrict__ in,
+                                                                double* __restrict__ out, int vf, int neumann)
 {
     const int lo = vf ? m.vlo : m.lo;
     const int ext = vf ? 3 : 0;
     const int hi[3] = {m.hi[0] + ext, m.hi[1] + ext, m.hi[2] + ext};
-    const long n0 = hi[0] - lo + 1, n1 = hi[1] - lo + 1, n2 = hi[2] - lo + 1;
-    const long total = n0 * n1 * n2;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-        const int i = lo + (int)(t % n0), j = lo + (int)((t / n0) % n1), k = lo + (int)(t / (n0 * n1));
-        /* farther than g from every end no ghost copies the cell: it is its own only preimage */
-        if (i > m.g && i <= m.N[0] - m.g && j > m.g && j <= m.N[1] - m.g && k > m.g && k <= m.N[2] - m.g) {
-            out[t] = in[t];
-            continue;
-        }
-        int pa[adj::MAXPRE], pb[adj::MAXPRE], pc[adj::MAXPRE];
-        const int na = adj::preimage_1d(i, m.N[0], m.g, m.per[0], neumann, lo, hi[0], pa);
-        const int nb = adj::preimage_1d(j, m.N[1], m.g, m.per[1], neumann, lo, hi[1], pb);
-        const int nc = adj::preimage_1d(k, m.N[2], m.g, m.per[2], neumann, lo, hi[2], pc);
-        double s = 0.0;
-        for (int c = 0; c < nc; ++c)
-            for (int b = 0; b < nb; ++b)
-                for (int a = 0; a < na; ++a)
-                    s += in[(long)(pa[a] - lo) + (long)(pb[b] - lo) * n0 + (long)(pc[c] - lo) * n0 * n1];
-        out[t] = s;
+    const long n0 = hi[0] - lo + 1, n1 = hi[1] - lo + 1;
+    const int x = blockIdx.x * FOLD_BX + threadIdx.x, y = blockIdx.y * FOLD_BY + threadIdx.y, z = blockIdx.z;
+    if (x >= n0 || y >= n1) return;
+    const int i = lo + x, j = lo + y, k = lo + z;
+    const long t = x + n0 * (y + n1 * z);
+    /* farther than g from every end no ghost copies the cell: it is its own only preimage */
+    if (i > m.g && i <= m.N[0] - m.g && j > m.g && j <= m.N[1] - m.g && k > m.g && k <= m.N[2] - m.g) {
+        out[t] = in[t];
+        return;
     }
+    int pa[adj::MAXPRE], pb[adj::MAXPRE], pc[adj::MAXPRE];
+    const int na = adj::preimage_1d(i, m.N[0], m.g, m.per[0], neumann, lo, hi[0], pa);
+    const int nb = adj::preimage_1d(j, m.N[1], m.g, m.per[1], neumann, lo, hi[1], pb);
+    const int nc = adj::preimage_1d(k, m.N[2], m.g, m.per[2], neumann, lo, hi[2], pc);
+    double s = 0.0;
+    for (int c = 0; c < nc; ++c)
+        for (int b = 0; b < nb; ++b)
+            for (int a = 0; a < na; ++a)
+                s += in[(long)(pa[a] - lo) + (long)(pb[b] - lo) * n0 + (long)(pc[c] - lo) * n0 * n1];
+    out[t] = s;
+}
+
+/* One thread per entry of a cell array (vf = 0) or of VF (vf = 1), (x, y) from the tile and the
+ * plane from the grid: no index divides. */
+void fold(const DevMesh& m, const double* in, double* out, int vf, int neumann, cudaStream_t s)
+{
+    const int ext = vf ? 3 : 0, lo = vf ? m.vlo : m.lo;
+    const int n0 = m.hi[0] + ext - lo + 1, n1 = m.hi[1] + ext - lo + 1, n2 = m.hi[2] + ext - lo + 1;
+    const dim3 grid((n0 + FOLD_BX - 1) / FOLD_BX, (n1 + FOLD_BY - 1) / FOLD_BY, n2);
+    k_adj_fold<<<grid, dim3(FOLD_BX, FOLD_BY), 0, s>>>(m, in, out, vf, neumann);
 }
 
 /* Cells outside the band: VFnew = VF, the derivative passes through.  Band cells with a
  * nonzero incoming derivative go to the list. */
-__global__ void k_adj_split(DevMesh m, const short* __restrict__ band, const double* __restrict__ gfold,
-                            double* __restrict__ gout, int* list, int* count)
+__global__ void __launch_bounds__(FOLD_BX * FOLD_BY) k_adj_split(DevMesh m, const short* __restrict__ band,
+                                                                 const double* __restrict__ gfold,
+                                                                 double* __restrict__ gout, int* list, int* count)
 {
-    const long total = (long)m.N[0] * m.N[1] * m.N[2];
-    for (long L = (long)blockIdx.x * blockDim.x + threadIdx.x; L < total; L += (long)gridDim.x * blockDim.x) {
-        const int i = 1 + (int)(L % m.N[0]), j = 1 + (int)((L / m.N[0]) % m.N[1]), k = 1 + (int)(L / ((long)m.N[0] * m.N[1]));
+    const int i = 1 + blockIdx.x * FOLD_BX + threadIdx.x, j = 1 + blockIdx.y * FOLD_BY + threadIdx.y;
+    const int k = 1 + blockIdx.z;
+    bool take = false;
+    int L = 0;
+    if (i <= m.N[0] && j <= m.N[1]) {
+        L = (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1];
         const long v = vidx(m, i, j, k);
         const double g = gfold[v];
         const int b = band[cidx(m, i, j, k)];
         const bool sl = (b < 0 ? -b : b) <= m.nband;
         if (!sl) gout[v] = g;
-        warp_append(sl && g != 0.0, (int)L, list, count);
+        take = sl && g != 0.0;
     }
+    warp_append(take, L, list, count);
 }
 
 /* ---- SL reverse in three kernels ------------------------------------------------------
@@ -253,12 +271,14 @@ __global__ void k_adj_elvira(DevMesh m, const double* __restrict__ VF, const sig
 
 void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s)
 {
-    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, gin, gout, 1, 1);
+    (void)nsm;
+    fold(m, gin, gout, 1, 1, s);
 }
 
 void launch_adjoint_fold_cell(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s)
 {
-    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, gin, gout, 0, 0);
+    (void)nsm;
+    fold(m, gin, gout, 0, 0, s);
 }
 
 void launch_adjoint_elvira(const DevMesh& m, const double* VF, const signed char* cand, const AdjBuffers& b, int nsm,
@@ -277,8 +297,9 @@ void launch_adjoint_head(const DevMesh& m, const short* band, const AdjBuffers& 
     cudaMemsetAsync(b.gD, 0, cbytes, s);
     cudaMemsetAsync(count, 0, sizeof(int), s);
     cudaMemsetAsync(count2, 0, sizeof(int), s);
-    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gin, b.gfold, 1, 1);
-    k_adj_split<<<nsm * 8, 256, 0, s>>>(m, band, b.gfold, b.gout, list, count);
+    fold(m, b.gin, b.gfold, 1, 1, s);
+    const dim3 grid((m.N[0] + FOLD_BX - 1) / FOLD_BX, (m.N[1] + FOLD_BY - 1) / FOLD_BY, m.N[2]);
+    k_adj_split<<<grid, dim3(FOLD_BX, FOLD_BY), 0, s>>>(m, band, b.gfold, b.gout, list, count);
 }
 
 void launch_adjoint_pre(const DevMesh& m, double dt, const double* uf, const double* vf, const double* wf,
@@ -301,9 +322,9 @@ void launch_adjoint_tail(const DevMesh& m, double dt, const double* VF, const do
     adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD, phase};
     k_adj_tet<<<nsm * 16, ADJ_SL_THREADS, 0, s>>>(m, P, b.cells, count2, b.tets, errw);
     k_adj_vert<<<nsm * 8, 128, 0, s>>>(m, dt, V, GV, b.cells, b.tets, count2, errw);
-    k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gD, b.gDf, 0, 0);
+    fold(m, b.gD, b.gDf, 0, 0, s);
     k_adj_dist<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, D, b.gDf, b.gn[0], b.gn[1], b.gn[2], b.gout, errw);
-    for (int q = 0; q < 3; ++q) k_adj_fold<<<nsm * 8, 256, 0, s>>>(m, b.gn[q], b.gnf[q], 0, 0);
+    for (int q = 0; q < 3; ++q) fold(m, b.gn[q], b.gnf[q], 0, 0, s);
     k_adj_elvira<<<nsm * 8, 256, 0, s>>>(m, VF, cand, b.gnf[0], b.gnf[1], b.gnf[2], b.gout);
 }
 
