@@ -3,6 +3,7 @@ restatement, with the reference's shape-error measure.
 
     python -m ns_multiphase_gb300.config_runs 2d [--steps 1024]   # 64^2 single vortex to t = T
     python -m ns_multiphase_gb300.config_runs 3d [--steps 8]      # 128^3 sphere deformation
+    python -m ns_multiphase_gb300.config_runs drift [--steps 64]  # 256^3 mass: FP64, FP64 on FP32 velocities, mixed
 
 2d: [0,1]^2, 64x64x1 (z periodic), circle r = 0.15 at (0.5, 0.75) by 10x10 sub-sampling,
     single-vortex face velocities sampled at the faces (period T = 8) at t_n + dt/2,
@@ -82,13 +83,45 @@ def run(which: str, steps: int | None = None, precision: str = "fp64", cpu: bool
     return out
 
 
+def drift(steps: int = 64):
+    """Mass after `steps` steps of the 256^3 benchmark workload (200 spheres, seed 20261203,
+    Deformation3D at t = dt/2, frozen, CFL 0.5) in three runs: the FP64 path, the FP64 path fed
+    the face velocities rounded to FP32 (the mixed path's input precision), and the mixed path.
+    Separates the effect of the FP32 velocity input from that of the FP32 geometry."""
+    from .slvof import SLVOF
+    m = Mesh(Nx=256, Ny=256, Nz=256, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    centres, radii = cases.config_spheres(200, 20261203)
+    dt = 0.5 * m.dx / 2.0
+    vel = cases.deformation3d_faces(m, 0.5 * dt, 3.0)
+    vel32 = tuple(a.astype(np.float32).astype(np.float64) for a in vel)
+    out = {"workload": "256^3, 200 spheres seed 20261203, Deformation3D T=3 at t=dt/2, CFL 0.5", "steps": steps}
+    for name, precision, v in (("fp64", "fp64", vel), ("fp64_on_fp32_velocities", "fp64", vel32),
+                               ("mixed", "mixed", vel)):
+        g = SLVOF(m, precision)
+        g.case_vf_spheres(centres, radii, nF=20, dims=3)
+        g.init_state()
+        g.upload_velocity(*v)
+        M0 = g.mass()
+        for _ in range(steps):
+            M = g.step(dt)
+        g.close()
+        out[name] = {"mass0": M0, "mass": M, "rel_change": abs(M - M0) / M0}
+    ref = out["fp64"]["mass"]
+    for name in ("fp64_on_fp32_velocities", "mixed"):
+        out[name]["rel_diff_vs_fp64"] = abs(out[name]["mass"] - ref) / abs(ref)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("config", choices=["2d", "3d"])
+    ap.add_argument("config", choices=["2d", "3d", "drift"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu", action="store_true")
     a = ap.parse_args()
+    if a.config == "drift":
+        print(json.dumps(drift(a.steps or 64)))
+        return
     print(json.dumps(run(a.config, a.steps, a.precision, not a.no_cpu)))
 
 
