@@ -107,23 +107,6 @@ __device__ __forceinline__ void form_child32(const Frame32& F, const CutCase* ta
     }
 }
 
-/* Phase code shared by every donor cell of an index box (+1 all liquid, -1 all gas, 0 mixed
- * or interface).  Boxes wider than 2 cells in some direction report 0. */
-__device__ __forceinline__ int box_phase(const DevMesh& m, const signed char* __restrict__ phase, int i0, int j0,
-                                         int k0, int lo0, int hi0, int lo1, int hi1, int lo2, int hi2)
-{
-    if (hi0 - lo0 > 1 || hi1 - lo1 > 1 || hi2 - lo2 > 1) return 0;
-    int ph = 2;
-    for (int c = lo2; c <= hi2; ++c)
-        for (int b = lo1; b <= hi1; ++b)
-            for (int a = lo0; a <= hi0; ++a) {
-                const int p = __ldg(phase + cidx(m, i0 + a, j0 + b, k0 + c));
-                if (p == 0 || (ph != 2 && p != ph)) return 0;
-                ph = p;
-            }
-    return ph;
-}
-
 /* Side of a point set against every donor PLIC plane of an index box (at most 2x2x2 cells):
  * +1 when every point is strictly on the liquid side of every donor's plane, -1 when strictly
  * on the gas side of every one, 0 otherwise.  Every PLIC leaf under a (sub-)tet with +1 is
