@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--n", type=int, default=256)
     p.add_argument("--fp64-steps", type=int, default=3)
     p.add_argument("--drift-steps", type=int, default=8)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--adj-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu", action="store_true")
@@ -381,16 +381,22 @@ def main():
         tw, hwf = pinned(wf, shp)
         tV, hVF = pinned(None, tuple(reversed(m.vf_shape)))
         ge = make_ctx(m, centres, radii, "mixed", 0.5 * dt, VF0)
-        ge.step_host(dt, huf, hvf, hwf, hVF)  # warm
+        for _ in range(max(3, args.warmup)):  # warm: first touches of the pinned buffers
+            ge.step_host(dt, huf, hvf, hwf, hVF)
         torch.cuda.synchronize()
+        per_step = []
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            ge.step_host(dt, huf, hvf, hwf, hVF)
+            t1 = time.perf_counter()
+            ge.step_host(dt, huf, hvf, hwf, hVF)  # synchronous: returns with VF on the host
+            per_step.append(time.perf_counter() - t1)
         e2e_s = time.perf_counter() - t0
         ge.close()
         e2e = {"value": cells * args.e2e_steps / e2e_s, "unit": "cell-updates/s",
                "h2d_bytes_per_step": int(3 * huf.nbytes), "d2h_bytes_per_step": int(hVF.nbytes + 8),
-               "api": "slvof_step_host (pinned host face velocities in, VF + mass out)"}
+               "api": "slvof_step_host (pinned host face velocities in, VF + mass out)",
+               "ms_per_step": {"mean": 1e3 * e2e_s / args.e2e_steps, "min": 1e3 * min(per_step),
+                               "median": 1e3 * statistics.median(per_step), "max": 1e3 * max(per_step)}}
 
         # ---- CPU restatement on a bounded slab ---------------------------------------------
         cpu = None
