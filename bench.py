@@ -71,6 +71,19 @@ def dist_env():
     return ws, rank, local
 
 
+def aggregate_rate(ms, cells, steps, ws, device):
+    """Whole-job throughput of ws replicas, each advancing `cells` cells `steps` steps: every
+    rank's cells over the slowest rank's time (all-reduce MAX of the per-rank milliseconds on
+    `device`: "cuda" under NCCL, "cpu" under gloo).  Returns (cell-updates/s, ms)."""
+    if ws > 1:
+        import torch
+        import torch.distributed as tdist
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ws * cells * steps / (ms / 1e3), ms
+
+
 def workload(n):
     from ns_multiphase_gb300 import cases
     from ns_multiphase_gb300.mesh import Mesh
@@ -322,11 +335,7 @@ def main():
         ms, stage = timed_steps(g, dt, args.steps, torch)
     clocks = ck.summary()
     counters = g.counters()
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * cells * args.steps / (ms / 1e3)
+    value, ms = aggregate_rate(ms, cells, args.steps, ws, "cuda")
     ms_step = ms / args.steps
     g.close()
 
