@@ -282,10 +282,15 @@ __global__ void __launch_bounds__(PURE_BX * PURE_BY) k_sl_classify(DevMesh m, co
     warp_append(sl, L, list, count);
 }
 
+/* FP64 array to FP32 times a scale (face velocities to cells per unit time): the conversion
+ * first and the scale in FP32, so that only the conversion issues on GB300's narrow FP64 pipe
+ * (with the double multiply as well the kernel was FP64-bound at 2.7 TB/s).  For a power-of-two
+ * scale, 1/dx on a 2^k grid of a unit box, the result equals the rounded double product. */
 __global__ void k_to_float(const double* __restrict__ a, float* __restrict__ b, long n, double scale)
 {
+    const float s = (float)scale;
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
-        b[t] = (float)(a[t] * scale);
+        b[t] = __double2float_rn(a[t]) * s;
 }
 
 /* ---- synthetic inputs ------------------------------------------------------------------
