@@ -476,7 +476,11 @@ def main():
                "accuracy": {"steps": args.drift_steps, "mass_rel_diff_mixed_vs_fp64": drift_vs_fp64,
                             "max_abs_dVF_mixed_vs_fp64": dVF, "mass_rel_change_fp64": abs(m64 - M0) / M0},
                "adjoint": adjoint,
-               "stages_ms": stage, "work_lists": counters, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+               "stages_ms": stage,
+               "stages_note": "CUDA events per stage on the stream each stage runs on; the band runs on a second "
+                              "stream beside elvira_candidates and plic, so its span overlaps theirs and the "
+                              "stages sum to more than ms_per_step",
+               "work_lists": counters, "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                "gpu_launches": launches_per_step(m) * args.steps}
         print(json.dumps(out), flush=True)
     if ws > 1:
