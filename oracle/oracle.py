@@ -63,6 +63,8 @@ def lib():
         L.orc_ndual.argtypes = []
         L.orc_sl_forward.restype = i
         L.orc_sl_forward.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p, p, p]
+        L.orc_rollout_forward.restype = i
+        L.orc_rollout_forward.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p]
         L.orc_count_ops.restype = i
         L.orc_count_ops.argtypes = [p, d, p, p, p, p, p, p, p, p, i, p, i, p, p, p]
         L.orc_curvature.restype = i
@@ -196,6 +198,29 @@ class Oracle:
 
     def ndual(self):
         return self.L.orc_ndual()
+
+    def rollout_forward(self, dt, steps, VF0, uf, vf, wf, face_seeds, vf_seeds, w):
+        """Forward-mode derivatives of L = sum(w * VF_T) over a `steps`-step rollout from VF0
+        (initial state and every step's normals, PLIC and band included) with frozen face
+        velocities.  face_seeds: (array 0/1/2, parent index) face entries; vf_seeds: parent
+        indices of VF0 entries; at most ndual() together.  Returns (L, dL per seed)."""
+        m = self.mesh
+        K = self.L.orc_ndual()
+        assert len(face_seeds) + len(vf_seeds) <= K
+        slots = [np.full(m.cell_shape, -1, dtype=np.int32, order="F") for _ in range(3)]
+        for s, (a, idx) in enumerate(face_seeds):
+            slots[a][idx] = s
+        svf = np.full(m.vf_shape, -1, dtype=np.int32, order="F")
+        for s, idx in enumerate(vf_seeds):
+            svf[idx] = len(face_seeds) + s
+        wv = np.ascontiguousarray(np.asarray(w, dtype=np.float64).ravel(order="F"))
+        Lv = ctypes.c_double()
+        dL = np.zeros(K)
+        f = self.L.orc_rollout_forward(_m(m), dt, steps, _p(VF0), _p(uf), _p(vf), _p(wf), *[_p(x) for x in slots],
+                                       _p(svf), wv.ctypes.data, ctypes.byref(Lv), dL.ctypes.data)
+        if f:
+            raise RuntimeError(f"restatement flags {f}")
+        return Lv.value, dL[:len(face_seeds) + len(vf_seeds)]
 
     def count_ops(self, dt, VF, uf, vf, wf, nx, ny, nz, D, if_cells, band_cells, values=False):
         """Algorithmic operation counts of a step's per-cell parts (each +, -, *, / and each

@@ -121,6 +121,30 @@ inline Cnt f_sin(const Cnt& x) { ++g_nops; return Cnt(detm_sin(x.v)); }
 inline Cnt f_cos(const Cnt& x) { ++g_nops; return Cnt(detm_cos(x.v)); }
 inline Cnt f_abs(const Cnt& x) { return Cnt(std::fabs(x.v)); }
 
+/* The same for Dual: comparisons on the value, derivatives of the math functions. */
+inline Dual& operator-=(Dual& a, const Dual& b) { a = a - b; return a; }
+inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+inline Dual dual_chain(double v, const Dual& a, double dv)
+{
+    Dual r(v);
+    for (int q = 0; q < NDUAL; ++q) r.d[q] = a.d[q] * dv;
+    return r;
+}
+inline Dual f_sqrt(const Dual& x) { const double v = std::sqrt(x.v); return dual_chain(v, x, 0.5 / v); }
+inline Dual f_cbrt(const Dual& x) { const double v = detm_cbrt(x.v); return dual_chain(v, x, 1.0 / (3.0 * v * v)); }
+inline Dual f_acos(const Dual& x) { return dual_chain(detm_acos(x.v), x, -1.0 / std::sqrt(1.0 - x.v * x.v)); }
+inline Dual f_sin(const Dual& x) { return dual_chain(detm_sin(x.v), x, detm_cos(x.v)); }
+inline Dual f_cos(const Dual& x) { return dual_chain(detm_cos(x.v), x, -detm_sin(x.v)); }
+inline Dual f_abs(const Dual& x) { return x.v < 0.0 ? -x : x; }
+
+/* Result stores of the generic paths. */
+inline void store(double& o, double x) { o = x; }
+inline void store(double& o, const Cnt& x) { o = x.v; }
+inline void store(Dual& o, const Dual& x) { o = x; }
+
 /* Julia min/max on Float64: NaN-propagating. */
 template <class R>
 inline R jmax(const R& a, const R& b)
@@ -473,15 +497,17 @@ void update_borders(const Grid& G, Arr3<T>& A)
 /* ---------------------------------------------------------------------------------------
  * ELVIRA, src/ELVIRA.jl:6-137.
  * ------------------------------------------------------------------------------------- */
-struct Fields {
+template <class T>
+struct FieldsT {
     const Grid* G;
-    const double* VF;
-    double VFat(int i, int j, int k) const { return VF[G->v(i, j, k)]; }
+    const T* VF;
+    T VFat(int i, int j, int k) const { return VF[G->v(i, j, k)]; }
 };
+using Fields = FieldsT<double>;
 
-template <class R>
-void check_normal(const Grid& G, const Fields& F, R& err, R nx_, R ny_, R nz_, double* nx, double* ny, double* nz,
-                  int i, int j, int k, Err* e)
+template <class R, class FT, class OT>
+void check_normal(const Grid& G, const FT& F, R& err, R nx_, R ny_, R nz_, OT* nx, OT* ny, OT* nz, int i, int j,
+                  int k, Err* e)
 {
     R err_(0.0);
     const R norm = f_sqrt((nx_ * nx_ + ny_ * ny_) + nz_ * nz_);
@@ -494,15 +520,15 @@ void check_normal(const Grid& G, const Fields& F, R& err, R nx_, R ny_, R nz_, d
                 const R r = R(F.VFat(ii, jj, kk)) - VF_;
                 err_ += r * r;
             }
-    if (err_ < err) {
+    if (val(err_) < val(err)) {
         err = err_;
         const long c = G.c(i, j, k);
-        nx[c] = val(nx_); ny[c] = val(ny_); nz[c] = val(nz_);
+        store(nx[c], nx_); store(ny[c], ny_); store(nz[c], nz_);
     }
 }
 
-template <class R = double>
-void elvira_calc(const Grid& G, const Fields& F, double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
+template <class R = double, class FT = Fields, class OT = double>
+void elvira_calc(const Grid& G, const FT& F, OT* nx, OT* ny, OT* nz, int i, int j, int k, Err* e)
 {
     const orc_mesh* M = G.m;
     R err(INFINITY);
@@ -518,8 +544,8 @@ void elvira_calc(const Grid& G, const Fields& F, double* nx, double* ny, double*
                 const R s2y = (V(i, jj2, k - 1) * M->dz + V(i, jj2, k) * M->dz) + V(i, jj2, k + 1) * M->dz;
                 const R s1y = (V(i, jj1, k - 1) * M->dz + V(i, jj1, k) * M->dz) + V(i, jj1, k + 1) * M->dz;
                 const R ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
-                const R nz_ = V(i, j, k + 1) > V(i, j, k - 1) ? R(-1.0) : R(1.0);
-                check_normal<R>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+                const R nz_ = val(V(i, j, k + 1)) > val(V(i, j, k - 1)) ? R(-1.0) : R(1.0);
+                check_normal<R, FT, OT>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
             }
     }
     if (M->Ny > 1) {
@@ -529,51 +555,53 @@ void elvira_calc(const Grid& G, const Fields& F, double* nx, double* ny, double*
                 const R s2x = (V(ii2, j - 1, k) * M->dy + V(ii2, j, k) * M->dy) + V(ii2, j + 1, k) * M->dy;
                 const R s1x = (V(ii1, j - 1, k) * M->dy + V(ii1, j, k) * M->dy) + V(ii1, j + 1, k) * M->dy;
                 const R nx_ = -(s2x - s1x) / (G.xm(ii2) - G.xm(ii1));
-                const R ny_ = V(i, j + 1, k) > V(i, j - 1, k) ? R(-1.0) : R(1.0);
+                const R ny_ = val(V(i, j + 1, k)) > val(V(i, j - 1, k)) ? R(-1.0) : R(1.0);
                 const R s2z = (V(i, j - 1, kk2) * M->dy + V(i, j, kk2) * M->dy) + V(i, j + 1, kk2) * M->dy;
                 const R s1z = (V(i, j - 1, kk1) * M->dy + V(i, j, kk1) * M->dy) + V(i, j + 1, kk1) * M->dy;
                 const R nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
-                check_normal<R>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+                check_normal<R, FT, OT>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
             }
     }
     if (M->Nx > 1) {
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
                 const int kk1 = k + P[a][0], kk2 = k + P[a][1], jj1 = j + P[b][0], jj2 = j + P[b][1];
-                const R nx_ = V(i + 1, j, k) > V(i - 1, j, k) ? R(-1.0) : R(1.0);
+                const R nx_ = val(V(i + 1, j, k)) > val(V(i - 1, j, k)) ? R(-1.0) : R(1.0);
                 const R s2y = (V(i - 1, jj2, k) * M->dx + V(i, jj2, k) * M->dx) + V(i + 1, jj2, k) * M->dx;
                 const R s1y = (V(i - 1, jj1, k) * M->dx + V(i, jj1, k) * M->dx) + V(i + 1, jj1, k) * M->dx;
                 const R ny_ = -(s2y - s1y) / (G.ym(jj2) - G.ym(jj1));
                 const R s2z = (V(i - 1, j, kk2) * M->dx + V(i, j, kk2) * M->dx) + V(i + 1, j, kk2) * M->dx;
                 const R s1z = (V(i - 1, j, kk1) * M->dx + V(i, j, kk1) * M->dx) + V(i + 1, j, kk1) * M->dx;
                 const R nz_ = -(s2z - s1z) / (G.zm(kk2) - G.zm(kk1));
-                check_normal<R>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
+                check_normal<R, FT, OT>(G, F, err, nx_, ny_, nz_, nx, ny, nz, i, j, k, e);
             }
     }
 }
 
-void elvira_cell(const Grid& G, const Fields& F, double* nx, double* ny, double* nz, int i, int j, int k, Err* e)
+template <class R = double, class FT = Fields, class OT = double>
+void elvira_cell(const Grid& G, const FT& F, OT* nx, OT* ny, OT* nz, int i, int j, int k, Err* e)
 {
     const orc_mesh* M = G.m;
     const double lo = M->VFlo, hi = M->VFhi;
-    const double v = F.VFat(i, j, k);
+    auto V = [&](int a, int b, int c) { return val(F.VFat(a, b, c)); };
+    const double v = V(i, j, k);
     const long c = G.c(i, j, k);
     if (v >= lo && v <= hi) {
-        elvira_calc(G, F, nx, ny, nz, i, j, k, e);
+        elvira_calc<R, FT, OT>(G, F, nx, ny, nz, i, j, k, e);
     } else if (v < lo) {
-        if (F.VFat(i - 1, j, k) > hi) nx[c] = 1;
-        else if (F.VFat(i + 1, j, k) > hi) nx[c] = -1;
-        else if (F.VFat(i, j - 1, k) > hi) ny[c] = 1;
-        else if (F.VFat(i, j + 1, k) > hi) ny[c] = -1;
-        else if (F.VFat(i, j, k - 1) > hi) nz[c] = 1;
-        else if (F.VFat(i, j, k + 1) > hi) nz[c] = -1;
+        if (V(i - 1, j, k) > hi) nx[c] = 1;
+        else if (V(i + 1, j, k) > hi) nx[c] = -1;
+        else if (V(i, j - 1, k) > hi) ny[c] = 1;
+        else if (V(i, j + 1, k) > hi) ny[c] = -1;
+        else if (V(i, j, k - 1) > hi) nz[c] = 1;
+        else if (V(i, j, k + 1) > hi) nz[c] = -1;
     } else if (v > hi) {
-        if (F.VFat(i - 1, j, k) < lo) nx[c] = -1;
-        else if (F.VFat(i + 1, j, k) < lo) nx[c] = 1;
-        else if (F.VFat(i, j - 1, k) < lo) ny[c] = -1;
-        else if (F.VFat(i, j + 1, k) < lo) ny[c] = 1;
-        else if (F.VFat(i, j, k - 1) < lo) nz[c] = -1;
-        else if (F.VFat(i, j, k + 1) < lo) nz[c] = 1;
+        if (V(i - 1, j, k) < lo) nx[c] = -1;
+        else if (V(i + 1, j, k) < lo) nx[c] = 1;
+        else if (V(i, j - 1, k) < lo) ny[c] = -1;
+        else if (V(i, j + 1, k) < lo) ny[c] = 1;
+        else if (V(i, j, k - 1) < lo) nz[c] = -1;
+        else if (V(i, j, k + 1) < lo) nz[c] = 1;
     }
 }
 
@@ -700,7 +728,9 @@ inline void pt2index(const Grid& G, int I[3], const Dual pt[3], int i, int j, in
 /* ---------------------------------------------------------------------------------------
  * cutTet, src/VFgeom.jl:713-900, kept recursive as in the reference.
  * ------------------------------------------------------------------------------------- */
-struct Plic { const double *nx, *ny, *nz, *D; };
+template <class T>
+struct PlicT { const T *nx, *ny, *nz, *D; };
+using Plic = PlicT<double>;
 /* cell-centred velocities and densities for the momentum sums of transport! (may be absent) */
 struct Mom { const double *u, *v, *w; double rho_liq, rho_gas; };
 
@@ -708,8 +738,8 @@ template <class R>
 struct CutOutT { R vol, vLiq, vrhoU, vrhoV, vrhoW, vrho; };
 using CutOut = CutOutT<double>;
 
-template <class R>
-CutOutT<R> cut_tet(const Grid& G, const Plic& P, const Mom* M, R tet[4][3], int ind[4][3], bool xdone, bool ydone,
+template <class R, class PT = Plic>
+CutOutT<R> cut_tet(const Grid& G, const PT& P, const Mom* M, R tet[4][3], int ind[4][3], bool xdone, bool ydone,
                bool zdone, int lvl, Err* e)
 {
     if (lvl > 64) { e->flags |= E_DEPTH; return {R(0.0), R(0.0), R(0.0), R(0.0), R(0.0), R(0.0)}; }
@@ -819,7 +849,7 @@ CutOutT<R> cut_tet(const Grid& G, const Plic& P, const Mom* M, R tet[4][3], int 
                 ci[nn][p] = vind[vt][p][side];
             }
         }
-        const CutOutT<R> r = cut_tet<R>(G, P, M, ct, ci, xdone, ydone, zdone, lvl + 1, e);
+        const CutOutT<R> r = cut_tet<R, PT>(G, P, M, ct, ci, xdone, ydone, zdone, lvl + 1, e);
         acc.vol += r.vol;
         acc.vLiq += r.vLiq;
         acc.vrhoU += r.vrhoU;
@@ -835,8 +865,8 @@ void correction_tets(const Grid& G, const Vel& V, int i, int j, int k, double dt
 
 /* SL update of one cell, src/Transport.jl:111-148 with cell2tets!(project_verts=true,
  * compute_indices=true) (src/VFgeom.jl:345-420). Returns VFnew. */
-template <class R = double>
-R sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, int k, Err* e, double* vol_out,
+template <class R = double, class PT = Plic>
+R sl_cell(const Grid& G, const Vel& V, const PT& P, double dt, int i, int j, int k, Err* e, double* vol_out,
           const Mom* M = nullptr, double* mom_out = nullptr)
 {
     double v0[15][3];
@@ -861,7 +891,7 @@ R sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, i
                 tet[n][p] = verts[tv[n]][p];
                 ind[n][p] = vInds[tv[n]][p];
             }
-        const CutOutT<R> r = cut_tet<R>(G, P, M, tet, ind, false, false, false, 1, e);
+        const CutOutT<R> r = cut_tet<R, PT>(G, P, M, tet, ind, false, false, false, 1, e);
         vol += tetsign * r.vol;
         vLiq += tetsign * r.vLiq;
         vrhoU += tetsign * r.vrhoU;
@@ -877,7 +907,7 @@ R sl_cell(const Grid& G, const Vel& V, const Plic& P, double dt, int i, int j, i
         for (int t = 0; t < 12; ++t) {
             int ind[4][3];
             for (int n = 0; n < 4; ++n) pt2index(G, ind[n], ct[t][n], i, j, k, e);
-            const CutOutT<R> r = cut_tet<R>(G, P, M, ct[t], ind, false, false, false, 1, e);
+            const CutOutT<R> r = cut_tet<R, PT>(G, P, M, ct[t], ind, false, false, false, 1, e);
             vol += tetsign * r.vol;
             vLiq += tetsign * r.vLiq;
             vrhoU += tetsign * r.vrhoU;
@@ -1448,6 +1478,85 @@ int orc_props(const orc_mesh* M, const double* VF, double rho_liq, double rho_ga
  * to up to orc_ndual() face velocities, selected by the slot arrays su, sv, sw (cell-array
  * shaped: the derivative slot of each face value, -1 for none).  grad is ncells x orc_ndual(). */
 int orc_ndual() { return NDUAL; }
+
+/* Forward-mode derivatives of a rollout, the CPU analogue of a ForwardDiff.jl gradient of
+ * run_solver's transport loop: from VF0, the initial state (Neumann + VF borders,
+ * computeBand!, computeNormal!, computePLIC!), then `steps` steps (SL update of the band cells,
+ * VF copy and ghost fill, normals, PLIC and band again), every value a Dual.  Up to NDUAL
+ * directions are seeded: face values of the frozen velocities (su/sv/sw: the slot of each
+ * parent entry, -1 none) and entries of VF0 (sVF, same convention, VF layout).  The band is
+ * recomputed from the values, as it switches discretely.  L = sum of w * VF_T over the
+ * interior (w: Nx*Ny*Nz, i fastest); dL[q] its derivative along direction q. */
+int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* VF0, const double* uf,
+                        const double* vf, const double* wf, const int* su, const int* sv, const int* sw,
+                        const int* sVF, const double* w, double* L, double* dL)
+{
+    Grid G(M);
+    const long nvf = (long)G.vn[0] * G.vn[1] * G.vn[2], ncell = (long)G.n[0] * G.n[1] * G.n[2];
+    std::vector<Dual> VF(nvf), VFn(nvf), nx(ncell), ny(ncell), nz(ncell), D(ncell);
+    std::vector<double> vfv(nvf);
+    std::vector<int16_t> band(ncell);
+    for (long t = 0; t < nvf; ++t) {
+        VF[t] = Dual(VF0[t]);
+        if (sVF && sVF[t] >= 0) VF[t].d[sVF[t]] = 1.0;
+    }
+    Err e;
+    auto ghost = [&]() {
+        Arr3<Dual> A(VF.data(), G.vlo, G.vhi);
+        neumann(G, A);
+        update_borders(G, A);
+    };
+    auto geometry = [&](bool do_band) {
+        for (long t = 0; t < nvf; ++t) vfv[t] = VF[t].v;
+        if (do_band) orc_compute_band(M, band.data(), vfv.data());
+        std::fill(nx.begin(), nx.end(), Dual(0.0));
+        std::fill(ny.begin(), ny.end(), Dual(0.0));
+        std::fill(nz.begin(), nz.end(), Dual(0.0));
+        FieldsT<Dual> F{&G, VF.data()};
+        for (int k = 1; k <= G.N[2]; ++k)
+            for (int j = 1; j <= G.N[1]; ++j)
+                for (int i = 1; i <= G.N[0]; ++i)
+                    elvira_cell<Dual, FieldsT<Dual>, Dual>(G, F, nx.data(), ny.data(), nz.data(), i, j, k, &e);
+        Arr3<Dual> A(nx.data(), G.lo, G.hi), B(ny.data(), G.lo, G.hi), C(nz.data(), G.lo, G.hi);
+        update_borders(G, A); update_borders(G, B); update_borders(G, C);
+        for (int k = G.lo[2]; k <= G.hi[2]; ++k)
+            for (int j = G.lo[1]; j <= G.hi[1]; ++j)
+                for (int i = G.lo[0]; i <= G.hi[0]; ++i) {
+                    const long c = G.c(i, j, k);
+                    D[c] = compute_dist<Dual>(G, i, j, k, nx[c], ny[c], nz[c], VF[G.v(i, j, k)]);
+                }
+        Arr3<Dual> Dd(D.data(), G.lo, G.hi);
+        update_borders(G, Dd);
+    };
+    ghost();
+    geometry(true);
+    Vel V{uf, vf, wf, su, sv, sw};
+    for (int s = 0; s < steps; ++s) {
+        PlicT<Dual> P{nx.data(), ny.data(), nz.data(), D.data()};
+        for (int k = 1; k <= G.N[2]; ++k)
+            for (int j = 1; j <= G.N[1]; ++j)
+                for (int i = 1; i <= G.N[0]; ++i) {
+                    const long c = G.c(i, j, k), v = G.v(i, j, k);
+                    if (std::abs((int)band[c]) <= M->nband)
+                        VFn[v] = sl_cell<Dual, PlicT<Dual>>(G, V, P, dt, i, j, k, &e, nullptr);
+                    else
+                        VFn[v] = VF[v];
+                }
+        for (int k = 1; k <= G.N[2]; ++k)
+            for (int j = 1; j <= G.N[1]; ++j)
+                for (int i = 1; i <= G.N[0]; ++i) VF[G.v(i, j, k)] = VFn[G.v(i, j, k)];
+        ghost();
+        geometry(true);
+    }
+    Dual acc(0.0);
+    long q = 0;
+    for (int k = 1; k <= G.N[2]; ++k)
+        for (int j = 1; j <= G.N[1]; ++j)
+            for (int i = 1; i <= G.N[0]; ++i, ++q) acc = acc + Dual(w[q]) * VF[G.v(i, j, k)];
+    *L = acc.v;
+    for (int d = 0; d < NDUAL; ++d) dL[d] = acc.d[d];
+    return e.flags;
+}
 
 /* Algorithmic operation counts (see Cnt) of one step's per-cell parts, summed over the given
  * cells (interior cells as linear indices (i-1) + Nx*((j-1) + Ny*(k-1))), on one thread:

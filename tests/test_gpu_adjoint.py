@@ -349,3 +349,46 @@ def forward_mode_check(mesh_vf, precision, tol):
     fwd = forward_mode_grads(o, st, cells, weights, entries)
     rev = np.array([grads[a][idx] for a, idx in entries])
     assert np.max(np.abs(fwd - rev)) <= tol * np.max(np.abs(fwd))
+
+
+def test_rollout_against_forward_mode(built):
+    """The FP64 reverse of a 3-step rollout (checkpoint every step) against forward-mode
+    derivatives of the restatement's whole rollout (Dual numbers through the initial state and
+    every step's SL update, normals, PLIC and band: the analogue of a ForwardDiff.jl gradient of
+    the transport loop), on 12^3 with the velocities frozen over the rollout.  The entries are
+    the 32 largest face-velocity derivatives and 16 interface entries of VF0, whose derivatives
+    run back through every step's ELVIRA and plane-constant solve to the initial state's.  The
+    FP64 path is the restatement bit for bit, so both take the same branches and agree to
+    rounding."""
+    m, VF0 = sphere3d(12)
+    dt = 0.5 * m.dx / 2.0
+    steps = 3
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + 0.5 * dt, 3.0)
+    vel, _ = noisy(m, base, 0.05, 23)
+    w = np.random.default_rng(8).standard_normal((m.Nx, m.Ny, m.Nz))
+    L, gVF0, gu, gv, gw = gpu_gradients(m, VF0, vel, dt, steps, w, every=1, precision="fp64")
+    o = Oracle(m)
+    uf, vf, wf = vel(0)
+    grads = (gu, gv, gw)
+    entries = [(a, tuple(int(x) for x in idx)) for a in range(3) for idx in np.argwhere(grads[a] != 0.0)]
+    entries.sort(key=lambda e: -abs(grads[e[0]][e[1]]))
+    faces = entries[:32]
+    g3 = m.nghost + 3
+    vfi = m.interior(VF0)
+    iface = np.argwhere((vfi > 0.02) & (vfi < 0.98))
+    cells = [tuple(int(x) for x in iface[q]) for q in np.linspace(0, len(iface) - 1, 16).astype(int)]
+    K = o.ndual()
+    fwd, rev = [], []
+    for c0 in range(0, len(faces), K):
+        batch = faces[c0:c0 + K]
+        Lo, dL = o.rollout_forward(dt, steps, VF0, uf, vf, wf, batch, [], w)
+        fwd += list(dL)
+        rev += [grads[a][idx] for a, idx in batch]
+    assert abs(L - Lo) <= 1e-12 * max(1.0, abs(Lo))
+    parents = [tuple(q + g3 for q in c) for c in cells]
+    Lo, dL = o.rollout_forward(dt, steps, VF0, uf, vf, wf, [], parents, w)
+    fwd += list(dL)
+    rev += [gVF0[p] for p in parents]  # the derivative comes back in VF layout
+    fwd, rev = np.array(fwd), np.array(rev)
+    assert np.max(np.abs(fwd[32:])) > 0
+    assert np.max(np.abs(fwd - rev)) <= 1e-9 * np.max(np.abs(fwd)), np.max(np.abs(fwd - rev)) / np.max(np.abs(fwd))
