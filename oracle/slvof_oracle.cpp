@@ -53,10 +53,12 @@ namespace {
 
 const double EPS = 2.220446049250313e-16; /* Julia eps() */
 
-/* Forward-mode dual numbers for the derivative checks: the SL path below is written for a
- * generic scalar, instantiated with double (the restatement) and with Dual (value plus K
- * directional derivatives, the CPU analogue of ForwardDiff.jl's Dual).  Branches and
- * comparisons use the value; the double instantiation is the plain restatement. */
+/* Forward-mode dual numbers for the derivative checks: the SL path, ELVIRA and the plane-
+ * constant solve below are written for a generic scalar, instantiated with double (the
+ * restatement), with Dual (value plus K directional derivatives, the CPU analogue of
+ * ForwardDiff.jl's Dual; orc_sl_forward, orc_rollout_forward) and with Cnt (the operation
+ * count, orc_count_ops).  Branches and comparisons use the value; the double instantiation is
+ * the plain restatement. */
 constexpr int NDUAL = 16;
 struct Dual {
     double v = 0.0;
