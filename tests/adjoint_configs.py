@@ -1,7 +1,7 @@
 """The two adjoint configurations of the SL-VOF path, with their finite-difference checks.
 
-    python -m ns_multiphase_gb300.adjoint_configs 2d [--fd 64]      # 256^2, 40 steps
-    python -m ns_multiphase_gb300.adjoint_configs 3d [--fd 16] [--precision mixed]
+    python tests/adjoint_configs.py 2d [--fd 64]      # 256^2, 40 steps
+    python tests/adjoint_configs.py 3d [--fd 16] [--precision mixed]
 
 2d: single-vortex deformation on 256x256 (Nz = 1, z periodic), circle r = 0.15 at
     (0.5, 0.75) by 10x10 sub-sampling, stream-function face velocities (period T = 8) at
@@ -22,14 +22,19 @@ those with a nonzero derivative (the rest are exactly zero on both sides).
 """
 from __future__ import annotations
 
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
 import argparse
 import json
 import time
 
 import numpy as np
 
-from . import cases
-from .mesh import Mesh
+from ns_multiphase_gb300 import cases
+from ns_multiphase_gb300.mesh import Mesh
 
 SEED = 20261203
 H = 1e-6
@@ -90,7 +95,7 @@ def rollout_cpu(cfg, p):
 
 
 def rollout_gpu(cfg, p, precision="fp64"):
-    from .slvof import SLVOF
+    from ns_multiphase_gb300.slvof import SLVOF
     g = SLVOF(cfg.mesh, precision)
     g.upload_vf(cfg.VF0)
     g.vf_ghost_fill()
@@ -110,8 +115,8 @@ def loss(cfg, VF):
 
 def gradient(cfg, precision="fp64"):
     """(loss, dL/dp, timings) by the library's reverse pass."""
-    from .adjoint import Rollout
-    from .slvof import SLVOF
+    from ns_multiphase_gb300.adjoint import Rollout
+    from ns_multiphase_gb300.slvof import SLVOF
     m = cfg.mesh
     g = SLVOF(m, precision)
     g.upload_vf(cfg.VF0)

@@ -1,9 +1,9 @@
 """The two FP64 transport configurations at their own sizes, on the GPU path and on the CPU
 restatement, with the reference's shape-error measure.
 
-    python -m ns_multiphase_gb300.config_runs 2d [--steps 1024]   # 64^2 single vortex to t = T
-    python -m ns_multiphase_gb300.config_runs 3d [--steps 8]      # 128^3 sphere deformation
-    python -m ns_multiphase_gb300.config_runs drift [--steps 64]  # 256^3 mass: FP64, FP64 on FP32 velocities, mixed
+    python tests/config_runs.py 2d [--steps 1024]   # 64^2 single vortex to t = T
+    python tests/config_runs.py 3d [--steps 8]      # 128^3 sphere deformation
+    python tests/config_runs.py drift [--steps 64]  # 256^3 mass: FP64, FP64 on FP32 velocities, mixed
 
 2d: [0,1]^2, 64x64x1 (z periodic), circle r = 0.15 at (0.5, 0.75) by 10x10 sub-sampling,
     single-vortex face velocities sampled at the faces (period T = 8) at t_n + dt/2,
@@ -19,14 +19,19 @@ relative volume change over the run, and the shape error sum|VF_T - VF_0| / N_ce
 """
 from __future__ import annotations
 
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
 import argparse
 import json
 import time
 
 import numpy as np
 
-from . import cases
-from .mesh import Mesh
+from ns_multiphase_gb300 import cases
+from ns_multiphase_gb300.mesh import Mesh
 
 
 def config2d():
@@ -46,7 +51,7 @@ def config3d():
 
 
 def run(which: str, steps: int | None = None, precision: str = "fp64", cpu: bool = True):
-    from .slvof import SLVOF
+    from ns_multiphase_gb300.slvof import SLVOF
     m, VF0, dt, vel, full = config2d() if which == "2d" else config3d()
     steps = full if steps is None else steps
     g = SLVOF(m, precision)
@@ -88,7 +93,7 @@ def drift(steps: int = 64):
     Deformation3D at t = dt/2, frozen, CFL 0.5) in three runs: the FP64 path, the FP64 path fed
     the face velocities rounded to FP32 (the mixed path's input precision), and the mixed path.
     Separates the effect of the FP32 velocity input from that of the FP32 geometry."""
-    from .slvof import SLVOF
+    from ns_multiphase_gb300.slvof import SLVOF
     m = Mesh(Nx=256, Ny=256, Nz=256, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
     centres, radii = cases.config_spheres(200, 20261203)
     dt = 0.5 * m.dx / 2.0

@@ -272,11 +272,11 @@ def test_mixed_reverse_with_the_step_result_given(built):
 
 @pytest.mark.parametrize("which", ["2d", "3d"])
 def test_adjoint_configurations_at_reduced_size(built, which):
-    """The two adjoint configurations (ns_multiphase_gb300.adjoint_configs) at reduced size,
+    """The two adjoint configurations (tests/adjoint_configs.py) at reduced size,
     checked against central differences of the CPU restatement on random entries of the
     derivative's support: 2D 32^2 vortex + noise on every face (8 steps, checkpoint every 3),
     3D 16^3 deformation + curl of the 3 x 512-coefficient potential (4 steps, every 2)."""
-    from ns_multiphase_gb300 import adjoint_configs as A
+    import adjoint_configs as A
     if which == "2d":
         cfg = A.config2d(N=32, steps=8, every=3)
         out = A.check(cfg, 12, "cpu")

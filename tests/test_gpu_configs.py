@@ -1,6 +1,6 @@
 """The FP64 path at the transport configurations' own sizes against the CPU restatement, bit
 for bit: the 2D single vortex on 64^2 run to t = T (1024 steps) and the 3D sphere deformation on
-128^3 for 6 steps (ns_multiphase_gb300.config_runs)."""
+128^3 for 6 steps (tests/config_runs.py)."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -18,7 +18,7 @@ def built():
 
 @pytest.mark.parametrize("which,steps", [("2d", None), ("3d", 6)])
 def test_configuration_bit_identical(built, which, steps):
-    from ns_multiphase_gb300.config_runs import run
+    from config_runs import run
     out = run(which, steps)
     assert out["bit_identical"], out
     assert out["max_abs_dVF_vs_restatement"] <= 1e-12
