@@ -64,7 +64,7 @@ def lib():
         L.orc_sl_forward.restype = i
         L.orc_sl_forward.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p, p, p]
         L.orc_rollout_forward.restype = i
-        L.orc_rollout_forward.argtypes = [p, d, i, p, p, p, p, p, p, p, p, p, p, p]
+        L.orc_rollout_forward.argtypes = [p, d, i, i, p, p, p, p, p, p, p, p, p, p, p]
         L.orc_count_ops.restype = i
         L.orc_count_ops.argtypes = [p, d, p, p, p, p, p, p, p, p, i, p, i, p, p, p]
         L.orc_curvature.restype = i
@@ -201,10 +201,15 @@ class Oracle:
 
     def rollout_forward(self, dt, steps, VF0, uf, vf, wf, face_seeds, vf_seeds, w):
         """Forward-mode derivatives of L = sum(w * VF_T) over a `steps`-step rollout from VF0
-        (initial state and every step's normals, PLIC and band included) with frozen face
-        velocities.  face_seeds: (array 0/1/2, parent index) face entries; vf_seeds: parent
-        indices of VF0 entries; at most ndual() together.  Returns (L, dL per seed)."""
+        (initial state and every step's normals, PLIC and band included).  uf, vf, wf: arrays
+        (frozen velocities) or lists of per-step arrays.  face_seeds: (array 0/1/2, parent index)
+        face entries, the same entry of every step's velocities; vf_seeds: parent indices of VF0
+        entries; at most ndual() together.  Returns (L, dL per seed)."""
         m = self.mesh
+        per_step = isinstance(uf, (list, tuple))
+        nv = len(uf) if per_step else 1
+        pack = lambda a: np.concatenate([np.asfortranarray(x).ravel(order="F") for x in a]) if per_step else a
+        uf, vf, wf = pack(uf), pack(vf), pack(wf)
         K = self.L.orc_ndual()
         assert len(face_seeds) + len(vf_seeds) <= K
         slots = [np.full(m.cell_shape, -1, dtype=np.int32, order="F") for _ in range(3)]
@@ -216,8 +221,9 @@ class Oracle:
         wv = np.ascontiguousarray(np.asarray(w, dtype=np.float64).ravel(order="F"))
         Lv = ctypes.c_double()
         dL = np.zeros(K)
-        f = self.L.orc_rollout_forward(_m(m), dt, steps, _p(VF0), _p(uf), _p(vf), _p(wf), *[_p(x) for x in slots],
-                                       _p(svf), wv.ctypes.data, ctypes.byref(Lv), dL.ctypes.data)
+        f = self.L.orc_rollout_forward(_m(m), dt, steps, nv, _p(VF0), _p(uf), _p(vf), _p(wf),
+                                       *[_p(x) for x in slots], _p(svf), wv.ctypes.data, ctypes.byref(Lv),
+                                       dL.ctypes.data)
         if f:
             raise RuntimeError(f"restatement flags {f}")
         return Lv.value, dL[:len(face_seeds) + len(vf_seeds)]

@@ -1485,11 +1485,14 @@ int orc_ndual() { return NDUAL; }
  * run_solver's transport loop: from VF0, the initial state (Neumann + VF borders,
  * computeBand!, computeNormal!, computePLIC!), then `steps` steps (SL update of the band cells,
  * VF copy and ghost fill, normals, PLIC and band again), every value a Dual.  Up to NDUAL
- * directions are seeded: face values of the frozen velocities (su/sv/sw: the slot of each
- * parent entry, -1 none) and entries of VF0 (sVF, same convention, VF layout).  The band is
- * recomputed from the values, as it switches discretely.  L = sum of w * VF_T over the
- * interior (w: Nx*Ny*Nz, i fastest); dL[q] its derivative along direction q. */
-int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* VF0, const double* uf,
+ * directions are seeded: face values of the velocities (su/sv/sw: the slot of each parent entry,
+ * -1 none; the same entry of every step's velocities, as for a perturbation added to every
+ * step) and entries of VF0 (sVF, same convention, VF layout).  uf, vf, wf hold vel_steps
+ * consecutive cell arrays: step s uses array min(s, vel_steps - 1) (1: frozen velocities).
+ * The band is recomputed from the values, as it switches discretely.  L = sum of w * VF_T over
+ * the interior (w: Nx*Ny*Nz, i fastest); dL[q] its derivative along direction q.  Cells are
+ * processed in parallel (OpenMP); each cell's arithmetic is the restatement's. */
+int orc_rollout_forward(const orc_mesh* M, double dt, int steps, int vel_steps, const double* VF0, const double* uf,
                         const double* vf, const double* wf, const int* su, const int* sv, const int* sw,
                         const int* sVF, const double* w, double* L, double* dL)
 {
@@ -1502,7 +1505,7 @@ int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* V
         VF[t] = Dual(VF0[t]);
         if (sVF && sVF[t] >= 0) VF[t].d[sVF[t]] = 1.0;
     }
-    Err e;
+    int flags = 0;
     auto ghost = [&]() {
         Arr3<Dual> A(VF.data(), G.vlo, G.vhi);
         neumann(G, A);
@@ -1515,12 +1518,19 @@ int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* V
         std::fill(ny.begin(), ny.end(), Dual(0.0));
         std::fill(nz.begin(), nz.end(), Dual(0.0));
         FieldsT<Dual> F{&G, VF.data()};
+        int fl = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : fl)
         for (int k = 1; k <= G.N[2]; ++k)
-            for (int j = 1; j <= G.N[1]; ++j)
+            for (int j = 1; j <= G.N[1]; ++j) {
+                Err e;
                 for (int i = 1; i <= G.N[0]; ++i)
                     elvira_cell<Dual, FieldsT<Dual>, Dual>(G, F, nx.data(), ny.data(), nz.data(), i, j, k, &e);
+                fl |= e.flags;
+            }
+        flags |= fl;
         Arr3<Dual> A(nx.data(), G.lo, G.hi), B(ny.data(), G.lo, G.hi), C(nz.data(), G.lo, G.hi);
         update_borders(G, A); update_borders(G, B); update_borders(G, C);
+#pragma omp parallel for collapse(2)
         for (int k = G.lo[2]; k <= G.hi[2]; ++k)
             for (int j = G.lo[1]; j <= G.hi[1]; ++j)
                 for (int i = G.lo[0]; i <= G.hi[0]; ++i) {
@@ -1532,11 +1542,15 @@ int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* V
     };
     ghost();
     geometry(true);
-    Vel V{uf, vf, wf, su, sv, sw};
     for (int s = 0; s < steps; ++s) {
+        const long off = (long)std::min(s, std::max(vel_steps, 1) - 1) * ncell;
+        Vel V{uf + off, vf + off, wf + off, su, sv, sw};
         PlicT<Dual> P{nx.data(), ny.data(), nz.data(), D.data()};
+        int fl = 0;
+#pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : fl)
         for (int k = 1; k <= G.N[2]; ++k)
-            for (int j = 1; j <= G.N[1]; ++j)
+            for (int j = 1; j <= G.N[1]; ++j) {
+                Err e;
                 for (int i = 1; i <= G.N[0]; ++i) {
                     const long c = G.c(i, j, k), v = G.v(i, j, k);
                     if (std::abs((int)band[c]) <= M->nband)
@@ -1544,6 +1558,9 @@ int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* V
                     else
                         VFn[v] = VF[v];
                 }
+                fl |= e.flags;
+            }
+        flags |= fl;
         for (int k = 1; k <= G.N[2]; ++k)
             for (int j = 1; j <= G.N[1]; ++j)
                 for (int i = 1; i <= G.N[0]; ++i) VF[G.v(i, j, k)] = VFn[G.v(i, j, k)];
@@ -1557,7 +1574,7 @@ int orc_rollout_forward(const orc_mesh* M, double dt, int steps, const double* V
             for (int i = 1; i <= G.N[0]; ++i, ++q) acc = acc + Dual(w[q]) * VF[G.v(i, j, k)];
     *L = acc.v;
     for (int d = 0; d < NDUAL; ++d) dL[d] = acc.d[d];
-    return e.flags;
+    return flags;
 }
 
 /* Algorithmic operation counts (see Cnt) of one step's per-cell parts, summed over the given

@@ -2,6 +2,8 @@
 
     python tests/adjoint_configs.py 2d [--fd 64]      # 256^2, 40 steps
     python tests/adjoint_configs.py 3d [--fd 16] [--precision mixed]
+    python tests/adjoint_configs.py 2d --save-gradient g.npz   # the reverse pass (GPU)
+    python tests/adjoint_configs.py 2d --forward-mode g.npz    # against forward mode (CPU)
 
 2d: single-vortex deformation on 256x256 (Nz = 1, z periodic), circle r = 0.15 at
     (0.5, 0.75) by 10x10 sub-sampling, stream-function face velocities (period T = 8) at
@@ -188,6 +190,56 @@ def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=(), sweep
                         for q, (idx, (a, f)) in enumerate(zip(picks, rows))]}
 
 
+def save_gradient(cfg, path, precision="fp64"):
+    """The reverse pass's gradient of the configuration (GPU), with its loss, saved for
+    forward_mode_check (which needs no GPU)."""
+    cfg.target = rollout_gpu(cfg, np.zeros_like(cfg.p0))
+    L, G, times = gradient(cfg, precision)
+    np.savez(path, loss=L, grad=G, precision=precision, steps=cfg.steps, every=cfg.every)
+    return {"config": cfg.name, "saved": path, "loss": L, "timings": times}
+
+
+def forward_mode_check(cfg, path, count, seed=7):
+    """The saved reverse-pass gradient against forward-mode derivatives of the restatement's
+    whole rollout (Dual numbers through the initial state and every step's SL update, normals,
+    PLIC and band; the analogue of a ForwardDiff.jl gradient), on `count` entries drawn as check
+    draws them.  For L = 1/2 ||VF_T - target||^2, dL = sum((VF_T - target) * dVF_T).  Face
+    parameters only (the 2D configuration's per-face noise): each seed perturbs one face of
+    every step's velocities."""
+    from oracle.oracle import Oracle
+    saved = np.load(path)
+    G = saved["grad"]
+    m = cfg.mesh
+    cfg.target = rollout_cpu(cfg, np.zeros_like(cfg.p0))
+    VFT = rollout_cpu(cfg, cfg.p0)
+    w = m.interior(VFT) - m.interior(cfg.target)
+    rng = np.random.default_rng(seed)
+    support = np.argwhere(np.abs(G) > 0)
+    picks = [tuple(int(x) for x in support[k]) for k in rng.choice(len(support), size=min(count, len(support)),
+                                                                  replace=False)]
+    o = Oracle(m)
+    vel = [cfg.vel(n, cfg.p0) for n in range(cfg.steps)]
+    us, vs, ws = [v[0] for v in vel], [v[1] for v in vel], [v[2] for v in vel]
+    K = o.ndual()
+    fwd = []
+    t0 = time.perf_counter()
+    for c0 in range(0, len(picks), K):
+        batch = [(idx[0], idx[1:]) for idx in picks[c0:c0 + K]]
+        Lf, dL = o.rollout_forward(cfg.dt, cfg.steps, cfg.VF0, us, vs, ws, batch, [], w)
+        fwd += list(dL)
+    secs = time.perf_counter() - t0
+    fwd = np.array(fwd)
+    adj = np.array([float(G[idx]) for idx in picks])
+    scale = float(np.max(np.abs(fwd)))
+    return {"config": cfg.name, "grid": list(m.cell_shape), "steps": cfg.steps, "checkpoint_every": cfg.every,
+            "reverse_precision": str(saved["precision"]), "reverse_loss": float(saved["loss"]),
+            "loss_restatement": loss(cfg, VFT), "checked": len(picks),
+            "max_abs_err_over_max_forward_mode": float(np.max(np.abs(adj - fwd)) / scale) if scale > 0 else None,
+            "max_forward_mode": scale, "forward_mode_seconds": secs,
+            "entries": [{"index": list(idx), "adjoint": float(a), "forward_mode": float(f)}
+                        for idx, a, f in zip(picks, adj, fwd)]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("config", choices=["2d", "3d"])
@@ -199,7 +251,19 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--also", choices=["fp64", "mixed"], nargs="*", default=[])
     ap.add_argument("--sweep-all", action="store_true", help="central differences with h/8 for every entry")
+    ap.add_argument("--save-gradient", metavar="FILE", help="save the reverse pass's gradient (GPU) and stop")
+    ap.add_argument("--forward-mode", metavar="FILE",
+                    help="check a saved gradient against forward-mode derivatives of the restatement (2d, CPU)")
     a = ap.parse_args()
+    if a.save_gradient or a.forward_mode:
+        cfg = config2d(N=a.n or 256, steps=a.steps or 40, every=a.every) if a.config == "2d" else \
+            config3d(N=a.n or 128, steps=a.steps or 30, every=a.every)
+        if a.save_gradient:
+            print(json.dumps(save_gradient(cfg, a.save_gradient, a.precision)))
+        else:
+            assert a.config == "2d", "forward mode seeds face parameters: the 2d configuration"
+            print(json.dumps(forward_mode_check(cfg, a.forward_mode, a.fd or 64)))
+        return
     if a.config == "2d":
         cfg = config2d(N=a.n or 256, steps=a.steps or 40, every=a.every)
         out = check(cfg, a.fd or 64, a.fd_backend or "cpu", a.precision, also=a.also, sweep_all=a.sweep_all)
