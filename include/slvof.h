@@ -65,8 +65,9 @@ typedef struct slvof_mesh {
                             24 "24_tets" (src/VFgeom.jl:229-332) */
     int32_t pressure_scheme; /* param.pressure_scheme (src/Parameters.jl:60): SLVOF_PRESSURE_SEMI_LAGRANGIAN
                                 (0, the default) or SLVOF_PRESSURE_FINITE_DIFFERENCE (1), whose band cells
-                                add the flux-correction tets (src/Transport.jl:121-124; 5_tets, FP64
-                                context) and whose band-edge momentum fluxes are finite differences */
+                                add the flux-correction tets (src/Transport.jl:121-124; 5_tets; a mixed
+                                context runs this scheme's update with the FP64 clip) and whose
+                                band-edge momentum fluxes are finite differences */
 } slvof_mesh;
 
 #define SLVOF_PRESSURE_SEMI_LAGRANGIAN 0

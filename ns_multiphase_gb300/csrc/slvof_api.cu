@@ -242,7 +242,9 @@ int st_transport(slvof_ctx* c, double dt)
     launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
     s_end(c, S_CLASSIFY);
     s_beg(c, S_SL);
-    if (c->precision == SLVOF_FP64)
+    /* the finite-difference scheme's correction tets join each band cell's FP64 sums, so a
+     * mixed context runs the FP64 clip for it (with its own normals and plane constants) */
+    if (c->precision == SLVOF_FP64 || c->m.fd)
         launch_sl64(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->phase,
                     c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
     else
@@ -359,8 +361,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
         return SLVOF_E_ARG;
     /* the flux-correction tets of the finite-difference scheme exist for 5_tets in the
      * reference (add_correction_tets keeps the first five tets), and run in FP64 here */
-    if (mesh->pressure_scheme == SLVOF_PRESSURE_FINITE_DIFFERENCE &&
-        (precision != SLVOF_FP64 || (mesh->tesselation != 0 && mesh->tesselation != 5)))
+    if (mesh->pressure_scheme == SLVOF_PRESSURE_FINITE_DIFFERENCE && mesh->tesselation != 0 && mesh->tesselation != 5)
         return SLVOF_E_UNSUPPORTED;
     /* the pure/interface thresholds are compared as bit patterns, which orders doubles like the
      * floating-point compare only against positive finite thresholds */

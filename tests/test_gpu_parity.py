@@ -333,10 +333,47 @@ def test_finite_difference_scheme_correction_tets():
     g2.close()
 
 
-@pytest.mark.parametrize("precision,tess", [("mixed", "5_tets"), ("fp64", "24_tets")])
+def test_finite_difference_scheme_in_a_mixed_context():
+    """A mixed context with the finite-difference scheme: mixed normals and plane constants, and
+    the update with the correction tets through the FP64 clip.  VF within the mixed path's
+    tolerance of the restatement over several steps, and the momentum call like an FP64
+    context's on the same inputs."""
+    m = Mesh(Nx=20, Ny=20, Nz=20, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, pressure_scheme="finite-difference")
+    VF = cases.vf_spheres(m, [[0.45, 0.52, 0.5]], [0.22], nF=10)
+    o, g, VFo, band, nx, ny, nz, D = init_both(m, VF, "mixed")
+    dt = 0.5 * m.dx / 2.0
+    rng = np.random.default_rng(8)
+    noise = [0.05 * rng.standard_normal(m.cell_shape) for _ in range(3)]
+    for s in range(4):
+        uf, vf, wf = (a + e for a, e in zip(cases.deformation3d_faces(m, 0.2 + (s + 0.5) * dt, 3.0), noise))
+        uf, vf, wf = (np.asfortranarray(x) for x in (uf, vf, wf))
+        g.upload_velocity(uf, vf, wf)
+        mass = g.step(dt)
+        assert o.step(dt, VFo, uf, vf, wf, nx, ny, nz, D, band) == 0
+    # the plane constants differ from the FP64 ones in their last bits, so VF does too
+    d = np.abs(m.interior(g.download_vf()) - m.interior(VFo))
+    assert d.max() <= 5e-3 and np.quantile(d, 0.99) <= 1e-6, (d.max(), np.quantile(d, 0.99))
+    mo = o.mass(VFo)
+    assert abs(mass - mo) <= 1e-10 * abs(mo)
+    g.close()
+    mm = Mesh(Nx=18, Ny=16, Nz=14, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, rho_liq=1000.0, rho_gas=1.2,
+              pressure_scheme="finite-difference")
+    _, _, VF2, band2, nx2, ny2, nz2, D2, uf2, vf2, wf2, u2, v2, w2, dt2 = momentum_state("5_tets")
+    out = []
+    for prec in ("fp64", "mixed"):
+        g2 = ctx(mm, prec)
+        VFg = VF2.copy(order="F")
+        r = g2.transportSL_momentum(dt2, VFg, uf2, vf2, wf2, nx2, ny2, nz2, D2, band2, u2, v2, w2)
+        out.append((VFg, *r))
+        g2.close()
+    for a, b, name in zip(out[0], out[1], ("VF", "us", "vs", "ws")):
+        assert_same(a, b, name)
+
+
+@pytest.mark.parametrize("precision,tess", [("mixed", "24_tets"), ("fp64", "24_tets"), ("mixed", "6_tets")])
 def test_finite_difference_scheme_unsupported_combinations(precision, tess):
-    """The correction tets are defined for 5_tets (the reference keeps the first five tets) and
-    built for FP64 contexts; other combinations are refused at creation."""
+    """The correction tets are defined for 5_tets (the reference keeps the first five tets);
+    other tessellations are refused at creation."""
     from ns_multiphase_gb300.slvof import SLVOF
     m = Mesh(Nx=8, Ny=8, Nz=8, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess, pressure_scheme="finite-difference")
     with pytest.raises(RuntimeError):
