@@ -44,6 +44,8 @@ extern "C" {
 
 #define SLVOF_STEP_BAND 1 /* recompute the band after the step (run_solver, src/NavierStokes_Parallel.jl:143) */
 #define SLVOF_STEP_MASS 2 /* return sum(VF)*dx*dy*dz over the interior (src/WriteData.jl:33) */
+#define SLVOF_STEP_DEFER 4 /* slvof_step_host only: leave the new state's normals, PLIC (and band) to
+                              the next call, which builds them while its velocities upload */
 
 /* Mesh and parameters.  Mirrors mesh_struct (src/Mesh.jl:1-53) and the parameters knobs the
  * path reads (src/Parameters.jl:68-77).  Coordinate arrays are the parents of mesh.x/y/z
@@ -169,7 +171,12 @@ int slvof_transportSL_momentum(slvof_ctx* ctx, double dt, double* VF, const doub
 /* Per-step drop-in for run_solver's loop with the state resident between calls: uploads
  * this step's face velocities, runs slvof_step and downloads VF (and the mass).  VF is
  * downloaded on a second stream while the new state's normals, PLIC, band and mass are built;
- * the call returns when both are done.  VF must not be null. */
+ * the call returns when both are done.  VF must not be null.
+ * With SLVOF_STEP_DEFER the new state's normals, PLIC and (with SLVOF_STEP_BAND) band are built
+ * at the start of the next slvof_step_host call with that flag, beside its velocity upload, and
+ * the mass is summed from VF directly; the results are the same as without the flag.  Any other
+ * entry point builds the deferred state first; device errors of those stages are reported by
+ * the first status after them that reports device errors.  No counterpart in the reference (its loop is on the CPU). */
 int slvof_step_host(slvof_ctx* ctx, double dt, int flags, const double* uf, const double* vf, const double* wf,
                     double* VF, double* mass);
 

@@ -73,13 +73,18 @@ struct slvof_ctx {
     double* spheres = nullptr;
     int spheres_n = 0;
     bool normals_valid = false;
+    /* slvof_step_host with SLVOF_STEP_DEFER left the new state's normals and PLIC (and its band
+     * when deferred_band) to the next call; deferred_err holds device error bits of deferred
+     * stages that another entry point ran, until its status reports them */
+    bool deferred = false, deferred_band = false;
+    int deferred_err = 0;
     double rho_liq = 1.0, rho_gas = 1.0;
     double last_ms = 0.0;
     cudaStream_t own_stream = nullptr;
     /* slvof_step_host copies VF out on copy_stream while the next state's geometry is built;
      * the steps build the band on band_stream beside the normals and PLIC */
     cudaStream_t copy_stream = nullptr, band_stream = nullptr;
-    cudaEvent_t ev_state = nullptr, ev_copied = nullptr, ev_band = nullptr;
+    cudaEvent_t ev_state = nullptr, ev_copied = nullptr, ev_band = nullptr, ev_up = nullptr;
     cudaEvent_t sev[SLVOF_NSTAGES][2] = {};
     bool sran[SLVOF_NSTAGES] = {};
     std::string err;
@@ -102,12 +107,26 @@ int fail(slvof_ctx* c, int code, const std::string& msg)
         if (e_ != cudaSuccess) return fail(c, SLVOF_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+#define TRY(x)                \
+    do {                      \
+        int r_ = (x);         \
+        if (r_ < 0) return r_; \
+    } while (0)
+
 enum { S_CLASSIFY, S_SL, S_VFGHOST, S_PURE, S_IFACE, S_NGHOST, S_PLIC, S_BAND, S_MASS };
 
-int begin(slvof_ctx* c)
+int flush_deferred(slvof_ctx* c);
+
+/* Every entry point starts here; all but a deferring slvof_step_host first build the state a
+ * deferring call left (flush). */
+int begin(slvof_ctx* c, bool flush = true)
 {
     if (!c) return SLVOF_E_ARG;
     CK(cudaSetDevice(c->device));
+    if (flush && c->deferred) {
+        const int r = flush_deferred(c);
+        if (r < 0) return r;
+    }
     CK(cudaEventRecord(c->ev0, c->stream));
     for (bool& r : c->sran) r = false;
     return 0;
@@ -133,6 +152,8 @@ int finish(slvof_ctx* c, bool read_err = true)
     if (!read_err) return SLVOF_OK;
     int e = 0;
     CK(cudaMemcpy(&e, c->ctr + C_ERR, sizeof(int), cudaMemcpyDeviceToHost));
+    e |= c->deferred_err;
+    c->deferred_err = 0;
     if (e) {
         char buf[160];
         snprintf(buf, sizeof buf, "device error bits 0x%x (1 index range, 2 clip depth, 4 NaN distance, 8 volume)", e);
@@ -337,11 +358,58 @@ int up_velocity(slvof_ctx* c, const double* uf, const double* vf, const double* 
     return 0;
 }
 
-#define TRY(x)                \
-    do {                      \
-        int r_ = (x);         \
-        if (r_ < 0) return r_; \
-    } while (0)
+/* The state a deferring slvof_step_host left (normals, PLIC and, when asked, the band of its
+ * VF), built on the call's stream while this call's face velocities upload on copy_stream.
+ * The stages read VF, the normals and the band, never the face velocities, so nothing orders
+ * them against the upload; the upload waits only for the caller's earlier work on the stream.
+ * The kernels are enqueued before the copies, since a copy from pageable memory returns only
+ * once its data is staged. */
+int up_velocity_beside(slvof_ctx* c, const double* uf, const double* vf, const double* wf)
+{
+    if (!uf || !vf || !wf) return fail(c, SLVOF_E_ARG, "null host pointer");
+    CK(cudaEventRecord(c->ev_state, c->stream));
+    CK(cudaStreamWaitEvent(c->copy_stream, c->ev_state, 0));
+    if (!c->normals_valid) {
+        const bool band = c->deferred && c->deferred_band;
+        int r = band ? st_band_side(c) : 0;
+        if (r >= 0) r = st_normals(c);
+        if (r >= 0) r = st_plic(c);
+        if (band) r = join_band(c, r);
+        if (r < 0) return r;
+    }
+    c->deferred = c->deferred_band = false;
+    const size_t b = c->ncell * sizeof(double);
+    cudaError_t e = cudaMemcpyAsync(c->uf, uf, b, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->vf, vf, b, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->wf, wf, b, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_up, c->copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_up, 0);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(c->copy_stream);
+        return fail(c, SLVOF_E_CUDA, std::string("velocity upload: ") + cudaGetErrorString(e));
+    }
+    to_float_velocity(c);
+    return 0;
+}
+
+/* Builds the state a deferring slvof_step_host left, before another entry point reads or
+ * replaces it; the device error bits of these stages join that entry point's status. */
+int flush_deferred(slvof_ctx* c)
+{
+    const bool band = c->deferred_band;
+    c->deferred = c->deferred_band = false;
+    TRY(clear_err(c));
+    if (band) TRY(st_band(c));
+    if (!c->normals_valid) {
+        TRY(st_normals(c));
+        TRY(st_plic(c));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    int e = 0;
+    CK(cudaMemcpy(&e, c->ctr + C_ERR, sizeof(int), cudaMemcpyDeviceToHost));
+    c->deferred_err |= e;
+    return 0;
+}
 
 } // namespace
 
@@ -385,7 +453,8 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
         cudaStreamCreateWithFlags(&c->band_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_state, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_copied, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_band, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->ev_band, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_up, cudaEventDisableTiming) != cudaSuccess)
         return bail(SLVOF_E_CUDA);
     for (int q = 0; q < SLVOF_NSTAGES; ++q)
         if (cudaEventCreate(&c->sev[q][0]) != cudaSuccess || cudaEventCreate(&c->sev[q][1]) != cudaSuccess)
@@ -459,6 +528,7 @@ int slvof_destroy(slvof_ctx* c)
     if (c->ev_state) cudaEventDestroy(c->ev_state);
     if (c->ev_copied) cudaEventDestroy(c->ev_copied);
     if (c->ev_band) cudaEventDestroy(c->ev_band);
+    if (c->ev_up) cudaEventDestroy(c->ev_up);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->band_stream) cudaStreamDestroy(c->band_stream);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
@@ -701,14 +771,19 @@ int slvof_transportSL(slvof_ctx* c, double dt, double* VF, const double* uf, con
 int slvof_step_host(slvof_ctx* c, double dt, int flags, const double* uf, const double* vf, const double* wf,
                     double* VF, double* mass)
 {
-    TRY(begin(c));
+    const bool defer = (flags & SLVOF_STEP_DEFER) != 0;
+    TRY(begin(c, !defer));
     if ((flags & SLVOF_STEP_MASS) && !mass) return fail(c, SLVOF_E_ARG, "mass requested with a null pointer");
     if (!VF) return fail(c, SLVOF_E_ARG, "null host pointer");
     TRY(clear_err(c));
-    TRY(up_velocity(c, uf, vf, wf));
-    if (!c->normals_valid) {
-        TRY(st_normals(c));
-        TRY(st_plic(c));
+    if (defer) {
+        TRY(up_velocity_beside(c, uf, vf, wf));
+    } else {
+        TRY(up_velocity(c, uf, vf, wf));
+        if (!c->normals_valid) {
+            TRY(st_normals(c));
+            TRY(st_plic(c));
+        }
     }
     TRY(st_transport(c, dt));
     /* the new VF is final here (normals, PLIC, band and mass only read it): it goes to the host
@@ -720,7 +795,13 @@ int slvof_step_host(slvof_ctx* c, double dt, int flags, const double* uf, const 
     if (ce == cudaSuccess) ce = cudaEventRecord(c->ev_copied, c->copy_stream);
     int r = 0;
     const bool band = (flags & SLVOF_STEP_BAND) != 0;
-    if (ce == cudaSuccess) {
+    if (ce == cudaSuccess && defer) {
+        /* the next call builds this state's normals, PLIC and band beside its upload */
+        if (flags & SLVOF_STEP_MASS) r = st_mass(c, mass, false);
+        c->deferred = true;
+        c->deferred_band = band;
+        ce = cudaStreamWaitEvent(c->stream, c->ev_copied, 0);
+    } else if (ce == cudaSuccess) {
         r = band ? st_band_side(c) : 0;
         if (r >= 0) r = st_normals(c);
         if (r >= 0) r = st_plic(c);

@@ -23,6 +23,7 @@ FP64 = 0
 MIXED = 1
 STEP_BAND = 1
 STEP_MASS = 2
+STEP_DEFER = 4
 
 # (name, restype, argtypes) of every symbol declared in include/slvof.h
 _P, _I, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
@@ -406,9 +407,9 @@ class SLVOF:
                                              _ptr(ny, np.float64, s), _ptr(nz, np.float64, s),
                                              _ptr(D, np.float64, s), _ptr(band, np.int16, s)), "transportSL")
 
-    def step_host(self, dt, uf, vf, wf, VF_out, band=True, mass=True):
+    def step_host(self, dt, uf, vf, wf, VF_out, band=True, mass=True, defer=False):
         s = self.mesh.cell_shape
-        flags = (STEP_BAND if band else 0) | (STEP_MASS if mass else 0)
+        flags = (STEP_BAND if band else 0) | (STEP_MASS if mass else 0) | (STEP_DEFER if defer else 0)
         m = ctypes.c_double(np.nan)
         self._check(self.L.slvof_step_host(self.h, dt, flags, _ptr(uf, np.float64, s), _ptr(vf, np.float64, s),
                                            _ptr(wf, np.float64, s), _ptr(VF_out, np.float64, self.mesh.vf_shape),
