@@ -249,7 +249,9 @@ int slvof_adjoint_zero_velocity(slvof_ctx* ctx);
  * (as slvof_step or slvof_prepare leave them), the step's face velocities, and dL/dVF of the
  * step's result in the VF-derivative buffer.  After it the buffer holds dL/dVF of the
  * starting VF (ghost entries: derivatives with respect to the ghost values) and dL/d(face
- * velocities) of the step has been added to the velocity buffers.  The state is unchanged. */
+ * velocities) of the step has been added to the velocity buffers.  The state is unchanged.
+ * With SLVOF_PRESSURE_FINITE_DIFFERENCE the reverse includes the flux-correction tets in an
+ * FP64 context; a mixed context returns SLVOF_E_UNSUPPORTED. */
 int slvof_adjoint_step(slvof_ctx* ctx, double dt);
 /* The same with the step's result given: d_VFnext is the VF (VF-array shaped, device) that
  * slvof_step(ctx, dt, SLVOF_STEP_BAND, .) produces from the current state, e.g. the next

@@ -755,6 +755,275 @@ SLVOF_HD double sl_cell(const DevMesh& m, const CutCase* tab, const Vel& V, cons
     return VF;
 }
 
+/* ---- the finite-difference scheme's flux-correction tets ------------------------------------
+ * add_correction_tets (src/VFgeom.jl:514-664, 5_tets): on each face of a band cell two tets
+ * (a,b,d,e), (b,c,d,e) over the quad a,b,c,d of the face's projected flux-volume nodes, whose
+ * apex e is the quad's mean moved along the face normal by 6 (vol - V(mean)) / N, with
+ * vol = +-(dt * area * face velocity - SLfluxVol) and N the normal component of
+ * a x b + d x a + b x c + c x d.  Their clipped volumes join the cell's sums. */
+
+/* The finite-difference path calls the clip, project! and their reverses from several places
+ * per cell; these are compiled once as calls instead of being inlined at every site. */
+#if defined(__CUDACC__)
+#define SLVOF_HD_CALL __host__ __device__ __noinline__
+#else
+#define SLVOF_HD_CALL inline
+#endif
+SLVOF_HD_CALL void clip_call(const DevMesh& m, const CutCase* tab, const Plic& P, const double tet[4][3],
+                             const int ind[4][3], double s, Frame* st, double& vol_out, double& liq_out,
+                             double gtet[4][3], int& kinds, int& err)
+{
+    clip(m, tab, P, tet, ind, s, st, vol_out, liq_out, gtet, kinds, err);
+}
+SLVOF_HD_CALL void project_call(const DevMesh& m, const Vel& V, double* pt, int i, int j, int k, double dt)
+{
+    double x[3][3];
+    project(m, V, pt, i, j, k, dt, x);
+}
+SLVOF_HD_CALL void project_reverse_call(const DevMesh& m, const Vel& V, const VelGrad& G, const double* p0, int i,
+                                        int j, int k, double dt, const double* gp)
+{
+    project_reverse(m, V, G, p0, i, j, k, dt, gp);
+}
+
+/* Node n of the flux volume of face `dir` at the low side of cell (fi, fj, fk) (SLfluxVol,
+ * src/VFgeom.jl:428-509): its grid node's offsets from that cell, and whether it is projected.
+ * Along the face normal each node pair holds the projected node first in even cells and
+ * second in odd ones (oddEvenCell mirrors x). */
+SLVOF_HD bool flux_node(int dir, bool even, int n, int off[3])
+{
+    const int b0 = n & 1, b1 = (n >> 1) & 1, b2 = (n >> 2) & 1;
+    if (dir == 0) {
+        off[0] = 0; off[1] = b1; off[2] = b2;
+        return even ? b0 == 0 : b0 == 1;
+    }
+    off[0] = even ? b0 : 1 - b0;
+    if (dir == 1) {
+        off[1] = 0; off[2] = b2;
+        return b1 == 0;
+    }
+    off[1] = b1; off[2] = 0;
+    return b2 == 0;
+}
+
+/* Corner q of the face quad a, b, c, d (the projected nodes, src/VFgeom.jl:590-646). */
+SLVOF_HD int flux_quad(int dir, bool even, int q)
+{
+    if (dir == 0) return even ? (q == 0 ? 4 : (q == 1 ? 6 : (q == 2 ? 2 : 0))) : (q == 0 ? 7 : (q == 1 ? 5 : (q == 2 ? 1 : 3)));
+    if (dir == 1) return q == 0 ? 1 : (q == 1 ? 5 : (q == 2 ? 4 : 0));
+    return q == 0 ? 1 : (q == 1 ? 0 : (q == 2 ? 2 : 3));
+}
+
+/* One face's flux volume, target volume and apex, as the forward builds them. */
+struct CorrFace {
+    double fv[8][3]; /* flux-volume nodes */
+    double mean[3], e[3];
+    double A, sgn, vol, v0, N; /* dt * face area, +-1 (oddEvenCell of the face's cell) */
+    int dir, fi, fj, fk;
+    bool even;
+};
+
+/* Face f (x-, x+, y-, y+, z-, z+) of cell (i, j, k). */
+SLVOF_HD_CALL void corr_face(const DevMesh& m, const Vel& V, int i, int j, int k, double dt, int f, CorrFace& C)
+{
+    const int dir = f >> 1, up = f & 1;
+    C.dir = dir;
+    C.fi = i + (dir == 0 ? up : 0);
+    C.fj = j + (dir == 1 ? up : 0);
+    C.fk = k + (dir == 2 ? up : 0);
+    C.even = tess_even(m.tess, C.fi, C.fj, C.fk);
+    C.sgn = C.even ? 1.0 : -1.0;
+    for (int n = 0; n < 8; ++n) {
+        int off[3];
+        const bool proj = flux_node(dir, C.even, n, off);
+        C.fv[n][0] = fc(m, 0, C.fi + off[0]);
+        C.fv[n][1] = fc(m, 1, C.fj + off[1]);
+        C.fv[n][2] = fc(m, 2, C.fk + off[2]);
+        if (proj) project_call(m, V, C.fv[n], C.fi, C.fj, C.fk, dt);
+    }
+    double flux = 0.0; /* tets_vol, src/VFgeom.jl:683-689 */
+    for (int t = 0; t < tess_ntets(m.tess); ++t)
+        flux += tet_vol(C.fv[tess_tet(m.tess, t, 0)], C.fv[tess_tet(m.tess, t, 1)], C.fv[tess_tet(m.tess, t, 2)],
+                        C.fv[tess_tet(m.tess, t, 3)]);
+    flux = flux * C.sgn;
+    const long t = ci(m, C.fi, C.fj, C.fk);
+    C.A = dir == 0 ? (dt * m.d[1]) * m.d[2] : (dir == 1 ? (dt * m.d[0]) * m.d[2] : (dt * m.d[0]) * m.d[1]);
+    const double divg = C.A * ld((dir == 0 ? V.uf : (dir == 1 ? V.vf : V.wf)) + t);
+    C.vol = C.even ? (divg - flux) : -(divg - flux);
+    const double *a = C.fv[flux_quad(dir, C.even, 0)], *b = C.fv[flux_quad(dir, C.even, 1)],
+                 *c = C.fv[flux_quad(dir, C.even, 2)], *d = C.fv[flux_quad(dir, C.even, 3)];
+    for (int p = 0; p < 3; ++p) {
+        C.mean[p] = 0.25 * (((a[p] + b[p]) + c[p]) + d[p]);
+        C.e[p] = C.mean[p];
+    }
+    C.v0 = tet_vol(a, b, d, C.e) + tet_vol(b, c, d, C.e);
+    const int p1 = (dir + 1) % 3, p2 = (dir + 2) % 3;
+    C.N = (((a[p1] * b[p2] - a[p2] * b[p1]) + (d[p1] * a[p2] - d[p2] * a[p1])) + (b[p1] * c[p2] - b[p2] * c[p1])) +
+          (c[p1] * d[p2] - c[p2] * d[p1]);
+    C.e[dir] += 6.0 * (C.vol - C.v0) / C.N;
+}
+
+/* Tet h (0: a,b,d,e; 1: b,c,d,e) of a face. */
+SLVOF_HD void corr_tet(const CorrFace& C, int h, double tet[4][3])
+{
+    const int q0 = flux_quad(C.dir, C.even, h), q1 = flux_quad(C.dir, C.even, h + 1),
+              q3 = flux_quad(C.dir, C.even, 3);
+    for (int p = 0; p < 3; ++p) {
+        tet[0][p] = C.fv[q0][p];
+        tet[1][p] = C.fv[q1][p];
+        tet[2][p] = C.fv[q3][p];
+        tet[3][p] = C.e[p];
+    }
+}
+
+/* Reverse of a face: gT[h][n] = dL/d(vertex n of tet h) to the face velocity of the target
+ * volume and, through the quad, the apex and the flux volume, to the projected nodes. */
+SLVOF_HD_CALL void corr_face_reverse(const DevMesh& m, const Vel& V, const VelGrad& G, double dt, const CorrFace& C,
+                                const double (*gT)[4][3])
+{
+    const int dir = C.dir, p1 = (dir + 1) % 3, p2 = (dir + 2) % 3;
+    const int qa = flux_quad(dir, C.even, 0), qb = flux_quad(dir, C.even, 1), qc = flux_quad(dir, C.even, 2),
+              qd = flux_quad(dir, C.even, 3);
+    const double *a = C.fv[qa], *b = C.fv[qb], *c = C.fv[qc], *d = C.fv[qd];
+    double ga[3], gb[3], gc[3], gd[3], gm[3];
+    for (int p = 0; p < 3; ++p) {
+        ga[p] = gT[0][0][p];
+        gb[p] = gT[0][1][p] + gT[1][0][p];
+        gc[p] = gT[1][1][p];
+        gd[p] = gT[0][2][p] + gT[1][2][p];
+        gm[p] = gT[0][3][p] + gT[1][3][p]; /* e = mean + (shift along dir) */
+    }
+    const double se = gm[dir];
+    const double gvol = 6.0 * se / C.N, gv0 = -gvol, gN = -6.0 * se * (C.vol - C.v0) / (C.N * C.N);
+    /* v0 = V(a, b, d, mean) + V(b, c, d, mean) */
+    tet_vol_grad(a, b, d, C.mean, gv0, ga, gb, gd, gm);
+    tet_vol_grad(b, c, d, C.mean, gv0, gb, gc, gd, gm);
+    /* N = cr(a, b) + cr(d, a) + cr(b, c) + cr(c, d), cr(u, w) = u[p1] w[p2] - u[p2] w[p1] */
+    auto crg = [&](const double* u, const double* w, double* gu, double* gw) {
+        gu[p1] += gN * w[p2];
+        gu[p2] -= gN * w[p1];
+        gw[p2] += gN * u[p1];
+        gw[p1] -= gN * u[p2];
+    };
+    crg(a, b, ga, gb);
+    crg(d, a, gd, ga);
+    crg(b, c, gb, gc);
+    crg(c, d, gc, gd);
+    double gfv[8][3];
+    for (int n = 0; n < 8; ++n) gfv[n][0] = gfv[n][1] = gfv[n][2] = 0.0;
+    for (int p = 0; p < 3; ++p) {
+        gfv[qa][p] += ga[p] + 0.25 * gm[p];
+        gfv[qb][p] += gb[p] + 0.25 * gm[p];
+        gfv[qc][p] += gc[p] + 0.25 * gm[p];
+        gfv[qd][p] += gd[p] + 0.25 * gm[p];
+    }
+    /* vol = sgn (A U - flux), flux = sgn * sum of the flux volume's tet volumes */
+    const long t = ci(m, C.fi, C.fj, C.fk);
+    acc((dir == 0 ? G.guf : (dir == 1 ? G.gvf : G.gwf)) + t, gvol * C.sgn * C.A);
+    const double gsum = -gvol * C.sgn * C.sgn;
+    for (int q = 0; q < tess_ntets(m.tess); ++q) {
+        const int n0 = tess_tet(m.tess, q, 0), n1 = tess_tet(m.tess, q, 1), n2 = tess_tet(m.tess, q, 2),
+                  n3 = tess_tet(m.tess, q, 3);
+        tet_vol_grad(C.fv[n0], C.fv[n1], C.fv[n2], C.fv[n3], gsum, gfv[n0], gfv[n1], gfv[n2], gfv[n3]);
+    }
+    for (int n = 0; n < 8; ++n) {
+        int off[3];
+        if (!flux_node(dir, C.even, n, off)) continue;
+        if (gfv[n][0] == 0.0 && gfv[n][1] == 0.0 && gfv[n][2] == 0.0) continue;
+        const double p0[3] = {fc(m, 0, C.fi + off[0]), fc(m, 1, C.fj + off[1]), fc(m, 2, C.fk + off[2])};
+        project_reverse_call(m, V, G, p0, C.fi, C.fj, C.fk, dt, gfv[n]);
+    }
+}
+
+/* Reverse of the SL update of band cell (i, j, k) under pressure_scheme "finite-difference"
+ * (src/Transport.jl:111-148 with add_correction_tets, src/Transport.jl:121-124): the cell's
+ * five tets and the twelve correction tets (vertex cells by pt2index! seeded at the cell), all
+ * clipped and their sums divided; g = dL/dVFnew.  Adds dL/d(face velocities) and
+ * dL/d(donor planes); returns VFnew. */
+SLVOF_HD double sl_cell_fd(const DevMesh& m, const CutCase* tab, const Vel& V, const VelGrad& GV, const Plic& P,
+                           double dt, int i, int j, int k, double g, Frame* st, int& err)
+{
+    double p0[8][3], p[8][3], gvt[8][3];
+    const double tetsign = cell_verts(m, i, j, k, p0);
+    int pind[8][3];
+    for (int n = 0; n < 8; ++n) {
+        for (int q = 0; q < 3; ++q) { p[n][q] = p0[n][q]; gvt[n][q] = 0.0; }
+        project_call(m, V, p[n], i, j, k, dt);
+        pt2index(m, pind[n], p[n], i, j, k, err);
+    }
+    const int nt = tess_ntets(m.tess);
+    CorrFace C;
+    /* the uncut volume, which the clipped pieces add up to */
+    double volu = 0.0;
+    for (int t = 0; t < nt; ++t)
+        volu += tetsign * tet_vol(p[tess_tet(m.tess, t, 0)], p[tess_tet(m.tess, t, 1)], p[tess_tet(m.tess, t, 2)],
+                                  p[tess_tet(m.tess, t, 3)]);
+    for (int f = 0; f < 6; ++f) {
+        corr_face(m, V, i, j, k, dt, f, C);
+        for (int h = 0; h < 2; ++h) {
+            double tet[4][3];
+            corr_tet(C, h, tet);
+            volu += tetsign * tet_vol(tet[0], tet[1], tet[2], tet[3]);
+        }
+    }
+    const double s = (g != 0.0 && volu != 0.0) ? tetsign * g / volu : 0.0;
+    double vol = 0.0, vLiq = 0.0;
+    int kinds = 0;
+    for (int t = 0; t < nt; ++t) {
+        double tet[4][3], gtet[4][3];
+        int ind[4][3];
+        for (int n = 0; n < 4; ++n)
+            for (int q = 0; q < 3; ++q) {
+                tet[n][q] = p[tess_tet(m.tess, t, n)][q];
+                ind[n][q] = pind[tess_tet(m.tess, t, n)][q];
+            }
+        double rv, rl;
+        clip_call(m, tab, P, tet, ind, s, st, rv, rl, gtet, kinds, err);
+        vol += tetsign * rv;
+        vLiq += tetsign * rl;
+        for (int n = 0; n < 4; ++n)
+            for (int q = 0; q < 3; ++q) gvt[tess_tet(m.tess, t, n)][q] += gtet[n][q];
+    }
+    double gct[12][4][3];
+    for (int f = 0; f < 6; ++f) {
+        corr_face(m, V, i, j, k, dt, f, C);
+        for (int h = 0; h < 2; ++h) {
+            double tet[4][3];
+            int ind[4][3];
+            corr_tet(C, h, tet);
+            for (int n = 0; n < 4; ++n) pt2index(m, ind[n], tet[n], i, j, k, err);
+            double rv, rl;
+            clip_call(m, tab, P, tet, ind, s, st, rv, rl, gct[2 * f + h], kinds, err);
+            vol += tetsign * rv;
+            vLiq += tetsign * rl;
+        }
+    }
+    if (!(vol > 0.0) || !std::isfinite(vol)) err |= E_VOLUME;
+    const double VF = vLiq / vol;
+    if (s == 0.0 || kinds == LEAF_LIQ || kinds == LEAF_GAS) return VF;
+    /* d(VF)/d(vol) part: -g VF / vol times d(vol)/d(vertices) of every tet */
+    const double w = -g * VF / vol;
+    for (int t = 0; t < nt; ++t) {
+        const int a = tess_tet(m.tess, t, 0), b = tess_tet(m.tess, t, 1), c = tess_tet(m.tess, t, 2),
+                  e = tess_tet(m.tess, t, 3);
+        tet_vol_grad(p[a], p[b], p[c], p[e], w * tetsign, gvt[a], gvt[b], gvt[c], gvt[e]);
+    }
+    for (int n = 0; n < 8; ++n)
+        if (gvt[n][0] != 0.0 || gvt[n][1] != 0.0 || gvt[n][2] != 0.0)
+            project_reverse_call(m, V, GV, p0[n], i, j, k, dt, gvt[n]);
+    for (int f = 0; f < 6; ++f) {
+        corr_face(m, V, i, j, k, dt, f, C);
+        for (int h = 0; h < 2; ++h) {
+            double tet[4][3];
+            corr_tet(C, h, tet);
+            double(*gt)[3] = gct[2 * f + h];
+            tet_vol_grad(tet[0], tet[1], tet[2], tet[3], w * tetsign, gt[0], gt[1], gt[2], gt[3]);
+        }
+        corr_face_reverse(m, V, GV, dt, C, gct + 2 * f);
+    }
+    return VF;
+}
+
 /* ---- computeDist ----------------------------------------------------------------------- */
 /* dD/d(nx, ny, nz) and dD/dVF of computeDist (src/VF.jl:109-156) at cell (i, j, k) with plane
  * (n, D): from F(n, D) = VF, F the liquid fraction of the cell under n.x < D (the five-tet

@@ -220,6 +220,29 @@ __global__ void k_adj_vert(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV, co
     if (err) atomicOr(errw, err);
 }
 
+/* pressure_scheme "finite-difference": thread per band cell, the whole reverse of its SL update
+ * with the twelve flux-correction tets (adj::sl_cell_fd), seeded with the folded dL/dVFnew.
+ * The correction tets of a cell reach the flux volumes of all six faces, so this path keeps
+ * the cell in one thread instead of splitting it into tets and vertices. */
+__global__ void __launch_bounds__(ADJ_SL_THREADS) k_adj_sl_fd(DevMesh m, double dt, adj::Vel V, adj::VelGrad GV,
+                                                              adj::Plic P, const int* __restrict__ list,
+                                                              const int* __restrict__ count,
+                                                              const double* __restrict__ gfold, int* errw)
+{
+    __shared__ CutCase s_tab[16];
+    load_cut_table(s_tab);
+    adj::Frame st[adj::STACK];
+    const int n = *count;
+    int err = 0;
+    for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < n; item += gridDim.x * blockDim.x) {
+        const int L = list[item];
+        const int i = 1 + L % m.N[0], j = 1 + (L / m.N[0]) % m.N[1], k = 1 + L / (m.N[0] * m.N[1]);
+        const double g = gfold[vidx(m, i, j, k)];
+        if (g != 0.0) adj::sl_cell_fd(m, s_tab, V, GV, P, dt, i, j, k, g, st, err);
+    }
+    if (err) atomicOr(errw, err);
+}
+
 /* computeDist backwards at every cell (ghosts included): gDf -> gn (+=) and gout. */
 __global__ void k_adj_dist(DevMesh m, const double* __restrict__ VF, const double* __restrict__ nx,
                            const double* __restrict__ ny, const double* __restrict__ nz, const double* __restrict__ D,
@@ -312,6 +335,17 @@ void launch_adjoint_pre(const DevMesh& m, double dt, const double* uf, const dou
     k_adj_pre<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, list, count, b.gfold, b.cells, count2, errw);
 }
 
+/* computeDist and ELVIRA backwards, after the SL update's reverse has filled gD and gn. */
+static void adjoint_geometry(const DevMesh& m, const double* VF, const double* nx, const double* ny,
+                             const double* nz, const double* D, const signed char* cand, const AdjBuffers& b,
+                             int* errw, int nsm, cudaStream_t s)
+{
+    fold(m, b.gD, b.gDf, 0, 0, s);
+    k_adj_dist<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, D, b.gDf, b.gn[0], b.gn[1], b.gn[2], b.gout, errw);
+    for (int q = 0; q < 3; ++q) fold(m, b.gn[q], b.gnf[q], 0, 0, s);
+    k_adj_elvira<<<nsm * 8, 256, 0, s>>>(m, VF, cand, b.gnf[0], b.gnf[1], b.gnf[2], b.gout);
+}
+
 void launch_adjoint_tail(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
                          const signed char* cand, const signed char* phase, const AdjBuffers& b, const int* count2,
@@ -322,10 +356,19 @@ void launch_adjoint_tail(const DevMesh& m, double dt, const double* VF, const do
     adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD, phase};
     k_adj_tet<<<nsm * 16, ADJ_SL_THREADS, 0, s>>>(m, P, b.cells, count2, b.tets, errw);
     k_adj_vert<<<nsm * 8, 128, 0, s>>>(m, dt, V, GV, b.cells, b.tets, count2, errw);
-    fold(m, b.gD, b.gDf, 0, 0, s);
-    k_adj_dist<<<nsm * 8, 128, 0, s>>>(m, VF, nx, ny, nz, D, b.gDf, b.gn[0], b.gn[1], b.gn[2], b.gout, errw);
-    for (int q = 0; q < 3; ++q) fold(m, b.gn[q], b.gnf[q], 0, 0, s);
-    k_adj_elvira<<<nsm * 8, 256, 0, s>>>(m, VF, cand, b.gnf[0], b.gnf[1], b.gnf[2], b.gout);
+    adjoint_geometry(m, VF, nx, ny, nz, D, cand, b, errw, nsm, s);
+}
+
+void launch_adjoint_fd(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
+                       const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                       const signed char* cand, const signed char* phase, const AdjBuffers& b, const int* list,
+                       const int* count, int* errw, int nsm, cudaStream_t s)
+{
+    adj::Vel V{uf, vf, wf};
+    adj::VelGrad GV{b.guf, b.gvf, b.gwf};
+    adj::Plic P{nx, ny, nz, D, b.gn[0], b.gn[1], b.gn[2], b.gD, phase};
+    k_adj_sl_fd<<<nsm * 16, ADJ_SL_THREADS, 0, s>>>(m, dt, V, GV, P, list, count, b.gfold, errw);
+    adjoint_geometry(m, VF, nx, ny, nz, D, cand, b, errw, nsm, s);
 }
 
 } // namespace slvof

@@ -92,6 +92,12 @@ void launch_adjoint_tail(const DevMesh& m, double dt, const double* VF, const do
                          const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
                          const signed char* cand, const signed char* phase, const AdjBuffers& b, const int* count2,
                          int* errw, int nsm, cudaStream_t s);
+/* pressure_scheme "finite-difference" (FP64): the band cells' reverse with the flux-correction
+ * tets, one thread per cell of the head's list, then the same computeDist and ELVIRA reverse. */
+void launch_adjoint_fd(const DevMesh& m, double dt, const double* VF, const double* uf, const double* vf,
+                       const double* wf, const double* nx, const double* ny, const double* nz, const double* D,
+                       const signed char* cand, const signed char* phase, const AdjBuffers& b, const int* list,
+                       const int* count, int* errw, int nsm, cudaStream_t s);
 void launch_adjoint_fold_vf(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s);
 void launch_adjoint_fold_cell(const DevMesh& m, const double* gin, double* gout, int nsm, cudaStream_t s);
 void launch_adjoint_elvira(const DevMesh& m, const double* VF, const signed char* cand, const AdjBuffers& b, int nsm,

@@ -49,7 +49,8 @@ double adjh_sl_cell(const slvof_mesh* M, double dt, int i, int j, int k, const d
     adj::Plic P{nx, ny, nz, D, gnx, gny, gnz, gD, phase.data()};
     std::vector<adj::Frame> st(adj::STACK);
     int e = 0;
-    const double r = adj::sl_cell(H.m, TAB, V, G, P, dt, i, j, k, g, st.data(), e);
+    const double r = H.m.fd ? adj::sl_cell_fd(H.m, TAB, V, G, P, dt, i, j, k, g, st.data(), e)
+                            : adj::sl_cell(H.m, TAB, V, G, P, dt, i, j, k, g, st.data(), e);
     if (err) *err = e;
     return r;
 }

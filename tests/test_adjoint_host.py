@@ -62,8 +62,8 @@ def ptr(a):
     return a.ctypes.data
 
 
-def sphere_state(N=10, centre=(0.45, 0.52, 0.55), r=0.27, t=0.4, tess="5_tets"):
-    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess)
+def sphere_state(N=10, centre=(0.45, 0.52, 0.55), r=0.27, t=0.4, tess="5_tets", scheme="semi-lagrangian"):
+    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, tesselation=tess, pressure_scheme=scheme)
     o = Oracle(m)
     VF = cases.vf_spheres(m, np.array([centre]), np.array([r]), nF=8)
     band, nx, ny, nz, D = o.init_state(VF)
@@ -176,6 +176,42 @@ def test_sl_cell_plane_gradient_matches_finite_differences(hlib, state):
         _, grads, err = harness_grads(hlib, m, state, c)
         assert err == 0
         worst, n = check_entries(o, state, c, [(nx, grads[3]), (ny, grads[4]), (nz, grads[5]), (D, grads[6])])
+        assert n >= 4
+        assert worst <= RTOL, (c, worst)
+
+
+@pytest.fixture(scope="module")
+def fd_state():
+    return sphere_state(scheme="finite-difference")
+
+
+def test_sl_cell_with_correction_tets_forward_matches_restatement(hlib, fd_state):
+    """pressure_scheme "finite-difference": the cell's tets and its twelve flux-correction tets
+    (add_correction_tets, src/VFgeom.jl:514-664) give the restatement's VFnew to rounding."""
+    m, o = fd_state[0], fd_state[1]
+    _, _, VF, band, nx, ny, nz, D, uf, vf, wf, dt = fd_state
+    cells = interface_preimage_cells(m, o, fd_state, 12)
+    assert len(cells) >= 8
+    for c in cells:
+        r, _, err = harness_grads(hlib, m, fd_state, c)
+        ref, _, flags = o.sl_cell(dt, *c, uf, vf, wf, nx, ny, nz, D)
+        assert err == 0 and flags == 0
+        assert abs(r - ref) <= 1e-14, (c, r, ref)
+
+
+def test_sl_cell_with_correction_tets_gradients_match_finite_differences(hlib, fd_state):
+    """The reverse through the correction tets' apex solve, the flux volume and the face
+    velocity of the target volume, against central differences of the restatement."""
+    m, o = fd_state[0], fd_state[1]
+    _, _, VF, band, nx, ny, nz, D, uf, vf, wf, dt = fd_state
+    cells = interface_preimage_cells(m, o, fd_state, 6)
+    for c in cells:
+        _, grads, err = harness_grads(hlib, m, fd_state, c)
+        assert err == 0
+        worst, n = check_entries(o, fd_state, c, [(uf, grads[0]), (vf, grads[1]), (wf, grads[2])])
+        assert n >= 9
+        assert worst <= RTOL, (c, worst)
+        worst, n = check_entries(o, fd_state, c, [(nx, grads[3]), (ny, grads[4]), (nz, grads[5]), (D, grads[6])])
         assert n >= 4
         assert worst <= RTOL, (c, worst)
 

@@ -7,6 +7,8 @@ h = 1e-6, of the restatement's FP64 step (the reference's CPU path restated).  V
 carry seeded noise on every face, as the adjoint configurations do.  Tolerance: 1e-6 relative
 to the largest sampled derivative.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -109,8 +111,8 @@ def check_velocity(m, VF0, base, noise, dt, steps, w, grads, count=12):
     return worst, n
 
 
-def sphere3d(N=12):
-    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+def sphere3d(N=12, scheme="semi-lagrangian"):
+    m = Mesh(Nx=N, Ny=N, Nz=N, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, pressure_scheme=scheme)
     VF0 = cases.vf_spheres(m, np.array([[0.45, 0.52, 0.55]]), np.array([0.27]), nF=8)
     return m, VF0
 
@@ -351,7 +353,8 @@ def forward_mode_check(mesh_vf, precision, tol):
     assert np.max(np.abs(fwd - rev)) <= tol * np.max(np.abs(fwd))
 
 
-def test_rollout_against_forward_mode(built):
+@pytest.mark.parametrize("scheme", ["semi-lagrangian", "finite-difference"])
+def test_rollout_against_forward_mode(built, scheme):
     """The FP64 reverse of a 3-step rollout (checkpoint every step) against forward-mode
     derivatives of the restatement's whole rollout (Dual numbers through the initial state and
     every step's SL update, normals, PLIC and band: the analogue of a ForwardDiff.jl gradient of
@@ -359,8 +362,10 @@ def test_rollout_against_forward_mode(built):
     the 32 largest face-velocity derivatives and 16 interface entries of VF0, whose derivatives
     run back through every step's ELVIRA and plane-constant solve to the initial state's.  The
     FP64 path is the restatement bit for bit, so both take the same branches and agree to
-    rounding."""
-    m, VF0 = sphere3d(12)
+    rounding.  With pressure_scheme "finite-difference" every band cell also clips its twelve
+    flux-correction tets (add_correction_tets, src/VFgeom.jl:514-664), whose reverse runs
+    through their apex solve, the faces' flux volumes and the face velocities."""
+    m, VF0 = sphere3d(12, scheme)
     dt = 0.5 * m.dx / 2.0
     steps = 3
     base = lambda n: cases.deformation3d_faces(m, 0.3 + 0.5 * dt, 3.0)
@@ -392,3 +397,17 @@ def test_rollout_against_forward_mode(built):
     fwd, rev = np.array(fwd), np.array(rev)
     assert np.max(np.abs(fwd[32:])) > 0
     assert np.max(np.abs(fwd - rev)) <= 1e-9 * np.max(np.abs(fwd)), np.max(np.abs(fwd - rev)) / np.max(np.abs(fwd))
+
+
+def test_finite_difference_reverse_refused_in_a_mixed_context(built):
+    """The correction tets' reverse is built for FP64 contexts; a mixed context refuses it
+    before any work."""
+    from ns_multiphase_gb300.slvof import SLVOF
+    m, VF0 = sphere3d(8, "finite-difference")
+    g = SLVOF(m, "mixed")
+    g.upload_vf(VF0)
+    g.vf_ghost_fill()
+    g.init_state()
+    rc = g.L.slvof_adjoint_step(g.h, ctypes.c_double(0.5 * m.dx / 2.0))
+    assert rc == -3
+    g.close()
