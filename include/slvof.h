@@ -250,8 +250,8 @@ int slvof_adjoint_zero_velocity(slvof_ctx* ctx);
  * step's result in the VF-derivative buffer.  After it the buffer holds dL/dVF of the
  * starting VF (ghost entries: derivatives with respect to the ghost values) and dL/d(face
  * velocities) of the step has been added to the velocity buffers.  The state is unchanged.
- * With SLVOF_PRESSURE_FINITE_DIFFERENCE the reverse includes the flux-correction tets in an
- * FP64 context; a mixed context returns SLVOF_E_UNSUPPORTED. */
+ * With SLVOF_PRESSURE_FINITE_DIFFERENCE the reverse includes the flux-correction tets; it runs
+ * in FP64 in either precision, as that scheme's update does. */
 int slvof_adjoint_step(slvof_ctx* ctx, double dt);
 /* The same with the step's result given: d_VFnext is the VF (VF-array shaped, device) that
  * slvof_step(ctx, dt, SLVOF_STEP_BAND, .) produces from the current state, e.g. the next

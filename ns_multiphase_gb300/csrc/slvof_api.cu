@@ -1178,8 +1178,6 @@ int adjoint_step(slvof_ctx* c, double dt, const double* d_next)
     TRY(begin(c));
     TRY(adj_alloc(c));
     if (!c->normals_valid) return fail(c, SLVOF_E_ARG, "normals/PLIC/band of the current VF are not computed (slvof_prepare)");
-    if (c->m.fd && c->precision == SLVOF_MIXED)
-        return fail(c, SLVOF_E_UNSUPPORTED, "the reverse pass of the flux-correction tets is built for FP64 contexts");
     TRY(clear_err(c));
     AdjBuffers b{};
     b.gin = c->gvf[0];
@@ -1194,14 +1192,16 @@ int adjoint_step(slvof_ctx* c, double dt, const double* d_next)
     /* head: fold, pass-through of cells outside the band, band list; its count sizes the
      * pre-image records, the pre-pass's count the per-tet records */
     launch_adjoint_head(c->m, c->band[c->bcur], b, c->list_adj, c->ctr + C_ADJ, c->ctr + C_ADJ2, c->nsm, c->stream);
-    if (c->precision == SLVOF_MIXED) {
-        TRY(adjoint_step32(c, dt, d_next, b));
-        std::swap(c->gvf[0], c->gvf[1]);
-        return finish(c);
-    }
+    /* the finite-difference scheme's update runs the FP64 clip in either precision (on the
+     * mixed context's FP64 winner normals and plane constants), and so does its reverse */
     if (c->m.fd) {
         launch_adjoint_fd(c->m, dt, c->VF[c->vcur], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->cand, c->phase,
                           b, c->list_adj, c->ctr + C_ADJ, c->ctr + C_ERR, c->nsm, c->stream);
+        std::swap(c->gvf[0], c->gvf[1]);
+        return finish(c);
+    }
+    if (c->precision == SLVOF_MIXED) {
+        TRY(adjoint_step32(c, dt, d_next, b));
         std::swap(c->gvf[0], c->gvf[1]);
         return finish(c);
     }

@@ -7,8 +7,6 @@ h = 1e-6, of the restatement's FP64 step (the reference's CPU path restated).  V
 carry seeded noise on every face, as the adjoint configurations do.  Tolerance: 1e-6 relative
 to the largest sampled derivative.
 """
-import ctypes
-
 import numpy as np
 import pytest
 
@@ -399,15 +397,19 @@ def test_rollout_against_forward_mode(built, scheme):
     assert np.max(np.abs(fwd - rev)) <= 1e-9 * np.max(np.abs(fwd)), np.max(np.abs(fwd - rev)) / np.max(np.abs(fwd))
 
 
-def test_finite_difference_reverse_refused_in_a_mixed_context(built):
-    """The correction tets' reverse is built for FP64 contexts; a mixed context refuses it
-    before any work."""
-    from ns_multiphase_gb300.slvof import SLVOF
-    m, VF0 = sphere3d(8, "finite-difference")
-    g = SLVOF(m, "mixed")
-    g.upload_vf(VF0)
-    g.vf_ghost_fill()
-    g.init_state()
-    rc = g.L.slvof_adjoint_step(g.h, ctypes.c_double(0.5 * m.dx / 2.0))
-    assert rc == -3
-    g.close()
+def test_finite_difference_reverse_in_a_mixed_context(built):
+    """A mixed context's finite-difference update runs the FP64 clip on its FP64 winner normals
+    and plane constants, and its reverse is the FP64 one: against the FP64 context's reverse on
+    the same rollout (relative L2 over all face and initial-VF derivatives)."""
+    m, VF0 = sphere3d(12, "finite-difference")
+    dt = 0.5 * m.dx / 2.0
+    base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
+    vel, _ = noisy(m, base, 0.05, 29)
+    w = np.random.default_rng(9).standard_normal((m.Nx, m.Ny, m.Nz))
+    a = gpu_gradients(m, VF0, vel, dt, 2, w, every=1, precision="fp64")
+    b = gpu_gradients(m, VF0, vel, dt, 2, w, every=1, precision="mixed")
+    ga = np.concatenate([x.ravel() for x in a[2:]])
+    gb = np.concatenate([x.ravel() for x in b[2:]])
+    assert np.linalg.norm(ga) > 0
+    assert np.linalg.norm(ga - gb) <= 1e-6 * np.linalg.norm(ga), np.linalg.norm(ga - gb) / np.linalg.norm(ga)
+    assert np.linalg.norm(a[1] - b[1]) <= 1e-6 * np.linalg.norm(a[1]), np.linalg.norm(a[1] - b[1]) / np.linalg.norm(a[1])
