@@ -393,7 +393,7 @@ def main():
         tV, hVF = pinned(None, tuple(reversed(m.vf_shape)))
         def e2e_run(defer):
             ge = make_ctx(m, centres, radii, "mixed", 0.5 * dt, VF0)
-            for _ in range(max(3, args.warmup)):  # warm: first touches of the pinned buffers
+            for _ in range(max(5, args.warmup)):  # warm: first touches of the pinned buffers
                 ge.step_host(dt, huf, hvf, hwf, hVF, defer=defer)
             torch.cuda.synchronize()
             per_step = []
@@ -406,7 +406,8 @@ def main():
             ge.close()
             return {"value": cells * args.e2e_steps / e2e_s, "unit": "cell-updates/s",
                     "ms_per_step": {"mean": 1e3 * e2e_s / args.e2e_steps, "min": 1e3 * min(per_step),
-                                    "median": 1e3 * statistics.median(per_step), "max": 1e3 * max(per_step)}}
+                                    "median": 1e3 * statistics.median(per_step), "max": 1e3 * max(per_step),
+                                    "each": [round(1e3 * t, 3) for t in per_step]}}
 
         # each call uploads its velocities while the previous state's normals, PLIC and band
         # are built (SLVOF_STEP_DEFER): in the steady state every step still does all the work
