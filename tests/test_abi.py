@@ -104,3 +104,11 @@ def test_create_refuses_grids_past_32_bit_cell_indices(lib, shape):
     h = ctypes.c_void_p()
     lib.slvof_create.restype = ctypes.c_int
     assert lib.slvof_create(ctypes.byref(m.desc()), 1, ctypes.byref(h)) == -3
+
+
+def test_python_mirror_constants_match_the_header():
+    """The precision and step-flag constants of the Python mirror are the header's."""
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "slvof.h")).read()
+    defs = {k: int(v) for k, v in re.findall(r"#define SLVOF_(\w+) \(?(-?\d+)\)?", hdr)}
+    for name in ("FP64", "MIXED", "STEP_BAND", "STEP_MASS", "STEP_DEFER"):
+        assert getattr(slvof, name) == defs[name], name
