@@ -63,6 +63,12 @@ def parse():
     p.add_argument("--count-sample", type=int, default=1500,
                    help="interface cells sampled for the operation count of the CPU leg (twice as many band "
                         "cells); 0 skips it")
+    p.add_argument("--stage-run", choices=["step", "adjoint", "fd-adjoint"], default=None,
+                   help="workload for kernel profilers only (no JSON line): 'step' runs --steps resident steps "
+                        "of the --n^3 workload in --precision and prints each step's stage times; 'adjoint' "
+                        "then runs --steps reverse steps from the last state (the step's result given); "
+                        "'fd-adjoint' runs two reverse steps of the finite-difference scheme at 64^3 (FP64)")
+    p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     return p.parse_args()
 
 
@@ -305,8 +311,64 @@ def reference_arm(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def stage_run(args):
+    """Small workloads for kernel-profiler captures: no timing legs and no JSON line."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from ns_multiphase_gb300 import cases
+    from ns_multiphase_gb300.mesh import Mesh
+    torch.cuda.set_device(0)
+    if args.stage_run == "fd-adjoint":
+        # 64^3, pressure_scheme "finite-difference", 12 spheres (seed 11, nF 6), Deformation3D
+        # at t = 0.3 (T = 3), CFL 0.5; reverse of one step seeded with normal weights (seed 1)
+        from ns_multiphase_gb300.slvof import SLVOF
+        m = Mesh(Nx=64, Ny=64, Nz=64, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, pressure_scheme="finite-difference")
+        c, r = cases.config_spheres(12, seed=11)
+        g = SLVOF(m, "fp64")
+        g.case_vf_spheres(c, r, nF=6)
+        g.init_state()
+        dt = 0.5 * m.dx / 2.0
+        g.case_deformation3d(0.3, 3.0)
+        gv = m.vf_array()
+        m.interior(gv)[...] = np.random.default_rng(1).standard_normal((m.Nx, m.Ny, m.Nz))
+        for _ in range(2):
+            g.adjoint_set_vf(gv)
+            g.adjoint_zero_velocity()
+            t0 = time.perf_counter()
+            g.adjoint_step(dt)
+            print("adjoint step (fd, fp64, 64^3)", round(1e3 * (time.perf_counter() - t0), 3), "ms", flush=True)
+        g.close()
+        return
+    m, centres, radii, dt = workload(args.n)
+    g = make_ctx(m, centres, radii, args.precision, 0.5 * dt)
+    for s in range(args.steps):
+        g.step(dt)
+        print(s, {k: round(v, 3) for k, v in g.stage_ms().items()}, g.counters(), flush=True)
+    if args.stage_run == "adjoint":
+        nvf = int(np.prod(m.vf_shape))
+        s0 = torch.empty(nvf, dtype=torch.float64, device="cuda")
+        s1 = torch.empty_like(s0)
+        g.copy_vf_device(s0.data_ptr())
+        g.step(dt, band=True, mass=False)
+        g.copy_vf_device(s1.data_ptr())
+        g.load_vf_device(s0.data_ptr())
+        g.prepare()
+        gT = m.vf_array()
+        m.interior(gT)[...] = np.random.default_rng(SEED).standard_normal((m.Nx, m.Ny, m.Nz))
+        g.adjoint_set_vf(gT)
+        g.adjoint_zero_velocity()
+        for s in range(args.steps):
+            g.adjoint_step(dt, s1.data_ptr())
+            print("adjoint", s, round(g.last_kernel_ms(), 3), flush=True)
+    g.close()
+
+
 def main():
     args = parse()
+    if args.stage_run:
+        stage_run(args)
+        return
     ws, rank, local = dist_env()
     import torch
     if ws > 1:

@@ -280,9 +280,10 @@ int slvof_case_deformation3d(slvof_ctx* ctx, double t, double T);
  * allocating library routine.  Its scratch, one compensated partial sum per z-plane, is a
  * fixed static device array of the library, held on every device that loads the library
  * until the process exits; grids with Nz > SLVOF_NOALLOC_MAX_PLANES return SLVOF_E_TOO_LARGE.
- * The first call on a device looks up that array's device address, so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU race, so order
- * them.  Only Nx, Ny, Nz, nghost, dx, dy, dz of *mesh are read.  The result is written in
+ * The first call on a device looks up that array's device address in the current CUDA
+ * context, so make it before any stream capture; a call in a different context (one the
+ * caller made current, or the primary context created again after a device reset) looks it
+ * up again.  All calls share the array: calls that overlap on the GPU race, so order them.  Only Nx, Ny, Nz, nghost, dx, dy, dz of *mesh are read.  The result is written in
  * stream order; synchronise the stream before reading it. */
 #define SLVOF_NOALLOC_MAX_PLANES 8192
 int slvof_mass_noalloc(const slvof_mesh* mesh, const double* d_VF, double* d_mass, void* stream);

@@ -6,10 +6,14 @@
  * and the cell volume is 1.  This needs a uniform mesh, which create_mesh builds
  * (src/Mesh.jl:83-100); slvof_create rejects the mixed mode otherwise.
  *
- *   k_sl32_*         : SL update (src/Transport.jl:111-148) in three stages: FP32 RK
- *                      trajectories through FP32 face velocities (one thread per band cell),
- *                      FP32 recursive clip of each tet (same cut tables and recursion as
- *                      cutTet, one thread per tet), FP64 accumulation of the clipped volumes.
+ *   k_sl32_pre       : the eight FP32 RK pre-image vertices of every band cell through FP32
+ *                      face velocities (thread per cell); cells whose pre-image is strictly
+ *                      on one side of every donor plane it reaches are finished there, the
+ *                      others are compacted with their vertices for the clip.
+ *   k_sl32_clipw     : warp-cooperative FP32 clip of those cells' tets (cutTet's cut tables
+ *                      and cuts, src/VFgeom.jl:713-900), with the pending sub-tets of a batch
+ *                      of cells in a shared-memory stack and each cell's volume and liquid
+ *                      volume summed in float-float, then VFnew = vLiq/vol in FP64.
  */
 #include "slvof_kernels.h"
 #include "slvof_dev.cuh"

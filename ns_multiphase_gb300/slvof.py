@@ -24,6 +24,13 @@ MIXED = 1
 STEP_BAND = 1
 STEP_MASS = 2
 STEP_DEFER = 4
+# status codes (SLVOF_OK, SLVOF_E_*)
+OK = 0
+E_ARG = -1
+E_CUDA = -2
+E_UNSUPPORTED = -3
+E_NOMEM = -4
+E_TOO_LARGE = -5
 
 # (name, restype, argtypes) of every symbol declared in include/slvof.h
 _P, _I, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double

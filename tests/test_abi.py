@@ -107,8 +107,9 @@ def test_create_refuses_grids_past_32_bit_cell_indices(lib, shape):
 
 
 def test_python_mirror_constants_match_the_header():
-    """The precision and step-flag constants of the Python mirror are the header's."""
+    """The precision, step-flag and status constants of the Python mirror are the header's."""
     hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "slvof.h")).read()
     defs = {k: int(v) for k, v in re.findall(r"#define SLVOF_(\w+) \(?(-?\d+)\)?", hdr)}
-    for name in ("FP64", "MIXED", "STEP_BAND", "STEP_MASS", "STEP_DEFER"):
+    for name in ("FP64", "MIXED", "STEP_BAND", "STEP_MASS", "STEP_DEFER", "OK", "E_ARG", "E_CUDA",
+                 "E_UNSUPPORTED", "E_NOMEM", "E_TOO_LARGE"):
         assert getattr(slvof, name) == defs[name], name
