@@ -225,24 +225,59 @@ def adjoint_mixed(g, m, dt, steps, torch):
     return given, recompute
 
 
-def cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, budget_s):
-    """CPU restatement on a centred z-slab: ELVIRA of the slab cells and the SL update of the
-    slab's band cells, all host threads.  Returns (cell-updates/s, slab layers, seconds)."""
-    from oracle.oracle import Oracle
-    o = Oracle(m)
-    N = m.Nz
-    nk = 2
-    while True:
+class CpuSample:
+    """The CPU restatement of one step on a centred z-slab of the state, all host threads:
+    the SL update of the slab's band cells (src/Transport.jl:108-151), the VF ghost fill
+    (:179-181), ELVIRA (src/ELVIRA.jl:6-55), computePLIC! (src/VF.jl:94-103) and computeBand!
+    (src/VF.jl:16-74) of the slab's cells; the ghost fill runs on the whole grid.  The slab's
+    layer count is set once so that a sample takes about budget_s / 4."""
+
+    def __init__(self, m, VF, uf, vf, wf, nx, ny, nz, D, band, dt):
+        from oracle.oracle import Oracle
+        self.o = Oracle(m)
+        self.m, self.dt = m, dt
+        self.state = (VF, uf, vf, wf, nx, ny, nz, D, band)
+        self.VFn = m.vf_array()
+        self.out = (m.cell_array(), m.cell_array(), m.cell_array(), m.cell_array(), band.copy(order="F"))
+        self.nk = 2
+
+    def run(self):
+        VF, uf, vf, wf, nx, ny, nz, D, band = self.state
+        o, N, nk = self.o, self.m.Nz, self.nk
         klo = N // 2 - nk // 2 + 1
         khi = klo + nk - 1
+        np.copyto(self.VFn, VF)  # cells outside the slab keep their VF, as non-band cells do
+        nx2, ny2, nz2, D2, band2 = self.out
         t0 = time.perf_counter()
-        o.transport(dt, VF, uf, vf, wf, nx, ny, nz, D, band, klo=klo, khi=khi)
-        o.ELVIRA(VF, klo=klo, khi=khi)
+        f, _ = o.transport(self.dt, VF, uf, vf, wf, nx, ny, nz, D, band, klo=klo, khi=khi, VFnew=self.VFn)
+        o.vf_ghost_fill(self.VFn)
+        o.ELVIRA(self.VFn, nx2, ny2, nz2, klo=klo, khi=khi)
+        o.computePLIC_slab(nx2, ny2, nz2, self.VFn, D2, klo, khi)
+        o.computeBand_slab(self.VFn, band2, klo, khi)
         sec = time.perf_counter() - t0
-        if sec >= budget_s / 4 or nk >= N:
-            break
-        nk = min(N, max(nk * 2, int(nk * budget_s / 4 / max(sec, 1e-3))))
-    return m.Nx * m.Ny * nk / sec, nk, sec
+        if f:
+            raise RuntimeError(f"restatement flags {f}")
+        return self.m.Nx * self.m.Ny * nk / sec, sec
+
+    def calibrate(self, budget_s):
+        N = self.m.Nz
+        while True:
+            _, sec = self.run()
+            if sec >= budget_s / 4 or self.nk >= N:
+                return
+            self.nk = min(N, max(self.nk * 2, int(self.nk * budget_s / 4 / max(sec, 1e-3))))
+
+    def describe(self, sec):
+        return (f"SL update + VF ghost fill + ELVIRA + computePLIC! + computeBand! of {self.nk} centred z-layers "
+                f"of the {self.m.Nx}^3 state ({sec:.1f} s), C++ restatement, OpenMP on all host cores")
+
+
+def cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, budget_s):
+    """One calibrated CpuSample: (cell-updates/s, description)."""
+    cs = CpuSample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt)
+    cs.calibrate(budget_s)
+    v, sec = cs.run()
+    return v, cs.describe(sec)
 
 
 def op_counts(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, counters, n_if):
@@ -274,38 +309,47 @@ def op_counts(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, counters, n_if):
                       f"{n_if_step} interface and {n_band_step} band cells"}
 
 
+def workload_config(n):
+    """config of both arms' JSON lines: the workload and the L2 note, nothing else."""
+    return {"workload": f"SL-VOF transport step, {n}^3, 200 spheres seed {SEED}, Deformation3D T=3, CFL 0.5, "
+                        f"nband 1, RK4, 5 tets",
+            "l2": "every field > L2 (no flush needed)"}
+
+
 def reference_arm(args, rank):
-    """--impl reference: the CPU restatement (the Julia reference cannot run here)."""
-    import torch
+    """--impl reference: the CPU restatement of the reference (the Julia reference cannot run
+    here) on the host cores, for the same workload.  Nothing here loads the GPU library: the
+    state is generated on the CPU (VFsphere's rule, then computeBand!, ELVIRA and computePLIC!
+    of the whole grid by the restatement), and each step is a bounded sample of the step's
+    stages on a centred z-slab (CpuSample)."""
     from oracle.oracle import Oracle, build
+    from ns_multiphase_gb300 import cases
     build()
-    m, centres, radii, dt = workload(args.n)
     if rank != 0:
         return
-    torch.cuda.set_device(0)
-    g = make_ctx(m, centres, radii, "fp64", 0.5 * dt)
-    VF = g.download_vf()
-    nx, ny, nz = g.download_normals()
-    D = g.download_plic()
-    band = g.download_band()
-    from ns_multiphase_gb300 import cases
+    m, centres, radii, dt = workload(args.n)
+    o = Oracle(m)
+    VF = o.vf_spheres(centres, radii, nF=20, dims=3)
+    band, nx, ny, nz, D = o.init_state(VF)
     uf, vf, wf = cases.deformation3d_faces(m, 0.5 * dt, 3.0)
-    g.close()
-    vals = []
-    layers = 0
-    for s in range(max(1, args.steps)):
-        v, layers, sec = cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt,
-                                    budget_s=min(args.cpu_seconds, 120.0 / max(1, args.steps)))
+    cs = CpuSample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt)
+    cs.calibrate(min(args.cpu_seconds, 120.0 / max(1, args.steps)))
+    for _ in range(args.warmup):
+        cs.run()
+    vals, secs = [], []
+    for _ in range(max(1, args.steps)):
+        v, sec = cs.run()
         vals.append(v)
+        secs.append(sec)
     value = statistics.median(vals)
     cores = os.cpu_count()
     line = {"metric": METRIC, "impl": "reference", "value": value, "unit": "cell-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"SL-VOF 256^3 200-sphere deformation (slab sample at {args.n}^3)"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * m.Nx * m.Ny * m.Nz / value,
+            "higher_is_better": True, "scaling": "weak", "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args.n),
             "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": cores, "kind": "port",
-                             "sample": f"ELVIRA + SL update of {layers} centred z-layers of the {args.n}^3 state, "
-                                       f"C++ restatement (the Julia reference is not installed)"},
+                             "sample": cs.describe(statistics.median(secs)) + " (the Julia reference is not "
+                                       "installed: no julia on this machine or the GPU box)"},
             "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "vs_baseline": None}
     print(json.dumps(line), flush=True)
@@ -370,16 +414,15 @@ def main():
         stage_run(args)
         return
     ws, rank, local = dist_env()
+    if args.impl == "reference":
+        # the CPU restatement on the host cores: rank 0 alone, no GPU and no process group
+        if rank == 0:
+            reference_arm(args, rank)
+        return
     import torch
     if ws > 1:
         import torch.distributed as tdist
         tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    if args.impl == "reference":
-        if rank == 0:
-            reference_arm(args, rank)
-        if ws > 1:
-            tdist.destroy_process_group()
-        return
 
     import __graft_entry__
     __graft_entry__.build()
@@ -488,10 +531,8 @@ def main():
                 ops = op_counts(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, counters, args.count_sample)
             from oracle.oracle import build
             build()
-            v, layers, sec = cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, args.cpu_seconds)
-            cpu = {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"ELVIRA + SL update of {layers} centred z-layers ({sec:.1f} s) of the {args.n}^3 "
-                             f"state, C++ restatement, OpenMP on all host cores"}
+            v, desc = cpu_sample(m, VF, uf, vf, wf, nx, ny, nz, D, band, dt, args.cpu_seconds)
+            cpu = {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
 
         # ---- roofline of the dominant kernel -----------------------------------------------
         peaks = {}
@@ -539,10 +580,8 @@ def main():
         out = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-               "config": {"workload": f"SL-VOF transport step, {args.n}^3, 200 spheres seed {SEED}, "
-                                      f"Deformation3D T=3, CFL 0.5, nband 1, RK4, 5 tets",
-                          "precision": "mixed", "parallelism": "replicas" if ws > 1 else "1 GPU",
-                          "l2": "every field > L2 (no flush needed)"},
+               "config": workload_config(args.n), "precision": "mixed",
+               "parallelism": "replicas" if ws > 1 else "1 GPU",
                "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "speedup_mixed": value / ws / value64,
                         "stages_ms": stage64},
                "accuracy": {"steps": args.drift_steps, "mass_rel_diff_mixed_vs_fp64": drift_vs_fp64,

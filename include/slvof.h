@@ -99,11 +99,12 @@ int slvof_stage_ms(const slvof_ctx* ctx, double* ms, int n);
  * reference (CPU only). */
 int slvof_set_stream(slvof_ctx* ctx, void* stream);
 /* Work-list sizes of the last step: [0] band cells updated by the SL clip pipeline,
- * [1] interface cells given ELVIRA candidates, [2] band cells that needed the full clip (mixed
- * mode; the rest were all-liquid/all-gas pre-images), [3] cells whose PLIC plane constant was
- * solved, [4] interface cells whose ELVIRA choice was arbitrated in FP64 (mixed mode).
- * No counterpart in the reference. */
-#define SLVOF_NCOUNTERS 5
+ * [1] interface cells given ELVIRA candidates, [2] band cells that needed the full clip (the
+ * mixed reverse pass; the rest were all-liquid/all-gas pre-images), [3] cells whose PLIC
+ * plane constant was solved, [4] interface cells whose ELVIRA choice was arbitrated in FP64
+ * (mixed mode), and for the mixed mode's flux-form SL update [5] grid nodes traced, [6] faces
+ * swept, [7] faces that needed the clip.  No counterpart in the reference. */
+#define SLVOF_NCOUNTERS 8
 int slvof_counters(const slvof_ctx* ctx, int* out, int n);
 
 /* ---- host <-> device ---------------------------------------------------------------------- */

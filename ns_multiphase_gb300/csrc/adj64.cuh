@@ -765,7 +765,8 @@ SLVOF_HD double sl_cell(const DevMesh& m, const CutCase* tab, const Vel& V, cons
 /* The finite-difference path calls the clip, project! and their reverses from several places
  * per cell; these are compiled once as calls instead of being inlined at every site. */
 #if defined(__CUDACC__)
-#define SLVOF_HD_CALL __host__ __device__ __noinline__
+/* static: each translation unit that includes this header keeps its own copy */
+#define SLVOF_HD_CALL static __host__ __device__ __noinline__
 #else
 #define SLVOF_HD_CALL inline
 #endif

@@ -18,31 +18,14 @@
 #include "slvof_kernels.h"
 #include "slvof_dev.cuh"
 #include "mixed32.cuh"
+#include "adj64.cuh"
+#include "flux.cuh"
 
 namespace slvof {
 
 /* ======================================================================================
  * SL update in FP32 local coordinates.
  * ==================================================================================== */
-/* float-float running sum (TwoSum error-free transformation): ~48-bit accumulation of the
- * FP32 sub-tet volumes without using the FP64 pipe. */
-struct FF {
-    float hi, lo;
-};
-__device__ __forceinline__ void ff_add(FF& a, float x)
-{
-    const float s = a.hi + x;
-    const float bb = s - a.hi;
-    const float e = (a.hi - (s - bb)) + (x - bb);
-    a.hi = s;
-    a.lo += e;
-}
-__device__ __forceinline__ void ff_add(FF& a, const FF& b)
-{
-    ff_add(a, b.hi);
-    a.lo += b.lo;
-}
-
 /* One cutTet recursion level: parent tet (vertices 0-3), new vertices on the cutting mesh
  * plane (4-7), their side-1 cell indices packed as bytes, the children's running sums, and
  * case / next child / direction / done flags / cut index packed in meta. */
@@ -240,20 +223,6 @@ __device__ void clip32(const DevMesh& m, const CutCase* tab, const Plane32& PL, 
 
 constexpr int SL32_THREADS = 128;
 
-/* Warp-aggregated slot reservation: returns this lane's slot (or -1 if !flag). */
-__device__ __forceinline__ int warp_slot(bool flag, int* count)
-{
-    const unsigned act = __activemask();
-    const unsigned ballot = __ballot_sync(act, flag);
-    if (!ballot) return -1;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(ballot) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(count, __popc(ballot));
-    base = __shfl_sync(act, base, leader);
-    return flag ? base + __popc(ballot & ((1u << lane) - 1)) : -1;
-}
-
 /* Stage 1 of the SL update, uniform work per band cell: the eight RK pre-image vertices
  * (cell2tets! with project_verts, src/VFgeom.jl:345-420) and their cells (pt2index!).  A cell
  * whose pre-image lies strictly on one side of every donor plane it reaches is finished here
@@ -407,19 +376,6 @@ struct ClipShared {
     uint2 msk[CLIPW_WARPS][CLIPW_BATCH];
 };
 
-__device__ __forceinline__ unsigned wbits(const float4& v) { return (unsigned)__float_as_int(v.w); }
-__device__ __forceinline__ float sel4(float a, float b, float c, float d, int i)
-{
-    return i == 0 ? a : (i == 1 ? b : (i == 2 ? c : d));
-}
-
-/* A donor plane's constant moved from the donor's frame to the frame of the cell at index
- * offset -(a, b, c) from it: w + n.(a, b, c). */
-__device__ __forceinline__ float rel_dt(const float4& p, int a, int b, int c)
-{
-    return p.w + p.x * (float)a + p.y * (float)b + p.z * (float)c;
-}
-
 /* Donor plane at index offset (a, b, c) from the batch cell (i0, j0, k0), in the batch cell's
  * frame: the cache holds the 3x3x3 neighbourhood already moved. */
 __device__ __forceinline__ float4 nbr_plane(const DevMesh& m, const Plane32& PL, const float4* cache, int i0, int j0,
@@ -430,20 +386,6 @@ __device__ __forceinline__ float4 nbr_plane(const DevMesh& m, const Plane32& PL,
     float4 p = __ldg(PL.P + cidx(m, i0 + a, j0 + b, k0 + c));
     p.w = rel_dt(p, a, b, c);
     return p;
-}
-
-/* Side of a node's four vertices against one donor plane (in the batch cell's frame): 1 all
- * strictly liquid, -1 all strictly gas, 0 otherwise. */
-__device__ __forceinline__ int plane_side4(const float4& p, const float4* v)
-{
-    bool neg = true, pos = true;
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-        const float d = fmaf(p.x, v[n].x, fmaf(p.y, v[n].y, fmaf(p.z, v[n].z, -p.w)));
-        neg = neg && d < 0.f;
-        pos = pos && d > 0.f;
-    }
-    return neg ? 1 : (pos ? -1 : 0);
 }
 
 /* box_plane_side for a node: the common side of its four vertices against every donor plane
@@ -764,6 +706,598 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
     if (err) atomicOr(errw, err);
 }
 
+/* ======================================================================================
+ * SL update in flux form (flux.cuh): each face of the band region is swept once and its
+ * volume and liquid are shared by the two cells beside it.
+ *
+ *   k_flux_lists : per band cell, the grid nodes it owns (the first band cell among the
+ *                  node's eight, in offset order) and the faces it owns (its three low
+ *                  faces, and a high face when the cell across it is not a band cell).
+ *   k_flux_nodes : per owned node, its RK pre-image (project!, src/Tools.jl:392-418) as a
+ *                  displacement in cell units; every face that holds the node reads this one
+ *                  value, so neighbouring prisms share their vertices exactly.
+ *   k_flux_faces : per face, the swept volume V of its prisms in FP64 from the node
+ *                  displacements; a face whose points lie strictly on one side of every donor
+ *                  plane of their index box gets its liquid F = V (or 0) here, the others are
+ *                  listed for the clip.
+ *   k_flux_clip  : warp-cooperative FP32 clip of the listed faces' prism tets (cutTet's cuts
+ *                  and cut tables, src/VFgeom.jl:713-900), five faces per warp batch; each
+ *                  face's liquid and volume are summed in float-float and its liquid F is
+ *                  rescaled to the FP64 volume (below).
+ *   k_flux_cells : per band cell, VFnew = (L + sum +-F) / (1 + sum +-V) in cell units.
+ *
+ * The FP32 clip's liquid F32 and volume V32 of a face are sums over the same pieces.  The
+ * face's volume enters every cell in FP64 (V), and its liquid as F = F32 + (V - V32) w with
+ * w = 1 when the face met no gas piece, 0 when it met no liquid piece, else F32/V32 clamped to
+ * [0, 1]: a prism entirely in liquid then carries exactly its volume, so a cell whose
+ * neighbourhood is all liquid keeps VF = 1 exactly (as the reference's vLiq/vol of equal
+ * sums), and one in gas keeps 0.
+ * ==================================================================================== */
+struct FluxBufs {
+    double* nd[3];    /* node displacement (cell units), indexed by the node's cell index */
+    double2* fvf[3];  /* per face direction, by the high cell's index: (V, F) for the low cell */
+    unsigned* nodes;  /* owned nodes: cell index of the node */
+    unsigned* faces;  /* owned faces: (cell index of h) << 2 | dir */
+    unsigned* clip;   /* faces for the clip */
+    int* n_nodes;
+    int* n_faces;
+    int* n_clip;
+    int* work;        /* clip work counter */
+};
+
+__device__ __forceinline__ bool in_band(const DevMesh& m, const short* __restrict__ band, int i, int j, int k)
+{
+    if (i < 1 || j < 1 || k < 1 || i > m.N[0] || j > m.N[1] || k > m.N[2]) return false;
+    return abs((int)band[cidx(m, i, j, k)]) <= m.nband;
+}
+
+__device__ __forceinline__ void cell_of_index(const DevMesh& m, long c, int& i, int& j, int& k)
+{
+    i = m.lo + (int)(c % m.cs1);
+    j = m.lo + (int)((c / m.cs1) % (m.cs2 / m.cs1));
+    k = m.lo + (int)(c / m.cs2);
+}
+
+constexpr int FLUX_THREADS = 128;
+
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_lists(DevMesh m, const short* __restrict__ band,
+                                                             const int* __restrict__ list, const int* __restrict__ count,
+                                                             FluxBufs F)
+{
+    const int n = *count;
+    for (int base = blockIdx.x * FLUX_THREADS; base < n; base += gridDim.x * FLUX_THREADS) {
+        const int t = base + threadIdx.x;
+        const bool act = t < n;
+        int i = 0, j = 0, k = 0;
+        if (act) cell_of(m, list[t], i, j, k);
+        for (int o = 0; o < 8; ++o) {
+            const int a = o & 1, b = (o >> 1) & 1, c = o >> 2;
+            bool own = act;
+            for (int o2 = 0; o2 < o; ++o2)
+                own = own && !in_band(m, band, i + a - (o2 & 1), j + b - ((o2 >> 1) & 1), k + c - (o2 >> 2));
+            const int slot = warp_slot(own, F.n_nodes);
+            if (slot >= 0) F.nodes[slot] = (unsigned)cidx(m, i + a, j + b, k + c);
+        }
+        for (int f = 0; f < 6; ++f) {
+            const int dir = f >> 1;
+            int h[3] = {i, j, k};
+            const bool high = f & 1;
+            if (high) h[dir] += 1;
+            const bool own = act && (!high || !in_band(m, band, h[0], h[1], h[2]));
+            const int slot = warp_slot(own, F.n_faces);
+            if (slot >= 0) F.faces[slot] = ((unsigned)cidx(m, h[0], h[1], h[2]) << 2) | (unsigned)dir;
+        }
+    }
+}
+
+/* FP32 trajectories (project32 from the node itself, so the result is the displacement). */
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32(DevMesh m, float dt, Vel32 V, FluxBufs F)
+{
+    const int n = *F.n_nodes;
+    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
+        const unsigned c = F.nodes[t];
+        int i, j, k;
+        cell_of_index(m, c, i, j, k);
+        float x = 0.f, y = 0.f, z = 0.f;
+        project32(m, V, i, j, k, dt, x, y, z);
+        F.nd[0][c] = x;
+        F.nd[1][c] = y;
+        F.nd[2][c] = z;
+    }
+}
+
+/* FP64 trajectories through the FP64 face velocities (project! in the reference's order). */
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes64(DevMesh m, double dt, adj::Vel V, FluxBufs F)
+{
+    const int n = *F.n_nodes;
+    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
+        const unsigned c = F.nodes[t];
+        int i, j, k;
+        cell_of_index(m, c, i, j, k);
+        const double o[3] = {fco(m, 0, i), fco(m, 1, j), fco(m, 2, k)};
+        double p[3] = {o[0], o[1], o[2]}, xs[3][3];
+        adj::project(m, V, p, i, j, k, dt, xs);
+        F.nd[0][c] = (p[0] - o[0]) / m.d[0];
+        F.nd[1][c] = (p[1] - o[1]) / m.d[1];
+        F.nd[2][c] = (p[2] - o[2]) / m.d[2];
+    }
+}
+
+/* The face's points in the low cell's frame (cell units): corners P[0..3] and, for 24_tets,
+ * the face centre P[4]; their moved copies Q. */
+__device__ __forceinline__ void face_points(const DevMesh& m, const FluxBufs& F, int dir, int hi, int hj, int hk,
+                                            double (*P)[3], double (*Q)[3])
+{
+    int s, t;
+    flux::face_axes(dir, s, t);
+    for (int p = 0; p < 4; ++p) {
+        int i, j, k;
+        flux::corner_node(dir, hi, hj, hk, p, i, j, k);
+        const long c = cidx(m, i, j, k);
+        P[p][dir] = 1.0;
+        P[p][s] = (double)flux::corner_s(p);
+        P[p][t] = (double)flux::corner_t(p);
+        for (int q = 0; q < 3; ++q) Q[p][q] = P[p][q] + F.nd[q][c];
+    }
+    P[4][dir] = 1.0;
+    P[4][s] = 0.5;
+    P[4][t] = 0.5;
+    for (int q = 0; q < 3; ++q) Q[4][q] = 0.25 * (((Q[0][q] + Q[1][q]) + Q[3][q]) + Q[2][q]);
+}
+
+__device__ __forceinline__ void face_decode(const DevMesh& m, unsigned code, int& dir, int& hi, int& hj, int& hk)
+{
+    dir = (int)(code & 3u);
+    cell_of_index(m, (long)(code >> 2), hi, hj, hk);
+}
+
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
+{
+    const int n = *F.n_faces;
+    int err = 0;
+    for (int base = blockIdx.x * FLUX_THREADS; base < n; base += gridDim.x * FLUX_THREADS) {
+        const int t = base + threadIdx.x;
+        bool clip = false;
+        unsigned code = 0;
+        if (t < n) {
+            code = F.faces[t];
+            int dir, hi, hj, hk;
+            face_decode(m, code, dir, hi, hj, hk);
+            double P[5][3], Q[5][3];
+            face_points(m, F, dir, hi, hj, hk, P, Q);
+            const int npt = m.tess == 24 ? 5 : 4;
+            const long hc = (long)(code >> 2);
+            bool flat = true;
+            for (int p = 0; p < npt; ++p) flat = flat && Q[p][dir] == 1.0;
+            if (flat) {
+                F.fvf[dir][hc] = make_double2(0.0, 0.0); /* no motion across the face: a flat prism */
+            } else {
+                int tri[4][3], sg[4];
+                const int nt = flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk),
+                                                    tri, sg);
+                double V = 0.0;
+                for (int tr = 0; tr < nt; ++tr) {
+                    double vt = 0.0;
+                    for (int pn = 0; pn < 3; ++pn) {
+                        int q[4];
+                        flux::prism_tet(tri[tr], pn, q);
+                        const double* a = q[0] < 5 ? P[q[0]] : Q[q[0] - 5];
+                        const double* b = q[1] < 5 ? P[q[1]] : Q[q[1] - 5];
+                        const double* c = q[2] < 5 ? P[q[2]] : Q[q[2] - 5];
+                        const double* d = q[3] < 5 ? P[q[3]] : Q[q[3] - 5];
+                        vt += tet_vol<double>(a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2], d[0], d[1], d[2]);
+                    }
+                    V += sg[tr] > 0 ? vt : -vt;
+                }
+                /* index box of the prism points, relative to the low cell l = h - e_dir */
+                int li = hi, lj = hj, lk = hk;
+                if (dir == 0) --li; else if (dir == 1) --lj; else --lk;
+                int rlo[3], rhi[3];
+                rel_bounds(m, li, lj, lk, rlo, rhi);
+                float px[10], py[10], pz[10];
+                int lo[3] = {0, 0, 0}, hiB[3] = {0, 0, 0};
+                lo[dir] = 1 << 20; hiB[dir] = -(1 << 20);
+                for (int p = 0; p < npt; ++p) {
+                    px[p] = (float)P[p][0]; py[p] = (float)P[p][1]; pz[p] = (float)P[p][2];
+                    px[npt + p] = (float)Q[p][0]; py[npt + p] = (float)Q[p][1]; pz[npt + p] = (float)Q[p][2];
+                    const float u[3] = {px[npt + p], py[npt + p], pz[npt + p]};
+                    for (int q = 0; q < 3; ++q) {
+                        const int I = idx32(u[q], 0, rlo[q], rhi[q], err);
+                        lo[q] = min(lo[q], I);
+                        hiB[q] = max(hiB[q], I);
+                    }
+                }
+                int side = 0;
+                if (m.fast_pure) {
+                    side = npt == 5 ? box_plane_side<10>(m, PL, li, lj, lk, lo[0], hiB[0], lo[1], hiB[1], lo[2], hiB[2],
+                                                         px, py, pz)
+                                    : box_plane_side<8>(m, PL, li, lj, lk, lo[0], hiB[0], lo[1], hiB[1], lo[2], hiB[2],
+                                                        px, py, pz);
+                }
+                F.fvf[dir][hc] = make_double2(V, side > 0 ? V : 0.0);
+                clip = side == 0;
+            }
+        }
+        const int slot = warp_slot(clip, F.n_clip);
+        if (slot >= 0) F.clip[slot] = code;
+    }
+    if (err) atomicOr(errw, err);
+}
+
+constexpr int FCLIP_BATCH = 5; /* faces per warp batch: 30 seed tets for 5_tets and 6_tets */
+constexpr int FCLIP_CAP = 120; /* stack nodes per warp: keeps the block at 55.3 KB, four per SM */
+
+__device__ __forceinline__ void facc_add(FF* acc, int b, float x)
+{
+#pragma unroll
+    for (int q = 0; q < FCLIP_BATCH; ++q)
+        if (q == b) ff_add(acc[q], x);
+}
+__device__ __forceinline__ void facc_add(FF* acc, int b, const FF& x)
+{
+#pragma unroll
+    for (int q = 0; q < FCLIP_BATCH; ++q)
+        if (q == b) ff_add(acc[q], x);
+}
+__device__ __forceinline__ void fflag_or(int* f, int b, int x)
+{
+#pragma unroll
+    for (int q = 0; q < FCLIP_BATCH; ++q)
+        if (q == b) f[q] |= x;
+}
+
+struct FluxShared {
+    CutCase tab[16];
+    float4 stk[CLIPW_WARPS][4][FCLIP_CAP];
+    float4 scr[8][CLIPW_WARPS * 32];
+    float4 pl[CLIPW_WARPS][FCLIP_BATCH][CLIPW_NBR];
+    uint2 msk[CLIPW_WARPS][FCLIP_BATCH];
+};
+
+enum : int { PIECE_LIQ = 1, PIECE_GAS = 2 };
+
+__global__ void __launch_bounds__(CLIPW_WARPS * 32) k_flux_clip(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
+{
+    extern __shared__ __align__(16) unsigned char flux_smem[];
+    FluxShared& S = *reinterpret_cast<FluxShared*>(flux_smem);
+    for (int t = threadIdx.x; t < 16 * (int)sizeof(CutCase); t += blockDim.x)
+        reinterpret_cast<char*>(S.tab)[t] = reinterpret_cast<const char*>(c_cut)[t];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+    const unsigned lanemask_lt = (1u << lane) - 1u;
+    const int n_faces = *F.n_clip;
+    const int ntet = m.tess == 24 ? 12 : 6; /* prism tets per face */
+    const int B = m.tess == 24 ? 2 : FCLIP_BATCH;
+    int err = 0;
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(F.work, B);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n_faces) break;
+        const int nb = min(B, n_faces - base);
+        /* lane b < nb holds face b: its code and low cell */
+        unsigned code_ = 0;
+        int fd_ = 0, li_ = 0, lj_ = 0, lk_ = 0;
+        if (lane < nb) {
+            code_ = F.clip[base + lane];
+            int hi, hj, hk;
+            face_decode(m, code_, fd_, hi, hj, hk);
+            li_ = hi - (fd_ == 0); lj_ = hj - (fd_ == 1); lk_ = hk - (fd_ == 2);
+        }
+        /* donor planes of each face's low cell's 3x3x3 neighbourhood, in that cell's frame */
+        for (int t0 = 0; t0 < FCLIP_BATCH * CLIPW_NBR; t0 += 32) {
+            const int t = t0 + lane;
+            const int b = min(t / CLIPW_NBR, FCLIP_BATCH - 1);
+            const int ii = __shfl_sync(0xffffffffu, li_, b), jj = __shfl_sync(0xffffffffu, lj_, b),
+                      kk = __shfl_sync(0xffffffffu, lk_, b);
+            if (t < nb * CLIPW_NBR) {
+                const int r = t - b * CLIPW_NBR;
+                const int a = r % 3 - 1, bq = (r / 3) % 3 - 1, c = r / 9 - 1;
+                float4 p = __ldg(PL.P + cidx(m, ii + a, jj + bq, kk + c));
+                p.w = rel_dt(p, a, bq, c);
+                S.pl[w][b][r] = p;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int bb = 0; bb < FCLIP_BATCH; ++bb) {
+            float4 p = make_float4(1.f, 0.f, 0.f, 0.f);
+            if (bb < nb && lane < CLIPW_NBR) p = S.pl[w][bb][lane];
+            const bool pure = p.x == 0.f && p.y == 0.f && p.z == 0.f;
+            const unsigned l_ = __ballot_sync(0xffffffffu, pure && p.w > 0.f);
+            const unsigned g_ = __ballot_sync(0xffffffffu, pure && p.w < 0.f);
+            if (lane == 0) S.msk[w][bb] = make_uint2(l_, g_);
+        }
+        __syncwarp();
+        /* seed: lane q < ntet*nb takes prism tet q % ntet of face q / ntet, oriented for the
+         * low cell (two vertices swapped where sigma is -1); its tag (face in batch) in
+         * vertex 0 */
+        FF acc[FCLIP_BATCH], avol[FCLIP_BATCH];
+        int flg[FCLIP_BATCH];
+#pragma unroll
+        for (int b = 0; b < FCLIP_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; flg[b] = 0; }
+        const unsigned code = __shfl_sync(0xffffffffu, code_, min(lane / ntet, FCLIP_BATCH - 1));
+        if (lane < ntet * nb) {
+            const int b = lane / ntet, n = lane - ntet * b;
+            int dir, hi, hj, hk;
+            face_decode(m, code, dir, hi, hj, hk);
+            double P[5][3], Q[5][3];
+            face_points(m, F, dir, hi, hj, hk, P, Q);
+            int tri[4][3], sg[4];
+            flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
+            int q[4];
+            flux::prism_tet(tri[n / 3], n % 3, q);
+            if (sg[n / 3] < 0) { const int x = q[0]; q[0] = q[1]; q[1] = x; }
+            const int li = hi - (dir == 0), lj = hj - (dir == 1), lk = hk - (dir == 2);
+            int rlo[3], rhi[3];
+            rel_bounds(m, li, lj, lk, rlo, rhi);
+            float4 v[4];
+            int I[4][3];
+            int mlo = 1 << 20;
+            for (int nn = 0; nn < 4; ++nn) {
+                const double* x = q[nn] < 5 ? P[q[nn]] : Q[q[nn] - 5];
+                v[nn] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
+                if (q[nn] >= 5) {
+                    I[nn][0] = idx32(v[nn].x, 0, rlo[0], rhi[0], err);
+                    I[nn][1] = idx32(v[nn].y, 0, rlo[1], rhi[1], err);
+                    I[nn][2] = idx32(v[nn].z, 0, rlo[2], rhi[2], err);
+                    mlo = min(mlo, I[nn][dir]);
+                }
+            }
+            /* the face's own points lie on the plane between l (0) and h (1) and inside the
+             * tangential range of l's column: index 0 across, and along dir the side of this
+             * tet's moved points (either index contains them) */
+            for (int nn = 0; nn < 4; ++nn)
+                if (q[nn] < 5) {
+                    I[nn][0] = I[nn][1] = I[nn][2] = 0;
+                    I[nn][dir] = mlo >= 1 ? 1 : 0;
+                }
+            for (int nn = 0; nn < 4; ++nn) {
+                unsigned pk = pack3(I[nn][0], I[nn][1], I[nn][2]);
+                if (nn == 0) pk |= (unsigned)b << 24;
+                v[nn].w = __int_as_float((int)pk);
+                S.stk[w][nn][lane] = v[nn];
+            }
+        }
+        int size = ntet * nb;
+        __syncwarp();
+        int guard = 0;
+        while (size > 0) {
+            if (++guard > 1 << 20) { err |= ERR_DEPTH; break; }
+            const int n = min(32, size);
+            const int top = size - n;
+            const bool act = lane < n;
+            float4 v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = act ? S.stk[w][q][top + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+            __syncwarp();
+            size = top;
+            const unsigned tag = wbits(v[0]) >> 24;
+            const int b = (int)(tag & 7u);
+            int flags = (int)((tag >> 3) & 7u);
+            const int i0 = __shfl_sync(0xffffffffu, li_, b), j0 = __shfl_sync(0xffffffffu, lj_, b),
+                      k0 = __shfl_sync(0xffffffffu, lk_, b);
+            const float4* cache = S.pl[w][b];
+            int mode = 0; /* 0 idle, 1 leaf (pruned or PLIC), 2 cut */
+            int cs = 0, dir = -1, cut = 0, nchild = 0;
+            int rlo[3], rhi[3];
+            int cind[4][3];
+            float d0 = 0.f, d1 = 0.f, d2 = 0.f, d3 = 0.f;
+            if (act) {
+                rel_bounds(m, i0, j0, k0, rlo, rhi);
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) cind[nn][q] = unpack(wbits(v[nn]), q);
+                int lo[3], hi[3];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    lo[q] = min(min(cind[0][q], cind[1][q]), min(cind[2][q], cind[3][q]));
+                    hi[q] = max(max(cind[0][q], cind[1][q]), max(cind[2][q], cind[3][q]));
+                }
+                const uint2 mk = S.msk[w][b];
+                const int bp = m.fast_pure ? node_side(m, PL, cache, mk.x, mk.y, i0, j0, k0, lo, hi, v) : 0;
+                if (bp != 0) {
+                    mode = 1;
+                    cs = bp > 0 ? 0 : 15;
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        if (dir >= 0 || (flags & (1 << q))) continue;
+                        if (hi[q] > lo[q]) { dir = q; cut = hi[q]; }
+                        else flags |= 1 << q;
+                    }
+                    if (dir < 0) {
+                        mode = 1;
+                        const float4 p = nbr_plane(m, PL, cache, i0, j0, k0, cind[0][0], cind[0][1], cind[0][2]);
+                        const float Dt = p.w;
+                        d0 = p.x * v[0].x + p.y * v[0].y + p.z * v[0].z - Dt;
+                        d1 = p.x * v[1].x + p.y * v[1].y + p.z * v[1].z - Dt;
+                        d2 = p.x * v[2].x + p.y * v[2].y + p.z * v[2].z - Dt;
+                        d3 = p.x * v[3].x + p.y * v[3].y + p.z * v[3].z - Dt;
+                    } else {
+                        mode = 2;
+                        const float pl = (float)cut;
+                        d0 = (dir == 0 ? v[0].x : (dir == 1 ? v[0].y : v[0].z)) - pl;
+                        d1 = (dir == 0 ? v[1].x : (dir == 1 ? v[1].y : v[1].z)) - pl;
+                        d2 = (dir == 0 ? v[2].x : (dir == 1 ? v[2].y : v[2].z)) - pl;
+                        d3 = (dir == 0 ? v[3].x : (dir == 1 ? v[3].y : v[3].z)) - pl;
+                    }
+                    cs = d2case(d0, d1, d2, d3, 1e-30f, err);
+                    if (mode == 2) nchild = S.tab[cs].ntets;
+                }
+            }
+            int incl = nchild;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, off);
+                if (lane >= off) incl += y;
+            }
+            const unsigned cutmask = __ballot_sync(0xffffffffu, mode == 2);
+            const int later_cuts = __popc(cutmask) - __popc(cutmask & (lanemask_lt | (1u << lane)));
+            const bool fits = mode == 2 && size + incl + later_cuts <= FCLIP_CAP;
+            const unsigned fitmask = __ballot_sync(0xffffffffu, fits);
+            bool back = mode == 2 && !fits;
+            bool priv = false;
+            if (!fitmask && cutmask && lane == __ffs(cutmask) - 1) { back = false; priv = true; }
+            const int pushed = fits ? nchild : 0;
+            int ipush = pushed;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, ipush, off);
+                if (lane >= off) ipush += y;
+            }
+            const int tot_push = __shfl_sync(0xffffffffu, ipush, 31);
+            const unsigned backmask = __ballot_sync(0xffffffffu, back);
+            if (mode == 1 || fits) {
+                const CutCase& C = S.tab[cs];
+                unsigned s1p[4];
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn) {
+                    int a0 = cind[nn][0], a1 = cind[nn][1], a2 = cind[nn][2];
+                    if (mode == 2) {
+                        if (dir == 0) a0 = min(a0, cut - 1);
+                        else if (dir == 1) a1 = min(a1, cut - 1);
+                        else a2 = min(a2, cut - 1);
+                    }
+                    s1p[nn] = pack3(a0, a1, a2);
+                    S.scr[nn][tid] = make_float4(v[nn].x, v[nn].y, v[nn].z, __int_as_float((int)s1p[nn]));
+                }
+                const int nvert = C.nvert;
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn) {
+                    if (nn >= nvert) break;
+                    const int e1 = C.v1[nn], e2 = C.v2[nn];
+                    const float4 A = S.scr[e1][tid], Bv = S.scr[e2][tid];
+                    const float da = sel4(d0, d1, d2, d3, e1), db = sel4(d0, d1, d2, d3, e2);
+                    const float den = db - da;
+                    const float mu = fminf(1.f, fmaxf(0.f, den != 0.f ? -da / den : 1.f));
+                    const float x = fmaf(mu, Bv.x - A.x, A.x);
+                    const float y = fmaf(mu, Bv.y - A.y, A.y);
+                    const float z = fmaf(mu, Bv.z - A.z, A.z);
+                    unsigned pk = 0u;
+                    if (mode == 2) {
+                        const unsigned pa = wbits(A), pb = wbits(Bv);
+                        int nv[3];
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const float u = q == 0 ? x : (q == 1 ? y : z);
+                            const int Iv = idx32(u, unpack(s1p[nn], q), rlo[q], rhi[q], err);
+                            const int a1 = unpack(pa, q), a2 = unpack(pb, q);
+                            nv[q] = min(max(Iv, min(a1, a2)), max(a1, a2));
+                        }
+                        if (dir == 0) nv[0] = cut - 1;
+                        else if (dir == 1) nv[1] = cut - 1;
+                        else nv[2] = cut - 1;
+                        pk = pack3(nv[0], nv[1], nv[2]);
+                    }
+                    S.scr[4 + nn][tid] = make_float4(x, y, z, __int_as_float((int)pk));
+                }
+                const int nt = C.ntets;
+                if (mode == 1) {
+                    int fl = 0;
+                    for (int c = 0; c < nt; ++c) {
+                        const float4 P0 = S.scr[C.vtet[c][0]][tid], P1 = S.scr[C.vtet[c][1]][tid];
+                        const float4 P2 = S.scr[C.vtet[c][2]][tid], P3 = S.scr[C.vtet[c][3]][tid];
+                        const float tv = tet_vol<float>(P0.x, P0.y, P0.z, P1.x, P1.y, P1.z, P2.x, P2.y, P2.z, P3.x,
+                                                        P3.y, P3.z);
+                        facc_add(avol, b, tv);
+                        if (C.side[c] == 0) { facc_add(acc, b, tv); fl |= PIECE_LIQ; }
+                        else fl |= PIECE_GAS;
+                    }
+                    fflag_or(flg, b, fl);
+                } else {
+                    const int pos = size + ipush - pushed;
+                    const unsigned tagc = ((unsigned)b | ((unsigned)flags << 3)) << 24;
+                    const int sh = 8 * dir;
+                    for (int c = 0; c < nt; ++c) {
+                        const bool up = C.side[c] == 1;
+#pragma unroll
+                        for (int nn = 0; nn < 4; ++nn) {
+                            float4 qv = S.scr[C.vtet[c][nn]][tid];
+                            unsigned pk = wbits(qv);
+                            if (up) pk = (pk & ~(255u << sh)) | ((unsigned)(cut + 128) << sh);
+                            if (nn == 0) pk |= tagc;
+                            qv.w = __int_as_float((int)pk);
+                            S.stk[w][nn][pos + c] = qv;
+                        }
+                    }
+                }
+            } else if (priv) {
+                FF rv, rl;
+                float cx[4], cy[4], cz[4];
+#pragma unroll
+                for (int nn = 0; nn < 4; ++nn) { cx[nn] = v[nn].x; cy[nn] = v[nn].y; cz[nn] = v[nn].z; }
+                clip32(m, S.tab, PL, nullptr, i0, j0, k0, rlo, rhi, cx, cy, cz, cind, rv, rl, err);
+                facc_add(avol, b, rv);
+                facc_add(acc, b, rl);
+                fflag_or(flg, b, PIECE_LIQ | PIECE_GAS);
+            }
+            if (back) {
+                const int p = size + tot_push + __popc(backmask & lanemask_lt);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) S.stk[w][q][p] = v[q];
+            }
+            size += tot_push + __popc(backmask);
+            __syncwarp();
+        }
+        /* per face: fixed-order shuffle tree, then the liquid rescaled to the FP64 volume */
+#pragma unroll
+        for (int b = 0; b < FCLIP_BATCH; ++b) {
+            if (b >= nb) break;
+            double fl = (double)acc[b].hi + (double)acc[b].lo;
+            double u = (double)avol[b].hi + (double)avol[b].lo;
+            int fg = flg[b];
+            for (int off = 16; off > 0; off >>= 1) {
+                fl += __shfl_xor_sync(0xffffffffu, fl, off);
+                u += __shfl_xor_sync(0xffffffffu, u, off);
+                fg |= __shfl_xor_sync(0xffffffffu, fg, off);
+            }
+            if (lane == b) {
+                double2* out = F.fvf[fd_] + (code_ >> 2);
+                const double V = out->x;
+                double wgt;
+                if (!(fg & PIECE_GAS)) wgt = 1.0;
+                else if (!(fg & PIECE_LIQ)) wgt = 0.0;
+                else wgt = u != 0.0 ? fmin(1.0, fmax(0.0, fl / u)) : 0.5;
+                out->y = fl + (V - u) * wgt;
+            }
+        }
+        __syncwarp();
+    }
+    if (err) atomicOr(errw, err);
+}
+
+/* VFnew = (L + sum +-F) / (1 + sum +-V) over the cell's six faces, in cell units; L is the
+ * cell's own liquid, VF (0 below VFlo, 1 above VFhi). */
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const double* __restrict__ VFin,
+                                                             double* __restrict__ VFout, const int* __restrict__ list,
+                                                             const int* __restrict__ count, FluxBufs F, int* errw)
+{
+    const int n = *count;
+    int err = 0;
+    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
+        int i, j, k;
+        cell_of(m, list[t], i, j, k);
+        const long v = vidx(m, i, j, k);
+        const double vf = VFin[v];
+        double vol = 1.0, liq = vf < m.VFlo ? 0.0 : (vf > m.VFhi ? 1.0 : vf);
+        const long c = cidx(m, i, j, k);
+        const long st[3] = {1, m.cs1, m.cs2};
+#pragma unroll
+        for (int dir = 0; dir < 3; ++dir) {
+            const double2 lo = F.fvf[dir][c], hi = F.fvf[dir][c + st[dir]];
+            vol -= lo.x;
+            liq -= lo.y;
+            vol += hi.x;
+            liq += hi.y;
+        }
+        if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
+        VFout[v] = liq / vol;
+    }
+    if (err) atomicOr(errw, err);
+}
+
 /* ---- launchers ------------------------------------------------------------------------ */
 void launch_sl32_pre(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
                      const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
@@ -794,6 +1328,31 @@ void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, co
     launch_sl32_pre(m, dt, VFout, uf, vf, wf, planes, phase, list, count, work, slow_cells, slow_verts, slow_count,
                     errw, nsm, s);
     launch_sl32_clip(m, VFout, planes, work2, slow_cells, slow_verts, slow_count, errw, nsm, s);
+}
+
+
+void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* VFout, const float* uf32,
+                      const float* vf32, const float* wf32, const double* uf, const double* vf, const double* wf,
+                      const float4* planes, const short* band, const int* list, const int* count,
+                      const FluxLaunch& L, int* errw, int nsm, cudaStream_t s)
+{
+    FluxBufs F{{L.nd[0], L.nd[1], L.nd[2]}, {L.fvf[0], L.fvf[1], L.fvf[2]}, L.nodes, L.faces, L.clip,
+               L.ctr, L.ctr + 1, L.ctr + 2, L.ctr + 3};
+    Plane32 PL{planes};
+    cudaMemsetAsync(L.ctr, 0, 4 * sizeof(int), s);
+    k_flux_lists<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, band, list, count, F);
+#if SLVOF_FLUX_TRAJ64
+    (void)uf32; (void)vf32; (void)wf32;
+    k_flux_nodes64<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, adj::Vel{uf, vf, wf}, F);
+#else
+    (void)uf; (void)vf; (void)wf;
+    k_flux_nodes32<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, (float)dt, Vel32{uf32, vf32, wf32}, F);
+#endif
+    k_flux_faces<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, PL, F, errw);
+    const int smem = (int)sizeof(FluxShared);
+    cudaFuncSetAttribute(k_flux_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_flux_clip<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, PL, F, errw);
+    k_flux_cells<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, VFin, VFout, list, count, F, errw);
 }
 
 } // namespace slvof

@@ -126,4 +126,65 @@ __device__ __forceinline__ void rel_bounds(const DevMesh& m, int i, int j, int k
     rhi[0] = min(m.hi[0] - i, REL); rhi[1] = min(m.hi[1] - j, REL); rhi[2] = min(m.hi[2] - k, REL);
 }
 
+/* ---- pieces of the warp-cooperative clips (k_mixed.cu, k_flux.cu) ------------------- */
+/* float-float running sum (TwoSum error-free transformation): ~48-bit accumulation of the
+ * FP32 sub-tet volumes without using the FP64 pipe. */
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF& a, float x)
+{
+    const float s = a.hi + x;
+    const float bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (x - bb);
+    a.hi = s;
+    a.lo += e;
+}
+__device__ __forceinline__ void ff_add(FF& a, const FF& b)
+{
+    ff_add(a, b.hi);
+    a.lo += b.lo;
+}
+
+/* Warp-aggregated slot reservation: returns this lane's slot (or -1 if !flag). */
+__device__ __forceinline__ int warp_slot(bool flag, int* count)
+{
+    const unsigned act = __activemask();
+    const unsigned ballot = __ballot_sync(act, flag);
+    if (!ballot) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(ballot) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(ballot));
+    base = __shfl_sync(act, base, leader);
+    return flag ? base + __popc(ballot & ((1u << lane) - 1)) : -1;
+}
+
+__device__ __forceinline__ unsigned wbits(const float4& v) { return (unsigned)__float_as_int(v.w); }
+__device__ __forceinline__ float sel4(float a, float b, float c, float d, int i)
+{
+    return i == 0 ? a : (i == 1 ? b : (i == 2 ? c : d));
+}
+
+/* A donor plane's constant moved from the donor's frame to the frame of the cell at index
+ * offset -(a, b, c) from it: w + n.(a, b, c). */
+__device__ __forceinline__ float rel_dt(const float4& p, int a, int b, int c)
+{
+    return p.w + p.x * (float)a + p.y * (float)b + p.z * (float)c;
+}
+
+/* Side of a node's four vertices against one donor plane (in the batch cell's frame): 1 all
+ * strictly liquid, -1 all strictly gas, 0 otherwise. */
+__device__ __forceinline__ int plane_side4(const float4& p, const float4* v)
+{
+    bool neg = true, pos = true;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        const float d = fmaf(p.x, v[n].x, fmaf(p.y, v[n].y, fmaf(p.z, v[n].z, -p.w)));
+        neg = neg && d < 0.f;
+        pos = pos && d > 0.f;
+    }
+    return neg ? 1 : (pos ? -1 : 0);
+}
+
 } // namespace slvof

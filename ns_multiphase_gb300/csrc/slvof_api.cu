@@ -38,6 +38,7 @@ struct slvof_ctx {
     int2* arb = nullptr;          /* mixed ELVIRA: near-tie cells (cell, contending lanes) for FP64 scoring */
     int* slow_cells = nullptr;    /* mixed SL: cells that need the clip */
     float4* slow_verts = nullptr; /* mixed SL: their pre-image vertices (cell units) + packed indices */
+    FluxLaunch flux{};            /* mixed SL in flux form: node displacements, face sums, lists */
     signed char* phase = nullptr; /* pure-donor codes of the PLIC pass */
     signed char* cand = nullptr;  /* ELVIRA: chosen candidate lane of each interface cell */
     /* reverse pass (allocated on first use) */
@@ -253,6 +254,20 @@ int join_band(slvof_ctx* c, int r)
     return 0;
 }
 
+/* Mixed SL update of the band cells into VF[o]: the flux form (each face swept once, its
+ * volume in FP64 and its liquid from the FP32 clip, shared by the two cells beside it). */
+void st_sl32(slvof_ctx* c, double dt, int o)
+{
+#if SLVOF_SL_CELLFORM
+    launch_sl32(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
+                c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR,
+                c->nsm, c->stream);
+#else
+    launch_sl32_flux(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf32, c->vf32, c->wf32, c->uf, c->vf, c->wf, c->planes,
+                     c->band[c->bcur], c->list_sl, c->ctr + C_SL, c->flux, c->ctr + C_ERR, c->nsm, c->stream);
+#endif
+}
+
 int st_transport(slvof_ctx* c, double dt)
 {
     const int o = 1 - c->vcur;
@@ -269,9 +284,7 @@ int st_transport(slvof_ctx* c, double dt)
         launch_sl64(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->phase,
                     c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
     else
-        launch_sl32(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
-                    c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW,
-                    c->ctr + C_ERR, c->nsm, c->stream);
+        st_sl32(c, dt, o);
     s_end(c, S_SL);
     s_beg(c, S_VFGHOST);
     launch_vf_ghost(c->m, c->VF[c->vcur], c->VF[o], c->nsm, c->stream);
@@ -438,6 +451,8 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
     const long N[3] = {mesh->Nx, mesh->Ny, mesh->Nz};
     const long n0 = N[0] + 2 * g, n1 = N[1] + 2 * g, n2 = N[2] + 2 * g;
     if (n0 * n1 * n2 > (1L << 31) - 1 || N[0] > 30000 || N[1] > 30000 || N[2] > 30000) return SLVOF_E_UNSUPPORTED;
+    /* the mixed path's face lists hold (cell index << 2 | direction) in 32 bits */
+    if (precision == SLVOF_MIXED && n0 * n1 * n2 >= (1L << 30)) return SLVOF_E_UNSUPPORTED;
     slvof_ctx* c = new slvof_ctx();
     c->precision = precision;
     auto bail = [&](int code) {
@@ -483,6 +498,15 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
              alloc((void**)&c->slow_cells, interior * sizeof(int)) &&
              alloc((void**)&c->slow_verts, interior * (mesh->tesselation == 24 ? 16 : 8) * sizeof(float4)) &&
              alloc((void**)&c->arb, interior * sizeof(int2));
+    if (ok && precision == SLVOF_MIXED) {
+        for (int q = 0; q < 3 && ok; ++q)
+            ok = alloc((void**)&c->flux.nd[q], c->ncell * sizeof(double)) &&
+                 alloc((void**)&c->flux.fvf[q], c->ncell * sizeof(double2));
+        ok = ok && alloc((void**)&c->flux.nodes, c->ncell * sizeof(unsigned)) &&
+             alloc((void**)&c->flux.faces, 3 * c->ncell * sizeof(unsigned)) &&
+             alloc((void**)&c->flux.clip, 3 * c->ncell * sizeof(unsigned)) &&
+             alloc((void**)&c->flux.ctr, 4 * sizeof(int));
+    }
     if (!ok) return bail(SLVOF_E_NOMEM);
     /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
     std::vector<double> h(ncoord);
@@ -516,6 +540,8 @@ int slvof_destroy(slvof_ctx* c)
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],
                     c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
                     c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo, c->gvel32[0], c->gvel32[1], c->gvel32[2],
+                    c->flux.nd[0], c->flux.nd[1], c->flux.nd[2], c->flux.fvf[0], c->flux.fvf[1], c->flux.fvf[2],
+                    c->flux.nodes, c->flux.faces, c->flux.clip, c->flux.ctr,
                     c->cu, c->cv, c->cw, c->us, c->vs, c->ws, c->pr[0], c->pr[1], c->pr[2], c->pr[3],
                     c->pr[4], c->pr[5], c->pr[6], c->pr[7], c->pr[8], c->pr[9], c->pr[10], c->pr_band};
     for (void* b : bufs)
@@ -565,7 +591,10 @@ int slvof_counters(const slvof_ctx* c, int* out, int n)
     if (!c || !out || n < 0) return SLVOF_E_ARG;
     int h[C_N] = {0};
     if (cudaMemcpy(h, c->ctr, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) return SLVOF_E_CUDA;
-    const int v[SLVOF_NCOUNTERS] = {h[C_SL], h[C_IF], h[C_SLOW], h[C_PL], h[C_ARB]};
+    int f[4] = {0, 0, 0, 0};
+    if (c->flux.ctr && cudaMemcpy(f, c->flux.ctr, sizeof f, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return SLVOF_E_CUDA;
+    const int v[SLVOF_NCOUNTERS] = {h[C_SL], h[C_IF], h[C_SLOW], h[C_PL], h[C_ARB], f[0], f[1], f[2]};
     for (int q = 0; q < n && q < SLVOF_NCOUNTERS; ++q) out[q] = v[q];
     return SLVOF_OK;
 }
@@ -1159,8 +1188,8 @@ int adjoint_step32(slvof_ctx* c, double dt, const double* d_next, AdjBuffers& b)
     launch_sl32_pre(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
                     c->ctr + C_SLW, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR, c->nsm, c->stream);
     if (!d_next) {
-        launch_sl32_clip(c->m, c->VF[o], c->planes, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW,
-                         c->ctr + C_ERR, c->nsm, c->stream);
+        /* the step's result as the forward computes it */
+        st_sl32(c, dt, o);
         d_next = c->VF[o];
     }
     launch_adjoint32_sl(c->m, dt, d_next, c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->slow_cells,

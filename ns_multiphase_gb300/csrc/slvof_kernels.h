@@ -52,6 +52,21 @@ void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const doub
                           const int* list, const int* count, int* work, int* errw, int nsm, cudaStream_t s);
 
 /* k_mixed.cu, k_elvira_mixed.cu */
+/* the mixed path's SL update in flux form: node displacements and per-direction face
+ * (volume, liquid) arrays indexed like the cell arrays, the node / face / clip-face lists
+ * (capacity: cells, 3 x cells, 3 x cells) and four counters */
+struct FluxLaunch {
+    double* nd[3];
+    double2* fvf[3];
+    unsigned* nodes;
+    unsigned* faces;
+    unsigned* clip;
+    int* ctr;
+};
+void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* VFout, const float* uf32,
+                      const float* vf32, const float* wf32, const double* uf, const double* vf, const double* wf,
+                      const float4* planes, const short* band, const int* list, const int* count,
+                      const FluxLaunch& L, int* errw, int nsm, cudaStream_t s);
 /* mixed ELVIRA: FP32 scoring (warp per cell), FP64 arbitration of the near-ties listed in arb
  * (n_arb zeroed by the caller; capacity: the interface count), FP64 winner normals */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,

@@ -174,7 +174,8 @@ class SLVOF:
         self.L.slvof_stage_ms(self.h, a.ctypes.data, len(a))
         return dict(zip(self.STAGES, a.tolist()))
 
-    COUNTERS = ("band_cells", "interface_cells", "clipped_cells", "plic_solves", "fp64_arbitrations")
+    COUNTERS = ("band_cells", "interface_cells", "clipped_cells", "plic_solves", "fp64_arbitrations",
+                "traced_nodes", "swept_faces", "clipped_faces")
 
     def counters(self) -> dict:
         a = np.zeros(len(self.COUNTERS), dtype=np.int32)

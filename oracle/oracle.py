@@ -79,6 +79,12 @@ def lib():
         L.orc_compute_band.argtypes = [p, p, p]
         L.orc_vf_ghost_fill.restype = i
         L.orc_vf_ghost_fill.argtypes = [p, p]
+        L.orc_compute_plic_slab.restype = i
+        L.orc_compute_plic_slab.argtypes = [p, p, p, p, p, p, i, i]
+        L.orc_compute_band_slab.restype = i
+        L.orc_compute_band_slab.argtypes = [p, p, p, i, i]
+        L.orc_vf_spheres.restype = i
+        L.orc_vf_spheres.argtypes = [p, p, p, i, i, i, p]
         L.orc_transport.restype = i
         L.orc_transport.argtypes = [p, d, p, p, p, p, p, p, p, p, p, p, i, i]
         L.orc_sl_cell.restype = d
@@ -123,6 +129,26 @@ class Oracle:
 
     def vf_ghost_fill(self, VF):
         self.L.orc_vf_ghost_fill(_m(self.mesh), _p(VF))
+
+    def vf_spheres(self, centres, radii, nF=20, dims=3):
+        """VF of a union of spheres by VFsphere's rule (src/Tools.jl:907-922), ghosts filled:
+        the CPU baseline's copy of the workload the GPU library generates on the device."""
+        c = np.ascontiguousarray(centres, dtype=np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(radii, dtype=np.float64).reshape(-1)
+        VF = self.mesh.vf_array()
+        self.L.orc_vf_spheres(_m(self.mesh), c.ctypes.data, r.ctypes.data, len(r), nF, dims, _p(VF))
+        self.vf_ghost_fill(VF)
+        return VF
+
+    def computePLIC_slab(self, nx, ny, nz, VF, D, klo, khi):
+        """computePLIC!'s per-cell work on the cells k in [klo, khi] (CPU baseline sample)."""
+        self.L.orc_compute_plic_slab(_m(self.mesh), _p(D), _p(nx), _p(ny), _p(nz), _p(VF), klo, khi)
+        return D
+
+    def computeBand_slab(self, VF, band, klo, khi):
+        """computeBand!'s per-cell passes on the cells k in [klo, khi] (CPU baseline sample)."""
+        self.L.orc_compute_band_slab(_m(self.mesh), _p(band), _p(VF), klo, khi)
+        return band
 
     def ELVIRA(self, VF, nx=None, ny=None, nz=None, klo=1, khi=0):
         m = self.mesh

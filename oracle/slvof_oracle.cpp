@@ -1203,10 +1203,19 @@ int orc_elvira(const orc_mesh* M, const double* VF, double* nx, double* ny, doub
 {
     Grid G(M);
     const long ncell = G.n[0] * G.n[1] * G.n[2];
-    if (klo > khi) { klo = 1; khi = G.N[2]; }
-    std::fill(nx, nx + ncell, 0.0);
-    std::fill(ny, ny + ncell, 0.0);
-    std::fill(nz, nz + ncell, 0.0);
+    if (klo > khi) {
+        klo = 1;
+        khi = G.N[2];
+        std::fill(nx, nx + ncell, 0.0);
+        std::fill(ny, ny + ncell, 0.0);
+        std::fill(nz, nz + ncell, 0.0);
+    } else {
+        /* sample: the slab's own layers are zeroed, as the whole arrays are for the full grid */
+        const long a = G.c(G.lo[0], G.lo[1], klo), b = G.c(G.lo[0], G.lo[1], khi + 1);
+        std::fill(nx + a, nx + b, 0.0);
+        std::fill(ny + a, ny + b, 0.0);
+        std::fill(nz + a, nz + b, 0.0);
+    }
     Fields F{&G, VF};
     int flags = 0;
 #pragma omp parallel for collapse(2) schedule(dynamic, 1) reduction(| : flags)
@@ -1237,13 +1246,32 @@ int orc_compute_plic(const orc_mesh* M, double* D, const double* nx, const doubl
     return 0;
 }
 
-/* computeBand! (src/VF.jl:16-74).  Julia's combined for-loop "break" leaves all three loops. */
-int orc_compute_band(const orc_mesh* M, int16_t* band, const double* VF)
+/* computePLIC!'s per-cell work on the cells k in [klo, khi] only (CPU baseline sample). */
+int orc_compute_plic_slab(const orc_mesh* M, double* D, const double* nx, const double* ny, const double* nz,
+                          const double* VF, int klo, int khi)
+{
+    Grid G(M);
+#pragma omp parallel for collapse(2)
+    for (int k = klo; k <= khi; ++k)
+        for (int j = G.lo[1]; j <= G.hi[1]; ++j)
+            for (int i = G.lo[0]; i <= G.hi[0]; ++i) {
+                const long c = G.c(i, j, k);
+                D[c] = compute_dist(G, i, j, k, nx[c], ny[c], nz[c], VF[G.v(i, j, k)]);
+            }
+    return 0;
+}
+
+/* computeBand! (src/VF.jl:16-74) on the cells k in [klo, khi]; the ghost updates only for
+ * the whole grid (the CPU baseline's sample times the per-cell passes of a slab).  Julia's
+ * combined for-loop "break" leaves all three loops. */
+static void compute_band_k(const orc_mesh* M, int16_t* band, const double* VF, int klo, int khi, bool borders)
 {
     Grid G(M);
     const int nb = M->nband;
     Arr3<int16_t> B(band, G.lo, G.hi);
-    for (int k = 1; k <= G.N[2]; ++k)
+    /* the first pass reads VF only: cells are independent; the sweeps update in place */
+#pragma omp parallel for collapse(2)
+    for (int k = klo; k <= khi; ++k)
         for (int j = 1; j <= G.N[1]; ++j)
             for (int i = 1; i <= G.N[0]; ++i) {
                 const double v = VF[G.v(i, j, k)];
@@ -1266,10 +1294,12 @@ int orc_compute_band(const orc_mesh* M, int16_t* band, const double* VF)
                     b = 0;
                 }
             }
-    neumann(G, B);
-    update_borders(G, B);
+    if (borders) {
+        neumann(G, B);
+        update_borders(G, B);
+    }
     for (int n = 1; n <= nb; ++n) {
-        for (int k = 1; k <= G.N[2]; ++k)
+        for (int k = klo; k <= khi; ++k)
             for (int j = 1; j <= G.N[1]; ++j)
                 for (int i = 1; i <= G.N[0]; ++i) {
                     int16_t& b = B.at(i, j, k);
@@ -1280,8 +1310,20 @@ int orc_compute_band(const orc_mesh* M, int16_t* band, const double* VF)
                                     if (std::abs((int)B.at(ii, jj, kk)) == n - 1) b = (int16_t)(n * (b > 0 ? 1 : (b < 0 ? -1 : 0)));
                     }
                 }
-        update_borders(G, B);
+        if (borders) update_borders(G, B);
     }
+}
+
+int orc_compute_band(const orc_mesh* M, int16_t* band, const double* VF)
+{
+    compute_band_k(M, band, VF, 1, M->Nz, true);
+    return 0;
+}
+
+/* computeBand!'s per-cell passes on the cells k in [klo, khi] only (CPU baseline sample). */
+int orc_compute_band_slab(const orc_mesh* M, int16_t* band, const double* VF, int klo, int khi)
+{
+    compute_band_k(M, band, VF, klo, khi, false);
     return 0;
 }
 
@@ -1681,6 +1723,76 @@ int orc_project(const orc_mesh* M, double pt[3], int i, int j, int k, const doub
     Grid G(M);
     Vel V{uf, vf, wf};
     project(G, V, pt, i, j, k, dt);
+    return 0;
+}
+
+/* VFsphere's rule (src/Tools.jl:907-922) for a union of spheres (dims 3) or circles in x-y
+ * (dims 2), over every cell of the cell-array extent (ghosts included): nF points per direction
+ * at xmin + i/(nF+1)*(xmax-xmin); a point is liquid when rad^2 - ((xh-xo)^2 + (yh-yo)^2 +
+ * (zh-zo)^2) > 0 for some sphere; VF is the sequential sum of count copies of 1/nF^dims.  Cells
+ * whose box is entirely inside a sphere take the full sum without sampling.  The workload
+ * generator of the CPU baseline (the GPU library generates the same field on the device); the
+ * caller fills the VF ghost layers afterwards.  VF must be zeroed by the caller. */
+int orc_vf_spheres(const orc_mesh* M, const double* cen, const double* rad, int ns, int nF, int dims, double* VF)
+{
+    Grid G(M);
+    const int npts = dims == 3 ? nF * nF * nF : nF * nF;
+    std::vector<double> table(npts + 1);
+    const double sub = 1.0 / (double)npts;
+    double acc = 0.0;
+    table[0] = 0.0;
+    for (int q = 1; q <= npts; ++q) { acc = acc + sub; table[q] = acc; }
+#pragma omp parallel for collapse(2) schedule(dynamic, 4)
+    for (int k = G.lo[2]; k <= G.hi[2]; ++k)
+        for (int j = G.lo[1]; j <= G.hi[1]; ++j) {
+            std::vector<int> cand;
+            for (int i = G.lo[0]; i <= G.hi[0]; ++i) {
+                const double x0 = G.x(i), x1 = G.x(i + 1), y0 = G.y(j), y1 = G.y(j + 1), z0 = G.z(k), z1 = G.z(k + 1);
+                cand.clear();
+                bool full = false;
+                for (int s = 0; s < ns; ++s) {
+                    const double cx = cen[3 * s], cy = cen[3 * s + 1], cz = cen[3 * s + 2], r = rad[s];
+                    if (x1 < cx - r || x0 > cx + r || y1 < cy - r || y0 > cy + r) continue;
+                    if (dims == 3 && (z1 < cz - r || z0 > cz + r)) continue;
+                    const double fx = std::fmax(std::fabs(x0 - cx), std::fabs(x1 - cx));
+                    const double fy = std::fmax(std::fabs(y0 - cy), std::fabs(y1 - cy));
+                    const double fz = dims == 3 ? std::fmax(std::fabs(z0 - cz), std::fabs(z1 - cz)) : 0.0;
+                    if (fx * fx + fy * fy + fz * fz < r * r * (1.0 - 1e-12)) { full = true; break; }
+                    cand.push_back(s);
+                }
+                int cnt = 0;
+                if (full) {
+                    cnt = npts;
+                } else if (!cand.empty()) {
+                    const int nzp = dims == 3 ? nF : 1;
+                    for (int c = 1; c <= nzp; ++c) {
+                        const double zh = z0 + (double)c / (double)(nF + 1) * (z1 - z0);
+                        for (int b = 1; b <= nF; ++b) {
+                            const double yh = y0 + (double)b / (double)(nF + 1) * (y1 - y0);
+                            for (int a = 1; a <= nF; ++a) {
+                                const double xh = x0 + (double)a / (double)(nF + 1) * (x1 - x0);
+                                bool hit = false;
+                                for (size_t q = 0; q < cand.size() && !hit; ++q) {
+                                    const int s = cand[q];
+                                    const double r = rad[s];
+                                    const double ex = xh - cen[3 * s], ey = yh - cen[3 * s + 1];
+                                    double Gv;
+                                    if (dims == 3) {
+                                        const double ez = zh - cen[3 * s + 2];
+                                        Gv = r * r - ((ex * ex + ey * ey) + ez * ez);
+                                    } else {
+                                        Gv = r * r - (ex * ex + ey * ey);
+                                    }
+                                    hit = Gv > 0.0;
+                                }
+                                cnt += hit;
+                            }
+                        }
+                    }
+                }
+                VF[G.v(i, j, k)] = table[cnt];
+            }
+        }
     return 0;
 }
 

@@ -3,7 +3,8 @@ restatement, with the reference's shape-error measure.
 
     python tests/config_runs.py 2d [--steps 1024]   # 64^2 single vortex to t = T
     python tests/config_runs.py 3d [--steps 8]      # 128^3 sphere deformation
-    python tests/config_runs.py drift [--steps 64]  # 256^3 mass: FP64, FP64 on FP32 velocities, mixed
+    python tests/config_runs.py drift [--steps 64] [--n 256] [--frozen]
+        # benchmark workload's mass: FP64, FP64 on FP32 velocities, mixed
 
 2d: [0,1]^2, 64x64x1 (z periodic), circle r = 0.15 at (0.5, 0.75) by 10x10 sub-sampling,
     single-vortex face velocities sampled at the faces (period T = 8) at t_n + dt/2,
@@ -88,32 +89,63 @@ def run(which: str, steps: int | None = None, precision: str = "fp64", cpu: bool
     return out
 
 
-def drift(steps: int = 64):
-    """Mass after `steps` steps of the 256^3 benchmark workload (200 spheres, seed 20261203,
-    Deformation3D at t = dt/2, frozen, CFL 0.5) in three runs: the FP64 path, the FP64 path fed
-    the face velocities rounded to FP32 (the mixed path's input precision), and the mixed path.
-    Separates the effect of the FP32 velocity input from that of the FP32 geometry."""
+def drift(steps: int = 64, n: int = 256, frozen: bool = False, marks=(8, 64, 256, 1024, 3072)):
+    """Mixed-vs-FP64 mass difference over `steps` steps of the benchmark workload at n^3 (200
+    spheres, seed 20261203, Deformation3D with T = 3, CFL 0.5, dt = 0.25 dx), in three runs: the
+    FP64 path, the FP64 path fed the face velocities rounded to FP32 (the mixed path's input
+    precision), and the mixed path.  The face velocities follow the field in time, evaluated at
+    t_n + dt/2 for step n (frozen=True keeps the field of step 0).  Reports, at each step in
+    `marks` (and the last), each run's mass, the relative mass difference against the FP64 run,
+    and for the mixed run the largest and the 99th-percentile per-cell |dVF| over interface
+    cells."""
     from ns_multiphase_gb300.slvof import SLVOF
-    m = Mesh(Nx=256, Ny=256, Nz=256, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    m = Mesh(Nx=n, Ny=n, Nz=n, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
     centres, radii = cases.config_spheres(200, 20261203)
     dt = 0.5 * m.dx / 2.0
-    vel = cases.deformation3d_faces(m, 0.5 * dt, 3.0)
-    vel32 = tuple(a.astype(np.float32).astype(np.float64) for a in vel)
-    out = {"workload": "256^3, 200 spheres seed 20261203, Deformation3D T=3 at t=dt/2, CFL 0.5", "steps": steps}
-    for name, precision, v in (("fp64", "fp64", vel), ("fp64_on_fp32_velocities", "fp64", vel32),
-                               ("mixed", "mixed", vel)):
+    marks = sorted({s for s in marks if s <= steps} | {steps})
+    out = {"workload": f"{n}^3, 200 spheres seed 20261203, Deformation3D T=3 "
+                       f"({'frozen at t=dt/2' if frozen else 'at t_n + dt/2'}), CFL 0.5", "steps": steps,
+           "marks": marks}
+    runs = (("fp64", "fp64", False), ("fp64_on_fp32_velocities", "fp64", True), ("mixed", "mixed", False))
+    ctx = {}
+    for name, precision, round32 in runs:
         g = SLVOF(m, precision)
         g.case_vf_spheres(centres, radii, nF=20, dims=3)
         g.init_state()
-        g.upload_velocity(*v)
-        M0 = g.mass()
-        for _ in range(steps):
+        ctx[name] = (g, round32)
+        out[name] = {"mass0": g.mass(), "mass": {}}
+    vel_cache = None
+    t0 = time.perf_counter()
+    for s in range(steps):
+        t = 0.5 * dt if frozen else (s + 0.5) * dt
+        for name, (g, round32) in ctx.items():
+            if round32:
+                if vel_cache is None or not frozen:
+                    vel_cache = tuple(a.astype(np.float32).astype(np.float64)
+                                      for a in cases.deformation3d_faces(m, t, 3.0))
+                if s == 0 or not frozen:
+                    g.upload_velocity(*vel_cache)
+            elif s == 0 or not frozen:
+                g.case_deformation3d(t, 3.0)
             M = g.step(dt)
+            if s + 1 in marks:
+                out[name]["mass"][s + 1] = M
+        if s + 1 in marks:
+            V64 = m.interior(ctx["fp64"][0].download_vf())
+            V32 = m.interior(ctx["mixed"][0].download_vf())
+            iface = (V64 >= m.VFlo) & (V64 <= m.VFhi)
+            d = np.abs(V32 - V64)
+            out["mixed"].setdefault("max_abs_dVF", {})[s + 1] = float(d.max())
+            out["mixed"].setdefault("p99_abs_dVF_interface", {})[s + 1] = float(np.percentile(d[iface], 99))
+            print(json.dumps({"step": s + 1, "seconds": round(time.perf_counter() - t0, 1),
+                              "mixed_rel_diff": abs(out["mixed"]["mass"][s + 1] - out["fp64"]["mass"][s + 1])
+                              / abs(out["fp64"]["mass"][s + 1])}), file=sys.stderr, flush=True)
+    for g, _ in ctx.values():
         g.close()
-        out[name] = {"mass0": M0, "mass": M, "rel_change": abs(M - M0) / M0}
     ref = out["fp64"]["mass"]
     for name in ("fp64_on_fp32_velocities", "mixed"):
-        out[name]["rel_diff_vs_fp64"] = abs(out[name]["mass"] - ref) / abs(ref)
+        out[name]["rel_diff_vs_fp64"] = {s: abs(out[name]["mass"][s] - ref[s]) / abs(ref[s]) for s in marks}
+    out["fp64"]["rel_change"] = {s: abs(ref[s] - out["fp64"]["mass0"]) / out["fp64"]["mass0"] for s in marks}
     return out
 
 
@@ -123,9 +155,11 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=256, help="drift: grid size")
+    ap.add_argument("--frozen", action="store_true", help="drift: keep the field of step 0")
     a = ap.parse_args()
     if a.config == "drift":
-        print(json.dumps(drift(a.steps or 64)))
+        print(json.dumps(drift(a.steps or 64, a.n, a.frozen)))
         return
     print(json.dumps(run(a.config, a.steps, a.precision, not a.no_cpu)))
 
