@@ -113,3 +113,64 @@ double fluxh_sl_cell(const slvof_mesh* M, double dt, int i, int j, int k, const 
 }
 
 } // extern "C"
+
+extern "C" {
+/* VFnew in flux form for a list of cells (i, j, k triples) of one state. */
+int fluxh_sl_cells(const slvof_mesh* M, double dt, int n, const int* cells, const double* VF, const double* uf,
+                   const double* vf, const double* wf, const double* nx, const double* ny, const double* nz,
+                   const double* D, double* out)
+{
+    HostMesh H(M);
+    const DevMesh& m = H.m;
+    adj::Vel V{uf, vf, wf};
+    const long nc = m.cs2 * (m.N[2] + 2 * m.g);
+    std::vector<signed char> phase(nc);
+    for (long t = 0; t < nc; ++t) {
+        const double l1 = std::fabs(nx[t]) + std::fabs(ny[t]) + std::fabs(nz[t]);
+        phase[t] = (l1 <= 1.0 && D[t] == m.Lsum) ? 1 : ((l1 <= 1.0 && D[t] == -m.Lsum) ? -1 : 0);
+    }
+    adj::Plic P{nx, ny, nz, D, nullptr, nullptr, nullptr, nullptr, phase.data()};
+    int e = 0;
+    for (int q = 0; q < n; ++q) {
+        const int c0[3] = {cells[3 * q], cells[3 * q + 1], cells[3 * q + 2]};
+        const double vfc = VF[adj::vi(m, c0[0], c0[1], c0[2])];
+        double vol = 1.0 * m.cellvol, liq = (vfc < m.VFlo ? 0.0 : (vfc > m.VFhi ? 1.0 : vfc)) * m.cellvol;
+        for (int dir = 0; dir < 3; ++dir)
+            for (int side = 0; side < 2; ++side) {
+                int h[3] = {c0[0], c0[1], c0[2]};
+                if (side == 1) h[dir] += 1;
+                double fv, fl;
+                face_flux(m, V, P, dt, dir, h[0], h[1], h[2], fv, fl, e);
+                const double s = side == 1 ? 1.0 : -1.0;
+                vol += s * fv;
+                liq += s * fl;
+            }
+        out[q] = liq / vol;
+    }
+    return e;
+}
+}
+
+extern "C" {
+/* Swept volume and liquid (for the low cell) of face (dir, h) in FP64, in cell units. */
+int fluxh_face(const slvof_mesh* M, double dt, int dir, int hi, int hj, int hk, const double* uf, const double* vf,
+               const double* wf, const double* nx, const double* ny, const double* nz, const double* D, double* out)
+{
+    HostMesh H(M);
+    const DevMesh& m = H.m;
+    adj::Vel V{uf, vf, wf};
+    const long nc = m.cs2 * (m.N[2] + 2 * m.g);
+    std::vector<signed char> phase(nc);
+    for (long t = 0; t < nc; ++t) {
+        const double l1 = std::fabs(nx[t]) + std::fabs(ny[t]) + std::fabs(nz[t]);
+        phase[t] = (l1 <= 1.0 && D[t] == m.Lsum) ? 1 : ((l1 <= 1.0 && D[t] == -m.Lsum) ? -1 : 0);
+    }
+    adj::Plic P{nx, ny, nz, D, nullptr, nullptr, nullptr, nullptr, phase.data()};
+    int e = 0;
+    double fv, fl;
+    face_flux(m, V, P, dt, dir, hi, hj, hk, fv, fl, e);
+    out[0] = fv / m.cellvol;
+    out[1] = fl / m.cellvol;
+    return e;
+}
+}

@@ -27,3 +27,20 @@ def test_configuration_bit_identical(built, which, steps):
         # the vortex returns the circle at t = T; the reference's measure of how well it does
         # (8.1e-3 with these face samples) stays that of a converged interface, not a smeared one
         assert out["shape_error"] < 2e-2, out
+
+
+def test_benchmark_state_generated_alike_on_gpu_and_cpu(built):
+    """The benchmark's initial VF (union of spheres by VFsphere's rule) generated by the GPU
+    library and by the restatement (the reference arm's state) is the same to the bit."""
+    import numpy as np
+    from ns_multiphase_gb300 import cases
+    from ns_multiphase_gb300.mesh import Mesh
+    from ns_multiphase_gb300.slvof import SLVOF
+    from oracle.oracle import Oracle
+    m = Mesh(Nx=48, Ny=40, Nz=44, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
+    c, r = cases.config_spheres(200, 20261203)
+    with SLVOF(m, "fp64") as g:
+        g.case_vf_spheres(c, 2.0 * r, nF=20, dims=3)
+        Vg = g.download_vf()
+    Vo = Oracle(m).vf_spheres(c, 2.0 * r, nF=20, dims=3)
+    assert np.array_equal(Vg, Vo), float(np.max(np.abs(Vg - Vo)))
