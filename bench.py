@@ -55,7 +55,12 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=256)
     p.add_argument("--fp64-steps", type=int, default=3)
-    p.add_argument("--drift-steps", type=int, default=8)
+    p.add_argument("--drift-steps", type=int, default=256,
+                   help="steps of the mixed-vs-FP64 mass comparison (time-varying field); the FP64 masses come "
+                        "from tests/golden/drift_fp64_<n>.json when it covers them (checked live over the first "
+                        "8 steps), else from a live FP64 run")
+    p.add_argument("--drift-record", action="store_true",
+                   help="run the FP64 path for --drift-steps steps and write tests/golden/drift_fp64_<n>.json")
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--adj-steps", type=int, default=2)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -99,6 +104,87 @@ def workload(n):
     centres, radii = cases.config_spheres(200, SEED)
     dt = 0.5 * m.dx / 2.0
     return m, centres, radii, dt
+
+
+DRIFT_MARKS = (8, 16, 32, 64, 128, 256, 512, 1024, 2048, 3072)
+
+
+def drift_record_path(n):
+    return os.path.join(ROOT, "tests", "golden", f"drift_fp64_{n}.json")
+
+
+def drift_run(m, centres, radii, dt, steps, precision, VF0, marks):
+    """The workload advanced `steps` steps with the face velocities of Deformation3D at
+    t_n + dt/2 for step n (the field follows time, as the 3D deformation run does); returns the
+    context and the masses at the marks."""
+    g = make_ctx(m, centres, radii, precision, 0.5 * dt, VF0)
+    masses = {}
+    for s in range(steps):
+        g.case_deformation3d((s + 0.5) * dt, 3.0)
+        M = g.step(dt)
+        if s + 1 in marks:
+            masses[s + 1] = M
+    return g, masses
+
+
+def drift_record(args):
+    """--drift-record: the FP64 path's masses over the drift run, as a fixture for the bench."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    torch.cuda.set_device(0)
+    m, centres, radii, dt = workload(args.n)
+    marks = [k for k in DRIFT_MARKS if k <= args.drift_steps]
+    t0 = time.time()
+    g, masses = drift_run(m, centres, radii, dt, args.drift_steps, "fp64", None, set(marks))
+    g.close()
+    rec = {"workload": workload_config(args.n)["workload"], "field": "Deformation3D T=3 at t_n + dt/2",
+           "dt": dt, "made_by": f"python bench.py --drift-record --n {args.n} --drift-steps {args.drift_steps} "
+                                f"(the FP64 path, deterministic: bit-identical to the CPU restatement)",
+           "mass": {str(k): v for k, v in masses.items()}}
+    with open(drift_record_path(args.n), "w") as fh:
+        json.dump(rec, fh, indent=1)
+        fh.write("\n")
+    print(json.dumps({"recorded": drift_record_path(args.n), "seconds": time.time() - t0}), flush=True)
+
+
+def drift_leg(m, centres, radii, dt, steps, VF0):
+    """Mixed-vs-FP64 mass difference over `steps` steps at the marks, the FP64 masses from the
+    recorded run when it covers them (its first mark is reproduced live: the FP64 path is
+    deterministic), and the per-cell |dVF| of the two paths after the first mark."""
+    marks = sorted(k for k in DRIFT_MARKS if k <= steps)
+    rec = None
+    try:
+        rec = json.load(open(drift_record_path(m.Nx)))
+        if not all(str(k) in rec["mass"] for k in marks) or rec["dt"] != dt:
+            rec = None
+    except (OSError, ValueError, KeyError):
+        rec = None
+    first = marks[0]
+    g64, m64 = drift_run(m, centres, radii, dt, first if rec else steps, "fp64", VF0, set(marks))
+    g32, m32 = drift_run(m, centres, radii, dt, first, "mixed", VF0, set(marks))
+    V64, V32 = m.interior(g64.download_vf()), m.interior(g32.download_vf())
+    iface = (V64 >= m.VFlo) & (V64 <= m.VFhi)
+    d = np.abs(V64 - V32)
+    cell = {"step": first, "max_abs_dVF": float(d.max()), "p99_abs_dVF_interface": float(np.percentile(d[iface], 99))}
+    g64.close()
+    for s in range(first, steps):
+        g32.case_deformation3d((s + 0.5) * dt, 3.0)
+        M = g32.step(dt)
+        if s + 1 in marks:
+            m32[s + 1] = M
+    g32.close()
+    source = "live FP64 run"
+    if rec:
+        ref = {k: rec["mass"][str(k)] for k in marks}
+        source = ("tests/golden/drift_fp64_%d.json (made by %s); its step-%d mass reproduced live: %s"
+                  % (m.Nx, rec["made_by"], first, "bit-identical" if ref[first] == m64[first] else
+                     "DIFFERENT (%r live)" % m64[first]))
+    else:
+        ref = m64
+    curve = {str(k): abs(m32[k] - ref[k]) / abs(ref[k]) for k in marks}
+    return {"steps": steps, "field": "Deformation3D T=3 at t_n + dt/2 (time-varying)",
+            "mass_rel_diff_mixed_vs_fp64": curve, "fp64_masses": source, "per_cell": cell}
 
 
 def make_ctx(m, centres, radii, precision, t, VF0=None):
@@ -413,6 +499,9 @@ def main():
     if args.stage_run:
         stage_run(args)
         return
+    if args.drift_record:
+        drift_record(args)
+        return
     ws, rank, local = dist_env()
     if args.impl == "reference":
         # the CPU restatement on the host cores: rank 0 alone, no GPU and no process group
@@ -448,22 +537,20 @@ def main():
 
     out = None
     if rank == 0:
-        # ---- FP64 arm and mixed-vs-FP64 accuracy on the same state ------------------------
+        # ---- mixed-vs-FP64 mass over the drift run ------------------------------------------
+        accuracy = drift_leg(m, centres, radii, dt, args.drift_steps, VF0)
+        # ---- FP64 arm on the benchmark state, and the reverse passes ---------------------------
         g64 = make_ctx(m, centres, radii, "fp64", 0.5 * dt, VF0)
         g32 = make_ctx(m, centres, radii, "mixed", 0.5 * dt, VF0)
-        M0 = g64.mass()
-        for s in range(args.drift_steps):
-            m64 = g64.step(dt)
-            m32 = g32.step(dt)
-        V64, V32 = g64.download_vf(), g32.download_vf()
-        dVF = float(np.max(np.abs(m.interior(V64) - m.interior(V32))))
-        drift_vs_fp64 = abs(m32 - m64) / abs(m64)
+        for s in range(3):
+            g64.step(dt)
+            g32.step(dt)
         ms64, stage64 = timed_steps(g64, dt, args.fp64_steps, torch)
         value64 = cells * args.fp64_steps / (ms64 / 1e3)
         adj32, adj32_re = adjoint_mixed(g32, m, dt, args.adj_steps, torch)
         g32.close()
         adj64 = adjoint_timing(g64, m, dt, args.adj_steps, torch)
-        adjoint = {"workload": f"{m.Nx}^3 benchmark state after the accuracy steps, reverse of one step seeded with "
+        adjoint = {"workload": f"{m.Nx}^3 benchmark state after 3 steps, reverse of one step seeded with "
                                "normal weights on every interior cell",
                    "adj_ms_per_step": adj32, "fwd_mixed_ms_per_step": ms_step, "adj_over_fwd_mixed": adj32 / ms_step,
                    "mixed": "boundary-form reverse (FP32 cell-local geometry, FP64 accumulation), the step's "
@@ -584,8 +671,7 @@ def main():
                "parallelism": "replicas" if ws > 1 else "1 GPU",
                "fp64": {"value": value64, "ms_per_step": ms64 / args.fp64_steps, "speedup_mixed": value / ws / value64,
                         "stages_ms": stage64},
-               "accuracy": {"steps": args.drift_steps, "mass_rel_diff_mixed_vs_fp64": drift_vs_fp64,
-                            "max_abs_dVF_mixed_vs_fp64": dVF, "mass_rel_change_fp64": abs(m64 - M0) / M0},
+               "accuracy": accuracy,
                "adjoint": adjoint,
                "stages_ms": stage,
                "stages_note": "CUDA events per stage on the stream each stage runs on; the band runs on a second "

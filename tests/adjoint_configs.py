@@ -4,6 +4,8 @@
     python tests/adjoint_configs.py 3d [--fd 16] [--precision mixed]
     python tests/adjoint_configs.py 2d --save-gradient g.npz   # the reverse pass (GPU)
     python tests/adjoint_configs.py 2d --forward-mode g.npz    # against forward mode (CPU)
+    python tests/adjoint_configs.py 3d --h-sweep --also mixed --out tests/golden/adjoint_3d.json
+        # per-entry deviations at h = 1e-5, 1e-6, 1e-7 (check_sweep)
 
 2d: single-vortex deformation on 256x256 (Nz = 1, z periodic), circle r = 0.15 at
     (0.5, 0.75) by 10x10 sub-sampling, stream-function face velocities (period T = 8) at
@@ -190,6 +192,64 @@ def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=(), sweep
                         for q, (idx, (a, f)) in enumerate(zip(picks, rows))]}
 
 
+H_SWEEP = (1e-5, 1e-6, 1e-7)
+
+
+def check_sweep(cfg, count, fd_backend="gpu", precision="fp64", seed=7, also=()):
+    """Per-entry check with a step sweep: central differences at h = 1e-5, 1e-6 and 1e-7 for
+    every entry, each entry's relative deviation |adj - FD| / |FD| at every h, and its best h.
+    An entry is smooth when the differences at its two largest steps agree to 1e-6 of |FD| (the
+    loss is then differentiable on that scale and the remaining deviation is the reverse pass's
+    or the differences' rounding); otherwise a discrete choice of the step switches within +-h
+    and the entry is listed as not smooth.  `also` lists further forward precisions whose
+    reverse-pass gradients are reported on the same entries."""
+    evaluate = rollout_cpu if fd_backend == "cpu" else rollout_gpu
+    cfg.target = evaluate(cfg, np.zeros_like(cfg.p0))
+    L, G, times = gradient(cfg, precision)
+    others = {pr: gradient(cfg, pr) for pr in also}
+    rng = np.random.default_rng(seed)
+    support = np.argwhere(np.abs(G) > 0)
+    picks = [tuple(support[k]) for k in rng.choice(len(support), size=min(count, len(support)), replace=False)]
+
+    def fd_at(idx, h):
+        vals = []
+        for sgn in (1.0, -1.0):
+            p = cfg.p0.copy()
+            p[idx] += sgn * h
+            vals.append(loss(cfg, evaluate(cfg, p)))
+        return (vals[0] - vals[1]) / (2 * h)
+
+    t0 = time.perf_counter()
+    entries = []
+    for idx in picks:
+        a = float(G[idx])
+        fds = {h: fd_at(idx, h) for h in H_SWEEP}
+        rel = {h: abs(a - f) / abs(f) if f != 0 else None for h, f in fds.items()}
+        best = min((h for h in H_SWEEP if rel[h] is not None), key=lambda h: rel[h])
+        smooth = abs(fds[H_SWEEP[0]] - fds[H_SWEEP[1]]) <= 1e-6 * abs(fds[H_SWEEP[1]])
+        e = {"index": [int(x) for x in idx], "adjoint": a, "fd": {str(h): f for h, f in fds.items()},
+             "rel_err": {str(h): r for h, r in rel.items()}, "best_h": best, "rel_err_best": rel[best],
+             "smooth": bool(smooth)}
+        for pr, (Lp, Gp, tp) in others.items():
+            ap = float(Gp[idx])
+            e["adjoint_" + pr] = ap
+            e["rel_err_best_" + pr] = abs(ap - fds[best]) / abs(fds[best]) if fds[best] != 0 else None
+        entries.append(e)
+    sm = [e for e in entries if e["smooth"]]
+    return {"config": cfg.name, "grid": list(cfg.mesh.cell_shape), "steps": cfg.steps,
+            "checkpoint_every": cfg.every, "precision_forward": precision, "fd_backend": fd_backend,
+            "h_sweep": list(H_SWEEP), "loss": L, "params": int(cfg.p0.size), "support": int(len(support)),
+            "checked": len(entries), "smooth_entries": len(sm),
+            "max_rel_err_best_smooth": max((e["rel_err_best"] for e in sm), default=None),
+            "smooth_entries_within_1e-6": sum(1 for e in sm if e["rel_err_best"] <= 1e-6),
+            "not_smooth": [e["index"] for e in entries if not e["smooth"]],
+            "fd_seconds": time.perf_counter() - t0, "timings": times,
+            "also": {pr: {"loss": Lp, "rel_l2_vs_" + precision: float(np.linalg.norm(Gp - G) / np.linalg.norm(G)),
+                          "max_rel_err_best_smooth": max((e["rel_err_best_" + pr] for e in sm), default=None),
+                          "timings": tp} for pr, (Lp, Gp, tp) in others.items()},
+            "entries": entries}
+
+
 def save_gradient(cfg, path, precision="fp64"):
     """The reverse pass's gradient of the configuration (GPU), with its loss, saved for
     forward_mode_check (which needs no GPU)."""
@@ -251,6 +311,9 @@ def main():
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--also", choices=["fp64", "mixed"], nargs="*", default=[])
     ap.add_argument("--sweep-all", action="store_true", help="central differences with h/8 for every entry")
+    ap.add_argument("--h-sweep", action="store_true",
+                    help="per-entry relative deviations at h = 1e-5, 1e-6, 1e-7 (check_sweep)")
+    ap.add_argument("--out", metavar="FILE", help="also write the JSON result to FILE")
     ap.add_argument("--save-gradient", metavar="FILE", help="save the reverse pass's gradient (GPU) and stop")
     ap.add_argument("--forward-mode", metavar="FILE",
                     help="check a saved gradient against forward-mode derivatives of the restatement (2d, CPU)")
@@ -266,11 +329,19 @@ def main():
         return
     if a.config == "2d":
         cfg = config2d(N=a.n or 256, steps=a.steps or 40, every=a.every)
-        out = check(cfg, a.fd or 64, a.fd_backend or "cpu", a.precision, also=a.also, sweep_all=a.sweep_all)
+        count, backend = a.fd or 64, a.fd_backend or "cpu"
     else:
         cfg = config3d(N=a.n or 128, steps=a.steps or 30, every=a.every)
-        out = check(cfg, a.fd or 16, a.fd_backend or "gpu", a.precision, also=a.also, sweep_all=a.sweep_all)
+        count, backend = a.fd or 16, a.fd_backend or "gpu"
+    if a.h_sweep:
+        out = check_sweep(cfg, count, backend, a.precision, also=a.also)
+    else:
+        out = check(cfg, count, backend, a.precision, also=a.also, sweep_all=a.sweep_all)
     print(json.dumps(out))
+    if a.out:
+        with open(a.out, "w") as fh:
+            json.dump(out, fh, indent=1)
+            fh.write("\n")
 
 
 if __name__ == "__main__":
