@@ -235,9 +235,12 @@ void launch_plic_iface_newton(const DevMesh& m, const double* VF, const double* 
 
 /* Candidate normal of lane (family f, outer a, inner b) from a 3x3x3 VF block; R = float
  * for the error pass, double to form candidates exactly as the FP64 path does. */
+/* sg[0..2]: the family's third component, -1 where the +1 neighbour along that axis holds
+ * more liquid than the -1 neighbour, else +1 (VF[+1] > VF[-1] ? -1 : 1), decided on the FP64
+ * VF in both precisions: two values that differ in FP64 can round to the same float. */
 template <class R>
 __device__ __forceinline__ void candidate(const R* sv, int f, int a, int b, R dx, R dy, R dz, const R* hx, const R* hy,
-                                          const R* hz, R& cx, R& cy, R& cz)
+                                          const R* hz, const R* sg, R& cx, R& cy, R& cz)
 {
     /* h[0] = xm[i]-xm[i-1], h[1] = xm[i+1]-xm[i-1], h[2] = xm[i+1]-xm[i]: the reference's
      * pairs {i-1,i}, {i-1,i+1}, {i,i+1} (src/ELVIRA.jl:72,82,92) */
@@ -251,17 +254,17 @@ __device__ __forceinline__ void candidate(const R* sv, int f, int a, int b, R dx
         const R s2y = (V3(0, o2, -1) * dz + V3(0, o2, 0) * dz) + V3(0, o2, 1) * dz;
         const R s1y = (V3(0, o1, -1) * dz + V3(0, o1, 0) * dz) + V3(0, o1, 1) * dz;
         cy = -(s2y - s1y) / hy[a];
-        cz = V3(0, 0, 1) > V3(0, 0, -1) ? R(-1) : R(1);
+        cz = sg[2];
     } else if (f == 1) {
         const R s2x = (V3(i2, -1, 0) * dy + V3(i2, 0, 0) * dy) + V3(i2, 1, 0) * dy;
         const R s1x = (V3(i1, -1, 0) * dy + V3(i1, 0, 0) * dy) + V3(i1, 1, 0) * dy;
         cx = -(s2x - s1x) / hx[b];
-        cy = V3(0, 1, 0) > V3(0, -1, 0) ? R(-1) : R(1);
+        cy = sg[1];
         const R s2z = (V3(0, -1, o2) * dy + V3(0, 0, o2) * dy) + V3(0, 1, o2) * dy;
         const R s1z = (V3(0, -1, o1) * dy + V3(0, 0, o1) * dy) + V3(0, 1, o1) * dy;
         cz = -(s2z - s1z) / hz[a];
     } else {
-        cx = V3(1, 0, 0) > V3(-1, 0, 0) ? R(-1) : R(1);
+        cx = sg[0];
         const R s2y = (V3(-1, i2, 0) * dx + V3(0, i2, 0) * dx) + V3(1, i2, 0) * dx;
         const R s1y = (V3(-1, i1, 0) * dx + V3(0, i1, 0) * dx) + V3(1, i1, 0) * dx;
         cy = -(s2y - s1y) / hy[b];
@@ -293,7 +296,10 @@ __device__ __forceinline__ void candidate64(const DevMesh& m, const double* sv, 
                           cco(m, 1, j + 1) - cco(m, 1, j)};
     const double hz[3] = {cco(m, 2, k) - cco(m, 2, k - 1), cco(m, 2, k + 1) - cco(m, 2, k - 1),
                           cco(m, 2, k + 1) - cco(m, 2, k)};
-    candidate<double>(sv, lane_family(fam_on, c), (c % 9) / 3, c % 3, m.d[0], m.d[1], m.d[2], hx, hy, hz, cx, cy, cz);
+    /* VF[+1] > VF[-1] ? -1 : 1 along x, y, z (src/ELVIRA.jl:72-98) */
+    const double sg[3] = {sv[14] > sv[12] ? -1.0 : 1.0, sv[16] > sv[10] ? -1.0 : 1.0, sv[22] > sv[4] ? -1.0 : 1.0};
+    candidate<double>(sv, lane_family(fam_on, c), (c % 9) / 3, c % 3, m.d[0], m.d[1], m.d[2], hx, hy, hz, sg, cx, cy,
+                      cz);
     const double norm = sqrt((cx * cx + cy * cy) + cz * cz);
     cx = cx / norm; cy = cy / norm; cz = cz / norm;
 }
@@ -319,7 +325,16 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
         const int i = 1 + L % m.N[0];
         const int j = 1 + (L / m.N[0]) % m.N[1];
         const int k = 1 + L / (m.N[0] * m.N[1]);
-        if (lane < 27) s_vf[w][lane] = (float)VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
+        double v64 = 0.0;
+        if (lane < 27) {
+            v64 = VF[vidx(m, i - 1 + lane % 3, j - 1 + (lane / 3) % 3, k - 1 + lane / 9)];
+            s_vf[w][lane] = (float)v64;
+        }
+        /* the candidates' third components from the FP64 VF of the face neighbours */
+        const double vxp = __shfl_sync(0xffffffffu, v64, 14), vxm = __shfl_sync(0xffffffffu, v64, 12);
+        const double vyp = __shfl_sync(0xffffffffu, v64, 16), vym = __shfl_sync(0xffffffffu, v64, 10);
+        const double vzp = __shfl_sync(0xffffffffu, v64, 22), vzm = __shfl_sync(0xffffffffu, v64, 4);
+        const float sg[3] = {vxp > vxm ? -1.f : 1.f, vyp > vym ? -1.f : 1.f, vzp > vzm ? -1.f : 1.f};
         __syncwarp();
         const float* sv = s_vf[w];
         float err_ = INFINITY, tol = 0.f;
@@ -328,7 +343,7 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
             const int a = (lane % 9) / 3, b = lane % 3;
             float cx, cy, cz;
             const float hx[3] = {dx, 2.f * dx, dx}, hy[3] = {dy, 2.f * dy, dy}, hz[3] = {dz, 2.f * dz, dz};
-            candidate<float>(sv, f, a, b, dx, dy, dz, hx, hy, hz, cx, cy, cz);
+            candidate<float>(sv, f, a, b, dx, dy, dz, hx, hy, hz, sg, cx, cy, cz);
             const float nrm = sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
             cx /= nrm; cy /= nrm; cz /= nrm;
             /* computeDist in cell units: mm = n*d/|n*d|_1; neighbour (p,r,s) holds the cube
@@ -352,7 +367,10 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
             }
             err_ = e2;
             /* bound on the FP32 error of e2: each fraction is good to a few 1e-7 */
-            tol = 4e-6f * sa + 1e-5f * e2 + 1e-12f;
+#ifndef SLVOF_ELVIRA_TOL_SCALE
+#define SLVOF_ELVIRA_TOL_SCALE 1.0f
+#endif
+            tol = SLVOF_ELVIRA_TOL_SCALE * (4e-6f * sa + 1e-5f * e2 + 1e-12f);
         }
         /* FP32 winner and the set of candidates that could beat it in exact arithmetic */
         const bool fin = err_ < INFINITY;

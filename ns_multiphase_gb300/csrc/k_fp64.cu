@@ -394,13 +394,18 @@ __device__ __forceinline__ void form_child64(const Frame64<MOM>& F, const CutCas
 }
 
 /* cutTet (src/VFgeom.jl:713-900) with an explicit stack; the children's sums are added in the
- * reference's order.  out = (vol, vLiq[, vrhoU, vrhoV, vrhoW, vrho]). */
+ * reference's order.  out = (vol, vLiq[, vrhoU, vrhoV, vrhoW, vrho]).  The first SL64_SMEM_FRAMES
+ * levels live in the calling thread's slot of shared memory (sm), which holds every tree at
+ * CFL <= 1 (one cut per direction); deeper levels of larger CFL numbers use a local array. */
+constexpr int SL64_SMEM_FRAMES = 3;
+
 template <bool MOM>
 __device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P, double* cx, double* cy, double* cz,
-                           int (*ci)[3], double* out, int& err)
+                           int (*ci)[3], double* out, int& err, Frame64<MOM>* sm)
 {
     constexpr int NA = MOM ? 6 : 2;
-    Frame64<MOM> st[CLIP_STACK];
+    Frame64<MOM> st_deep[CLIP_STACK - SL64_SMEM_FRAMES];
+    auto frame = [&](int d) -> Frame64<MOM>& { return d < SL64_SMEM_FRAMES ? sm[d] : st_deep[d - SL64_SMEM_FRAMES]; };
     int depth = 0, flags = 0, leaves = 0;
     for (;;) {
         int dir = -1, cut = 0;
@@ -421,7 +426,7 @@ __device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P
             }
             leaf64<MOM>(m, tab, P, cx, cy, cz, ci[0][0], ci[0][1], ci[0][2], r, err);
         } else {
-            Frame64<MOM>& F = st[depth];
+            Frame64<MOM>& F = frame(depth);
             const double pl = fco(m, dir, cut);
             const double* cd = dir == 0 ? cx : (dir == 1 ? cy : cz);
             double d[4];
@@ -466,7 +471,7 @@ __device__ void clip_tet64(const DevMesh& m, const CutCase* tab, const Plic64& P
                 for (int q = 0; q < NA; ++q) out[q] = r[q];
                 return;
             }
-            Frame64<MOM>& F = st[depth - 1];
+            Frame64<MOM>& F = frame(depth - 1);
             for (int q = 0; q < NA; ++q) F.acc[q] += r[q];
             if (F.next < tab[F.cs].ntets) {
                 form_child64<MOM>(F, tab, F.next, cx, cy, cz, ci);
@@ -587,7 +592,7 @@ template <bool MOM>
 __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, double dt,
                                           const signed char* __restrict__ phase, double* __restrict__ VFout,
                                           const Vel64& V, const Plic64& P, int L, double* us, double* vs, double* ws,
-                                          int& err)
+                                          int& err, Frame64<MOM>* sm)
 {
     const int i = 1 + L % m.N[0];
     const int j = 1 + (L / m.N[0]) % m.N[1];
@@ -651,7 +656,7 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
             ci[n][0] = vi[v][0]; ci[n][1] = vi[v][1]; ci[n][2] = vi[v][2];
         }
         double r[NA];
-        clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err);
+        clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err, sm);
         for (int q = 0; q < NA; ++q) sum[q] += tetsign * r[q];
     }
     if (m.fd) {
@@ -669,7 +674,7 @@ __device__ __forceinline__ void sl_cell64(const DevMesh& m, const CutCase* tab, 
                 ci[n][2] = pt2index1(m, 2, cz[n], k, err);
             }
             double r[NA];
-            clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err);
+            clip_tet64<MOM>(m, tab, P, cx, cy, cz, ci, r, err, sm);
             for (int q = 0; q < NA; ++q) sum[q] += tetsign * r[q];
         }
     }
@@ -690,6 +695,8 @@ __global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const
                                                      int* work, double* us, double* vs, double* ws, int* errw)
 {
     __shared__ CutCase s_tab[16];
+    extern __shared__ __align__(16) unsigned char sl64_smem[];
+    Frame64<MOM>* sm = reinterpret_cast<Frame64<MOM>*>(sl64_smem) + threadIdx.x * SL64_SMEM_FRAMES;
     load_table(s_tab);
     const int lane = threadIdx.x & 31;
     const int n_items = *count;
@@ -700,7 +707,7 @@ __global__ void __launch_bounds__(SL_THREADS) k_sl64(DevMesh m, double dt, const
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_items) break;
         const int item = base + lane;
-        if (item < n_items) sl_cell64<MOM>(m, s_tab, dt, phase, VFout, V, P, list[item], us, vs, ws, err);
+        if (item < n_items) sl_cell64<MOM>(m, s_tab, dt, phase, VFout, V, P, list[item], us, vs, ws, err, sm);
         __syncwarp();
     }
     if (err) atomicOr(errw, err);
@@ -915,8 +922,11 @@ void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout,
     (void)VFin;
     Vel64 V{uf, vf, wf};
     Plic64 P{nx, ny, nz, D, nullptr, nullptr, nullptr, 0.0, 0.0};
-    k_sl64<false><<<nsm * 8, SL_THREADS, 0, s>>>(m, dt, phase, VFout, V, P, list, count, work, nullptr, nullptr,
-                                                 nullptr, errw);
+    /* the clip frames' shared-memory share: 3 frames x 128 threads (101 KB, two blocks per SM) */
+    const int smem = SL_THREADS * SL64_SMEM_FRAMES * (int)sizeof(Frame64<false>);
+    cudaFuncSetAttribute(k_sl64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_sl64<false><<<nsm * 2, SL_THREADS, smem, s>>>(m, dt, phase, VFout, V, P, list, count, work, nullptr, nullptr,
+                                                    nullptr, errw);
 }
 
 void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const double* uf, const double* vf,
@@ -927,7 +937,9 @@ void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const doub
 {
     Vel64 V{uf, vf, wf};
     Plic64 P{nx, ny, nz, D, u, v, w, rho_liq, rho_gas};
-    k_sl64<true><<<nsm * 8, SL_THREADS, 0, s>>>(m, dt, phase, VFout, V, P, list, count, work, us, vs, ws, errw);
+    const int smem = SL_THREADS * SL64_SMEM_FRAMES * (int)sizeof(Frame64<true>);
+    cudaFuncSetAttribute(k_sl64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_sl64<true><<<nsm * 2, SL_THREADS, smem, s>>>(m, dt, phase, VFout, V, P, list, count, work, us, vs, ws, errw);
     k_mom_flux64<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, band, us, vs, ws);
 }
 

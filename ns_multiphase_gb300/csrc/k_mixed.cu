@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(SL32_THREADS) k_sl32_pre(DevMesh m, float dt, 
                         vol += tet_vol32(px, py, pz, tet5(t, 0), tet5(t, 1), tet5(t, 2), tet5(t, 3));
                     vol *= even ? 1.f : -1.f;
                     if (vol > 0.25f && vol < 4.f) {
-                        VFout[vidx(m, i, j, k)] = ph > 0 ? 1.0 : 0.0;
+                        if (VFout) VFout[vidx(m, i, j, k)] = ph > 0 ? 1.0 : 0.0;
                         slow = false;
                     }
                 }
@@ -806,6 +806,105 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32(DevMesh m, float 
     }
 }
 
+/* Staggered trilinear interpolation split as base + correction: the base is the input value
+ * at the cell's low corner (exact), the correction the weighted sum of the other corners'
+ * differences from it, small where the field is smooth, so its FP32 rounding is small too. */
+__device__ __forceinline__ void tri32s(const DevMesh& m, const float* __restrict__ f, int I, int J, int K, float wx,
+                                       float wy, float wz, float& base, float& corr)
+{
+    const long b = cidx(m, I, J, K);
+    const long sj = m.cs1, sk = m.cs2;
+    const float f000 = __ldg(f + b);
+    const float d100 = __ldg(f + b + 1) - f000, d010 = __ldg(f + b + sj) - f000, d110 = __ldg(f + b + 1 + sj) - f000;
+    const float d001 = __ldg(f + b + sk) - f000, d101 = __ldg(f + b + 1 + sk) - f000,
+                d011 = __ldg(f + b + sj + sk) - f000, d111 = __ldg(f + b + 1 + sj + sk) - f000;
+    const float x00 = wx * d100, x10 = d010 + wx * (d110 - d010);
+    const float x01 = d001 + wx * (d101 - d001), x11 = d011 + wx * (d111 - d011);
+    const float y0 = x00 + wy * (x10 - x00), y1 = x01 + wy * (x11 - x01);
+    base = f000;
+    corr = y0 + wz * (y1 - y0);
+}
+
+/* vel32 with each component as base + correction */
+__device__ __forceinline__ void vel32s(const DevMesh& m, const Vel32& V, int i0, int j0, int k0, float x, float y,
+                                       float z, float* b, float* c)
+{
+    const float B = 1.0e6f;
+    const float fx = fminf(fmaxf(floorf(x), -B), B), fy = fminf(fmaxf(floorf(y), -B), B), fz = fminf(fmaxf(floorf(z), -B), B);
+    const float gx = fminf(fmaxf(floorf(x - 0.5f), -B), B), gy = fminf(fmaxf(floorf(y - 0.5f), -B), B),
+                gz = fminf(fmaxf(floorf(z - 0.5f), -B), B);
+    const int Fx = clampi(i0 + (int)fx, m.lo, m.hi[0] - 1), Cx = clampi(i0 + (int)gx, m.lo, m.hi[0] - 1);
+    const int Fy = clampi(j0 + (int)fy, m.lo, m.hi[1] - 1), Cy = clampi(j0 + (int)gy, m.lo, m.hi[1] - 1);
+    const int Fz = clampi(k0 + (int)fz, m.lo, m.hi[2] - 1), Cz = clampi(k0 + (int)gz, m.lo, m.hi[2] - 1);
+    const float wfx = x - (float)(Fx - i0), wcx = x - ((float)(Cx - i0) + 0.5f);
+    const float wfy = y - (float)(Fy - j0), wcy = y - ((float)(Cy - j0) + 0.5f);
+    const float wfz = z - (float)(Fz - k0), wcz = z - ((float)(Cz - k0) + 0.5f);
+    tri32s(m, V.uf, Fx, Cy, Cz, wfx, wcy, wcz, b[0], c[0]);
+    tri32s(m, V.vf, Cx, Fy, Cz, wcx, wfy, wcz, b[1], c[1]);
+    tri32s(m, V.wf, Cx, Cy, Fz, wcx, wcy, wfz, b[2], c[2]);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+/* RK4 displacement of a grid node in FP32 with compensated sums: the stages' base values are
+ * summed exactly in float-float (their weights 1, 2, 2, 1 are exact), the corrections in FP32,
+ * and the product with -dt/6 is formed as a float-float product, so the displacement (cell
+ * units) carries about 1e-9 of a cell of rounding instead of FP32's 6e-8 at coordinates of
+ * order one.  The other projections use project32. */
+__device__ __forceinline__ void node_disp32c(const DevMesh& m, const Vel32& V, int i, int j, int k, double dt,
+                                             double* disp)
+{
+    if (m.projection != 2) {
+        float x = 0.f, y = 0.f, z = 0.f;
+        project32(m, V, i, j, k, (float)dt, x, y, z);
+        disp[0] = x; disp[1] = y; disp[2] = z;
+        return;
+    }
+    const float h = (float)(0.5 * dt), dtf = (float)dt;
+    float b1[3], c1[3], b2[3], c2[3], b3[3], c3[3], b4[3], c4[3];
+    vel32s(m, V, i, j, k, 0.f, 0.f, 0.f, b1, c1);
+    vel32s(m, V, i, j, k, -h * (b1[0] + c1[0]), -h * (b1[1] + c1[1]), -h * (b1[2] + c1[2]), b2, c2);
+    vel32s(m, V, i, j, k, -h * (b2[0] + c2[0]), -h * (b2[1] + c2[1]), -h * (b2[2] + c2[2]), b3, c3);
+    vel32s(m, V, i, j, k, -dtf * (b3[0] + c3[0]), -dtf * (b3[1] + c3[1]), -dtf * (b3[2] + c3[2]), b4, c4);
+    const double kk = -dt / 6.0;
+    const float khi = (float)kk, klo = (float)(kk - (double)khi);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        float s, e, s2, e2;
+        two_sum(b1[q], 2.f * b2[q], s, e);
+        two_sum(s, 2.f * b3[q], s2, e2);
+        e += e2;
+        two_sum(s2, b4[q], s, e2);
+        e += e2;
+        e += ((c1[q] + 2.f * c2[q]) + 2.f * c3[q]) + c4[q];
+        /* (s + e) * (khi + klo) */
+        const float p = khi * s;
+        const float pe = fmaf(khi, s, -p) + (khi * e + klo * s);
+        disp[q] = (double)p + (double)pe;
+    }
+}
+
+/* FP32 trajectories with compensated sums (node_disp32c). */
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32c(DevMesh m, double dt, Vel32 V, FluxBufs F)
+{
+    const int n = *F.n_nodes;
+    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
+        const unsigned c = F.nodes[t];
+        int i, j, k;
+        cell_of_index(m, c, i, j, k);
+        double d[3];
+        node_disp32c(m, V, i, j, k, dt, d);
+        F.nd[0][c] = d[0];
+        F.nd[1][c] = d[1];
+        F.nd[2][c] = d[2];
+    }
+}
+
 /* FP64 trajectories through the FP64 face velocities (project! in the reference's order). */
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes64(DevMesh m, double dt, adj::Vel V, FluxBufs F)
 {
@@ -1269,10 +1368,27 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_flux_clip(DevMesh m, Plane
 }
 
 /* VFnew = (L + sum +-F) / (1 + sum +-V) over the cell's six faces, in cell units; L is the
- * cell's own liquid, VF (0 below VFlo, 1 above VFhi). */
+ * cell's own liquid, VF (0 below VFlo, 1 above VFhi).  A cell whose eight traced corners lie
+ * strictly on one side of every donor plane of their index box has a pre-image entirely in
+ * liquid (or gas): VFnew is 1 (or 0) exactly, as the reference's vLiq/vol of equal sums gives,
+ * instead of the faces' rounded sum.
+ *
+ * The faces' FP32 liquid carries rounding of order 1e-7 of a face's flux, which cancels
+ * between the two cells of a face but not within one cell: a cell whose pre-image holds no
+ * liquid (or only liquid), where the reference gives exactly 0 (or 1), would come out at
+ * +-1e-7 and turn into an interface cell of its own.  Cells whose flux-form value lies within
+ * NEAR_PURE of 0 or 1 are therefore listed, with their pre-image vertices (the same traced
+ * nodes), for the cell-form clip (k_sl32_clipw), whose liquid and volume are sums over the same
+ * pieces: exactly 0 or 1 when every piece is gas or liquid, and otherwise a liquid volume with
+ * rounding proportional to itself. */
+constexpr double NEAR_PURE = 1e-6;
+
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const double* __restrict__ VFin,
-                                                             double* __restrict__ VFout, const int* __restrict__ list,
-                                                             const int* __restrict__ count, FluxBufs F, int* errw)
+                                                             double* __restrict__ VFout, Plane32 PL,
+                                                             const int* __restrict__ list,
+                                                             const int* __restrict__ count, FluxBufs F,
+                                                             int* slow_cells, float4* slow_verts, int* slow_count,
+                                                             int* errw)
 {
     const int n = *count;
     int err = 0;
@@ -1293,7 +1409,63 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const do
             liq += hi.y;
         }
         if (!(vol > 0.0) || !isfinite(vol)) err |= ERR_VOLUME;
-        VFout[v] = liq / vol;
+        double r = liq / vol;
+        int rlo[3], rhi[3];
+        rel_bounds(m, i, j, k, rlo, rhi);
+        if (m.fast_pure && vol > 0.25 && vol < 4.0) {
+            float px[8], py[8], pz[8];
+            int lo[3] = {1 << 20, 1 << 20, 1 << 20}, hi[3] = {-(1 << 20), -(1 << 20), -(1 << 20)};
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int a = q & 1, b = (q >> 1) & 1, e = q >> 2;
+                const long nc = c + a + b * m.cs1 + e * m.cs2;
+                px[q] = (float)((double)a + F.nd[0][nc]);
+                py[q] = (float)((double)b + F.nd[1][nc]);
+                pz[q] = (float)((double)e + F.nd[2][nc]);
+                const int I[3] = {idx32(px[q], 0, rlo[0], rhi[0], err), idx32(py[q], 0, rlo[1], rhi[1], err),
+                                  idx32(pz[q], 0, rlo[2], rhi[2], err)};
+                for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], I[d]); hi[d] = max(hi[d], I[d]); }
+            }
+            const int side = box_plane_side<8>(m, PL, i, j, k, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], px, py, pz);
+            if (side != 0) r = side > 0 ? 1.0 : 0.0;
+        }
+        VFout[v] = r;
+        const bool near = r != 0.0 && r != 1.0 && (fabs(r) < NEAR_PURE || fabs(1.0 - r) < NEAR_PURE);
+        const int slot = warp_slot(near, slow_count);
+        if (slot >= 0) {
+            /* the cell's pre-image vertices in cell2verts! order (x mirrored on odd cells under
+             * 5_tets), as k_sl32_pre stores them, from the traced nodes */
+            const bool even = tess_even(m.tess, i, j, k);
+            const int stride = m.tess == 24 ? 16 : 8;
+            float px[8], py[8], pz[8];
+            for (int q = 0; q < 8; ++q) {
+                const int a = even ? (q & 1) : 1 - (q & 1), b = (q >> 1) & 1, e = q >> 2;
+                const long nc = c + a + b * m.cs1 + e * m.cs2;
+                px[q] = (float)((double)a + F.nd[0][nc]);
+                py[q] = (float)((double)b + F.nd[1][nc]);
+                pz[q] = (float)((double)e + F.nd[2][nc]);
+                const unsigned pk = pack3(idx32(px[q], 0, rlo[0], rhi[0], err), idx32(py[q], 0, rlo[1], rhi[1], err),
+                                          idx32(pz[q], 0, rlo[2], rhi[2], err));
+                slow_verts[(long)slot * stride + q] = make_float4(px[q], py[q], pz[q], __int_as_float((int)pk));
+            }
+            if (m.tess == 24) {
+                for (int f = -1; f < 6; ++f) {
+                    const int nv = f < 0 ? 8 : 4;
+                    float x = 0.f, y = 0.f, z = 0.f;
+                    for (int q = 0; q < nv; ++q) {
+                        const int w = f < 0 ? q : face24(f, q);
+                        x = q == 0 ? px[w] : x + px[w];
+                        y = q == 0 ? py[w] : y + py[w];
+                        z = q == 0 ? pz[w] : z + pz[w];
+                    }
+                    x /= (float)nv; y /= (float)nv; z /= (float)nv;
+                    const unsigned pk = pack3(idx32(x, 0, rlo[0], rhi[0], err), idx32(y, 0, rlo[1], rhi[1], err),
+                                              idx32(z, 0, rlo[2], rhi[2], err));
+                    slow_verts[(long)slot * 16 + 9 + f] = make_float4(x, y, z, __int_as_float((int)pk));
+                }
+            }
+            slow_cells[slot] = list[t];
+        }
     }
     if (err) atomicOr(errw, err);
 }
@@ -1334,7 +1506,8 @@ void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, co
 void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* VFout, const float* uf32,
                       const float* vf32, const float* wf32, const double* uf, const double* vf, const double* wf,
                       const float4* planes, const short* band, const int* list, const int* count,
-                      const FluxLaunch& L, int* errw, int nsm, cudaStream_t s)
+                      const FluxLaunch& L, int* slow_cells, float4* slow_verts, int* slow_count, int* work2,
+                      int* errw, int nsm, cudaStream_t s)
 {
     FluxBufs F{{L.nd[0], L.nd[1], L.nd[2]}, {L.fvf[0], L.fvf[1], L.fvf[2]}, L.nodes, L.faces, L.clip,
                L.ctr, L.ctr + 1, L.ctr + 2, L.ctr + 3};
@@ -1344,6 +1517,9 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
 #if SLVOF_FLUX_TRAJ64
     (void)uf32; (void)vf32; (void)wf32;
     k_flux_nodes64<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, adj::Vel{uf, vf, wf}, F);
+#elif SLVOF_FLUX_TRAJ32C
+    (void)uf; (void)vf; (void)wf;
+    k_flux_nodes32c<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32{uf32, vf32, wf32}, F);
 #else
     (void)uf; (void)vf; (void)wf;
     k_flux_nodes32<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, (float)dt, Vel32{uf32, vf32, wf32}, F);
@@ -1352,7 +1528,9 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
     const int smem = (int)sizeof(FluxShared);
     cudaFuncSetAttribute(k_flux_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_flux_clip<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, PL, F, errw);
-    k_flux_cells<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, VFin, VFout, list, count, F, errw);
+    k_flux_cells<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, VFin, VFout, PL, list, count, F, slow_cells, slow_verts,
+                                                   slow_count, errw);
+    launch_sl32_clip(m, VFout, planes, work2, slow_cells, slow_verts, slow_count, errw, nsm, s);
 }
 
 } // namespace slvof

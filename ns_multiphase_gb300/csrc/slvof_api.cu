@@ -263,8 +263,10 @@ void st_sl32(slvof_ctx* c, double dt, int o)
                 c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR,
                 c->nsm, c->stream);
 #else
+    cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream); /* near-pure cells, their clip work */
     launch_sl32_flux(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf32, c->vf32, c->wf32, c->uf, c->vf, c->wf, c->planes,
-                     c->band[c->bcur], c->list_sl, c->ctr + C_SL, c->flux, c->ctr + C_ERR, c->nsm, c->stream);
+                     c->band[c->bcur], c->list_sl, c->ctr + C_SL, c->flux, c->slow_cells, c->slow_verts,
+                     c->ctr + C_SLOW, c->ctr + C_SLW2, c->ctr + C_ERR, c->nsm, c->stream);
 #endif
 }
 
@@ -1183,15 +1185,17 @@ int adjoint_step32(slvof_ctx* c, double dt, const double* d_next, AdjBuffers& b)
     const int o = 1 - c->vcur;
     CK(cudaMemsetAsync(c->ctr + C_SL, 0, sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->ctr + C_SLW, 0, sizeof(int), c->stream));
-    CK(cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream)); /* clip count, clip work */
     launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
-    launch_sl32_pre(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
-                    c->ctr + C_SLW, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR, c->nsm, c->stream);
     if (!d_next) {
         /* the step's result as the forward computes it */
         st_sl32(c, dt, o);
         d_next = c->VF[o];
     }
+    /* the band cells' FP32 pre-images and the list of those the reverse clips (VF untouched) */
+    CK(cudaMemsetAsync(c->ctr + C_SLW, 0, sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream)); /* clip count, clip work */
+    launch_sl32_pre(c->m, dt, nullptr, c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
+                    c->ctr + C_SLW, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR, c->nsm, c->stream);
     launch_adjoint32_sl(c->m, dt, d_next, c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->slow_cells,
                         c->slow_verts, c->ctr + C_SLOW, c->cinfo, c->gvtx[0], c->gvtx[1], c->gvtx[2], c->gvel32, b,
                         c->ctr + C_ERR, c->nsm, c->stream);

@@ -66,7 +66,8 @@ struct FluxLaunch {
 void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* VFout, const float* uf32,
                       const float* vf32, const float* wf32, const double* uf, const double* vf, const double* wf,
                       const float4* planes, const short* band, const int* list, const int* count,
-                      const FluxLaunch& L, int* errw, int nsm, cudaStream_t s);
+                      const FluxLaunch& L, int* slow_cells, float4* slow_verts, int* slow_count, int* work2,
+                      int* errw, int nsm, cudaStream_t s);
 /* mixed ELVIRA: FP32 scoring (warp per cell), FP64 arbitration of the near-ties listed in arb
  * (n_arb zeroed by the caller; capacity: the interface count), FP64 winner normals */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
