@@ -809,10 +809,12 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32(DevMesh m, float 
 /* Staggered trilinear interpolation split as base + correction: the base is the input value
  * at the cell's low corner (exact), the correction the weighted sum of the other corners'
  * differences from it, small where the field is smooth, so its FP32 rounding is small too. */
-__device__ __forceinline__ void tri32s(const DevMesh& m, const float* __restrict__ f, int I, int J, int K, float wx,
-                                       float wy, float wz, float& base, float& corr)
+__device__ __forceinline__ void tri32s(const DevMesh& m, const float* __restrict__ f, const float* __restrict__ fl,
+                                       int I, int J, int K, float wx, float wy, float wz, float& base, float& corr)
 {
     const long b = cidx(m, I, J, K);
+    /* the residuals (FP64 value - FP32 value) interpolated plainly: they are tiny */
+    const float r = tri32(m, fl, I, J, K, wx, wy, wz);
     const long sj = m.cs1, sk = m.cs2;
     const float f000 = __ldg(f + b);
     const float d100 = __ldg(f + b + 1) - f000, d010 = __ldg(f + b + sj) - f000, d110 = __ldg(f + b + 1 + sj) - f000;
@@ -822,11 +824,16 @@ __device__ __forceinline__ void tri32s(const DevMesh& m, const float* __restrict
     const float x01 = d001 + wx * (d101 - d001), x11 = d011 + wx * (d111 - d011);
     const float y0 = x00 + wy * (x10 - x00), y1 = x01 + wy * (x11 - x01);
     base = f000;
-    corr = y0 + wz * (y1 - y0);
+    corr = (y0 + wz * (y1 - y0)) + r;
 }
 
 /* vel32 with each component as base + correction */
-__device__ __forceinline__ void vel32s(const DevMesh& m, const Vel32& V, int i0, int j0, int k0, float x, float y,
+struct Vel32x {
+    const float *uf, *vf, *wf; /* face velocities in cells per unit time, FP32 */
+    const float *ul, *vl, *wl; /* their FP32 residuals: uf + ul is the FP64 value to ~48 bits */
+};
+
+__device__ __forceinline__ void vel32s(const DevMesh& m, const Vel32x& V, int i0, int j0, int k0, float x, float y,
                                        float z, float* b, float* c)
 {
     const float B = 1.0e6f;
@@ -839,9 +846,9 @@ __device__ __forceinline__ void vel32s(const DevMesh& m, const Vel32& V, int i0,
     const float wfx = x - (float)(Fx - i0), wcx = x - ((float)(Cx - i0) + 0.5f);
     const float wfy = y - (float)(Fy - j0), wcy = y - ((float)(Cy - j0) + 0.5f);
     const float wfz = z - (float)(Fz - k0), wcz = z - ((float)(Cz - k0) + 0.5f);
-    tri32s(m, V.uf, Fx, Cy, Cz, wfx, wcy, wcz, b[0], c[0]);
-    tri32s(m, V.vf, Cx, Fy, Cz, wcx, wfy, wcz, b[1], c[1]);
-    tri32s(m, V.wf, Cx, Cy, Fz, wcx, wcy, wfz, b[2], c[2]);
+    tri32s(m, V.uf, V.ul, Fx, Cy, Cz, wfx, wcy, wcz, b[0], c[0]);
+    tri32s(m, V.vf, V.vl, Cx, Fy, Cz, wcx, wfy, wcz, b[1], c[1]);
+    tri32s(m, V.wf, V.wl, Cx, Cy, Fz, wcx, wcy, wfz, b[2], c[2]);
 }
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
@@ -856,12 +863,12 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
  * and the product with -dt/6 is formed as a float-float product, so the displacement (cell
  * units) carries about 1e-9 of a cell of rounding instead of FP32's 6e-8 at coordinates of
  * order one.  The other projections use project32. */
-__device__ __forceinline__ void node_disp32c(const DevMesh& m, const Vel32& V, int i, int j, int k, double dt,
+__device__ __forceinline__ void node_disp32c(const DevMesh& m, const Vel32x& V, int i, int j, int k, double dt,
                                              double* disp)
 {
     if (m.projection != 2) {
         float x = 0.f, y = 0.f, z = 0.f;
-        project32(m, V, i, j, k, (float)dt, x, y, z);
+        project32(m, Vel32{V.uf, V.vf, V.wf}, i, j, k, (float)dt, x, y, z);
         disp[0] = x; disp[1] = y; disp[2] = z;
         return;
     }
@@ -890,7 +897,7 @@ __device__ __forceinline__ void node_disp32c(const DevMesh& m, const Vel32& V, i
 }
 
 /* FP32 trajectories with compensated sums (node_disp32c). */
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32c(DevMesh m, double dt, Vel32 V, FluxBufs F)
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32c(DevMesh m, double dt, Vel32x V, FluxBufs F)
 {
     const int n = *F.n_nodes;
     for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
@@ -1519,7 +1526,7 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
     k_flux_nodes64<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, adj::Vel{uf, vf, wf}, F);
 #elif SLVOF_FLUX_TRAJ32C
     (void)uf; (void)vf; (void)wf;
-    k_flux_nodes32c<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32{uf32, vf32, wf32}, F);
+    k_flux_nodes32c<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
 #else
     (void)uf; (void)vf; (void)wf;
     k_flux_nodes32<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, (float)dt, Vel32{uf32, vf32, wf32}, F);
