@@ -259,27 +259,36 @@ __global__ void __launch_bounds__(BX * BY) k_band_sweep(DevMesh m, const short* 
 }
 
 /* transport! band gate (src/Transport.jl:111,153): band cells go to the SL list, the rest
- * keep VF.  Thread per interior cell on the pure-cell tiles ((i, j) from the block, k from the
- * grid), so no index divides: a warp reads one row of 32 band entries and copies one row of
- * VF. */
+ * keep VF.  Thread per (i, j) column of CLS_K cells in k on the pure-cell tiles, so no index
+ * divides: a warp reads rows of 32 band entries and copies rows of VF.  Every band entry and
+ * VF value of the column is loaded before any is used (the VF of band cells too, which are
+ * about a tenth), so the loads of a thread overlap instead of waiting on each other. */
+constexpr int CLS_K = 4;
+
 __global__ void __launch_bounds__(PURE_BX * PURE_BY) k_sl_classify(DevMesh m, const short* __restrict__ band,
                                                                    const double* __restrict__ VFin,
                                                                    double* __restrict__ VFout, int* list,
                                                                    int* count)
 {
     const int i = 1 + blockIdx.x * PURE_BX + threadIdx.x, j = 1 + blockIdx.y * PURE_BY + threadIdx.y;
-    const int k = 1 + blockIdx.z;
-    bool sl = false;
-    int L = 0;
-    if (i <= m.N[0] && j <= m.N[1]) {
-        L = (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1];
-        sl = abs((int)band[cidx(m, i, j, k)]) <= m.nband;
-        if (!sl) {
-            const long v = vidx(m, i, j, k);
-            VFout[v] = VFin[v];
-        }
+    const int k0 = 1 + blockIdx.z * CLS_K;
+    const bool col = i <= m.N[0] && j <= m.N[1];
+    short b[CLS_K];
+    double v[CLS_K];
+#pragma unroll
+    for (int q = 0; q < CLS_K; ++q) {
+        const bool in = col && k0 + q <= m.N[2];
+        b[q] = in ? __ldg(band + cidx(m, i, j, k0 + q)) : (short)0;
+        v[q] = in ? __ldg(VFin + vidx(m, i, j, k0 + q)) : 0.0;
     }
-    warp_append(sl, L, list, count);
+#pragma unroll
+    for (int q = 0; q < CLS_K; ++q) {
+        const int k = k0 + q;
+        const bool in = col && k <= m.N[2];
+        const bool sl = in && abs((int)b[q]) <= m.nband;
+        if (in && !sl) VFout[vidx(m, i, j, k)] = v[q];
+        warp_append(sl, (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1], list, count);
+    }
 }
 
 /* FP64 array to FP32 times a scale (face velocities to cells per unit time): the conversion
@@ -497,7 +506,7 @@ void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin,
                         int nsm, cudaStream_t s)
 {
     (void)nsm;
-    const dim3 grid((m.N[0] + PURE_BX - 1) / PURE_BX, (m.N[1] + PURE_BY - 1) / PURE_BY, m.N[2]);
+    const dim3 grid((m.N[0] + PURE_BX - 1) / PURE_BX, (m.N[1] + PURE_BY - 1) / PURE_BY, (m.N[2] + CLS_K - 1) / CLS_K);
     k_sl_classify<<<grid, dim3(PURE_BX, PURE_BY), 0, s>>>(m, band, VFin, VFout, list, count);
 }
 /* The same FP32 value plus its residual: lo = a * scale - hi rounded to FP32, so that hi + lo

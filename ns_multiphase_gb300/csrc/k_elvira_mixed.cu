@@ -335,6 +335,9 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
         const double vyp = __shfl_sync(0xffffffffu, v64, 16), vym = __shfl_sync(0xffffffffu, v64, 10);
         const double vzp = __shfl_sync(0xffffffffu, v64, 22), vzm = __shfl_sync(0xffffffffu, v64, 4);
         const float sg[3] = {vxp > vxm ? -1.f : 1.f, vyp > vym ? -1.f : 1.f, vzp > vzm ? -1.f : 1.f};
+        const double vc64 = __shfl_sync(0xffffffffu, v64, 13);
+        const bool upper_c = vc64 > 0.5;
+        const float vo_c = (float)(upper_c ? 1.0 - vc64 : vc64);
         __syncwarp();
         const float* sv = s_vf[w];
         float err_ = INFINITY, tol = 0.f;
@@ -352,10 +355,11 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
             const float n1 = fabsf(m0) + fabsf(m1) + fabsf(m2);
             m0 /= n1; m1 /= n1; m2 /= n1;
             const Cube q = make_cube(fabsf(m0), fabsf(m1), fabsf(m2));
-            const float vc = sv[13];
-            const float vo = vc > 0.5f ? 1.f - vc : vc;
-            float al = cube_alpha(q, vo);
-            al = vc > 0.5f ? 1.f - al : al;
+            /* min(VF, 1 - VF) of the cell itself from its FP64 value: a VF within 3e-8 of 1
+             * rounds to 1 in FP32, and the plane constant of a nearly full (or empty) cell
+             * goes with the cube root of that small volume */
+            float al = cube_alpha(q, vo_c);
+            al = upper_c ? 1.f - al : al;
             float e2 = 0.f, sa = 0.f;
 #pragma unroll
             for (int c = 0; c < 27; ++c) {

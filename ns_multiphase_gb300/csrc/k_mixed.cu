@@ -896,6 +896,74 @@ __device__ __forceinline__ void node_disp32c(const DevMesh& m, const Vel32x& V, 
     }
 }
 
+/* Staggered trilinear interpolation in FP64 of the cell-unit face velocities held as FP32
+ * value + FP32 residual (hi + lo, the FP64 velocity to ~48 bits). */
+__device__ __forceinline__ double tri64x(const DevMesh& m, const float* __restrict__ f, const float* __restrict__ fl,
+                                        int I, int J, int K, double wx, double wy, double wz)
+{
+    const long b = cidx(m, I, J, K);
+    const long sj = m.cs1, sk = m.cs2;
+    auto v = [&](long o) { return (double)__ldg(f + b + o) + (double)__ldg(fl + b + o); };
+    const double f000 = v(0), f100 = v(1), f010 = v(sj), f110 = v(1 + sj);
+    const double f001 = v(sk), f101 = v(1 + sk), f011 = v(sj + sk), f111 = v(1 + sj + sk);
+    const double x00 = f000 + wx * (f100 - f000), x10 = f010 + wx * (f110 - f010);
+    const double x01 = f001 + wx * (f101 - f001), x11 = f011 + wx * (f111 - f011);
+    const double y0 = x00 + wy * (x10 - x00), y1 = x01 + wy * (x11 - x01);
+    return y0 + wz * (y1 - y0);
+}
+
+__device__ __forceinline__ void vel64x(const DevMesh& m, const Vel32x& V, int i0, int j0, int k0, double x, double y,
+                                       double z, double* u)
+{
+    const double B = 1.0e6;
+    const double fx = fmin(fmax(floor(x), -B), B), fy = fmin(fmax(floor(y), -B), B), fz = fmin(fmax(floor(z), -B), B);
+    const double gx = fmin(fmax(floor(x - 0.5), -B), B), gy = fmin(fmax(floor(y - 0.5), -B), B),
+                 gz = fmin(fmax(floor(z - 0.5), -B), B);
+    const int Fx = clampi(i0 + (int)fx, m.lo, m.hi[0] - 1), Cx = clampi(i0 + (int)gx, m.lo, m.hi[0] - 1);
+    const int Fy = clampi(j0 + (int)fy, m.lo, m.hi[1] - 1), Cy = clampi(j0 + (int)gy, m.lo, m.hi[1] - 1);
+    const int Fz = clampi(k0 + (int)fz, m.lo, m.hi[2] - 1), Cz = clampi(k0 + (int)gz, m.lo, m.hi[2] - 1);
+    const double wfx = x - (double)(Fx - i0), wcx = x - ((double)(Cx - i0) + 0.5);
+    const double wfy = y - (double)(Fy - j0), wcy = y - ((double)(Cy - j0) + 0.5);
+    const double wfz = z - (double)(Fz - k0), wcz = z - ((double)(Cz - k0) + 0.5);
+    u[0] = tri64x(m, V.uf, V.ul, Fx, Cy, Cz, wfx, wcy, wcz);
+    u[1] = tri64x(m, V.vf, V.vl, Cx, Fy, Cz, wcx, wfy, wcz);
+    u[2] = tri64x(m, V.wf, V.wl, Cx, Cy, Fz, wcx, wcy, wfz);
+}
+
+/* RK4 displacement of a grid node in FP64, cell units, through the velocities' hi + lo. */
+__device__ __forceinline__ void node_disp64x(const DevMesh& m, const Vel32x& V, int i, int j, int k, double dt,
+                                             double* disp)
+{
+    if (m.projection != 2) {
+        node_disp32c(m, V, i, j, k, dt, disp);
+        return;
+    }
+    const double h = 0.5 * dt;
+    double u1[3], u2[3], u3[3], u4[3];
+    vel64x(m, V, i, j, k, 0.0, 0.0, 0.0, u1);
+    vel64x(m, V, i, j, k, -h * u1[0], -h * u1[1], -h * u1[2], u2);
+    vel64x(m, V, i, j, k, -h * u2[0], -h * u2[1], -h * u2[2], u3);
+    vel64x(m, V, i, j, k, -dt * u3[0], -dt * u3[1], -dt * u3[2], u4);
+    const double c = -dt / 6.0;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) disp[q] = c * (((u1[q] + 2.0 * u2[q]) + 2.0 * u3[q]) + u4[q]);
+}
+
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes64x(DevMesh m, double dt, Vel32x V, FluxBufs F)
+{
+    const int n = *F.n_nodes;
+    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
+        const unsigned c = F.nodes[t];
+        int i, j, k;
+        cell_of_index(m, c, i, j, k);
+        double d[3];
+        node_disp64x(m, V, i, j, k, dt, d);
+        F.nd[0][c] = d[0];
+        F.nd[1][c] = d[1];
+        F.nd[2][c] = d[2];
+    }
+}
+
 /* FP32 trajectories with compensated sums (node_disp32c). */
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32c(DevMesh m, double dt, Vel32x V, FluxBufs F)
 {
@@ -1524,6 +1592,9 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
 #if SLVOF_FLUX_TRAJ64
     (void)uf32; (void)vf32; (void)wf32;
     k_flux_nodes64<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, adj::Vel{uf, vf, wf}, F);
+#elif SLVOF_FLUX_TRAJ64X
+    (void)uf; (void)vf; (void)wf;
+    k_flux_nodes64x<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
 #elif SLVOF_FLUX_TRAJ32C
     (void)uf; (void)vf; (void)wf;
     k_flux_nodes32c<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
