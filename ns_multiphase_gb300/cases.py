@@ -74,6 +74,25 @@ def deformation3d_faces(mesh: Mesh, t: float, T: float = 3.0):
     return (np.asfortranarray(uf), np.asfortranarray(vf), np.asfortranarray(wf))
 
 
+class Deformation3DFaces:
+    """deformation3d_faces with the time-independent products formed once: faces(t, T) returns
+    the same arrays bit for bit (each component is (space product) * cos(pi t/T), multiplied in
+    the same order), for runs that need the field at many times."""
+
+    def __init__(self, mesh: Mesh):
+        x, y, z = mesh.x[:-1], mesh.y[:-1], mesh.z[:-1]
+        xm, ym, zm = mesh.xm, mesh.ym, mesh.zm
+        s2 = lambda a: np.sin(PI * a) ** 2
+        s2pi = lambda a: np.sin(2 * PI * a)
+        self.p = (np.asfortranarray((2.0 * s2(x)[:, None, None]) * s2pi(ym)[None, :, None] * s2pi(zm)[None, None, :]),
+                  np.asfortranarray((-s2(y)[None, :, None]) * s2pi(xm)[:, None, None] * s2pi(zm)[None, None, :]),
+                  np.asfortranarray((-s2(z)[None, None, :]) * s2pi(xm)[:, None, None] * s2pi(ym)[None, :, None]))
+
+    def faces(self, t: float, T: float = 3.0):
+        ct = math.cos(PI * t / T)
+        return tuple(np.asfortranarray(a * ct) for a in self.p)
+
+
 def uniform_faces(mesh: Mesh, u: float, v: float, w: float):
     uf, vf, wf = mesh.cell_array(), mesh.cell_array(), mesh.cell_array()
     uf[...] = u

@@ -18,7 +18,6 @@
 #include "slvof_kernels.h"
 #include "slvof_dev.cuh"
 #include "mixed32.cuh"
-#include "adj64.cuh"
 #include "flux.cuh"
 
 namespace slvof {
@@ -790,22 +789,6 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_lists(DevMesh m, const sh
     }
 }
 
-/* FP32 trajectories (project32 from the node itself, so the result is the displacement). */
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32(DevMesh m, float dt, Vel32 V, FluxBufs F)
-{
-    const int n = *F.n_nodes;
-    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
-        const unsigned c = F.nodes[t];
-        int i, j, k;
-        cell_of_index(m, c, i, j, k);
-        float x = 0.f, y = 0.f, z = 0.f;
-        project32(m, V, i, j, k, dt, x, y, z);
-        F.nd[0][c] = x;
-        F.nd[1][c] = y;
-        F.nd[2][c] = z;
-    }
-}
-
 /* Staggered trilinear interpolation split as base + correction: the base is the input value
  * at the cell's low corner (exact), the correction the weighted sum of the other corners'
  * differences from it, small where the field is smooth, so its FP32 rounding is small too. */
@@ -977,23 +960,6 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32c(DevMesh m, doubl
         F.nd[0][c] = d[0];
         F.nd[1][c] = d[1];
         F.nd[2][c] = d[2];
-    }
-}
-
-/* FP64 trajectories through the FP64 face velocities (project! in the reference's order). */
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes64(DevMesh m, double dt, adj::Vel V, FluxBufs F)
-{
-    const int n = *F.n_nodes;
-    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
-        const unsigned c = F.nodes[t];
-        int i, j, k;
-        cell_of_index(m, c, i, j, k);
-        const double o[3] = {fco(m, 0, i), fco(m, 1, j), fco(m, 2, k)};
-        double p[3] = {o[0], o[1], o[2]}, xs[3][3];
-        adj::project(m, V, p, i, j, k, dt, xs);
-        F.nd[0][c] = (p[0] - o[0]) / m.d[0];
-        F.nd[1][c] = (p[1] - o[1]) / m.d[1];
-        F.nd[2][c] = (p[2] - o[2]) / m.d[2];
     }
 }
 
@@ -1589,19 +1555,12 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
     Plane32 PL{planes};
     cudaMemsetAsync(L.ctr, 0, 4 * sizeof(int), s);
     k_flux_lists<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, band, list, count, F);
-#if SLVOF_FLUX_TRAJ64
-    (void)uf32; (void)vf32; (void)wf32;
-    k_flux_nodes64<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, adj::Vel{uf, vf, wf}, F);
-#elif SLVOF_FLUX_TRAJ64X
-    (void)uf; (void)vf; (void)wf;
-    k_flux_nodes64x<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
-#elif SLVOF_FLUX_TRAJ32C
-    (void)uf; (void)vf; (void)wf;
+#if SLVOF_FLUX_TRAJ32C
     k_flux_nodes32c<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
 #else
-    (void)uf; (void)vf; (void)wf;
-    k_flux_nodes32<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, (float)dt, Vel32{uf32, vf32, wf32}, F);
+    k_flux_nodes64x<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
 #endif
+    (void)uf; (void)vf; (void)wf;
     k_flux_faces<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, PL, F, errw);
     const int smem = (int)sizeof(FluxShared);
     cudaFuncSetAttribute(k_flux_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

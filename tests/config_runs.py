@@ -47,7 +47,8 @@ def config3d():
     m = Mesh(Nx=128, Ny=128, Nz=128, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5)
     VF0 = cases.vf_spheres(m, np.array([[0.35, 0.35, 0.35]]), np.array([0.15]), nF=20)
     dt = 0.5 * m.dx / 2.0
-    vel = lambda n: cases.deformation3d_faces(m, (n + 0.5) * dt, 3.0)
+    field = cases.Deformation3DFaces(m)
+    vel = lambda n: field.faces((n + 0.5) * dt, 3.0)
     return m, VF0, dt, vel, 1536
 
 
