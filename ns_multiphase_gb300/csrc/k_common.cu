@@ -509,23 +509,6 @@ void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin,
     const dim3 grid((m.N[0] + PURE_BX - 1) / PURE_BX, (m.N[1] + PURE_BY - 1) / PURE_BY, (m.N[2] + CLS_K - 1) / CLS_K);
     k_sl_classify<<<grid, dim3(PURE_BX, PURE_BY), 0, s>>>(m, band, VFin, VFout, list, count);
 }
-/* The same FP32 value plus its residual: lo = a * scale - hi rounded to FP32, so that hi + lo
- * carries the FP64 product to about 48 bits. */
-__global__ void k_to_float2(const double* __restrict__ a, float* __restrict__ hi, float* __restrict__ lo, long n,
-                            double scale)
-{
-    const float s = (float)scale;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-        const double x = a[t];
-        const float h = __double2float_rn(x) * s;
-        hi[t] = h;
-        lo[t] = __double2float_rn(x * scale - (double)h);
-    }
-}
-void launch_to_float2(const double* a, float* hi, float* lo, long n, double scale, int nsm, cudaStream_t s)
-{
-    k_to_float2<<<nsm * 8, 256, 0, s>>>(a, hi, lo, n, scale);
-}
 void launch_to_float(const double* a, float* b, long n, double scale, int nsm, cudaStream_t s)
 {
     k_to_float<<<nsm * 8, 256, 0, s>>>(a, b, n, scale);

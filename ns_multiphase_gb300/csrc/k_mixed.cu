@@ -129,7 +129,8 @@ __device__ __forceinline__ int box_plane_side(const DevMesh& m, const Plane32& P
  * A (sub-)tet whose donor box is uniformly pure is one leaf: every PLIC leaf below it would
  * be d2case case 1 (or 16), so its clipped volume is the tet's own volume, all liquid (or
  * all gas); the mesh-plane cuts under it are skipped. */
-__device__ void clip32(const DevMesh& m, const CutCase* tab, const Plane32& PL, const signed char* __restrict__ phase,
+__device__ __noinline__ void clip32(const DevMesh& m, const CutCase* tab, const Plane32& PL,
+                                    const signed char* __restrict__ phase,
                        int i0, int j0, int k0, const int* rlo, const int* rhi, float* cx, float* cy, float* cz,
                        int (*ci)[3], FF& out_v, FF& out_l, int& err)
 {
@@ -789,113 +790,31 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_lists(DevMesh m, const sh
     }
 }
 
-/* Staggered trilinear interpolation split as base + correction: the base is the input value
- * at the cell's low corner (exact), the correction the weighted sum of the other corners'
- * differences from it, small where the field is smooth, so its FP32 rounding is small too. */
-__device__ __forceinline__ void tri32s(const DevMesh& m, const float* __restrict__ f, const float* __restrict__ fl,
-                                       int I, int J, int K, float wx, float wy, float wz, float& base, float& corr)
-{
-    const long b = cidx(m, I, J, K);
-    /* the residuals (FP64 value - FP32 value) interpolated plainly: they are tiny */
-    const float r = tri32(m, fl, I, J, K, wx, wy, wz);
-    const long sj = m.cs1, sk = m.cs2;
-    const float f000 = __ldg(f + b);
-    const float d100 = __ldg(f + b + 1) - f000, d010 = __ldg(f + b + sj) - f000, d110 = __ldg(f + b + 1 + sj) - f000;
-    const float d001 = __ldg(f + b + sk) - f000, d101 = __ldg(f + b + 1 + sk) - f000,
-                d011 = __ldg(f + b + sj + sk) - f000, d111 = __ldg(f + b + 1 + sj + sk) - f000;
-    const float x00 = wx * d100, x10 = d010 + wx * (d110 - d010);
-    const float x01 = d001 + wx * (d101 - d001), x11 = d011 + wx * (d111 - d011);
-    const float y0 = x00 + wy * (x10 - x00), y1 = x01 + wy * (x11 - x01);
-    base = f000;
-    corr = (y0 + wz * (y1 - y0)) + r;
-}
-
-/* vel32 with each component as base + correction */
-struct Vel32x {
-    const float *uf, *vf, *wf; /* face velocities in cells per unit time, FP32 */
-    const float *ul, *vl, *wl; /* their FP32 residuals: uf + ul is the FP64 value to ~48 bits */
-};
-
-__device__ __forceinline__ void vel32s(const DevMesh& m, const Vel32x& V, int i0, int j0, int k0, float x, float y,
-                                       float z, float* b, float* c)
-{
-    const float B = 1.0e6f;
-    const float fx = fminf(fmaxf(floorf(x), -B), B), fy = fminf(fmaxf(floorf(y), -B), B), fz = fminf(fmaxf(floorf(z), -B), B);
-    const float gx = fminf(fmaxf(floorf(x - 0.5f), -B), B), gy = fminf(fmaxf(floorf(y - 0.5f), -B), B),
-                gz = fminf(fmaxf(floorf(z - 0.5f), -B), B);
-    const int Fx = clampi(i0 + (int)fx, m.lo, m.hi[0] - 1), Cx = clampi(i0 + (int)gx, m.lo, m.hi[0] - 1);
-    const int Fy = clampi(j0 + (int)fy, m.lo, m.hi[1] - 1), Cy = clampi(j0 + (int)gy, m.lo, m.hi[1] - 1);
-    const int Fz = clampi(k0 + (int)fz, m.lo, m.hi[2] - 1), Cz = clampi(k0 + (int)gz, m.lo, m.hi[2] - 1);
-    const float wfx = x - (float)(Fx - i0), wcx = x - ((float)(Cx - i0) + 0.5f);
-    const float wfy = y - (float)(Fy - j0), wcy = y - ((float)(Cy - j0) + 0.5f);
-    const float wfz = z - (float)(Fz - k0), wcz = z - ((float)(Cz - k0) + 0.5f);
-    tri32s(m, V.uf, V.ul, Fx, Cy, Cz, wfx, wcy, wcz, b[0], c[0]);
-    tri32s(m, V.vf, V.vl, Cx, Fy, Cz, wcx, wfy, wcz, b[1], c[1]);
-    tri32s(m, V.wf, V.wl, Cx, Cy, Fz, wcx, wcy, wfz, b[2], c[2]);
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
-{
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-
-/* RK4 displacement of a grid node in FP32 with compensated sums: the stages' base values are
- * summed exactly in float-float (their weights 1, 2, 2, 1 are exact), the corrections in FP32,
- * and the product with -dt/6 is formed as a float-float product, so the displacement (cell
- * units) carries about 1e-9 of a cell of rounding instead of FP32's 6e-8 at coordinates of
- * order one.  The other projections use project32. */
-__device__ __forceinline__ void node_disp32c(const DevMesh& m, const Vel32x& V, int i, int j, int k, double dt,
-                                             double* disp)
-{
-    if (m.projection != 2) {
-        float x = 0.f, y = 0.f, z = 0.f;
-        project32(m, Vel32{V.uf, V.vf, V.wf}, i, j, k, (float)dt, x, y, z);
-        disp[0] = x; disp[1] = y; disp[2] = z;
-        return;
-    }
-    const float h = (float)(0.5 * dt), dtf = (float)dt;
-    float b1[3], c1[3], b2[3], c2[3], b3[3], c3[3], b4[3], c4[3];
-    vel32s(m, V, i, j, k, 0.f, 0.f, 0.f, b1, c1);
-    vel32s(m, V, i, j, k, -h * (b1[0] + c1[0]), -h * (b1[1] + c1[1]), -h * (b1[2] + c1[2]), b2, c2);
-    vel32s(m, V, i, j, k, -h * (b2[0] + c2[0]), -h * (b2[1] + c2[1]), -h * (b2[2] + c2[2]), b3, c3);
-    vel32s(m, V, i, j, k, -dtf * (b3[0] + c3[0]), -dtf * (b3[1] + c3[1]), -dtf * (b3[2] + c3[2]), b4, c4);
-    const double kk = -dt / 6.0;
-    const float khi = (float)kk, klo = (float)(kk - (double)khi);
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        float s, e, s2, e2;
-        two_sum(b1[q], 2.f * b2[q], s, e);
-        two_sum(s, 2.f * b3[q], s2, e2);
-        e += e2;
-        two_sum(s2, b4[q], s, e2);
-        e += e2;
-        e += ((c1[q] + 2.f * c2[q]) + 2.f * c3[q]) + c4[q];
-        /* (s + e) * (khi + klo) */
-        const float p = khi * s;
-        const float pe = fmaf(khi, s, -p) + (khi * e + klo * s);
-        disp[q] = (double)p + (double)pe;
-    }
-}
-
-/* Staggered trilinear interpolation in FP64 of the cell-unit face velocities held as FP32
- * value + FP32 residual (hi + lo, the FP64 velocity to ~48 bits). */
-__device__ __forceinline__ double tri64x(const DevMesh& m, const float* __restrict__ f, const float* __restrict__ fl,
-                                        int I, int J, int K, double wx, double wy, double wz)
+/* Staggered trilinear interpolation of an FP64 face-velocity array (physical units), in
+ * the reference's lerp order along x, then y, then z. */
+__device__ __forceinline__ double tri64(const DevMesh& m, const double* __restrict__ f, int I, int J, int K, double wx,
+                                       double wy, double wz)
 {
     const long b = cidx(m, I, J, K);
     const long sj = m.cs1, sk = m.cs2;
-    auto v = [&](long o) { return (double)__ldg(f + b + o) + (double)__ldg(fl + b + o); };
-    const double f000 = v(0), f100 = v(1), f010 = v(sj), f110 = v(1 + sj);
-    const double f001 = v(sk), f101 = v(1 + sk), f011 = v(sj + sk), f111 = v(1 + sj + sk);
+    const double f000 = __ldg(f + b), f100 = __ldg(f + b + 1), f010 = __ldg(f + b + sj), f110 = __ldg(f + b + 1 + sj);
+    const double f001 = __ldg(f + b + sk), f101 = __ldg(f + b + 1 + sk), f011 = __ldg(f + b + sj + sk),
+                 f111 = __ldg(f + b + 1 + sj + sk);
     const double x00 = f000 + wx * (f100 - f000), x10 = f010 + wx * (f110 - f010);
     const double x01 = f001 + wx * (f101 - f001), x11 = f011 + wx * (f111 - f011);
     const double y0 = x00 + wy * (x10 - x00), y1 = x01 + wy * (x11 - x01);
     return y0 + wz * (y1 - y0);
 }
 
-__device__ __forceinline__ void vel64x(const DevMesh& m, const Vel32x& V, int i0, int j0, int k0, double x, double y,
+struct Vel64c {
+    const double *uf, *vf, *wf; /* face velocities, physical units */
+    double id[3];               /* 1/dx, 1/dy, 1/dz: to cells per unit time */
+};
+
+/* get_velocity_{u,v,w}face (src/Tools.jl:516-641) on the uniform mesh, at a point given in
+ * cell units relative to cell (i0, j0, k0): floor() for the interval search, clamped to
+ * [imino_, imaxo_-1]; the result in cells per unit time. */
+__device__ __forceinline__ void vel64c(const DevMesh& m, const Vel64c& V, int i0, int j0, int k0, double x, double y,
                                        double z, double* u)
 {
     const double B = 1.0e6;
@@ -908,31 +827,45 @@ __device__ __forceinline__ void vel64x(const DevMesh& m, const Vel32x& V, int i0
     const double wfx = x - (double)(Fx - i0), wcx = x - ((double)(Cx - i0) + 0.5);
     const double wfy = y - (double)(Fy - j0), wcy = y - ((double)(Cy - j0) + 0.5);
     const double wfz = z - (double)(Fz - k0), wcz = z - ((double)(Cz - k0) + 0.5);
-    u[0] = tri64x(m, V.uf, V.ul, Fx, Cy, Cz, wfx, wcy, wcz);
-    u[1] = tri64x(m, V.vf, V.vl, Cx, Fy, Cz, wcx, wfy, wcz);
-    u[2] = tri64x(m, V.wf, V.wl, Cx, Cy, Fz, wcx, wcy, wfz);
+    u[0] = tri64(m, V.uf, Fx, Cy, Cz, wfx, wcy, wcz) * V.id[0];
+    u[1] = tri64(m, V.vf, Cx, Fy, Cz, wcx, wfy, wcz) * V.id[1];
+    u[2] = tri64(m, V.wf, Cx, Cy, Fz, wcx, wcy, wfz) * V.id[2];
 }
 
-/* RK4 displacement of a grid node in FP64, cell units, through the velocities' hi + lo. */
-__device__ __forceinline__ void node_disp64x(const DevMesh& m, const Vel32x& V, int i, int j, int k, double dt,
-                                             double* disp)
+/* A grid node's pre-image (project!, src/Tools.jl:392-418) as a displacement in cell units, in
+ * FP64: the face volumes that enter the mass are only as good as the nodes they are built on
+ * (the Zalesak rotation uses the FP32 form of the other kernels). */
+__device__ __forceinline__ void node_disp64(const DevMesh& m, const Vel64c& V, const Vel32& V32, int i, int j, int k,
+                                            double dt, double* disp)
 {
-    if (m.projection != 2) {
-        node_disp32c(m, V, i, j, k, dt, disp);
+    if (m.projection == 3) {
+        float x = 0.f, y = 0.f, z = 0.f;
+        project32(m, V32, i, j, k, (float)dt, x, y, z);
+        disp[0] = x; disp[1] = y; disp[2] = z;
+        return;
+    }
+    double u1[3];
+    vel64c(m, V, i, j, k, 0.0, 0.0, 0.0, u1);
+    if (m.projection == 0) {
+        for (int q = 0; q < 3; ++q) disp[q] = -dt * u1[q];
         return;
     }
     const double h = 0.5 * dt;
-    double u1[3], u2[3], u3[3], u4[3];
-    vel64x(m, V, i, j, k, 0.0, 0.0, 0.0, u1);
-    vel64x(m, V, i, j, k, -h * u1[0], -h * u1[1], -h * u1[2], u2);
-    vel64x(m, V, i, j, k, -h * u2[0], -h * u2[1], -h * u2[2], u3);
-    vel64x(m, V, i, j, k, -dt * u3[0], -dt * u3[1], -dt * u3[2], u4);
+    double u2[3];
+    vel64c(m, V, i, j, k, -h * u1[0], -h * u1[1], -h * u1[2], u2);
+    if (m.projection == 1) {
+        for (int q = 0; q < 3; ++q) disp[q] = -dt * u2[q];
+        return;
+    }
+    double u3[3], u4[3];
+    vel64c(m, V, i, j, k, -h * u2[0], -h * u2[1], -h * u2[2], u3);
+    vel64c(m, V, i, j, k, -dt * u3[0], -dt * u3[1], -dt * u3[2], u4);
     const double c = -dt / 6.0;
 #pragma unroll
     for (int q = 0; q < 3; ++q) disp[q] = c * (((u1[q] + 2.0 * u2[q]) + 2.0 * u3[q]) + u4[q]);
 }
 
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes64x(DevMesh m, double dt, Vel32x V, FluxBufs F)
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes(DevMesh m, double dt, Vel64c V, Vel32 V32, FluxBufs F)
 {
     const int n = *F.n_nodes;
     for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
@@ -940,23 +873,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes64x(DevMesh m, doubl
         int i, j, k;
         cell_of_index(m, c, i, j, k);
         double d[3];
-        node_disp64x(m, V, i, j, k, dt, d);
-        F.nd[0][c] = d[0];
-        F.nd[1][c] = d[1];
-        F.nd[2][c] = d[2];
-    }
-}
-
-/* FP32 trajectories with compensated sums (node_disp32c). */
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_nodes32c(DevMesh m, double dt, Vel32x V, FluxBufs F)
-{
-    const int n = *F.n_nodes;
-    for (int t = blockIdx.x * FLUX_THREADS + threadIdx.x; t < n; t += gridDim.x * FLUX_THREADS) {
-        const unsigned c = F.nodes[t];
-        int i, j, k;
-        cell_of_index(m, c, i, j, k);
-        double d[3];
-        node_disp32c(m, V, i, j, k, dt, d);
+        node_disp64(m, V, V32, i, j, k, dt, d);
         F.nd[0][c] = d[0];
         F.nd[1][c] = d[1];
         F.nd[2][c] = d[2];
@@ -1015,19 +932,40 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
                 int tri[4][3], sg[4];
                 const int nt = flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk),
                                                     tri, sg);
+                /* the prism's three tet volumes in closed form: with e1 = b - a, e2 = c - a in
+                 * the face plane and displacements da, db, dc (a' = a + da, ...),
+                 *   6 V = (e1 x e2).(da + db + dc) + e1.(dc x db) + da.(e1 x dc) + da.(db x e2)
+                 *         + da.(db x dc),
+                 * the sum of tet_vol over (a,b,c,c'), (a,b,c',b'), (a,a',b',c') */
                 double V = 0.0;
+                auto cross = [](const double* u, const double* w, double* r) {
+                    r[0] = u[1] * w[2] - u[2] * w[1];
+                    r[1] = u[2] * w[0] - u[0] * w[2];
+                    r[2] = u[0] * w[1] - u[1] * w[0];
+                };
+                auto dot = [](const double* u, const double* w) { return (u[0] * w[0] + u[1] * w[1]) + u[2] * w[2]; };
                 for (int tr = 0; tr < nt; ++tr) {
-                    double vt = 0.0;
-                    for (int pn = 0; pn < 3; ++pn) {
-                        int q[4];
-                        flux::prism_tet(tri[tr], pn, q);
-                        const double* a = q[0] < 5 ? P[q[0]] : Q[q[0] - 5];
-                        const double* b = q[1] < 5 ? P[q[1]] : Q[q[1] - 5];
-                        const double* c = q[2] < 5 ? P[q[2]] : Q[q[2] - 5];
-                        const double* d = q[3] < 5 ? P[q[3]] : Q[q[3] - 5];
-                        vt += tet_vol<double>(a[0], a[1], a[2], b[0], b[1], b[2], c[0], c[1], c[2], d[0], d[1], d[2]);
+                    const int ia = tri[tr][0], ib = tri[tr][1], ic = tri[tr][2];
+                    double e1[3], e2[3], da[3], db[3], dc[3], sd[3], N[3], t[3];
+                    for (int q = 0; q < 3; ++q) {
+                        e1[q] = P[ib][q] - P[ia][q];
+                        e2[q] = P[ic][q] - P[ia][q];
+                        da[q] = Q[ia][q] - P[ia][q];
+                        db[q] = Q[ib][q] - P[ib][q];
+                        dc[q] = Q[ic][q] - P[ic][q];
+                        sd[q] = (da[q] + db[q]) + dc[q];
                     }
-                    V += sg[tr] > 0 ? vt : -vt;
+                    cross(e1, e2, N);
+                    double six = dot(N, sd);
+                    cross(dc, db, t);
+                    six += dot(e1, t);
+                    cross(e1, dc, t);
+                    six += dot(da, t);
+                    cross(db, e2, t);
+                    six += dot(da, t);
+                    cross(db, dc, t);
+                    six += dot(da, t);
+                    V += sg[tr] > 0 ? six / 6.0 : -six / 6.0;
                 }
                 /* index box of the prism points, relative to the low cell l = h - e_dir */
                 int li = hi, lj = hj, lk = hk;
@@ -1047,6 +985,10 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
                         hiB[q] = max(hiB[q], I);
                     }
                 }
+                /* along dir the prism also spans the layers between the face (between
+                 * layers 0 and 1) and its moved points */
+                lo[dir] = min(lo[dir], 1);
+                hiB[dir] = max(hiB[dir], 0);
                 int side = 0;
                 if (m.fast_pure) {
                     side = npt == 5 ? box_plane_side<10>(m, PL, li, lj, lk, lo[0], hiB[0], lo[1], hiB[1], lo[2], hiB[2],
@@ -1096,7 +1038,7 @@ struct FluxShared {
 
 enum : int { PIECE_LIQ = 1, PIECE_GAS = 2 };
 
-__global__ void __launch_bounds__(CLIPW_WARPS * 32) k_flux_clip(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
+__global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
 {
     extern __shared__ __align__(16) unsigned char flux_smem[];
     FluxShared& S = *reinterpret_cast<FluxShared*>(flux_smem);
@@ -1335,16 +1277,20 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_flux_clip(DevMesh m, Plane
                 }
                 const int nt = C.ntets;
                 if (mode == 1) {
+                    /* the node's pieces summed here, then added to its face's sums once */
                     int fl = 0;
+                    FF nv{0.f, 0.f}, nl{0.f, 0.f};
                     for (int c = 0; c < nt; ++c) {
                         const float4 P0 = S.scr[C.vtet[c][0]][tid], P1 = S.scr[C.vtet[c][1]][tid];
                         const float4 P2 = S.scr[C.vtet[c][2]][tid], P3 = S.scr[C.vtet[c][3]][tid];
                         const float tv = tet_vol<float>(P0.x, P0.y, P0.z, P1.x, P1.y, P1.z, P2.x, P2.y, P2.z, P3.x,
                                                         P3.y, P3.z);
-                        facc_add(avol, b, tv);
-                        if (C.side[c] == 0) { facc_add(acc, b, tv); fl |= PIECE_LIQ; }
+                        ff_add(nv, tv);
+                        if (C.side[c] == 0) { ff_add(nl, tv); fl |= PIECE_LIQ; }
                         else fl |= PIECE_GAS;
                     }
+                    facc_add(avol, b, nv);
+                    facc_add(acc, b, nl);
                     fflag_or(flg, b, fl);
                 } else {
                     const int pos = size + ipush - pushed;
@@ -1555,12 +1501,8 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
     Plane32 PL{planes};
     cudaMemsetAsync(L.ctr, 0, 4 * sizeof(int), s);
     k_flux_lists<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, band, list, count, F);
-#if SLVOF_FLUX_TRAJ32C
-    k_flux_nodes32c<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
-#else
-    k_flux_nodes64x<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel32x{uf32, vf32, wf32, L.vlo[0], L.vlo[1], L.vlo[2]}, F);
-#endif
-    (void)uf; (void)vf; (void)wf;
+    k_flux_nodes<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel64c{uf, vf, wf, {1.0 / m.d[0], 1.0 / m.d[1], 1.0 / m.d[2]}},
+                                                   Vel32{uf32, vf32, wf32}, F);
     k_flux_faces<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, PL, F, errw);
     const int smem = (int)sizeof(FluxShared);
     cudaFuncSetAttribute(k_flux_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -33,7 +33,6 @@ struct slvof_ctx {
     int vcur = 0;
     double *uf = nullptr, *vf = nullptr, *wf = nullptr;
     float *uf32 = nullptr, *vf32 = nullptr, *wf32 = nullptr;
-    float *uf32lo = nullptr, *vf32lo = nullptr, *wf32lo = nullptr; /* FP32 residuals of the above */
     double *nx = nullptr, *ny = nullptr, *nz = nullptr, *D = nullptr;
     float4* planes = nullptr;     /* mixed: donor planes in cell units */
     int2* arb = nullptr;          /* mixed ELVIRA: near-tie cells (cell, contending lanes) for FP64 scoring */
@@ -265,9 +264,6 @@ void st_sl32(slvof_ctx* c, double dt, int o)
                 c->nsm, c->stream);
 #else
     cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream); /* near-pure cells, their clip work */
-    c->flux.vlo[0] = c->uf32lo;
-    c->flux.vlo[1] = c->vf32lo;
-    c->flux.vlo[2] = c->wf32lo;
     launch_sl32_flux(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf32, c->vf32, c->wf32, c->uf, c->vf, c->wf, c->planes,
                      c->band[c->bcur], c->list_sl, c->ctr + C_SL, c->flux, c->slow_cells, c->slow_verts,
                      c->ctr + C_SLOW, c->ctr + C_SLW2, c->ctr + C_ERR, c->nsm, c->stream);
@@ -363,9 +359,9 @@ int d2h(slvof_ctx* c, void* dst, const void* src, size_t bytes)
 void to_float_velocity(slvof_ctx* c)
 {
     if (c->precision != SLVOF_MIXED) return;
-    launch_to_float2(c->uf, c->uf32, c->uf32lo, c->ncell, 1.0 / c->m.d[0], c->nsm, c->stream);
-    launch_to_float2(c->vf, c->vf32, c->vf32lo, c->ncell, 1.0 / c->m.d[1], c->nsm, c->stream);
-    launch_to_float2(c->wf, c->wf32, c->wf32lo, c->ncell, 1.0 / c->m.d[2], c->nsm, c->stream);
+    launch_to_float(c->uf, c->uf32, c->ncell, 1.0 / c->m.d[0], c->nsm, c->stream);
+    launch_to_float(c->vf, c->vf32, c->ncell, 1.0 / c->m.d[1], c->nsm, c->stream);
+    launch_to_float(c->wf, c->wf32, c->ncell, 1.0 / c->m.d[2], c->nsm, c->stream);
 }
 
 int up_velocity(slvof_ctx* c, const double* uf, const double* vf, const double* wf)
@@ -500,9 +496,7 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
               alloc((void**)&c->mass_d, sizeof(double));
     if (ok && precision == SLVOF_MIXED)
         ok = alloc((void**)&c->uf32, c->ncell * sizeof(float)) && alloc((void**)&c->vf32, c->ncell * sizeof(float)) &&
-             alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->uf32lo, c->ncell * sizeof(float)) &&
-             alloc((void**)&c->vf32lo, c->ncell * sizeof(float)) && alloc((void**)&c->wf32lo, c->ncell * sizeof(float)) &&
-             alloc((void**)&c->planes, c->ncell * sizeof(float4)) &&
+             alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4)) &&
              alloc((void**)&c->slow_cells, interior * sizeof(int)) &&
              alloc((void**)&c->slow_verts, interior * (mesh->tesselation == 24 ? 16 : 8) * sizeof(float4)) &&
              alloc((void**)&c->arb, interior * sizeof(int2));
@@ -542,8 +536,7 @@ int slvof_destroy(slvof_ctx* c)
     if (!c) return SLVOF_OK;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    void* bufs[] = {c->coords, c->VF[0], c->VF[1], c->uf, c->vf, c->wf, c->uf32, c->vf32, c->wf32, c->uf32lo,
-                    c->vf32lo, c->wf32lo, c->nx, c->ny,
+    void* bufs[] = {c->coords, c->VF[0], c->VF[1], c->uf, c->vf, c->wf, c->uf32, c->vf32, c->wf32, c->nx, c->ny,
                     c->nz, c->D, c->planes, c->phase, c->cand, c->band[0], c->band[1], c->list_sl, c->list_if,
                     c->list_plic, c->slow_cells, c->slow_verts, c->arb, c->ctr, c->partials, c->mass_d, c->table,
                     c->spheres, c->gvf[0], c->gvf[1], c->gfold, c->gn[0], c->gn[1], c->gn[2], c->gD, c->gnf[0],

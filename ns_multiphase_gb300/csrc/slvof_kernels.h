@@ -21,8 +21,6 @@ void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, i
 void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin, double* VFout, int* list, int* count,
                         int nsm, cudaStream_t s);
 void launch_to_float(const double* a, float* b, long n, double scale, int nsm, cudaStream_t s);
-/* FP32 value and FP32 residual of a * scale (hi + lo good to about 48 bits) */
-void launch_to_float2(const double* a, float* hi, float* lo, long n, double scale, int nsm, cudaStream_t s);
 void launch_case_spheres(const DevMesh& m, const double* cen, const double* rad, int n, int nF, int dims,
                          const double* table, double* VF, int nsm, cudaStream_t s);
 void launch_case_deformation3d(const DevMesh& m, double t, double T, double* uf, double* vf, double* wf, int nsm,
@@ -58,7 +56,6 @@ void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const doub
  * (volume, liquid) arrays indexed like the cell arrays, the node / face / clip-face lists
  * (capacity: cells, 3 x cells, 3 x cells) and four counters */
 struct FluxLaunch {
-    const float* vlo[3]; /* FP32 residuals of the cell-unit face velocities */
     double* nd[3];
     double2* fvf[3];
     unsigned* nodes;
@@ -71,7 +68,6 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
                       const float4* planes, const short* band, const int* list, const int* count,
                       const FluxLaunch& L, int* slow_cells, float4* slow_verts, int* slow_count, int* work2,
                       int* errw, int nsm, cudaStream_t s);
-/* FluxLaunch's node pass also reads the FP32 residuals of the face velocities (velocity_lo) */
 /* mixed ELVIRA: FP32 scoring (warp per cell), FP64 arbitration of the near-ties listed in arb
  * (n_arb zeroed by the caller; capacity: the interface count), FP64 winner normals */
 void launch_elvira_iface32(const DevMesh& m, const double* VF, double* nx, double* ny, double* nz, const int* list,
