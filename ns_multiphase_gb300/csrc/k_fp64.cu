@@ -922,11 +922,14 @@ void launch_sl64(const DevMesh& m, double dt, const double* VFin, double* VFout,
     (void)VFin;
     Vel64 V{uf, vf, wf};
     Plic64 P{nx, ny, nz, D, nullptr, nullptr, nullptr, 0.0, 0.0};
-    /* the clip frames' shared-memory share: 3 frames x 128 threads (101 KB, two blocks per SM) */
+    /* the clip frames' shared-memory share: 3 frames x 128 threads (101 KB, two blocks per SM);
+     * the grid holds as many blocks as fit at once, which fetch their cells from the list */
     const int smem = SL_THREADS * SL64_SMEM_FRAMES * (int)sizeof(Frame64<false>);
     cudaFuncSetAttribute(k_sl64<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k_sl64<false><<<nsm * 2, SL_THREADS, smem, s>>>(m, dt, phase, VFout, V, P, list, count, work, nullptr, nullptr,
-                                                    nullptr, errw);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl64<false>, SL_THREADS, smem);
+    k_sl64<false><<<nsm * max(per_sm, 1), SL_THREADS, smem, s>>>(m, dt, phase, VFout, V, P, list, count, work,
+                                                                 nullptr, nullptr, nullptr, errw);
 }
 
 void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const double* uf, const double* vf,
@@ -939,7 +942,10 @@ void launch_sl64_momentum(const DevMesh& m, double dt, double* VFout, const doub
     Plic64 P{nx, ny, nz, D, u, v, w, rho_liq, rho_gas};
     const int smem = SL_THREADS * SL64_SMEM_FRAMES * (int)sizeof(Frame64<true>);
     cudaFuncSetAttribute(k_sl64<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k_sl64<true><<<nsm * 2, SL_THREADS, smem, s>>>(m, dt, phase, VFout, V, P, list, count, work, us, vs, ws, errw);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sl64<true>, SL_THREADS, smem);
+    k_sl64<true><<<nsm * max(per_sm, 1), SL_THREADS, smem, s>>>(m, dt, phase, VFout, V, P, list, count, work, us, vs,
+                                                                ws, errw);
     k_mom_flux64<<<nsm * 8, 128, 0, s>>>(m, dt, V, P, band, us, vs, ws);
 }
 
