@@ -31,6 +31,7 @@ extern "C" {
 #define SLVOF_DEV_DEPTH 2  /* cutTet recursion deeper than the clip stack (src/VFgeom.jl:713-900) */
 #define SLVOF_DEV_NAN 4    /* NaN signed distance in a cut (reference: InexactError in d2case) */
 #define SLVOF_DEV_VOLUME 8 /* non-positive or non-finite pre-image volume (src/Transport.jl:145) */
+#define SLVOF_DEV_WAIT 16  /* a kernel's bounded wait on its own bulk copies ran out (its output is incomplete) */
 /* host errors */
 #define SLVOF_E_ARG (-1)
 #define SLVOF_E_CUDA (-2)

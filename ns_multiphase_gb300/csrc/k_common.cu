@@ -4,6 +4,7 @@
  */
 #include "slvof_kernels.h"
 #include "slvof_dev.cuh"
+#include "tma.cuh"
 
 namespace slvof {
 
@@ -86,7 +87,12 @@ __global__ void __launch_bounds__(PURE_BX * PURE_BY) k_elvira_pure(DevMesh m, co
             nx[o] = ax; ny[o] = ay; nz[o] = az;
         }
     }
-    if (list) warp_append(iface, L, list, count);
+    if (list) {
+        __shared__ int s_app[PURE_BX * PURE_BY / 32 + 1];
+        const bool f[1] = {iface};
+        const int it[1] = {L};
+        block_append<1, PURE_BX * PURE_BY / 32>(f, it, list, count, s_app);
+    }
     /* block sum: exact, so its order does not matter */
     for (int off = 16; off > 0; off >>= 1) acc += i128_shfl_down(acc, off);
     __shared__ long long sh_hi[PURE_BX * PURE_BY / 32];
@@ -224,6 +230,91 @@ __global__ void __launch_bounds__(BX * BY) k_band_first(DevMesh m, const double*
     band_march(m, cls, fin);
 }
 
+/* The first pass with each (tile + halo) plane of VF brought into shared memory by the TMA
+ * unit: a ring of TB_STAGES planes, the load of plane p + TB_STAGES issued as soon as plane p
+ * is classified, so the loads run ahead of the march instead of every thread issuing its
+ * own.  The tile's first halo element sits at an odd VF element on grids with g = 3 (VF
+ * starts 3 + g cells before cell 1) and a bulk tensor copy must start on a 16-byte boundary,
+ * so the box starts one element lower where needed and is TB_W = BX + 4 elements wide.  A
+ * wait that runs out sets ERR_WAIT and the block stops (after waiting, bounded again, for its
+ * copies in flight). */
+constexpr int TB_STAGES = 4;
+constexpr int TB_W = BX + 4, TB_H = BY + 2;
+constexpr int TB_BYTES = TB_W * TB_H * (int)sizeof(double);
+constexpr int TB_STRIDE = (TB_BYTES + 127) / 128 * 128;
+
+__global__ void __launch_bounds__(BX * BY) k_band_first_tma(DevMesh m, const __grid_constant__ CUtensorMap map,
+                                                           short* __restrict__ bout, int* errw)
+{
+    __shared__ __align__(128) unsigned char stage[TB_STAGES * TB_STRIDE];
+    __shared__ __align__(8) unsigned long long bar[TB_STAGES];
+    __shared__ unsigned char raw[BY + 2][BX + 2];
+    __shared__ unsigned char dil[3][BY][BX];
+    __shared__ int stop;
+    const short nb1 = (short)(m.nband + 1);
+    const long long lob = dbits(m.VFlo), hib = dbits(m.VFhi);
+    const int tid = threadIdx.y * BX + threadIdx.x;
+    const int i0 = 1 + blockIdx.x * BX, j0 = 1 + blockIdx.y * BY;
+    const int kbeg = 1 + blockIdx.z * BZ, kend = min(kbeg + BZ - 1, m.N[2]);
+    const int nplanes = kend - kbeg + 3; /* planes kbeg-1 .. kend+1 */
+    const int x0 = i0 - 1 - m.vlo, xa = x0 & ~1, xoff = x0 - xa;
+    const int y0 = j0 - 1 - m.vlo, z0 = kbeg - 1 - m.vlo;
+    if (tid == 0) {
+        for (int r = 0; r < TB_STAGES; ++r) tma::bar_init(&bar[r], 1);
+        tma::fence_bar_init();
+        stop = 0;
+        for (int p = 0; p < min(TB_STAGES, nplanes); ++p) {
+            tma::bar_arrive_expect(&bar[p], TB_BYTES);
+            tma::load_3d(stage + p * TB_STRIDE, &map, xa, y0, z0 + p, &bar[p]);
+        }
+    }
+    __syncthreads();
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    long long cprev = 0;
+    int p = 0;
+    for (; p < nplanes; ++p) {
+        const int r = p % TB_STAGES;
+        if (!tma::bar_wait(&bar[r], (unsigned)(p / TB_STAGES) & 1u)) stop = 1;
+        __syncthreads();
+        if (stop) break;
+        const double* V = reinterpret_cast<const double*>(stage + r * TB_STRIDE);
+        for (int t = tid; t < (BX + 2) * (BY + 2); t += BX * BY) {
+            const int a = t % (BX + 2), b = t / (BX + 2);
+            const long long v = dbits(V[b * TB_W + a + xoff]);
+            raw[b][a] = (unsigned char)((!bits_below(v, hib) ? 1 : 0) | (!bits_above(v, lob) ? 2 : 0));
+        }
+        const long long ccur = dbits(V[(threadIdx.y + 1) * TB_W + threadIdx.x + 1 + xoff]);
+        __syncthreads(); /* raw complete; every thread is done with stage r */
+        if (tid == 0 && p + TB_STAGES < nplanes) {
+            tma::fence_proxy_async();
+            tma::bar_arrive_expect(&bar[r], TB_BYTES);
+            tma::load_3d(stage + r * TB_STRIDE, &map, xa, y0, z0 + p + TB_STAGES, &bar[r]);
+        }
+        unsigned char d = 0;
+#pragma unroll
+        for (int b = 0; b <= 2; ++b)
+#pragma unroll
+            for (int a = 0; a <= 2; ++a) d |= raw[threadIdx.y + b][threadIdx.x + a];
+        dil[p % 3][threadIdx.y][threadIdx.x] = d;
+        __syncthreads();
+        if (p >= 2 && i <= m.N[0] && j <= m.N[1]) {
+            /* cell (i, j, k) of plane p - 1, its 3x3x3 block in the three dilated planes */
+            const int k = kbeg - 2 + p;
+            const unsigned char any = dil[0][threadIdx.y][threadIdx.x] | dil[1][threadIdx.y][threadIdx.x] |
+                                      dil[2][threadIdx.y][threadIdx.x];
+            short bv = 0;
+            if (bits_below(cprev, lob)) bv = (any & 1) ? (short)0 : (short)-nb1;
+            else if (bits_above(cprev, hib)) bv = (any & 2) ? (short)0 : nb1;
+            bout[cidx(m, i, j, k)] = bv;
+        }
+        cprev = ccur;
+    }
+    if (stop && tid == 0) {
+        atomicOr(errw, ERR_WAIT);
+        for (int q = p; q < min(p + TB_STAGES, nplanes); ++q) tma::bar_wait(&bar[q % TB_STAGES], (unsigned)(q / TB_STAGES) & 1u);
+    }
+}
+
 /* Neumann!(band) + update_borders!(band) (neumann=true) or update_borders!(band) alone. */
 __global__ void k_band_ghost(DevMesh m, const short* __restrict__ bin, short* __restrict__ bout, bool neumann)
 {
@@ -262,7 +353,8 @@ __global__ void __launch_bounds__(BX * BY) k_band_sweep(DevMesh m, const short* 
  * keep VF.  Thread per (i, j) column of CLS_K cells in k on the pure-cell tiles, so no index
  * divides: a warp reads rows of 32 band entries and copies rows of VF.  Every band entry and
  * VF value of the column is loaded before any is used (the VF of band cells too, which are
- * about a tenth), so the loads of a thread overlap instead of waiting on each other. */
+ * about a tenth), so the loads of a thread overlap instead of waiting on each other; the band
+ * cells of a block join the list with one atomic. */
 constexpr int CLS_K = 4;
 
 __global__ void __launch_bounds__(PURE_BX * PURE_BY) k_sl_classify(DevMesh m, const short* __restrict__ band,
@@ -281,14 +373,18 @@ __global__ void __launch_bounds__(PURE_BX * PURE_BY) k_sl_classify(DevMesh m, co
         b[q] = in ? __ldg(band + cidx(m, i, j, k0 + q)) : (short)0;
         v[q] = in ? __ldg(VFin + vidx(m, i, j, k0 + q)) : 0.0;
     }
+    bool sl[CLS_K];
+    int item[CLS_K];
 #pragma unroll
     for (int q = 0; q < CLS_K; ++q) {
         const int k = k0 + q;
         const bool in = col && k <= m.N[2];
-        const bool sl = in && abs((int)b[q]) <= m.nband;
-        if (in && !sl) VFout[vidx(m, i, j, k)] = v[q];
-        warp_append(sl, (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1], list, count);
+        sl[q] = in && abs((int)b[q]) <= m.nband;
+        item[q] = (i - 1) + (j - 1) * m.N[0] + (k - 1) * m.N[0] * m.N[1];
+        if (in && !sl[q]) VFout[vidx(m, i, j, k)] = v[q];
     }
+    __shared__ int s_app[PURE_BX * PURE_BY / 32 * CLS_K + 1];
+    block_append<CLS_K, PURE_BX * PURE_BY / 32>(sl, item, list, count, s_app);
 }
 
 /* FP64 array to FP32 times a scale (face velocities to cells per unit time): the conversion
@@ -488,10 +584,52 @@ void launch_mass_final(const long long* partials, long nblocks, double cellvol, 
 {
     k_mass_final<<<1, MASS_THREADS, 0, s>>>(partials, nblocks, cellvol, out);
 }
-void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s)
+/* cuTensorMapEncodeTiled, from the driver through the runtime (no link against libcuda) */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled()
 {
+    static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return reinterpret_cast<EncodeTiledFn>(f);
+    }();
+    return fn;
+}
+
+/* The TMA map of a VF array for k_band_first_tma: 3D, FP64, box TB_W x TB_H x 1, zero fill
+ * outside the array (only cells past N + 1 of a partial tile read there, and no output
+ * depends on them).  False where the row or plane stride is not a multiple of 16 bytes (an
+ * odd Nx) or the base is not 16-byte aligned: the plain kernel runs then. */
+static bool band_tma_map(const DevMesh& m, const double* VF, CUtensorMap* map)
+{
+    const EncodeTiledFn enc = encode_tiled();
+    if (!enc || (m.vs1 * sizeof(double)) % 16 != 0 || (m.vs2 * sizeof(double)) % 16 != 0 ||
+        reinterpret_cast<uintptr_t>(VF) % 16 != 0)
+        return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)m.vs1, (cuuint64_t)(m.vs2 / m.vs1),
+                                (cuuint64_t)(m.N[2] + 2 * m.g + 6)};
+    const cuuint64_t strides[2] = {(cuuint64_t)m.vs1 * sizeof(double), (cuuint64_t)m.vs2 * sizeof(double)};
+    const cuuint32_t box[3] = {TB_W, TB_H, 1}, estr[3] = {1, 1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(VF), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+void launch_band_first(const DevMesh& m, const double* VF, short* bout, int* errw, int nsm, cudaStream_t s)
+{
+    (void)nsm;
     const dim3 grid((m.N[0] + BX - 1) / BX, (m.N[1] + BY - 1) / BY, (m.N[2] + BZ - 1) / BZ);
-    k_band_first<<<grid, dim3(BX, BY), 0, s>>>(m, VF, bout);
+    CUtensorMap map;
+    if (band_tma_map(m, VF, &map))
+        k_band_first_tma<<<grid, dim3(BX, BY), 0, s>>>(m, map, bout, errw);
+    else
+        k_band_first<<<grid, dim3(BX, BY), 0, s>>>(m, VF, bout);
 }
 void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neumann, int nsm, cudaStream_t s)
 {

@@ -371,10 +371,7 @@ __global__ void __launch_bounds__(EL32_WARPS * 32) k_elvira_iface32(DevMesh m, c
             }
             err_ = e2;
             /* bound on the FP32 error of e2: each fraction is good to a few 1e-7 */
-#ifndef SLVOF_ELVIRA_TOL_SCALE
-#define SLVOF_ELVIRA_TOL_SCALE 1.0f
-#endif
-            tol = SLVOF_ELVIRA_TOL_SCALE * (4e-6f * sa + 1e-5f * e2 + 1e-12f);
+            tol = 4e-6f * sa + 1e-5f * e2 + 1e-12f;
         }
         /* FP32 winner and the set of candidates that could beat it in exact arithmetic */
         const bool fin = err_ < INFINITY;

@@ -151,35 +151,56 @@ __global__ void __launch_bounds__(EL_WARPS * 32) k_elvira_iface64(DevMesh m, con
  * layers), so its phase code is +-1, and the plane (0, 0, 0, D) in its cell frame puts every
  * point of the domain on the same side as its own plane does: no normals are read and no FP64
  * arithmetic is done for the 97% of cells that are pure.  Threads map to (i, j) of a plane
- * and blocks to k, so no index divides. */
-__global__ void k_plic_pure(DevMesh m, const double* __restrict__ VF, double* __restrict__ D,
-                            float4* __restrict__ planes, signed char* __restrict__ phase, int* list, int* count,
-                            float Lsum_f)
+ * and blocks to PLIC_PK planes in k, so no index divides. */
+constexpr int PLIC_PK = 4; /* planes per thread */
+
+__global__ void __launch_bounds__(256) k_plic_pure(DevMesh m, const double* __restrict__ VF, double* __restrict__ D,
+                                                   float4* __restrict__ planes, signed char* __restrict__ phase,
+                                                   int* list, int* count, float Lsum_f)
 {
     /* the thresholds are tested on the bit patterns (integer pipe), the outputs are copies */
     const long long lob = dbits(m.VFlo), hib = dbits(m.VFhi);
-    const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g;
+    const int n0 = m.N[0] + 2 * m.g, n1 = m.N[1] + 2 * m.g, n2 = m.N[2] + 2 * m.g;
     const int a = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y * blockDim.y + threadIdx.y;
-    const int c = blockIdx.z;
-    bool defer = false;
-    long t = 0;
-    if (a < n0 && b < n1) {
-        const int ip = a + m.lo, jp = b + m.lo, kp = c + m.lo;
-        t = (long)a + (long)b * n0 + (long)c * n0 * n1;
-        const int i = ghost_src_1d(ip, m.N[0], m.g, m.per[0], false);
-        const int j = ghost_src_1d(jp, m.N[1], m.g, m.per[1], false);
-        const int k = ghost_src_1d(kp, m.N[2], m.g, m.per[2], false);
-        const long long v = dbits(VF[vidx(m, i, j, k)]);
-        const bool gas = bits_below(v, lob);
-        if (gas || bits_above(v, hib)) {
-            D[t] = gas ? -m.Lsum : m.Lsum;
-            phase[t] = gas ? -1 : 1;
-            if (planes) planes[t] = make_float4(0.f, 0.f, 0.f, gas ? -Lsum_f : Lsum_f);
-        } else {
-            defer = true; /* interface (or NaN) source */
+    const int c0 = blockIdx.z * PLIC_PK;
+    const bool col = a < n0 && b < n1;
+    const int ip = a + m.lo, jp = b + m.lo;
+    const int i = ghost_src_1d(ip, m.N[0], m.g, m.per[0], false);
+    const int j = ghost_src_1d(jp, m.N[1], m.g, m.per[1], false);
+    /* every load of the thread's column first (VF of the border source and the stored code),
+     * so they overlap */
+    long long v[PLIC_PK];
+    signed char old[PLIC_PK];
+    long t[PLIC_PK];
+#pragma unroll
+    for (int q = 0; q < PLIC_PK; ++q) {
+        const bool in = col && c0 + q < n2;
+        t[q] = (long)a + (long)b * n0 + (long)(c0 + q) * n0 * n1;
+        const int k = ghost_src_1d(c0 + q + m.lo, m.N[2], m.g, m.per[2], false);
+        v[q] = in ? dbits(VF[vidx(m, i, j, k)]) : 0;
+        old[q] = in ? phase[t[q]] : (signed char)0;
+    }
+    bool defer[PLIC_PK];
+    int item[PLIC_PK];
+#pragma unroll
+    for (int q = 0; q < PLIC_PK; ++q) {
+        const bool in = col && c0 + q < n2;
+        const bool gas = bits_below(v[q], lob);
+        const bool pure = in && (gas || bits_above(v[q], hib));
+        defer[q] = in && !pure; /* interface (or NaN) source */
+        item[q] = (int)t[q];
+        /* a stored code of -1 or +1 comes with D = -/+Lsum and a plane with every point of
+         * the domain on that side (written here or by plic_outputs; the buffers start at
+         * code 0), so only cells whose code changes are written */
+        const signed char want = gas ? -1 : 1;
+        if (pure && old[q] != want) {
+            D[t[q]] = gas ? -m.Lsum : m.Lsum;
+            phase[t[q]] = want;
+            if (planes) planes[t[q]] = make_float4(0.f, 0.f, 0.f, gas ? -Lsum_f : Lsum_f);
         }
     }
-    warp_append(defer, (int)t, list, count);
+    __shared__ int s_app[8 * PLIC_PK + 1];
+    block_append<PLIC_PK, 8>(defer, item, list, count, s_app); /* blocks of 32 x 8 */
 }
 
 /* computeDist (src/VF.jl:109-156) for the deferred cells: D(p) = computeDist at the border
@@ -906,7 +927,8 @@ void launch_elvira_iface64(const DevMesh& m, const double* VF, double* nx, doubl
 void launch_plic64(const DevMesh& m, const double* VF, const double* nx, const double* ny, const double* nz, double* D,
                    float4* planes, signed char* phase, int* list, int* count, bool newton_root, int nsm, cudaStream_t s)
 {
-    const dim3 grid((m.N[0] + 2 * m.g + 31) / 32, (m.N[1] + 2 * m.g + 7) / 8, m.N[2] + 2 * m.g);
+    const dim3 grid((m.N[0] + 2 * m.g + 31) / 32, (m.N[1] + 2 * m.g + 7) / 8,
+                    (m.N[2] + 2 * m.g + PLIC_PK - 1) / PLIC_PK);
     k_plic_pure<<<grid, dim3(32, 8), 0, s>>>(m, VF, D, planes, phase, list, count, (float)m.Lsum);
     if (newton_root)
         launch_plic_iface_newton(m, VF, nx, ny, nz, D, planes, phase, list, count, nsm, s);

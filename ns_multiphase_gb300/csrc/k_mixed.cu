@@ -6,14 +6,26 @@
  * and the cell volume is 1.  This needs a uniform mesh, which create_mesh builds
  * (src/Mesh.jl:83-100); slvof_create rejects the mixed mode otherwise.
  *
- *   k_sl32_pre       : the eight FP32 RK pre-image vertices of every band cell through FP32
- *                      face velocities (thread per cell); cells whose pre-image is strictly
- *                      on one side of every donor plane it reaches are finished there, the
- *                      others are compacted with their vertices for the clip.
- *   k_sl32_clipw     : warp-cooperative FP32 clip of those cells' tets (cutTet's cut tables
- *                      and cuts, src/VFgeom.jl:713-900), with the pending sub-tets of a batch
- *                      of cells in a shared-memory stack and each cell's volume and liquid
- *                      volume summed in float-float, then VFnew = vLiq/vol in FP64.
+ * The step's SL update is the flux form: VFnew = (L + sum +-F_f) / (1 + sum +-V_f) over each band
+ * cell's six faces, with F_f the liquid and V_f the volume swept through face f (the prism
+ * between the face and its traced pre-image, split as the cell pre-images of the reference are,
+ * src/VFgeom.jl:229-332), so each face is computed once and shared by the two cells beside it.
+ *
+ *   k_flux_lists     : band-cell nodes and faces, each listed by the band cell that owns it.
+ *   k_flux_nodes     : the RK trace of every listed grid node (FP64, from the FP64 face
+ *                      velocities), stored once and read by every prism that uses the node.
+ *   k_flux_faces     : each face's swept volume V_f in FP64 (closed form); faces whose prism
+ *                      lies in cells of one phase take F_f = V_f or 0, the others are listed.
+ *   k_flux_clip      : warp-cooperative FP32 clip of the listed faces' prism tets (cutTet's cut
+ *                      tables and cuts, src/VFgeom.jl:713-900), pending sub-tets of a batch of
+ *                      faces in a shared-memory stack, liquid and volume summed in float-float;
+ *                      the liquid is then rescaled to the FP64 volume.
+ *   k_flux_cells     : VFnew per band cell; cells with an all-liquid or all-gas pre-image give
+ *                      exactly 1 or 0, cells within 1e-6 of 0 or 1 are listed for the cell form.
+ *   k_sl32_pre       : the cell form's eight FP32 pre-image vertices per band cell (the
+ *                      reverse pass's input).
+ *   k_sl32_clipw     : the cell form's warp-cooperative clip of listed cells' tets (the flux
+ *                      form's near-pure cells).
  */
 #include "slvof_kernels.h"
 #include "slvof_dev.cuh"
@@ -1038,6 +1050,56 @@ struct FluxShared {
 
 enum : int { PIECE_LIQ = 1, PIECE_GAS = 2 };
 
+#if SLVOF_FCLIP_COLD
+/* Seed tet n of face b of a batch: the prism tet oriented for the low cell, its vertices'
+ * cell indices, the face's batch slot in vertex 0's tag; written to stk[0..3] (the lane's
+ * column of the warp's node stack).  Out of line: it runs once per batch. */
+__device__ __noinline__ void flux_seed(const DevMesh& m, const FluxBufs F, unsigned code, int b, int n,
+                                       float4* stk0, float4* stk1, float4* stk2, float4* stk3, int& err)
+{
+    float4* stk[4] = {stk0, stk1, stk2, stk3};
+                int dir, hi, hj, hk;
+        face_decode(m, code, dir, hi, hj, hk);
+        double P[5][3], Q[5][3];
+        face_points(m, F, dir, hi, hj, hk, P, Q);
+        int tri[4][3], sg[4];
+        flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
+        int q[4];
+        flux::prism_tet(tri[n / 3], n % 3, q);
+        if (sg[n / 3] < 0) { const int x = q[0]; q[0] = q[1]; q[1] = x; }
+        const int li = hi - (dir == 0), lj = hj - (dir == 1), lk = hk - (dir == 2);
+        int rlo[3], rhi[3];
+        rel_bounds(m, li, lj, lk, rlo, rhi);
+        float4 v[4];
+        int I[4][3];
+        int mlo = 1 << 20;
+        for (int nn = 0; nn < 4; ++nn) {
+            const double* x = q[nn] < 5 ? P[q[nn]] : Q[q[nn] - 5];
+            v[nn] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
+            if (q[nn] >= 5) {
+                I[nn][0] = idx32(v[nn].x, 0, rlo[0], rhi[0], err);
+                I[nn][1] = idx32(v[nn].y, 0, rlo[1], rhi[1], err);
+                I[nn][2] = idx32(v[nn].z, 0, rlo[2], rhi[2], err);
+                mlo = min(mlo, I[nn][dir]);
+            }
+        }
+        /* the face's own points lie on the plane between l (0) and h (1) and inside the
+         * tangential range of l's column: index 0 across, and along dir the side of this
+         * tet's moved points (either index contains them) */
+        for (int nn = 0; nn < 4; ++nn)
+            if (q[nn] < 5) {
+                I[nn][0] = I[nn][1] = I[nn][2] = 0;
+                I[nn][dir] = mlo >= 1 ? 1 : 0;
+            }
+        for (int nn = 0; nn < 4; ++nn) {
+            unsigned pk = pack3(I[nn][0], I[nn][1], I[nn][2]);
+            if (nn == 0) pk |= (unsigned)b << 24;
+            v[nn].w = __int_as_float((int)pk);
+            *stk[nn] = v[nn];
+        }
+}
+#endif
+
 __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
 {
     extern __shared__ __align__(16) unsigned char flux_smem[];
@@ -1099,6 +1161,13 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
 #pragma unroll
         for (int b = 0; b < FCLIP_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; flg[b] = 0; }
         const unsigned code = __shfl_sync(0xffffffffu, code_, min(lane / ntet, FCLIP_BATCH - 1));
+#if SLVOF_FCLIP_COLD
+        if (lane < ntet * nb) {
+            const int b = lane / ntet, n = lane - ntet * b;
+            flux_seed(m, F, code, b, n, &S.stk[w][0][lane], &S.stk[w][1][lane], &S.stk[w][2][lane],
+                      &S.stk[w][3][lane], err);
+        }
+#else
         if (lane < ntet * nb) {
             const int b = lane / ntet, n = lane - ntet * b;
             int dir, hi, hj, hk;
@@ -1141,6 +1210,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                 S.stk[w][nn][lane] = v[nn];
             }
         }
+#endif
         int size = ntet * nb;
         __syncwarp();
         int guard = 0;
@@ -1246,9 +1316,14 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                     S.scr[nn][tid] = make_float4(v[nn].x, v[nn].y, v[nn].z, __int_as_float((int)s1p[nn]));
                 }
                 const int nvert = C.nvert;
+#if SLVOF_FCLIP_ROLL
+#pragma unroll 1
+                for (int nn = 0; nn < nvert; ++nn) {
+#else
 #pragma unroll
                 for (int nn = 0; nn < 4; ++nn) {
                     if (nn >= nvert) break;
+#endif
                     const int e1 = C.v1[nn], e2 = C.v2[nn];
                     const float4 A = S.scr[e1][tid], Bv = S.scr[e2][tid];
                     const float da = sel4(d0, d1, d2, d3, e1), db = sel4(d0, d1, d2, d3, e2);
@@ -1264,7 +1339,11 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
 #pragma unroll
                         for (int q = 0; q < 3; ++q) {
                             const float u = q == 0 ? x : (q == 1 ? y : z);
+#if SLVOF_FCLIP_ROLL
+                            const int Iv = idx32(u, unpack(wbits(S.scr[nn][tid]), q), rlo[q], rhi[q], err);
+#else
                             const int Iv = idx32(u, unpack(s1p[nn], q), rlo[q], rhi[q], err);
+#endif
                             const int a1 = unpack(pa, q), a2 = unpack(pb, q);
                             nv[q] = min(max(Iv, min(a1, a2)), max(a1, a2));
                         }
@@ -1478,17 +1557,6 @@ void launch_sl32_clip(const DevMesh& m, double* VFout, const float4* planes, int
     k_sl32_clipw<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, VFout, PL, slow_cells, slow_verts, slow_count, work2,
                                                           errw);
 }
-
-void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
-                 const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
-                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, int* errw,
-                 int nsm, cudaStream_t s)
-{
-    launch_sl32_pre(m, dt, VFout, uf, vf, wf, planes, phase, list, count, work, slow_cells, slow_verts, slow_count,
-                    errw, nsm, s);
-    launch_sl32_clip(m, VFout, planes, work2, slow_cells, slow_verts, slow_count, errw, nsm, s);
-}
-
 
 void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* VFout, const float* uf32,
                       const float* vf32, const float* wf32, const double* uf, const double* vf, const double* wf,

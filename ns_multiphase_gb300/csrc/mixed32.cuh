@@ -126,7 +126,7 @@ __device__ __forceinline__ void rel_bounds(const DevMesh& m, int i, int j, int k
     rhi[0] = min(m.hi[0] - i, REL); rhi[1] = min(m.hi[1] - j, REL); rhi[2] = min(m.hi[2] - k, REL);
 }
 
-/* ---- pieces of the warp-cooperative clips (k_mixed.cu, k_flux.cu) ------------------- */
+/* ---- pieces of the warp-cooperative clips (k_sl32_clipw, k_flux_clip) ----------------- */
 /* float-float running sum (TwoSum error-free transformation): ~48-bit accumulation of the
  * FP32 sub-tet volumes without using the FP64 pipe. */
 struct FF {

@@ -217,7 +217,7 @@ int st_band(slvof_ctx* c, cudaStream_t st = nullptr)
     cudaStream_t s = st ? st : c->stream;
     int b = c->bcur;
     s_beg(c, S_BAND, s);
-    launch_band_first(c->m, c->VF[c->vcur], c->band[1 - b], c->nsm, s);
+    launch_band_first(c->m, c->VF[c->vcur], c->band[1 - b], c->ctr + C_ERR, c->nsm, s);
     launch_band_ghost(c->m, c->band[b], c->band[1 - b], true, c->nsm, s);
     b = 1 - b;
     for (int n = 1; n <= c->m.nband; ++n) {
@@ -258,16 +258,10 @@ int join_band(slvof_ctx* c, int r)
  * volume in FP64 and its liquid from the FP32 clip, shared by the two cells beside it). */
 void st_sl32(slvof_ctx* c, double dt, int o)
 {
-#if SLVOF_SL_CELLFORM
-    launch_sl32(c->m, dt, c->VF[o], c->uf32, c->vf32, c->wf32, c->planes, c->phase, c->list_sl, c->ctr + C_SL,
-                c->ctr + C_SLW, c->ctr + C_SLW2, c->slow_cells, c->slow_verts, c->ctr + C_SLOW, c->ctr + C_ERR,
-                c->nsm, c->stream);
-#else
     cudaMemsetAsync(c->ctr + C_SLOW, 0, 2 * sizeof(int), c->stream); /* near-pure cells, their clip work */
     launch_sl32_flux(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf32, c->vf32, c->wf32, c->uf, c->vf, c->wf, c->planes,
                      c->band[c->bcur], c->list_sl, c->ctr + C_SL, c->flux, c->slow_cells, c->slow_verts,
                      c->ctr + C_SLOW, c->ctr + C_SLW2, c->ctr + C_ERR, c->nsm, c->stream);
-#endif
 }
 
 int st_transport(slvof_ctx* c, double dt)

@@ -21,7 +21,7 @@ constexpr int CLIP_MAX_LEAVES = 4096;            /* leaf budget of one top-level
 constexpr int CLIP_STACK32 = 8;                  /* FP32 clip nesting (pruned subtrees are shallow) */
 
 /* Error bits, same values as SLVOF_DEV_* in include/slvof.h. */
-enum : int { ERR_INDEX = 1, ERR_DEPTH = 2, ERR_NAN = 4, ERR_VOLUME = 8 };
+enum : int { ERR_INDEX = 1, ERR_DEPTH = 2, ERR_NAN = 4, ERR_VOLUME = 8, ERR_WAIT = 16 };
 
 __device__ __forceinline__ long cidx(const DevMesh& m, int i, int j, int k)
 {
@@ -158,6 +158,40 @@ __device__ __forceinline__ double compute_dist64(const DevMesh& m, int i, int j,
     double dist = alpha * norm;
     dist += (nx * cco(m, 0, i) + ny * cco(m, 1, j)) + nz * cco(m, 2, k);
     return dist;
+}
+
+/* Block-aggregated append of K items per thread: one atomic on the list counter per block
+ * instead of one per warp and item (band cells are a few percent of the grid, so with warp
+ * atomics thousands of warps queue on the one counter).  Every thread of the block calls it
+ * (it holds two __syncthreads); s holds NW * K + 1 ints of shared memory, NW the block's
+ * warps.  Items land in (warp, k) order within the block's run. */
+template <int K, int NW>
+__device__ __forceinline__ void block_append(const bool (&flag)[K], const int (&item)[K], int* list, int* count, int* s)
+{
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, w = tid >> 5;
+    unsigned bal[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+        bal[q] = __ballot_sync(0xffffffffu, flag[q]);
+        if (lane == 0) s[w * K + q] = __popc(bal[q]);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int run = 0;
+        for (int e = 0; e < NW * K; ++e) {
+            const int c = s[e];
+            s[e] = run;
+            run += c;
+        }
+        s[NW * K] = run > 0 ? atomicAdd(count, run) : 0;
+    }
+    __syncthreads();
+    const int base = s[NW * K];
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int q = 0; q < K; ++q)
+        if (flag[q]) list[base + s[w * K + q] + __popc(bal[q] & lt)] = item[q];
 }
 
 /* Warp-aggregated append of flagged items to a list. */

@@ -15,7 +15,7 @@ void launch_elvira_pure(const DevMesh& m, const double* VF, double* nx, double* 
                         long long* partials, cudaStream_t s);
 void launch_normal_ghost(const DevMesh& m, double* nx, double* ny, double* nz, int nsm, cudaStream_t s);
 void launch_mass_final(const long long* partials, long nblocks, double cellvol, double* out, cudaStream_t s);
-void launch_band_first(const DevMesh& m, const double* VF, short* bout, int nsm, cudaStream_t s);
+void launch_band_first(const DevMesh& m, const double* VF, short* bout, int* errw, int nsm, cudaStream_t s);
 void launch_band_ghost(const DevMesh& m, const short* bin, short* bout, bool neumann, int nsm, cudaStream_t s);
 void launch_band_sweep(const DevMesh& m, const short* bin, short* bout, int n, int nsm, cudaStream_t s);
 void launch_sl_classify(const DevMesh& m, const short* band, const double* VFin, double* VFout, int* list, int* count,
@@ -149,9 +149,5 @@ void launch_sl32_pre(const DevMesh& m, double dt, double* VFout, const float* uf
                      int* slow_cells, float4* slow_verts, int* slow_count, int* errw, int nsm, cudaStream_t s);
 void launch_sl32_clip(const DevMesh& m, double* VFout, const float4* planes, int* work2, const int* slow_cells,
                       const float4* slow_verts, const int* slow_count, int* errw, int nsm, cudaStream_t s);
-void launch_sl32(const DevMesh& m, double dt, double* VFout, const float* uf, const float* vf, const float* wf,
-                 const float4* planes, const signed char* phase, const int* list, const int* count, int* work,
-                 int* work2, int* slow_cells, float4* slow_verts, int* slow_count, int* errw,
-                 int nsm, cudaStream_t s);
 
 } // namespace slvof

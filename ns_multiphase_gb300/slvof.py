@@ -31,6 +31,12 @@ E_CUDA = -2
 E_UNSUPPORTED = -3
 E_NOMEM = -4
 E_TOO_LARGE = -5
+# device error bits (SLVOF_DEV_*), OR-ed into a positive status
+DEV_INDEX = 1
+DEV_DEPTH = 2
+DEV_NAN = 4
+DEV_VOLUME = 8
+DEV_WAIT = 16
 
 # (name, restype, argtypes) of every symbol declared in include/slvof.h
 _P, _I, _D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
@@ -107,7 +113,8 @@ def load_library(path: str = LIB_PATH):
 
 
 class DeviceError(RuntimeError):
-    """A kernel raised SLVOF_DEV_* bits (index range, clip depth, NaN distance, volume)."""
+    """A kernel raised SLVOF_DEV_* bits (index range, clip depth, NaN distance, volume, bounded
+    wait)."""
 
     def __init__(self, bits: int, msg: str):
         super().__init__(msg)

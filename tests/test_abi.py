@@ -111,5 +111,6 @@ def test_python_mirror_constants_match_the_header():
     hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "slvof.h")).read()
     defs = {k: int(v) for k, v in re.findall(r"#define SLVOF_(\w+) \(?(-?\d+)\)?", hdr)}
     for name in ("FP64", "MIXED", "STEP_BAND", "STEP_MASS", "STEP_DEFER", "OK", "E_ARG", "E_CUDA",
-                 "E_UNSUPPORTED", "E_NOMEM", "E_TOO_LARGE"):
+                 "E_UNSUPPORTED", "E_NOMEM", "E_TOO_LARGE", "DEV_INDEX", "DEV_DEPTH", "DEV_NAN", "DEV_VOLUME",
+                 "DEV_WAIT"):
         assert getattr(slvof, name) == defs[name], name
