@@ -920,6 +920,27 @@ __device__ __forceinline__ void face_decode(const DevMesh& m, unsigned code, int
     cell_of_index(m, (long)(code >> 2), hi, hj, hk);
 }
 
+/* Point id (0..3 corners, 5..8 their moved copies) of a 5_tets or 6_tets face, as face_points
+ * forms it (the same FP64 sum for a moved corner, so the same bits), rounded to FP32: a seed
+ * lane forms only the four points of its own tet. */
+__device__ __forceinline__ float4 seed_point(const DevMesh& m, const FluxBufs& F, int dir, int hi, int hj, int hk,
+                                             int id)
+{
+    int s, t;
+    flux::face_axes(dir, s, t);
+    const int p = id < 5 ? id : id - 5;
+    const float cs = (float)flux::corner_s(p), ct = (float)flux::corner_t(p);
+    const float b0 = dir == 0 ? 1.f : (s == 0 ? cs : ct);
+    const float b1 = dir == 1 ? 1.f : (s == 1 ? cs : ct);
+    const float b2 = dir == 2 ? 1.f : (s == 2 ? cs : ct);
+    if (id < 5) return make_float4(b0, b1, b2, 0.f);
+    int i, j, k;
+    flux::corner_node(dir, hi, hj, hk, p, i, j, k);
+    const long c = cidx(m, i, j, k);
+    return make_float4((float)((double)b0 + F.nd[0][c]), (float)((double)b1 + F.nd[1][c]),
+                       (float)((double)b2 + F.nd[2][c]), 0.f);
+}
+
 __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
 {
     const int n = *F.n_faces;
@@ -1172,8 +1193,6 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
             const int b = lane / ntet, n = lane - ntet * b;
             int dir, hi, hj, hk;
             face_decode(m, code, dir, hi, hj, hk);
-            double P[5][3], Q[5][3];
-            face_points(m, F, dir, hi, hj, hk, P, Q);
             int tri[4][3], sg[4];
             flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
             int q[4];
@@ -1185,9 +1204,17 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
             float4 v[4];
             int I[4][3];
             int mlo = 1 << 20;
+            if (m.tess == 24) {
+                double P[5][3], Q[5][3];
+                face_points(m, F, dir, hi, hj, hk, P, Q);
+                for (int nn = 0; nn < 4; ++nn) {
+                    const double* x = q[nn] < 5 ? P[q[nn]] : Q[q[nn] - 5];
+                    v[nn] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
+                }
+            } else {
+                for (int nn = 0; nn < 4; ++nn) v[nn] = seed_point(m, F, dir, hi, hj, hk, q[nn]);
+            }
             for (int nn = 0; nn < 4; ++nn) {
-                const double* x = q[nn] < 5 ? P[q[nn]] : Q[q[nn] - 5];
-                v[nn] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
                 if (q[nn] >= 5) {
                     I[nn][0] = idx32(v[nn].x, 0, rlo[0], rhi[0], err);
                     I[nn][1] = idx32(v[nn].y, 0, rlo[1], rhi[1], err);
@@ -1406,19 +1433,22 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
             size += tot_push + __popc(backmask);
             __syncwarp();
         }
-        /* per face: fixed-order shuffle tree, then the liquid rescaled to the FP64 volume */
+        /* per face: fixed-order float-float shuffle tree (no FP64 on the warp), then on the
+         * face's lane the liquid rescaled to the FP64 volume */
 #pragma unroll
         for (int b = 0; b < FCLIP_BATCH; ++b) {
             if (b >= nb) break;
-            double fl = (double)acc[b].hi + (double)acc[b].lo;
-            double u = (double)avol[b].hi + (double)avol[b].lo;
+            FF a = acc[b], vv = avol[b];
             int fg = flg[b];
             for (int off = 16; off > 0; off >>= 1) {
-                fl += __shfl_xor_sync(0xffffffffu, fl, off);
-                u += __shfl_xor_sync(0xffffffffu, u, off);
+                const FF oa{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)};
+                const FF ov{__shfl_xor_sync(0xffffffffu, vv.hi, off), __shfl_xor_sync(0xffffffffu, vv.lo, off)};
+                ff_add(a, oa);
+                ff_add(vv, ov);
                 fg |= __shfl_xor_sync(0xffffffffu, fg, off);
             }
             if (lane == b) {
+                const double fl = (double)a.hi + (double)a.lo, u = (double)vv.hi + (double)vv.lo;
                 double2* out = F.fvf[fd_] + (code_ >> 2);
                 const double V = out->x;
                 double wgt;

@@ -195,14 +195,69 @@ def check(cfg, count, fd_backend="cpu", precision="fp64", seed=7, also=(), sweep
 H_SWEEP = (1e-5, 1e-6, 1e-7)
 
 
+def sweep_entry(a, fds, others=None):
+    """One entry of a step sweep: the reverse pass's derivative `a` against central differences
+    `fds` (h -> value).  Its relative deviation at every h (the absolute one where the difference
+    is exactly zero), its best h, and whether the loss is smooth on the check's scale: the
+    differences at h = 1e-6 and 1e-7 agree to 1e-6 of |FD|.  Where they do not, a discrete
+    choice of the step (an ELVIRA candidate, a d2case sign, a band bit) switches within +-1e-6
+    of the input, and neither difference there is a derivative, or the differences at the
+    smaller steps are dominated by the loss's rounding (which grows as 1/h).  That rounding is
+    estimated for h = 1e-5 from the spread between h = 1e-6 and 1e-7, and the entry is also
+    judged against 1e-6 of |FD| plus that estimate.  `others` maps further precisions to their
+    reverse-pass derivatives."""
+    rel = {h: (abs(a - f) / abs(f) if f != 0 else None) for h, f in fds.items()}
+    cands = [h for h in H_SWEEP if rel[h] is not None]
+    best = min(cands, key=lambda h: rel[h]) if cands else None
+    f5, f6, f7 = fds[1e-5], fds[1e-6], fds[1e-7]
+    smooth = abs(f6 - f7) <= 1e-6 * max(abs(f6), abs(f7)) if (f6 != 0 or f7 != 0) else True
+    # rounding of the loss enters a central difference as 1/h: the spread between h = 1e-6 and
+    # 1e-7 (dominated by the smaller step's) scaled to h = 1e-5 estimates that difference's noise
+    noise5 = abs(f7 - f6) * 1e-2
+    e = {"adjoint": a, "fd": {str(h): f for h, f in fds.items()},
+         "rel_err": {str(h): r for h, r in rel.items()}, "abs_err": {str(h): abs(a - f) for h, f in fds.items()},
+         "best_h": best, "rel_err_best": rel[best] if best is not None else None,
+         "fd_zero": best is None, "smooth": bool(smooth),
+         "fd_noise_rel_h_1e-5": noise5 / abs(f5) if f5 != 0 else None,
+         "within_1e-6_plus_fd_noise_at_h_1e-5": bool(f5 != 0 and abs(a - f5) <= 1e-6 * abs(f5) + noise5)}
+    for pr, ap in (others or {}).items():
+        e["adjoint_" + pr] = ap
+        e["rel_err_best_" + pr] = abs(ap - fds[best]) / abs(fds[best]) if best is not None else None
+    return e
+
+
+def sweep_summary(entries, precisions=()):
+    """Counts over a sweep's entries: smooth ones, their worst relative deviation at their best
+    h, how many are within 1e-6, the not-smooth and zero-difference ones, and for each further
+    precision its worst deviation over the smooth entries.  The scale for zero differences is
+    the largest |FD| at h = 1e-6 of the check."""
+    scale = max(abs(e["fd"][str(1e-6)]) for e in entries)
+    sm = [e for e in entries if e["smooth"] and not e["fd_zero"]]
+    nz = [e for e in entries if not e["fd_zero"]]
+    out = {"checked": len(entries),
+           "within_1e-6_at_best_h": sum(1 for e in nz if e["rel_err_best"] <= 1e-6),
+           "within_1e-6_plus_fd_noise_at_h_1e-5": sum(1 for e in nz if e["within_1e-6_plus_fd_noise_at_h_1e-5"]),
+           "neither": [{"index": e["index"], "rel_err": e["rel_err"], "fd_noise_rel_h_1e-5": e["fd_noise_rel_h_1e-5"]}
+                       for e in nz if e["rel_err_best"] > 1e-6 and not e["within_1e-6_plus_fd_noise_at_h_1e-5"]],
+           "smooth_entries": len(sm),
+           "max_rel_err_best_smooth": max((e["rel_err_best"] for e in sm), default=None),
+           "smooth_entries_within_1e-6": sum(1 for e in sm if e["rel_err_best"] <= 1e-6),
+           "not_smooth": [{"index": e["index"], "rel_err_best": e["rel_err_best"], "best_h": e["best_h"]}
+                          for e in entries if not e["smooth"]],
+           "fd_zero": [{"index": e["index"], "adjoint": e["adjoint"],
+                        "abs_adjoint_over_max_fd": abs(e["adjoint"]) / scale if scale > 0 else None}
+                       for e in entries if e["fd_zero"]],
+           "max_fd_h_1e-6": scale}
+    for pr in precisions:
+        out["max_rel_err_best_smooth_" + pr] = max((e["rel_err_best_" + pr] for e in sm
+                                                    if e.get("rel_err_best_" + pr) is not None), default=None)
+    return out
+
+
 def check_sweep(cfg, count, fd_backend="gpu", precision="fp64", seed=7, also=()):
     """Per-entry check with a step sweep: central differences at h = 1e-5, 1e-6 and 1e-7 for
-    every entry, each entry's relative deviation |adj - FD| / |FD| at every h, and its best h.
-    An entry is smooth when the differences at its two largest steps agree to 1e-6 of |FD| (the
-    loss is then differentiable on that scale and the remaining deviation is the reverse pass's
-    or the differences' rounding); otherwise a discrete choice of the step switches within +-h
-    and the entry is listed as not smooth.  `also` lists further forward precisions whose
-    reverse-pass gradients are reported on the same entries."""
+    every entry (sweep_entry), summarised by sweep_summary.  `also` lists further forward
+    precisions whose reverse-pass gradients are reported on the same entries."""
     evaluate = rollout_cpu if fd_backend == "cpu" else rollout_gpu
     cfg.target = evaluate(cfg, np.zeros_like(cfg.p0))
     L, G, times = gradient(cfg, precision)
@@ -222,32 +277,40 @@ def check_sweep(cfg, count, fd_backend="gpu", precision="fp64", seed=7, also=())
     t0 = time.perf_counter()
     entries = []
     for idx in picks:
-        a = float(G[idx])
-        fds = {h: fd_at(idx, h) for h in H_SWEEP}
-        rel = {h: abs(a - f) / abs(f) if f != 0 else None for h, f in fds.items()}
-        best = min((h for h in H_SWEEP if rel[h] is not None), key=lambda h: rel[h])
-        smooth = abs(fds[H_SWEEP[0]] - fds[H_SWEEP[1]]) <= 1e-6 * abs(fds[H_SWEEP[1]])
-        e = {"index": [int(x) for x in idx], "adjoint": a, "fd": {str(h): f for h, f in fds.items()},
-             "rel_err": {str(h): r for h, r in rel.items()}, "best_h": best, "rel_err_best": rel[best],
-             "smooth": bool(smooth)}
-        for pr, (Lp, Gp, tp) in others.items():
-            ap = float(Gp[idx])
-            e["adjoint_" + pr] = ap
-            e["rel_err_best_" + pr] = abs(ap - fds[best]) / abs(fds[best]) if fds[best] != 0 else None
-        entries.append(e)
-    sm = [e for e in entries if e["smooth"]]
-    return {"config": cfg.name, "grid": list(cfg.mesh.cell_shape), "steps": cfg.steps,
-            "checkpoint_every": cfg.every, "precision_forward": precision, "fd_backend": fd_backend,
-            "h_sweep": list(H_SWEEP), "loss": L, "params": int(cfg.p0.size), "support": int(len(support)),
-            "checked": len(entries), "smooth_entries": len(sm),
-            "max_rel_err_best_smooth": max((e["rel_err_best"] for e in sm), default=None),
-            "smooth_entries_within_1e-6": sum(1 for e in sm if e["rel_err_best"] <= 1e-6),
-            "not_smooth": [e["index"] for e in entries if not e["smooth"]],
-            "fd_seconds": time.perf_counter() - t0, "timings": times,
-            "also": {pr: {"loss": Lp, "rel_l2_vs_" + precision: float(np.linalg.norm(Gp - G) / np.linalg.norm(G)),
-                          "max_rel_err_best_smooth": max((e["rel_err_best_" + pr] for e in sm), default=None),
-                          "timings": tp} for pr, (Lp, Gp, tp) in others.items()},
-            "entries": entries}
+        e = sweep_entry(float(G[idx]), {h: fd_at(idx, h) for h in H_SWEEP},
+                        {pr: float(Gp[idx]) for pr, (Lp, Gp, tp) in others.items()})
+        entries.append({"index": [int(x) for x in idx], **e})
+    out = {"config": cfg.name, "grid": list(cfg.mesh.cell_shape), "steps": cfg.steps,
+           "checkpoint_every": cfg.every, "precision_forward": precision, "fd_backend": fd_backend,
+           "h_sweep": list(H_SWEEP), "loss": L, "params": int(cfg.p0.size), "support": int(len(support)),
+           **sweep_summary(entries, tuple(others)),
+           "fd_seconds": time.perf_counter() - t0, "timings": times,
+           "also": {pr: {"loss": Lp, "rel_l2_vs_" + precision: float(np.linalg.norm(Gp - G) / np.linalg.norm(G)),
+                         "timings": tp} for pr, (Lp, Gp, tp) in others.items()},
+           "entries": entries}
+    return out
+
+
+def resummarize(path):
+    """A saved sweep's entries re-evaluated by sweep_entry and sweep_summary (the differences
+    and derivatives themselves are kept)."""
+    d = json.load(open(path))
+    prs = tuple(d.get("also", {}))
+    entries = []
+    for e in d["entries"]:
+        fds = {h: e["fd"][str(h)] for h in H_SWEEP}
+        entries.append({"index": e["index"], **sweep_entry(e["adjoint"], fds,
+                                                           {pr: e["adjoint_" + pr] for pr in prs})})
+    for k in ("checked", "smooth_entries", "max_rel_err_best_smooth", "smooth_entries_within_1e-6", "not_smooth",
+              "fd_zero", "max_fd_h_1e-6", "within_1e-6_at_best_h", "within_1e-6_plus_fd_noise_at_h_1e-5", "neither"):
+        d.pop(k, None)
+    for pr in prs:
+        d.pop("max_rel_err_best_smooth_" + pr, None)
+        d.get("also", {}).get(pr, {}).pop("max_rel_err_best_smooth", None)
+    ent = d.pop("entries")
+    d.update(sweep_summary(entries, prs))
+    d["entries"] = entries
+    return d
 
 
 def save_gradient(cfg, path, precision="fp64"):
@@ -314,10 +377,19 @@ def main():
     ap.add_argument("--h-sweep", action="store_true",
                     help="per-entry relative deviations at h = 1e-5, 1e-6, 1e-7 (check_sweep)")
     ap.add_argument("--out", metavar="FILE", help="also write the JSON result to FILE")
+    ap.add_argument("--resummarize", metavar="FILE",
+                    help="re-evaluate a saved --h-sweep result's per-entry verdicts and summary (no GPU)")
     ap.add_argument("--save-gradient", metavar="FILE", help="save the reverse pass's gradient (GPU) and stop")
     ap.add_argument("--forward-mode", metavar="FILE",
                     help="check a saved gradient against forward-mode derivatives of the restatement (2d, CPU)")
     a = ap.parse_args()
+    if a.resummarize:
+        out = resummarize(a.resummarize)
+        with open(a.out or a.resummarize, "w") as fh:
+            json.dump(out, fh, indent=1)
+            fh.write("\n")
+        print(json.dumps({k: v for k, v in out.items() if k not in ("entries", "timings")}))
+        return
     if a.save_gradient or a.forward_mode:
         cfg = config2d(N=a.n or 256, steps=a.steps or 40, every=a.every) if a.config == "2d" else \
             config3d(N=a.n or 128, steps=a.steps or 30, every=a.every)
