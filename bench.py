@@ -641,8 +641,10 @@ def main():
                 "frac": achieved / hbm, "traffic": profiled_traffic(dom),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
                 "algorithmic_bytes": alg, "kernel_ms": stage[dom],
-                "note": "sl_update = k_sl32_pre + k_sl32_clipw; branch- and latency-bound (see profiles/), "
-                        "the HBM fraction is reported per the contract",
+                "note": "sl_update = k_flux_lists + k_flux_nodes + k_flux_faces + k_flux_clip + k_flux_cells + "
+                        "k_sl32_clipw (the flux form); issue-, latency- and FP64-bound, not HBM-bound "
+                        "(profiles/sl_update_256_mixed_dram.txt, profiles/k_flux_clip_128_mixed_ncu.txt); the HBM "
+                        "fraction is reported per the contract",
                 "step": {"algorithmic_bytes": 28 * cells, "achieved_gbs": 28 * cells / (ms_step / 1e3) / 1e9,
                          "frac": 28 * cells / (ms_step / 1e3) / 1e9 / hbm}}
         if ops is not None:
@@ -714,7 +716,7 @@ def algorithmic_bytes(m, stage, ctr):
 
 def profiled_traffic(stage):
     """dram read+write bytes per launch from the committed ncu summary, if present."""
-    path = os.path.join(ROOT, "profiles", "slvof_256_mixed_ncu.txt")
+    path = os.path.join(ROOT, "profiles", "sl_update_256_mixed_dram.txt")
     try:
         for line in open(path):
             parts = line.split()
@@ -726,9 +728,10 @@ def profiled_traffic(stage):
 
 
 def launches_per_step(m):
-    # classify, SL, VF ghost, ELVIRA pure, ELVIRA candidates, normal ghost, PLIC,
-    # band (first + ghost + nband*(sweep + ghost)), mass final
-    return 7 + 2 + 2 * int(m.nband) + 1
+    # mixed step: classify; SL update (flux lists, nodes, faces, clip, cells, near-pure cells);
+    # VF ghost; ELVIRA pure; ELVIRA candidates (FP32 scoring, FP64 arbitration, FP64 winner);
+    # normal ghost; PLIC (pure, Newton); band (first + ghost + nband*(sweep + ghost)); mass final
+    return 1 + 6 + 1 + 1 + 3 + 1 + 2 + 2 + 2 * int(m.nband) + 1
 
 
 if __name__ == "__main__":

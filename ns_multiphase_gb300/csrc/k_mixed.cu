@@ -1347,9 +1347,8 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
 #pragma unroll 1
                 for (int nn = 0; nn < nvert; ++nn) {
 #else
-#pragma unroll
-                for (int nn = 0; nn < 4; ++nn) {
-                    if (nn >= nvert) break;
+#pragma unroll 1 /* rolled: a smaller loop body (the kernel is instruction-fetch bound) */
+                for (int nn = 0; nn < nvert; ++nn) {
 #endif
                     const int e1 = C.v1[nn], e2 = C.v2[nn];
                     const float4 A = S.scr[e1][tid], Bv = S.scr[e2][tid];
@@ -1369,7 +1368,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
 #if SLVOF_FCLIP_ROLL
                             const int Iv = idx32(u, unpack(wbits(S.scr[nn][tid]), q), rlo[q], rhi[q], err);
 #else
-                            const int Iv = idx32(u, unpack(s1p[nn], q), rlo[q], rhi[q], err);
+                            const int Iv = idx32(u, unpack(wbits(S.scr[nn][tid]), q), rlo[q], rhi[q], err);
 #endif
                             const int a1 = unpack(pa, q), a2 = unpack(pb, q);
                             nv[q] = min(max(Iv, min(a1, a2)), max(a1, a2));

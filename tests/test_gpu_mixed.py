@@ -8,9 +8,9 @@ the FP64 path's in at least 99.5% of interface cells.  Over short deformation ru
 must stay within 5e-3 of the FP64 path, and 99% of the interface cells within 1e-5 except for
 the sphere centred at (0.35,0.35,0.35): on a uniform grid its three mirror planes hold exact
 FP64 ties between mirror candidates, which the ~1e-7 VF differences of the FP32 transport can
-break the other way.  The total volume must agree within
-1e-6 * cell volume * sqrt(steps * interface cells) (FP32 vertex positions carry ~1e-7 of a
-cell, with independent signs from cell to cell).
+break the other way.  The total volume must agree within a relative bound per case, a few
+times the measured difference (2e-10 to 1e-8 over 10 steps on these small grids), and on the
+benchmark's own 200-sphere state at 128^3 within the metric's 1e-10 after 64 steps.
 """
 import numpy as np
 import pytest
@@ -122,7 +122,11 @@ def test_mixed_tracks_fp64(shape):
     iface = (V64 >= 1e-10) & (V64 <= 1 - 1e-10)
     print(f"{shape}: mass rel diff {abs(M32 - M64) / M64:.3e}, p99 {np.percentile(d[iface], 99):.3e}, "
           f"max {d.max():.3e}")
-    assert abs(M32 - M64) <= 1e-6 * cv * np.sqrt(n_if), (M32, M64, abs(M32 - M64) / M64)
+    # measured 4.5e-10 (one sphere of radius 4.8 cells), 2.8e-11 (twelve spheres), 2.3e-9 (2D,
+    # 48^2): small grids hold few interface cells per unit of mass, so their relative drift is
+    # larger than the 256^3 benchmark's 1e-11 level
+    bound = {"sphere3d": 2e-9, "spheres3d": 2e-10, "vortex2d": 1e-8}[shape]
+    assert abs(M32 - M64) <= bound * M64, (M32, M64, abs(M32 - M64) / M64)
     if shape != "sphere3d":
         assert float(np.percentile(d[iface], 99)) <= 1e-5, float(np.percentile(d[iface], 99))
     assert float(d.max()) <= 5e-3, float(d.max())
