@@ -787,34 +787,6 @@ SLVOF_HD_CALL void project_reverse_call(const DevMesh& m, const Vel& V, const Ve
     project_reverse(m, V, G, p0, i, j, k, dt, gp);
 }
 
-/* Node n of the flux volume of face `dir` at the low side of cell (fi, fj, fk) (SLfluxVol,
- * src/VFgeom.jl:428-509): its grid node's offsets from that cell, and whether it is projected.
- * Along the face normal each node pair holds the projected node first in even cells and
- * second in odd ones (oddEvenCell mirrors x). */
-SLVOF_HD bool flux_node(int dir, bool even, int n, int off[3])
-{
-    const int b0 = n & 1, b1 = (n >> 1) & 1, b2 = (n >> 2) & 1;
-    if (dir == 0) {
-        off[0] = 0; off[1] = b1; off[2] = b2;
-        return even ? b0 == 0 : b0 == 1;
-    }
-    off[0] = even ? b0 : 1 - b0;
-    if (dir == 1) {
-        off[1] = 0; off[2] = b2;
-        return b1 == 0;
-    }
-    off[1] = b1; off[2] = 0;
-    return b2 == 0;
-}
-
-/* Corner q of the face quad a, b, c, d (the projected nodes, src/VFgeom.jl:590-646). */
-SLVOF_HD int flux_quad(int dir, bool even, int q)
-{
-    if (dir == 0) return even ? (q == 0 ? 4 : (q == 1 ? 6 : (q == 2 ? 2 : 0))) : (q == 0 ? 7 : (q == 1 ? 5 : (q == 2 ? 1 : 3)));
-    if (dir == 1) return q == 0 ? 1 : (q == 1 ? 5 : (q == 2 ? 4 : 0));
-    return q == 0 ? 1 : (q == 1 ? 0 : (q == 2 ? 2 : 3));
-}
-
 /* One face's flux volume, target volume and apex, as the forward builds them. */
 struct CorrFace {
     double fv[8][3]; /* flux-volume nodes */

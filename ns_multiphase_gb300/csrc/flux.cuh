@@ -114,5 +114,51 @@ SLVOF_HD void corner_node(int dir, int hi, int hj, int hk, int p, int& i, int& j
     i = n[0]; j = n[1]; k = n[2];
 }
 
+/* add_correction_tets (src/VFgeom.jl:514-664; pressure_scheme "finite-difference", 5_tets) of one
+ * face, on the flux form's traced nodes, in cell units and the low cell's frame.  The face's
+ * flux volume (SLfluxVol, src/VFgeom.jl:428-509: the hexahedron between the face and its
+ * projection, split by the five-tet pattern of the face's cell) and the finite-difference
+ * volume dt * u_face / d give the volume that the tets (a, b, d, e) and (b, c, d, e) over the
+ * projected quad must add; the apex e moves from the quad's mean along the face normal until
+ * they do (the two volumes are affine in e).  A band cell adds these tets with its own parity
+ * sign, and the two cells of a face have opposite parities, so like the swept prism they are a
+ * face quantity: the result is the tets' FP64 volume signed for the low cell, and e. */
+SLVOF_HD double face_correction(int dir, int hi, int hj, int hk, double dtu, const double (*P)[3], const double (*Q)[3],
+                                double* e)
+{
+    int s, t;
+    face_axes(dir, s, t);
+    const bool ev = tess_even(5, hi, hj, hk);
+    double fv[8][3];
+    for (int n = 0; n < 8; ++n) {
+        int off[3];
+        const bool proj = flux_node(dir, ev, n, off);
+        const int p = off[s] + 2 * off[t]; /* the corner at (s, t) offsets: PA, PB, PD, PC */
+        for (int q = 0; q < 3; ++q) fv[n][q] = proj ? Q[p][q] : P[p][q];
+    }
+    auto tv = [](const double* a, const double* b, const double* c, const double* d) {
+        /* tet_vol, src/VFgeom.jl:669-681, in the reference's expansion order */
+        const double a1 = a[0] - d[0], a2 = a[1] - d[1], a3 = a[2] - d[2];
+        const double b1 = b[0] - d[0], b2 = b[1] - d[1], b3 = b[2] - d[2];
+        const double c1 = c[0] - d[0], c2 = c[1] - d[1], c3 = c[2] - d[2];
+        return (-1.0 / 6.0) * ((a1 * (b2 * c3 - c2 * b3) - a2 * (b1 * c3 - c1 * b3)) + a3 * (b1 * c2 - c1 * b2));
+    };
+    double flux = 0.0;
+    for (int q = 0; q < 5; ++q) flux += tv(fv[tet5(q, 0)], fv[tet5(q, 1)], fv[tet5(q, 2)], fv[tet5(q, 3)]);
+    if (!ev) flux = -flux;
+    const double vol = ev ? (dtu - flux) : -(dtu - flux);
+    const double *a = fv[flux_quad(dir, ev, 0)], *b = fv[flux_quad(dir, ev, 1)], *c = fv[flux_quad(dir, ev, 2)],
+                 *d = fv[flux_quad(dir, ev, 3)];
+    for (int q = 0; q < 3; ++q) e[q] = 0.25 * (((a[q] + b[q]) + c[q]) + d[q]);
+    const double v0 = tv(a, b, d, e) + tv(b, c, d, e);
+    const int p1 = (dir + 1) % 3, p2 = (dir + 2) % 3;
+    const double N = (((a[p1] * b[p2] - a[p2] * b[p1]) + (d[p1] * a[p2] - d[p2] * a[p1])) +
+                      (b[p1] * c[p2] - b[p2] * c[p1])) +
+                     (c[p1] * d[p2] - c[p2] * d[p1]);
+    e[dir] += 6.0 * (vol - v0) / N;
+    const double vt = tv(a, b, d, e) + tv(b, c, d, e);
+    return ev ? -vt : vt; /* the low cell's parity is the opposite of the face's cell's */
+}
+
 } // namespace flux
 } // namespace slvof

@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
     for (;;) {
         int base = 0;
         /* cells per batch: every tet of the batch is seeded in one round (<= 32 lanes) */
-        const int B = m.tess == 24 ? 1 : CLIPW_BATCH;
+        const int B = (m.tess == 24 || m.fd) ? 1 : CLIPW_BATCH;
         if (lane == 0) base = atomicAdd(work, B);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n_cells) break;
@@ -494,12 +494,35 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32) k_sl32_clipw(DevMesh m, doub
         FF acc[CLIPW_BATCH], avol[CLIPW_BATCH];
 #pragma unroll
         for (int b = 0; b < CLIPW_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; }
-        const int ntet = tess_ntets(m.tess), stride = m.tess == 24 ? 16 : 8;
+        /* under pressure_scheme "finite-difference" (5_tets, one cell a batch) lanes 5..16 seed
+         * the twelve correction tets: (a, b, d, e) and (b, c, d, e) of each face, a..d its
+         * projected corners (four of the cell's eight) and e its apex; a cell's liquid and volume
+         * both carry its parity sign, which cancels in their ratio, as the cell tets' mirrored
+         * corners do */
+        const int ntet = tess_ntets(m.tess) + (m.fd ? 12 : 0), stride = (m.tess == 24 || m.fd) ? 16 : 8;
+        const int ci0 = __shfl_sync(0xffffffffu, ci_, 0), cj0 = __shfl_sync(0xffffffffu, cj_, 0),
+                  ck0 = __shfl_sync(0xffffffffu, ck_, 0); /* the batch's cell when it holds one */
         if (lane < ntet * nb) {
             const int b = lane / ntet, t = lane - ntet * b;
+            int vid[4];
+            if (t < 5 || m.tess != 5 || !m.fd) {
+                for (int n = 0; n < 4; ++n) vid[n] = tess_tet(m.tess, t, n);
+            } else {
+                const int f = (t - 5) >> 1, hh = (t - 5) & 1, dir = f >> 1, up = f & 1;
+                const bool ev_c = tess_even(5, ci0, cj0, ck0);
+                const bool ev_h = up ? !ev_c : ev_c; /* the face's cell h = c + up e_dir */
+                const int qn[3] = {flux_quad(dir, ev_h, hh), flux_quad(dir, ev_h, hh + 1), flux_quad(dir, ev_h, 3)};
+                for (int r = 0; r < 3; ++r) {
+                    int off[3];
+                    flux_node(dir, ev_h, qn[r], off);
+                    off[dir] += up; /* from h to the cell */
+                    vid[r] = (ev_c ? off[0] : 1 - off[0]) + 2 * off[1] + 4 * off[2];
+                }
+                vid[3] = 8 + f;
+            }
 #pragma unroll
             for (int n = 0; n < 4; ++n) {
-                float4 q = __ldg(slow_verts + (long)(base + b) * stride + tess_tet(m.tess, t, n));
+                float4 q = __ldg(slow_verts + (long)(base + b) * stride + vid[n]);
                 if (n == 0) q.w = __int_as_float((int)(wbits(q) | ((unsigned)b << 24)));
                 S.stk[w][n][lane] = q;
             }
@@ -751,6 +774,8 @@ struct FluxBufs {
     unsigned* nodes;  /* owned nodes: cell index of the node */
     unsigned* faces;  /* owned faces: (cell index of h) << 2 | dir */
     unsigned* clip;   /* faces for the clip */
+    float4* fapex[3]; /* pressure_scheme "finite-difference": each face's correction apex (the low
+                       * cell's frame), by direction and the high cell's index */
     int* n_nodes;
     int* n_faces;
     int* n_clip;
@@ -942,7 +967,8 @@ __device__ __forceinline__ float4 seed_point(const DevMesh& m, const FluxBufs& F
                        (float)((double)b2 + F.nd[2][c]), 0.f);
 }
 
-__global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
+__global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 PL, FluxBufs F, double dt, Vel64c U,
+                                                             int* errw)
 {
     const int n = *F.n_faces;
     int err = 0;
@@ -950,6 +976,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
         const int t = base + threadIdx.x;
         bool clip = false;
         unsigned code = 0;
+        float4 cap = make_float4(0.f, 0.f, 0.f, 0.f);
         if (t < n) {
             code = F.faces[t];
             int dir, hi, hj, hk;
@@ -958,7 +985,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
             face_points(m, F, dir, hi, hj, hk, P, Q);
             const int npt = m.tess == 24 ? 5 : 4;
             const long hc = (long)(code >> 2);
-            bool flat = true;
+            bool flat = !m.fd; /* with the correction tets every face carries volume */
             for (int p = 0; p < npt; ++p) flat = flat && Q[p][dir] == 1.0;
             if (flat) {
                 F.fvf[dir][hc] = make_double2(0.0, 0.0); /* no motion across the face: a flat prism */
@@ -1004,7 +1031,12 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
                     six += dot(da, t);
                     V6 += sg[tr] > 0 ? six : -six;
                 }
-                const double V = V6 / 6.0;
+                double V = V6 / 6.0;
+                double ape[3] = {0.0, 0.0, 0.0};
+                if (m.fd) {
+                    const double* u = dir == 0 ? U.uf : (dir == 1 ? U.vf : U.wf);
+                    V += flux::face_correction(dir, hi, hj, hk, dt * (u[hc] * U.id[dir]), P, Q, ape);
+                }
                 /* index box of the prism points, relative to the low cell l = h - e_dir */
                 int li = hi, lj = hj, lk = hk;
                 if (dir == 0) --li; else if (dir == 1) --lj; else --lk;
@@ -1027,14 +1059,28 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
                  * layers 0 and 1) and its moved points */
                 lo[dir] = min(lo[dir], 1);
                 hiB[dir] = max(hiB[dir], 0);
+                if (m.fd) {
+                    /* the correction tets span the moved corners and the apex */
+                    px[8] = (float)ape[0]; py[8] = (float)ape[1]; pz[8] = (float)ape[2];
+                    cap = make_float4(px[8], py[8], pz[8], 0.f);
+                    const float u[3] = {px[8], py[8], pz[8]};
+                    for (int q = 0; q < 3; ++q) {
+                        const int I = idx32(u[q], 0, rlo[q], rhi[q], err);
+                        lo[q] = min(lo[q], I);
+                        hiB[q] = max(hiB[q], I);
+                    }
+                }
                 int side = 0;
                 if (m.fast_pure) {
                     side = npt == 5 ? box_plane_side<10>(m, PL, li, lj, lk, lo[0], hiB[0], lo[1], hiB[1], lo[2], hiB[2],
                                                          px, py, pz)
+                         : m.fd     ? box_plane_side<9>(m, PL, li, lj, lk, lo[0], hiB[0], lo[1], hiB[1], lo[2], hiB[2],
+                                                        px, py, pz)
                                     : box_plane_side<8>(m, PL, li, lj, lk, lo[0], hiB[0], lo[1], hiB[1], lo[2], hiB[2],
                                                         px, py, pz);
                 }
                 F.fvf[dir][hc] = make_double2(V, side > 0 ? V : 0.0);
+                if (m.fd) F.fapex[dir][hc] = cap;
                 clip = side == 0;
             }
         }
@@ -1045,6 +1091,7 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_faces(DevMesh m, Plane32 
 }
 
 constexpr int FCLIP_BATCH = 5; /* faces per warp batch: 30 seed tets for 5_tets and 6_tets */
+constexpr int CAPEX = 10;      /* seed point id of a face's correction apex */
 constexpr int FCLIP_CAP = 120; /* stack nodes per warp: keeps the block at 55.3 KB, four per SM */
 
 __device__ __forceinline__ void facc_add(FF* acc, int b, float x)
@@ -1076,55 +1123,6 @@ struct FluxShared {
 
 enum : int { PIECE_LIQ = 1, PIECE_GAS = 2 };
 
-#if SLVOF_FCLIP_COLD
-/* Seed tet n of face b of a batch: the prism tet oriented for the low cell, its vertices'
- * cell indices, the face's batch slot in vertex 0's tag; written to stk[0..3] (the lane's
- * column of the warp's node stack).  Out of line: it runs once per batch. */
-__device__ __noinline__ void flux_seed(const DevMesh& m, const FluxBufs F, unsigned code, int b, int n,
-                                       float4* stk0, float4* stk1, float4* stk2, float4* stk3, int& err)
-{
-    float4* stk[4] = {stk0, stk1, stk2, stk3};
-                int dir, hi, hj, hk;
-        face_decode(m, code, dir, hi, hj, hk);
-        double P[5][3], Q[5][3];
-        face_points(m, F, dir, hi, hj, hk, P, Q);
-        int tri[4][3], sg[4];
-        flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
-        int q[4];
-        flux::prism_tet(tri[n / 3], n % 3, q);
-        if (sg[n / 3] < 0) { const int x = q[0]; q[0] = q[1]; q[1] = x; }
-        const int li = hi - (dir == 0), lj = hj - (dir == 1), lk = hk - (dir == 2);
-        int rlo[3], rhi[3];
-        rel_bounds(m, li, lj, lk, rlo, rhi);
-        float4 v[4];
-        int I[4][3];
-        int mlo = 1 << 20;
-        for (int nn = 0; nn < 4; ++nn) {
-            const double* x = q[nn] < 5 ? P[q[nn]] : Q[q[nn] - 5];
-            v[nn] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
-            if (q[nn] >= 5) {
-                I[nn][0] = idx32(v[nn].x, 0, rlo[0], rhi[0], err);
-                I[nn][1] = idx32(v[nn].y, 0, rlo[1], rhi[1], err);
-                I[nn][2] = idx32(v[nn].z, 0, rlo[2], rhi[2], err);
-                mlo = min(mlo, I[nn][dir]);
-            }
-        }
-        /* the face's own points lie on the plane between l (0) and h (1) and inside the
-         * tangential range of l's column: index 0 across, and along dir the side of this
-         * tet's moved points (either index contains them) */
-        for (int nn = 0; nn < 4; ++nn)
-            if (q[nn] < 5) {
-                I[nn][0] = I[nn][1] = I[nn][2] = 0;
-                I[nn][dir] = mlo >= 1 ? 1 : 0;
-            }
-        for (int nn = 0; nn < 4; ++nn) {
-            unsigned pk = pack3(I[nn][0], I[nn][1], I[nn][2]);
-            if (nn == 0) pk |= (unsigned)b << 24;
-            v[nn].w = __int_as_float((int)pk);
-            *stk[nn] = v[nn];
-        }
-}
-#endif
 
 __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
 {
@@ -1136,8 +1134,10 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
     const unsigned lanemask_lt = (1u << lane) - 1u;
     const int n_faces = *F.n_clip;
-    const int ntet = m.tess == 24 ? 12 : 6; /* prism tets per face */
-    const int B = m.tess == 24 ? 2 : FCLIP_BATCH;
+    /* seed tets per face: the prism's, and under pressure_scheme "finite-difference" (5_tets)
+     * the two correction tets */
+    const int ntet = m.tess == 24 ? 12 : (m.fd ? 8 : 6);
+    const int B = m.tess == 24 ? 2 : (m.fd ? 4 : FCLIP_BATCH);
     int err = 0;
     for (;;) {
         int base = 0;
@@ -1187,22 +1187,33 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
 #pragma unroll
         for (int b = 0; b < FCLIP_BATCH; ++b) { acc[b] = FF{0.f, 0.f}; avol[b] = FF{0.f, 0.f}; flg[b] = 0; }
         const unsigned code = __shfl_sync(0xffffffffu, code_, min(lane / ntet, FCLIP_BATCH - 1));
-#if SLVOF_FCLIP_COLD
-        if (lane < ntet * nb) {
-            const int b = lane / ntet, n = lane - ntet * b;
-            flux_seed(m, F, code, b, n, &S.stk[w][0][lane], &S.stk[w][1][lane], &S.stk[w][2][lane],
-                      &S.stk[w][3][lane], err);
-        }
-#else
         if (lane < ntet * nb) {
             const int b = lane / ntet, n = lane - ntet * b;
             int dir, hi, hj, hk;
             face_decode(m, code, dir, hi, hj, hk);
-            int tri[4][3], sg[4];
-            flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
             int q[4];
-            flux::prism_tet(tri[n / 3], n % 3, q);
-            if (sg[n / 3] < 0) { const int x = q[0]; q[0] = q[1]; q[1] = x; }
+            if (n < 6 || m.tess == 24) {
+                int tri[4][3], sg[4];
+                flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
+                flux::prism_tet(tri[n / 3], n % 3, q);
+                if (sg[n / 3] < 0) { const int x = q[0]; q[0] = q[1]; q[1] = x; }
+            } else {
+                /* correction tet n - 6: (a, b, d, e) or (b, c, d, e) over the projected quad
+                 * (moved corners), e the apex (id CAPEX); with the low cell's parity sign, so
+                 * swapped where the face's cell is even */
+                int s_, t_;
+                flux::face_axes(dir, s_, t_);
+                const bool ev = tess_even(5, hi, hj, hk);
+                const int h = n - 6;
+                const int qn[3] = {flux_quad(dir, ev, h), flux_quad(dir, ev, h + 1), flux_quad(dir, ev, 3)};
+                for (int r = 0; r < 3; ++r) {
+                    int off[3];
+                    flux_node(dir, ev, qn[r], off);
+                    q[r] = off[s_] + 2 * off[t_] + flux::MOVED;
+                }
+                q[3] = CAPEX;
+                if (ev) { const int x = q[0]; q[0] = q[1]; q[1] = x; }
+            }
             const int li = hi - (dir == 0), lj = hj - (dir == 1), lk = hk - (dir == 2);
             int rlo[3], rhi[3];
             rel_bounds(m, li, lj, lk, rlo, rhi);
@@ -1217,7 +1228,14 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                     v[nn] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.f);
                 }
             } else {
-                for (int nn = 0; nn < 4; ++nn) v[nn] = seed_point(m, F, dir, hi, hj, hk, q[nn]);
+                for (int nn = 0; nn < 4; ++nn) {
+                    if (q[nn] == CAPEX) {
+                        const float4 e = F.fapex[dir][(long)(code >> 2)];
+                        v[nn] = make_float4(e.x, e.y, e.z, 0.f);
+                    } else {
+                        v[nn] = seed_point(m, F, dir, hi, hj, hk, q[nn]);
+                    }
+                }
             }
             for (int nn = 0; nn < 4; ++nn) {
                 if (q[nn] >= 5) {
@@ -1242,7 +1260,6 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                 S.stk[w][nn][lane] = v[nn];
             }
         }
-#endif
         int size = ntet * nb;
         __syncwarp();
         int guard = 0;
@@ -1348,13 +1365,8 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                     S.scr[nn][tid] = make_float4(v[nn].x, v[nn].y, v[nn].z, __int_as_float((int)s1p[nn]));
                 }
                 const int nvert = C.nvert;
-#if SLVOF_FCLIP_ROLL
-#pragma unroll 1
-                for (int nn = 0; nn < nvert; ++nn) {
-#else
 #pragma unroll 1 /* rolled: a smaller loop body (the kernel is instruction-fetch bound) */
                 for (int nn = 0; nn < nvert; ++nn) {
-#endif
                     const int e1 = C.v1[nn], e2 = C.v2[nn];
                     const float4 A = S.scr[e1][tid], Bv = S.scr[e2][tid];
                     const float da = sel4(d0, d1, d2, d3, e1), db = sel4(d0, d1, d2, d3, e2);
@@ -1370,11 +1382,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
 #pragma unroll
                         for (int q = 0; q < 3; ++q) {
                             const float u = q == 0 ? x : (q == 1 ? y : z);
-#if SLVOF_FCLIP_ROLL
                             const int Iv = idx32(u, unpack(wbits(S.scr[nn][tid]), q), rlo[q], rhi[q], err);
-#else
-                            const int Iv = idx32(u, unpack(wbits(S.scr[nn][tid]), q), rlo[q], rhi[q], err);
-#endif
                             const int a1 = unpack(pa, q), a2 = unpack(pb, q);
                             nv[q] = min(max(Iv, min(a1, a2)), max(a1, a2));
                         }
@@ -1512,8 +1520,10 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const do
         double r = liq / vol;
         int rlo[3], rhi[3];
         rel_bounds(m, i, j, k, rlo, rhi);
+        /* with correction tets (pressure_scheme "finite-difference") the pre-image also reaches
+         * the six faces' apexes (stored in each face's low cell's frame) */
         if (m.fast_pure && vol > 0.25 && vol < 4.0) {
-            float px[8], py[8], pz[8];
+            float px[14], py[14], pz[14];
             int lo[3] = {1 << 20, 1 << 20, 1 << 20}, hi[3] = {-(1 << 20), -(1 << 20), -(1 << 20)};
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
@@ -1526,7 +1536,24 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const do
                                   idx32(pz[q], 0, rlo[2], rhi[2], err)};
                 for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], I[d]); hi[d] = max(hi[d], I[d]); }
             }
-            const int side = box_plane_side<8>(m, PL, i, j, k, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], px, py, pz);
+            int side;
+            if (m.fd) {
+#pragma unroll
+                for (int f = 0; f < 6; ++f) {
+                    const int dir = f >> 1, up = f & 1;
+                    const float4 e = F.fapex[dir][c + (up ? st[dir] : 0)];
+                    /* a low face's apex is in the lower neighbour's frame: one cell back */
+                    px[8 + f] = e.x - (!up && dir == 0 ? 1.f : 0.f);
+                    py[8 + f] = e.y - (!up && dir == 1 ? 1.f : 0.f);
+                    pz[8 + f] = e.z - (!up && dir == 2 ? 1.f : 0.f);
+                    const int I[3] = {idx32(px[8 + f], 0, rlo[0], rhi[0], err), idx32(py[8 + f], 0, rlo[1], rhi[1], err),
+                                      idx32(pz[8 + f], 0, rlo[2], rhi[2], err)};
+                    for (int d = 0; d < 3; ++d) { lo[d] = min(lo[d], I[d]); hi[d] = max(hi[d], I[d]); }
+                }
+                side = box_plane_side<14>(m, PL, i, j, k, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], px, py, pz);
+            } else {
+                side = box_plane_side<8>(m, PL, i, j, k, lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], px, py, pz);
+            }
             if (side != 0) r = side > 0 ? 1.0 : 0.0;
         }
         VFout[v] = r;
@@ -1534,9 +1561,11 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const do
         const int slot = warp_slot(near, slow_count);
         if (slot >= 0) {
             /* the cell's pre-image vertices in cell2verts! order (x mirrored on odd cells under
-             * 5_tets), as k_sl32_pre stores them, from the traced nodes */
+             * 5_tets), as k_sl32_pre stores them, from the traced nodes; under pressure_scheme
+             * "finite-difference" then its six faces' correction apexes (x-, x+, y-, ... in
+             * the cell's frame) */
             const bool even = tess_even(m.tess, i, j, k);
-            const int stride = m.tess == 24 ? 16 : 8;
+            const int stride = (m.tess == 24 || m.fd) ? 16 : 8;
             float px[8], py[8], pz[8];
             for (int q = 0; q < 8; ++q) {
                 const int a = even ? (q & 1) : 1 - (q & 1), b = (q >> 1) & 1, e = q >> 2;
@@ -1547,6 +1576,18 @@ __global__ void __launch_bounds__(FLUX_THREADS) k_flux_cells(DevMesh m, const do
                 const unsigned pk = pack3(idx32(px[q], 0, rlo[0], rhi[0], err), idx32(py[q], 0, rlo[1], rhi[1], err),
                                           idx32(pz[q], 0, rlo[2], rhi[2], err));
                 slow_verts[(long)slot * stride + q] = make_float4(px[q], py[q], pz[q], __int_as_float((int)pk));
+            }
+            if (m.fd) {
+                for (int f = 0; f < 6; ++f) {
+                    const int dir = f >> 1, up = f & 1;
+                    const float4 e = F.fapex[dir][c + (up ? st[dir] : 0)];
+                    const float x = e.x - (!up && dir == 0 ? 1.f : 0.f);
+                    const float y = e.y - (!up && dir == 1 ? 1.f : 0.f);
+                    const float z = e.z - (!up && dir == 2 ? 1.f : 0.f);
+                    const unsigned pk = pack3(idx32(x, 0, rlo[0], rhi[0], err), idx32(y, 0, rlo[1], rhi[1], err),
+                                              idx32(z, 0, rlo[2], rhi[2], err));
+                    slow_verts[(long)slot * 16 + 8 + f] = make_float4(x, y, z, __int_as_float((int)pk));
+                }
             }
             if (m.tess == 24) {
                 for (int f = -1; f < 6; ++f) {
@@ -1599,18 +1640,20 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
                       int* errw, int nsm, cudaStream_t s)
 {
     FluxBufs F{{L.nd[0], L.nd[1], L.nd[2]}, {L.fvf[0], L.fvf[1], L.fvf[2]}, L.nodes, L.faces, L.clip,
-               L.ctr, L.ctr + 1, L.ctr + 2, L.ctr + 3};
+               {L.fapex[0], L.fapex[1], L.fapex[2]}, L.ctr, L.ctr + 1, L.ctr + 2, L.ctr + 3};
+    const Vel64c V64{uf, vf, wf, {1.0 / m.d[0], 1.0 / m.d[1], 1.0 / m.d[2]}};
     Plane32 PL{planes};
     cudaMemsetAsync(L.ctr, 0, 4 * sizeof(int), s);
     k_flux_lists<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, band, list, count, F);
-    k_flux_nodes<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, Vel64c{uf, vf, wf, {1.0 / m.d[0], 1.0 / m.d[1], 1.0 / m.d[2]}},
-                                                   Vel32{uf32, vf32, wf32}, F);
-    k_flux_faces<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, PL, F, errw);
+    k_flux_nodes<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, V64, Vel32{uf32, vf32, wf32}, F);
+    k_flux_faces<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, PL, F, dt, V64, errw);
     const int smem = (int)sizeof(FluxShared);
     cudaFuncSetAttribute(k_flux_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_flux_clip<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, PL, F, errw);
     k_flux_cells<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, VFin, VFout, PL, list, count, F, slow_cells, slow_verts,
                                                    slow_count, errw);
+    /* near-pure cells: the cell form's FP32 clip (with the correction tets under
+     * pressure_scheme "finite-difference") */
     launch_sl32_clip(m, VFout, planes, work2, slow_cells, slow_verts, slow_count, errw, nsm, s);
 }
 

@@ -274,9 +274,7 @@ int st_transport(slvof_ctx* c, double dt)
     launch_sl_classify(c->m, c->band[c->bcur], c->VF[c->vcur], c->VF[o], c->list_sl, c->ctr + C_SL, c->nsm, c->stream);
     s_end(c, S_CLASSIFY);
     s_beg(c, S_SL);
-    /* the finite-difference scheme's correction tets join each band cell's FP64 sums, so a
-     * mixed context runs the FP64 clip for it (with its own normals and plane constants) */
-    if (c->precision == SLVOF_FP64 || c->m.fd)
+    if (c->precision == SLVOF_FP64)
         launch_sl64(c->m, dt, c->VF[c->vcur], c->VF[o], c->uf, c->vf, c->wf, c->nx, c->ny, c->nz, c->D, c->phase,
                     c->list_sl, c->ctr + C_SL, c->ctr + C_SLW, c->ctr + C_ERR, c->nsm, c->stream);
     else
@@ -492,7 +490,10 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
         ok = alloc((void**)&c->uf32, c->ncell * sizeof(float)) && alloc((void**)&c->vf32, c->ncell * sizeof(float)) &&
              alloc((void**)&c->wf32, c->ncell * sizeof(float)) && alloc((void**)&c->planes, c->ncell * sizeof(float4)) &&
              alloc((void**)&c->slow_cells, interior * sizeof(int)) &&
-             alloc((void**)&c->slow_verts, interior * (mesh->tesselation == 24 ? 16 : 8) * sizeof(float4)) &&
+             alloc((void**)&c->slow_verts, interior *
+                                               ((mesh->tesselation == 24 ||
+                                                 mesh->pressure_scheme == SLVOF_PRESSURE_FINITE_DIFFERENCE) ? 16 : 8) *
+                                               sizeof(float4)) &&
              alloc((void**)&c->arb, interior * sizeof(int2));
     if (ok && precision == SLVOF_MIXED) {
         for (int q = 0; q < 3 && ok; ++q)
@@ -502,6 +503,8 @@ int slvof_create(const slvof_mesh* mesh, int precision, slvof_ctx** out)
              alloc((void**)&c->flux.faces, 3 * c->ncell * sizeof(unsigned)) &&
              alloc((void**)&c->flux.clip, 3 * c->ncell * sizeof(unsigned)) &&
              alloc((void**)&c->flux.ctr, 4 * sizeof(int));
+        for (int q = 0; q < 3 && ok && mesh->pressure_scheme == SLVOF_PRESSURE_FINITE_DIFFERENCE; ++q)
+            ok = alloc((void**)&c->flux.fapex[q], c->ncell * sizeof(float4));
     }
     if (!ok) return bail(SLVOF_E_NOMEM);
     /* coordinates: x, y, z (faces) then xm, ym, zm (centres) */
@@ -537,7 +540,8 @@ int slvof_destroy(slvof_ctx* c)
                     c->gnf[1], c->gnf[2], c->gDf, c->guf, c->gvf_, c->gwf, c->list_adj, c->adj_cells, c->adj_tets,
                     c->gvtx[0], c->gvtx[1], c->gvtx[2], c->cinfo, c->gvel32[0], c->gvel32[1], c->gvel32[2],
                     c->flux.nd[0], c->flux.nd[1], c->flux.nd[2], c->flux.fvf[0], c->flux.fvf[1], c->flux.fvf[2],
-                    c->flux.nodes, c->flux.faces, c->flux.clip, c->flux.ctr,
+                    c->flux.nodes, c->flux.faces, c->flux.clip, c->flux.fapex[0], c->flux.fapex[1], c->flux.fapex[2],
+                    c->flux.ctr,
                     c->cu, c->cv, c->cw, c->us, c->vs, c->ws, c->pr[0], c->pr[1], c->pr[2], c->pr[3],
                     c->pr[4], c->pr[5], c->pr[6], c->pr[7], c->pr[8], c->pr[9], c->pr[10], c->pr_band};
     for (void* b : bufs)

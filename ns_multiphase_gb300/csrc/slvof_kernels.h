@@ -61,6 +61,7 @@ struct FluxLaunch {
     unsigned* nodes;
     unsigned* faces;
     unsigned* clip;
+    float4* fapex[3]; /* pressure_scheme "finite-difference": each face's correction apex */
     int* ctr;
 };
 void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* VFout, const float* uf32,

@@ -69,6 +69,23 @@ void face_flux(const DevMesh& m, const adj::Vel& V, const adj::Plic& P, double d
             vol += sigma[t] * rv;
             liq += sigma[t] * rl;
         }
+    if (m.fd) {
+        /* pressure_scheme "finite-difference": the face's two correction tets (the low face of
+         * h), with the low cell's parity sign, the opposite of h's */
+        adj::CorrFace C;
+        adj::corr_face(m, V, hi, hj, hk, dt, 2 * dir, C);
+        for (int hh = 0; hh < 2; ++hh) {
+            double tet[4][3], gtet[4][3];
+            adj::corr_tet(C, hh, tet);
+            int tind[4][3];
+            for (int a = 0; a < 4; ++a) adj::pt2index(m, tind[a], tet[a], hi, hj, hk, err);
+            double rv = 0.0, rl = 0.0;
+            int kinds = 0;
+            adj::clip(m, TAB, P, tet, tind, 0.0, st.data(), rv, rl, gtet, kinds, err);
+            vol -= C.sgn * rv;
+            liq -= C.sgn * rl;
+        }
+    }
 }
 } // namespace
 
@@ -174,3 +191,54 @@ int fluxh_face(const slvof_mesh* M, double dt, int dir, int hi, int hj, int hk, 
     return e;
 }
 }
+
+extern "C" {
+
+/* The correction tets of face (dir, h) two ways: out[0..3] = the FP64 reverse's corr_face in
+ * physical units (apex, and the tets' volume signed for the low cell); out[4..7] = the mixed
+ * path's flux::face_correction in cell units on the same traced corners, mapped back
+ * (apex * d + the low cell's corner, volume * |cell|). */
+int fluxh_face_correction(const slvof_mesh* M, double dt, int dir, int hi, int hj, int hk, const double* uf,
+                          const double* vf, const double* wf, double* out)
+{
+    HostMesh H(M);
+    const DevMesh& m = H.m;
+    adj::Vel V{uf, vf, wf};
+    adj::CorrFace C;
+    adj::corr_face(m, V, hi, hj, hk, dt, 2 * dir, C);
+    double tet[4][3];
+    double vt = 0.0;
+    for (int hh = 0; hh < 2; ++hh) {
+        adj::corr_tet(C, hh, tet);
+        vt += adj::tet_vol(tet[0], tet[1], tet[2], tet[3]);
+    }
+    for (int q = 0; q < 3; ++q) out[q] = C.e[q];
+    out[3] = -C.sgn * vt;
+    /* cell units, the low cell's frame */
+    const int l[3] = {hi - (dir == 0), hj - (dir == 1), hk - (dir == 2)};
+    const double o[3] = {adj::fc(m, 0, l[0]), adj::fc(m, 1, l[1]), adj::fc(m, 2, l[2])};
+    const double d[3] = {m.d[0], m.d[1], m.d[2]};
+    int s_, t_;
+    flux::face_axes(dir, s_, t_);
+    double P[5][3], Q[5][3];
+    for (int c = 0; c < 4; ++c) {
+        int i, j, k;
+        flux::corner_node(dir, hi, hj, hk, c, i, j, k);
+        double x[3] = {adj::fc(m, 0, i), adj::fc(m, 1, j), adj::fc(m, 2, k)};
+        double w[3][3];
+        adj::project(m, V, x, hi, hj, hk, dt, w);
+        P[c][dir] = 1.0;
+        P[c][s_] = flux::corner_s(c);
+        P[c][t_] = flux::corner_t(c);
+        for (int q = 0; q < 3; ++q) Q[c][q] = (x[q] - o[q]) / d[q];
+    }
+    const double* u = dir == 0 ? uf : (dir == 1 ? vf : wf);
+    const double dtu = dt * u[adj::ci(m, hi, hj, hk)] / d[dir];
+    double e[3];
+    const double vc = flux::face_correction(dir, hi, hj, hk, dtu, P, Q, e);
+    for (int q = 0; q < 3; ++q) out[4 + q] = e[q] * d[q] + o[q];
+    out[7] = vc * (d[0] * d[1] * d[2]);
+    return 0;
+}
+
+} // extern "C"

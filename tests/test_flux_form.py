@@ -38,6 +38,8 @@ def flib():
     d, i, p = ctypes.c_double, ctypes.c_int, ctypes.c_void_p
     L.fluxh_sl_cell.restype = d
     L.fluxh_sl_cell.argtypes = [p, d, i, i, i] + [p] * 8 + [p]
+    L.fluxh_face_correction.restype = i
+    L.fluxh_face_correction.argtypes = [p, d, i, i, i, i, p, p, p, p]
     return L
 
 
@@ -45,7 +47,7 @@ def ptr(a):
     return a.ctypes.data
 
 
-def state(tess, projection, cfl, dims):
+def state(tess, projection, cfl, dims, scheme="semi-lagrangian"):
     if dims == 2:
         m = Mesh(Nx=14, Ny=14, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / 14, CFL=cfl, zper=True, tesselation=tess,
                  projection=projection)
@@ -53,7 +55,8 @@ def state(tess, projection, cfl, dims):
         uf, vf, wf = cases.deformation2d_faces(m, 0.7, 8.0)
         vmax = 1.0
     else:
-        m = Mesh(Nx=10, Ny=10, Nz=10, Lx=1.0, Ly=1.0, Lz=1.0, CFL=cfl, tesselation=tess, projection=projection)
+        m = Mesh(Nx=10, Ny=10, Nz=10, Lx=1.0, Ly=1.0, Lz=1.0, CFL=cfl, tesselation=tess, projection=projection,
+                 pressure_scheme=scheme)
         VF = cases.vf_spheres(m, np.array([[0.45, 0.52, 0.55]]), np.array([0.27]), nF=8)
         uf, vf, wf = cases.deformation3d_faces(m, 0.4, 3.0)
         vmax = 2.0
@@ -71,9 +74,14 @@ CASES = [("5_tets", "RK4", 0.5, 3), ("6_tets", "RK4", 0.5, 3), ("24_tets", "RK4"
          ("5_tets", "RK4", 0.5, 2), ("24_tets", "RK4", 0.5, 2)]
 
 
-@pytest.mark.parametrize("tess,projection,cfl,dims", CASES)
-def test_flux_form_equals_cell_form_in_fp64(flib, tess, projection, cfl, dims):
-    m, o, VF, band, nx, ny, nz, D, uf, vf, wf, dt = state(tess, projection, cfl, dims)
+@pytest.mark.parametrize("tess,projection,cfl,dims,scheme",
+                         [c + ("semi-lagrangian",) for c in CASES] +
+                         [("5_tets", "RK4", 0.5, 3, "finite-difference"), ("5_tets", "RK4", 2.5, 3, "finite-difference")])
+def test_flux_form_equals_cell_form_in_fp64(flib, tess, projection, cfl, dims, scheme):
+    """With pressure_scheme "finite-difference" each band cell also adds its faces' correction
+    tets (src/Transport.jl:121-124) with its parity sign; a face's tets depend on the face alone
+    and its two cells' parities differ, so they join the face's flux like its prism."""
+    m, o, VF, band, nx, ny, nz, D, uf, vf, wf, dt = state(tess, projection, cfl, dims, scheme)
     desc = m.desc()
     err = ctypes.c_int()
     worst, n = 0.0, 0
@@ -91,3 +99,28 @@ def test_flux_form_equals_cell_form_in_fp64(flib, tess, projection, cfl, dims):
                 n += 1
     assert n > 50
     assert worst <= TOL, worst
+
+
+def test_face_correction_in_cell_units_matches_the_fp64_reverse(flib):
+    """The mixed path's correction apex and volume (flux::face_correction, cell units on the
+    traced corners) against the FP64 reverse's own construction (adj::corr_face, physical
+    units), face by face over the band of a deforming sphere, both in FP64: the same
+    construction in different units, so they agree to rounding."""
+    m, o, VF, band, nx, ny, nz, D, uf, vf, wf, dt = state("5_tets", "RK4", 0.5, 3, "finite-difference")
+    desc = m.desc()
+    out = (ctypes.c_double * 8)()
+    worst_e, worst_v, n = 0.0, 0.0, 0
+    scale = m.dx * m.dy * m.dz
+    for k in range(2, m.Nz + 1):
+        for j in range(2, m.Ny + 1):
+            for i in range(2, m.Nx + 1):
+                if abs(int(band[m.cidx(i, j, k)])) > m.nband:
+                    continue
+                for d in range(3):
+                    assert flib.fluxh_face_correction(ctypes.byref(desc), dt, d, i, j, k, ptr(uf), ptr(vf), ptr(wf),
+                                                      out) == 0
+                    worst_e = max(worst_e, max(abs(out[q] - out[4 + q]) for q in range(3)) / m.dx)
+                    worst_v = max(worst_v, abs(out[3] - out[7]) / scale)
+                    n += 1
+    assert n > 100
+    assert worst_e <= 1e-12 and worst_v <= 1e-13, (worst_e, worst_v)

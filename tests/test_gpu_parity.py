@@ -335,9 +335,11 @@ def test_finite_difference_scheme_correction_tets():
 
 def test_finite_difference_scheme_in_a_mixed_context():
     """A mixed context with the finite-difference scheme: mixed normals and plane constants, and
-    the update with the correction tets through the FP64 clip.  VF within the mixed path's
-    tolerance of the restatement over several steps, and the momentum call like an FP64
-    context's on the same inputs."""
+    the update in flux form with each face's correction tets (apex and volume in FP64, their
+    liquid from the FP32 clip; near-pure cells by the cell form with the cell's twelve
+    correction tets).  VF within the mixed path's tolerance of the restatement over several
+    steps, and the momentum call (FP64 clip in either precision) like an FP64 context's on the
+    same inputs."""
     m = Mesh(Nx=20, Ny=20, Nz=20, Lx=1.0, Ly=1.0, Lz=1.0, CFL=0.5, pressure_scheme="finite-difference")
     VF = cases.vf_spheres(m, [[0.45, 0.52, 0.5]], [0.22], nF=10)
     o, g, VFo, band, nx, ny, nz, D = init_both(m, VF, "mixed")
