@@ -925,14 +925,17 @@ SLVOF_HD double sl_cell_fd(const DevMesh& m, const CutCase* tab, const Vel& V, c
         pt2index(m, pind[n], p[n], i, j, k, err);
     }
     const int nt = tess_ntets(m.tess);
-    CorrFace C;
+    /* the six faces' flux volumes and apexes, formed once (each traces its face's four
+     * corners) and used by the volume, the clips and the reverse below */
+    CorrFace CF[6];
+    for (int f = 0; f < 6; ++f) corr_face(m, V, i, j, k, dt, f, CF[f]);
     /* the uncut volume, which the clipped pieces add up to */
     double volu = 0.0;
     for (int t = 0; t < nt; ++t)
         volu += tetsign * tet_vol(p[tess_tet(m.tess, t, 0)], p[tess_tet(m.tess, t, 1)], p[tess_tet(m.tess, t, 2)],
                                   p[tess_tet(m.tess, t, 3)]);
     for (int f = 0; f < 6; ++f) {
-        corr_face(m, V, i, j, k, dt, f, C);
+        const CorrFace& C = CF[f];
         for (int h = 0; h < 2; ++h) {
             double tet[4][3];
             corr_tet(C, h, tet);
@@ -959,7 +962,7 @@ SLVOF_HD double sl_cell_fd(const DevMesh& m, const CutCase* tab, const Vel& V, c
     }
     double gct[12][4][3];
     for (int f = 0; f < 6; ++f) {
-        corr_face(m, V, i, j, k, dt, f, C);
+        const CorrFace& C = CF[f];
         for (int h = 0; h < 2; ++h) {
             double tet[4][3];
             int ind[4][3];
@@ -985,7 +988,7 @@ SLVOF_HD double sl_cell_fd(const DevMesh& m, const CutCase* tab, const Vel& V, c
         if (gvt[n][0] != 0.0 || gvt[n][1] != 0.0 || gvt[n][2] != 0.0)
             project_reverse_call(m, V, GV, p0[n], i, j, k, dt, gvt[n]);
     for (int f = 0; f < 6; ++f) {
-        corr_face(m, V, i, j, k, dt, f, C);
+        const CorrFace& C = CF[f];
         for (int h = 0; h < 2; ++h) {
             double tet[4][3];
             corr_tet(C, h, tet);

@@ -398,9 +398,10 @@ def test_rollout_against_forward_mode(built, scheme):
 
 
 def test_finite_difference_reverse_in_a_mixed_context(built):
-    """A mixed context's finite-difference update runs the FP64 clip on its FP64 winner normals
-    and plane constants, and its reverse is the FP64 one: against the FP64 context's reverse on
-    the same rollout (relative L2 over all face and initial-VF derivatives)."""
+    """A mixed context's finite-difference step runs the flux form with the correction tets, on
+    its FP64 winner normals and plane constants, and its reverse is the FP64 one (k_adj_sl_fd):
+    against the FP64 context's reverse on the same rollout (relative L2 over all face and
+    initial-VF derivatives)."""
     m, VF0 = sphere3d(12, "finite-difference")
     dt = 0.5 * m.dx / 2.0
     base = lambda n: cases.deformation3d_faces(m, 0.3 + (n + 0.5) * dt, 3.0)
