@@ -50,7 +50,7 @@ def ptr(a):
 def state(tess, projection, cfl, dims, scheme="semi-lagrangian"):
     if dims == 2:
         m = Mesh(Nx=14, Ny=14, Nz=1, Lx=1.0, Ly=1.0, Lz=1.0 / 14, CFL=cfl, zper=True, tesselation=tess,
-                 projection=projection)
+                 projection=projection, pressure_scheme=scheme)
         VF = cases.vf_spheres(m, np.array([[0.45, 0.55, 0.0]]), np.array([0.27]), nF=8, dims=2)
         uf, vf, wf = cases.deformation2d_faces(m, 0.7, 8.0)
         vmax = 1.0
@@ -76,7 +76,8 @@ CASES = [("5_tets", "RK4", 0.5, 3), ("6_tets", "RK4", 0.5, 3), ("24_tets", "RK4"
 
 @pytest.mark.parametrize("tess,projection,cfl,dims,scheme",
                          [c + ("semi-lagrangian",) for c in CASES] +
-                         [("5_tets", "RK4", 0.5, 3, "finite-difference"), ("5_tets", "RK4", 2.5, 3, "finite-difference")])
+                         [("5_tets", "RK4", 0.5, 3, "finite-difference"), ("5_tets", "RK4", 2.5, 3, "finite-difference"),
+                          ("5_tets", "RK4", 0.5, 2, "finite-difference")])
 def test_flux_form_equals_cell_form_in_fp64(flib, tess, projection, cfl, dims, scheme):
     """With pressure_scheme "finite-difference" each band cell also adds its faces' correction
     tets (src/Transport.jl:121-124) with its parity sign; a face's tets depend on the face alone
