@@ -40,8 +40,9 @@ extern "C" {
 #define SLVOF_E_TOO_LARGE (-5) /* grid larger than a fixed scratch maximum (slvof_mass_noalloc) */
 
 #define SLVOF_FP64 0  /* every stage in FP64, rounding identical to the CPU restatement */
-#define SLVOF_MIXED 1 /* FP32 trajectories, interpolation, clip geometry and ELVIRA candidate errors;
-                         FP64 PLIC root, volume accumulation and mass sums */
+#define SLVOF_MIXED 1 /* the SL update in flux form (FP64 node traces and swept-face volumes, FP32 clip
+                         geometry), FP32 ELVIRA candidate errors with FP64 arbitration; FP64 PLIC
+                         root, volume accumulation and mass sums */
 
 #define SLVOF_STEP_BAND 1 /* recompute the band after the step (run_solver, src/NavierStokes_Parallel.jl:143) */
 #define SLVOF_STEP_MASS 2 /* return sum(VF)*dx*dy*dz over the interior (src/WriteData.jl:33) */
@@ -69,7 +70,7 @@ typedef struct slvof_mesh {
     int32_t pressure_scheme; /* param.pressure_scheme (src/Parameters.jl:60): SLVOF_PRESSURE_SEMI_LAGRANGIAN
                                 (0, the default) or SLVOF_PRESSURE_FINITE_DIFFERENCE (1), whose band cells
                                 add the flux-correction tets (src/Transport.jl:121-124; 5_tets; a mixed
-                                context runs this scheme's update with the FP64 clip) and whose
+                                context adds them to its flux form, clipped in FP32) and whose
                                 band-edge momentum fluxes are finite differences */
 } slvof_mesh;
 
@@ -100,8 +101,9 @@ int slvof_stage_ms(const slvof_ctx* ctx, double* ms, int n);
  * reference (CPU only). */
 int slvof_set_stream(slvof_ctx* ctx, void* stream);
 /* Work-list sizes of the last step: [0] band cells updated by the SL clip pipeline,
- * [1] interface cells given ELVIRA candidates, [2] band cells that needed the full clip (the
- * mixed reverse pass; the rest were all-liquid/all-gas pre-images), [3] cells whose PLIC
+ * [1] interface cells given ELVIRA candidates, [2] band cells clipped whole in FP32 (in a mixed
+ * step the flux form's near-pure cells; in the mixed reverse pass the cells whose pre-image is
+ * not all liquid or all gas), [3] cells whose PLIC
  * plane constant was solved, [4] interface cells whose ELVIRA choice was arbitrated in FP64
  * (mixed mode), and for the mixed mode's flux-form SL update [5] grid nodes traced, [6] faces
  * swept, [7] faces that needed the clip.  No counterpart in the reference. */
