@@ -11,8 +11,9 @@ fill, ELVIRA, PLIC distances, band, mass.  1 cell-update = 1 interior cell advan
 over the timed window; every field is larger than L2 (129 MB), so no flush is needed.
 
 Arms:
-  value      mixed precision (FP32 trajectories/geometry/ELVIRA errors, FP64 PLIC root,
-             volume sums, mass), device-resident, CUDA events on the launching stream;
+  value      mixed precision (the SL update in flux form: FP64 node traces and face volumes,
+             FP32 clip; FP32 ELVIRA errors with FP64 arbitration; FP64 PLIC root, volume sums,
+             mass), device-resident, CUDA events on the launching stream;
   fp64       the plain FP64 path (bit-identical to the CPU restatement) on the same state;
   e2e        slvof_step_host: H2D of the step's face velocities from pinned memory, the
              step, D2H of VF and the mass; with SLVOF_STEP_DEFER, which builds each state's
