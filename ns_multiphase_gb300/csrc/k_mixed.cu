@@ -1094,17 +1094,19 @@ constexpr int FCLIP_BATCH = 5; /* faces per warp batch: 30 seed tets for 5_tets 
 constexpr int CAPEX = 10;      /* seed point id of a face's correction apex */
 constexpr int FCLIP_CAP = 120; /* stack nodes per warp: keeps the block at 55.3 KB, four per SM */
 
-__device__ __forceinline__ void facc_add(FF* acc, int b, float x)
-{
-#pragma unroll
-    for (int q = 0; q < FCLIP_BATCH; ++q)
-        if (q == b) ff_add(acc[q], x);
-}
+/* acc[b] += x for a lane-varying b over register-held accumulators: the accumulator is
+ * selected, added to once and written back (one float-float add in the code instead of one
+ * per face of the batch) */
 __device__ __forceinline__ void facc_add(FF* acc, int b, const FF& x)
 {
+    FF s = acc[0];
+#pragma unroll
+    for (int q = 1; q < FCLIP_BATCH; ++q)
+        if (q == b) s = acc[q];
+    ff_add(s, x);
 #pragma unroll
     for (int q = 0; q < FCLIP_BATCH; ++q)
-        if (q == b) ff_add(acc[q], x);
+        if (q == b) acc[q] = s;
 }
 __device__ __forceinline__ void fflag_or(int* f, int b, int x)
 {
@@ -1123,7 +1125,12 @@ struct FluxShared {
 
 enum : int { PIECE_LIQ = 1, PIECE_GAS = 2 };
 
+/* The clip's seeding by tessellation and pressure scheme, fixed per instantiation: the
+ * kernel is bound by instruction fetch, and each instantiation carries only its own seeding
+ * code. */
+enum : int { SEED_PRISM = 0, SEED_FD = 1, SEED_24 = 2 };
 
+template <int SEED>
 __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Plane32 PL, FluxBufs F, int* errw)
 {
     extern __shared__ __align__(16) unsigned char flux_smem[];
@@ -1136,8 +1143,9 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
     const int n_faces = *F.n_clip;
     /* seed tets per face: the prism's, and under pressure_scheme "finite-difference" (5_tets)
      * the two correction tets */
-    const int ntet = m.tess == 24 ? 12 : (m.fd ? 8 : 6);
-    const int B = m.tess == 24 ? 2 : (m.fd ? 4 : FCLIP_BATCH);
+    constexpr bool T24 = SEED == SEED_24, FD = SEED == SEED_FD;
+    const int ntet = T24 ? 12 : (FD ? 8 : 6);
+    const int B = T24 ? 2 : (FD ? 4 : FCLIP_BATCH);
     int err = 0;
     for (;;) {
         int base = 0;
@@ -1192,7 +1200,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
             int dir, hi, hj, hk;
             face_decode(m, code, dir, hi, hj, hk);
             int q[4];
-            if (n < 6 || m.tess == 24) {
+            if (!FD || n < 6) {
                 int tri[4][3], sg[4];
                 flux::face_triangles(m.tess, dir, flux::face_main_diagonal(m.tess, dir, hi, hj, hk), tri, sg);
                 flux::prism_tet(tri[n / 3], n % 3, q);
@@ -1220,7 +1228,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
             float4 v[4];
             int I[4][3];
             int mlo = 1 << 20;
-            if (m.tess == 24) {
+            if (T24) {
                 double P[5][3], Q[5][3];
                 face_points(m, F, dir, hi, hj, hk, P, Q);
                 for (int nn = 0; nn < 4; ++nn) {
@@ -1229,7 +1237,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                 }
             } else {
                 for (int nn = 0; nn < 4; ++nn) {
-                    if (q[nn] == CAPEX) {
+                    if (FD && q[nn] == CAPEX) {
                         const float4 e = F.fapex[dir][(long)(code >> 2)];
                         v[nn] = make_float4(e.x, e.y, e.z, 0.f);
                     } else {
@@ -1398,6 +1406,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                     /* the node's pieces summed here, then added to its face's sums once */
                     int fl = 0;
                     FF nv{0.f, 0.f}, nl{0.f, 0.f};
+#pragma unroll 1 /* rolled, as the loops below: less code (the kernel is instruction-fetch bound) */
                     for (int c = 0; c < nt; ++c) {
                         const float4 P0 = S.scr[C.vtet[c][0]][tid], P1 = S.scr[C.vtet[c][1]][tid];
                         const float4 P2 = S.scr[C.vtet[c][2]][tid], P3 = S.scr[C.vtet[c][3]][tid];
@@ -1414,6 +1423,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
                     const int pos = size + ipush - pushed;
                     const unsigned tagc = ((unsigned)b | ((unsigned)flags << 3)) << 24;
                     const int sh = 8 * dir;
+#pragma unroll 1
                     for (int c = 0; c < nt; ++c) {
                         const bool up = C.side[c] == 1;
 #pragma unroll
@@ -1452,6 +1462,7 @@ __global__ void __launch_bounds__(CLIPW_WARPS * 32, 4) k_flux_clip(DevMesh m, Pl
             if (b >= nb) break;
             FF a = acc[b], vv = avol[b];
             int fg = flg[b];
+#pragma unroll 1
             for (int off = 16; off > 0; off >>= 1) {
                 const FF oa{__shfl_xor_sync(0xffffffffu, a.hi, off), __shfl_xor_sync(0xffffffffu, a.lo, off)};
                 const FF ov{__shfl_xor_sync(0xffffffffu, vv.hi, off), __shfl_xor_sync(0xffffffffu, vv.lo, off)};
@@ -1648,8 +1659,9 @@ void launch_sl32_flux(const DevMesh& m, double dt, const double* VFin, double* V
     k_flux_nodes<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, dt, V64, Vel32{uf32, vf32, wf32}, F);
     k_flux_faces<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, PL, F, dt, V64, errw);
     const int smem = (int)sizeof(FluxShared);
-    cudaFuncSetAttribute(k_flux_clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    k_flux_clip<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, PL, F, errw);
+    auto clip = m.tess == 24 ? k_flux_clip<SEED_24> : (m.fd ? k_flux_clip<SEED_FD> : k_flux_clip<SEED_PRISM>);
+    cudaFuncSetAttribute(clip, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    clip<<<nsm * 4, CLIPW_WARPS * 32, smem, s>>>(m, PL, F, errw);
     k_flux_cells<<<nsm * 8, FLUX_THREADS, 0, s>>>(m, VFin, VFout, PL, list, count, F, slow_cells, slow_verts,
                                                    slow_count, errw);
     /* near-pure cells: the cell form's FP32 clip (with the correction tets under
